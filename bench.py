@@ -1,0 +1,365 @@
+"""Benchmark: Poisson solves/s at 256^3 to 1e-6 relative residual (pressure projection + magnetic potential).
+
+One step = one SimFerrofluid substep's pair of grid solves on the 256^3 pool+sphere scene (pool depth 0.2,
+sphere r=0.15 at (0.5,0.55,0.5), chi=2, dipole field of moment (0,1,0) at (0.5,-0.3,0.5), velocity
+N(0,0.5^2), walls on the grid faces): a fresh velocity is copied in, the pressure is projected (assembly,
+MGPCG solve to 1e-6, velocity update) and the potential is solved from zero (assembly, solve to 1e-6, H on
+faces).  ``value`` counts 2 solves per step, inputs resident in HBM, timed with CUDA events on the library's
+stream.  ``e2e`` runs the same step through the host-pointer C ABI with pinned host buffers (H2D of every
+input, D2H of velocity, pressure, potential and H inside the timed region).
+
+--impl reference times the CPU restatement of the reference's path (the oracle: the reference cannot be
+built here) on the host cores.  With WORLD_SIZE > 1 every rank runs an independent replica (the path does not
+shard; replicas only).
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "simferrofluid-cuda_gb300"
+
+METRIC = "Poisson solves/s at 256^3 to 1e-6 rel. residual (pressure + magnetic potential)"
+UNIT = "solves/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64-arm", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-n", type=int, default=64, help="grid of the bounded CPU sample")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------------------------ distributed
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if _cuda_ok() else "gloo"
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def _cuda_ok():
+    import torch
+    return torch.cuda.is_available()
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if _cuda_ok() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+        self.th = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.th:
+            self.th.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------------ our arm
+def algorithmic_bytes_per_half_sweep(n_cells, precision):
+    """Red-black Gauss-Seidel, one colour: half of a full sweep's x r/w + b + 3 couplings + diagonal term.
+
+    Full sweep per cell: FP64 x(8 r + 8 w) + b 8 + 3*8 couplings + 8 (1/D) = 56 B; mixed FP32 level 0:
+    x(4 + 4) + b 4 + 3*4 couplings + 4 (dex) = 28 B."""
+    per_cell = 56.0 if precision == "fp64" else 28.0
+    return per_cell / 2 * n_cells
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    pkg = importlib.import_module(PKG)
+    scenes = importlib.import_module(PKG + ".scenes")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    # torch work (velocity reset) and the library share one stream, so CUDA events on it bracket both
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    ctx = pkg.Context(local, stream=stream.cuda_stream)
+
+    t0 = time.time()
+    sc = scenes.pool_sphere(args.n, seed=1234 + rank)
+    t_scene = time.time() - t0
+    g = sc.grid
+    P = pkg.Pressure(g, ctx)
+    M = pkg.MagneticField(g, sc.chi, sc.band_width, ctx)
+
+    def todev(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+    phi = todev(sc.phi)
+    frac = [todev(f) for f in sc.frac]
+    vel0 = [todev(v) for v in sc.vel]
+    vel = [v.clone() for v in vel0]
+    hext = [todev(h) for h in sc.hext]
+    p_out = torch.zeros(g.shape, dtype=torch.float64, device=dev)
+    psi = torch.zeros(g.shape, dtype=torch.float64, device=dev)
+    H = [torch.zeros(g.face_shape(a), dtype=torch.float64, device=dev) for a in range(3)]
+    torch.cuda.synchronize(dev)
+
+    def opts(which, precision, profile=0):
+        return pkg.options(which, precision=precision, tol=args.tol, warm_start=0, report_ref_residual=0,
+                           profile=profile)
+
+    def step(precision, profile=0, record=None):
+        for a in range(3):
+            vel[a].copy_(vel0[a])
+        sp = P.project(vel, phi, frac, opts=opts("pressure", precision, profile), device=True, p_out=p_out)
+        sm = M.solve(phi, hext, opts=opts("magnetic", precision, profile), device=True, psi_out=psi, H_out=H)
+        if record is not None:
+            record.append((sp, sm))
+        return sp, sm
+
+    def timed(precision, steps, warmup, clocks=False):
+        for _ in range(warmup):
+            step(precision)
+        rec = []
+        barrier(ws)
+        torch.cuda.synchronize(dev)
+        cs = ClockSampler(local) if clocks else None
+        if cs:
+            cs.start()
+            time.sleep(0.5)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step(precision, record=rec)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier(ws)
+        clk = cs.stop() if cs else None
+        ms = e0.elapsed_time(e1)
+        return max_over_ranks(ws, ms), rec, clk
+
+    # headline arm
+    ms, rec, clk = timed(args.precision, args.steps, args.warmup, clocks=True)
+    value = 2 * args.steps * ws / (ms / 1e3)
+    it_p = [r[0]["iters"] for r in rec]
+    it_m = [r[1]["iters"] for r in rec]
+    res_p = max(r[0]["rel_residual"] for r in rec)
+    res_m = max(r[1]["rel_residual"] for r in rec)
+    launches = sum(r[0]["kernel_launches"] + r[1]["kernel_launches"] for r in rec) + 3 * args.steps
+
+    # plain FP64 MGPCG arm (the denominator of the mixed-precision speed-up)
+    fp64 = None
+    if not args.no_fp64_arm and args.precision != "fp64":
+        ms64, rec64, _ = timed("fp64", max(2, args.steps // 2), 2)
+        fp64 = {"solves_per_s": 2 * max(2, args.steps // 2) * ws / (ms64 / 1e3),
+                "ms_per_step": ms64 / max(2, args.steps // 2),
+                "iters_pressure": [r[0]["iters"] for r in rec64], "iters_magnetic": [r[1]["iters"] for r in rec64]}
+
+    # dominant kernel: finest-level red-black smoother, timed live with CUDA events (a separate profiled pass)
+    prec = []
+    for _ in range(2):
+        step(args.precision, profile=1, record=prec)
+    sp, sm = prec[-1]
+    n_launch = sp["smooth_launches"] + sm["smooth_launches"]
+    ms_launch = (sp["smooth_ms"] + sm["smooth_ms"]) / max(n_launch, 1)
+    bytes_launch = algorithmic_bytes_per_half_sweep(g.num_cells, args.precision)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    achieved = bytes_launch / (ms_launch / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_rbgs (finest level, one colour)", "achieved": round(achieved, 1),
+                "peak": peak, "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": None, "bytes_per_launch": bytes_launch, "ms_per_launch": ms_launch,
+                "launches_timed": n_launch}
+
+    # e2e: host pointers, pinned buffers
+    e2e = None
+    if not args.no_e2e:
+        def pinned(a):
+            t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+            t.numpy()[...] = a
+            return t.numpy()
+        phi_h = pinned(sc.phi)
+        frac_h = [pinned(f) for f in sc.frac]
+        vel0_h = [np.array(v) for v in sc.vel]
+        vel_h = [pinned(v) for v in sc.vel]
+        hext_h = [pinned(h) for h in sc.hext]
+        p_h = pinned(np.zeros(g.shape))
+        psi_h = pinned(np.zeros(g.shape))
+        H_h = [pinned(np.zeros(g.face_shape(a))) for a in range(3)]
+
+        def estep():
+            for a in range(3):
+                np.copyto(vel_h[a], vel0_h[a])
+            t = time.perf_counter()
+            sp = P.project(vel_h, phi_h, frac_h, opts=opts("pressure", args.precision), p_out=p_h)
+            smm = M.solve(phi_h, hext_h, opts=opts("magnetic", args.precision), psi_out=psi_h, H_out=H_h)
+            return time.perf_counter() - t, sp, smm
+
+        for _ in range(max(1, args.warmup)):
+            estep()
+        tot = 0.0
+        h2d = d2h = 0
+        esteps = max(2, args.steps // 2)
+        for _ in range(esteps):
+            dt, sp, smm = estep()
+            tot += dt
+            h2d = sp["h2d_bytes"] + smm["h2d_bytes"]
+            d2h = sp["d2h_bytes"] + smm["d2h_bytes"]
+        tot = max_over_ranks(ws, tot)
+        e2e = {"value": round(2 * esteps * ws / tot, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "steps": esteps}
+
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32/f16" if args.precision == "mixed" else "f64",
+        "data": "synthetic (seeded pool+sphere scene, no dataset)",
+        "config": {"workload": f"pool_sphere {args.n}^3 chi=2 dipole field, pressure+potential per step, "
+                               f"{args.precision} MGPCG to {args.tol:g} from zero",
+                   "grid": [args.n] * 3, "precision": args.precision, "tol": args.tol,
+                   "l2": "inputs larger than L2 (each field 134 MB at 256^3)", "parallelism": f"replicas x{ws}"},
+        "iters": {"pressure": it_p, "magnetic": it_m}, "max_rel_residual": {"pressure": res_p, "magnetic": res_m},
+        "fp64_mgpcg": fp64,
+        "speedup_vs_fp64": round(value / fp64["solves_per_s"], 3) if fp64 else None,
+        "roofline": roofline, "clocks": clk, "e2e": e2e, "gpu_launches": int(launches),
+        "scene_build_s": round(t_scene, 2),
+    }
+    ctx_bytes = ctx.device_bytes()
+    out["device_bytes"] = ctx_bytes
+    return out
+
+
+# ------------------------------------------------------------------------------------------------ CPU arm
+def cpu_baseline(args, sample_n=None, steps=1):
+    """Oracle (CPU restatement of the reference path) on a bounded sample: the same scene at sample_n^3."""
+    from oracle import oracle as O
+    O.build()
+    scenes = importlib.import_module(PKG + ".scenes")
+    n = sample_n or args.cpu_n
+    sc = scenes.pool_sphere(n, seed=1234)
+    og = O.Grid(*sc.grid.shape, sc.grid.spacing, tuple(sc.grid.origin))
+    t = time.perf_counter()
+    for _ in range(steps):
+        O.pressure_project(og, sc.phi, sc.frac, sc.vel, tol=args.tol)
+        O.magnetic_solve(og, sc.phi, sc.chi, sc.band_width, sc.hext, tol=args.tol)
+    dt = time.perf_counter() - t
+    return {"value": round(2 * steps / dt, 4), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+            "sample": f"pool_sphere {n}^3 (same scene family, reduced grid), oracle assembly + Jacobi-PCG "
+                      f"to {args.tol:g}, {steps} step(s) of 2 solves, {dt:.1f} s"}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return None
+    steps = args.steps
+    cb = cpu_baseline(args, steps=1)
+    for _ in range(max(0, min(args.warmup, 1))):
+        pass
+    v = cb["value"]
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": 1, "warmup": 0,
+            "ms_per_step": round(2000.0 / v, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded pool+sphere scene)", "impl": "reference",
+            "config": {"workload": cb["sample"], "requested_steps": steps},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_init()
+    if args.impl == "reference":
+        out = run_reference(args, ws, rank)
+        if rank == 0 and out is not None:
+            print(json.dumps(out))
+        return
+    out = run_ours(args, ws, rank, local)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(args)
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,177 @@
+/*
+ * sfgpu.h -- C ABI of the GB300 (sm_103a) library that replaces the two grid solves of a SimFerrofluid
+ * substep: the ghost-fluid pressure projection and the FDM magnetostatic potential solve.
+ *
+ * Every entry point takes plain pointers and sizes.  Arrays use the reference's layout (core/Grid.h:28):
+ *   cell (i,j,k)            -> k + nz*(j + ny*i)                  (nx*ny*nz doubles)
+ *   face (i,j,k) of axis a  -> same formula on the face grid of size res + e_a (core/StaggeredGrid.h:16-20)
+ * Face arrays are passed as `const double *x[3]` (x, y, z face grids).  `_dev` variants take device
+ * pointers (cudaMalloc'ed or managed, on the context's device) and run without host<->device copies.
+ *
+ * Thread safety: one context per host thread; calls on one context are serialised by the caller.  A context
+ * owns a CUDA stream (or borrows one) and all device workspaces; the solvers' warm-start state (the last
+ * pressure for Reproject, the last potential for the magnetic warm start) lives in the context, like the
+ * members m_RdP (core/Pressure.h:49) and m_Sol (core/MagneticField.h:66) of the reference classes.
+ */
+#ifndef SFGPU_H
+#define SFGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SFGPU_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define SF_EXPORT __attribute__((visibility("default")))
+#else
+#define SF_EXPORT
+#endif
+
+typedef enum {
+    SF_OK = 0,
+    SF_NOT_CONVERGED = 1,   /* iteration cap reached; outputs hold the last iterate */
+    SF_BAD_ARG = 2,         /* null pointer, non-positive size, unknown option value */
+    SF_CUDA_ERROR = 3,      /* a CUDA call failed; sf_last_error() has the message */
+    SF_NO_DEVICE = 4,       /* no CUDA device, or the device is not sm_103 */
+    SF_OUT_OF_MEMORY = 5,
+    SF_STALLED_FALLBACK = 6, /* learned solve stalled; the plain MGPCG finished the solve (not an error) */
+    SF_NOT_READY = 7        /* Reproject called before any Project on this context / grid */
+} sf_status;
+
+typedef enum {
+    SF_PREC_FP64 = 0,  /* plain method: FP64 MGPCG */
+    SF_PREC_MIXED = 1  /* FP32 V-cycle, FP16 coarse coefficients, inner FP32 FCG, FP64 iterative refinement */
+} sf_precision;
+
+/* Cell grid of a staggered grid: resolution, spacing and corner (StaggeredGrid ctor,
+ * core/StaggeredGrid.h:8-21: origin = center - res*h/2). */
+typedef struct {
+    int nx, ny, nz;
+    double h;
+    double origin[3];
+} sf_grid;
+
+typedef struct {
+    int precision;       /* sf_precision */
+    double tol;          /* stop when ||b - A x|| <= tol * ||b|| (the reference's amgcl criterion) */
+    int max_iters;       /* PCG iterations (FP64) or total inner iterations (mixed) */
+    int pre_smooth;      /* red-black Gauss-Seidel sweeps before restriction */
+    int post_smooth;     /* ... after prolongation */
+    int coarse_sweeps;   /* symmetric sweep pairs on the coarsest level */
+    int max_levels;      /* 0 = coarsen until every dimension is <= coarse_dim */
+    int coarse_dim;      /* default 8 */
+    int warm_start;      /* magnetic: start from the context's last potential (reference behaviour, default 1);
+                            pressure Project always starts from zero (core/Pressure.cpp:122) */
+    int use_graph;       /* capture one PCG iteration in a CUDA graph (default 1) */
+    int check_every;     /* read the residual norm back every k iterations (default 1) */
+    int report_ref_residual; /* also compute the residual on the reference's own operator (default 1) */
+    double inner_tol;    /* mixed: floor of the inner relative reduction (default 1e-4) */
+    int profile;         /* time every finest-level smoother launch with CUDA events (disables graphs) */
+    int reserved[7];
+} sf_solve_opts;
+
+typedef struct {
+    int iters;               /* PCG iterations (FP64) or inner FCG iterations summed over outer steps */
+    int outer_iters;         /* mixed: iterative-refinement steps; FP64: 0 */
+    int levels;              /* multigrid levels used */
+    int converged;
+    long long unknowns;      /* liquid cells (pressure) or all cells (magnetic) */
+    double rel_residual;     /* ||b - A x|| / ||b|| of the solved system, FP64, recomputed after the solve */
+    double rel_residual_ref; /* same on the reference's operator (pinned row 0 for the potential) */
+    double ms_build, ms_solve, ms_post, ms_total; /* device time per phase (CUDA events), ms_total = wall */
+    long long h2d_bytes, d2h_bytes;
+    int status_detail;       /* 1: Krylov breakdown (non-positive curvature) */
+    int smooth_launches;     /* profile: finest-level smoother launches timed */
+    double smooth_ms;        /* profile: their summed device time */
+    long long kernel_launches; /* kernels this call launched (graph nodes counted per replay) */
+    int reserved[4];
+} sf_solve_stats;
+
+/* ----- context ------------------------------------------------------------------------------------------- */
+SF_EXPORT sf_status sf_create(int device, void *cuda_stream /* NULL = own non-blocking stream */, void **ctx_out);
+SF_EXPORT void sf_destroy(void *ctx);
+SF_EXPORT const char *sf_status_string(int status);
+SF_EXPORT const char *sf_last_error(void *ctx);
+SF_EXPORT int sf_abi_version(void);
+/* which: 0 = pressure defaults (tol 1e-8, amgcl's default), 1 = magnetic defaults (tol 1e-6,
+ * core/MagneticField.cpp:93). */
+SF_EXPORT void sf_default_opts(sf_solve_opts *opts, int which);
+/* Device bytes the context holds right now. */
+SF_EXPORT long long sf_device_bytes(void *ctx);
+
+/* ----- pressure projection ------------------------------------------------------------------------------
+ * Replaces Pressure::Project (core/Pressure.cpp:17-26): SetUnKnowns (:104-123), BuildProjectionMatrix
+ * (:38-78), SolveLinearSystem (:125-135, amgcl SA+SPAI0 BiCGStab there, MGPCG here) and ApplyProjection
+ * (:137-166).
+ *   vel[3]      in/out MAC velocity (face arrays)
+ *   phi         level set on cells; liquid where phi <= 0
+ *   frac[3]     collider solid fraction per face (Collider::GetFraction, 1 = solid)
+ *   solid_vel[3] collider velocity per face (Collider::Velocity), or NULL = 0
+ *   jump[3]     per-face value of the pressure-jump callback J(axis, face, theta) = p_liquid - p_air
+ *               (core/Pressure.h:20-22), read on liquid-air faces only, or NULL = no callback.  The shipped
+ *               callback ignores theta (core/Simulation.cpp:216-235); a theta-dependent callback cannot be
+ *               expressed as an array.
+ *   vol_error   volume-correction source added to every liquid row (core/Pressure.cpp:75)
+ *   p_out       optional (nx*ny*nz) pressure on cells, 0 in air
+ * Faces on the outer boundary of the grid are treated as closed walls (the reference reads outside its
+ * arrays there if they are open). */
+SF_EXPORT sf_status sf_pressure_project(void *ctx, const sf_grid *g, double *const vel[3], const double *phi,
+                              const double *const frac[3], const double *const solid_vel[3],
+                              const double *const jump[3], double vol_error, double *p_out,
+                              const sf_solve_opts *opts, sf_solve_stats *stats);
+SF_EXPORT sf_status sf_pressure_project_dev(void *ctx, const sf_grid *g, double *const vel[3], const double *phi,
+                                  const double *const frac[3], const double *const solid_vel[3],
+                                  const double *const jump[3], double vol_error, double *p_out,
+                                  const sf_solve_opts *opts, sf_solve_stats *stats);
+/* Replaces Pressure::Reproject (core/Pressure.cpp:28-36): keeps the unknowns and matrix of the last
+ * Project on this context, rebuilds only the right-hand side (SetRightHandSide, :80-102, no jump terms),
+ * starts from the last pressure and applies the projection with `jump`. */
+SF_EXPORT sf_status sf_pressure_reproject(void *ctx, const sf_grid *g, double *const vel[3], const double *phi,
+                                const double *const frac[3], const double *const solid_vel[3],
+                                const double *const jump[3], double vol_error, double *p_out,
+                                const sf_solve_opts *opts, sf_solve_stats *stats);
+SF_EXPORT sf_status sf_pressure_reproject_dev(void *ctx, const sf_grid *g, double *const vel[3], const double *phi,
+                                    const double *const frac[3], const double *const solid_vel[3],
+                                    const double *const jump[3], double vol_error, double *p_out,
+                                    const sf_solve_opts *opts, sf_solve_stats *stats);
+
+/* ----- magnetic potential -------------------------------------------------------------------------------
+ * Replaces MagneticField::Solve (core/MagneticField.cpp:29-35): mu on faces from the smoothed Heaviside of
+ * phi (BuildMatrix :51-60, Heaviside core/MagneticField.h:44-54), the full-grid variable-coefficient
+ * Laplacian with homogeneous Neumann walls and psi[0] = 0 (:62-90), the right-hand side (AssembleRHS
+ * :97-118), the solve (amgcl SA+SPAI0 CG there, MGPCG here) and AssignTotalField (:125-143).
+ *   phi          level set on the simulation's cell grid
+ *   chi          susceptibility (SetSusceptibility), band_width the Heaviside half-width (SetBandWidth)
+ *   hext[3]      applied field on faces
+ *   psi_out      optional (nx*ny*nz) potential, psi[0] = 0
+ *   H_out[3]     optional total field H = Hext - grad psi on faces (m_TotalField)
+ * The solve starts from the context's last potential on the same grid when opts->warm_start (m_Sol). */
+SF_EXPORT sf_status sf_magnetic_solve(void *ctx, const sf_grid *g, const double *phi, double chi, double band_width,
+                            const double *const hext[3], double *psi_out, double *const H_out[3],
+                            const sf_solve_opts *opts, sf_solve_stats *stats);
+SF_EXPORT sf_status sf_magnetic_solve_dev(void *ctx, const sf_grid *g, const double *phi, double chi, double band_width,
+                                const double *const hext[3], double *psi_out, double *const H_out[3],
+                                const sf_solve_opts *opts, sf_solve_stats *stats);
+/* ----- collider inputs ----------------------------------------------------------------------------------
+ * Solid fractions of the pressure solve (host code, run once per scene).
+ * sf_collider_box_fractions replaces Collider(sgrid) + Collider::Finish for the domain-box walls
+ * (core/Collider.cpp:8-19,21-45): node level set -0.01 h - sdf_box, FastMarching::Solve(LevelSet, -1)
+ * (core/FastMarching.cpp:25-62), then CalcFaceFraction (core/Collider.cpp:47-73) on every face.
+ * boundary_width is the staggered grid's boundary width (the box spans origin + bw h .. origin + (res-bw) h).
+ * node_ls_out (optional) receives the (nx+1)(ny+1)(nz+1) redistanced node level set.
+ * sf_collider_face_fractions runs CalcFaceFraction alone on a caller-supplied node level set. */
+SF_EXPORT sf_status sf_collider_box_fractions(const sf_grid *g, int boundary_width, double *const frac_out[3],
+                                              double *node_ls_out);
+SF_EXPORT sf_status sf_collider_face_fractions(const sf_grid *g, const double *node_ls, double *const frac_out[3]);
+
+/* Forget the magnetic warm start (MagneticField ctor zeroes m_Sol, core/MagneticField.cpp:26). */
+SF_EXPORT sf_status sf_magnetic_reset(void *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SFGPU_H */

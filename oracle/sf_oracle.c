@@ -1,0 +1,707 @@
+/*
+ * sf_oracle.c -- CPU restatement of the SimFerrofluid ghost-fluid pressure projection and the FDM
+ * magnetostatic potential solve.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: tests, the smoke check and the CPU-baseline leg of the
+ * benchmark call it to check (or time beside) the CUDA library.  Nothing in the product links it.
+ *
+ * Parity status: parity unpinned.  The reference ships no tests, no golden vectors and no known-answer data,
+ * and it cannot be compiled here (Eigen, amgcl, TBB, fmt/spdlog, yaml-cpp and cxxopts are absent), so this
+ * restatement is pinned only by the known-answer tests in tests/ (hydrostatic pressure, chi=0, slab field),
+ * by a second, independent pure-Python restatement on small grids, and by the committed fixtures that
+ * script generates.
+ *
+ * Floating point: compiled with -ffp-contract=off so that every a*b+c rounds twice, as in the reference's
+ * x86 build; the assembly loops evaluate each expression in the reference's order so that the CSR matrix
+ * and right-hand side are bit-identical to what the reference assembles from the same inputs.
+ *
+ * Layout (core/Grid.h:28): cell (i,j,k) -> k + nz*(j + ny*i), z fastest.  Face grid of axis a has size
+ * res + e_a (core/StaggeredGrid.h:16-20) with the same z-fastest indexing.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef struct {
+    int nx, ny, nz;
+    double h;
+    double ox, oy, oz; /* staggered-grid corner (StaggeredGrid::GetOrigin) */
+} or_grid;
+
+static inline int64_t cidx(const or_grid *g, int i, int j, int k) {
+    return (int64_t)k + (int64_t)g->nz * ((int64_t)j + (int64_t)g->ny * i);
+}
+static inline void fdims(const or_grid *g, int a, int *fx, int *fy, int *fz) {
+    *fx = g->nx + (a == 0);
+    *fy = g->ny + (a == 1);
+    *fz = g->nz + (a == 2);
+}
+static inline int64_t fidx(const or_grid *g, int a, int i, int j, int k) {
+    int fx, fy, fz;
+    fdims(g, a, &fx, &fy, &fz);
+    (void)fx;
+    return (int64_t)k + (int64_t)fz * ((int64_t)j + (int64_t)fy * i);
+}
+static inline int cell_valid(const or_grid *g, int i, int j, int k) {
+    return i >= 0 && j >= 0 && k >= 0 && i < g->nx && j < g->ny && k < g->nz;
+}
+/* Grid::NeighborOf / StaggeredGrid::FaceOfCell, FaceSideOfCell (core/Grid.h:37-40, core/StaggeredGrid.h:55-57):
+ * ord 0..5 = (-x,+x,-y,+y,-z,+z); face of cell = cell + e_axis*(ord&1); side = ord&1 ? +1 : -1. */
+static const int NB[6][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+
+int or_version(void) { return 3; }
+
+/* ------------------------------------------------------------------------------------------------------------
+ * Pressure::SetUnKnowns (core/Pressure.cpp:104-123): liquid = phi <= 0, numbered in (x,y,z) lexicographic
+ * order.  Returns n; fills grid2mat (N, -1 = air) and mat2grid (n).
+ * ---------------------------------------------------------------------------------------------------------- */
+int64_t or_pressure_unknowns(const or_grid *g, const double *phi, int32_t *grid2mat, int64_t *mat2grid) {
+    int64_t n = 0, N = (int64_t)g->nx * g->ny * g->nz;
+    for (int64_t c = 0; c < N; c++) {
+        if (phi[c] <= 0) {
+            grid2mat[c] = (int32_t)n;
+            mat2grid[n++] = c;
+        } else {
+            grid2mat[c] = -1;
+        }
+    }
+    return n;
+}
+
+/* Faces on the outer boundary of the grid have no cell on their far side.  The reference reads outside its
+ * arrays when such a face is open (weight > 0); this restatement, like the CUDA library, treats them as
+ * closed walls (weight 0).  The shipped scenes and every test scene have fraction 1 there. */
+static inline double face_weight(const or_grid *g, const double *const frac[3], int a, int i, int j, int k,
+                                 int ord) {
+    int ni = i + NB[ord][0], nj = j + NB[ord][1], nk = k + NB[ord][2];
+    if (!cell_valid(g, ni, nj, nk)) return 0.0;
+    int fi = i + (a == 0) * (ord & 1), fj = j + (a == 1) * (ord & 1), fk = k + (a == 2) * (ord & 1);
+    return 1.0 - frac[a][fidx(g, a, fi, fj, fk)];
+}
+
+/* ------------------------------------------------------------------------------------------------------------
+ * Pressure::BuildProjectionMatrix (core/Pressure.cpp:38-78).  CSR with ascending columns per row (Eigen's
+ * setFromTriplets order).  jump[a] is the per-face value J(axis, face, theta) of the reference's pressure-jump
+ * callback (core/Pressure.h:20-22); the shipped callback ignores theta (core/Simulation.cpp:216-235).
+ * us (solid velocity) and jump may be NULL (zero / no callback).  rowptr has n+1 entries; col/val up to 7n.
+ * ---------------------------------------------------------------------------------------------------------- */
+int64_t or_pressure_assemble(const or_grid *g, const double *phi, const double *const frac[3],
+                             const double *const u[3], const double *const us[3], const double *const jump[3],
+                             double volError, const int32_t *grid2mat, const int64_t *mat2grid, int64_t n,
+                             int64_t *rowptr, int32_t *col, double *val, double *rhs) {
+    int64_t nnz = 0;
+    rowptr[0] = 0;
+    for (int64_t r = 0; r < n; r++) {
+        int64_t c = mat2grid[r];
+        int i = (int)(c / g->nz / g->ny), j = (int)(c / g->nz % g->ny), k = (int)(c % g->nz);
+        double diag = 0, div = 0;
+        int32_t cc[7];
+        double cv[7];
+        int m = 0;
+        for (int ord = 0; ord < 6; ord++) {
+            int a = ord >> 1, side = (ord & 1) ? 1 : -1;
+            int fi = i + (a == 0) * (ord & 1), fj = j + (a == 1) * (ord & 1), fk = k + (a == 2) * (ord & 1);
+            int ni = i + NB[ord][0], nj = j + NB[ord][1], nk = k + NB[ord][2];
+            double w = face_weight(g, frac, a, i, j, k, ord);
+            int64_t f = fidx(g, a, fi, fj, fk);
+            if (w > 0) {
+                int64_t nb = cidx(g, ni, nj, nk);
+                int32_t cn = grid2mat[nb];
+                if (cn >= 0) {
+                    diag += w;
+                    cc[m] = cn;
+                    cv[m] = -w;
+                    m++;
+                } else {
+                    double theta = phi[c] / (phi[c] - phi[nb]);
+                    double ic = 1. / (theta < .001 ? .001 : theta); /* std::max(theta, .001) */
+                    diag += w * ic;
+                    if (jump) div += jump[a][f] * w * ic;
+                }
+                div -= (double)side * w * u[a][f];
+            }
+            if (w < 1) {
+                double usv = us ? us[a][f] : 0.0;
+                div -= (double)side * (1 - w) * usv;
+            }
+        }
+        div += volError;
+        rhs[r] = div;
+        cc[m] = (int32_t)r;
+        cv[m] = diag != 0 ? diag : 1.;
+        m++;
+        /* insertion sort by column */
+        for (int x = 1; x < m; x++) {
+            int32_t kc = cc[x];
+            double kv = cv[x];
+            int y = x - 1;
+            while (y >= 0 && cc[y] > kc) {
+                cc[y + 1] = cc[y];
+                cv[y + 1] = cv[y];
+                y--;
+            }
+            cc[y + 1] = kc;
+            cv[y + 1] = kv;
+        }
+        for (int x = 0; x < m; x++) {
+            col[nnz] = cc[x];
+            val[nnz] = cv[x];
+            nnz++;
+        }
+        rowptr[r + 1] = nnz;
+    }
+    return nnz;
+}
+
+/* Pressure::SetRightHandSide (core/Pressure.cpp:80-102): divergence + solid + volError, no jump terms. */
+void or_pressure_rhs(const or_grid *g, const double *const frac[3], const double *const u[3],
+                     const double *const us[3], double volError, const int64_t *mat2grid, int64_t n, double *rhs) {
+    for (int64_t r = 0; r < n; r++) {
+        int64_t c = mat2grid[r];
+        int i = (int)(c / g->nz / g->ny), j = (int)(c / g->nz % g->ny), k = (int)(c % g->nz);
+        double div = 0;
+        for (int ord = 0; ord < 6; ord++) {
+            int a = ord >> 1, side = (ord & 1) ? 1 : -1;
+            int fi = i + (a == 0) * (ord & 1), fj = j + (a == 1) * (ord & 1), fk = k + (a == 2) * (ord & 1);
+            double w = face_weight(g, frac, a, i, j, k, ord);
+            int64_t f = fidx(g, a, fi, fj, fk);
+            if (w > 0) div -= (double)side * w * u[a][f];
+            if (w < 1) {
+                double usv = us ? us[a][f] : 0.0;
+                div -= (double)side * (1 - w) * usv;
+            }
+        }
+        div += volError;
+        rhs[r] = div;
+    }
+}
+
+/* ------------------------------------------------------------------------------------------------------------
+ * Pressure::ApplyProjection (core/Pressure.cpp:137-166).  p is the reduced (liquid-only) solution.
+ * ---------------------------------------------------------------------------------------------------------- */
+void or_pressure_apply(const or_grid *g, const double *phi, const double *const frac[3], const double *const jump[3],
+                       const int32_t *grid2mat, const double *p, double *const u[3]) {
+    for (int a = 0; a < 3; a++) {
+        int fx, fy, fz;
+        fdims(g, a, &fx, &fy, &fz);
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int i = 0; i < fx; i++)
+            for (int j = 0; j < fy; j++)
+                for (int k = 0; k < fz; k++) {
+                    int64_t f = fidx(g, a, i, j, k);
+                    /* AdjCellOfFace(axis, face, 0) = face - e_axis, (.., 1) = face */
+                    int i0 = i - (a == 0), j0 = j - (a == 1), k0 = k - (a == 2);
+                    if (!cell_valid(g, i0, j0, k0) || !cell_valid(g, i, j, k)) continue; /* closed wall */
+                    double w = 1. - frac[a][f];
+                    if (w == 0.) continue;
+                    int64_t c0 = cidx(g, i0, j0, k0), c1 = cidx(g, i, j, k);
+                    int32_t id0 = grid2mat[c0], id1 = grid2mat[c1];
+                    if (id0 < 0 && id1 < 0) continue;
+                    if (id0 >= 0 && id1 >= 0) {
+                        u[a][f] -= (p[id1] - p[id0]) * w;
+                    } else {
+                        double phi0 = phi[c0], phi1 = phi[c1];
+                        double theta = phi0 / (phi0 - phi1);
+                        double pin = id0 >= 0 ? p[id0] : p[id1];
+                        double pj = jump ? jump[a][f] : 0.;
+                        double t = id0 >= 0 ? theta : 1 - theta;
+                        double ic = 1. / (t < .001 ? .001 : t);
+                        u[a][f] -= (id0 >= 0 ? +1 : -1) * (pj - pin) * ic * w;
+                    }
+                }
+    }
+}
+
+/* ------------------------------------------------------------------------------------------------------------
+ * Magnetic field (core/MagneticField.cpp, core/MagneticField.h:44-54, core/TriLerp.h:22-67).
+ * The solve grid is a boundary-width-0 staggered grid whose center is origin + res*h/2 of the simulation
+ * grid (core/MagneticField.cpp:13-16); its corner is recomputed from that center exactly as the reference
+ * does, so it can differ from the simulation corner in the last bit.
+ * ---------------------------------------------------------------------------------------------------------- */
+static double heaviside(double phi, double bw) {
+    const double pi = 3.141592653589793238462643383279502884;
+    if (phi < -bw) return 0.;
+    if (phi > bw) return 1.;
+    return .5 * (1. + phi / bw + sin(pi * phi / bw) / pi);
+}
+
+/* TriLerp::Interpolate(levelSet, pos) with Grid::CalcLower<1>, CalcLowerFrac and clamped At(). */
+static double trilerp_cell(const or_grid *g, const double *phi, double px, double py, double pz) {
+    double co[3] = {g->ox + g->h / 2, g->oy + g->h / 2, g->oz + g->h / 2}; /* cell grid origin */
+    double invh = 1 / g->h;
+    double p[3] = {px, py, pz};
+    int lo[3];
+    double fr[3];
+    int sz[3] = {g->nx, g->ny, g->nz};
+    for (int a = 0; a < 3; a++) {
+        lo[a] = (int)floor((p[a] - co[a]) * invh - 0.0);
+        fr[a] = (p[a] - co[a] - (double)lo[a] * g->h) * invh;
+    }
+    double w[2][3];
+    for (int a = 0; a < 3; a++) {
+        w[0][a] = 1. - fr[a];
+        w[1][a] = fr[a];
+    }
+    double val = 0;
+    for (int q = 0; q < 8; q++) {
+        int dx = q & 1, dy = (q >> 1) & 1, dz = (q >> 2) & 1;
+        int ci[3] = {lo[0] + dx, lo[1] + dy, lo[2] + dz};
+        for (int a = 0; a < 3; a++) ci[a] = ci[a] < 0 ? 0 : (ci[a] > sz[a] - 1 ? sz[a] - 1 : ci[a]);
+        double wt = w[dx][0] * w[dy][1] * w[dz][2];
+        val += phi[cidx(g, ci[0], ci[1], ci[2])] * wt;
+    }
+    return val;
+}
+
+void or_magnetic_grid_origin(const or_grid *g, double out[3]) {
+    int res[3] = {g->nx, g->ny, g->nz};
+    double o[3] = {g->ox, g->oy, g->oz};
+    for (int a = 0; a < 3; a++) {
+        double half = (double)res[a] * g->h / 2.;
+        double center = o[a] + half;
+        out[a] = center - (double)res[a] * g->h / 2;
+    }
+}
+
+/* BuildMatrix coefficient pass (core/MagneticField.cpp:51-60): mu on every face; 1 on boundary faces. */
+void or_magnetic_coeff(const or_grid *g, const double *phi, double chi, double bw, double *const mu[3]) {
+    double eo[3];
+    or_magnetic_grid_origin(g, eo);
+    for (int a = 0; a < 3; a++) {
+        int fx, fy, fz;
+        fdims(g, a, &fx, &fy, &fz);
+        int res_a = a == 0 ? g->nx : (a == 1 ? g->ny : g->nz);
+        double fo[3] = {eo[0] + (a == 0 ? 0 : 1) * g->h / 2, eo[1] + (a == 1 ? 0 : 1) * g->h / 2,
+                        eo[2] + (a == 2 ? 0 : 1) * g->h / 2};
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int i = 0; i < fx; i++)
+            for (int j = 0; j < fy; j++)
+                for (int k = 0; k < fz; k++) {
+                    int fa = a == 0 ? i : (a == 1 ? j : k);
+                    int64_t f = fidx(g, a, i, j, k);
+                    if (fa <= 0 || fa >= res_a) {
+                        mu[a][f] = 1.;
+                    } else {
+                        double px = fo[0] + (double)i * g->h, py = fo[1] + (double)j * g->h,
+                               pz = fo[2] + (double)k * g->h;
+                        mu[a][f] = 1. + (1. - heaviside(trilerp_cell(g, phi, px, py, pz), bw)) * chi;
+                    }
+                }
+    }
+}
+
+/* BuildMatrix matrix pass (core/MagneticField.cpp:62-90): row 0 pinned, column 0 dropped, Neumann walls. */
+int64_t or_magnetic_assemble(const or_grid *g, const double *const mu[3], int64_t *rowptr, int32_t *col,
+                             double *val) {
+    int64_t N = (int64_t)g->nx * g->ny * g->nz, nnz = 0;
+    rowptr[0] = 0;
+    for (int64_t r = 0; r < N; r++) {
+        if (r == 0) {
+            col[nnz] = 0;
+            val[nnz] = 1.;
+            nnz++;
+            rowptr[1] = nnz;
+            continue;
+        }
+        int i = (int)(r / g->nz / g->ny), j = (int)(r / g->nz % g->ny), k = (int)(r % g->nz);
+        double diag = 0.;
+        int32_t cc[7];
+        double cv[7];
+        int m = 0;
+        for (int ord = 0; ord < 6; ord++) {
+            int ni = i + NB[ord][0], nj = j + NB[ord][1], nk = k + NB[ord][2];
+            if (!cell_valid(g, ni, nj, nk)) continue;
+            int a = ord >> 1;
+            int fi = i + (a == 0) * (ord & 1), fj = j + (a == 1) * (ord & 1), fk = k + (a == 2) * (ord & 1);
+            double w = mu[a][fidx(g, a, fi, fj, fk)];
+            int64_t cn = cidx(g, ni, nj, nk);
+            if (cn != 0) {
+                cc[m] = (int32_t)cn;
+                cv[m] = -w;
+                m++;
+            }
+            diag += w;
+        }
+        cc[m] = (int32_t)r;
+        cv[m] = diag;
+        m++;
+        for (int x = 1; x < m; x++) {
+            int32_t kc = cc[x];
+            double kv = cv[x];
+            int y = x - 1;
+            while (y >= 0 && cc[y] > kc) {
+                cc[y + 1] = cc[y];
+                cv[y + 1] = cv[y];
+                y--;
+            }
+            cc[y + 1] = kc;
+            cv[y + 1] = kv;
+        }
+        for (int x = 0; x < m; x++) {
+            col[nnz] = cc[x];
+            val[nnz] = cv[x];
+            nnz++;
+        }
+        rowptr[r + 1] = nnz;
+    }
+    return nnz;
+}
+
+/* AssembleRHS (core/MagneticField.cpp:97-118).  rhs[0] = 0 as in the reference.  If rhs0_neumann is not NULL
+ * it receives the value row 0 would have had without the pin (used to check the compatibility identity). */
+void or_magnetic_rhs(const or_grid *g, const double *const mu[3], const double *const hext[3], double *rhs,
+                     double *rhs0_neumann) {
+    int64_t N = (int64_t)g->nx * g->ny * g->nz;
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < N; r++) {
+        int i = (int)(r / g->nz / g->ny), j = (int)(r / g->nz % g->ny), k = (int)(r % g->nz);
+        double b = 0;
+        for (int ord = 0; ord < 6; ord++) {
+            int ni = i + NB[ord][0], nj = j + NB[ord][1], nk = k + NB[ord][2];
+            if (!cell_valid(g, ni, nj, nk)) continue;
+            int a = ord >> 1, side = (ord & 1) ? 1 : -1;
+            int fi = i + (a == 0) * (ord & 1), fj = j + (a == 1) * (ord & 1), fk = k + (a == 2) * (ord & 1);
+            int64_t f = fidx(g, a, fi, fj, fk);
+            double w = mu[a][f];
+            b += (w - 1.) * hext[a][f] * (double)(-side) * g->h;
+        }
+        if (r == 0) {
+            if (rhs0_neumann) *rhs0_neumann = b;
+            rhs[r] = 0;
+        } else {
+            rhs[r] = b;
+        }
+    }
+}
+
+/* AssignTotalField (core/MagneticField.cpp:125-143): H = (psi_c0 - psi_c1)/h + Hext, Hext on boundary faces. */
+void or_magnetic_total_field(const or_grid *g, const double *psi, const double *const hext[3], double *const H[3]) {
+    double invh = 1 / g->h;
+    for (int a = 0; a < 3; a++) {
+        int fx, fy, fz;
+        fdims(g, a, &fx, &fy, &fz);
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int i = 0; i < fx; i++)
+            for (int j = 0; j < fy; j++)
+                for (int k = 0; k < fz; k++) {
+                    int64_t f = fidx(g, a, i, j, k);
+                    int i0 = i - (a == 0), j0 = j - (a == 1), k0 = k - (a == 2);
+                    double v = 0.;
+                    if (cell_valid(g, i0, j0, k0) && cell_valid(g, i, j, k))
+                        v = (psi[cidx(g, i0, j0, k0)] - psi[cidx(g, i, j, k)]) * invh;
+                    v += hext[a][f];
+                    H[a][f] = v;
+                }
+    }
+}
+
+/* ------------------------------------------------------------------------------------------------------------
+ * CSR helpers and an FP64 Jacobi-preconditioned CG used to produce the reference solution of a restated
+ * system to a tight tolerance.
+ * ---------------------------------------------------------------------------------------------------------- */
+void or_csr_spmv(int64_t n, const int64_t *rowptr, const int32_t *col, const double *val, const double *x,
+                 double *y) {
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < n; r++) {
+        double s = 0;
+        for (int64_t e = rowptr[r]; e < rowptr[r + 1]; e++) s += val[e] * x[col[e]];
+        y[r] = s;
+    }
+}
+
+static double dotp(int64_t n, const double *a, const double *b) {
+    double s = 0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+    for (int64_t i = 0; i < n; i++) s += a[i] * b[i];
+    return s;
+}
+
+/* Returns iterations (negative if not converged).  x is the initial guess on entry.  Stops on
+ * ||b - A x|| <= tol * ||b||. */
+int or_csr_pcg(int64_t n, const int64_t *rowptr, const int32_t *col, const double *val, const double *b,
+               double *x, double tol, int maxit, double *relres_out) {
+    double *r = malloc(sizeof(double) * n), *z = malloc(sizeof(double) * n), *p = malloc(sizeof(double) * n),
+           *q = malloc(sizeof(double) * n), *dinv = malloc(sizeof(double) * n);
+    for (int64_t i = 0; i < n; i++) {
+        double d = 0;
+        for (int64_t e = rowptr[i]; e < rowptr[i + 1]; e++)
+            if (col[e] == i) d = val[e];
+        dinv[i] = d != 0 ? 1.0 / d : 1.0;
+    }
+    or_csr_spmv(n, rowptr, col, val, x, q);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) r[i] = b[i] - q[i];
+    double nb = sqrt(dotp(n, b, b));
+    if (nb == 0) nb = 1;
+    double rr = sqrt(dotp(n, r, r));
+    int it = 0;
+    if (rr / nb <= tol) goto done;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+        z[i] = dinv[i] * r[i];
+        p[i] = z[i];
+    }
+    double rz = dotp(n, r, z);
+    for (it = 1; it <= maxit; it++) {
+        or_csr_spmv(n, rowptr, col, val, p, q);
+        double alpha = rz / dotp(n, p, q);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; i++) {
+            x[i] += alpha * p[i];
+            r[i] -= alpha * q[i];
+        }
+        rr = sqrt(dotp(n, r, r));
+        if (rr / nb <= tol) break;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; i++) z[i] = dinv[i] * r[i];
+        double rz2 = dotp(n, r, z);
+        double beta = rz2 / rz;
+        rz = rz2;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; i++) p[i] = z[i] + beta * p[i];
+    }
+done:
+    /* true residual */
+    or_csr_spmv(n, rowptr, col, val, x, q);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) r[i] = b[i] - q[i];
+    if (relres_out) *relres_out = sqrt(dotp(n, r, r)) / nb;
+    free(r);
+    free(z);
+    free(p);
+    free(q);
+    free(dinv);
+    return it > maxit ? -maxit : it;
+}
+
+int or_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------------------------------------------
+ * Collider inputs of the pressure solve (core/Collider.cpp:8-19,21-45,47-73): the node level set of the domain
+ * box walls, FastMarching::Solve(LevelSet, -1) (core/FastMarching.cpp:25-62) and the per-face solid fraction.
+ * bw is the staggered grid's boundary width; the domain box is [origin + bw*h, origin + (res - bw)*h].
+ * ---------------------------------------------------------------------------------------------------------- */
+typedef struct {
+    double v;
+    int64_t i;
+} heap_el;
+typedef struct {
+    heap_el *a;
+    int64_t n, cap;
+} heap_t;
+static int hless(heap_el x, heap_el y) { return x.v < y.v || (x.v == y.v && x.i < y.i); }
+static void hpush(heap_t *h, double v, int64_t i) {
+    if (h->n == h->cap) {
+        h->cap = h->cap ? h->cap * 2 : 1024;
+        h->a = realloc(h->a, sizeof(heap_el) * h->cap);
+    }
+    int64_t c = h->n++;
+    heap_el e = {v, i};
+    while (c > 0) {
+        int64_t p = (c - 1) / 2;
+        if (!hless(e, h->a[p])) break;
+        h->a[c] = h->a[p];
+        c = p;
+    }
+    h->a[c] = e;
+}
+static heap_el hpop(heap_t *h) {
+    heap_el top = h->a[0], last = h->a[--h->n];
+    int64_t c = 0;
+    for (;;) {
+        int64_t l = 2 * c + 1, r = l + 1, m = c;
+        heap_el best = last;
+        if (l < h->n && hless(h->a[l], best)) {
+            m = l;
+            best = h->a[l];
+        }
+        if (r < h->n && hless(h->a[r], best)) m = r;
+        if (m == c) break;
+        h->a[c] = h->a[m];
+        c = m;
+    }
+    if (h->n > 0) h->a[c] = last;
+    return top;
+}
+static inline double dmin(double a, double b) { return (b < a) ? b : a; } /* std::min(a, b) */
+
+static double sq2(double p0, double p1, double dx) { /* SolveQuadratic(p0, p1, dx) */
+    if (p0 > p1) {
+        double t = p0;
+        p0 = p1;
+        p1 = t;
+    }
+    if (isinf(p1) || p1 - p0 > dx) return p0 + dx;
+    return ((p0 + p1) + sqrt(2 * dx * dx - (p0 - p1) * (p0 - p1))) * .5;
+}
+static double sq3(double p0, double p1, double p2, double dx) { /* SolveQuadratic(p0, p1, p2, dx) */
+    double t;
+    if (p0 > p1) { t = p0; p0 = p1; p1 = t; }
+    if (p1 > p2) { t = p1; p1 = p2; p2 = t; }
+    if (isinf(p2) || (p2 - p0) * (p2 - p0) + (p2 - p1) * (p2 - p1) > dx * dx) return sq2(p0, p1, dx);
+    return (p0 + p1 + p2 + sqrt((p0 + p1 + p2) * (p0 + p1 + p2) - 3 * (p0 * p0 + p1 * p1 + p2 * p2 - dx * dx))) / 3;
+}
+
+typedef struct {
+    int sx, sy, sz;
+    double h;
+} ngrid;
+static inline int nvalid(const ngrid *g, int i, int j, int k) {
+    return i >= 0 && j >= 0 && k >= 0 && i < g->sx && j < g->sy && k < g->sz;
+}
+static inline int64_t nidx(const ngrid *g, int i, int j, int k) {
+    return (int64_t)k + (int64_t)g->sz * ((int64_t)j + (int64_t)g->sy * i);
+}
+static double eikonal(const ngrid *g, int i, int j, int k, const int8_t *vis, const double *tent) {
+    double tp[3] = {INFINITY, INFINITY, INFINITY};
+    for (int ord = 0; ord < 6; ord++) {
+        int ni = i + NB[ord][0], nj = j + NB[ord][1], nk = k + NB[ord][2];
+        if (nvalid(g, ni, nj, nk) && vis[nidx(g, ni, nj, nk)]) tp[ord >> 1] = dmin(tp[ord >> 1], tent[nidx(g, ni, nj, nk)]);
+    }
+    return sq3(tp[0], tp[1], tp[2], g->h);
+}
+static void update_nbs(const ngrid *g, int i, int j, int k, const int8_t *vis, double *tent, heap_t *hp) {
+    for (int ord = 0; ord < 6; ord++) {
+        int ni = i + NB[ord][0], nj = j + NB[ord][1], nk = k + NB[ord][2];
+        if (!nvalid(g, ni, nj, nk)) continue;
+        int64_t nb = nidx(g, ni, nj, nk);
+        if (vis[nb]) continue;
+        double t = eikonal(g, ni, nj, nk, vis, tent);
+        if (t < tent[nb]) {
+            tent[nb] = t;
+            hpush(hp, t, nb);
+        }
+    }
+}
+
+/* FastMarching::Solve(phi, maxSteps <= 0): full-grid redistancing of a node level set. */
+void or_fast_marching(int sx, int sy, int sz, double h, double *phi) {
+    ngrid g = {sx, sy, sz, h};
+    int64_t M = (int64_t)sx * sy * sz;
+    int8_t *vis = calloc(M, 1);
+    double *tent = malloc(sizeof(double) * M);
+    int64_t *intf = malloc(sizeof(int64_t) * M), nintf = 0;
+    heap_t hp = {0, 0, 0};
+    for (int64_t c = 0; c < M; c++) tent[c] = INFINITY;
+    for (int i = 0; i < sx; i++)
+        for (int j = 0; j < sy; j++)
+            for (int k = 0; k < sz; k++) {
+                int64_t c = nidx(&g, i, j, k);
+                double tp[3] = {INFINITY, INFINITY, INFINITY};
+                for (int ord = 0; ord < 6; ord++) {
+                    int ni = i + NB[ord][0], nj = j + NB[ord][1], nk = k + NB[ord][2];
+                    if (!nvalid(&g, ni, nj, nk)) continue;
+                    int64_t nb = nidx(&g, ni, nj, nk);
+                    if (phi[c] * phi[nb] <= 0) tp[ord >> 1] = dmin(tp[ord >> 1], phi[c] / (phi[c] - phi[nb]) * h);
+                }
+                if (isfinite(tp[0]) || isfinite(tp[1]) || isfinite(tp[2])) {
+                    double a = 1. / tp[0], b = 1. / tp[1], d = 1. / tp[2];
+                    tent[c] = 1. / sqrt((a * a + b * b) + d * d);
+                    vis[c] = 1;
+                    intf[nintf++] = c;
+                }
+            }
+    for (int64_t q = 0; q < nintf; q++) {
+        int64_t c = intf[q];
+        update_nbs(&g, (int)(c / sz / sy), (int)(c / sz % sy), (int)(c % sz), vis, tent, &hp);
+    }
+    while (hp.n > 0) {
+        heap_el e = hpop(&hp);
+        if (tent[e.i] != e.v) continue;
+        vis[e.i] = 1;
+        update_nbs(&g, (int)(e.i / sz / sy), (int)(e.i / sz % sy), (int)(e.i % sz), vis, tent, &hp);
+    }
+    for (int64_t c = 0; c < M; c++) phi[c] = (phi[c] <= 0 ? -1 : 1) * tent[c];
+    free(vis);
+    free(tent);
+    free(intf);
+    free(hp.a);
+}
+
+/* ImplicitBox::SignedDistanceTo (core/ImplicitSurface.h:82-111). */
+static double box_sdf(const double c[3], const double hl[3], const double p[3]) {
+    double q[3];
+    int inside = 1;
+    for (int a = 0; a < 3; a++) {
+        q[a] = fabs(p[a] - c[a]) - hl[a];
+        if (!(q[a] <= 0)) inside = 0;
+    }
+    if (inside) {
+        double m = q[0];
+        if (q[1] > m) m = q[1];
+        if (q[2] > m) m = q[2];
+        return m;
+    }
+    double s = 0;
+    double t[3];
+    for (int a = 0; a < 3; a++) t[a] = q[a] > 0 ? q[a] : 0;
+    s = (t[0] * t[0] + t[1] * t[1]) + t[2] * t[2];
+    return sqrt(s);
+}
+
+/* Collider ctor node level set (core/Collider.cpp:14-18): LS = -0.01 h - sdf_box(node). */
+void or_collider_box_levelset(const or_grid *g, int bw, double *ls) {
+    int sx = g->nx + 1, sy = g->ny + 1, sz = g->nz + 1;
+    int res[3] = {g->nx, g->ny, g->nz};
+    double o[3] = {g->ox, g->oy, g->oz};
+    double c[3], hl[3];
+    for (int a = 0; a < 3; a++) {
+        double mn = o[a] + (double)bw * g->h;
+        double len = (double)(res[a] - bw * 2) * g->h;
+        c[a] = mn + len / 2;
+        hl[a] = len / 2;
+    }
+    for (int i = 0; i < sx; i++)
+        for (int j = 0; j < sy; j++)
+            for (int k = 0; k < sz; k++) {
+                double p[3] = {o[0] + (double)i * g->h, o[1] + (double)j * g->h, o[2] + (double)k * g->h};
+                ls[(int64_t)k + (int64_t)sz * ((int64_t)j + (int64_t)sy * i)] = -.01 * g->h - box_sdf(c, hl, p);
+            }
+}
+
+static double tri_fraction(double p0, double p1, double p2) {
+    double t;
+    if (p0 > p1) { t = p0; p0 = p1; p1 = t; }
+    if (p1 > p2) { t = p1; p1 = p2; p2 = t; }
+    if (p0 > p1) { t = p0; p0 = p1; p1 = t; }
+    if (p2 <= 0) return 1.;
+    if (p1 <= 0) return 1. - (p2 / (p2 - p0)) * (p2 / (p2 - p1));
+    if (p0 <= 0) return (p0 / (p0 - p1)) * (p0 / (p0 - p2));
+    return 0.;
+}
+
+/* Collider::CalcFaceFraction (core/Collider.cpp:47-73) over all faces of the three face grids. */
+void or_collider_face_fractions(const or_grid *g, const double *ls, double *const frac[3]) {
+    int sy = g->ny + 1, sz = g->nz + 1;
+    for (int a = 0; a < 3; a++) {
+        int fx, fy, fz;
+        fdims(g, a, &fx, &fy, &fz);
+        int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int i = 0; i < fx; i++)
+            for (int j = 0; j < fy; j++)
+                for (int k = 0; k < fz; k++) {
+                    double p[4];
+                    for (int q = 0; q < 4; q++) {
+                        int n[3] = {i, j, k};
+                        n[b1] += q & 1;
+                        n[b2] += (q >> 1) & 1;
+                        p[q] = ls[(int64_t)n[2] + (int64_t)sz * ((int64_t)n[1] + (int64_t)sy * n[0])];
+                    }
+                    double cp = (p[0] + p[1] + p[2] + p[3]) * .25;
+                    double ff = (tri_fraction(cp, p[0], p[1]) + tri_fraction(cp, p[1], p[3]) +
+                                 tri_fraction(cp, p[3], p[2]) + tri_fraction(cp, p[2], p[0])) * .25;
+                    frac[a][fidx(g, a, i, j, k)] = ff > .9 ? 1. : ff;
+                }
+    }
+}

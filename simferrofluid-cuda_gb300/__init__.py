@@ -1,0 +1,281 @@
+"""sf-gb300: GB300-native (sm_103a) drop-in for the two grid solves of a SimFerrofluid substep.
+
+Host-side mirror of the reference's solver classes over the C ABI (include/sfgpu.h):
+
+* :class:`Pressure` -- ``Pressure(StaggeredGrid)``, ``SetPressureJump``, ``Project``, ``Reproject``
+  (core/Pressure.h:8-22).
+* :class:`MagneticField` -- ``MagneticField(StaggeredGrid, chi, bandWidth)``, ``SetSusceptibility``,
+  ``SetBandWidth``, ``Solve`` (core/MagneticField.h:24-36); the potential and the total field, private in
+  the reference, are exposed as ``potential`` and ``total_field``.
+* :class:`StaggeredGrid` -- the geometry of core/StaggeredGrid.h:8-21 (cell grid and face grids).
+
+Arrays are numpy float64 in the reference's layout (C-contiguous ``(nx, ny, nz)`` cells, face grid ``a`` of
+shape ``res + e_a``) for the host entry points, or CUDA tensors / objects with ``data_ptr()`` for the
+device entry points (``device=True``).  Every call runs the CUDA library; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import SF_PREC_FP64, SF_PREC_MIXED  # noqa: F401
+
+__all__ = ["StaggeredGrid", "Context", "Pressure", "MagneticField", "SolveError", "options", "load_library",
+           "SF_PREC_FP64", "SF_PREC_MIXED"]
+
+
+def load_library():
+    return _abi.load()
+
+
+class SolveError(RuntimeError):
+    def __init__(self, status, msg, stats=None):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+        self.stats = stats
+
+
+@dataclass(frozen=True)
+class StaggeredGrid:
+    """StaggeredGrid(boundaryWidth, spacing, resolution, center) (core/StaggeredGrid.h:10-21)."""
+    boundary_width: int
+    spacing: float
+    resolution: tuple
+    center: tuple = (0.0, 0.0, 0.0)
+
+    @property
+    def origin(self):
+        # m_Origin = center - resolution * spacing / 2
+        return tuple(float(c) - float(r) * float(self.spacing) / 2 for c, r in zip(self.center, self.resolution))
+
+    @property
+    def shape(self):
+        return tuple(int(r) for r in self.resolution)
+
+    @property
+    def num_cells(self):
+        nx, ny, nz = self.shape
+        return nx * ny * nz
+
+    def face_shape(self, axis):
+        s = list(self.shape)
+        s[axis] += 1
+        return tuple(s)
+
+    def domain_origin(self):
+        return tuple(o + self.boundary_width * self.spacing for o in self.origin)
+
+    @staticmethod
+    def from_origin(spacing, resolution, origin=(0.0, 0.0, 0.0), boundary_width=0):
+        """Grid whose corner is ``origin`` (center computed back from it)."""
+        center = tuple(float(o) + float(r) * float(spacing) / 2 for o, r in zip(origin, resolution))
+        g = StaggeredGrid(boundary_width, spacing, tuple(resolution), center)
+        return g
+
+    def c_grid(self, origin=None):
+        g = _abi.sf_grid()
+        g.nx, g.ny, g.nz = self.shape
+        g.h = float(self.spacing)
+        o = self.origin if origin is None else origin
+        for a in range(3):
+            g.origin[a] = float(o[a])
+        return g
+
+
+def options(which="pressure", **kw):
+    """sf_solve_opts with the library defaults (tol 1e-8 pressure, 1e-6 magnetic) updated by ``kw``.
+
+    ``precision`` accepts "fp64" / "mixed" or the SF_PREC_* constants."""
+    lib = load_library()
+    o = _abi.sf_solve_opts()
+    lib.sf_default_opts(C.byref(o), 0 if which == "pressure" else 1)
+    for k, v in kw.items():
+        if k == "precision" and isinstance(v, str):
+            v = {"fp64": SF_PREC_FP64, "mixed": SF_PREC_MIXED}[v]
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o
+
+
+class Context:
+    """One CUDA stream and the device workspaces of both solvers (sf_create / sf_destroy)."""
+
+    def __init__(self, device: int = 0, stream=None):
+        self.lib = load_library()
+        h = C.c_void_p()
+        s = self.lib.sf_create(int(device), C.c_void_p(int(stream) if stream is not None else 0), C.byref(h))
+        if s != _abi.SF_OK:
+            raise SolveError(s, "sf_create failed: " + self.lib.sf_status_string(s).decode())
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.sf_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_error(self):
+        return self.lib.sf_last_error(self.handle).decode()
+
+    def device_bytes(self):
+        return int(self.lib.sf_device_bytes(self.handle))
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _host_f64(a, shape, name, writable=False):
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+        if writable:
+            raise TypeError(f"{name}: must be a C-contiguous float64 numpy array (updated in place)")
+        a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.shape != tuple(shape) and a.size != int(np.prod(shape)):
+        raise ValueError(f"{name}: shape {a.shape}, expected {tuple(shape)}")
+    return a
+
+
+def _ptr(a, shape, name, device, writable=False, keep=None):
+    if a is None:
+        return None
+    if device:
+        n = a.numel() if hasattr(a, "numel") else None
+        if n is not None and n != int(np.prod(shape)):
+            raise ValueError(f"{name}: {n} elements, expected {int(np.prod(shape))}")
+        return int(a.data_ptr())
+    a = _host_f64(a, shape, name, writable)
+    if keep is not None:
+        keep.append(a)
+    return a.ctypes.data
+
+
+def _check(ctx, status, stats, what, raise_on_nonconv):
+    if status == _abi.SF_OK or status == _abi.SF_STALLED_FALLBACK:
+        return
+    if status == _abi.SF_NOT_CONVERGED and not raise_on_nonconv:
+        return
+    raise SolveError(status, f"{what}: {ctx.last_error()}", stats)
+
+
+class Pressure:
+    """Ghost-fluid pressure projection (core/Pressure.h:8-56) on the GPU."""
+
+    def __init__(self, sgrid: StaggeredGrid, ctx: Context | None = None):
+        self.grid = sgrid
+        self.ctx = ctx or default_context()
+        self.jump = None
+        self.pressure = None
+        self.stats = None
+
+    def set_pressure_jump(self, jump):
+        """Per-face J(axis, face) = p_liquid - p_air on liquid-air faces (three face arrays), or None.
+
+        The reference takes a callback J(axis, face, theta) (core/Pressure.h:20-22); the shipped one ignores
+        theta (core/Simulation.cpp:216-235), so an array of its values per face is equivalent."""
+        self.jump = jump
+
+    def _call(self, fn, velocity, level_set, fraction, solid_velocity, vol_error, opts, device, p_out,
+              raise_on_nonconv):
+        g = self.grid
+        keep = []
+        fs = [g.face_shape(a) for a in range(3)]
+        vel = [_ptr(velocity[a], fs[a], f"velocity[{a}]", device, True, keep) for a in range(3)]
+        fr = [_ptr(fraction[a], fs[a], f"fraction[{a}]", device, False, keep) for a in range(3)]
+        phi = _ptr(level_set, g.shape, "level_set", device, False, keep)
+        us = None if solid_velocity is None else [_ptr(solid_velocity[a], fs[a], "solid_velocity", device,
+                                                       False, keep) for a in range(3)]
+        jp = None if self.jump is None else [_ptr(self.jump[a], fs[a], "jump", device, False, keep)
+                                             for a in range(3)]
+        if p_out is None and not device:
+            p_out = np.zeros(g.shape)
+        pp = _ptr(p_out, g.shape, "p_out", device, True) if p_out is not None else None
+        us_ref = _abi.p3_ref(us)
+        jp_ref = _abi.p3_ref(jp)
+        st = _abi.sf_solve_stats()
+        o = opts if opts is not None else options("pressure")
+        s = fn(self.ctx.handle, C.byref(g.c_grid()), _abi.p3(vel), C.c_void_p(phi), _abi.p3(fr),
+               us_ref[0] if us_ref else None, jp_ref[0] if jp_ref else None, float(vol_error),
+               C.c_void_p(pp) if pp else None, C.byref(o), C.byref(st))
+        self.stats = st.as_dict()
+        _check(self.ctx, s, self.stats, "pressure projection", raise_on_nonconv)
+        self.pressure = p_out
+        self.status = s
+        return self.stats
+
+    def project(self, velocity, level_set, fraction, solid_velocity=None, vol_error=0.0, opts=None, device=False,
+                p_out=None, raise_on_nonconv=True):
+        """Pressure::Project: velocity (3 face arrays) is updated in place; returns the solve statistics."""
+        fn = self.ctx.lib.sf_pressure_project_dev if device else self.ctx.lib.sf_pressure_project
+        return self._call(fn, velocity, level_set, fraction, solid_velocity, vol_error, opts, device, p_out,
+                          raise_on_nonconv)
+
+    def reproject(self, velocity, level_set, fraction, solid_velocity=None, vol_error=0.0, opts=None, device=False,
+                  p_out=None, raise_on_nonconv=True):
+        """Pressure::Reproject: same unknowns and matrix as the last project(), new right-hand side."""
+        fn = self.ctx.lib.sf_pressure_reproject_dev if device else self.ctx.lib.sf_pressure_reproject
+        return self._call(fn, velocity, level_set, fraction, solid_velocity, vol_error, opts, device, p_out,
+                          raise_on_nonconv)
+
+
+class MagneticField:
+    """FDM magnetostatic potential (core/MagneticField.h:15-71) on the GPU."""
+
+    def __init__(self, sgrid: StaggeredGrid, susceptibility: float, band_width: float, ctx: Context | None = None):
+        self.grid = sgrid
+        self.ctx = ctx or default_context()
+        self.chi = float(susceptibility)
+        self.band_width = float(band_width)
+        self.potential = None
+        self.total_field = None
+        self.stats = None
+        self.ctx.lib.sf_magnetic_reset(self.ctx.handle)  # m_Sol starts at zero (core/MagneticField.cpp:26)
+
+    def set_susceptibility(self, chi):
+        self.chi = float(chi)
+
+    def set_band_width(self, bw):
+        self.band_width = float(bw)
+
+    def solve(self, level_set, external_field, opts=None, device=False, psi_out=None, H_out=None,
+              raise_on_nonconv=True):
+        """MagneticField::Solve: returns statistics; ``potential`` and ``total_field`` hold the results."""
+        g = self.grid
+        keep = []
+        fs = [g.face_shape(a) for a in range(3)]
+        phi = _ptr(level_set, g.shape, "level_set", device, False, keep)
+        he = [_ptr(external_field[a], fs[a], f"external_field[{a}]", device, False, keep) for a in range(3)]
+        if not device:
+            if psi_out is None:
+                psi_out = np.zeros(g.shape)
+            if H_out is None:
+                H_out = [np.zeros(fs[a]) for a in range(3)]
+        pp = _ptr(psi_out, g.shape, "psi_out", device, True) if psi_out is not None else None
+        hp = None if H_out is None else [_ptr(H_out[a], fs[a], "H_out", device, True) for a in range(3)]
+        hp_ref = _abi.p3_ref(hp)
+        st = _abi.sf_solve_stats()
+        o = opts if opts is not None else options("magnetic")
+        fn = self.ctx.lib.sf_magnetic_solve_dev if device else self.ctx.lib.sf_magnetic_solve
+        s = fn(self.ctx.handle, C.byref(g.c_grid()), C.c_void_p(phi), self.chi, self.band_width, _abi.p3(he),
+               C.c_void_p(pp) if pp else None, hp_ref[0] if hp_ref else None, C.byref(o), C.byref(st))
+        self.stats = st.as_dict()
+        _check(self.ctx, s, self.stats, "magnetic solve", raise_on_nonconv)
+        self.potential = psi_out
+        self.total_field = H_out
+        self.status = s
+        return self.stats

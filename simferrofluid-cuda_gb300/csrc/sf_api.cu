@@ -1,0 +1,440 @@
+// sf_api.cu -- the C ABI (include/sfgpu.h): context, host<->device staging and the two solve entry points.
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "sf_ops.h"
+#include "sf_solver.h"
+#include "sfgpu.h"
+
+using namespace sf;
+
+namespace {
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    std::string err;
+    std::unique_ptr<MGSolver> pres, mag;
+    bool pres_ready = false;
+    Dims pres_dims{0, 0, 0, 0};
+    bool mag_has_x = false;
+    Dims mag_dims{0, 0, 0, 0};
+    // staging buffers for the host-pointer entry points
+    DevBuf phi, frac[3], vel[3], us[3], jump[3], hext[3], H[3], cells;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+Ctx *C(void *p) { return reinterpret_cast<Ctx *>(p); }
+
+sf_status fail(Ctx *c, sf_status s, const std::string &msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+sf_status cuda_fail(Ctx *c, cudaError_t e, const char *where) {
+    return fail(c, e == cudaErrorMemoryAllocation ? SF_OUT_OF_MEMORY : SF_CUDA_ERROR,
+                std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                        \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, #call);          \
+    } while (0)
+
+bool grid_ok(const sf_grid *g) {
+    return g && g->nx > 0 && g->ny > 0 && g->nz > 0 && g->h > 0 && std::isfinite(g->h) &&
+           (long long)g->nx * g->ny * g->nz < (1LL << 31) && (long long)(g->nx + 1) * (g->ny + 1) * (g->nz + 1) < (1LL << 31);
+}
+
+long long face_count(const sf_grid *g, int a) {
+    return (long long)(g->nx + (a == 0)) * (g->ny + (a == 1)) * (g->nz + (a == 2));
+}
+
+SolverParams params_from(const sf_solve_opts *o, int which) {
+    sf_solve_opts def;
+    sf_default_opts(&def, which);
+    if (!o) o = &def;
+    SolverParams p;
+    p.precision = o->precision;
+    p.tol = o->tol > 0 ? o->tol : def.tol;
+    p.max_iters = o->max_iters > 0 ? o->max_iters : def.max_iters;
+    p.pre = o->pre_smooth > 0 ? o->pre_smooth : def.pre_smooth;
+    p.post = o->post_smooth > 0 ? o->post_smooth : def.post_smooth;
+    p.coarse_sweeps = o->coarse_sweeps > 0 ? o->coarse_sweeps : def.coarse_sweeps;
+    p.max_levels = o->max_levels;
+    p.coarse_dim = o->coarse_dim > 0 ? o->coarse_dim : def.coarse_dim;
+    p.use_graph = o->use_graph != 0;
+    p.check_every = o->check_every > 0 ? o->check_every : 1;
+    p.inner_tol = o->inner_tol > 0 ? o->inner_tol : def.inner_tol;
+    p.flexible = false;
+    p.profile = o->profile != 0;
+    return p;
+}
+
+bool opts_ok(const sf_solve_opts *o) {
+    if (!o) return true;
+    if (o->precision != SF_PREC_FP64 && o->precision != SF_PREC_MIXED) return false;
+    if (o->max_levels < 0 || o->coarse_dim < 0) return false;
+    return true;
+}
+
+// Stage a host array into a device buffer (or pass a device pointer through).
+sf_status stage_in(Ctx *c, DevBuf &buf, const double *src, long long n, bool dev, const double **out, long long &h2d) {
+    if (!src) {
+        *out = nullptr;
+        return SF_OK;
+    }
+    if (dev) {
+        *out = src;
+        return SF_OK;
+    }
+    CK(buf.ensure(8 * (size_t)n));
+    CK(cudaMemcpyAsync(buf.get(), src, 8 * (size_t)n, cudaMemcpyHostToDevice, c->st));
+    h2d += 8 * n;
+    *out = (const double *)buf.get();
+    return SF_OK;
+}
+
+void fill_stats(sf_solve_stats *s, const SolveResult &r, long long unknowns) {
+    if (!s) return;
+    s->iters = r.iters;
+    s->outer_iters = r.outer;
+    s->levels = r.levels;
+    s->converged = r.converged ? 1 : 0;
+    s->unknowns = unknowns;
+    s->smooth_launches = r.smooth_launches;
+    s->smooth_ms = r.smooth_ms;
+}
+
+float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+// ------------------------------------------------------------------------------------------------ pressure
+sf_status pressure_impl(Ctx *c, const sf_grid *g, double *const vel[3], const double *phi, const double *const frac[3],
+                        const double *const us[3], const double *const jump[3], double vol_error, double *p_out,
+                        const sf_solve_opts *opts, sf_solve_stats *stats, bool dev, bool reproject) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!c) return SF_BAD_ARG;
+    if (!grid_ok(g) || !vel || !phi || !frac || !opts_ok(opts)) return fail(c, SF_BAD_ARG, "bad grid, pointer or option");
+    for (int a = 0; a < 3; a++)
+        if (!vel[a] || !frac[a]) return fail(c, SF_BAD_ARG, "null velocity or fraction array");
+    if (us)
+        for (int a = 0; a < 3; a++)
+            if (!us[a]) return fail(c, SF_BAD_ARG, "solid_vel must hold three arrays or be NULL");
+    if (jump)
+        for (int a = 0; a < 3; a++)
+            if (!jump[a]) return fail(c, SF_BAD_ARG, "jump must hold three arrays or be NULL");
+    if (!std::isfinite(vol_error)) return fail(c, SF_BAD_ARG, "vol_error is not finite");
+    CK(cudaSetDevice(c->device));
+    const Dims d = make_dims(g->nx, g->ny, g->nz);
+    if (reproject && !(c->pres_ready && c->pres_dims.nx == d.nx && c->pres_dims.ny == d.ny && c->pres_dims.nz == d.nz))
+        return fail(c, SF_NOT_READY, "Reproject needs a previous Project on the same grid");
+    if (stats) memset(stats, 0, sizeof(*stats));
+    long long h2d = 0, d2h = 0;
+    const double *dphi;
+    Faces ffrac{}, fvel{}, fus{}, fjump{};
+    sf_status s;
+    if ((s = stage_in(c, c->phi, phi, d.n, dev, &dphi, h2d)) != SF_OK) return s;
+    for (int a = 0; a < 3; a++) {
+        const long long nf = face_count(g, a);
+        if ((s = stage_in(c, c->frac[a], frac[a], nf, dev, &ffrac.p[a], h2d)) != SF_OK) return s;
+        if ((s = stage_in(c, c->vel[a], vel[a], nf, dev, &fvel.p[a], h2d)) != SF_OK) return s;
+        if ((s = stage_in(c, c->us[a], us ? us[a] : nullptr, nf, dev, &fus.p[a], h2d)) != SF_OK) return s;
+        if ((s = stage_in(c, c->jump[a], jump ? jump[a] : nullptr, nf, dev, &fjump.p[a], h2d)) != SF_OK) return s;
+    }
+    if (!c->pres) c->pres = std::make_unique<MGSolver>(c->st);
+    MGSolver &S = *c->pres;
+    SolverParams prm = params_from(opts, 0);
+    CK(S.configure(d, prm));
+    CK(cudaEventRecord(c->ev[0], c->st));
+    launch_build_pressure(c->st, d, dphi, ffrac, fvel, fus, fjump, vol_error, S.fine(), S.b(), reproject);
+    if (!reproject) CK(S.build_hierarchy());
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(c->ev[1], c->st));
+    SolveResult res;
+    // Project starts from zero (core/Pressure.cpp:122); Reproject from the last pressure (:33)
+    CK(S.solve(!reproject, res));
+    double relres = res.relres, bn = res.bnorm;
+    const bool report = !opts || opts->report_ref_residual;
+    if (report) CK(S.true_relres(false, relres, bn));
+    CK(cudaEventRecord(c->ev[2], c->st));
+    launch_apply_projection(c->st, d, dphi, ffrac, fjump, S.x(), fvel);
+    double *pdst = nullptr;
+    if (p_out) {
+        if (dev) {
+            pdst = p_out;
+        } else {
+            CK(c->cells.ensure(8 * (size_t)d.n));
+            pdst = (double *)c->cells.get();
+        }
+        launch_gather_cells(c->st, d.n, S.fine().D, S.x(), pdst);
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(c->ev[3], c->st));
+    if (!dev) {
+        for (int a = 0; a < 3; a++) {
+            const long long nf = face_count(g, a);
+            CK(cudaMemcpyAsync(vel[a], fvel.p[a], 8 * (size_t)nf, cudaMemcpyDeviceToHost, c->st));
+            d2h += 8 * nf;
+        }
+        if (p_out) {
+            CK(cudaMemcpyAsync(p_out, pdst, 8 * (size_t)d.n, cudaMemcpyDeviceToHost, c->st));
+            d2h += 8 * d.n;
+        }
+    }
+    CK(cudaStreamSynchronize(c->st));
+    c->pres_ready = true;
+    c->pres_dims = d;
+    fill_stats(stats, res, -1);
+    if (stats) stats->kernel_launches = S.take_launches() + 1 + 3 + (p_out ? 1 : 0);
+    if (stats) {
+        stats->rel_residual = relres;
+        stats->rel_residual_ref = relres;
+        stats->ms_build = ev_ms(c->ev[0], c->ev[1]);
+        stats->ms_solve = ev_ms(c->ev[1], c->ev[2]);
+        stats->ms_post = ev_ms(c->ev[2], c->ev[3]);
+        stats->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        stats->h2d_bytes = h2d;
+        stats->d2h_bytes = d2h;
+        stats->status_detail = res.breakdown ? 1 : 0;
+    }
+    return res.converged ? SF_OK : fail(c, SF_NOT_CONVERGED, "pressure solve did not reach the tolerance");
+}
+
+// ------------------------------------------------------------------------------------------------ magnetic
+sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi, double bw, const double *const hext[3],
+                        double *psi_out, double *const H_out[3], const sf_solve_opts *opts, sf_solve_stats *stats,
+                        bool dev) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!c) return SF_BAD_ARG;
+    if (!grid_ok(g) || !phi || !hext || !opts_ok(opts) || !std::isfinite(chi) || !(bw > 0) || !std::isfinite(bw))
+        return fail(c, SF_BAD_ARG, "bad grid, pointer, chi, band width or option");
+    for (int a = 0; a < 3; a++)
+        if (!hext[a]) return fail(c, SF_BAD_ARG, "null applied-field array");
+    if (H_out)
+        for (int a = 0; a < 3; a++)
+            if (!H_out[a]) return fail(c, SF_BAD_ARG, "H_out must hold three arrays or be NULL");
+    CK(cudaSetDevice(c->device));
+    const Dims d = make_dims(g->nx, g->ny, g->nz);
+    if (stats) memset(stats, 0, sizeof(*stats));
+    long long h2d = 0, d2h = 0;
+    const double *dphi;
+    Faces fh{};
+    sf_status s;
+    if ((s = stage_in(c, c->phi, phi, d.n, dev, &dphi, h2d)) != SF_OK) return s;
+    for (int a = 0; a < 3; a++)
+        if ((s = stage_in(c, c->hext[a], hext[a], face_count(g, a), dev, &fh.p[a], h2d)) != SF_OK) return s;
+    if (!c->mag) c->mag = std::make_unique<MGSolver>(c->st);
+    MGSolver &S = *c->mag;
+    SolverParams prm = params_from(opts, 1);
+    const bool same_grid = c->mag_has_x && c->mag_dims.nx == d.nx && c->mag_dims.ny == d.ny && c->mag_dims.nz == d.nz;
+    CK(S.configure(d, prm));
+    const bool warm = (!opts || opts->warm_start) && same_grid;
+    CK(cudaEventRecord(c->ev[0], c->st));
+    launch_build_magnetic(c->st, d, dphi, chi, bw, fh, g->h, S.fine(), S.b());
+    CK(S.build_hierarchy());
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(c->ev[1], c->st));
+    SolveResult res;
+    CK(S.solve(!warm, res));
+    CK(S.shift_to_zero_at_origin());
+    double relres = res.relres, relref = res.relres, bn = res.bnorm;
+    const bool report = !opts || opts->report_ref_residual;
+    if (report) {
+        CK(S.true_relres(false, relres, bn));
+        CK(S.true_relres(true, relref, bn));
+    }
+    CK(cudaEventRecord(c->ev[2], c->st));
+    const double invh = 1 / g->h;  // Grid::m_InvSpacing
+    Faces fH{};
+    if (H_out) {
+        for (int a = 0; a < 3; a++) {
+            if (dev) {
+                fH.p[a] = H_out[a];
+            } else {
+                CK(c->H[a].ensure(8 * (size_t)face_count(g, a)));
+                fH.p[a] = (const double *)c->H[a].get();
+            }
+        }
+        launch_total_field(c->st, d, S.x(), fh, invh, fH);
+    }
+    if (psi_out && dev) launch_copy(c->st, d.n, S.x(), psi_out);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(c->ev[3], c->st));
+    if (!dev) {
+        if (H_out)
+            for (int a = 0; a < 3; a++) {
+                const long long nf = face_count(g, a);
+                CK(cudaMemcpyAsync(H_out[a], fH.p[a], 8 * (size_t)nf, cudaMemcpyDeviceToHost, c->st));
+                d2h += 8 * nf;
+            }
+        if (psi_out) {
+            CK(cudaMemcpyAsync(psi_out, S.x(), 8 * (size_t)d.n, cudaMemcpyDeviceToHost, c->st));
+            d2h += 8 * d.n;
+        }
+    }
+    CK(cudaStreamSynchronize(c->st));
+    c->mag_has_x = true;
+    c->mag_dims = d;
+    fill_stats(stats, res, d.n);
+    if (stats) stats->kernel_launches = S.take_launches() + 1 + (H_out ? 3 : 0) + ((psi_out && dev) ? 1 : 0);
+    if (stats) {
+        stats->rel_residual = relres;
+        stats->rel_residual_ref = relref;
+        stats->ms_build = ev_ms(c->ev[0], c->ev[1]);
+        stats->ms_solve = ev_ms(c->ev[1], c->ev[2]);
+        stats->ms_post = ev_ms(c->ev[2], c->ev[3]);
+        stats->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        stats->h2d_bytes = h2d;
+        stats->d2h_bytes = d2h;
+        stats->status_detail = res.breakdown ? 1 : 0;
+    }
+    return res.converged ? SF_OK : fail(c, SF_NOT_CONVERGED, "magnetic solve did not reach the tolerance");
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------ C ABI
+extern "C" {
+
+int sf_abi_version(void) { return SFGPU_ABI_VERSION; }
+
+const char *sf_status_string(int s) {
+    switch (s) {
+        case SF_OK: return "ok";
+        case SF_NOT_CONVERGED: return "not converged";
+        case SF_BAD_ARG: return "bad argument";
+        case SF_CUDA_ERROR: return "CUDA error";
+        case SF_NO_DEVICE: return "no sm_103 CUDA device";
+        case SF_OUT_OF_MEMORY: return "out of device memory";
+        case SF_STALLED_FALLBACK: return "learned solve stalled; plain MGPCG finished it";
+        case SF_NOT_READY: return "no previous projection on this context";
+        default: return "unknown status";
+    }
+}
+
+void sf_default_opts(sf_solve_opts *o, int which) {
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->precision = SF_PREC_FP64;
+    o->tol = which == 1 ? 1e-6 : 1e-8;
+    o->max_iters = 200;
+    o->pre_smooth = 2;
+    o->post_smooth = 2;
+    o->coarse_sweeps = 24;
+    o->max_levels = 0;
+    o->coarse_dim = 8;
+    o->warm_start = 1;
+    o->use_graph = 1;
+    o->check_every = 1;
+    o->report_ref_residual = 1;
+    o->inner_tol = 1e-4;
+}
+
+sf_status sf_create(int device, void *stream, void **out) {
+    if (!out) return SF_BAD_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0 || device < 0 || device >= n) return SF_NO_DEVICE;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return SF_NO_DEVICE;
+    if (prop.major != 10 || prop.minor != 3) return SF_NO_DEVICE;  // built for sm_103a only
+    auto *c = new Ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        delete c;
+        return SF_NO_DEVICE;
+    }
+    if (stream) {
+        c->st = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+            delete c;
+            return SF_CUDA_ERROR;
+        }
+        c->own_stream = true;
+    }
+    for (auto &e : c->ev) cudaEventCreate(&e);
+    *out = c;
+    return SF_OK;
+}
+
+void sf_destroy(void *p) {
+    Ctx *c = C(p);
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->st) cudaStreamSynchronize(c->st);
+    c->pres.reset();
+    c->mag.reset();
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->own_stream) cudaStreamDestroy(c->st);
+    delete c;
+}
+
+const char *sf_last_error(void *p) { return p ? C(p)->err.c_str() : "null context"; }
+
+long long sf_device_bytes(void *p) {
+    Ctx *c = C(p);
+    if (!c) return 0;
+    long long b = 0;
+    if (c->pres) b += (long long)c->pres->device_bytes();
+    if (c->mag) b += (long long)c->mag->device_bytes();
+    DevBuf *bs[] = {&c->phi, &c->frac[0], &c->frac[1], &c->frac[2], &c->vel[0], &c->vel[1], &c->vel[2],
+                    &c->us[0], &c->us[1], &c->us[2], &c->jump[0], &c->jump[1], &c->jump[2], &c->hext[0],
+                    &c->hext[1], &c->hext[2], &c->H[0], &c->H[1], &c->H[2], &c->cells};
+    for (DevBuf *x : bs) b += (long long)x->bytes();
+    return b;
+}
+
+sf_status sf_pressure_project(void *ctx, const sf_grid *g, double *const vel[3], const double *phi,
+                              const double *const frac[3], const double *const solid_vel[3],
+                              const double *const jump[3], double vol_error, double *p_out, const sf_solve_opts *opts,
+                              sf_solve_stats *stats) {
+    return pressure_impl(C(ctx), g, vel, phi, frac, solid_vel, jump, vol_error, p_out, opts, stats, false, false);
+}
+sf_status sf_pressure_project_dev(void *ctx, const sf_grid *g, double *const vel[3], const double *phi,
+                                  const double *const frac[3], const double *const solid_vel[3],
+                                  const double *const jump[3], double vol_error, double *p_out,
+                                  const sf_solve_opts *opts, sf_solve_stats *stats) {
+    return pressure_impl(C(ctx), g, vel, phi, frac, solid_vel, jump, vol_error, p_out, opts, stats, true, false);
+}
+sf_status sf_pressure_reproject(void *ctx, const sf_grid *g, double *const vel[3], const double *phi,
+                                const double *const frac[3], const double *const solid_vel[3],
+                                const double *const jump[3], double vol_error, double *p_out,
+                                const sf_solve_opts *opts, sf_solve_stats *stats) {
+    return pressure_impl(C(ctx), g, vel, phi, frac, solid_vel, jump, vol_error, p_out, opts, stats, false, true);
+}
+sf_status sf_pressure_reproject_dev(void *ctx, const sf_grid *g, double *const vel[3], const double *phi,
+                                    const double *const frac[3], const double *const solid_vel[3],
+                                    const double *const jump[3], double vol_error, double *p_out,
+                                    const sf_solve_opts *opts, sf_solve_stats *stats) {
+    return pressure_impl(C(ctx), g, vel, phi, frac, solid_vel, jump, vol_error, p_out, opts, stats, true, true);
+}
+sf_status sf_magnetic_solve(void *ctx, const sf_grid *g, const double *phi, double chi, double band_width,
+                            const double *const hext[3], double *psi_out, double *const H_out[3],
+                            const sf_solve_opts *opts, sf_solve_stats *stats) {
+    return magnetic_impl(C(ctx), g, phi, chi, band_width, hext, psi_out, H_out, opts, stats, false);
+}
+sf_status sf_magnetic_solve_dev(void *ctx, const sf_grid *g, const double *phi, double chi, double band_width,
+                                const double *const hext[3], double *psi_out, double *const H_out[3],
+                                const sf_solve_opts *opts, sf_solve_stats *stats) {
+    return magnetic_impl(C(ctx), g, phi, chi, band_width, hext, psi_out, H_out, opts, stats, true);
+}
+sf_status sf_magnetic_reset(void *ctx) {
+    Ctx *c = C(ctx);
+    if (!c) return SF_BAD_ARG;
+    c->mag_has_x = false;
+    return SF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,201 @@
+// sf_internal.cuh -- shared device-side definitions of the sm_103a solver library.
+//
+// Grid layout is the reference's (core/Grid.h:28): cell (i,j,k) -> k + nz*(j + ny*i), z fastest.  Every
+// multigrid level stores its 7-point operator in "face-coefficient" form on a dense cell grid:
+//   ax[c] = coupling across the lower x-face of cell c (between c - e_x and c); 0 on the grid boundary and
+//           wherever either cell is inactive (air for the pressure solve).  Likewise ay, az.
+//   (A v)_c = D_c v_c - sum over the 6 faces of (coupling * v_neighbour),  D_c = sum of the 6 couplings + dex_c
+//   dex_c  = diagonal excess (ghost-fluid Dirichlet terms, the isolated-cell 1); D_c == 0 marks an inactive cell.
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace sf {
+
+struct Dims {
+    int nx, ny, nz;
+    long long n;
+};
+
+static inline Dims make_dims(int nx, int ny, int nz) { return Dims{nx, ny, nz, (long long)nx * ny * nz}; }
+
+__host__ __device__ __forceinline__ long long cid(const Dims &d, int i, int j, int k) {
+    return (long long)k + (long long)d.nz * ((long long)j + (long long)d.ny * i);
+}
+
+// Operator storage of one level.  C = double | float | __half.
+//   double: dg = D (full diagonal), invd = 1/D (0 where inactive), dex kept for coarsening.
+//   float/__half: dg = dex, D is recomputed from the stored couplings so that the stored operator keeps
+//   exact row sums (a Neumann row stays singular, a Dirichlet row stays dominant) whatever the rounding.
+//   __half values are stored multiplied by `scale` (a power of two) and multiplied by `unscale` on load.
+template <class C>
+struct Coef {
+    C *ax, *ay, *az;
+    C *dex;
+    double *D, *invd;  // double levels only
+    float scale, unscale;
+};
+
+__device__ __forceinline__ double ldv(const double *p, long long i) { return p[i]; }
+__device__ __forceinline__ float ldv(const float *p, long long i) { return p[i]; }
+__device__ __forceinline__ float ldv(const __half *p, long long i) { return __half2float(p[i]); }
+
+template <class C>
+struct Acc;  // arithmetic type of a coefficient storage type
+template <>
+struct Acc<double> {
+    using T = double;
+};
+template <>
+struct Acc<float> {
+    using T = float;
+};
+template <>
+struct Acc<__half> {
+    using T = float;
+};
+
+__device__ __forceinline__ void stv(double *p, long long i, double v) { p[i] = v; }
+__device__ __forceinline__ void stv(float *p, long long i, float v) { p[i] = v; }
+__device__ __forceinline__ void stv(__half *p, long long i, float v) { p[i] = __float2half_rn(v); }
+
+// Sum of coupling * x over the 6 faces of cell (i,j,k) and (optionally) the sum of the couplings.
+// Returned values are already unscaled.
+template <class T, class C, bool SUMA>
+__device__ __forceinline__ T nbsum(const Dims &d, const Coef<C> &cf, const T *__restrict__ x, int i, int j,
+                                   int k, long long c, T &suma) {
+    using R = typename Acc<C>::T;
+    const long long sx = (long long)d.ny * d.nz, sy = d.nz;
+    R s = 0, sa = 0;
+    if (i > 0) {
+        R a = ldv(cf.ax, c);
+        s += a * (R)x[c - sx];
+        if (SUMA) sa += a;
+    }
+    if (i < d.nx - 1) {
+        R a = ldv(cf.ax, c + sx);
+        s += a * (R)x[c + sx];
+        if (SUMA) sa += a;
+    }
+    if (j > 0) {
+        R a = ldv(cf.ay, c);
+        s += a * (R)x[c - sy];
+        if (SUMA) sa += a;
+    }
+    if (j < d.ny - 1) {
+        R a = ldv(cf.ay, c + sy);
+        s += a * (R)x[c + sy];
+        if (SUMA) sa += a;
+    }
+    if (k > 0) {
+        R a = ldv(cf.az, c);
+        s += a * (R)x[c - 1];
+        if (SUMA) sa += a;
+    }
+    if (k < d.nz - 1) {
+        R a = ldv(cf.az, c + 1);
+        s += a * (R)x[c + 1];
+        if (SUMA) sa += a;
+    }
+    if (sizeof(C) == 2) {
+        s *= (R)cf.unscale;
+        sa *= (R)cf.unscale;
+    }
+    suma = (T)sa;
+    return (T)s;
+}
+
+// Diagonal of cell c given the (unscaled) sum of its couplings.
+template <class C>
+__device__ __forceinline__ typename Acc<C>::T diag_of(const Coef<C> &cf, long long c, typename Acc<C>::T suma) {
+    if (sizeof(C) == 8) return (typename Acc<C>::T)cf.D[c];
+    typename Acc<C>::T e = ldv(cf.dex, c);
+    if (sizeof(C) == 2) e *= cf.unscale;
+    return suma + e;
+}
+
+// --------------------------------------------------------------------------------------------------------
+// Deterministic reductions: each block writes its partial sums to `part`, the last block to finish (atomic
+// ticket) sums the partials in block order and runs a finaliser.  Same inputs -> same bits.
+// --------------------------------------------------------------------------------------------------------
+constexpr int kRedThreads = 256;
+
+template <int K>
+__device__ __forceinline__ void warp_sum(double (&v)[K]) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int q = 0; q < K; q++) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+}
+
+// Returns true in exactly one thread (linear thread 0 of the last block), with `tot` holding the grid totals.
+// Blocks must have kRedThreads threads (any shape); `tid` is the linear thread index.
+template <int K>
+__device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, unsigned *ticket, double (&tot)[K]) {
+    __shared__ double sh[K][kRedThreads / 32];
+    __shared__ double sh2[K][kRedThreads];
+    __shared__ bool last;
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nblk = gridDim.x * gridDim.y * gridDim.z;
+    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    warp_sum<K>(v);
+    const int lane = tid & 31, wid = tid >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < K; q++) sh[q][wid] = v[q];
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+        for (int q = 0; q < K; q++) {
+            double b = 0;
+            for (int w = 0; w < kRedThreads / 32; w++) b += sh[q][w];
+            part[(long long)q * nblk + bid] = b;
+        }
+        __threadfence();
+        unsigned t = atomicAdd(ticket, 1u);
+        last = (t == (unsigned)nblk - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double acc[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) acc[q] = 0;
+    for (int b = tid; b < nblk; b += kRedThreads)
+#pragma unroll
+        for (int q = 0; q < K; q++) acc[q] += ((volatile double *)part)[(long long)q * nblk + b];
+#pragma unroll
+    for (int q = 0; q < K; q++) sh2[q][tid] = acc[q];
+    __syncthreads();
+    for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+        if (tid < s)
+#pragma unroll
+            for (int q = 0; q < K; q++) sh2[q][tid] += sh2[q][tid + s];
+        __syncthreads();
+    }
+    if (tid != 0) return false;
+#pragma unroll
+    for (int q = 0; q < K; q++) tot[q] = sh2[q][0];
+    *ticket = 0u;  // re-arm for the next launch on the same stream
+    return true;
+}
+
+// Scalar slots shared by the PCG kernels (device array of doubles).
+enum Slot {
+    S_RHO = 0,   // (r, z) of the current iteration
+    S_RHONEW,    // (r, z) just computed
+    S_ZQ,        // (z, q) for the flexible (Polak-Ribiere) beta
+    S_PQ,        // (p, A p)
+    S_RR,        // (r, r)
+    S_BB,        // (b, b)
+    S_ALPHA,
+    S_BETA,
+    S_AUX0,
+    S_AUX1,
+    S_AUX2,
+    S_NSLOTS = 16
+};
+
+}  // namespace sf

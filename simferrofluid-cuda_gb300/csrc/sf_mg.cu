@@ -1,0 +1,873 @@
+// sf_mg.cu -- matrix-free geometric multigrid and (flexible) PCG for the 7-point variable-coefficient
+// operators of the pressure projection and the magnetic potential, for sm_103a.
+//
+// Multigrid design (own, from published methods):
+//   * cell-centred 2x2x2 aggregation: coarse dims = ceil(n/2), piecewise-constant prolongation P,
+//     restriction R = P^T (sum of the 8 children's residuals);
+//   * coarse operator = (1/2) P^T A P, which keeps the 7-point face-coefficient form: a coarse face gets half
+//     the sum of its 4 fine faces, a coarse cell half the diagonal excess of its 8 children.  The 1/2 is the
+//     over-correction that compensates piecewise-constant interpolation of smooth errors (Braess 1995,
+//     "Towards algebraic multigrid for elliptic problems of second order"; also used by aggregation AMG with
+//     over-correction);
+//   * red-black Gauss-Seidel smoothing, red-black before restriction and black-red after, a palindromic
+//     red-black sequence on the coarsest grid, so the V-cycle is a fixed symmetric operator and plain PCG
+//     applies (Tatebe 1993, "The multigrid preconditioned conjugate gradient method").
+// The FP64 form keeps everything in double.  The mixed form runs the V-cycle in FP32 with FP32 level-0 and
+// FP16 coarse coefficients inside an FP32 flexible CG, wrapped in FP64 iterative refinement: only the outer
+// residual r = b - A x, the update x += d and the dot products stay FP64.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "sf_solver.h"
+
+namespace sf {
+
+// ------------------------------------------------------------------------------------------------ buffers
+DevBuf::~DevBuf() { release(); }
+cudaError_t DevBuf::ensure(size_t bytes) {
+    if (bytes <= n_ && p_) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p_, bytes ? bytes : 256);
+    if (e != cudaSuccess) {
+        p_ = nullptr;
+        n_ = 0;
+        return e;
+    }
+    n_ = bytes;
+    return cudaSuccess;
+}
+void DevBuf::release() {
+    if (p_) cudaFree(p_);
+    p_ = nullptr;
+    n_ = 0;
+}
+
+int reduce_grid(long long rows) {
+    long long g = (rows + 7) / 8;
+    if (g > kMaxRedBlocks) g = kMaxRedBlocks;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+void Tracker::before(cudaStream_t st, bool fine) {
+    launches++;
+    if (!prof || !fine) return;
+    if (used + 2 > ev.size())
+        for (int q = 0; q < 64; q++) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            ev.push_back(e);
+        }
+    cudaEventRecord(ev[used++], st);
+}
+void Tracker::after(cudaStream_t st, bool fine) {
+    if (!prof || !fine) return;
+    cudaEventRecord(ev[used++], st);
+}
+void Tracker::collect(double &ms, int &n) {
+    ms = 0;
+    n = 0;
+    for (size_t q = 0; q + 1 < used; q += 2) {
+        float t = 0;
+        cudaEventElapsedTime(&t, ev[q], ev[q + 1]);
+        ms += t;
+        n++;
+    }
+    used = 0;
+}
+Tracker::~Tracker() {
+    for (auto e : ev) cudaEventDestroy(e);
+}
+
+// ------------------------------------------------------------------------------------------------ launch shapes
+// Stencil kernels: block (32, 8) over (z, y), grid.z = x.  Red-black kernels cover cell pairs along z.
+static inline dim3 blk2() { return dim3(32, 8, 1); }
+static inline dim3 grid_cells(const Dims &d) { return dim3((d.nz + 31) / 32, (d.ny + 7) / 8, d.nx); }
+static inline dim3 grid_pairs(const Dims &d) { return dim3(((d.nz + 1) / 2 + 31) / 32, (d.ny + 7) / 8, d.nx); }
+
+// ------------------------------------------------------------------------------------------------ smoothers
+template <class C>
+__device__ __forceinline__ typename Acc<C>::T inv_diag(const Coef<C> &cf, long long c, typename Acc<C>::T suma) {
+    using R = typename Acc<C>::T;
+    if (sizeof(C) == 8) return (R)cf.invd[c];
+    R D = diag_of(cf, c, suma);
+    return D > R(0) ? R(1) / D : R(0);
+}
+
+template <class T, class C>
+__device__ __forceinline__ T couplings_sum(const Dims &d, const Coef<C> &cf, int i, int j, int k, long long c) {
+    using R = typename Acc<C>::T;
+    const long long sx = (long long)d.ny * d.nz, sy = d.nz;
+    R sa = 0;
+    if (i > 0) sa += ldv(cf.ax, c);
+    if (i < d.nx - 1) sa += ldv(cf.ax, c + sx);
+    if (j > 0) sa += ldv(cf.ay, c);
+    if (j < d.ny - 1) sa += ldv(cf.ay, c + sy);
+    if (k > 0) sa += ldv(cf.az, c);
+    if (k < d.nz - 1) sa += ldv(cf.az, c + 1);
+    if (sizeof(C) == 2) sa *= (R)cf.unscale;
+    return (T)sa;
+}
+
+// Red-black Gauss-Seidel half sweep.  Thread (kp, j, i) owns cells (i, j, 2kp) and (i, j, 2kp+1) and updates
+// the one whose colour (i + j + k) & 1 equals `color`.  Inactive cells (D = 0) are written 0.
+// ZERO: first half sweep of a V-cycle from x = 0; the other cell of the pair is zeroed, so x needs no
+// clearing beforehand and never carries stale values into the sweep.
+template <class T, class C, bool ZERO>
+__global__ void __launch_bounds__(256) k_rbgs(Dims d, Coef<C> cf, T *__restrict__ x, const T *__restrict__ b,
+                                              int color) {
+    const int kp = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (j >= d.ny) return;
+    const int par = (i + j + color) & 1;
+    const int k = 2 * kp + par;
+    if (ZERO) {
+        const int ko = 2 * kp + (par ^ 1);
+        if (ko < d.nz) x[cid(d, i, j, ko)] = T(0);
+    }
+    if (k >= d.nz) return;
+    const long long c = cid(d, i, j, k);
+    T s, sa;
+    if (ZERO) {
+        s = T(0);
+        sa = (sizeof(C) == 8) ? T(0) : couplings_sum<T, C>(d, cf, i, j, k, c);
+    } else {
+        s = nbsum<T, C, sizeof(C) != 8>(d, cf, x, i, j, k, c, sa);
+    }
+    const T inv = (T)inv_diag<C>(cf, c, (typename Acc<C>::T)sa);
+    x[c] = (b[c] + s) * inv;
+}
+
+// r = b - A x on the fine level, summed over each coarse cell's (up to) 8 children -> coarse rhs.
+template <class T, class C>
+__global__ void __launch_bounds__(256) k_resid_restrict(Dims d, Coef<C> cf, const T *__restrict__ x,
+                                                        const T *__restrict__ b, Dims dc, T *__restrict__ bc) {
+    const int K = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int I = blockIdx.z;
+    if (K >= dc.nz || J >= dc.ny) return;
+    T acc = 0;
+#pragma unroll
+    for (int di = 0; di < 2; di++) {
+        const int i = 2 * I + di;
+        if (i >= d.nx) break;
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++) {
+            const int j = 2 * J + dj;
+            if (j >= d.ny) break;
+#pragma unroll
+            for (int dk = 0; dk < 2; dk++) {
+                const int k = 2 * K + dk;
+                if (k >= d.nz) break;
+                const long long c = cid(d, i, j, k);
+                T sa;
+                T s = nbsum<T, C, sizeof(C) != 8>(d, cf, x, i, j, k, c, sa);
+                T D = (T)diag_of<C>(cf, c, (typename Acc<C>::T)sa);
+                acc += (b[c] - D * x[c]) + s;
+            }
+        }
+    }
+    bc[cid(dc, I, J, K)] = acc;
+}
+
+// x += P xc (piecewise constant).
+template <class T>
+__global__ void __launch_bounds__(256) k_prolong(Dims d, T *__restrict__ x, Dims dc, const T *__restrict__ xc) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= d.nz || j >= d.ny) return;
+    x[cid(d, i, j, k)] += xc[cid(dc, i >> 1, j >> 1, k >> 1)];
+}
+
+// Coarsest level: one block, x = 0 then the palindromic sequence red, (black, red) x pairs.
+template <class T, class C>
+__global__ void __launch_bounds__(1024) k_coarse(Dims d, Coef<C> cf, T *__restrict__ x, const T *__restrict__ b,
+                                                 int pairs) {
+    for (long long c = threadIdx.x; c < d.n; c += blockDim.x) x[c] = T(0);
+    __syncthreads();
+    const int nh = 1 + 2 * pairs;
+    for (int h = 0; h < nh; h++) {
+        const int color = h & 1;
+        for (long long c = threadIdx.x; c < d.n; c += blockDim.x) {
+            const int k = (int)(c % d.nz), j = (int)((c / d.nz) % d.ny), i = (int)(c / ((long long)d.nz * d.ny));
+            if (((i + j + k) & 1) != color) continue;
+            T sa;
+            T s = nbsum<T, C, sizeof(C) != 8>(d, cf, x, i, j, k, c, sa);
+            const T inv = (T)inv_diag<C>(cf, c, (typename Acc<C>::T)sa);
+            x[c] = (b[c] + s) * inv;
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------------------------------------ coarsening
+template <class C>
+__device__ __forceinline__ double ldu(const Coef<C> &cf, const C *p, long long i) {
+    double v = (double)ldv(p, i);
+    if (sizeof(C) == 2) v *= (double)cf.unscale;
+    return v;
+}
+
+// Coarse operator (1/2) P^T A P in face-coefficient form.
+template <class CF, class CC>
+__global__ void __launch_bounds__(256) k_coarsen(Dims d, Coef<CF> f, Dims dc, Coef<CC> cc) {
+    const int K = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int I = blockIdx.z;
+    if (K >= dc.nz || J >= dc.ny) return;
+    // half the sum of the fine faces on the coarse face at coarse index (Ic, Jc, Kc) along `axis`
+    auto face = [&](int axis, int Ic, int Jc, int Kc) -> double {
+        int C3[3] = {Ic, Jc, Kc};
+        int dn[3] = {dc.nx, dc.ny, dc.nz};
+        if (C3[axis] <= 0 || C3[axis] >= dn[axis]) return 0.0;
+        const CF *arr = axis == 0 ? f.ax : (axis == 1 ? f.ay : f.az);
+        double s = 0;
+        for (int u = 0; u < 2; u++)
+            for (int v = 0; v < 2; v++) {
+                int fi[3];
+                fi[axis] = 2 * C3[axis];
+                int o1 = (axis + 1) % 3, o2 = (axis + 2) % 3;
+                fi[o1] = 2 * C3[o1] + u;
+                fi[o2] = 2 * C3[o2] + v;
+                if (fi[0] >= d.nx || fi[1] >= d.ny || fi[2] >= d.nz) continue;
+                s += ldu(f, arr, cid(d, fi[0], fi[1], fi[2]));
+            }
+        return 0.5 * s;
+    };
+    double dex = 0;
+    for (int di = 0; di < 2; di++)
+        for (int dj = 0; dj < 2; dj++)
+            for (int dk = 0; dk < 2; dk++) {
+                int i = 2 * I + di, j = 2 * J + dj, k = 2 * K + dk;
+                if (i >= d.nx || j >= d.ny || k >= d.nz) continue;
+                dex += ldu(f, f.dex, cid(d, i, j, k));
+            }
+    dex *= 0.5;
+    const long long c = cid(dc, I, J, K);
+    const double fx = face(0, I, J, K), fy = face(1, I, J, K), fz = face(2, I, J, K);
+    if (sizeof(CC) == 8) {
+        const double D = fx + face(0, I + 1, J, K) + fy + face(1, I, J + 1, K) + fz + face(2, I, J, K + 1) + dex;
+        stv(cc.ax, c, fx);
+        stv(cc.ay, c, fy);
+        stv(cc.az, c, fz);
+        stv(cc.dex, c, dex);
+        cc.D[c] = D;
+        cc.invd[c] = D > 0 ? 1.0 / D : 0.0;
+    } else {
+        const double sc = sizeof(CC) == 2 ? (double)cc.scale : 1.0;
+        stv(cc.ax, c, (float)(fx * sc));
+        stv(cc.ay, c, (float)(fy * sc));
+        stv(cc.az, c, (float)(fz * sc));
+        stv(cc.dex, c, (float)(dex * sc));
+    }
+}
+
+// FP64 level 0 -> FP32 copy (mixed form).
+__global__ void k_to32(long long n, Coef<double> f, Coef<float> o) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        o.ax[c] = (float)f.ax[c];
+        o.ay[c] = (float)f.ay[c];
+        o.az[c] = (float)f.az[c];
+        o.dex[c] = (float)f.dex[c];
+    }
+}
+
+// ------------------------------------------------------------------------------------------------ Krylov kernels
+// Row-parallel shape for reductions: block (32, 8); each warp walks z-lines (rows) of the grid.
+#define ROW_LOOP(d)                                                                                          \
+    const long long nrows = (long long)(d).nx * (d).ny;                                                      \
+    for (long long row = (long long)blockIdx.x * blockDim.y + threadIdx.y; row < nrows;                     \
+         row += (long long)gridDim.x * blockDim.y) {                                                         \
+        const int i = (int)(row / (d).ny), j = (int)(row % (d).ny);                                          \
+        for (int k = threadIdx.x; k < (d).nz; k += 32) {                                                     \
+            const long long c = (long long)k + (long long)(d).nz * row;
+
+#define ROW_LOOP_END \
+    }                \
+    }
+
+// q = A p ; slot PQ = (p, q) ; alpha = rho / pq (0 and breakdown flag if pq <= 0)
+template <class T, class C>
+__global__ void __launch_bounds__(256) k_apply_dot(Dims d, Coef<C> cf, const T *__restrict__ p, T *__restrict__ q,
+                                                   double *sc, double *part, unsigned *ticket) {
+    double v[1] = {0};
+    ROW_LOOP(d)
+    T sa;
+    T s = nbsum<T, C, sizeof(C) != 8>(d, cf, p, i, j, k, c, sa);
+    T D = (T)diag_of<C>(cf, c, (typename Acc<C>::T)sa);
+    T pc = p[c];
+    T qc = D * pc - s;
+    q[c] = qc;
+    v[0] += (double)pc * (double)qc;
+    ROW_LOOP_END
+    double tot[1];
+    if (grid_reduce<1>(v, part, ticket, tot)) {
+        sc[S_PQ] = tot[0];
+        if (tot[0] > 0 && isfinite(tot[0])) {
+            sc[S_ALPHA] = sc[S_RHO] / tot[0];
+        } else {
+            sc[S_ALPHA] = 0;
+            sc[S_AUX0] = 1;  // breakdown
+        }
+    }
+}
+
+// rho_new = (r, z), zq = (z, q); beta = flexible ? -alpha*zq/rho : rho_new/rho; rho = rho_new
+template <class T>
+__global__ void __launch_bounds__(256) k_dot_rz(long long n, const T *__restrict__ r, const T *__restrict__ z,
+                                                const T *__restrict__ q, int flexible, double *sc, double *part,
+                                                unsigned *ticket) {
+    double v[2] = {0, 0};
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
+        double zc = (double)z[c];
+        v[0] += (double)r[c] * zc;
+        v[1] += zc * (double)q[c];
+    }
+    double tot[2];
+    if (grid_reduce<2>(v, part, ticket, tot)) {
+        const double rho = sc[S_RHO];
+        double beta = flexible ? (-sc[S_ALPHA] * tot[1] / rho) : (tot[0] / rho);
+        if (!isfinite(beta)) beta = 0;
+        sc[S_RHONEW] = tot[0];
+        sc[S_ZQ] = tot[1];
+        sc[S_BETA] = beta;
+        sc[S_RHO] = tot[0];
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_xpby(long long n, const T *__restrict__ z, T *__restrict__ p,
+                                              const double *sc) {
+    const T beta = (T)sc[S_BETA];
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        p[c] = z[c] + beta * p[c];
+}
+
+// x += alpha p ; r -= alpha q ; slot RR = (r, r)
+template <class T>
+__global__ void __launch_bounds__(256) k_update(long long n, T *__restrict__ x, T *__restrict__ r,
+                                                const T *__restrict__ p, const T *__restrict__ q, double *sc,
+                                                double *part, unsigned *ticket) {
+    const T alpha = (T)sc[S_ALPHA];
+    double v[1] = {0};
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
+        x[c] += alpha * p[c];
+        T rc = r[c] - alpha * q[c];
+        r[c] = rc;
+        v[0] += (double)rc * (double)rc;
+    }
+    double tot[1];
+    if (grid_reduce<1>(v, part, ticket, tot)) sc[S_RR] = tot[0];
+}
+
+// r = b - A x (FP64 operator), written as TR (double, or float for the refinement's inner rhs);
+// slots: rr_slot = (r, r) in FP64, bb_slot = (b, b).  skip0: leave row 0 out of both sums.
+template <class TR>
+__global__ void __launch_bounds__(256) k_residual64(Dims d, Coef<double> cf, const double *__restrict__ x,
+                                                    const double *__restrict__ b, TR *__restrict__ r, int skip0,
+                                                    int rr_slot, int bb_slot, double *sc, double *part,
+                                                    unsigned *ticket) {
+    double v[2] = {0, 0};
+    ROW_LOOP(d)
+    double sa;
+    double s = nbsum<double, double, false>(d, cf, x, i, j, k, c, sa);
+    double rc = (b[c] - cf.D[c] * x[c]) + s;
+    if (r) r[c] = (TR)rc;
+    if (!(skip0 && c == 0)) {
+        v[0] += rc * rc;
+        v[1] += b[c] * b[c];
+    }
+    ROW_LOOP_END
+    double tot[2];
+    if (grid_reduce<2>(v, part, ticket, tot)) {
+        sc[rr_slot] = tot[0];
+        sc[bb_slot] = tot[1];
+    }
+}
+
+// x64 += d32
+__global__ void k_ir_update(long long n, double *__restrict__ x, const float *__restrict__ dlt) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        x[c] += (double)dlt[c];
+}
+
+__global__ void k_shift(long long n, double *__restrict__ x) {
+    const double x0 = x[0];  // x[0] itself is not touched here (cleared by a memset afterwards)
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x + 1; c < n; c += (long long)gridDim.x * blockDim.x)
+        x[c] -= x0;
+}
+
+template <class T>
+__global__ void k_copy_cast(long long n, const double *__restrict__ a, T *__restrict__ o) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        o[c] = (T)a[c];
+}
+
+static inline int flat_grid(long long n) {
+    long long g = (n + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+// ------------------------------------------------------------------------------------------------ V-cycle
+template <class T, class C>
+static void rb(cudaStream_t st, Tracker &tk, bool fine, bool zero, const Dims &d, const Coef<C> &cf, T *x, const T *b,
+               int color) {
+    const dim3 g = grid_pairs(d), bk = blk2();
+    tk.before(st, fine);
+    if (zero)
+        k_rbgs<T, C, true><<<g, bk, 0, st>>>(d, cf, x, b, color);
+    else
+        k_rbgs<T, C, false><<<g, bk, 0, st>>>(d, cf, x, b, color);
+    tk.after(st, fine);
+}
+
+template <class T, class C>
+static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const Coef<C> &cf, T *x, const T *b, int nu,
+                   bool pre) {
+    for (int s = 0; s < nu; s++) {
+        if (pre) {
+            rb<T, C>(st, tk, fine, s == 0, d, cf, x, b, 0);
+            rb<T, C>(st, tk, fine, false, d, cf, x, b, 1);
+        } else {
+            rb<T, C>(st, tk, fine, false, d, cf, x, b, 1);
+            rb<T, C>(st, tk, fine, false, d, cf, x, b, 0);
+        }
+    }
+}
+
+template <class T, class C>
+static void restrict_res(cudaStream_t st, Tracker &tk, const Dims &d, const Coef<C> &cf, const T *x, const T *b,
+                         const Dims &dc, T *bc) {
+    tk.launches++;
+    k_resid_restrict<T, C><<<grid_cells(dc), blk2(), 0, st>>>(d, cf, x, b, dc, bc);
+}
+
+template <class T, class C>
+static void coarse_solve(cudaStream_t st, Tracker &tk, const Dims &d, const Coef<C> &cf, T *x, const T *b, int pairs) {
+    tk.launches++;
+    int nt = d.n >= 1024 ? 1024 : (int)((d.n + 31) / 32 * 32);
+    k_coarse<T, C><<<1, nt, 0, st>>>(d, cf, x, b, pairs);
+}
+
+// V-cycle z = M r.  Level 0 uses coefficient type C0, coarse levels Cc (cc[l] for level l >= 1).
+template <class T, class C0, class Cc>
+static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, const Coef<C0> &c0,
+                   const std::vector<Coef<Cc>> &cc, T *z, const T *r, const std::vector<T *> &xs,
+                   const std::vector<T *> &bs, const SolverParams &p) {
+    const int L = (int)dims.size();
+    if (L == 1) {
+        coarse_solve<T, C0>(st, tk, dims[0], c0, z, r, p.coarse_sweeps);
+        return;
+    }
+    smooth<T, C0>(st, tk, true, dims[0], c0, z, r, p.pre, true);
+    restrict_res<T, C0>(st, tk, dims[0], c0, z, r, dims[1], bs[1]);
+    for (int l = 1; l < L - 1; l++) {
+        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], bs[l], p.pre, true);
+        restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1]);
+    }
+    coarse_solve<T, Cc>(st, tk, dims[L - 1], cc[L - 1], xs[L - 1], bs[L - 1], p.coarse_sweeps);
+    for (int l = L - 2; l >= 1; l--) {
+        tk.launches++;
+        k_prolong<T><<<grid_cells(dims[l]), blk2(), 0, st>>>(dims[l], xs[l], dims[l + 1], xs[l + 1]);
+        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], bs[l], p.post, false);
+    }
+    tk.launches++;
+    k_prolong<T><<<grid_cells(dims[0]), blk2(), 0, st>>>(dims[0], z, dims[1], xs[1]);
+    smooth<T, C0>(st, tk, true, dims[0], c0, z, r, p.post, false);
+}
+
+// ------------------------------------------------------------------------------------------------ MGSolver
+MGSolver::MGSolver(cudaStream_t s) : st_(s) {}
+MGSolver::~MGSolver() {
+    destroy_graphs();
+    free_all();
+}
+
+void MGSolver::destroy_graphs() {
+    if (g_iter64_) cudaGraphExecDestroy(g_iter64_);
+    if (g_iter32_) cudaGraphExecDestroy(g_iter32_);
+    g_iter64_ = g_iter32_ = nullptr;
+    graph_key_ = -1;
+}
+
+void MGSolver::free_all() {
+    bufs_.clear();
+    if (sc_host_) cudaFreeHost(sc_host_);
+    sc_host_ = nullptr;
+    bytes_ = 0;
+    configured_ = false;
+}
+
+void *MGSolver::alloc(size_t bytes) {
+    bytes = (bytes + 255) / 256 * 256;
+    auto b = std::make_unique<DevBuf>();
+    if (b->ensure(bytes) != cudaSuccess) return nullptr;
+    void *p = b->get();
+    bytes_ += bytes;
+    bufs_.push_back(std::move(b));
+    return p;
+}
+
+size_t MGSolver::device_bytes() const { return bytes_; }
+
+cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
+    // level dims
+    std::vector<Dims> dims{d};
+    const int cdim = p.coarse_dim > 0 ? p.coarse_dim : 8;
+    while (true) {
+        const Dims &t = dims.back();
+        if (p.max_levels > 0 && (int)dims.size() >= p.max_levels) break;
+        if (t.nx <= cdim && t.ny <= cdim && t.nz <= cdim) break;
+        dims.push_back(make_dims((t.nx + 1) / 2, (t.ny + 1) / 2, (t.nz + 1) / 2));
+    }
+    const bool same = configured_ && cfg_dims_.nx == d.nx && cfg_dims_.ny == d.ny && cfg_dims_.nz == d.nz &&
+                      cfg_prec_ == p.precision && cfg_levels_ == (int)dims.size() && cfg_cdim_ == cdim;
+    prm_ = p;
+    if (same) return cudaSuccess;
+    destroy_graphs();
+    free_all();
+    lev_dims_ = dims;
+    const int L = (int)dims.size();
+    const long long n = d.n;
+    auto A = [&](size_t bytes) -> void * { return alloc(bytes); };
+    bool ok = true;
+    auto chk = [&](void *q) {
+        if (!q) ok = false;
+        return q;
+    };
+    c64_.assign(p.precision == 0 ? L : 1, Coef<double>{});
+    for (int l = 0; l < (int)c64_.size(); l++) {
+        const long long m = dims[l].n;
+        Coef<double> &c = c64_[l];
+        c.ax = (double *)chk(A(8 * m));
+        c.ay = (double *)chk(A(8 * m));
+        c.az = (double *)chk(A(8 * m));
+        c.dex = (double *)chk(A(8 * m));
+        c.D = (double *)chk(A(8 * m));
+        c.invd = (double *)chk(A(8 * m));
+        c.scale = c.unscale = 1.f;
+    }
+    x_ = (double *)chk(A(8 * n));
+    b_ = (double *)chk(A(8 * n));
+    sc_ = (double *)chk(A(8 * S_NSLOTS));
+    part_ = (double *)chk(A(8 * 4 * (size_t)kMaxRedBlocks));
+    ticket_ = (unsigned *)chk(A(256));
+    if (p.precision == 0) {
+        x64_.assign(L, nullptr);
+        b64_.assign(L, nullptr);
+        for (int l = 1; l < L; l++) {
+            x64_[l] = (double *)chk(A(8 * dims[l].n));
+            b64_[l] = (double *)chk(A(8 * dims[l].n));
+        }
+        r_ = (double *)chk(A(8 * n));
+        z_ = (double *)chk(A(8 * n));
+        p_ = (double *)chk(A(8 * n));
+        q_ = (double *)chk(A(8 * n));
+    } else {
+        c32_.ax = (float *)chk(A(4 * n));
+        c32_.ay = (float *)chk(A(4 * n));
+        c32_.az = (float *)chk(A(4 * n));
+        c32_.dex = (float *)chk(A(4 * n));
+        c32_.D = c32_.invd = nullptr;
+        c32_.scale = c32_.unscale = 1.f;
+        c16_.assign(L, Coef<__half>{});
+        x32_.assign(L, nullptr);
+        b32_.assign(L, nullptr);
+        for (int l = 1; l < L; l++) {
+            const long long m = dims[l].n;
+            Coef<__half> &c = c16_[l];
+            c.ax = (__half *)chk(A(2 * m));
+            c.ay = (__half *)chk(A(2 * m));
+            c.az = (__half *)chk(A(2 * m));
+            c.dex = (__half *)chk(A(2 * m));
+            c.D = c.invd = nullptr;
+            // level-l couplings grow ~2^l and excesses up to 4^l: store scaled by 4^-l
+            c.scale = ldexpf(1.f, -2 * l);
+            c.unscale = ldexpf(1.f, 2 * l);
+            x32_[l] = (float *)chk(A(4 * m));
+            b32_[l] = (float *)chk(A(4 * m));
+        }
+        r32_ = (float *)chk(A(4 * n));
+        d32_ = (float *)chk(A(4 * n));
+        z32_ = (float *)chk(A(4 * n));
+        p32_ = (float *)chk(A(4 * n));
+        q32_ = (float *)chk(A(4 * n));
+        ri32_ = r32_;
+    }
+    if (!ok) {
+        free_all();
+        last_error = "device allocation failed";
+        return cudaErrorMemoryAllocation;
+    }
+    cudaError_t e = cudaMallocHost(&sc_host_, 8 * S_NSLOTS);
+    if (e != cudaSuccess) return e;
+    cudaMemsetAsync(ticket_, 0, 256, st_);
+    cudaMemsetAsync(sc_, 0, 8 * S_NSLOTS, st_);
+    cudaMemsetAsync(x_, 0, 8 * n, st_);
+    configured_ = true;
+    cfg_dims_ = d;
+    cfg_prec_ = p.precision;
+    cfg_levels_ = L;
+    cfg_cdim_ = cdim;
+    return cudaGetLastError();
+}
+
+cudaError_t MGSolver::build_hierarchy() {
+    const int L = (int)lev_dims_.size();
+    tk_.launches += prm_.precision == 0 ? (L - 1) : L;
+    if (prm_.precision == 0) {
+        for (int l = 1; l < L; l++)
+            k_coarsen<double, double><<<grid_cells(lev_dims_[l]), blk2(), 0, st_>>>(lev_dims_[l - 1], c64_[l - 1],
+                                                                                    lev_dims_[l], c64_[l]);
+    } else {
+        k_to32<<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0].n, c64_[0], c32_);
+        if (L > 1)
+            k_coarsen<double, __half><<<grid_cells(lev_dims_[1]), blk2(), 0, st_>>>(lev_dims_[0], c64_[0],
+                                                                                    lev_dims_[1], c16_[1]);
+        for (int l = 2; l < L; l++)
+            k_coarsen<__half, __half><<<grid_cells(lev_dims_[l]), blk2(), 0, st_>>>(lev_dims_[l - 1], c16_[l - 1],
+                                                                                    lev_dims_[l], c16_[l]);
+    }
+    return cudaGetLastError();
+}
+
+void MGSolver::enqueue_iter64() {
+    const Dims &d = lev_dims_[0];
+    const long long n = d.n;
+    const int rg = reduce_grid((long long)d.nx * d.ny);
+    const long long l0 = tk_.launches;
+    vcycle<double, double, double>(st_, tk_, lev_dims_, c64_[0], c64_, z_, r_, x64_, b64_, prm_);
+    k_dot_rz<double><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, r_, z_, q_, prm_.flexible ? 1 : 0, sc_, part_,
+                                                              ticket_);
+    k_xpby<double><<<flat_grid(n), 256, 0, st_>>>(n, z_, p_, sc_);
+    k_apply_dot<double, double><<<rg, dim3(32, 8), 0, st_>>>(d, c64_[0], p_, q_, sc_, part_, ticket_);
+    k_update<double><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, x_, r_, p_, q_, sc_, part_, ticket_);
+    tk_.launches += 4;
+    iter_launches64_ = tk_.launches - l0;
+    cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
+}
+
+void MGSolver::enqueue_iter32() {
+    const Dims &d = lev_dims_[0];
+    const long long n = d.n;
+    const int rg = reduce_grid((long long)d.nx * d.ny);
+    const long long l0 = tk_.launches;
+    vcycle<float, float, __half>(st_, tk_, lev_dims_, c32_, c16_, z32_, ri32_, x32_, b32_, prm_);
+    k_dot_rz<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, ri32_, z32_, q32_, 1, sc_, part_, ticket_);
+    k_xpby<float><<<flat_grid(n), 256, 0, st_>>>(n, z32_, p32_, sc_);
+    k_apply_dot<float, float><<<rg, dim3(32, 8), 0, st_>>>(d, c32_, p32_, q32_, sc_, part_, ticket_);
+    k_update<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, d32_, ri32_, p32_, q32_, sc_, part_, ticket_);
+    tk_.launches += 4;
+    iter_launches32_ = tk_.launches - l0;
+    cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
+}
+
+cudaError_t MGSolver::run_iter(bool mixed) {
+    cudaError_t e;
+    tk_.prof = prm_.profile;
+    if (!prm_.use_graph || prm_.profile) {
+        if (mixed)
+            enqueue_iter32();
+        else
+            enqueue_iter64();
+        return cudaGetLastError();
+    }
+    const int key = (prm_.pre << 0) | (prm_.post << 4) | (prm_.coarse_sweeps << 8) | ((prm_.flexible ? 1 : 0) << 20);
+    if (key != graph_key_) destroy_graphs();
+    graph_key_ = key;
+    cudaGraphExec_t &ge = mixed ? g_iter32_ : g_iter64_;
+    if (!ge) {
+        cudaGraph_t g;
+        const long long before = tk_.launches;
+        e = cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        if (mixed)
+            enqueue_iter32();
+        else
+            enqueue_iter64();
+        e = cudaStreamEndCapture(st_, &g);
+        if (e != cudaSuccess) return e;
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        tk_.launches = before;  // counted at replay
+        if (e != cudaSuccess) {
+            ge = nullptr;
+            return e;
+        }
+    }
+    tk_.launches += mixed ? iter_launches32_ : iter_launches64_;
+    return cudaGraphLaunch(ge, st_);
+}
+
+cudaError_t MGSolver::read_slots() {
+    cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
+    return cudaStreamSynchronize(st_);
+}
+
+cudaError_t MGSolver::solve(bool x_is_zero, SolveResult &res) {
+    res = SolveResult{};
+    res.levels = (int)lev_dims_.size();
+    tk_.prof = prm_.profile;
+    cudaError_t e = prm_.precision == 0 ? solve64(x_is_zero, res) : solve_mixed(x_is_zero, res);
+    if (e != cudaSuccess) return e;
+    if (prm_.profile) {
+        e = cudaStreamSynchronize(st_);
+        if (e != cudaSuccess) return e;
+        tk_.collect(res.smooth_ms, res.smooth_launches);
+    }
+    return cudaSuccess;
+}
+
+cudaError_t MGSolver::solve64(bool x_is_zero, SolveResult &res) {
+    const Dims &d = lev_dims_[0];
+    const long long n = d.n;
+    const int rg = reduce_grid((long long)d.nx * d.ny);
+    cudaError_t e;
+    if (x_is_zero) cudaMemsetAsync(x_, 0, 8 * n, st_);
+    // r = b - A x, (r,r), (b,b)
+    k_residual64<double><<<rg, dim3(32, 8), 0, st_>>>(d, c64_[0], x_, b_, r_, 0, S_RR, S_BB, sc_, part_, ticket_);
+    tk_.launches++;
+    cudaMemsetAsync(p_, 0, 8 * n, st_);
+    cudaMemsetAsync(q_, 0, 8 * n, st_);
+    {
+        double init[S_NSLOTS] = {0};
+        // S_RHO = 1 so that the first beta multiplies a zero p; ALPHA = 0 for the flexible form
+        init[S_RHO] = 1.0;
+        // keep RR/BB computed above: copy only the first 4 slots and ALPHA/BETA/AUX0
+        cudaMemcpyAsync(sc_ + S_RHO, &init[S_RHO], 8 * 4, cudaMemcpyHostToDevice, st_);
+        cudaMemcpyAsync(sc_ + S_ALPHA, &init[S_ALPHA], 8 * 3, cudaMemcpyHostToDevice, st_);
+    }
+    if ((e = read_slots()) != cudaSuccess) return e;
+    const double bb = sc_host_[S_BB];
+    res.bnorm = std::sqrt(bb);
+    if (bb == 0.0) {  // amgcl returns x = 0 for a zero right-hand side
+        cudaMemsetAsync(x_, 0, 8 * n, st_);
+        res.converged = true;
+        res.relres = 0;
+        return cudaStreamSynchronize(st_);
+    }
+    const double tol2 = prm_.tol * prm_.tol * bb;
+    double rr = sc_host_[S_RR];
+    if (rr <= tol2) {
+        res.converged = true;
+        res.relres = std::sqrt(rr / bb);
+        return cudaSuccess;
+    }
+    const int every = prm_.check_every > 0 ? prm_.check_every : 1;
+    int it = 0;
+    while (it < prm_.max_iters) {
+        for (int s = 0; s < every && it < prm_.max_iters; s++, it++)
+            if ((e = run_iter(false)) != cudaSuccess) return e;
+        if ((e = cudaStreamSynchronize(st_)) != cudaSuccess) return e;
+        rr = sc_host_[S_RR];
+        if (sc_host_[S_AUX0] != 0) {
+            res.breakdown = true;
+            break;
+        }
+        if (rr <= tol2 || !std::isfinite(rr)) break;
+    }
+    res.iters = it;
+    res.relres = std::sqrt(rr / bb);
+    res.converged = rr <= tol2;
+    return cudaSuccess;
+}
+
+cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
+    const Dims &d = lev_dims_[0];
+    const long long n = d.n;
+    const int rg = reduce_grid((long long)d.nx * d.ny);
+    cudaError_t e;
+    if (x_is_zero) cudaMemsetAsync(x_, 0, 8 * n, st_);
+    double bb = -1, rr = 0;
+    int total_inner = 0, outer = 0;
+    const int max_outer = 30;
+    while (true) {
+        // outer FP64 residual, cast to the FP32 inner right-hand side
+        k_residual64<float><<<rg, dim3(32, 8), 0, st_>>>(d, c64_[0], x_, b_, r32_, 0, S_AUX1, S_BB, sc_, part_,
+                                                         ticket_);
+        tk_.launches++;
+        if ((e = read_slots()) != cudaSuccess) return e;
+        rr = sc_host_[S_AUX1];
+        if (bb < 0) {
+            bb = sc_host_[S_BB];
+            res.bnorm = std::sqrt(bb);
+            if (bb == 0.0) {
+                cudaMemsetAsync(x_, 0, 8 * n, st_);
+                res.converged = true;
+                return cudaStreamSynchronize(st_);
+            }
+        }
+        const double rel = std::sqrt(rr / bb);
+        if (rel <= prm_.tol || !std::isfinite(rr) || outer >= max_outer || total_inner >= prm_.max_iters) break;
+        // inner FCG on A32 d = r32, d = 0
+        double tau = 0.5 * prm_.tol / rel;
+        if (tau < prm_.inner_tol) tau = prm_.inner_tol;
+        if (tau > 0.5) tau = 0.5;
+        const double in_tol2 = tau * tau * rr;
+        cudaMemsetAsync(d32_, 0, 4 * n, st_);
+        cudaMemsetAsync(p32_, 0, 4 * n, st_);
+        cudaMemsetAsync(q32_, 0, 4 * n, st_);
+        {
+            double init[4] = {1.0, 0.0, 0.0, 0.0};
+            cudaMemcpyAsync(sc_ + S_RHO, init, 8, cudaMemcpyHostToDevice, st_);
+            cudaMemcpyAsync(sc_ + S_ALPHA, init + 1, 8 * 3, cudaMemcpyHostToDevice, st_);
+        }
+        int it = 0;
+        double rin = rr;
+        const int every = prm_.check_every > 0 ? prm_.check_every : 1;
+        const int budget = prm_.max_iters - total_inner;
+        while (it < budget) {
+            for (int s = 0; s < every && it < budget; s++, it++)
+                if ((e = run_iter(true)) != cudaSuccess) return e;
+            if ((e = cudaStreamSynchronize(st_)) != cudaSuccess) return e;
+            rin = sc_host_[S_RR];
+            if (sc_host_[S_AUX0] != 0) break;
+            if (rin <= in_tol2 || !std::isfinite(rin)) break;
+        }
+        total_inner += it;
+        k_ir_update<<<flat_grid(n), 256, 0, st_>>>(n, x_, d32_);
+        tk_.launches++;
+        outer++;
+        if (sc_host_[S_AUX0] != 0) {
+            res.breakdown = true;
+            // one more residual evaluation happens at the loop head; stop after it
+        }
+        if (it == 0) break;
+    }
+    res.iters = total_inner;
+    res.outer = outer;
+    res.relres = std::sqrt(rr / bb);
+    res.converged = res.relres <= prm_.tol;
+    return cudaGetLastError();
+}
+
+cudaError_t MGSolver::true_relres(bool skip0, double &relres, double &bnorm) {
+    const Dims &d = lev_dims_[0];
+    const int rg = reduce_grid((long long)d.nx * d.ny);
+    k_residual64<double><<<rg, dim3(32, 8), 0, st_>>>(d, c64_[0], x_, b_, (double *)nullptr, skip0 ? 1 : 0,
+                                                      S_AUX1, S_AUX2, sc_, part_, ticket_);
+    tk_.launches++;
+    cudaError_t e = read_slots();
+    if (e != cudaSuccess) return e;
+    const double rr = sc_host_[S_AUX1], bb = sc_host_[S_AUX2];
+    bnorm = std::sqrt(bb);
+    relres = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+    return cudaSuccess;
+}
+
+cudaError_t MGSolver::shift_to_zero_at_origin() {
+    const long long n = lev_dims_[0].n;
+    k_shift<<<flat_grid(n), 256, 0, st_>>>(n, x_);
+    tk_.launches++;
+    cudaMemsetAsync(x_, 0, 8, st_);
+    return cudaGetLastError();
+}
+
+}  // namespace sf

@@ -1,0 +1,263 @@
+// sf_ops.cu -- assembly and post-solve kernels of the pressure projection and the magnetic potential.
+//
+// Compiled with -fmad=false: every expression below rounds exactly as the reference's C++ does (no fused
+// multiply-add), so the fine-level operator and right-hand side are bit-identical to the reference's CSR
+// assembly on the same inputs, and the velocity / field updates are too.
+#include <cmath>
+
+#include "sf_ops.h"
+
+namespace sf {
+
+static inline dim3 blk2() { return dim3(32, 8, 1); }
+static inline dim3 grid3(int nx, int ny, int nz) { return dim3((nz + 31) / 32, (ny + 7) / 8, nx); }
+
+__device__ __forceinline__ long long fid(const Dims &d, int a, int i, int j, int k) {
+    const int fy = d.ny + (a == 1), fz = d.nz + (a == 2);
+    return (long long)k + (long long)fz * ((long long)j + (long long)fy * i);
+}
+
+// ------------------------------------------------------------------------------------------------ pressure
+// Pressure::SetUnKnowns + BuildProjectionMatrix (core/Pressure.cpp:104-123, 38-78) for one cell.
+// Liquid cells are phi <= 0.  The face weight is w = 1 - fraction; faces on the outer grid boundary are
+// closed (w = 0).  D is the reference's diagonal bit for bit (same summation order, 1 for an isolated cell).
+__global__ void __launch_bounds__(256) k_build_pressure(Dims d, const double *__restrict__ phi, Faces frac,
+                                                        Faces u, Faces us, Faces jump, double vol_error,
+                                                        Coef<double> cf, double *__restrict__ b, int rhs_only) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= d.nz || j >= d.ny) return;
+    const long long c = cid(d, i, j, k);
+    if (rhs_only) {
+        // Pressure::SetRightHandSide (:80-102) on the unknowns of the last build (D > 0)
+        if (!(cf.D[c] > 0)) {
+            b[c] = 0;
+            return;
+        }
+    }
+    const double pc = phi[c];
+    const bool liquid = rhs_only ? true : (pc <= 0);
+    double lower[3] = {0, 0, 0};
+    double diag = 0, dexv = 0, div = 0;
+    if (liquid) {
+        const int dn[3] = {d.nx, d.ny, d.nz};
+#pragma unroll
+        for (int ord = 0; ord < 6; ord++) {
+            const int a = ord >> 1;
+            const int up = ord & 1;
+            const double side = up ? 1.0 : -1.0;
+            int f3[3] = {i, j, k};
+            f3[a] += up;
+            int n3[3] = {i, j, k};
+            n3[a] += up ? 1 : -1;
+            const bool valid = n3[a] >= 0 && n3[a] < dn[a];
+            const long long f = fid(d, a, f3[0], f3[1], f3[2]);
+            const double w = valid ? 1. - frac.p[a][f] : 0.0;
+            if (w > 0) {
+                if (!rhs_only) {
+                    const long long nb = cid(d, n3[0], n3[1], n3[2]);
+                    const double pn = phi[nb];
+                    if (pn <= 0) {
+                        diag += w;
+                        if (!up) lower[a] = w;
+                    } else {
+                        const double theta = pc / (pc - pn);
+                        const double ic = 1. / (theta < .001 ? .001 : theta);
+                        diag += w * ic;
+                        dexv += w * ic;
+                        if (jump.p[0]) div += jump.p[a][f] * w * ic;
+                    }
+                }
+                div -= side * w * u.p[a][f];
+            }
+            if (w < 1) {
+                const double usv = us.p[0] ? us.p[a][f] : 0.0;
+                div -= side * (1 - w) * usv;
+            }
+        }
+        div += vol_error;
+    }
+    b[c] = liquid ? div : 0.0;
+    if (rhs_only) return;
+    const double D = liquid ? (diag != 0 ? diag : 1.) : 0.0;
+    if (liquid && diag == 0) dexv = 1.;
+    cf.ax[c] = lower[0];
+    cf.ay[c] = lower[1];
+    cf.az[c] = lower[2];
+    cf.dex[c] = dexv;
+    cf.D[c] = D;
+    cf.invd[c] = D > 0 ? 1. / D : 0.0;
+}
+
+// Pressure::ApplyProjection (core/Pressure.cpp:137-166) for the faces of axis a.  p is the solution on
+// cells; liquid = phi <= 0.
+__global__ void __launch_bounds__(256) k_apply_projection(Dims d, int a, const double *__restrict__ phi, Faces frac,
+                                                          Faces jump, const double *__restrict__ p,
+                                                          double *__restrict__ u) {
+    const int fx = d.nx + (a == 0), fy = d.ny + (a == 1), fz = d.nz + (a == 2);
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= fz || j >= fy || i >= fx) return;
+    int c0i[3] = {i, j, k};
+    c0i[a] -= 1;
+    const int dn[3] = {d.nx, d.ny, d.nz};
+    const int fa = a == 0 ? i : (a == 1 ? j : k);
+    if (fa <= 0 || fa >= dn[a]) return;  // closed boundary face
+    const long long f = (long long)k + (long long)fz * ((long long)j + (long long)fy * i);
+    const double w = 1. - frac.p[a][f];
+    if (w == 0.) return;
+    const long long c1 = cid(d, i, j, k);
+    const long long c0 = cid(d, c0i[0], c0i[1], c0i[2]);
+    const double phi0 = phi[c0], phi1 = phi[c1];
+    const bool l0 = phi0 <= 0, l1 = phi1 <= 0;
+    if (!l0 && !l1) return;
+    double v = u[f];
+    if (l0 && l1) {
+        v -= (p[c1] - p[c0]) * w;
+    } else {
+        const double theta = phi0 / (phi0 - phi1);
+        const double pin = l0 ? p[c0] : p[c1];
+        const double pj = jump.p[0] ? jump.p[a][f] : 0.;
+        const double t = l0 ? theta : 1 - theta;
+        const double ic = 1. / (t < .001 ? .001 : t);
+        v -= (l0 ? 1.0 : -1.0) * (pj - pin) * ic * w;
+    }
+    u[f] = v;
+}
+
+// p_out on cells: solution in liquid cells (D > 0 in the stored operator), 0 elsewhere.
+__global__ void k_gather_cells(long long n, const double *__restrict__ D, const double *__restrict__ x,
+                               double *__restrict__ out) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        out[c] = D[c] > 0 ? x[c] : 0.0;
+}
+
+// ------------------------------------------------------------------------------------------------ magnetic
+// MagneticField::Heaviside (core/MagneticField.h:44-54).
+__device__ __forceinline__ double heaviside(double phi, double bw) {
+    const double pi = 3.141592653589793238462643383279502884;
+    if (phi < -bw) return 0.;
+    if (phi > bw) return 1.;
+    return .5 * (1. + phi / bw + sin(pi * phi / bw) / pi);
+}
+
+// mu on an interior face between cells lo and hi (core/MagneticField.cpp:57-58).  The reference samples phi
+// trilinearly at the face centre; at a face centre the trilinear weights are exactly (1/2, 1/2, 0, ...) when
+// the grid coordinates are exact binary fractions, which this expression reproduces bit for bit; otherwise
+// it differs from the reference's weights (1/2 +- 1 ulp) by a few ulp of phi.
+__device__ __forceinline__ double mu_face(double philo, double phihi, double chi, double bw) {
+    const double pf = 0.5 * philo + 0.5 * phihi;
+    return 1. + (1. - heaviside(pf, bw)) * chi;
+}
+
+// BuildMatrix + AssembleRHS (core/MagneticField.cpp:50-118) for one cell, in Neumann form: D = sum of mu over
+// in-grid faces, couplings mu, b in the reference's face order (row 0 gets its unpinned value; the pinned
+// row 0 of the reference is recovered by the psi[0] = 0 gauge after the solve).
+__global__ void __launch_bounds__(256) k_build_magnetic(Dims d, const double *__restrict__ phi, double chi, double bw,
+                                                        Faces hext, double h, Coef<double> cf,
+                                                        double *__restrict__ b) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= d.nz || j >= d.ny) return;
+    const long long c = cid(d, i, j, k);
+    const int dn[3] = {d.nx, d.ny, d.nz};
+    const double pc = phi[c];
+    double lower[3] = {0, 0, 0};
+    double diag = 0., rhs = 0.;
+#pragma unroll
+    for (int ord = 0; ord < 6; ord++) {
+        const int a = ord >> 1;
+        const int up = ord & 1;
+        int n3[3] = {i, j, k};
+        n3[a] += up ? 1 : -1;
+        if (n3[a] < 0 || n3[a] >= dn[a]) continue;
+        int f3[3] = {i, j, k};
+        f3[a] += up;
+        const double pn = phi[cid(d, n3[0], n3[1], n3[2])];
+        const double mu = up ? mu_face(pc, pn, chi, bw) : mu_face(pn, pc, chi, bw);
+        if (!up) lower[a] = mu;
+        diag += mu;
+        const double side = up ? 1.0 : -1.0;
+        rhs += (mu - 1.) * hext.p[a][fid(d, a, f3[0], f3[1], f3[2])] * (-side) * h;
+    }
+    cf.ax[c] = lower[0];
+    cf.ay[c] = lower[1];
+    cf.az[c] = lower[2];
+    cf.dex[c] = 0.;
+    cf.D[c] = diag;
+    cf.invd[c] = diag > 0 ? 1. / diag : 0.;
+    b[c] = rhs;
+}
+
+// AssignTotalField (core/MagneticField.cpp:125-143) for the faces of axis a.
+__global__ void __launch_bounds__(256) k_total_field(Dims d, int a, const double *__restrict__ psi, Faces hext,
+                                                     double invh, double *__restrict__ H) {
+    const int fx = d.nx + (a == 0), fy = d.ny + (a == 1), fz = d.nz + (a == 2);
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= fz || j >= fy || i >= fx) return;
+    const long long f = (long long)k + (long long)fz * ((long long)j + (long long)fy * i);
+    const int fa = a == 0 ? i : (a == 1 ? j : k);
+    const int dn[3] = {d.nx, d.ny, d.nz};
+    double v = 0.;
+    if (fa > 0 && fa < dn[a]) {
+        int c0[3] = {i, j, k};
+        c0[a] -= 1;
+        v = (psi[cid(d, c0[0], c0[1], c0[2])] - psi[cid(d, i, j, k)]) * invh;
+    }
+    v += hext.p[a][f];
+    H[f] = v;
+}
+
+__global__ void k_copy(long long n, const double *__restrict__ a, double *__restrict__ o) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        o[c] = a[c];
+}
+
+static inline int flat_grid(long long n) {
+    long long g = (n + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+// ------------------------------------------------------------------------------------------------ launchers
+void launch_build_pressure(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &u,
+                           const Faces &us, const Faces &jump, double vol_error, Coef<double> &cf, double *b,
+                           bool rhs_only) {
+    k_build_pressure<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, frac, u, us, jump, vol_error, cf, b,
+                                                                  rhs_only ? 1 : 0);
+}
+
+void launch_apply_projection(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &jump,
+                             const double *p, const Faces &u) {
+    for (int a = 0; a < 3; a++)
+        k_apply_projection<<<grid3(d.nx + (a == 0), d.ny + (a == 1), d.nz + (a == 2)), blk2(), 0, st>>>(
+            d, a, phi, frac, jump, p, const_cast<double *>(u.p[a]));
+}
+
+void launch_gather_cells(cudaStream_t st, long long n, const double *D, const double *x, double *out) {
+    k_gather_cells<<<flat_grid(n), 256, 0, st>>>(n, D, x, out);
+}
+
+void launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, double chi, double bw,
+                           const Faces &hext, double h, Coef<double> &cf, double *b) {
+    k_build_magnetic<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, chi, bw, hext, h, cf, b);
+}
+
+void launch_total_field(cudaStream_t st, const Dims &d, const double *psi, const Faces &hext, double invh,
+                        const Faces &H) {
+    for (int a = 0; a < 3; a++)
+        k_total_field<<<grid3(d.nx + (a == 0), d.ny + (a == 1), d.nz + (a == 2)), blk2(), 0, st>>>(
+            d, a, psi, hext, invh, const_cast<double *>(H.p[a]));
+}
+
+void launch_copy(cudaStream_t st, long long n, const double *a, double *o) {
+    k_copy<<<flat_grid(n), 256, 0, st>>>(n, a, o);
+}
+
+}  // namespace sf

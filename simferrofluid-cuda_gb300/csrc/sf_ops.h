@@ -1,0 +1,26 @@
+// sf_ops.h -- launchers of the assembly and post-solve kernels (sf_ops.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sf_internal.cuh"
+
+namespace sf {
+
+// Three face arrays (x, y, z face grids) in the reference's layout; p[0] == nullptr means "absent".
+struct Faces {
+    const double *p[3];
+};
+
+void launch_build_pressure(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &u,
+                           const Faces &us, const Faces &jump, double vol_error, Coef<double> &cf, double *b,
+                           bool rhs_only);
+void launch_apply_projection(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &jump,
+                             const double *p, const Faces &u);
+void launch_gather_cells(cudaStream_t st, long long n, const double *D, const double *x, double *out);
+void launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, double chi, double bw,
+                           const Faces &hext, double h, Coef<double> &cf, double *b);
+void launch_total_field(cudaStream_t st, const Dims &d, const double *psi, const Faces &hext, double invh,
+                        const Faces &H);
+void launch_copy(cudaStream_t st, long long n, const double *a, double *o);
+
+}  // namespace sf

@@ -1,0 +1,156 @@
+// sf_solver.h -- host interface of the matrix-free geometric-multigrid PCG solver (sm_103a).
+//
+// The solver owns every device buffer of one grid size: the FP64 fine-level operator (filled by the
+// assembly kernels in sf_ops.cu), the right-hand side b, the solution x, the coarse hierarchy, the Krylov
+// vectors and the CUDA graphs of one iteration.  Buffers are reused across solves on the same grid, which
+// keeps graph node pointers stable.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "sf_internal.cuh"
+
+namespace sf {
+
+struct SolverParams {
+    int precision = 0;  // 0 FP64 MGPCG, 1 mixed (FP32/FP16 V-cycle + FP32 FCG inside FP64 refinement)
+    double tol = 1e-8;
+    int max_iters = 200;
+    int pre = 2, post = 2, coarse_sweeps = 24;
+    int max_levels = 0, coarse_dim = 8;
+    bool use_graph = true;
+    int check_every = 1;
+    double inner_tol = 1e-4;
+    bool flexible = false;  // Polak-Ribiere beta (needed when the preconditioner is not a fixed SPD operator)
+    bool profile = false;   // time finest-level smoother launches with events (no graphs)
+};
+
+// Counts kernel launches and, when profiling, brackets finest-level smoother launches with events.
+struct Tracker {
+    long long launches = 0;
+    bool prof = false;
+    std::vector<cudaEvent_t> ev;
+    size_t used = 0;
+    void before(cudaStream_t st, bool fine);
+    void after(cudaStream_t st, bool fine);
+    // after a stream sync: summed milliseconds and launch count of the bracketed launches; resets
+    void collect(double &ms, int &n);
+    ~Tracker();
+};
+
+struct SolveResult {
+    long long launches = 0;
+    double smooth_ms = 0;
+    int smooth_launches = 0;
+    int iters = 0, outer = 0, levels = 0;
+    bool converged = false;
+    bool breakdown = false;
+    double relres = 0, bnorm = 0;
+};
+
+class DevBuf {
+   public:
+    DevBuf() = default;
+    ~DevBuf();
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    void *get() const { return p_; }
+    size_t bytes() const { return n_; }
+    cudaError_t ensure(size_t bytes);
+    void release();
+
+   private:
+    void *p_ = nullptr;
+    size_t n_ = 0;
+};
+
+class MGSolver {
+   public:
+    explicit MGSolver(cudaStream_t s);
+    ~MGSolver();
+
+    // (Re)allocate for grid d and the solver configuration; cheap when nothing changed.
+    cudaError_t configure(const Dims &d, const SolverParams &p);
+    const Dims &dims() const { return lev_dims_[0]; }
+    int levels() const { return (int)lev_dims_.size(); }
+
+    // Fine-level FP64 operator and vectors (device).  The assembly kernels write ax/ay/az/dex/D/invd and b.
+    Coef<double> &fine() { return c64_[0]; }
+    double *b() { return b_; }
+    double *x() { return x_; }
+
+    // Build coarse levels (and the FP32/FP16 copies for the mixed form) from the fine operator.
+    cudaError_t build_hierarchy();
+
+    // Solve A x = b.  x holds the initial guess unless x_is_zero.  exclude_cell0_norm: report the residual
+    // without row 0 (the potential's pinned row).
+    cudaError_t solve(bool x_is_zero, SolveResult &res);
+
+    // ||b - A x|| / ||b|| on the fine FP64 operator; with skip0 row 0 is left out of both norms.
+    cudaError_t true_relres(bool skip0, double &relres, double &bnorm);
+
+    // Shift x so that x[0] == 0 (potential gauge).
+    cudaError_t shift_to_zero_at_origin();
+
+    size_t device_bytes() const;
+    long long take_launches() {
+        long long n = tk_.launches;
+        tk_.launches = 0;
+        return n;
+    }
+    std::string last_error;
+
+   private:
+    template <class T, class C0, class Cc>
+    friend struct HierOps;
+
+    cudaStream_t st_;
+    SolverParams prm_;
+    std::vector<Dims> lev_dims_;
+    std::vector<std::unique_ptr<DevBuf>> bufs_;
+    size_t bytes_ = 0;
+    bool configured_ = false;
+    Dims cfg_dims_{0, 0, 0, 0};
+    int cfg_prec_ = -1, cfg_levels_ = -1, cfg_cdim_ = -1;
+
+    // FP64 hierarchy (precision 0) or fine FP64 operator only (precision 1)
+    std::vector<Coef<double>> c64_;
+    std::vector<double *> x64_, b64_;  // coarse-level vectors (index 0 unused)
+    // mixed: level 0 FP32, levels >= 1 FP16
+    Coef<float> c32_{};
+    std::vector<Coef<__half>> c16_;  // index l-1 for level l
+    std::vector<float *> x32_, b32_;
+
+    double *x_ = nullptr, *b_ = nullptr;
+    // Krylov vectors
+    double *r_ = nullptr, *z_ = nullptr, *p_ = nullptr, *q_ = nullptr;
+    float *r32_ = nullptr, *d32_ = nullptr, *ri32_ = nullptr, *z32_ = nullptr, *p32_ = nullptr, *q32_ = nullptr;
+    double *sc_ = nullptr;       // scalar slots
+    double *sc_host_ = nullptr;  // pinned mirror
+    double *part_ = nullptr;     // reduction partials
+    unsigned *ticket_ = nullptr;
+
+    cudaGraphExec_t g_iter64_ = nullptr, g_iter32_ = nullptr;
+    int graph_key_ = -1;
+    long long iter_launches64_ = 0, iter_launches32_ = 0;
+    Tracker tk_;
+
+    void *alloc(size_t bytes);
+    void free_all();
+    void destroy_graphs();
+    cudaError_t solve64(bool x_is_zero, SolveResult &res);
+    cudaError_t solve_mixed(bool x_is_zero, SolveResult &res);
+    void enqueue_iter64();
+    void enqueue_iter32();
+    cudaError_t run_iter(bool mixed);
+    cudaError_t read_slots();
+};
+
+// Launch helpers shared with sf_ops.cu
+int reduce_grid(long long n);
+constexpr int kMaxRedBlocks = 152 * 8;
+
+}  // namespace sf

@@ -1,0 +1,107 @@
+"""CPU tests of the C ABI library: it loads, exports every symbol include/sfgpu.h declares, and its host-only
+entry points (options, collider) behave; no GPU compute is called."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, pkg, scenes
+
+HEADER = os.path.join(ROOT, "include", "sfgpu.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"SF_EXPORT\s+[\w\s\*]*?\b(sf_\w+)\s*\(", txt)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ["sf_create", "sf_destroy", "sf_pressure_project", "sf_pressure_project_dev", "sf_pressure_reproject",
+              "sf_magnetic_solve", "sf_magnetic_solve_dev", "sf_collider_box_fractions"]:
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol():
+    lib = pkg().load_library()
+    so = pkg()._abi.LIB_PATH
+    out = subprocess.run(["nm", "-D", "--defined-only", so], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT\s+(sf_\w+)", out))
+    for s in declared_symbols():
+        assert s in exported, s
+        assert hasattr(lib, s)
+    assert set(pkg()._abi.EXPORTED) == set(declared_symbols())
+
+
+def test_abi_version_and_defaults():
+    sf = pkg()
+    lib = sf.load_library()
+    assert lib.sf_abi_version() == 1
+    o = sf.options("pressure")
+    assert o.tol == 1e-8 and o.precision == sf.SF_PREC_FP64 and o.warm_start == 1
+    m = sf.options("magnetic", precision="mixed")
+    assert m.tol == 1e-6 and m.precision == sf.SF_PREC_MIXED
+    assert lib.sf_status_string(0) == b"ok"
+    assert lib.sf_status_string(1) == b"not converged"
+
+
+def test_structs_match_header_sizes():
+    """ctypes mirrors of sf_grid / sf_solve_opts / sf_solve_stats have the C sizes (compiled probe)."""
+    sf = pkg()
+    src = '#include "sfgpu.h"\n#include <stdio.h>\nint main(){printf("%zu %zu %zu\\n", sizeof(sf_grid), ' \
+          'sizeof(sf_solve_opts), sizeof(sf_solve_stats));return 0;}\n'
+    tmp = os.path.join(ROOT, "oracle", "_build")
+    os.makedirs(tmp, exist_ok=True)
+    c = os.path.join(tmp, "sizes.c")
+    exe = os.path.join(tmp, "sizes")
+    open(c, "w").write(src)
+    subprocess.check_call(["gcc", "-I" + os.path.join(ROOT, "include"), c, "-o", exe])
+    sizes = [int(v) for v in subprocess.check_output([exe]).split()]
+    assert sizes == [C.sizeof(sf._abi.sf_grid), C.sizeof(sf._abi.sf_solve_opts), C.sizeof(sf._abi.sf_solve_stats)]
+
+
+def test_create_without_gpu_fails_cleanly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = pkg().load_library()
+    h = C.c_void_p()
+    assert lib.sf_create(0, None, C.byref(h)) == 4  # SF_NO_DEVICE
+    assert not h.value
+
+
+def test_bad_arguments_rejected_without_gpu():
+    lib = pkg().load_library()
+    nulls = pkg()._abi.p3([0, 0, 0])
+    assert lib.sf_collider_box_fractions(None, 0, nulls, None) == 2  # SF_BAD_ARG
+    g = pkg().StaggeredGrid.from_origin(0.1, (4, 4, 4)).c_grid()
+    assert lib.sf_collider_box_fractions(C.byref(g), -1, nulls, None) == 2
+    assert lib.sf_collider_box_fractions(C.byref(g), 0, nulls, None) == 2
+
+
+@pytest.mark.parametrize("shape,bw", [((12, 9, 10), 0), ((16, 12, 16), 2), ((7, 5, 6), 1)])
+def test_collider_matches_oracle(oracle, shape, bw):
+    """Host collider (Collider ctor + FastMarching + CalcFaceFraction) is bit-identical to the oracle."""
+    sf = pkg()
+    g = sf.StaggeredGrid.from_origin(0.12 / 60, shape, origin=(-0.01, 0.02, 0.0), boundary_width=bw)
+    fr = scenes().box_fractions(g, bw)
+    og = oracle.Grid(*shape, g.spacing, tuple(g.origin))
+    fo = oracle.box_collider_fractions(og, bw)
+    for a in range(3):
+        assert np.array_equal(fr[a], fo[a])
+    # boundary faces of the grid are solid
+    for a in range(3):
+        sl = [slice(None)] * 3
+        sl[a] = 0
+        assert np.all(fr[a][tuple(sl)] == 1.0)
+
+
+def test_package_has_no_cpu_fallback(monkeypatch):
+    """The package raises when the library is missing instead of computing on the CPU."""
+    sf = pkg()
+    monkeypatch.setattr(sf._abi, "_lib", None)
+    with pytest.raises(ImportError):
+        sf._abi.load("/nonexistent/libsfgpu.so")
