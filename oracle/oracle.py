@@ -23,15 +23,19 @@ LIB = os.path.join(BUILD, "liboracle.so")
 
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc (OpenMP, no FMA contraction) into oracle/_build/liboracle.so."""
-    src = os.path.join(HERE, "sf_oracle.c")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("sf_oracle.c", "sf_amg.c")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in srcs):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + f".tmp{os.getpid()}"
     subprocess.check_call(["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-Wall",
-                           "-o", tmp, src, "-lm"])
+                           "-o", tmp, *srcs, "-lm"])
     os.replace(tmp, LIB)
     return LIB
+
+
+class _AmgInfo(C.Structure):
+    _fields_ = [("iters", C.c_int), ("resid", C.c_double), ("levels", C.c_int), ("setup_s", C.c_double)]
 
 
 class _Grid(C.Structure):
@@ -98,6 +102,9 @@ def lib():
         L.or_collider_box_levelset.argtypes = [G, C.c_int, _D]
         L.or_collider_face_fractions.argtypes = [G, _D, _D3]
         L.or_num_threads.restype = C.c_int
+        L.or_amg_solve.argtypes = [C.c_int, C.c_int64, _I64, _I32, _D, _D, _D, C.c_double, C.c_int,
+                                   C.POINTER(_AmgInfo)]
+        L.or_amg_solve.restype = C.c_int
     return _lib
 
 
@@ -143,6 +150,17 @@ class CSR:
         it = lib().or_csr_pcg(self.n, _p(self.rowptr, _I64), _p(self.col, _I32), _p(self.val), _p(b), _p(x),
                               tol, maxit, C.byref(rr))
         return x, it, rr.value
+
+    def amg_solve(self, b, kind, x0=None, tol=1e-8, maxit=100):
+        """Restated amgcl path: SA-AMG (SPAI-0) preconditioning BiCGStab (kind 0) or CG (kind 1).
+
+        Returns (x, info dict with iters, resid, levels, setup_s, converged)."""
+        x = np.zeros(self.n) if x0 is None else _f64(x0).copy()
+        b = _f64(b)
+        inf = _AmgInfo()
+        rc = lib().or_amg_solve(int(kind), self.n, _p(self.rowptr, _I64), _p(self.col, _I32), _p(self.val), _p(b),
+                                _p(x), float(tol), int(maxit), C.byref(inf))
+        return x, dict(iters=inf.iters, resid=inf.resid, levels=inf.levels, setup_s=inf.setup_s, converged=rc == 0)
 
 
 # ------------------------------------------------------------------------------------------------ pressure
@@ -193,15 +211,22 @@ def pressure_apply(g: Grid, phi, frac, jump, g2m, p_reduced, u):
     return out
 
 
-def pressure_project(g: Grid, phi, frac, u, us=None, jump=None, vol_error=0.0, tol=1e-12, maxit=20000):
-    """Pressure::Project with the linear system solved to ``tol`` (FP64 PCG).
+def pressure_project(g: Grid, phi, frac, u, us=None, jump=None, vol_error=0.0, tol=1e-12, maxit=20000,
+                     solver="pcg"):
+    """Pressure::Project with the linear system solved to ``tol``: solver "pcg" (Jacobi-PCG, the parity
+    reference) or "amg" (the restated amgcl SA-AMG + BiCGStab of core/Pressure.cpp:125-135, maxit 100).
 
     Returns (u_new, p_grid, info): p_grid is the pressure on every cell (0 in air cells)."""
     A, b, g2m, m2g = pressure_assemble(g, phi, frac, u, us, jump, vol_error)
     p_grid = np.zeros(g.N)
     if A.n == 0:
         return [_f64(a).copy() for a in u], p_grid.reshape(g.shape), dict(n=0, iters=0, relres=0.0)
-    p, it, rr = A.solve(b, tol=tol, maxit=maxit)
+    if solver == "amg":
+        p, inf = A.amg_solve(b, 0, tol=tol, maxit=min(maxit, 100))
+        it = inf["iters"]
+        rr = float(np.linalg.norm(b - A.matvec(p)) / max(np.linalg.norm(b), 1e-300))
+    else:
+        p, it, rr = A.solve(b, tol=tol, maxit=maxit)
     u_new = pressure_apply(g, phi, frac, jump, g2m, p, u)
     p_grid[m2g] = p
     return u_new, p_grid.reshape(g.shape), dict(n=A.n, iters=it, relres=rr, A=A, b=b, g2m=g2m, m2g=m2g)
@@ -247,13 +272,19 @@ def magnetic_total_field(g: Grid, psi, hext):
     return H
 
 
-def magnetic_solve(g: Grid, phi, chi, band_width, hext, psi0=None, tol=1e-12, maxit=20000):
-    """MagneticField::Solve with the pinned system solved to ``tol``.  Returns (psi, H, info)."""
+def magnetic_solve(g: Grid, phi, chi, band_width, hext, psi0=None, tol=1e-12, maxit=20000, solver="pcg"):
+    """MagneticField::Solve with the pinned system solved to ``tol`` ("pcg", or "amg" = the restated amgcl
+    SA-AMG + CG of core/MagneticField.cpp:92-94,120-123, warm start psi0).  Returns (psi, H, info)."""
     mu = magnetic_coeff(g, phi, chi, band_width)
     A = magnetic_assemble(g, mu)
     b, b0n = magnetic_rhs(g, mu, hext)
     x0 = None if psi0 is None else _f64(psi0).reshape(-1)
-    psi, it, rr = A.solve(b, x0=x0, tol=tol, maxit=maxit)
+    if solver == "amg":
+        psi, inf = A.amg_solve(b, 1, x0=x0, tol=tol, maxit=min(maxit, 100))
+        it = inf["iters"]
+        rr = float(np.linalg.norm(b - A.matvec(psi)) / max(np.linalg.norm(b), 1e-300))
+    else:
+        psi, it, rr = A.solve(b, x0=x0, tol=tol, maxit=maxit)
     H = magnetic_total_field(g, psi, hext)
     return psi.reshape(g.shape), H, dict(iters=it, relres=rr, A=A, b=b, mu=mu, rhs0_neumann=b0n)
 
