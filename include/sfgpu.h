@@ -71,7 +71,8 @@ typedef struct {
     int report_ref_residual; /* also compute the residual on the reference's own operator (default 1) */
     double inner_tol;    /* mixed: floor of the inner relative reduction (default 1e-4) */
     int profile;         /* time every finest-level smoother launch with CUDA events (disables graphs) */
-    int reserved[7];
+    int smoother;        /* 0: fused one-pass red-black sweep (default), 1: two in-place colour passes */
+    int reserved[6];
 } sf_solve_opts;
 
 typedef struct {
@@ -88,7 +89,8 @@ typedef struct {
     int smooth_launches;     /* profile: finest-level smoother launches timed */
     double smooth_ms;        /* profile: their summed device time */
     long long kernel_launches; /* kernels this call launched (graph nodes counted per replay) */
-    int reserved[4];
+    double smooth_bytes;     /* profile: algorithmic bytes of the timed smoother launches */
+    int reserved[2];
 } sf_solve_stats;
 
 /* ----- context ------------------------------------------------------------------------------------------- */

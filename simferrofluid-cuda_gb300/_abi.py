@@ -39,7 +39,7 @@ class sf_solve_opts(C.Structure):
                 ("post_smooth", C.c_int), ("coarse_sweeps", C.c_int), ("max_levels", C.c_int),
                 ("coarse_dim", C.c_int), ("warm_start", C.c_int), ("use_graph", C.c_int),
                 ("check_every", C.c_int), ("report_ref_residual", C.c_int), ("inner_tol", C.c_double),
-                ("profile", C.c_int), ("reserved", C.c_int * 7)]
+                ("profile", C.c_int), ("smoother", C.c_int), ("reserved", C.c_int * 6)]
 
 
 class sf_solve_stats(C.Structure):
@@ -48,7 +48,7 @@ class sf_solve_stats(C.Structure):
                 ("ms_build", C.c_double), ("ms_solve", C.c_double), ("ms_post", C.c_double),
                 ("ms_total", C.c_double), ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong),
                 ("status_detail", C.c_int), ("smooth_launches", C.c_int), ("smooth_ms", C.c_double),
-                ("kernel_launches", C.c_longlong), ("reserved", C.c_int * 4)]
+                ("kernel_launches", C.c_longlong), ("smooth_bytes", C.c_double), ("reserved", C.c_int * 2)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}

@@ -21,6 +21,7 @@ struct Ctx {
     std::string err;
     std::unique_ptr<MGSolver> pres, mag;
     bool pres_ready = false;
+    int pres_prec = -1;
     Dims pres_dims{0, 0, 0, 0};
     bool mag_has_x = false;
     Dims mag_dims{0, 0, 0, 0};
@@ -74,6 +75,7 @@ SolverParams params_from(const sf_solve_opts *o, int which) {
     p.inner_tol = o->inner_tol > 0 ? o->inner_tol : def.inner_tol;
     p.flexible = false;
     p.profile = o->profile != 0;
+    p.smoother = o->smoother == 1 ? 1 : 0;
     return p;
 }
 
@@ -81,6 +83,7 @@ bool opts_ok(const sf_solve_opts *o) {
     if (!o) return true;
     if (o->precision != SF_PREC_FP64 && o->precision != SF_PREC_MIXED) return false;
     if (o->max_levels < 0 || o->coarse_dim < 0) return false;
+    if (o->smoother != 0 && o->smoother != 1) return false;
     return true;
 }
 
@@ -110,6 +113,7 @@ void fill_stats(sf_solve_stats *s, const SolveResult &r, long long unknowns) {
     s->unknowns = unknowns;
     s->smooth_launches = r.smooth_launches;
     s->smooth_ms = r.smooth_ms;
+    s->smooth_bytes = r.smooth_bytes;
 }
 
 float ev_ms(cudaEvent_t a, cudaEvent_t b) {
@@ -136,8 +140,9 @@ sf_status pressure_impl(Ctx *c, const sf_grid *g, double *const vel[3], const do
     if (!std::isfinite(vol_error)) return fail(c, SF_BAD_ARG, "vol_error is not finite");
     CK(cudaSetDevice(c->device));
     const Dims d = make_dims(g->nx, g->ny, g->nz);
-    if (reproject && !(c->pres_ready && c->pres_dims.nx == d.nx && c->pres_dims.ny == d.ny && c->pres_dims.nz == d.nz))
-        return fail(c, SF_NOT_READY, "Reproject needs a previous Project on the same grid");
+    if (reproject && !(c->pres_ready && c->pres_dims.nx == d.nx && c->pres_dims.ny == d.ny && c->pres_dims.nz == d.nz &&
+                       c->pres_prec == (opts ? opts->precision : SF_PREC_FP64)))
+        return fail(c, SF_NOT_READY, "Reproject needs a previous Project on the same grid and precision");
     if (stats) memset(stats, 0, sizeof(*stats));
     long long h2d = 0, d2h = 0;
     const double *dphi;
@@ -156,7 +161,9 @@ sf_status pressure_impl(Ctx *c, const sf_grid *g, double *const vel[3], const do
     SolverParams prm = params_from(opts, 0);
     CK(S.configure(d, prm));
     CK(cudaEventRecord(c->ev[0], c->st));
-    launch_build_pressure(c->st, d, dphi, ffrac, fvel, fus, fjump, vol_error, S.fine(), S.b(), reproject);
+    // 1/D is read only by FP64 smoothers
+    launch_build_pressure(c->st, d, dphi, ffrac, fvel, fus, fjump, vol_error, S.fine(), S.b(), reproject,
+                          prm.precision == 0);
     if (!reproject) CK(S.build_hierarchy());
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->ev[1], c->st));
@@ -193,6 +200,7 @@ sf_status pressure_impl(Ctx *c, const sf_grid *g, double *const vel[3], const do
     }
     CK(cudaStreamSynchronize(c->st));
     c->pres_ready = true;
+    c->pres_prec = prm.precision;
     c->pres_dims = d;
     fill_stats(stats, res, -1);
     if (stats) stats->kernel_launches = S.take_launches() + 1 + 3 + (p_out ? 1 : 0);
@@ -240,7 +248,7 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
     CK(S.configure(d, prm));
     const bool warm = (!opts || opts->warm_start) && same_grid;
     CK(cudaEventRecord(c->ev[0], c->st));
-    launch_build_magnetic(c->st, d, dphi, chi, bw, fh, g->h, S.fine(), S.b());
+    launch_build_magnetic(c->st, d, dphi, chi, bw, fh, g->h, S.fine(), S.b(), prm.precision == 0);
     CK(S.build_hierarchy());
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->ev[1], c->st));
@@ -286,7 +294,7 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
     c->mag_has_x = true;
     c->mag_dims = d;
     fill_stats(stats, res, d.n);
-    if (stats) stats->kernel_launches = S.take_launches() + 1 + (H_out ? 3 : 0) + ((psi_out && dev) ? 1 : 0);
+    if (stats) stats->kernel_launches = S.take_launches() + 2 + (H_out ? 3 : 0) + ((psi_out && dev) ? 1 : 0);
     if (stats) {
         stats->rel_residual = relres;
         stats->rel_residual_ref = relref;

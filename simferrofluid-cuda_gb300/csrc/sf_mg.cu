@@ -61,11 +61,12 @@ void Tracker::before(cudaStream_t st, bool fine) {
         }
     cudaEventRecord(ev[used++], st);
 }
-void Tracker::after(cudaStream_t st, bool fine) {
+void Tracker::after(cudaStream_t st, bool fine, double algo_bytes) {
     if (!prof || !fine) return;
     cudaEventRecord(ev[used++], st);
+    bytes += algo_bytes;
 }
-void Tracker::collect(double &ms, int &n) {
+void Tracker::collect(double &ms, int &n, double &b) {
     ms = 0;
     n = 0;
     for (size_t q = 0; q + 1 < used; q += 2) {
@@ -74,6 +75,8 @@ void Tracker::collect(double &ms, int &n) {
         ms += t;
         n++;
     }
+    b = bytes;
+    bytes = 0;
     used = 0;
 }
 Tracker::~Tracker() {
@@ -138,6 +141,187 @@ __global__ void __launch_bounds__(256) k_rbgs(Dims d, Coef<C> cf, T *__restrict_
     }
     const T inv = (T)inv_diag<C>(cf, c, (typename Acc<C>::T)sa);
     x[c] = (b[c] + s) * inv;
+}
+
+// ------------------------------------------------------------------------------------------------ fused sweep
+// One full red-black Gauss-Seidel sweep in a single pass, out of place (xin -> xout), colour A then colour B.
+// A block owns a TY x TZ tile of (y, z) and marches along x over `xchunk` planes.  Colour-A values are
+// computed on the tile plus a one-cell ring in y and z, so the colour-B update needs no other block's
+// results: no inter-block dependency, no race, deterministic, and each array crosses HBM once per sweep
+// (x in, x out, b, couplings, diagonal) instead of twice.  Arithmetic order equals k_rbgs, so the result is
+// bit-identical to the two half sweeps.
+//   MODE 0: pre-smoothing from x = 0 (xin unused), A = red
+//   MODE 1: pre-smoothing, A = red, B = black
+//   MODE 2: post-smoothing, A = black, B = red
+constexpr int FTZ = 64, FTY = 8;
+
+__device__ __forceinline__ int mod3(int q) { return ((q % 3) + 3) % 3; }
+
+template <class T, class C, int MODE>
+__global__ void __launch_bounds__(256) k_rbgs_fused(Dims d, Coef<C> cf, const T *__restrict__ xin,
+                                                    T *__restrict__ xout, const T *__restrict__ b, int xchunk) {
+    constexpr int EZ = FTZ + 4, EY = FTY + 4, RZ = FTZ + 2, RY = FTY + 2;
+    using R = typename Acc<C>::T;
+    __shared__ T sx[3][EY][EZ];  // x_in planes (ring of 3), tile + 2 halo (unused from zero)
+    __shared__ T sa[3][RY][RZ];                  // colour-A values after the A update, tile + 1 halo
+    const int colA = (MODE == 2) ? 1 : 0;
+    const int z0 = blockIdx.x * FTZ, y0 = blockIdx.y * FTY;
+    const int x0 = blockIdx.z * xchunk;
+    const int x1 = min(x0 + xchunk, d.nx);
+    const int tid = threadIdx.x + 32 * threadIdx.y;
+    const long long sxs = (long long)d.ny * d.nz, sys = d.nz;
+
+    auto load_x = [&](int q) {
+        if constexpr (MODE == 0) return;
+        T(*dst)[EZ] = sx[mod3(q)];
+        const bool qin = q >= 0 && q < d.nx;
+        for (int e = tid; e < EY * EZ; e += 256) {
+            const int yy = e / EZ, zz = e - yy * EZ;
+            const int y = y0 - 2 + yy, z = z0 - 2 + zz;
+            T v = T(0);
+            if (qin && y >= 0 && y < d.ny && z >= 0 && z < d.nz) v = xin[cid(d, q, y, z)];
+            dst[yy][zz] = v;
+        }
+    };
+    // colour-A update of plane q on the tile + 1 ring; colour-B cells of the ring are not needed
+    auto compute_A = [&](int q) {
+        T(*dst)[RZ] = sa[mod3(q)];
+        const bool qin = q >= 0 && q < d.nx;
+        for (int e = tid; e < RY * (RZ / 2); e += 256) {
+            const int yy = e / (RZ / 2), pz = e - yy * (RZ / 2);
+            const int y = y0 - 1 + yy;
+            // zz parity so that (q + y + z) & 1 == colA with z = z0 - 1 + zz
+            const int par = (colA - q - y - z0 + 1) & 1;
+            const int zz = 2 * pz + par;
+            const int z = z0 - 1 + zz;
+            T v = T(0);
+            if (qin && y >= 0 && y < d.ny && z >= 0 && z < d.nz) {
+                const long long c = cid(d, q, y, z);
+                R s = 0, sum = 0;
+                if constexpr (MODE != 0) {
+                    const T(*xm)[EZ] = sx[mod3(q - 1)];
+                    const T(*x0p)[EZ] = sx[mod3(q)];
+                    const T(*xp)[EZ] = sx[mod3(q + 1)];
+                    const int sy_ = yy + 1, sz_ = zz + 1;
+                    if (q > 0) {
+                        R a = ldv(cf.ax, c);
+                        s += a * (R)xm[sy_][sz_];
+                        sum += a;
+                    }
+                    if (q < d.nx - 1) {
+                        R a = ldv(cf.ax, c + sxs);
+                        s += a * (R)xp[sy_][sz_];
+                        sum += a;
+                    }
+                    if (y > 0) {
+                        R a = ldv(cf.ay, c);
+                        s += a * (R)x0p[sy_ - 1][sz_];
+                        sum += a;
+                    }
+                    if (y < d.ny - 1) {
+                        R a = ldv(cf.ay, c + sys);
+                        s += a * (R)x0p[sy_ + 1][sz_];
+                        sum += a;
+                    }
+                    if (z > 0) {
+                        R a = ldv(cf.az, c);
+                        s += a * (R)x0p[sy_][sz_ - 1];
+                        sum += a;
+                    }
+                    if (z < d.nz - 1) {
+                        R a = ldv(cf.az, c + 1);
+                        s += a * (R)x0p[sy_][sz_ + 1];
+                        sum += a;
+                    }
+                    if (sizeof(C) == 2) {
+                        s *= (R)cf.unscale;
+                        sum *= (R)cf.unscale;
+                    }
+                } else {
+                    if (sizeof(C) != 8) sum = (R)couplings_sum<R, C>(d, cf, q, y, z, c);
+                }
+                const R inv = inv_diag<C>(cf, c, sum);
+                v = (T)(((R)b[c] + s) * inv);
+            }
+            dst[yy][zz] = v;
+        }
+    };
+    // colour-B update of plane p on the tile; writes both colours of plane p to xout
+    auto update_B = [&](int p) {
+        const int ty = threadIdx.y, y = y0 + ty;
+        if (y >= d.ny) return;
+        const T(*am)[RZ] = sa[mod3(p - 1)];
+        const T(*a0)[RZ] = sa[mod3(p)];
+        const T(*ap)[RZ] = sa[mod3(p + 1)];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int tz = 2 * threadIdx.x + h, z = z0 + tz;
+            if (z >= d.nz) continue;
+            const long long c = cid(d, p, y, z);
+            const int ry = ty + 1, rz = tz + 1;
+            if (((p + y + z) & 1) == colA) {
+                xout[c] = a0[ry][rz];
+                continue;
+            }
+            R s = 0, sum = 0;
+            if (p > 0) {
+                R a = ldv(cf.ax, c);
+                s += a * (R)am[ry][rz];
+                sum += a;
+            }
+            if (p < d.nx - 1) {
+                R a = ldv(cf.ax, c + sxs);
+                s += a * (R)ap[ry][rz];
+                sum += a;
+            }
+            if (y > 0) {
+                R a = ldv(cf.ay, c);
+                s += a * (R)a0[ry - 1][rz];
+                sum += a;
+            }
+            if (y < d.ny - 1) {
+                R a = ldv(cf.ay, c + sys);
+                s += a * (R)a0[ry + 1][rz];
+                sum += a;
+            }
+            if (z > 0) {
+                R a = ldv(cf.az, c);
+                s += a * (R)a0[ry][rz - 1];
+                sum += a;
+            }
+            if (z < d.nz - 1) {
+                R a = ldv(cf.az, c + 1);
+                s += a * (R)a0[ry][rz + 1];
+                sum += a;
+            }
+            if (sizeof(C) == 2) {
+                s *= (R)cf.unscale;
+                sum *= (R)cf.unscale;
+            }
+            const R inv = inv_diag<C>(cf, c, sum);
+            xout[c] = (T)(((R)b[c] + s) * inv);
+        }
+    };
+
+    // pipeline: plane q needs x_in planes q-1..q+1 for its colour-A update; plane q-1's colour-B update needs
+    // colour-A planes q-2..q.  Barriers separate every reuse of a ring slot from its last reader.
+    load_x(x0 - 2);
+    load_x(x0 - 1);
+    load_x(x0);
+    __syncthreads();
+    compute_A(x0 - 1);  // reads x_in x0-2 .. x0
+    __syncthreads();
+    load_x(x0 + 1);     // overwrites the slot of x0-2
+    __syncthreads();
+    compute_A(x0);
+    for (int q = x0 + 1; q <= x1; q++) {
+        __syncthreads();  // compute_A(q-1) and update_B(q-2) are complete
+        load_x(q + 1);    // slot of plane q-2, last read by compute_A(q-1)
+        __syncthreads();
+        compute_A(q);     // slot of colour-A plane q-3, last read by update_B(q-2)
+        __syncthreads();
+        update_B(q - 1);
+    }
 }
 
 // r = b - A x on the fine level, summed over each coarse cell's (up to) 8 children -> coarse rhs.
@@ -290,10 +474,12 @@ __global__ void k_to32(long long n, Coef<double> f, Coef<float> o) {
     }
 
 // q = A p ; slot PQ = (p, q) ; alpha = rho / pq (0 and breakdown flag if pq <= 0)
+// Per-thread partial sums are accumulated in the vector type (FP32 for FP32 vectors: FP64 arithmetic and
+// conversions are scarce on GB300) and promoted to FP64 for the cross-thread reduction.
 template <class T, class C>
 __global__ void __launch_bounds__(256) k_apply_dot(Dims d, Coef<C> cf, const T *__restrict__ p, T *__restrict__ q,
                                                    double *sc, double *part, unsigned *ticket) {
-    double v[1] = {0};
+    T acc = 0;
     ROW_LOOP(d)
     T sa;
     T s = nbsum<T, C, sizeof(C) != 8>(d, cf, p, i, j, k, c, sa);
@@ -301,8 +487,9 @@ __global__ void __launch_bounds__(256) k_apply_dot(Dims d, Coef<C> cf, const T *
     T pc = p[c];
     T qc = D * pc - s;
     q[c] = qc;
-    v[0] += (double)pc * (double)qc;
+    acc += pc * qc;
     ROW_LOOP_END
+    double v[1] = {(double)acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) {
         sc[S_PQ] = tot[0];
@@ -320,13 +507,14 @@ template <class T>
 __global__ void __launch_bounds__(256) k_dot_rz(long long n, const T *__restrict__ r, const T *__restrict__ z,
                                                 const T *__restrict__ q, int flexible, double *sc, double *part,
                                                 unsigned *ticket) {
-    double v[2] = {0, 0};
+    T a0 = 0, a1 = 0;
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
-        double zc = (double)z[c];
-        v[0] += (double)r[c] * zc;
-        v[1] += zc * (double)q[c];
+        const T zc = z[c];
+        a0 += r[c] * zc;
+        a1 += zc * q[c];
     }
+    double v[2] = {(double)a0, (double)a1};
     double tot[2];
     if (grid_reduce<2>(v, part, ticket, tot)) {
         const double rho = sc[S_RHO];
@@ -353,14 +541,15 @@ __global__ void __launch_bounds__(256) k_update(long long n, T *__restrict__ x, 
                                                 const T *__restrict__ p, const T *__restrict__ q, double *sc,
                                                 double *part, unsigned *ticket) {
     const T alpha = (T)sc[S_ALPHA];
-    double v[1] = {0};
+    T acc = 0;
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
         x[c] += alpha * p[c];
         T rc = r[c] - alpha * q[c];
         r[c] = rc;
-        v[0] += (double)rc * (double)rc;
+        acc += rc * rc;
     }
+    double v[1] = {(double)acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) sc[S_RR] = tot[0];
 }
@@ -376,17 +565,37 @@ __global__ void __launch_bounds__(256) k_residual64(Dims d, Coef<double> cf, con
     ROW_LOOP(d)
     double sa;
     double s = nbsum<double, double, false>(d, cf, x, i, j, k, c, sa);
-    double rc = (b[c] - cf.D[c] * x[c]) + s;
+    const double bc = b[c];
+    double rc = (bc - cf.D[c] * x[c]) + s;
     if (r) r[c] = (TR)rc;
     if (!(skip0 && c == 0)) {
         v[0] += rc * rc;
-        v[1] += b[c] * b[c];
+        if (bb_slot >= 0) v[1] += bc * bc;
     }
     ROW_LOOP_END
     double tot[2];
     if (grid_reduce<2>(v, part, ticket, tot)) {
         sc[rr_slot] = tot[0];
-        sc[bb_slot] = tot[1];
+        if (bb_slot >= 0) sc[bb_slot] = tot[1];
+    }
+}
+
+// r = b for x = 0 (the first refinement step): cast to the inner precision; slots rr = bb = (b, b).
+template <class TR>
+__global__ void __launch_bounds__(256) k_cast_rhs(long long n, const double *__restrict__ b, TR *__restrict__ r,
+                                                  int rr_slot, int bb_slot, double *sc, double *part,
+                                                  unsigned *ticket) {
+    double v[1] = {0};
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
+        const double bc = b[c];
+        r[c] = (TR)bc;
+        v[0] += bc * bc;
+    }
+    double tot[1];
+    if (grid_reduce<1>(v, part, ticket, tot)) {
+        sc[rr_slot] = tot[0];
+        sc[bb_slot] = tot[0];
     }
 }
 
@@ -420,24 +629,73 @@ template <class T, class C>
 static void rb(cudaStream_t st, Tracker &tk, bool fine, bool zero, const Dims &d, const Coef<C> &cf, T *x, const T *b,
                int color) {
     const dim3 g = grid_pairs(d), bk = blk2();
+    // algorithmic bytes of one colour: half of (x r/w + b + 3 couplings + diagonal term)
+    const double per = (sizeof(C) == 8 ? 56.0 : 28.0) / 2.0;
     tk.before(st, fine);
     if (zero)
         k_rbgs<T, C, true><<<g, bk, 0, st>>>(d, cf, x, b, color);
     else
         k_rbgs<T, C, false><<<g, bk, 0, st>>>(d, cf, x, b, color);
-    tk.after(st, fine);
+    tk.after(st, fine, per * d.n);
 }
 
+static inline int fused_chunk(const Dims &d) {
+    // planes per block along x: enough blocks to fill 152 SMs a few times over, long runs for reuse
+    const long long tiles = (long long)((d.nz + FTZ - 1) / FTZ) * ((d.ny + FTY - 1) / FTY);
+    int chunk = 32;
+    while (chunk > 4 && tiles * ((d.nx + chunk - 1) / chunk) < 152 * 6) chunk /= 2;
+    return chunk < d.nx ? chunk : d.nx;
+}
+
+template <class T, class C, int MODE>
+static void fused(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const Coef<C> &cf, const T *xin, T *xout,
+                  const T *b) {
+    const int chunk = fused_chunk(d);
+    const dim3 g((d.nz + FTZ - 1) / FTZ, (d.ny + FTY - 1) / FTY, (d.nx + chunk - 1) / chunk);
+    const double s = sizeof(C) == 8 ? 8.0 : 4.0;
+    // x in (not from zero) + x out + b + 3 couplings + diagonal term
+    const double per = (MODE == 0 ? 0.0 : s) + s + s + 3 * s + s;
+    tk.before(st, fine);
+    k_rbgs_fused<T, C, MODE><<<g, dim3(32, 8), 0, st>>>(d, cf, xin, xout, b, chunk);
+    tk.after(st, fine, per * d.n);
+}
+
+// nu sweeps; the result always ends in x.  pre: starts from x = 0 (x's input value is ignored).
+// fused (tmp != nullptr): one kernel per sweep, ping-ponging between x and tmp; else two in-place colours.
 template <class T, class C>
-static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const Coef<C> &cf, T *x, const T *b, int nu,
-                   bool pre) {
-    for (int s = 0; s < nu; s++) {
-        if (pre) {
-            rb<T, C>(st, tk, fine, s == 0, d, cf, x, b, 0);
-            rb<T, C>(st, tk, fine, false, d, cf, x, b, 1);
-        } else {
-            rb<T, C>(st, tk, fine, false, d, cf, x, b, 1);
-            rb<T, C>(st, tk, fine, false, d, cf, x, b, 0);
+static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const Coef<C> &cf, T *x, T *tmp,
+                   const T *b, int nu, bool pre) {
+    if (!tmp) {
+        for (int s = 0; s < nu; s++) {
+            if (pre) {
+                rb<T, C>(st, tk, fine, s == 0, d, cf, x, b, 0);
+                rb<T, C>(st, tk, fine, false, d, cf, x, b, 1);
+            } else {
+                rb<T, C>(st, tk, fine, false, d, cf, x, b, 1);
+                rb<T, C>(st, tk, fine, false, d, cf, x, b, 0);
+            }
+        }
+        return;
+    }
+    if (pre) {
+        T *prev = nullptr;
+        for (int s = 0; s < nu; s++) {
+            T *out = ((nu - 1 - s) % 2 == 0) ? x : tmp;
+            if (s == 0)
+                fused<T, C, 0>(st, tk, fine, d, cf, (const T *)nullptr, out, b);
+            else
+                fused<T, C, 1>(st, tk, fine, d, cf, prev, out, b);
+            prev = out;
+        }
+    } else {
+        for (int s = 0; s < nu; s++) {
+            const T *in = (s % 2 == 0) ? x : tmp;
+            T *out = (s % 2 == 0) ? tmp : x;
+            fused<T, C, 2>(st, tk, fine, d, cf, in, out, b);
+        }
+        if (nu % 2 == 1) {
+            tk.launches++;
+            cudaMemcpyAsync(x, tmp, sizeof(T) * d.n, cudaMemcpyDeviceToDevice, st);
         }
     }
 }
@@ -456,31 +714,32 @@ static void coarse_solve(cudaStream_t st, Tracker &tk, const Dims &d, const Coef
     k_coarse<T, C><<<1, nt, 0, st>>>(d, cf, x, b, pairs);
 }
 
-// V-cycle z = M r.  Level 0 uses coefficient type C0, coarse levels Cc (cc[l] for level l >= 1).
+// V-cycle z = M r.  Level 0 uses coefficient type C0, coarse levels Cc (cc[l] for level l >= 1).  ts[l] is a
+// scratch vector of level l for the fused smoother (nullptr entries select the in-place two-colour smoother).
 template <class T, class C0, class Cc>
 static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, const Coef<C0> &c0,
                    const std::vector<Coef<Cc>> &cc, T *z, const T *r, const std::vector<T *> &xs,
-                   const std::vector<T *> &bs, const SolverParams &p) {
+                   const std::vector<T *> &bs, const std::vector<T *> &ts, const SolverParams &p) {
     const int L = (int)dims.size();
     if (L == 1) {
         coarse_solve<T, C0>(st, tk, dims[0], c0, z, r, p.coarse_sweeps);
         return;
     }
-    smooth<T, C0>(st, tk, true, dims[0], c0, z, r, p.pre, true);
+    smooth<T, C0>(st, tk, true, dims[0], c0, z, ts[0], r, p.pre, true);
     restrict_res<T, C0>(st, tk, dims[0], c0, z, r, dims[1], bs[1]);
     for (int l = 1; l < L - 1; l++) {
-        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], bs[l], p.pre, true);
+        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], ts[l], bs[l], p.pre, true);
         restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1]);
     }
     coarse_solve<T, Cc>(st, tk, dims[L - 1], cc[L - 1], xs[L - 1], bs[L - 1], p.coarse_sweeps);
     for (int l = L - 2; l >= 1; l--) {
         tk.launches++;
         k_prolong<T><<<grid_cells(dims[l]), blk2(), 0, st>>>(dims[l], xs[l], dims[l + 1], xs[l + 1]);
-        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], bs[l], p.post, false);
+        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], ts[l], bs[l], p.post, false);
     }
     tk.launches++;
     k_prolong<T><<<grid_cells(dims[0]), blk2(), 0, st>>>(dims[0], z, dims[1], xs[1]);
-    smooth<T, C0>(st, tk, true, dims[0], c0, z, r, p.post, false);
+    smooth<T, C0>(st, tk, true, dims[0], c0, z, ts[0], r, p.post, false);
 }
 
 // ------------------------------------------------------------------------------------------------ MGSolver
@@ -562,6 +821,8 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     if (p.precision == 0) {
         x64_.assign(L, nullptr);
         b64_.assign(L, nullptr);
+        t64_.assign(L, nullptr);
+        for (int l = 0; l < L; l++) t64_[l] = (double *)chk(A(8 * dims[l].n));
         for (int l = 1; l < L; l++) {
             x64_[l] = (double *)chk(A(8 * dims[l].n));
             b64_[l] = (double *)chk(A(8 * dims[l].n));
@@ -580,6 +841,8 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
         c16_.assign(L, Coef<__half>{});
         x32_.assign(L, nullptr);
         b32_.assign(L, nullptr);
+        t32_.assign(L, nullptr);
+        for (int l = 0; l < L; l++) t32_[l] = (float *)chk(A(4 * dims[l].n));
         for (int l = 1; l < L; l++) {
             const long long m = dims[l].n;
             Coef<__half> &c = c16_[l];
@@ -643,7 +906,8 @@ void MGSolver::enqueue_iter64() {
     const long long n = d.n;
     const int rg = reduce_grid((long long)d.nx * d.ny);
     const long long l0 = tk_.launches;
-    vcycle<double, double, double>(st_, tk_, lev_dims_, c64_[0], c64_, z_, r_, x64_, b64_, prm_);
+    vcycle<double, double, double>(st_, tk_, lev_dims_, c64_[0], c64_, z_, r_, x64_, b64_,
+                                   prm_.smoother == 0 ? t64_ : std::vector<double *>(t64_.size(), nullptr), prm_);
     k_dot_rz<double><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, r_, z_, q_, prm_.flexible ? 1 : 0, sc_, part_,
                                                               ticket_);
     k_xpby<double><<<flat_grid(n), 256, 0, st_>>>(n, z_, p_, sc_);
@@ -659,7 +923,8 @@ void MGSolver::enqueue_iter32() {
     const long long n = d.n;
     const int rg = reduce_grid((long long)d.nx * d.ny);
     const long long l0 = tk_.launches;
-    vcycle<float, float, __half>(st_, tk_, lev_dims_, c32_, c16_, z32_, ri32_, x32_, b32_, prm_);
+    vcycle<float, float, __half>(st_, tk_, lev_dims_, c32_, c16_, z32_, ri32_, x32_, b32_,
+                                 prm_.smoother == 0 ? t32_ : std::vector<float *>(t32_.size(), nullptr), prm_);
     k_dot_rz<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, ri32_, z32_, q32_, 1, sc_, part_, ticket_);
     k_xpby<float><<<flat_grid(n), 256, 0, st_>>>(n, z32_, p32_, sc_);
     k_apply_dot<float, float><<<rg, dim3(32, 8), 0, st_>>>(d, c32_, p32_, q32_, sc_, part_, ticket_);
@@ -679,7 +944,8 @@ cudaError_t MGSolver::run_iter(bool mixed) {
             enqueue_iter64();
         return cudaGetLastError();
     }
-    const int key = (prm_.pre << 0) | (prm_.post << 4) | (prm_.coarse_sweeps << 8) | ((prm_.flexible ? 1 : 0) << 20);
+    const int key = (prm_.pre << 0) | (prm_.post << 4) | (prm_.coarse_sweeps << 8) | ((prm_.flexible ? 1 : 0) << 20) |
+                    (prm_.smoother << 21);
     if (key != graph_key_) destroy_graphs();
     graph_key_ = key;
     cudaGraphExec_t &ge = mixed ? g_iter32_ : g_iter64_;
@@ -720,7 +986,7 @@ cudaError_t MGSolver::solve(bool x_is_zero, SolveResult &res) {
     if (prm_.profile) {
         e = cudaStreamSynchronize(st_);
         if (e != cudaSuccess) return e;
-        tk_.collect(res.smooth_ms, res.smooth_launches);
+        tk_.collect(res.smooth_ms, res.smooth_launches, res.smooth_bytes);
     }
     return cudaSuccess;
 }
@@ -730,9 +996,13 @@ cudaError_t MGSolver::solve64(bool x_is_zero, SolveResult &res) {
     const long long n = d.n;
     const int rg = reduce_grid((long long)d.nx * d.ny);
     cudaError_t e;
-    if (x_is_zero) cudaMemsetAsync(x_, 0, 8 * n, st_);
-    // r = b - A x, (r,r), (b,b)
-    k_residual64<double><<<rg, dim3(32, 8), 0, st_>>>(d, c64_[0], x_, b_, r_, 0, S_RR, S_BB, sc_, part_, ticket_);
+    if (x_is_zero) {
+        cudaMemsetAsync(x_, 0, 8 * n, st_);
+        k_cast_rhs<double><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, b_, r_, S_RR, S_BB, sc_, part_, ticket_);
+    } else {
+        // r = b - A x, (r,r), (b,b)
+        k_residual64<double><<<rg, dim3(32, 8), 0, st_>>>(d, c64_[0], x_, b_, r_, 0, S_RR, S_BB, sc_, part_, ticket_);
+    }
     tk_.launches++;
     cudaMemsetAsync(p_, 0, 8 * n, st_);
     cudaMemsetAsync(q_, 0, 8 * n, st_);
@@ -788,10 +1058,16 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
     double bb = -1, rr = 0;
     int total_inner = 0, outer = 0;
     const int max_outer = 30;
+    bool x_zero = x_is_zero;
     while (true) {
         // outer FP64 residual, cast to the FP32 inner right-hand side
-        k_residual64<float><<<rg, dim3(32, 8), 0, st_>>>(d, c64_[0], x_, b_, r32_, 0, S_AUX1, S_BB, sc_, part_,
-                                                         ticket_);
+        if (x_zero) {
+            k_cast_rhs<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, b_, r32_, S_AUX1, S_BB, sc_, part_, ticket_);
+            x_zero = false;
+        } else {
+            k_residual64<float><<<rg, dim3(32, 8), 0, st_>>>(d, c64_[0], x_, b_, r32_, 0, S_AUX1, bb < 0 ? S_BB : -1,
+                                                             sc_, part_, ticket_);
+        }
         tk_.launches++;
         if ((e = read_slots()) != cudaSuccess) return e;
         rr = sc_host_[S_AUX1];

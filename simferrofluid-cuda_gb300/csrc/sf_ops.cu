@@ -23,7 +23,8 @@ __device__ __forceinline__ long long fid(const Dims &d, int a, int i, int j, int
 // closed (w = 0).  D is the reference's diagonal bit for bit (same summation order, 1 for an isolated cell).
 __global__ void __launch_bounds__(256) k_build_pressure(Dims d, const double *__restrict__ phi, Faces frac,
                                                         Faces u, Faces us, Faces jump, double vol_error,
-                                                        Coef<double> cf, double *__restrict__ b, int rhs_only) {
+                                                        Coef<double> cf, double *__restrict__ b, int rhs_only,
+                                                        int want_invd) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -87,7 +88,7 @@ __global__ void __launch_bounds__(256) k_build_pressure(Dims d, const double *__
     cf.az[c] = lower[2];
     cf.dex[c] = dexv;
     cf.D[c] = D;
-    cf.invd[c] = D > 0 ? 1. / D : 0.0;
+    if (want_invd) cf.invd[c] = D > 0 ? 1. / D : 0.0;
 }
 
 // Pressure::ApplyProjection (core/Pressure.cpp:137-166) for the faces of axis a.  p is the solution on
@@ -152,43 +153,55 @@ __device__ __forceinline__ double mu_face(double philo, double phihi, double chi
     return 1. + (1. - heaviside(pf, bw)) * chi;
 }
 
-// BuildMatrix + AssembleRHS (core/MagneticField.cpp:50-118) for one cell, in Neumann form: D = sum of mu over
-// in-grid faces, couplings mu, b in the reference's face order (row 0 gets its unpinned value; the pinned
-// row 0 of the reference is recovered by the psi[0] = 0 gauge after the solve).
-__global__ void __launch_bounds__(256) k_build_magnetic(Dims d, const double *__restrict__ phi, double chi, double bw,
-                                                        Faces hext, double h, Coef<double> cf,
-                                                        double *__restrict__ b) {
+// BuildMatrix, coefficient pass (core/MagneticField.cpp:51-60): mu on the lower x/y/z face of every cell,
+// stored directly as the lower-face couplings ax/ay/az (0 on the grid boundary, where the reference's mu = 1
+// is never used).  Each face is evaluated once.
+__global__ void __launch_bounds__(256) k_magnetic_mu(Dims d, const double *__restrict__ phi, double chi, double bw,
+                                                     Coef<double> cf) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
     if (k >= d.nz || j >= d.ny) return;
     const long long c = cid(d, i, j, k);
-    const int dn[3] = {d.nx, d.ny, d.nz};
     const double pc = phi[c];
-    double lower[3] = {0, 0, 0};
+    cf.ax[c] = i > 0 ? mu_face(phi[c - (long long)d.ny * d.nz], pc, chi, bw) : 0.0;
+    cf.ay[c] = j > 0 ? mu_face(phi[c - d.nz], pc, chi, bw) : 0.0;
+    cf.az[c] = k > 0 ? mu_face(phi[c - 1], pc, chi, bw) : 0.0;
+}
+
+// BuildMatrix, row pass + AssembleRHS (core/MagneticField.cpp:62-118) in Neumann form: D = sum of mu over the
+// in-grid faces in the reference's face order, rhs = sum (mu - 1) Hext (-side) h in the same order (faces with
+// mu == 1 add a signed zero, which leaves the sum unchanged, and are skipped).  Row 0 keeps its unpinned value:
+// the reference's pinned row 0 is recovered by the psi[0] = 0 gauge after the solve.
+__global__ void __launch_bounds__(256) k_magnetic_rows(Dims d, Faces hext, double h, Coef<double> cf,
+                                                       double *__restrict__ b, int want_invd) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= d.nz || j >= d.ny) return;
+    const long long c = cid(d, i, j, k);
+    const long long sx = (long long)d.ny * d.nz, sy = d.nz;
     double diag = 0., rhs = 0.;
+    // (mu, valid, face index) in ord order -x, +x, -y, +y, -z, +z
 #pragma unroll
     for (int ord = 0; ord < 6; ord++) {
-        const int a = ord >> 1;
-        const int up = ord & 1;
-        int n3[3] = {i, j, k};
-        n3[a] += up ? 1 : -1;
-        if (n3[a] < 0 || n3[a] >= dn[a]) continue;
-        int f3[3] = {i, j, k};
-        f3[a] += up;
-        const double pn = phi[cid(d, n3[0], n3[1], n3[2])];
-        const double mu = up ? mu_face(pc, pn, chi, bw) : mu_face(pn, pc, chi, bw);
-        if (!up) lower[a] = mu;
+        const int a = ord >> 1, up = ord & 1;
+        const int ia = a == 0 ? i : (a == 1 ? j : k);
+        const int na = a == 0 ? d.nx : (a == 1 ? d.ny : d.nz);
+        if (up ? (ia >= na - 1) : (ia <= 0)) continue;
+        const long long st = a == 0 ? sx : (a == 1 ? sy : 1);
+        const double *arr = a == 0 ? cf.ax : (a == 1 ? cf.ay : cf.az);
+        const double mu = up ? arr[c + st] : arr[c];
         diag += mu;
-        const double side = up ? 1.0 : -1.0;
-        rhs += (mu - 1.) * hext.p[a][fid(d, a, f3[0], f3[1], f3[2])] * (-side) * h;
+        if (mu != 1.) {
+            const int fi = i + (a == 0) * up, fj = j + (a == 1) * up, fk = k + (a == 2) * up;
+            const double side = up ? 1.0 : -1.0;
+            rhs += (mu - 1.) * hext.p[a][fid(d, a, fi, fj, fk)] * (-side) * h;
+        }
     }
-    cf.ax[c] = lower[0];
-    cf.ay[c] = lower[1];
-    cf.az[c] = lower[2];
     cf.dex[c] = 0.;
     cf.D[c] = diag;
-    cf.invd[c] = diag > 0 ? 1. / diag : 0.;
+    if (want_invd) cf.invd[c] = diag > 0 ? 1. / diag : 0.;
     b[c] = rhs;
 }
 
@@ -228,9 +241,9 @@ static inline int flat_grid(long long n) {
 // ------------------------------------------------------------------------------------------------ launchers
 void launch_build_pressure(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &u,
                            const Faces &us, const Faces &jump, double vol_error, Coef<double> &cf, double *b,
-                           bool rhs_only) {
+                           bool rhs_only, bool want_invd) {
     k_build_pressure<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, frac, u, us, jump, vol_error, cf, b,
-                                                                  rhs_only ? 1 : 0);
+                                                                  rhs_only ? 1 : 0, want_invd ? 1 : 0);
 }
 
 void launch_apply_projection(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &jump,
@@ -244,9 +257,11 @@ void launch_gather_cells(cudaStream_t st, long long n, const double *D, const do
     k_gather_cells<<<flat_grid(n), 256, 0, st>>>(n, D, x, out);
 }
 
-void launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, double chi, double bw,
-                           const Faces &hext, double h, Coef<double> &cf, double *b) {
-    k_build_magnetic<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, chi, bw, hext, h, cf, b);
+int launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, double chi, double bw,
+                          const Faces &hext, double h, Coef<double> &cf, double *b, bool want_invd) {
+    k_magnetic_mu<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, chi, bw, cf);
+    k_magnetic_rows<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, hext, h, cf, b, want_invd ? 1 : 0);
+    return 2;
 }
 
 void launch_total_field(cudaStream_t st, const Dims &d, const double *psi, const Faces &hext, double invh,

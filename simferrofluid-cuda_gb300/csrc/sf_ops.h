@@ -13,12 +13,12 @@ struct Faces {
 
 void launch_build_pressure(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &u,
                            const Faces &us, const Faces &jump, double vol_error, Coef<double> &cf, double *b,
-                           bool rhs_only);
+                           bool rhs_only, bool want_invd);
 void launch_apply_projection(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &jump,
                              const double *p, const Faces &u);
 void launch_gather_cells(cudaStream_t st, long long n, const double *D, const double *x, double *out);
-void launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, double chi, double bw,
-                           const Faces &hext, double h, Coef<double> &cf, double *b);
+int launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, double chi, double bw,
+                          const Faces &hext, double h, Coef<double> &cf, double *b, bool want_invd);
 void launch_total_field(cudaStream_t st, const Dims &d, const double *psi, const Faces &hext, double invh,
                         const Faces &H);
 void launch_copy(cudaStream_t st, long long n, const double *a, double *o);

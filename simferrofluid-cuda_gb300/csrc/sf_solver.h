@@ -26,6 +26,7 @@ struct SolverParams {
     double inner_tol = 1e-4;
     bool flexible = false;  // Polak-Ribiere beta (needed when the preconditioner is not a fixed SPD operator)
     bool profile = false;   // time finest-level smoother launches with events (no graphs)
+    int smoother = 0;       // 0: fused one-pass red-black sweep, 1: two in-place colour kernels
 };
 
 // Counts kernel launches and, when profiling, brackets finest-level smoother launches with events.
@@ -34,16 +35,18 @@ struct Tracker {
     bool prof = false;
     std::vector<cudaEvent_t> ev;
     size_t used = 0;
+    double bytes = 0;
     void before(cudaStream_t st, bool fine);
-    void after(cudaStream_t st, bool fine);
-    // after a stream sync: summed milliseconds and launch count of the bracketed launches; resets
-    void collect(double &ms, int &n);
+    void after(cudaStream_t st, bool fine, double algo_bytes);
+    // after a stream sync: summed milliseconds, launch count and algorithmic bytes of the bracketed
+    // launches; resets
+    void collect(double &ms, int &n, double &b);
     ~Tracker();
 };
 
 struct SolveResult {
     long long launches = 0;
-    double smooth_ms = 0;
+    double smooth_ms = 0, smooth_bytes = 0;
     int smooth_launches = 0;
     int iters = 0, outer = 0, levels = 0;
     bool converged = false;
@@ -119,10 +122,11 @@ class MGSolver {
     // FP64 hierarchy (precision 0) or fine FP64 operator only (precision 1)
     std::vector<Coef<double>> c64_;
     std::vector<double *> x64_, b64_;  // coarse-level vectors (index 0 unused)
+    std::vector<double *> t64_;        // smoother scratch per level
     // mixed: level 0 FP32, levels >= 1 FP16
     Coef<float> c32_{};
     std::vector<Coef<__half>> c16_;  // index l-1 for level l
-    std::vector<float *> x32_, b32_;
+    std::vector<float *> x32_, b32_, t32_;
 
     double *x_ = nullptr, *b_ = nullptr;
     // Krylov vectors
