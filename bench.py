@@ -45,6 +45,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64-arm", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--inner-tol", type=float, default=None, help="mixed form: inner relative reduction floor")
+    ap.add_argument("--coarse-dim", type=int, default=None)
+    ap.add_argument("--pre", type=int, default=None)
+    ap.add_argument("--post", type=int, default=None)
+    ap.add_argument("--smoother", type=int, default=None, help="0 two-colour (default), 1 fused one-pass")
     return ap.parse_args()
 
 
@@ -170,8 +175,14 @@ def run_ours(args, ws, rank, local):
     torch.cuda.synchronize(dev)
 
     def opts(which, precision, profile=0):
+        kw = {}
+        for name, key in (("inner_tol", "inner_tol"), ("coarse_dim", "coarse_dim"), ("pre", "pre_smooth"),
+                          ("post", "post_smooth"), ("smoother", "smoother")):
+            v = getattr(args, name)
+            if v is not None:
+                kw[key] = v
         return pkg.options(which, precision=precision, tol=args.tol, warm_start=0, report_ref_residual=0,
-                           profile=profile)
+                           profile=profile, **kw)
 
     def step(precision, profile=0, record=None):
         for a in range(3):
@@ -240,7 +251,9 @@ def run_ours(args, ws, rank, local):
     peak_src = "measured" if peak else "fallback"
     peak = peak or 6800.0
     achieved = bytes_tot / (ms_tot / 1e3) / 1e9 if ms_tot > 0 else 0.0
-    roofline = {"bound": "hbm", "kernel": "k_rbgs_fused (finest level, one full red-black sweep per launch)",
+    kname = "k_rbgs_fused (one full red-black sweep per launch)" if args.smoother == 1 else \
+        "k_rbgs (one colour of a red-black sweep per launch)"
+    roofline = {"bound": "hbm", "kernel": kname + ", finest level",
                 "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": None,
                 "bytes_per_launch": bytes_tot / max(n_launch, 1), "ms_per_launch": ms_tot / max(n_launch, 1),
@@ -292,7 +305,9 @@ def run_ours(args, ws, rank, local):
         "config": {"workload": f"pool_sphere {args.n}^3 chi=2 dipole field, pressure+potential per step, "
                                f"{args.precision} MGPCG to {args.tol:g} from zero",
                    "grid": [args.n] * 3, "precision": args.precision, "tol": args.tol,
-                   "l2": "inputs larger than L2 (each field 134 MB at 256^3)", "parallelism": f"replicas x{ws}"},
+                   "l2": "inputs larger than L2 (each field 134 MB at 256^3)", "parallelism": f"replicas x{ws}",
+                   "solver": {k: getattr(args, k) for k in ("inner_tol", "coarse_dim", "pre", "post", "smoother")
+                              if getattr(args, k) is not None}},
         "iters": {"pressure": it_p, "magnetic": it_m}, "max_rel_residual": {"pressure": res_p, "magnetic": res_m},
         "fp64_mgpcg": fp64,
         "speedup_vs_fp64": round(value / fp64["solves_per_s"], 3) if fp64 else None,

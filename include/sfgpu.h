@@ -71,7 +71,7 @@ typedef struct {
     int report_ref_residual; /* also compute the residual on the reference's own operator (default 1) */
     double inner_tol;    /* mixed: floor of the inner relative reduction (default 1e-4) */
     int profile;         /* time every finest-level smoother launch with CUDA events (disables graphs) */
-    int smoother;        /* 0: fused one-pass red-black sweep (default), 1: two in-place colour passes */
+    int smoother;        /* 0: two in-place colour passes (default), 1: fused one-pass red-black sweep */
     int reserved[6];
 } sf_solve_opts;
 

@@ -43,11 +43,11 @@ void DevBuf::release() {
     n_ = 0;
 }
 
-int reduce_grid(long long rows) {
-    long long g = (rows + 7) / 8;
-    if (g > kMaxRedBlocks) g = kMaxRedBlocks;
-    if (g < 1) g = 1;
-    return (int)g;
+dim3 tile_grid(const Dims &d, int &xpb) {
+    const long long tiles = (long long)((d.nz + 31) / 32) * ((d.ny + 7) / 8);
+    long long x = (tiles * d.nx + kMaxTileBlocks - 1) / kMaxTileBlocks;
+    xpb = (int)(x < 1 ? 1 : x);
+    return dim3((d.nz + 31) / 32, (d.ny + 7) / 8, (d.nx + xpb - 1) / xpb);
 }
 
 void Tracker::before(cudaStream_t st, bool fine) {
@@ -460,27 +460,27 @@ __global__ void k_to32(long long n, Coef<double> f, Coef<float> o) {
 }
 
 // ------------------------------------------------------------------------------------------------ Krylov kernels
-// Row-parallel shape for reductions: block (32, 8); each warp walks z-lines (rows) of the grid.
-#define ROW_LOOP(d)                                                                                          \
-    const long long nrows = (long long)(d).nx * (d).ny;                                                      \
-    for (long long row = (long long)blockIdx.x * blockDim.y + threadIdx.y; row < nrows;                     \
-         row += (long long)gridDim.x * blockDim.y) {                                                         \
-        const int i = (int)(row / (d).ny), j = (int)(row % (d).ny);                                          \
-        for (int k = threadIdx.x; k < (d).nz; k += 32) {                                                     \
-            const long long c = (long long)k + (long long)(d).nz * row;
+// Stencil kernels with a reduction: block (32, 8) over a (z, y) tile, each block walks `xpb` consecutive x
+// planes (so x +- 1 neighbours come from its own previous/next plane), at most kMaxTileBlocks blocks.  Threads
+// outside the grid keep looping so that every thread reaches the block reduction.
+#define TILE_LOOP(d, xpb)                                                                     \
+    const int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;           \
+    const bool inb = k < (d).nz && j < (d).ny;                                                \
+    const int i_end = min((d).nx, (int)(blockIdx.z + 1) * (xpb));                             \
+    for (int i = blockIdx.z * (xpb); i < i_end; i++) {                                        \
+        if (!inb) continue;                                                                   \
+        const long long c = cid((d), i, j, k);
 
-#define ROW_LOOP_END \
-    }                \
-    }
+#define TILE_LOOP_END }
 
 // q = A p ; slot PQ = (p, q) ; alpha = rho / pq (0 and breakdown flag if pq <= 0)
 // Per-thread partial sums are accumulated in the vector type (FP32 for FP32 vectors: FP64 arithmetic and
 // conversions are scarce on GB300) and promoted to FP64 for the cross-thread reduction.
 template <class T, class C>
-__global__ void __launch_bounds__(256) k_apply_dot(Dims d, Coef<C> cf, const T *__restrict__ p, T *__restrict__ q,
-                                                   double *sc, double *part, unsigned *ticket) {
+__global__ void __launch_bounds__(256) k_apply_dot(Dims d, int xpb, Coef<C> cf, const T *__restrict__ p,
+                                                   T *__restrict__ q, double *sc, double *part, unsigned *ticket) {
     T acc = 0;
-    ROW_LOOP(d)
+    TILE_LOOP(d, xpb)
     T sa;
     T s = nbsum<T, C, sizeof(C) != 8>(d, cf, p, i, j, k, c, sa);
     T D = (T)diag_of<C>(cf, c, (typename Acc<C>::T)sa);
@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(256) k_apply_dot(Dims d, Coef<C> cf, const T *
     T qc = D * pc - s;
     q[c] = qc;
     acc += pc * qc;
-    ROW_LOOP_END
+    TILE_LOOP_END
     double v[1] = {(double)acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) {
@@ -557,12 +557,12 @@ __global__ void __launch_bounds__(256) k_update(long long n, T *__restrict__ x, 
 // r = b - A x (FP64 operator), written as TR (double, or float for the refinement's inner rhs);
 // slots: rr_slot = (r, r) in FP64, bb_slot = (b, b).  skip0: leave row 0 out of both sums.
 template <class TR>
-__global__ void __launch_bounds__(256) k_residual64(Dims d, Coef<double> cf, const double *__restrict__ x,
+__global__ void __launch_bounds__(256) k_residual64(Dims d, int xpb, Coef<double> cf, const double *__restrict__ x,
                                                     const double *__restrict__ b, TR *__restrict__ r, int skip0,
                                                     int rr_slot, int bb_slot, double *sc, double *part,
                                                     unsigned *ticket) {
     double v[2] = {0, 0};
-    ROW_LOOP(d)
+    TILE_LOOP(d, xpb)
     double sa;
     double s = nbsum<double, double, false>(d, cf, x, i, j, k, c, sa);
     const double bc = b[c];
@@ -572,7 +572,7 @@ __global__ void __launch_bounds__(256) k_residual64(Dims d, Coef<double> cf, con
         v[0] += rc * rc;
         if (bb_slot >= 0) v[1] += bc * bc;
     }
-    ROW_LOOP_END
+    TILE_LOOP_END
     double tot[2];
     if (grid_reduce<2>(v, part, ticket, tot)) {
         sc[rr_slot] = tot[0];
@@ -816,7 +816,7 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     x_ = (double *)chk(A(8 * n));
     b_ = (double *)chk(A(8 * n));
     sc_ = (double *)chk(A(8 * S_NSLOTS));
-    part_ = (double *)chk(A(8 * 4 * (size_t)kMaxRedBlocks));
+    part_ = (double *)chk(A(8 * 4 * (size_t)(kMaxTileBlocks > kMaxRedBlocks ? kMaxTileBlocks : kMaxRedBlocks)));
     ticket_ = (unsigned *)chk(A(256));
     if (p.precision == 0) {
         x64_.assign(L, nullptr);
@@ -904,14 +904,15 @@ cudaError_t MGSolver::build_hierarchy() {
 void MGSolver::enqueue_iter64() {
     const Dims &d = lev_dims_[0];
     const long long n = d.n;
-    const int rg = reduce_grid((long long)d.nx * d.ny);
+    int xpb;
+    const dim3 tg = tile_grid(d, xpb);
     const long long l0 = tk_.launches;
     vcycle<double, double, double>(st_, tk_, lev_dims_, c64_[0], c64_, z_, r_, x64_, b64_,
-                                   prm_.smoother == 0 ? t64_ : std::vector<double *>(t64_.size(), nullptr), prm_);
+                                   prm_.smoother == 1 ? t64_ : std::vector<double *>(t64_.size(), nullptr), prm_);
     k_dot_rz<double><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, r_, z_, q_, prm_.flexible ? 1 : 0, sc_, part_,
                                                               ticket_);
     k_xpby<double><<<flat_grid(n), 256, 0, st_>>>(n, z_, p_, sc_);
-    k_apply_dot<double, double><<<rg, dim3(32, 8), 0, st_>>>(d, c64_[0], p_, q_, sc_, part_, ticket_);
+    k_apply_dot<double, double><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c64_[0], p_, q_, sc_, part_, ticket_);
     k_update<double><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, x_, r_, p_, q_, sc_, part_, ticket_);
     tk_.launches += 4;
     iter_launches64_ = tk_.launches - l0;
@@ -921,13 +922,14 @@ void MGSolver::enqueue_iter64() {
 void MGSolver::enqueue_iter32() {
     const Dims &d = lev_dims_[0];
     const long long n = d.n;
-    const int rg = reduce_grid((long long)d.nx * d.ny);
+    int xpb;
+    const dim3 tg = tile_grid(d, xpb);
     const long long l0 = tk_.launches;
     vcycle<float, float, __half>(st_, tk_, lev_dims_, c32_, c16_, z32_, ri32_, x32_, b32_,
-                                 prm_.smoother == 0 ? t32_ : std::vector<float *>(t32_.size(), nullptr), prm_);
+                                 prm_.smoother == 1 ? t32_ : std::vector<float *>(t32_.size(), nullptr), prm_);
     k_dot_rz<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, ri32_, z32_, q32_, 1, sc_, part_, ticket_);
     k_xpby<float><<<flat_grid(n), 256, 0, st_>>>(n, z32_, p32_, sc_);
-    k_apply_dot<float, float><<<rg, dim3(32, 8), 0, st_>>>(d, c32_, p32_, q32_, sc_, part_, ticket_);
+    k_apply_dot<float, float><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c32_, p32_, q32_, sc_, part_, ticket_);
     k_update<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, d32_, ri32_, p32_, q32_, sc_, part_, ticket_);
     tk_.launches += 4;
     iter_launches32_ = tk_.launches - l0;
@@ -994,14 +996,16 @@ cudaError_t MGSolver::solve(bool x_is_zero, SolveResult &res) {
 cudaError_t MGSolver::solve64(bool x_is_zero, SolveResult &res) {
     const Dims &d = lev_dims_[0];
     const long long n = d.n;
-    const int rg = reduce_grid((long long)d.nx * d.ny);
+    int xpb;
+    const dim3 tg = tile_grid(d, xpb);
     cudaError_t e;
     if (x_is_zero) {
         cudaMemsetAsync(x_, 0, 8 * n, st_);
         k_cast_rhs<double><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, b_, r_, S_RR, S_BB, sc_, part_, ticket_);
     } else {
         // r = b - A x, (r,r), (b,b)
-        k_residual64<double><<<rg, dim3(32, 8), 0, st_>>>(d, c64_[0], x_, b_, r_, 0, S_RR, S_BB, sc_, part_, ticket_);
+        k_residual64<double><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c64_[0], x_, b_, r_, 0, S_RR, S_BB, sc_, part_,
+                                                          ticket_);
     }
     tk_.launches++;
     cudaMemsetAsync(p_, 0, 8 * n, st_);
@@ -1052,7 +1056,8 @@ cudaError_t MGSolver::solve64(bool x_is_zero, SolveResult &res) {
 cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
     const Dims &d = lev_dims_[0];
     const long long n = d.n;
-    const int rg = reduce_grid((long long)d.nx * d.ny);
+    int xpb;
+    const dim3 tg = tile_grid(d, xpb);
     cudaError_t e;
     if (x_is_zero) cudaMemsetAsync(x_, 0, 8 * n, st_);
     double bb = -1, rr = 0;
@@ -1065,8 +1070,8 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
             k_cast_rhs<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, b_, r32_, S_AUX1, S_BB, sc_, part_, ticket_);
             x_zero = false;
         } else {
-            k_residual64<float><<<rg, dim3(32, 8), 0, st_>>>(d, c64_[0], x_, b_, r32_, 0, S_AUX1, bb < 0 ? S_BB : -1,
-                                                             sc_, part_, ticket_);
+            k_residual64<float><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c64_[0], x_, b_, r32_, 0, S_AUX1,
+                                                             bb < 0 ? S_BB : -1, sc_, part_, ticket_);
         }
         tk_.launches++;
         if ((e = read_slots()) != cudaSuccess) return e;
@@ -1096,7 +1101,8 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
             cudaMemcpyAsync(sc_ + S_ALPHA, init + 1, 8 * 3, cudaMemcpyHostToDevice, st_);
         }
         int it = 0;
-        double rin = rr;
+        double rin = rr, rprev = rr;
+        int slow = 0;
         const int every = prm_.check_every > 0 ? prm_.check_every : 1;
         const int budget = prm_.max_iters - total_inner;
         while (it < budget) {
@@ -1106,6 +1112,10 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
             rin = sc_host_[S_RR];
             if (sc_host_[S_AUX0] != 0) break;
             if (rin <= in_tol2 || !std::isfinite(rin)) break;
+            // FP32 stagnation: two consecutive iterations reducing ||r|| by less than 2x -> refine in FP64
+            slow = (rin > 0.25 * rprev) ? slow + 1 : 0;
+            rprev = rin;
+            if (slow >= 2) break;
         }
         total_inner += it;
         k_ir_update<<<flat_grid(n), 256, 0, st_>>>(n, x_, d32_);
@@ -1126,8 +1136,9 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
 
 cudaError_t MGSolver::true_relres(bool skip0, double &relres, double &bnorm) {
     const Dims &d = lev_dims_[0];
-    const int rg = reduce_grid((long long)d.nx * d.ny);
-    k_residual64<double><<<rg, dim3(32, 8), 0, st_>>>(d, c64_[0], x_, b_, (double *)nullptr, skip0 ? 1 : 0,
+    int xpb;
+    const dim3 tg = tile_grid(d, xpb);
+    k_residual64<double><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c64_[0], x_, b_, (double *)nullptr, skip0 ? 1 : 0,
                                                       S_AUX1, S_AUX2, sc_, part_, ticket_);
     tk_.launches++;
     cudaError_t e = read_slots();

@@ -4,6 +4,7 @@
 // multiply-add), so the fine-level operator and right-hand side are bit-identical to the reference's CSR
 // assembly on the same inputs, and the velocity / field updates are too.
 #include <cmath>
+#include <cstring>
 
 #include "sf_ops.h"
 
@@ -153,10 +154,28 @@ __device__ __forceinline__ double mu_face(double philo, double phihi, double chi
     return 1. + (1. - heaviside(pf, bw)) * chi;
 }
 
+// Order-preserving integer key of a double (IEEE total order on finite values): comparisons of keys are
+// integer instructions, so faces far from the interface are classified without FP64 arithmetic.
+__device__ __forceinline__ long long okey(double v) {
+    const long long b = __double_as_longlong(v);
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+
+// mu_face with a fast path: when both cell values lie beyond +-bw (1 + 2^-40) the face value is beyond +-bw
+// too, so H is exactly 0 or 1 and mu is exactly 1 + chi (precomputed, same rounding) or 1.
+__device__ __forceinline__ double mu_face_fast(double philo, double phihi, double chi, double bw, long long khi,
+                                               long long klo, double one_plus_chi) {
+    const long long a = okey(philo), b = okey(phihi);
+    if (a > khi && b > khi) return 1.;
+    if (a < klo && b < klo) return one_plus_chi;
+    return mu_face(philo, phihi, chi, bw);
+}
+
 // BuildMatrix, coefficient pass (core/MagneticField.cpp:51-60): mu on the lower x/y/z face of every cell,
 // stored directly as the lower-face couplings ax/ay/az (0 on the grid boundary, where the reference's mu = 1
 // is never used).  Each face is evaluated once.
 __global__ void __launch_bounds__(256) k_magnetic_mu(Dims d, const double *__restrict__ phi, double chi, double bw,
+                                                     long long khi, long long klo, double one_plus_chi,
                                                      Coef<double> cf) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -164,9 +183,9 @@ __global__ void __launch_bounds__(256) k_magnetic_mu(Dims d, const double *__res
     if (k >= d.nz || j >= d.ny) return;
     const long long c = cid(d, i, j, k);
     const double pc = phi[c];
-    cf.ax[c] = i > 0 ? mu_face(phi[c - (long long)d.ny * d.nz], pc, chi, bw) : 0.0;
-    cf.ay[c] = j > 0 ? mu_face(phi[c - d.nz], pc, chi, bw) : 0.0;
-    cf.az[c] = k > 0 ? mu_face(phi[c - 1], pc, chi, bw) : 0.0;
+    cf.ax[c] = i > 0 ? mu_face_fast(phi[c - (long long)d.ny * d.nz], pc, chi, bw, khi, klo, one_plus_chi) : 0.0;
+    cf.ay[c] = j > 0 ? mu_face_fast(phi[c - d.nz], pc, chi, bw, khi, klo, one_plus_chi) : 0.0;
+    cf.az[c] = k > 0 ? mu_face_fast(phi[c - 1], pc, chi, bw, khi, klo, one_plus_chi) : 0.0;
 }
 
 // BuildMatrix, row pass + AssembleRHS (core/MagneticField.cpp:62-118) in Neumann form: D = sum of mu over the
@@ -259,7 +278,15 @@ void launch_gather_cells(cudaStream_t st, long long n, const double *D, const do
 
 int launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, double chi, double bw,
                           const Faces &hext, double h, Coef<double> &cf, double *b, bool want_invd) {
-    k_magnetic_mu<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, chi, bw, cf);
+    // band thresholds as integer keys: |phi| > bw (1 + 2^-40) on both cells implies |phi_face| > bw exactly
+    const double t = bw * (1.0 + std::ldexp(1.0, -40));
+    auto key = [](double v) {
+        long long b;
+        std::memcpy(&b, &v, 8);
+        return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+    };
+    const double one_plus_chi = 1. + (1. - 0.) * chi;  // the reference's expression with H = 0
+    k_magnetic_mu<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, chi, bw, key(t), key(-t), one_plus_chi, cf);
     k_magnetic_rows<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, hext, h, cf, b, want_invd ? 1 : 0);
     return 2;
 }

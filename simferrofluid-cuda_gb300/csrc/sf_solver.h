@@ -26,7 +26,7 @@ struct SolverParams {
     double inner_tol = 1e-4;
     bool flexible = false;  // Polak-Ribiere beta (needed when the preconditioner is not a fixed SPD operator)
     bool profile = false;   // time finest-level smoother launches with events (no graphs)
-    int smoother = 0;       // 0: fused one-pass red-black sweep, 1: two in-place colour kernels
+    int smoother = 0;       // 0: two in-place colour kernels, 1: fused one-pass red-black sweep
 };
 
 // Counts kernel launches and, when profiling, brackets finest-level smoother launches with events.
@@ -153,8 +153,9 @@ class MGSolver {
     cudaError_t read_slots();
 };
 
-// Launch helpers shared with sf_ops.cu
-int reduce_grid(long long n);
+// Launch helpers
 constexpr int kMaxRedBlocks = 152 * 8;
+constexpr int kMaxTileBlocks = 16384;
+dim3 tile_grid(const Dims &d, int &xpb);
 
 }  // namespace sf
