@@ -43,8 +43,10 @@ typedef enum {
 } sf_status;
 
 typedef enum {
-    SF_PREC_FP64 = 0,  /* plain method: FP64 MGPCG */
-    SF_PREC_MIXED = 1  /* FP32 V-cycle, FP16 coarse coefficients, inner FP32 FCG, FP64 iterative refinement */
+    SF_PREC_FP64 = 0,   /* plain method: FP64 MGPCG */
+    SF_PREC_MIXED = 1,  /* FP32 V-cycle, FP16 coarse coefficients, inner FP32 FCG, FP64 iterative refinement */
+    SF_PREC_LEARNED = 2 /* mixed form started from the attached U-Net's scaled prediction (sf_set_network);
+                           a prediction worse than zero is discarded (SF_STALLED_FALLBACK) */
 } sf_precision;
 
 /* Cell grid of a staggered grid: resolution, spacing and corner (StaggeredGrid ctor,
@@ -90,7 +92,7 @@ typedef struct {
     double smooth_ms;        /* profile: their summed device time */
     long long kernel_launches; /* kernels this call launched (graph nodes counted per replay) */
     double smooth_bytes;     /* profile: algorithmic bytes of the timed smoother launches */
-    int reserved[2];
+    double guess_rel_residual; /* learned form: ||b - A x0|| / ||b|| of the network's initial guess (-1: none) */
 } sf_solve_stats;
 
 /* ----- context ------------------------------------------------------------------------------------------- */
@@ -169,6 +171,28 @@ SF_EXPORT sf_status sf_magnetic_solve_dev(void *ctx, const sf_grid *g, const dou
 SF_EXPORT sf_status sf_collider_box_fractions(const sf_grid *g, int boundary_width, double *const frac_out[3],
                                               double *node_ls_out);
 SF_EXPORT sf_status sf_collider_face_fractions(const sf_grid *g, const double *node_ls, double *const frac_out[3]);
+
+/* ----- learned form: the 3D U-Net (no counterpart in the reference) --------------------------------------
+ * 4 levels, 16/32/64/64 channels, 3x3x3 convolutions, BF16 weights and activations, FP32 accumulation on the
+ * tensor cores.  Input: 16 feature channels per cell (BF16, channels last); output: one FP32 value per cell.
+ * Parameters: a flat FP32 vector, layer by layer, weights [tap][cout][cin] then bias [cout].  All pointers in
+ * the _dev calls are device pointers on the context's device. */
+SF_EXPORT sf_status sf_unet_create(void *ctx, void **net_out);
+SF_EXPORT void sf_unet_destroy(void *net);
+SF_EXPORT long long sf_unet_num_params(void *net);
+SF_EXPORT sf_status sf_unet_set_params(void *net, const float *host_params, long long n);
+SF_EXPORT sf_status sf_unet_get_params(void *net, float *host_params, long long n);
+SF_EXPORT sf_status sf_unet_forward_dev(void *net, const sf_grid *g, const void *features_bf16, float *out);
+/* gradients of sum(dout * net(features)) w.r.t. the parameters, copied to grads_host (nullable) */
+SF_EXPORT sf_status sf_unet_backward_dev(void *net, const sf_grid *g, const void *features_bf16, const float *dout,
+                                         float *grads_host);
+/* one Adam step (lr) on the scale-invariant loss 1 - (o.t)^2 / (|o|^2 |t|^2); *loss receives the loss */
+SF_EXPORT sf_status sf_unet_train_step_dev(void *net, const sf_grid *g, const void *features_bf16,
+                                           const float *target, float lr, double *loss);
+/* attach (or detach with NULL) the network used by SF_PREC_LEARNED solves on this context */
+SF_EXPORT sf_status sf_set_network(void *ctx, void *net);
+/* features of the last assembled pressure (which = 0) or potential (1) system and its solution (FP32) */
+SF_EXPORT sf_status sf_system_features_dev(void *ctx, int which, void *features_bf16, float *solution);
 
 /* Forget the magnetic warm start (MagneticField ctor zeroes m_Sol, core/MagneticField.cpp:26). */
 SF_EXPORT sf_status sf_magnetic_reset(void *ctx);

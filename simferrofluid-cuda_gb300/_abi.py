@@ -21,12 +21,16 @@ SF_NOT_READY = 7
 
 SF_PREC_FP64 = 0
 SF_PREC_MIXED = 1
+SF_PREC_LEARNED = 2
 
 EXPORTED = [
     "sf_create", "sf_destroy", "sf_status_string", "sf_last_error", "sf_abi_version", "sf_default_opts",
     "sf_device_bytes", "sf_pressure_project", "sf_pressure_project_dev", "sf_pressure_reproject",
     "sf_pressure_reproject_dev", "sf_magnetic_solve", "sf_magnetic_solve_dev", "sf_magnetic_reset",
     "sf_collider_box_fractions", "sf_collider_face_fractions",
+    "sf_unet_create", "sf_unet_destroy", "sf_unet_num_params", "sf_unet_set_params", "sf_unet_get_params",
+    "sf_unet_forward_dev", "sf_unet_backward_dev", "sf_unet_train_step_dev", "sf_set_network",
+    "sf_system_features_dev",
 ]
 
 
@@ -48,7 +52,8 @@ class sf_solve_stats(C.Structure):
                 ("ms_build", C.c_double), ("ms_solve", C.c_double), ("ms_post", C.c_double),
                 ("ms_total", C.c_double), ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong),
                 ("status_detail", C.c_int), ("smooth_launches", C.c_int), ("smooth_ms", C.c_double),
-                ("kernel_launches", C.c_longlong), ("smooth_bytes", C.c_double), ("reserved", C.c_int * 2)]
+                ("kernel_launches", C.c_longlong), ("smooth_bytes", C.c_double),
+                ("guess_rel_residual", C.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
@@ -99,6 +104,26 @@ def load(path: str | None = None):
     L.sf_collider_box_fractions.restype = C.c_int
     L.sf_collider_face_fractions.argtypes = [G, V, _P3]
     L.sf_collider_face_fractions.restype = C.c_int
+    L.sf_unet_create.argtypes = [V, C.POINTER(V)]
+    L.sf_unet_create.restype = C.c_int
+    L.sf_unet_destroy.argtypes = [V]
+    L.sf_unet_destroy.restype = None
+    L.sf_unet_num_params.argtypes = [V]
+    L.sf_unet_num_params.restype = C.c_longlong
+    L.sf_unet_set_params.argtypes = [V, V, C.c_longlong]
+    L.sf_unet_set_params.restype = C.c_int
+    L.sf_unet_get_params.argtypes = [V, V, C.c_longlong]
+    L.sf_unet_get_params.restype = C.c_int
+    L.sf_unet_forward_dev.argtypes = [V, G, V, V]
+    L.sf_unet_forward_dev.restype = C.c_int
+    L.sf_unet_backward_dev.argtypes = [V, G, V, V, V]
+    L.sf_unet_backward_dev.restype = C.c_int
+    L.sf_unet_train_step_dev.argtypes = [V, G, V, V, C.c_float, C.POINTER(C.c_double)]
+    L.sf_unet_train_step_dev.restype = C.c_int
+    L.sf_set_network.argtypes = [V, V]
+    L.sf_set_network.restype = C.c_int
+    L.sf_system_features_dev.argtypes = [V, C.c_int, V, V]
+    L.sf_system_features_dev.restype = C.c_int
     _lib = L
     return L
 

@@ -25,6 +25,7 @@ UNITS = {
     "sf_mg.cu": [],
     "sf_api.cu": [],
     "sf_collider.cu": ["-Xcompiler", "-ffp-contract=off"],
+    "sf_unet.cu": [],
 }
 
 

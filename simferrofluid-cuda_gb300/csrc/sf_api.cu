@@ -8,6 +8,7 @@
 
 #include "sf_ops.h"
 #include "sf_solver.h"
+#include "sf_unet.h"
 #include "sfgpu.h"
 
 using namespace sf;
@@ -27,6 +28,9 @@ struct Ctx {
     Dims mag_dims{0, 0, 0, 0};
     // staging buffers for the host-pointer entry points
     DevBuf phi, frac[3], vel[3], us[3], jump[3], hext[3], H[3], cells;
+    // learned form: attached network (not owned) and its buffers
+    UNet *net = nullptr;
+    DevBuf feat, guess;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
@@ -62,7 +66,7 @@ SolverParams params_from(const sf_solve_opts *o, int which) {
     sf_default_opts(&def, which);
     if (!o) o = &def;
     SolverParams p;
-    p.precision = o->precision;
+    p.precision = o->precision == SF_PREC_FP64 ? 0 : 1;  // the learned form runs the mixed solver
     p.tol = o->tol > 0 ? o->tol : def.tol;
     p.max_iters = o->max_iters > 0 ? o->max_iters : def.max_iters;
     p.pre = o->pre_smooth > 0 ? o->pre_smooth : def.pre_smooth;
@@ -81,7 +85,7 @@ SolverParams params_from(const sf_solve_opts *o, int which) {
 
 bool opts_ok(const sf_solve_opts *o) {
     if (!o) return true;
-    if (o->precision != SF_PREC_FP64 && o->precision != SF_PREC_MIXED) return false;
+    if (o->precision != SF_PREC_FP64 && o->precision != SF_PREC_MIXED && o->precision != SF_PREC_LEARNED) return false;
     if (o->max_levels < 0 || o->coarse_dim < 0) return false;
     if (o->smoother != 0 && o->smoother != 1) return false;
     return true;
@@ -114,12 +118,28 @@ void fill_stats(sf_solve_stats *s, const SolveResult &r, long long unknowns) {
     s->smooth_launches = r.smooth_launches;
     s->smooth_ms = r.smooth_ms;
     s->smooth_bytes = r.smooth_bytes;
+    s->guess_rel_residual = r.guess_relres;
 }
 
 float ev_ms(cudaEvent_t a, cudaEvent_t b) {
     float ms = 0;
     cudaEventElapsedTime(&ms, a, b);
     return ms;
+}
+
+// Learned initial guess: network features of the assembled system -> U-Net -> x0 = gamma y on the solver.
+sf_status learned_guess(Ctx *c, MGSolver &S, const Dims &d, SolveResult &pre) {
+    if (!c->net) return fail(c, SF_NOT_READY, "learned precision needs a network (sf_set_network)");
+    CK(c->feat.ensure(2 * 16 * (size_t)d.n));
+    CK(c->guess.ensure(4 * (size_t)d.n));
+    auto *feat = (__nv_bfloat16 *)c->feat.get();
+    auto *y = (float *)c->guess.get();
+    CK(c->net->features(d, S.fine(), S.b(), feat));
+    CK(c->net->forward(d, feat, y));
+    double gamma = 0;
+    CK(S.set_guess_scaled(y, gamma));
+    (void)pre;
+    return SF_OK;
 }
 
 // ------------------------------------------------------------------------------------------------ pressure
@@ -168,8 +188,13 @@ sf_status pressure_impl(Ctx *c, const sf_grid *g, double *const vel[3], const do
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->ev[1], c->st));
     SolveResult res;
-    // Project starts from zero (core/Pressure.cpp:122); Reproject from the last pressure (:33)
-    CK(S.solve(!reproject, res));
+    bool zero = !reproject;  // Project starts from zero (core/Pressure.cpp:122); Reproject from the last pressure
+    if (opts && opts->precision == SF_PREC_LEARNED && !reproject) {
+        sf_status ls = learned_guess(c, S, d, res);
+        if (ls != SF_OK) return ls;
+        zero = false;
+    }
+    CK(S.solve(zero, res));
     double relres = res.relres, bn = res.bnorm;
     const bool report = !opts || opts->report_ref_residual;
     if (report) CK(S.true_relres(false, relres, bn));
@@ -215,7 +240,8 @@ sf_status pressure_impl(Ctx *c, const sf_grid *g, double *const vel[3], const do
         stats->d2h_bytes = d2h;
         stats->status_detail = res.breakdown ? 1 : 0;
     }
-    return res.converged ? SF_OK : fail(c, SF_NOT_CONVERGED, "pressure solve did not reach the tolerance");
+    if (!res.converged) return fail(c, SF_NOT_CONVERGED, "pressure solve did not reach the tolerance");
+    return res.fallback ? SF_STALLED_FALLBACK : SF_OK;
 }
 
 // ------------------------------------------------------------------------------------------------ magnetic
@@ -253,7 +279,13 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->ev[1], c->st));
     SolveResult res;
-    CK(S.solve(!warm, res));
+    bool zero = !warm;
+    if (opts && opts->precision == SF_PREC_LEARNED) {
+        sf_status ls = learned_guess(c, S, d, res);
+        if (ls != SF_OK) return ls;
+        zero = false;
+    }
+    CK(S.solve(zero, res));
     CK(S.shift_to_zero_at_origin());
     double relres = res.relres, relref = res.relres, bn = res.bnorm;
     const bool report = !opts || opts->report_ref_residual;
@@ -306,7 +338,8 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
         stats->d2h_bytes = d2h;
         stats->status_detail = res.breakdown ? 1 : 0;
     }
-    return res.converged ? SF_OK : fail(c, SF_NOT_CONVERGED, "magnetic solve did not reach the tolerance");
+    if (!res.converged) return fail(c, SF_NOT_CONVERGED, "magnetic solve did not reach the tolerance");
+    return res.fallback ? SF_STALLED_FALLBACK : SF_OK;
 }
 
 }  // namespace
@@ -442,6 +475,102 @@ sf_status sf_magnetic_reset(void *ctx) {
     Ctx *c = C(ctx);
     if (!c) return SF_BAD_ARG;
     c->mag_has_x = false;
+    return SF_OK;
+}
+
+// ----- learned form ------------------------------------------------------------------------------------------
+struct NetHandle {
+    Ctx *ctx;
+    std::unique_ptr<UNet> net;
+};
+
+sf_status sf_unet_create(void *ctx, void **out) {
+    Ctx *c = C(ctx);
+    if (!c || !out) return SF_BAD_ARG;
+    CK(cudaSetDevice(c->device));
+    auto *h = new NetHandle{c, std::make_unique<UNet>(c->st)};
+    if (!h->net->last_error.empty()) {
+        std::string m = h->net->last_error;
+        delete h;
+        return fail(c, SF_OUT_OF_MEMORY, m);
+    }
+    *out = h;
+    return SF_OK;
+}
+void sf_unet_destroy(void *net) {
+    auto *h = reinterpret_cast<NetHandle *>(net);
+    if (!h) return;
+    if (h->ctx->net == h->net.get()) h->ctx->net = nullptr;
+    cudaStreamSynchronize(h->ctx->st);
+    delete h;
+}
+long long sf_unet_num_params(void *net) {
+    auto *h = reinterpret_cast<NetHandle *>(net);
+    return h ? h->net->num_params() : 0;
+}
+sf_status sf_unet_set_params(void *net, const float *host, long long n) {
+    auto *h = reinterpret_cast<NetHandle *>(net);
+    if (!h || !host || n != h->net->num_params()) return SF_BAD_ARG;
+    Ctx *c = h->ctx;
+    CK(h->net->set_params(host));
+    return SF_OK;
+}
+sf_status sf_unet_get_params(void *net, float *host, long long n) {
+    auto *h = reinterpret_cast<NetHandle *>(net);
+    if (!h || !host || n != h->net->num_params()) return SF_BAD_ARG;
+    Ctx *c = h->ctx;
+    CK(h->net->get_params(host));
+    return SF_OK;
+}
+sf_status sf_unet_forward_dev(void *net, const sf_grid *g, const void *features, float *out) {
+    auto *h = reinterpret_cast<NetHandle *>(net);
+    if (!h || !grid_ok(g) || !features || !out) return SF_BAD_ARG;
+    Ctx *c = h->ctx;
+    CK(h->net->forward(make_dims(g->nx, g->ny, g->nz), (const __nv_bfloat16 *)features, out));
+    CK(cudaStreamSynchronize(c->st));
+    return SF_OK;
+}
+sf_status sf_unet_backward_dev(void *net, const sf_grid *g, const void *features, const float *dout, float *grads) {
+    auto *h = reinterpret_cast<NetHandle *>(net);
+    if (!h || !grid_ok(g) || !features || !dout) return SF_BAD_ARG;
+    Ctx *c = h->ctx;
+    const Dims d = make_dims(g->nx, g->ny, g->nz);
+    CK(h->net->forward(d, (const __nv_bfloat16 *)features, nullptr));
+    CK(h->net->backward(d, dout));
+    if (grads) CK(h->net->get_grads(grads));
+    CK(cudaStreamSynchronize(c->st));
+    return SF_OK;
+}
+sf_status sf_unet_train_step_dev(void *net, const sf_grid *g, const void *features, const float *target, float lr,
+                                 double *loss) {
+    auto *h = reinterpret_cast<NetHandle *>(net);
+    if (!h || !grid_ok(g) || !features || !target || !(lr > 0)) return SF_BAD_ARG;
+    Ctx *c = h->ctx;
+    double l = 0;
+    CK(h->net->train_step(make_dims(g->nx, g->ny, g->nz), (const __nv_bfloat16 *)features, target, lr, l));
+    if (loss) *loss = l;
+    return SF_OK;
+}
+sf_status sf_set_network(void *ctx, void *net) {
+    Ctx *c = C(ctx);
+    if (!c) return SF_BAD_ARG;
+    auto *h = reinterpret_cast<NetHandle *>(net);
+    if (h && h->ctx != c) return fail(c, SF_BAD_ARG, "network belongs to another context");
+    c->net = h ? h->net.get() : nullptr;
+    return SF_OK;
+}
+sf_status sf_system_features_dev(void *ctx, int which, void *features, float *solution) {
+    Ctx *c = C(ctx);
+    if (!c || (which != 0 && which != 1)) return SF_BAD_ARG;
+    MGSolver *S = which == 0 ? c->pres.get() : c->mag.get();
+    if (!S || (which == 0 && !c->pres_ready) || (which == 1 && !c->mag_has_x))
+        return fail(c, SF_NOT_READY, "no assembled system of that kind on this context");
+    if (!c->net) return fail(c, SF_NOT_READY, "features need a network (sf_set_network)");
+    const Dims d = S->dims();
+    if (features) CK(c->net->features(d, S->fine(), S->b(), (__nv_bfloat16 *)features));
+    if (solution) launch_to_f32(c->st, d.n, S->x(), solution);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->st));
     return SF_OK;
 }
 

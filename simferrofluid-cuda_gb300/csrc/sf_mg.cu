@@ -599,6 +599,23 @@ __global__ void __launch_bounds__(256) k_cast_rhs(long long n, const double *__r
     }
 }
 
+// (y, b) with y FP32 and b FP64 -> slot
+__global__ void __launch_bounds__(256) k_dot_fd(long long n, const float *__restrict__ y, const double *__restrict__ b,
+                                                int slot, double *sc, double *part, unsigned *ticket) {
+    double v[1] = {0};
+    float acc = 0.f;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) acc += y[c] * (float)b[c];
+    v[0] = acc;
+    double tot[1];
+    if (grid_reduce<1>(v, part, ticket, tot)) sc[slot] = tot[0];
+}
+
+__global__ void k_scale_to64(long long n, double g, const float *__restrict__ y, double *__restrict__ x) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        x[c] = g * (double)y[c];
+}
+
 // x64 += d32
 __global__ void k_ir_update(long long n, double *__restrict__ x, const float *__restrict__ dlt) {
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
@@ -981,6 +998,7 @@ cudaError_t MGSolver::read_slots() {
 
 cudaError_t MGSolver::solve(bool x_is_zero, SolveResult &res) {
     res = SolveResult{};
+    if (x_is_zero) guess_ = false;
     res.levels = (int)lev_dims_.size();
     tk_.prof = prm_.profile;
     cudaError_t e = prm_.precision == 0 ? solve64(x_is_zero, res) : solve_mixed(x_is_zero, res);
@@ -1085,6 +1103,18 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
                 return cudaStreamSynchronize(st_);
             }
         }
+        if (guess_) {
+            // a supplied initial guess that is worse than zero (or not finite) is discarded
+            guess_ = false;
+            res.guess_relres = std::sqrt(rr / bb);
+            if (!(rr <= bb)) {
+                res.fallback = true;
+                cudaMemsetAsync(x_, 0, 8 * n, st_);
+                x_zero = true;
+                bb = -1;
+                continue;
+            }
+        }
         const double rel = std::sqrt(rr / bb);
         if (rel <= prm_.tol || !std::isfinite(rr) || outer >= max_outer || total_inner >= prm_.max_iters) break;
         // inner FCG on A32 d = r32, d = 0
@@ -1131,6 +1161,25 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
     res.outer = outer;
     res.relres = std::sqrt(rr / bb);
     res.converged = res.relres <= prm_.tol;
+    return cudaGetLastError();
+}
+
+cudaError_t MGSolver::set_guess_scaled(const float *y, double &gamma) {
+    if (prm_.precision != 1) return cudaErrorInvalidValue;
+    const Dims &d = lev_dims_[0];
+    int xpb;
+    const dim3 tg = tile_grid(d, xpb);
+    // (y, A y) on the FP32 level-0 operator and (y, b); gamma minimises the A-norm error along y
+    k_apply_dot<float, float><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c32_, y, q32_, sc_, part_, ticket_);
+    k_dot_fd<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(d.n, y, b_, S_AUX2, sc_, part_, ticket_);
+    tk_.launches += 2;
+    cudaError_t e = read_slots();
+    if (e != cudaSuccess) return e;
+    const double yay = sc_host_[S_PQ], yb = sc_host_[S_AUX2];
+    gamma = (yay > 0 && std::isfinite(yay) && std::isfinite(yb)) ? yb / yay : 0.0;
+    k_scale_to64<<<flat_grid(d.n), 256, 0, st_>>>(d.n, gamma, y, x_);
+    tk_.launches++;
+    guess_ = true;
     return cudaGetLastError();
 }
 

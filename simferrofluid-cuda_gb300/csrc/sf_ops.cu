@@ -298,6 +298,15 @@ void launch_total_field(cudaStream_t st, const Dims &d, const double *psi, const
             d, a, psi, hext, invh, const_cast<double *>(H.p[a]));
 }
 
+__global__ void k_to_f32(long long n, const double *__restrict__ a, float *__restrict__ o) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        o[c] = (float)a[c];
+}
+
+void launch_to_f32(cudaStream_t st, long long n, const double *a, float *o) {
+    k_to_f32<<<flat_grid(n), 256, 0, st>>>(n, a, o);
+}
+
 void launch_copy(cudaStream_t st, long long n, const double *a, double *o) {
     k_copy<<<flat_grid(n), 256, 0, st>>>(n, a, o);
 }

@@ -22,5 +22,6 @@ int launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, dou
 void launch_total_field(cudaStream_t st, const Dims &d, const double *psi, const Faces &hext, double invh,
                         const Faces &H);
 void launch_copy(cudaStream_t st, long long n, const double *a, double *o);
+void launch_to_f32(cudaStream_t st, long long n, const double *a, float *o);
 
 }  // namespace sf

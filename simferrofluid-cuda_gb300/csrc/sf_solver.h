@@ -51,6 +51,8 @@ struct SolveResult {
     int iters = 0, outer = 0, levels = 0;
     bool converged = false;
     bool breakdown = false;
+    bool fallback = false;      // the supplied initial guess was discarded
+    double guess_relres = -1;   // relative residual of the supplied initial guess
     double relres = 0, bnorm = 0;
 };
 
@@ -95,6 +97,10 @@ class MGSolver {
     // ||b - A x|| / ||b|| on the fine FP64 operator; with skip0 row 0 is left out of both norms.
     cudaError_t true_relres(bool skip0, double &relres, double &bnorm);
 
+    // Initial guess x = gamma y, gamma = (y, b) / (y, A y) (mixed form); the next solve(false) starts from it
+    // and discards it if its residual exceeds ||b||.
+    cudaError_t set_guess_scaled(const float *y, double &gamma);
+
     // Shift x so that x[0] == 0 (potential gauge).
     cudaError_t shift_to_zero_at_origin();
 
@@ -116,6 +122,7 @@ class MGSolver {
     std::vector<std::unique_ptr<DevBuf>> bufs_;
     size_t bytes_ = 0;
     bool configured_ = false;
+    bool guess_ = false;
     Dims cfg_dims_{0, 0, 0, 0};
     int cfg_prec_ = -1, cfg_levels_ = -1, cfg_cdim_ = -1;
 

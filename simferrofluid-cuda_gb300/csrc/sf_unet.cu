@@ -1,0 +1,377 @@
+// sf_unet.cu -- host side of the learned solver's U-Net: parameters, workspaces, forward, backward, Adam.
+#include <cmath>
+#include <cstring>
+
+#include "sf_unet.h"
+#include "sf_unet_kernels.cuh"
+
+namespace sf {
+
+namespace {
+constexpr int kVchunkMin = 512;
+
+int flat_blocks(long long n) {
+    long long g = (n + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    return (int)(g < 1 ? 1 : g);
+}
+
+// cosine-loss dot products (o.t, o.o, t.t) with the deterministic grid reduction
+__global__ void __launch_bounds__(256) k_cos_dots(long long n, const float *__restrict__ o, const float *__restrict__ t,
+                                                  double *out, double *part, unsigned *ticket) {
+    float a0 = 0, a1 = 0, a2 = 0;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
+        const float oc = o[c], tc = t[c];
+        a0 += oc * tc;
+        a1 += oc * oc;
+        a2 += tc * tc;
+    }
+    double v[3] = {a0, a1, a2}, tot[3];
+    if (grid_reduce<3>(v, part, ticket, tot)) {
+        out[0] = tot[0];
+        out[1] = tot[1];
+        out[2] = tot[2];
+    }
+}
+
+// d/do of 1 - (o.t)^2 / (|o|^2 |t|^2)
+__global__ void k_cos_grad(long long n, const float *__restrict__ o, const float *__restrict__ t, const double *dots,
+                           float *__restrict__ g) {
+    const double ot = dots[0], oo = dots[1], tt = dots[2];
+    const float ct = (float)(-2.0 * ot / (oo * tt));
+    const float co = (float)(2.0 * ot * ot / (oo * oo * tt));
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        g[c] = ct * t[c] + co * o[c];
+}
+
+template <int CI, int CO>
+void launch_conv(cudaStream_t st, int epi, const Dims &d, const bf16 *x, const bf16 *w, const float *b, void *y,
+                 int taps) {
+    const int blocks = (int)((d.n + 127) / 128);
+    if (epi == 0)
+        k_conv_mma<CI, CO, 0><<<blocks, 128, 0, st>>>(d, x, w, b, y, taps);
+    else
+        k_conv_mma<CI, CO, 1><<<blocks, 128, 0, st>>>(d, x, w, b, y, taps);
+}
+
+void conv_dispatch(cudaStream_t st, int ci, int co, int epi, const Dims &d, const bf16 *x, const bf16 *w,
+                   const float *b, void *y, int taps) {
+#define CASE(A, B)                                                  \
+    if (ci == A && co == B) {                                       \
+        launch_conv<A, B>(st, epi, d, x, w, b, y, taps);            \
+        return;                                                     \
+    }
+    CASE(16, 16) CASE(16, 32) CASE(32, 16) CASE(32, 32) CASE(32, 64) CASE(64, 32) CASE(64, 64)
+#undef CASE
+}
+
+template <int CI, int CO>
+void launch_wgrad(cudaStream_t st, const Dims &d, const bf16 *dy, const bf16 *x, float *part, int taps, int vchunk,
+                  int chunks) {
+    k_wgrad_mma<CI, CO><<<dim3(chunks, taps), 128, 0, st>>>(d, dy, x, part, taps, vchunk);
+}
+
+void wgrad_dispatch(cudaStream_t st, int ci, int co, const Dims &d, const bf16 *dy, const bf16 *x, float *part,
+                    int taps, int vchunk, int chunks) {
+#define CASE(A, B)                                                          \
+    if (ci == A && co == B) {                                               \
+        launch_wgrad<A, B>(st, d, dy, x, part, taps, vchunk, chunks);       \
+        return;                                                             \
+    }
+    CASE(16, 16) CASE(16, 32) CASE(32, 16) CASE(32, 32) CASE(32, 64) CASE(64, 32) CASE(64, 64)
+#undef CASE
+}
+}  // namespace
+
+UNet::UNet(cudaStream_t st) : st_(st) {
+    struct S {
+        int ci, co, lv, taps;
+    };
+    const S spec[] = {{16, 16, 0, 27}, {16, 16, 0, 27}, {16, 32, 1, 27}, {32, 32, 1, 27}, {32, 64, 2, 27},
+                      {64, 64, 2, 27}, {64, 64, 3, 27}, {64, 64, 3, 27}, {64, 64, 2, 27}, {64, 32, 2, 27},
+                      {32, 32, 1, 27}, {32, 16, 1, 27}, {16, 16, 0, 27}, {16, 16, 0, 27}, {16, 1, 0, 1}};
+    long long off = 0, boff = 0;
+    for (const S &s : spec) {
+        ConvLayer L{s.ci, s.co, s.lv, s.taps, off, off + (long long)s.taps * s.co * s.ci, boff};
+        off = L.boff + s.co;
+        boff += (long long)s.taps * s.co * s.ci;
+        layers_.push_back(L);
+    }
+    nparams_ = off;
+    nbf_ = boff;
+    p_ = (float *)alloc(4 * nparams_);
+    g_ = (float *)alloc(4 * nparams_);
+    m1_ = (float *)alloc(4 * nparams_);
+    m2_ = (float *)alloc(4 * nparams_);
+    wb_ = (bf16 *)alloc(2 * nbf_);
+    wt_ = (bf16 *)alloc(2 * nbf_);
+    dots_ = (double *)alloc(8 * 8);
+    redpart_ = (double *)alloc(8 * 4 * 1216);
+    wpart_elems_ = 64LL * 27 * 64 * 64;
+    wpart_ = (float *)alloc(4 * wpart_elems_);
+    hpart_ = (float *)alloc(4 * 4096 * 17);
+    cudaMallocHost(&dots_host_, 8 * 8);
+    if (p_) {
+        cudaMemsetAsync(p_, 0, 4 * nparams_, st_);
+        cudaMemsetAsync(m1_, 0, 4 * nparams_, st_);
+        cudaMemsetAsync(m2_, 0, 4 * nparams_, st_);
+        cudaMemsetAsync(dots_, 0, 64, st_);
+    }
+}
+
+UNet::~UNet() {
+    for (void *p : ws_) cudaFree(p);
+    for (void *p : persist_) cudaFree(p);
+    if (dots_host_) cudaFreeHost(dots_host_);
+}
+
+void *UNet::alloc(size_t bytes) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes ? bytes : 256) != cudaSuccess) {
+        last_error = "device allocation failed";
+        return nullptr;
+    }
+    persist_.push_back(p);
+    return p;
+}
+
+void UNet::refresh_bf16() {
+    for (const ConvLayer &L : layers_) {
+        if (L.taps != 27) continue;
+        const long long m = (long long)L.taps * L.cout * L.cin;
+        k_f32_to_bf16<<<flat_blocks(m), 256, 0, st_>>>(m, p_ + L.woff, wb_ + L.wbf);
+        k_flip_weights<<<flat_blocks(m), 256, 0, st_>>>(L.taps, L.cout, L.cin, p_ + L.woff, wt_ + L.wbf);
+    }
+}
+
+cudaError_t UNet::set_params(const float *host) {
+    cudaError_t e = cudaMemcpyAsync(p_, host, 4 * nparams_, cudaMemcpyHostToDevice, st_);
+    if (e != cudaSuccess) return e;
+    refresh_bf16();
+    cudaMemsetAsync(m1_, 0, 4 * nparams_, st_);
+    cudaMemsetAsync(m2_, 0, 4 * nparams_, st_);
+    step_ = 0;
+    return cudaStreamSynchronize(st_);
+}
+
+cudaError_t UNet::get_params(float *host) {
+    cudaError_t e = cudaMemcpyAsync(host, p_, 4 * nparams_, cudaMemcpyDeviceToHost, st_);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(st_);
+}
+
+cudaError_t UNet::get_grads(float *host) {
+    cudaError_t e = cudaMemcpyAsync(host, g_, 4 * nparams_, cudaMemcpyDeviceToHost, st_);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(st_);
+}
+
+cudaError_t UNet::ensure(const Dims &d) {
+    if (have_ws_ && dims_[0].nx == d.nx && dims_[0].ny == d.ny && dims_[0].nz == d.nz) return cudaSuccess;
+    for (void *p : ws_) cudaFree(p);
+    ws_.clear();
+    have_ws_ = false;
+    dims_[0] = d;
+    for (int l = 1; l < 4; l++)
+        dims_[l] = make_dims((dims_[l - 1].nx + 1) / 2, (dims_[l - 1].ny + 1) / 2, (dims_[l - 1].nz + 1) / 2);
+    bool ok = true;
+    auto A = [&](size_t bytes) -> void * {
+        void *p = nullptr;
+        if (cudaMalloc(&p, bytes ? bytes : 256) != cudaSuccess) {
+            ok = false;
+            return nullptr;
+        }
+        ws_.push_back(p);
+        return p;
+    };
+    const long long n0 = dims_[0].n, n1 = dims_[1].n, n2 = dims_[2].n, n3 = dims_[3].n;
+    auto B = [&](long long n, int c) { return (bf16 *)A(2 * (size_t)n * c); };
+    A0a = B(n0, 16); S0 = B(n0, 16); U0 = B(n0, 16); D0a = B(n0, 16); D0b = B(n0, 16);
+    P1 = B(n1, 16); A1a = B(n1, 32); S1 = B(n1, 32); U1 = B(n1, 32); D1a = B(n1, 32); D1b = B(n1, 16);
+    P2 = B(n2, 32); A2a = B(n2, 64); S2 = B(n2, 64); U2 = B(n2, 64); D2a = B(n2, 64); D2b = B(n2, 32);
+    P3 = B(n3, 64); A3a = B(n3, 64); A3b = B(n3, 64);
+    const int cmax[4] = {16, 32, 64, 64};
+    const long long nl[4] = {n0, n1, n2, n3};
+    for (int l = 0; l < 4; l++) {
+        gA[l] = (float *)A(4 * (size_t)nl[l] * cmax[l]);
+        gB[l] = (float *)A(4 * (size_t)nl[l] * cmax[l]);
+        gbf[l] = B(nl[l], cmax[l]);
+        if (l < 3) gU[l] = (float *)A(4 * (size_t)nl[l] * cmax[l]);
+    }
+    out_ = (float *)A(4 * (size_t)n0);
+    dout_ = (float *)A(4 * (size_t)n0);
+    if (!ok) {
+        last_error = "U-Net workspace allocation failed";
+        return cudaErrorMemoryAllocation;
+    }
+    have_ws_ = true;
+    return cudaSuccess;
+}
+
+void UNet::conv_fwd(const ConvLayer &L, const Dims &d, const bf16 *x, bf16 *y) {
+    conv_dispatch(st_, L.cin, L.cout, 0, d, x, wb_ + L.wbf, p_ + L.boff, y, L.taps);
+}
+
+cudaError_t UNet::forward(const Dims &d, const bf16 *feat, float *out) {
+    cudaError_t e = ensure(d);
+    if (e != cudaSuccess) return e;
+    feat_ = feat;
+    const ConvLayer *Ls = layers_.data();
+    const Dims &d0 = dims_[0], &d1 = dims_[1], &d2 = dims_[2], &d3 = dims_[3];
+    conv_fwd(Ls[0], d0, feat, A0a);
+    conv_fwd(Ls[1], d0, A0a, S0);
+    k_pool<<<flat_blocks(d1.n * 16), 256, 0, st_>>>(d0, d1, 16, S0, P1);
+    conv_fwd(Ls[2], d1, P1, A1a);
+    conv_fwd(Ls[3], d1, A1a, S1);
+    k_pool<<<flat_blocks(d2.n * 32), 256, 0, st_>>>(d1, d2, 32, S1, P2);
+    conv_fwd(Ls[4], d2, P2, A2a);
+    conv_fwd(Ls[5], d2, A2a, S2);
+    k_pool<<<flat_blocks(d3.n * 64), 256, 0, st_>>>(d2, d3, 64, S2, P3);
+    conv_fwd(Ls[6], d3, P3, A3a);
+    conv_fwd(Ls[7], d3, A3a, A3b);
+    k_up_add<<<flat_blocks(d2.n * 64), 256, 0, st_>>>(d2, d3, 64, A3b, S2, U2);
+    conv_fwd(Ls[8], d2, U2, D2a);
+    conv_fwd(Ls[9], d2, D2a, D2b);
+    k_up_add<<<flat_blocks(d1.n * 32), 256, 0, st_>>>(d1, d2, 32, D2b, S1, U1);
+    conv_fwd(Ls[10], d1, U1, D1a);
+    conv_fwd(Ls[11], d1, D1a, D1b);
+    k_up_add<<<flat_blocks(d0.n * 16), 256, 0, st_>>>(d0, d1, 16, D1b, S0, U0);
+    conv_fwd(Ls[12], d0, U0, D0a);
+    conv_fwd(Ls[13], d0, D0a, D0b);
+    const ConvLayer &H = Ls[14];
+    k_head_fwd<<<flat_blocks(d0.n), 256, 0, st_>>>(d0.n, 16, D0b, p_ + H.woff, p_ + H.boff, out ? out : out_);
+    return cudaGetLastError();
+}
+
+// relu backward, weight/bias gradients and (optionally) the input gradient of one conv layer
+void UNet::conv_bwd(const ConvLayer &L, const Dims &d, const bf16 *x, const bf16 *post, const float *dpost,
+                    float *dx) {
+    const long long m = d.n * L.cout;
+    bf16 *dy = gbf[L.level];
+    k_relu_back<<<flat_blocks(m), 256, 0, st_>>>(m, dpost, post, dy);
+    long long vchunk = (d.n + 63) / 64;
+    if (vchunk < kVchunkMin) vchunk = kVchunkMin;
+    const int chunks = (int)((d.n + vchunk - 1) / vchunk);
+    wgrad_dispatch(st_, L.cin, L.cout, d, dy, x, wpart_, L.taps, (int)vchunk, chunks);
+    const long long mw = (long long)L.taps * L.cout * L.cin;
+    k_reduce_chunks<<<flat_blocks(mw), 256, 0, st_>>>(wpart_, chunks, mw, g_ + L.woff);
+    k_bias_grad<<<chunks, 64, 0, st_>>>(d, dy, L.cout, (int)vchunk, hpart_);
+    k_reduce_chunks<<<1, 64, 0, st_>>>(hpart_, chunks, L.cout, g_ + L.boff);
+    if (dx) conv_dispatch(st_, L.cout, L.cin, 1, d, dy, wt_ + L.wbf, nullptr, dx, L.taps);
+}
+
+cudaError_t UNet::backward(const Dims &d, const float *dout) {
+    if (!have_ws_ || dims_[0].nx != d.nx || dims_[0].ny != d.ny || dims_[0].nz != d.nz)
+        return cudaErrorInvalidValue;
+    const ConvLayer *Ls = layers_.data();
+    const Dims &d0 = dims_[0], &d1 = dims_[1], &d2 = dims_[2], &d3 = dims_[3];
+    // head (1x1): da = dout w, dw = sum dout a, db = sum dout
+    {
+        const ConvLayer &H = Ls[14];
+        long long vchunk = (d0.n + 4095) / 4096;
+        if (vchunk < 256) vchunk = 256;
+        const int chunks = (int)((d0.n + vchunk - 1) / vchunk);
+        k_head_back<<<chunks, 64, 0, st_>>>(d0.n, 16, D0b, p_ + H.woff, dout, gA[0], (int)vchunk, hpart_);
+        k_reduce_chunks<<<1, 64, 0, st_>>>(hpart_, chunks, 17, g_ + H.woff);  // 16 weights then the bias
+    }
+    conv_bwd(Ls[13], d0, D0a, D0b, gA[0], gB[0]);
+    conv_bwd(Ls[12], d0, U0, D0a, gB[0], gU[0]);
+    k_up_back<<<flat_blocks(d1.n * 16), 256, 0, st_>>>(d0, d1, 16, gU[0], gA[1]);
+    conv_bwd(Ls[11], d1, D1a, D1b, gA[1], gB[1]);
+    conv_bwd(Ls[10], d1, U1, D1a, gB[1], gU[1]);
+    k_up_back<<<flat_blocks(d2.n * 32), 256, 0, st_>>>(d1, d2, 32, gU[1], gA[2]);
+    conv_bwd(Ls[9], d2, D2a, D2b, gA[2], gB[2]);
+    conv_bwd(Ls[8], d2, U2, D2a, gB[2], gU[2]);
+    k_up_back<<<flat_blocks(d3.n * 64), 256, 0, st_>>>(d2, d3, 64, gU[2], gA[3]);
+    conv_bwd(Ls[7], d3, A3a, A3b, gA[3], gB[3]);
+    conv_bwd(Ls[6], d3, P3, A3a, gB[3], gA[3]);
+    k_pool_back<<<flat_blocks(d2.n * 64), 256, 0, st_>>>(d2, d3, 64, gA[3], gU[2], gA[2]);
+    conv_bwd(Ls[5], d2, A2a, S2, gA[2], gB[2]);
+    conv_bwd(Ls[4], d2, P2, A2a, gB[2], gA[2]);
+    k_pool_back<<<flat_blocks(d1.n * 32), 256, 0, st_>>>(d1, d2, 32, gA[2], gU[1], gA[1]);
+    conv_bwd(Ls[3], d1, A1a, S1, gA[1], gB[1]);
+    conv_bwd(Ls[2], d1, P1, A1a, gB[1], gA[1]);
+    k_pool_back<<<flat_blocks(d0.n * 16), 256, 0, st_>>>(d0, d1, 16, gA[1], gU[0], gA[0]);
+    conv_bwd(Ls[1], d0, A0a, S0, gA[0], gB[0]);
+    conv_bwd(Ls[0], d0, feat_, A0a, gB[0], nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t UNet::train_step(const Dims &d, const bf16 *feat, const float *target, float lr, double &loss) {
+    cudaError_t e = forward(d, feat, nullptr);
+    if (e != cudaSuccess) return e;
+    unsigned *ticket = reinterpret_cast<unsigned *>(dots_ + 4);
+    k_cos_dots<<<1216, dim3(32, 8), 0, st_>>>(d.n, out_, target, dots_, redpart_, ticket);
+    k_cos_grad<<<flat_blocks(d.n), 256, 0, st_>>>(d.n, out_, target, dots_, dout_);
+    e = backward(d, dout_);
+    if (e != cudaSuccess) return e;
+    step_++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)step_), c2 = 1.f - powf(b2, (float)step_);
+    k_adam<<<flat_blocks(nparams_), 256, 0, st_>>>(nparams_, p_, g_, m1_, m2_, lr, b1, b2, 1e-8f, c1, c2, nullptr);
+    refresh_bf16();
+    cudaMemcpyAsync(dots_host_, dots_, 24, cudaMemcpyDeviceToHost, st_);
+    e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return e;
+    const double ot = dots_host_[0], oo = dots_host_[1], tt = dots_host_[2];
+    loss = (oo > 0 && tt > 0) ? 1.0 - ot * ot / (oo * tt) : 1.0;
+    return cudaSuccess;
+}
+
+// ------------------------------------------------------------------------------------------------ features
+// Input channels of the network for a system A x = b in face-coefficient form (FP64 fine level):
+//   0: b / rms(b)  1: active (D > 0)  2-4: lower-face couplings ax, ay, az divided by D  5: dex / D
+//   6-15: zero.  Everything is dimensionless, so one network serves the pressure and the potential systems.
+__global__ void k_features(Dims d, Coef<double> cf, const double *__restrict__ b, double inv_rms, bf16 *__restrict__ f) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < d.n; c += (long long)gridDim.x * blockDim.x) {
+        const double D = cf.D[c];
+        const float inv = D > 0 ? (float)(1.0 / D) : 0.f;
+        float v[16] = {0};
+        v[0] = (float)(b[c] * inv_rms);
+        v[1] = D > 0 ? 1.f : 0.f;
+        v[2] = (float)cf.ax[c] * inv;
+        v[3] = (float)cf.ay[c] * inv;
+        v[4] = (float)cf.az[c] * inv;
+        v[5] = (float)cf.dex[c] * inv;
+        uint32_t w[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) w[q] = pack_bf16(v[2 * q], v[2 * q + 1]);
+        uint4 *dst = reinterpret_cast<uint4 *>(f + c * 16);
+        dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sumsq_active(long long n, const double *__restrict__ b,
+                                                      const double *__restrict__ D, double *out, double *part,
+                                                      unsigned *ticket) {
+    double v[2] = {0, 0};
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
+        if (D[c] > 0) {
+            v[0] += b[c] * b[c];
+            v[1] += 1.0;
+        }
+    }
+    double tot[2];
+    if (grid_reduce<2>(v, part, ticket, tot)) {
+        out[0] = tot[0];
+        out[1] = tot[1];
+    }
+}
+
+cudaError_t UNet::features(const Dims &d, const Coef<double> &cf, const double *b, bf16 *feat) {
+    unsigned *ticket = reinterpret_cast<unsigned *>(dots_ + 4);
+    k_sumsq_active<<<1216, dim3(32, 8), 0, st_>>>(d.n, b, cf.D, dots_, redpart_, ticket);
+    cudaMemcpyAsync(dots_host_, dots_, 16, cudaMemcpyDeviceToHost, st_);
+    cudaError_t e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return e;
+    const double cnt = dots_host_[1] > 0 ? dots_host_[1] : 1.0;
+    const double rms = std::sqrt(dots_host_[0] / cnt);
+    const double inv = rms > 0 ? 1.0 / rms : 0.0;
+    k_features<<<flat_blocks(d.n), 256, 0, st_>>>(d, cf, b, inv, feat);
+    return cudaGetLastError();
+}
+
+}  // namespace sf
