@@ -184,3 +184,86 @@ def flops_per_voxel(cin0: int) -> float:
     for name, ci, co, lv, ks in layer_specs(cin0):
         f += 2.0 * ks ** 3 * ci * co / 8.0 ** lv
     return f
+
+
+# ------------------------------------------------------------------------------------------------ BF16 emulation
+def bf16(a):
+    """Round to bfloat16 (nearest even) and return float32 values."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = a.view(np.uint32).astype(np.uint64)
+    r = ((b >> 16) & 1) + 0x7FFF
+    return ((b + r) & 0xFFFF0000).astype(np.uint32).view(np.float32)
+
+
+def flatten(P):
+    """Flat FP32 parameter vector in the CUDA network's order: per layer, weights then bias."""
+    return np.concatenate([np.concatenate([P[n + ".w"].ravel(), P[n + ".b"].ravel()]) for n, *_ in LAYERS]).astype(
+        np.float32)
+
+
+def unflatten(flat, cin0=16):
+    P, o = {}, 0
+    for name, ci, co, lv, ks in layer_specs(cin0):
+        m = ks ** 3 * co * ci
+        P[name + ".w"] = flat[o:o + m].reshape(ks ** 3, co, ci)
+        o += m
+        P[name + ".b"] = flat[o:o + co]
+        o += co
+    return P
+
+
+def forward_bf16(P, x):
+    """The CUDA forward's rounding: BF16 weights/features/stored activations, FP64 accumulation here."""
+    cache = {}
+    W = {k: (bf16(v) if k.endswith(".w") and not k.startswith("head") else v) for k, v in P.items()}
+
+    def cr(name, inp):
+        pre = conv(inp, W[name + ".w"], W[name + ".b"])
+        post = bf16(np.maximum(pre, 0.0))
+        cache[name] = (inp, post)
+        return post
+
+    x = bf16(x)
+    s0 = cr("e0b", cr("e0a", x))
+    s1 = cr("e1b", cr("e1a", bf16(pool(s0))))
+    s2 = cr("e2b", cr("e2a", bf16(pool(s1))))
+    a = cr("e3b", cr("e3a", bf16(pool(s2))))
+    a = cr("d2b", cr("d2a", bf16(up(a, s2.shape) + s2)))
+    a = cr("d1b", cr("d1a", bf16(up(a, s1.shape) + s1)))
+    a = cr("d0b", cr("d0a", bf16(up(a, s0.shape) + s0)))
+    out = conv(a, P["head.w"], P["head.b"])[..., 0]
+    cache["head"] = (a, None)
+    cache["shapes"] = (s0.shape, s1.shape, s2.shape)
+    cache["W"] = W
+    return out, cache
+
+
+def backward_bf16(P, cache, dout):
+    """Gradients with the CUDA backward's rounding: the ReLU-masked upstream gradient is BF16."""
+    G = {}
+    W = cache["W"]
+
+    def back(name, dpost, need_dx=True):
+        inp, post = cache[name]
+        dpre = bf16(dpost * (post > 0))
+        dx, dw, db = conv_grads(inp, W[name + ".w"], dpre)
+        G[name + ".w"] = dw
+        G[name + ".b"] = db
+        return dx
+
+    s0s, s1s, s2s = cache["shapes"]
+    a, _ = cache["head"]
+    G["head.w"] = np.einsum("xyz,xyzc->c", dout, a)[None, None, :]
+    G["head.b"] = np.array([dout.sum()])
+    d = dout[..., None] * P["head.w"][0, 0][None, None, None, :]
+    d = back("d0a", back("d0b", d))
+    ds0 = d
+    d = back("d1a", back("d1b", up_back(d, cache["d1b"][1].shape[:3])))
+    ds1 = d
+    d = back("d2a", back("d2b", up_back(d, cache["d2b"][1].shape[:3])))
+    ds2 = d
+    d = back("e3a", back("e3b", up_back(d, cache["e3b"][1].shape[:3])))
+    d = back("e2a", back("e2b", pool_back(d, s2s) + ds2))
+    d = back("e1a", back("e1b", pool_back(d, s1s) + ds1))
+    back("e0a", back("e0b", pool_back(d, s0s) + ds0))
+    return G

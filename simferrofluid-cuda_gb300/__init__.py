@@ -21,10 +21,10 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _abi
-from ._abi import SF_PREC_FP64, SF_PREC_MIXED  # noqa: F401
+from ._abi import SF_PREC_FP64, SF_PREC_LEARNED, SF_PREC_MIXED  # noqa: F401
 
-__all__ = ["StaggeredGrid", "Context", "Pressure", "MagneticField", "SolveError", "options", "load_library",
-           "SF_PREC_FP64", "SF_PREC_MIXED"]
+__all__ = ["StaggeredGrid", "Context", "Pressure", "MagneticField", "Network", "SolveError", "options",
+           "load_library", "SF_PREC_FP64", "SF_PREC_MIXED", "SF_PREC_LEARNED"]
 
 
 def load_library():
@@ -94,7 +94,7 @@ def options(which="pressure", **kw):
     lib.sf_default_opts(C.byref(o), 0 if which == "pressure" else 1)
     for k, v in kw.items():
         if k == "precision" and isinstance(v, str):
-            v = {"fp64": SF_PREC_FP64, "mixed": SF_PREC_MIXED}[v]
+            v = {"fp64": SF_PREC_FP64, "mixed": SF_PREC_MIXED, "learned": SF_PREC_LEARNED}[v]
         if not hasattr(o, k):
             raise KeyError(k)
         setattr(o, k, v)
@@ -129,6 +129,85 @@ class Context:
 
     def device_bytes(self):
         return int(self.lib.sf_device_bytes(self.handle))
+
+    def set_network(self, net):
+        """Attach the U-Net used by precision="learned" solves (None detaches)."""
+        s = self.lib.sf_set_network(self.handle, net.handle if net is not None else None)
+        if s != _abi.SF_OK:
+            raise SolveError(s, self.last_error())
+        self.network = net
+
+    def system_features(self, which, features=None, solution=None):
+        """Network features (BF16 [n][16], device) and FP32 solution of the last pressure (0) / potential (1)
+        system assembled on this context; arguments are CUDA tensors or None."""
+        s = self.lib.sf_system_features_dev(self.handle, int(which),
+                                            C.c_void_p(features.data_ptr()) if features is not None else None,
+                                            C.c_void_p(solution.data_ptr()) if solution is not None else None)
+        if s != _abi.SF_OK:
+            raise SolveError(s, self.last_error())
+
+
+class Network:
+    """The learned solver's 3D U-Net on a context (sf_unet_*).  Features and outputs are CUDA tensors."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        h = C.c_void_p()
+        s = ctx.lib.sf_unet_create(ctx.handle, C.byref(h))
+        if s != _abi.SF_OK:
+            raise SolveError(s, "sf_unet_create: " + ctx.last_error())
+        self.handle = h
+        self.num_params = int(ctx.lib.sf_unet_num_params(h))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.ctx.lib.sf_unet_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, s, what):
+        if s != _abi.SF_OK:
+            raise SolveError(s, f"{what}: {self.ctx.last_error()}")
+
+    def set_params(self, flat):
+        flat = np.ascontiguousarray(flat, dtype=np.float32)
+        self._ok(self.ctx.lib.sf_unet_set_params(self.handle, flat.ctypes.data, flat.size), "set_params")
+
+    def get_params(self):
+        out = np.empty(self.num_params, np.float32)
+        self._ok(self.ctx.lib.sf_unet_get_params(self.handle, out.ctypes.data, out.size), "get_params")
+        return out
+
+    def forward(self, grid: StaggeredGrid, features, out):
+        self._ok(self.ctx.lib.sf_unet_forward_dev(self.handle, C.byref(grid.c_grid()), features.data_ptr(),
+                                                   out.data_ptr()), "forward")
+        return out
+
+    def gradients(self, grid: StaggeredGrid, features, dout):
+        g = np.empty(self.num_params, np.float32)
+        self._ok(self.ctx.lib.sf_unet_backward_dev(self.handle, C.byref(grid.c_grid()), features.data_ptr(),
+                                                    dout.data_ptr(), g.ctypes.data), "backward")
+        return g
+
+    def train_step(self, grid: StaggeredGrid, features, target, lr):
+        loss = C.c_double()
+        self._ok(self.ctx.lib.sf_unet_train_step_dev(self.handle, C.byref(grid.c_grid()), features.data_ptr(),
+                                                      target.data_ptr(), float(lr), C.byref(loss)), "train_step")
+        return loss.value
+
+    def save(self, path):
+        self.get_params().tofile(path)
+
+    def load(self, path):
+        flat = np.fromfile(path, dtype=np.float32)
+        if flat.size != self.num_params:
+            raise ValueError(f"{path}: {flat.size} parameters, expected {self.num_params}")
+        self.set_params(flat)
 
 
 _default_ctx = None
