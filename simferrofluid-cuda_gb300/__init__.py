@@ -115,6 +115,7 @@ class Context:
 
     def close(self):
         if getattr(self, "handle", None):
+            self.network = None
             self.lib.sf_destroy(self.handle)
             self.handle = None
 

@@ -3,8 +3,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <memory>
 #include <string>
+#include <vector>
 
 #include "sf_ops.h"
 #include "sf_solver.h"
@@ -28,8 +30,10 @@ struct Ctx {
     Dims mag_dims{0, 0, 0, 0};
     // staging buffers for the host-pointer entry points
     DevBuf phi, frac[3], vel[3], us[3], jump[3], hext[3], H[3], cells;
-    // learned form: attached network (not owned) and its buffers
+    // learned form: attached network (not owned) and its buffers; every network created on this context is
+    // registered so that destroying the context first leaves the network handles safe to destroy later
     UNet *net = nullptr;
+    std::vector<void *> nets;
     DevBuf feat, guess;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
@@ -344,6 +348,11 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
 
 }  // namespace
 
+struct NetHandle {
+    Ctx *ctx;  // nullptr once the context is destroyed
+    std::unique_ptr<UNet> net;
+};
+
 // ------------------------------------------------------------------------------------------------ C ABI
 extern "C" {
 
@@ -414,6 +423,14 @@ void sf_destroy(void *p) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->st) cudaStreamSynchronize(c->st);
+    // networks created on this context lose their device state; their handles stay valid for sf_unet_destroy
+    for (void *p : c->nets) {
+        auto *h = reinterpret_cast<NetHandle *>(p);
+        h->net.reset();
+        h->ctx = nullptr;
+    }
+    c->nets.clear();
+    c->net = nullptr;
     c->pres.reset();
     c->mag.reset();
     for (auto &e : c->ev)
@@ -479,11 +496,6 @@ sf_status sf_magnetic_reset(void *ctx) {
 }
 
 // ----- learned form ------------------------------------------------------------------------------------------
-struct NetHandle {
-    Ctx *ctx;
-    std::unique_ptr<UNet> net;
-};
-
 sf_status sf_unet_create(void *ctx, void **out) {
     Ctx *c = C(ctx);
     if (!c || !out) return SF_BAD_ARG;
@@ -494,37 +506,42 @@ sf_status sf_unet_create(void *ctx, void **out) {
         delete h;
         return fail(c, SF_OUT_OF_MEMORY, m);
     }
+    c->nets.push_back(h);
     *out = h;
     return SF_OK;
 }
 void sf_unet_destroy(void *net) {
     auto *h = reinterpret_cast<NetHandle *>(net);
     if (!h) return;
-    if (h->ctx->net == h->net.get()) h->ctx->net = nullptr;
-    cudaStreamSynchronize(h->ctx->st);
+    if (Ctx *c = h->ctx) {
+        if (c->net == h->net.get()) c->net = nullptr;
+        c->nets.erase(std::remove(c->nets.begin(), c->nets.end(), net), c->nets.end());
+        cudaSetDevice(c->device);
+        cudaStreamSynchronize(c->st);
+    }
     delete h;
 }
 long long sf_unet_num_params(void *net) {
     auto *h = reinterpret_cast<NetHandle *>(net);
-    return h ? h->net->num_params() : 0;
+    return (h && h->ctx) ? h->net->num_params() : 0;
 }
 sf_status sf_unet_set_params(void *net, const float *host, long long n) {
     auto *h = reinterpret_cast<NetHandle *>(net);
-    if (!h || !host || n != h->net->num_params()) return SF_BAD_ARG;
+    if (!h || !h->ctx || !host || n != h->net->num_params()) return SF_BAD_ARG;
     Ctx *c = h->ctx;
     CK(h->net->set_params(host));
     return SF_OK;
 }
 sf_status sf_unet_get_params(void *net, float *host, long long n) {
     auto *h = reinterpret_cast<NetHandle *>(net);
-    if (!h || !host || n != h->net->num_params()) return SF_BAD_ARG;
+    if (!h || !h->ctx || !host || n != h->net->num_params()) return SF_BAD_ARG;
     Ctx *c = h->ctx;
     CK(h->net->get_params(host));
     return SF_OK;
 }
 sf_status sf_unet_forward_dev(void *net, const sf_grid *g, const void *features, float *out) {
     auto *h = reinterpret_cast<NetHandle *>(net);
-    if (!h || !grid_ok(g) || !features || !out) return SF_BAD_ARG;
+    if (!h || !h->ctx || !grid_ok(g) || !features || !out) return SF_BAD_ARG;
     Ctx *c = h->ctx;
     CK(h->net->forward(make_dims(g->nx, g->ny, g->nz), (const __nv_bfloat16 *)features, out));
     CK(cudaStreamSynchronize(c->st));
@@ -532,7 +549,7 @@ sf_status sf_unet_forward_dev(void *net, const sf_grid *g, const void *features,
 }
 sf_status sf_unet_backward_dev(void *net, const sf_grid *g, const void *features, const float *dout, float *grads) {
     auto *h = reinterpret_cast<NetHandle *>(net);
-    if (!h || !grid_ok(g) || !features || !dout) return SF_BAD_ARG;
+    if (!h || !h->ctx || !grid_ok(g) || !features || !dout) return SF_BAD_ARG;
     Ctx *c = h->ctx;
     const Dims d = make_dims(g->nx, g->ny, g->nz);
     CK(h->net->forward(d, (const __nv_bfloat16 *)features, nullptr));
@@ -544,7 +561,7 @@ sf_status sf_unet_backward_dev(void *net, const sf_grid *g, const void *features
 sf_status sf_unet_train_step_dev(void *net, const sf_grid *g, const void *features, const float *target, float lr,
                                  double *loss) {
     auto *h = reinterpret_cast<NetHandle *>(net);
-    if (!h || !grid_ok(g) || !features || !target || !(lr > 0)) return SF_BAD_ARG;
+    if (!h || !h->ctx || !grid_ok(g) || !features || !target || !(lr > 0)) return SF_BAD_ARG;
     Ctx *c = h->ctx;
     double l = 0;
     CK(h->net->train_step(make_dims(g->nx, g->ny, g->nz), (const __nv_bfloat16 *)features, target, lr, l));
@@ -555,7 +572,7 @@ sf_status sf_set_network(void *ctx, void *net) {
     Ctx *c = C(ctx);
     if (!c) return SF_BAD_ARG;
     auto *h = reinterpret_cast<NetHandle *>(net);
-    if (h && h->ctx != c) return fail(c, SF_BAD_ARG, "network belongs to another context");
+    if (h && h->ctx != c) return fail(c, SF_BAD_ARG, "network belongs to another (or a destroyed) context");
     c->net = h ? h->net.get() : nullptr;
     return SF_OK;
 }

@@ -65,28 +65,41 @@ class SampleSource:
         self.feat = torch.zeros((self.g.num_cells, 16), dtype=torch.bfloat16, device=self.dev)
         self.sol = torch.zeros(self.g.num_cells, dtype=torch.float32, device=self.dev)
 
-    def system(self, kind):
-        """Assemble and solve one system; returns the solver statistics (features in .feat, solution in .sol)."""
-        torch, g, sf = self.torch, self.g, self.sf
+    def draw(self, kind):
+        """Seeded random inputs of one system of the given kind (0 pressure, 1 potential)."""
+        torch, g = self.torch, self.g
         phi = random_scene_phi(torch, self.n, self.rng, self.dev)
         gen = torch.Generator(device=self.dev)
         gen.manual_seed(int(self.rng.integers(1 << 62)))
         if kind == 0:
             vel = [torch.randn(g.face_shape(a), dtype=torch.float64, device=self.dev, generator=gen) * 0.5
                    for a in range(3)]
-            st = self.P.project(vel, phi, self.frac, device=True,
-                                opts=sf.options("pressure", precision="fp64", tol=1e-8))
+            return dict(kind=0, phi=phi, vel=vel)
+        d = self.rng.normal(size=3)
+        d = d / np.linalg.norm(d) * self.rng.uniform(0.5, 2.0)
+        hext = [torch.full(g.face_shape(a), float(d[a]), dtype=torch.float64, device=self.dev) for a in range(3)]
+        return dict(kind=1, phi=phi, hext=hext, chi=float(self.rng.uniform(0.5, 3.0)))
+
+    def solve(self, inp, precision, tol):
+        """Solve a drawn system (inputs are not modified); returns the solver statistics."""
+        torch, g, sf = self.torch, self.g, self.sf
+        if inp["kind"] == 0:
+            vel = [v.clone() for v in inp["vel"]]
+            st = self.P.project(vel, inp["phi"], self.frac, device=True, raise_on_nonconv=False,
+                                opts=sf.options("pressure", precision=precision, tol=tol))
         else:
-            self.M.set_susceptibility(self.rng.uniform(0.5, 3.0))
-            d = self.rng.normal(size=3)
-            d = d / np.linalg.norm(d) * self.rng.uniform(0.5, 2.0)
-            hext = [torch.full(g.face_shape(a), float(d[a]), dtype=torch.float64, device=self.dev)
-                    for a in range(3)]
+            self.M.set_susceptibility(inp["chi"])
             psi = torch.zeros(g.shape, dtype=torch.float64, device=self.dev)
             H = [torch.zeros(g.face_shape(a), dtype=torch.float64, device=self.dev) for a in range(3)]
-            st = self.M.solve(phi, hext, device=True, psi_out=psi, H_out=H,
-                              opts=sf.options("magnetic", precision="fp64", tol=1e-8, warm_start=0))
+            st = self.M.solve(inp["phi"], inp["hext"], device=True, psi_out=psi, H_out=H, raise_on_nonconv=False,
+                              opts=sf.options("magnetic", precision=precision, tol=tol, warm_start=0))
         torch.cuda.synchronize(self.dev)
+        return st
+
+    def system(self, kind):
+        """Draw, solve with the plain FP64 method to 1e-8, and export features (.feat) and solution (.sol)."""
+        inp = self.draw(kind)
+        st = self.solve(inp, "fp64", 1e-8)
         self.ctx.system_features(kind, self.feat, self.sol)
         return st
 
@@ -105,6 +118,48 @@ def train(ctx, net, samples=2000, n=128, lr=1e-3, seed=2024, log_every=50, log=N
     return losses
 
 
+def evaluate(ctx, net, scenes=64, n=256, seed=777, tol=1e-6, log=None):
+    """Ablation on unseen seeded scenes: mixed-precision MGPCG from zero against the same solver started from
+    the network's prediction (with its fallback).  Returns per-scene iterations, times and guess residuals."""
+    import torch
+    src = SampleSource(ctx, n, seed)
+    rows = []
+    for i in range(scenes):
+        inp = src.draw(i % 2)
+        res = {}
+        for prec in ("mixed", "learned"):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            st = src.solve(inp, prec, tol)
+            res[prec] = dict(iters=st["iters"], outer=st["outer_iters"], ms=1e3 * (time.perf_counter() - t),
+                             relres=st["rel_residual"], guess=st["guess_rel_residual"])
+        rows.append(dict(kind=i % 2, **res))
+        if log:
+            log(f"scene {i:3d} kind {i % 2} plain {res['mixed']['iters']:3d} it {res['mixed']['ms']:7.2f} ms | "
+                f"learned {res['learned']['iters']:3d} it {res['learned']['ms']:7.2f} ms guess "
+                f"{res['learned']['guess']:.3f}")
+    return rows
+
+
+def summarize(rows):
+    out = {}
+    for kind in (0, 1):
+        rs = [r for r in rows if r["kind"] == kind]
+        if not rs:
+            continue
+        out["pressure" if kind == 0 else "potential"] = {
+            "scenes": len(rs),
+            "plain_iters": float(np.mean([r["mixed"]["iters"] for r in rs])),
+            "learned_iters": float(np.mean([r["learned"]["iters"] for r in rs])),
+            "plain_ms": float(np.mean([r["mixed"]["ms"] for r in rs])),
+            "learned_ms": float(np.mean([r["learned"]["ms"] for r in rs])),
+            "guess_rel_residual": float(np.mean([r["learned"]["guess"] for r in rs])),
+            "plain_solves_per_s": float(1e3 / np.mean([r["mixed"]["ms"] for r in rs])),
+            "learned_solves_per_s": float(1e3 / np.mean([r["learned"]["ms"] for r in rs])),
+        }
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--samples", type=int, default=2000)
@@ -113,6 +168,9 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--out", default=os.path.join(HERE, "weights", "unet.f32"))
     ap.add_argument("--init", default=None, help="start from these weights")
+    ap.add_argument("--eval", type=int, default=0, help="then evaluate on this many unseen scenes")
+    ap.add_argument("--eval-n", type=int, default=256)
+    ap.add_argument("--report", default=None, help="write the training/evaluation summary (JSON) here")
     args = ap.parse_args()
     sf = _pkg()
     import torch
@@ -131,12 +189,30 @@ def main():
             flat.append(np.zeros(co, np.float32))
         net.set_params(np.concatenate(flat))
     ctx.set_network(net)
-    losses = train(ctx, net, args.samples, args.n, args.lr, args.seed, log=lambda m: print(m, flush=True))
-    os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
-    net.save(args.out)
-    k = max(1, len(losses) // 10)
-    print(json.dumps({"samples": args.samples, "n": args.n, "loss_first": float(np.mean(losses[:k])),
-                      "loss_last": float(np.mean(losses[-k:])), "out": args.out}))
+    report = {"samples": args.samples, "n": args.n, "lr": args.lr, "seed": args.seed}
+    if args.samples > 0:
+        t0 = time.time()
+        losses = train(ctx, net, args.samples, args.n, args.lr, args.seed, log=lambda m: print(m, flush=True))
+        os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
+        net.save(args.out)
+        k = max(1, len(losses) // 10)
+        lp = [l for i, l in enumerate(losses) if i % 2 == 0]
+        lm = [l for i, l in enumerate(losses) if i % 2 == 1]
+        kk = max(1, len(lp) // 10)
+        report.update(train_s=round(time.time() - t0, 1), loss_first=float(np.mean(losses[:k])),
+                      loss_last=float(np.mean(losses[-k:])), pressure_loss_last=float(np.mean(lp[-kk:])),
+                      potential_loss_last=float(np.mean(lm[-kk:])), out=args.out)
+    if args.eval > 0:
+        rows = evaluate(ctx, net, args.eval, args.eval_n, log=lambda m: print(m, flush=True))
+        report["eval"] = summarize(rows)
+        report["eval_n"] = args.eval_n
+    print(json.dumps(report), flush=True)
+    if args.report:
+        with open(args.report, "w") as f:
+            json.dump(report, f, indent=1)
+    ctx.set_network(None)
+    net.close()
+    ctx.close()
 
 
 def _layer_table():

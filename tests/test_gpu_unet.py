@@ -108,3 +108,15 @@ def test_learned_solve_converges_and_falls_back(sfpkg, oracle, gpu_ctx, ref):
     assert st["converged"] == 1 and rel_l2(P.pressure[liq], p_or[liq]) <= 1e-5
     gpu_ctx.set_network(None)
     net.close()
+
+
+def test_network_outlives_context(sfpkg):
+    """Destroying the context before its network leaves the network handle safe to destroy."""
+    ctx = sfpkg.Context(0)
+    net = sfpkg.Network(ctx)
+    ctx.set_network(net)
+    lib = ctx.lib
+    h = net.handle
+    ctx.close()
+    assert lib.sf_unet_num_params(h) == 0  # orphaned: no device state left
+    net.close()
