@@ -201,6 +201,14 @@ class Network:
                                                       target.data_ptr(), float(lr), C.byref(loss)), "train_step")
         return loss.value
 
+    def set_mode(self, mode):
+        """Forward convolution kernels: "mma" (warp-level mma.sync) or "tcgen05" (TMA + TMEM)."""
+        m = {"mma": 0, "tcgen05": 1}.get(mode, mode)
+        self._ok(self.ctx.lib.sf_unet_set_mode(self.handle, int(m)), "set_mode")
+
+    def tc_launches(self):
+        return int(self.ctx.lib.sf_unet_tc_launches(self.handle))
+
     def save(self, path):
         self.get_params().tofile(path)
 

@@ -30,7 +30,7 @@ EXPORTED = [
     "sf_collider_box_fractions", "sf_collider_face_fractions",
     "sf_unet_create", "sf_unet_destroy", "sf_unet_num_params", "sf_unet_set_params", "sf_unet_get_params",
     "sf_unet_forward_dev", "sf_unet_backward_dev", "sf_unet_train_step_dev", "sf_set_network",
-    "sf_system_features_dev",
+    "sf_system_features_dev", "sf_unet_set_mode", "sf_unet_tc_launches",
 ]
 
 
@@ -120,6 +120,10 @@ def load(path: str | None = None):
     L.sf_unet_backward_dev.restype = C.c_int
     L.sf_unet_train_step_dev.argtypes = [V, G, V, V, C.c_float, C.POINTER(C.c_double)]
     L.sf_unet_train_step_dev.restype = C.c_int
+    L.sf_unet_set_mode.argtypes = [V, C.c_int]
+    L.sf_unet_set_mode.restype = C.c_int
+    L.sf_unet_tc_launches.argtypes = [V]
+    L.sf_unet_tc_launches.restype = C.c_longlong
     L.sf_set_network.argtypes = [V, V]
     L.sf_set_network.restype = C.c_int
     L.sf_system_features_dev.argtypes = [V, C.c_int, V, V]

@@ -140,6 +140,8 @@ sf_status learned_guess(Ctx *c, MGSolver &S, const Dims &d, SolveResult &pre) {
     auto *y = (float *)c->guess.get();
     CK(c->net->features(d, S.fine(), S.b(), feat));
     CK(c->net->forward(d, feat, y));
+    if (c->net->mode() == 1 && c->net->check_device_errors() != cudaSuccess)
+        return fail(c, SF_CUDA_ERROR, c->net->last_error);
     double gamma = 0;
     CK(S.set_guess_scaled(y, gamma));
     (void)pre;
@@ -544,8 +546,18 @@ sf_status sf_unet_forward_dev(void *net, const sf_grid *g, const void *features,
     if (!h || !h->ctx || !grid_ok(g) || !features || !out) return SF_BAD_ARG;
     Ctx *c = h->ctx;
     CK(h->net->forward(make_dims(g->nx, g->ny, g->nz), (const __nv_bfloat16 *)features, out));
-    CK(cudaStreamSynchronize(c->st));
+    if (h->net->check_device_errors() != cudaSuccess) return fail(c, SF_CUDA_ERROR, h->net->last_error);
     return SF_OK;
+}
+sf_status sf_unet_set_mode(void *net, int mode) {
+    auto *h = reinterpret_cast<NetHandle *>(net);
+    if (!h || !h->ctx || (mode != 0 && mode != 1)) return SF_BAD_ARG;
+    h->net->set_mode(mode);
+    return SF_OK;
+}
+long long sf_unet_tc_launches(void *net) {
+    auto *h = reinterpret_cast<NetHandle *>(net);
+    return (h && h->ctx) ? h->net->tc_launches() : 0;
 }
 sf_status sf_unet_backward_dev(void *net, const sf_grid *g, const void *features, const float *dout, float *grads) {
     auto *h = reinterpret_cast<NetHandle *>(net);

@@ -1,0 +1,256 @@
+// sf_conv_tc.cuh -- 3x3x3 convolution forward on the 5th-generation tensor cores (tcgen05 + TMA, sm_103a).
+//
+// Implicit GEMM per CTA: M = 128 output voxels (a 32 (z) x 4 (y) x 1 (x) brick), N = Cout, K = 27 taps x Cin.
+// Operands are staged by TMA in the no-swizzle K-major "core matrix" layout: one 4-D box of 8 channels x
+// (32 x 4 x 1) voxels per 8-channel chunk and tap lands as 128 rows x 16 B, i.e. 8-row x 16-B core matrices
+// with a 128-B stride along M and one 2-KB chunk per 8 channels along K; taps outside the grid are filled with
+// zeros by the TMA unit (the convolution's zero padding).  Weights [tap][Cout][Cin] are staged the same way.
+// One thread issues TMA loads and tcgen05.mma (M=128, N=Cout, K=16, BF16 in, FP32 accumulate in TMEM) through
+// a ring of stages guarded by mbarriers; all four warps read the accumulator back with tcgen05.ld and apply
+// bias + ReLU + BF16 conversion.  Every wait is bounded: on timeout the CTA records an error code and returns
+// after releasing its tensor memory.
+#pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "sf_internal.cuh"
+
+namespace sf {
+namespace tc {
+
+constexpr int kStages = 4;
+constexpr int kTmemCols = 64;          // FP32 accumulator columns (N <= 64)
+constexpr uint32_t kSpinLimit = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// bounded wait for the phase with the given parity; returns false on timeout
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kSpinLimit; it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int c0, int c1, int c2,
+                                            int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, %6}], "
+        "[%2];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int c0, int c1,
+                                            int c2) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
+        "[%2];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor, no swizzle, K-major: start, leading (K) and stride (M/N) byte offsets in
+// 16-byte units, descriptor version 1 (bits 46..48 = 0b001), swizzle mode 0.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo_bytes, uint32_t sbo_bytes) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo_bytes >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo_bytes >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t instr_desc_bf16(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void tmem_ld_x16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < 16; q++) v[q] = __uint_as_float(r[q]);
+}
+
+constexpr int kTileZ = 32, kTileY = 4;
+
+template <int CI, int CO>
+struct Layout {
+    static constexpr int kChunks = CI / 8;
+    static constexpr uint32_t kABytes = 128u * 16u * kChunks;  // 128 rows x 16 B per 8-channel chunk
+    static constexpr uint32_t kBBytes = (uint32_t)CO * 16u * kChunks;
+    static constexpr uint32_t kStageBytes = kABytes + kBBytes;
+    static constexpr uint32_t kNeed = kStages * kStageBytes + 1024 /* alignment */ + 256 /* barriers */;
+    // at least 30 KB so that at most 7 CTAs share an SM: 7 x 64 TMEM columns <= 512
+    static constexpr uint32_t kSmemBytes = kNeed > 30u * 1024u ? kNeed : 30u * 1024u;
+};
+
+// err: first error code of any CTA (1 = TMA/MMA wait timed out)
+template <int CI, int CO>
+__global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUtensorMap tmap_x,
+                                                    const __grid_constant__ CUtensorMap tmap_w, Dims d,
+                                                    const float *__restrict__ bias, __nv_bfloat16 *__restrict__ y,
+                                                    int *err) {
+    static_assert(CI % 16 == 0 && CO % 16 == 0 && CO <= kTmemCols, "shape");
+    using L = Layout<CI, CO>;
+    extern __shared__ uint8_t smem_raw[];
+    // 1024-byte aligned stage buffers, barriers after them
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * L::kStageBytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 1);  // [0] TMEM base, [1] status
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kStages), done = smem_u32(bars + 2 * kStages);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    const int tiles_z = (d.nz + kTileZ - 1) / kTileZ, tiles_y = (d.ny + kTileY - 1) / kTileY;
+    const int bz = blockIdx.x % tiles_z, by = (blockIdx.x / tiles_z) % tiles_y, bx = blockIdx.x / (tiles_z * tiles_y);
+    const int z0 = bz * kTileZ, y0 = by * kTileY, x0 = bx;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    volatile int *flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    if (threadIdx.x == 0) {
+        constexpr uint32_t idesc = instr_desc_bf16(CO);
+        constexpr int T = 27;
+        int issued = 0, waited = 0;
+        bool ok = true;
+        auto load = [&](int t, int s) {
+            const uint32_t a = smem_u32(smem + s * L::kStageBytes), b = a + L::kABytes;
+            const uint32_t bar = full0 + 8 * s;
+            mbar_expect_tx(bar, L::kStageBytes);
+            const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
+#pragma unroll
+            for (int c = 0; c < L::kChunks; c++) {
+                tma_load_4d(a + c * 2048u, &tmap_x, bar, 8 * c, z0 + dz, y0 + dy, x0 + dx);
+                tma_load_3d(b + c * (uint32_t)CO * 16u, &tmap_w, bar, 8 * c, 0, t);
+            }
+            issued = t + 1;
+        };
+        for (int t = 0; t < kStages && t < T; t++) load(t, t);
+        for (int t = 0; t < T; t++) {
+            const int s = t % kStages;
+            const uint32_t ph = (uint32_t)(t / kStages) & 1u;
+            if (!mbar_wait(full0 + 8 * s, ph)) {
+                ok = false;
+                break;
+            }
+            waited = t + 1;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a = smem_u32(smem + s * L::kStageBytes), b = a + L::kABytes;
+#pragma unroll
+            for (int j = 0; j < CI / 16; j++) {
+                // K = 16 spans two 8-channel chunks: leading (K) offset = one chunk, stride (M/N) = 8 rows
+                const uint64_t ad = smem_desc(a + j * 2u * 2048u, 2048u, 128u);
+                const uint64_t bd = smem_desc(b + j * 2u * (uint32_t)CO * 16u, (uint32_t)CO * 16u, 128u);
+                mma_bf16(tmem, ad, bd, idesc, (t > 0 || j > 0) ? 1u : 0u);
+            }
+            mma_commit(empty0 + 8 * s);
+            if (t + kStages < T) {
+                if (!mbar_wait(empty0 + 8 * s, ph)) {
+                    ok = false;
+                    break;
+                }
+                load(t + kStages, s);
+            }
+        }
+        // completion of every MMA issued so far (also on the error path, before TMEM is released)
+        mma_commit(done);
+        if (!mbar_wait(done, 0)) ok = false;
+        if (!ok) {
+            // drain loads still in flight into this CTA's shared memory (bounded)
+            for (int t = waited; t < issued; t++) mbar_wait(full0 + 8 * (t % kStages), (uint32_t)(t / kStages) & 1u);
+            atomicCAS(err, 0, 1);
+        }
+        *flag = ok ? 1 : 0;
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (*flag) {  // uniform across the CTA
+        const int r = 32 * warp + lane;  // TMEM lane = tile row
+        const int z = z0 + (r % kTileZ), yy = y0 + r / kTileZ;
+        const bool inb = z < d.nz && yy < d.ny && x0 < d.nx;
+        const long long v = inb ? cid(d, x0, yy, z) : 0;
+#pragma unroll
+        for (int c0 = 0; c0 < CO; c0 += 16) {
+            float acc[16];
+            tmem_ld_x16<16>(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, acc);
+            if (inb) {
+                uint32_t pk[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const float a0 = fmaxf(acc[2 * q] + bias[c0 + 2 * q], 0.f);
+                    const float a1 = fmaxf(acc[2 * q + 1] + bias[c0 + 2 * q + 1], 0.f);
+                    __nv_bfloat162 h2 = __floats2bfloat162_rn(a0, a1);
+                    pk[q] = *reinterpret_cast<uint32_t *>(&h2);
+                }
+                uint4 *dst = reinterpret_cast<uint4 *>(y + v * CO + c0);
+                dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+}  // namespace tc
+}  // namespace sf

@@ -19,6 +19,8 @@
 #include <cstdio>
 #include <cstring>
 
+#include <type_traits>
+
 #include "sf_solver.h"
 
 namespace sf {
@@ -322,6 +324,188 @@ __global__ void __launch_bounds__(256) k_rbgs_fused(Dims d, Coef<C> cf, const T 
         __syncthreads();
         update_B(q - 1);
     }
+}
+
+// ------------------------------------------------------------------------------------------------ pipelined sweep
+// Finest-level variant of the one-pass red-black sweep with every global load issued asynchronously two planes
+// ahead (cp.async, zero-fill outside the grid) into a ring of four planes of x and of the five operator arrays
+// over the tile plus a two-cell halo.  Compute phases read shared memory only, so the march along x is not
+// exposed to global-memory latency.  Same arithmetic order as k_rbgs: bit-identical results.
+// T = C = double (1/D stored) or float (D = sum of couplings + dex).
+constexpr int PEZ = FTZ + 4, PEY = FTY + 4, PRING = 4;
+
+__device__ __forceinline__ void cp_async_elem(void *dst, const void *src, bool valid, int bytes) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    if (bytes == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(s), "l"(src), "r"(valid ? 8 : 0) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(s), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+
+template <class T>
+constexpr size_t pipe_smem_bytes() {
+    return sizeof(T) * (size_t)(6 * PRING * PEY * PEZ + 3 * (FTY + 2) * (FTZ + 2));
+}
+
+template <class T, int MODE>
+__global__ void __launch_bounds__(256) k_rbgs_pipe(Dims d, Coef<T> cf, const T *__restrict__ xin, T *__restrict__ xout,
+                                                   const T *__restrict__ b, int xchunk) {
+    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "FP32 or FP64 finest level");
+    constexpr int RZ = FTZ + 2, RY = FTY + 2, PL = PEY * PEZ;
+    extern __shared__ __align__(16) uint8_t psm[];
+    T *ring = reinterpret_cast<T *>(psm);  // [array 0..5][slot][PEY][PEZ]: x, ax, ay, az, dg, b
+    T(*sa)[RY][RZ] = reinterpret_cast<T(*)[RY][RZ]>(ring + 6 * PRING * PL);
+    const T *dg = sizeof(T) == 8 ? reinterpret_cast<const T *>(cf.invd) : reinterpret_cast<const T *>(cf.dex);
+    const int colA = (MODE == 2) ? 1 : 0;
+    const int z0 = blockIdx.x * FTZ, y0 = blockIdx.y * FTY;
+    const int x0 = blockIdx.z * xchunk;
+    const int x1 = min(x0 + xchunk, d.nx);
+    const int tid = threadIdx.x + 32 * threadIdx.y;
+    auto slot = [](int q) { return ((q % PRING) + PRING) % PRING; };
+    auto E = [&](int arr, int q, int yy, int zz) -> T & { return ring[(arr * PRING + slot(q)) * PL + yy * PEZ + zz]; };
+
+    auto issue = [&](int q) {
+        const bool qin = q >= 0 && q < d.nx;
+        for (int e = tid; e < PL; e += 256) {
+            const int yy = e / PEZ, zz = e - yy * PEZ;
+            const int y = y0 - 2 + yy, z = z0 - 2 + zz;
+            const bool v = qin && y >= 0 && y < d.ny && z >= 0 && z < d.nz;
+            const long long c = v ? cid(d, q, y, z) : 0;
+            if (MODE != 0) cp_async_elem(&E(0, q, yy, zz), xin + c, v, sizeof(T));
+            cp_async_elem(&E(1, q, yy, zz), cf.ax + c, v, sizeof(T));
+            cp_async_elem(&E(2, q, yy, zz), cf.ay + c, v, sizeof(T));
+            cp_async_elem(&E(3, q, yy, zz), cf.az + c, v, sizeof(T));
+            cp_async_elem(&E(4, q, yy, zz), dg + c, v, sizeof(T));
+            cp_async_elem(&E(5, q, yy, zz), b + c, v, sizeof(T));
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    auto wait1 = []() { asm volatile("cp.async.wait_group 1;" ::: "memory"); };
+
+    // one cell update from the staged planes: neighbours `xv(dx, dy, dz)`, couplings at E-index (ey, ez)
+    auto update = [&](int q, int y, int z, int ey, int ez, auto xv) -> T {
+        T s = 0, sum = 0;
+        if (MODE != 0 || true) {
+            if (q > 0) {
+                const T a = E(1, q, ey, ez);
+                s += a * xv(-1, 0, 0);
+                sum += a;
+            }
+            if (q < d.nx - 1) {
+                const T a = E(1, q + 1, ey, ez);
+                s += a * xv(1, 0, 0);
+                sum += a;
+            }
+            if (y > 0) {
+                const T a = E(2, q, ey, ez);
+                s += a * xv(0, -1, 0);
+                sum += a;
+            }
+            if (y < d.ny - 1) {
+                const T a = E(2, q, ey + 1, ez);
+                s += a * xv(0, 1, 0);
+                sum += a;
+            }
+            if (z > 0) {
+                const T a = E(3, q, ey, ez);
+                s += a * xv(0, 0, -1);
+                sum += a;
+            }
+            if (z < d.nz - 1) {
+                const T a = E(3, q, ey, ez + 1);
+                s += a * xv(0, 0, 1);
+                sum += a;
+            }
+        }
+        T inv;
+        if (sizeof(T) == 8) {
+            inv = E(4, q, ey, ez);
+        } else {
+            const T D = sum + E(4, q, ey, ez);
+            inv = D > T(0) ? T(1) / D : T(0);
+        }
+        return (E(5, q, ey, ez) + s) * inv;
+    };
+
+    auto compute_A = [&](int q) {
+        T(*dst)[RZ] = sa[mod3(q)];
+        const bool qin = q >= 0 && q < d.nx;
+        for (int e = tid; e < RY * (RZ / 2); e += 256) {
+            const int yy = e / (RZ / 2), pz = e - yy * (RZ / 2);
+            const int y = y0 - 1 + yy;
+            const int zz = 2 * pz + ((colA - q - y - z0 + 1) & 1);
+            const int z = z0 - 1 + zz;
+            T v = T(0);
+            if (qin && y >= 0 && y < d.ny && z >= 0 && z < d.nz) {
+                const int ey = yy + 1, ez = zz + 1;
+                if (MODE == 0) {
+                    T sum = 0;
+                    if (sizeof(T) != 8) {
+                        if (q > 0) sum += E(1, q, ey, ez);
+                        if (q < d.nx - 1) sum += E(1, q + 1, ey, ez);
+                        if (y > 0) sum += E(2, q, ey, ez);
+                        if (y < d.ny - 1) sum += E(2, q, ey + 1, ez);
+                        if (z > 0) sum += E(3, q, ey, ez);
+                        if (z < d.nz - 1) sum += E(3, q, ey, ez + 1);
+                    }
+                    T inv;
+                    if (sizeof(T) == 8) {
+                        inv = E(4, q, ey, ez);
+                    } else {
+                        const T D = sum + E(4, q, ey, ez);
+                        inv = D > T(0) ? T(1) / D : T(0);
+                    }
+                    v = (E(5, q, ey, ez) + T(0)) * inv;
+                } else {
+                    v = update(q, y, z, ey, ez, [&](int dx, int dy, int dz) -> T {
+                        return E(0, q + dx, ey + dy, ez + dz);
+                    });
+                }
+            }
+            dst[yy][zz] = v;
+        }
+    };
+    auto update_B = [&](int p) {
+        const int ty = threadIdx.y, y = y0 + ty;
+        if (y >= d.ny) return;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int tz = 2 * threadIdx.x + h, z = z0 + tz;
+            if (z >= d.nz) continue;
+            const long long c = cid(d, p, y, z);
+            const int ry = ty + 1, rz = tz + 1;
+            if (((p + y + z) & 1) == colA) {
+                xout[c] = sa[mod3(p)][ry][rz];
+                continue;
+            }
+            xout[c] = update(p, y, z, ty + 2, tz + 2, [&](int dx, int dy, int dz) -> T {
+                return sa[mod3(p + dx)][ry + dy][rz + dz];
+            });
+        }
+    };
+
+    issue(x0 - 2);
+    issue(x0 - 1);
+    issue(x0);
+    issue(x0 + 1);
+    wait1();  // planes x0-2 .. x0 staged
+    __syncthreads();
+    compute_A(x0 - 1);
+    __syncthreads();
+    issue(x0 + 2);  // slot of x0-2, last read by compute_A(x0-1)
+    wait1();        // x0+1 staged
+    __syncthreads();
+    compute_A(x0);
+    for (int q = x0 + 1; q <= x1; q++) {
+        __syncthreads();  // compute_A(q-1) and update_B(q-2) are complete
+        issue(q + 2);     // slot of plane q-2
+        wait1();          // plane q+1 staged
+        __syncthreads();
+        compute_A(q);
+        __syncthreads();
+        update_B(q - 1);
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
 // r = b - A x on the fine level, summed over each coarse cell's (up to) 8 children -> coarse rhs.
@@ -667,6 +851,24 @@ static inline int fused_chunk(const Dims &d) {
 template <class T, class C, int MODE>
 static void fused(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const Coef<C> &cf, const T *xin, T *xout,
                   const T *b) {
+    if constexpr (std::is_same<T, C>::value) {
+        if (fine) {
+            // pipelined kernel: two blocks (FP32) or one (FP64) per SM, blocks marching 32 planes
+            const long long tiles = (long long)((d.nz + FTZ - 1) / FTZ) * ((d.ny + FTY - 1) / FTY);
+            int chunk = 32;
+            while (chunk > 4 && tiles * ((d.nx + chunk - 1) / chunk) < 152 * 6) chunk /= 2;
+            if (chunk > d.nx) chunk = d.nx;
+            const dim3 g((d.nz + FTZ - 1) / FTZ, (d.ny + FTY - 1) / FTY, (d.nx + chunk - 1) / chunk);
+            const size_t smem = pipe_smem_bytes<T>();
+            cudaFuncSetAttribute(k_rbgs_pipe<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            const double s = sizeof(T);
+            const double per = (MODE == 0 ? 0.0 : s) + s + s + 3 * s + s;
+            tk.before(st, fine);
+            k_rbgs_pipe<T, MODE><<<g, dim3(32, 8), smem, st>>>(d, cf, xin, xout, b, chunk);
+            tk.after(st, fine, per * d.n);
+            return;
+        }
+    }
     const int chunk = fused_chunk(d);
     const dim3 g((d.nz + FTZ - 1) / FTZ, (d.ny + FTY - 1) / FTY, (d.nx + chunk - 1) / chunk);
     const double s = sizeof(C) == 8 ? 8.0 : 4.0;
@@ -745,14 +947,14 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
     smooth<T, C0>(st, tk, true, dims[0], c0, z, ts[0], r, p.pre, true);
     restrict_res<T, C0>(st, tk, dims[0], c0, z, r, dims[1], bs[1]);
     for (int l = 1; l < L - 1; l++) {
-        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], ts[l], bs[l], p.pre, true);
+        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.pre, true);
         restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1]);
     }
     coarse_solve<T, Cc>(st, tk, dims[L - 1], cc[L - 1], xs[L - 1], bs[L - 1], p.coarse_sweeps);
     for (int l = L - 2; l >= 1; l--) {
         tk.launches++;
         k_prolong<T><<<grid_cells(dims[l]), blk2(), 0, st>>>(dims[l], xs[l], dims[l + 1], xs[l + 1]);
-        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], ts[l], bs[l], p.post, false);
+        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.post, false);
     }
     tk.launches++;
     k_prolong<T><<<grid_cells(dims[0]), blk2(), 0, st>>>(dims[0], z, dims[1], xs[1]);

@@ -2,6 +2,9 @@
 #include <cmath>
 #include <cstring>
 
+#include <cudaTypedefs.h>
+
+#include "sf_conv_tc.cuh"
 #include "sf_unet.h"
 #include "sf_unet_kernels.cuh"
 
@@ -66,6 +69,71 @@ void conv_dispatch(cudaStream_t st, int ci, int co, int epi, const Dims &d, cons
 #undef CASE
 }
 
+// ------------------------------------------------------------------------------------------------ tcgen05 path
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// The tcgen05 kernel takes 32 (z) x 4 (y) bricks: grids smaller than one brick use the warp-MMA kernel.
+bool tc_shape_ok(int ci, int co, const Dims &d) {
+    const bool ch = (ci == 16 || ci == 32 || ci == 64) && (co == 16 || co == 32 || co == 64);
+    return ch && d.nz >= tc::kTileZ && d.ny >= tc::kTileY;
+}
+
+template <int CI, int CO>
+cudaError_t launch_tc(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *w, const float *b, bf16 *y,
+                      int *err) {
+    auto enc = tensor_map_encoder();
+    if (!enc || !aligned16(x) || !aligned16(w) || !aligned16(y)) return cudaErrorInvalidValue;
+    CUtensorMap mx, mw;
+    const cuuint64_t xd[4] = {(cuuint64_t)CI, (cuuint64_t)d.nz, (cuuint64_t)d.ny, (cuuint64_t)d.nx};
+    const cuuint64_t xs[3] = {(cuuint64_t)CI * 2, (cuuint64_t)d.nz * CI * 2, (cuuint64_t)d.ny * d.nz * CI * 2};
+    const cuuint32_t xb[4] = {8, tc::kTileZ, tc::kTileY, 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    if (enc(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(x), xd, xs, xb, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    const cuuint64_t wd[3] = {(cuuint64_t)CI, (cuuint64_t)CO, 27};
+    const cuuint64_t ws[2] = {(cuuint64_t)CI * 2, (cuuint64_t)CO * CI * 2};
+    const cuuint32_t wb[3] = {8, (cuuint32_t)CO, 1};
+    if (enc(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16 *>(w), wd, ws, wb, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    using L = tc::Layout<CI, CO>;
+    cudaError_t e = cudaFuncSetAttribute(tc::k_conv_tc<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)L::kSmemBytes);
+    if (e != cudaSuccess) return e;
+    const long long tiles = (long long)((d.nz + tc::kTileZ - 1) / tc::kTileZ) * ((d.ny + tc::kTileY - 1) / tc::kTileY) *
+                            d.nx;
+    if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+    tc::k_conv_tc<CI, CO><<<(unsigned)tiles, 128, L::kSmemBytes, st>>>(mx, mw, d, b, y, err);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_dispatch(cudaStream_t st, int ci, int co, const Dims &d, const bf16 *x, const bf16 *w, const float *b,
+                        bf16 *y, int *err) {
+#define CASE(A, B) \
+    if (ci == A && co == B) return launch_tc<A, B>(st, d, x, w, b, y, err);
+    CASE(16, 16) CASE(16, 32) CASE(32, 16) CASE(32, 32) CASE(32, 64) CASE(64, 32) CASE(64, 64)
+#undef CASE
+    return cudaErrorInvalidValue;
+}
+
 template <int CI, int CO>
 void launch_wgrad(cudaStream_t st, const Dims &d, const bf16 *dy, const bf16 *x, float *part, int taps, int vchunk,
                   int chunks) {
@@ -111,12 +179,14 @@ UNet::UNet(cudaStream_t st) : st_(st) {
     wpart_elems_ = 64LL * 27 * 64 * 64;
     wpart_ = (float *)alloc(4 * wpart_elems_);
     hpart_ = (float *)alloc(4 * 4096 * 17);
+    err_ = (int *)alloc(256);
     cudaMallocHost(&dots_host_, 8 * 8);
     if (p_) {
         cudaMemsetAsync(p_, 0, 4 * nparams_, st_);
         cudaMemsetAsync(m1_, 0, 4 * nparams_, st_);
         cudaMemsetAsync(m2_, 0, 4 * nparams_, st_);
         cudaMemsetAsync(dots_, 0, 64, st_);
+        cudaMemsetAsync(err_, 0, 256, st_);
     }
 }
 
@@ -210,7 +280,29 @@ cudaError_t UNet::ensure(const Dims &d) {
 }
 
 void UNet::conv_fwd(const ConvLayer &L, const Dims &d, const bf16 *x, bf16 *y) {
+    if (mode_ == 1 && L.taps == 27 && tc_shape_ok(L.cin, L.cout, d)) {
+        cudaError_t e = tc_dispatch(st_, L.cin, L.cout, d, x, wb_ + L.wbf, p_ + L.boff, y, err_);
+        if (e == cudaSuccess) {
+            tc_launches_++;
+            return;
+        }
+        last_error = std::string("tcgen05 convolution not launched: ") + cudaGetErrorString(e);
+    }
     conv_dispatch(st_, L.cin, L.cout, 0, d, x, wb_ + L.wbf, p_ + L.boff, y, L.taps);
+}
+
+cudaError_t UNet::check_device_errors() {
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, err_, sizeof(int), cudaMemcpyDeviceToHost, st_);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return e;
+    if (h != 0) {
+        last_error = "tcgen05 convolution: a bounded wait timed out";
+        cudaMemsetAsync(err_, 0, sizeof(int), st_);
+        return cudaErrorLaunchFailure;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t UNet::forward(const Dims &d, const bf16 *feat, float *out) {

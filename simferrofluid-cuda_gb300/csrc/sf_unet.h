@@ -46,6 +46,12 @@ class UNet {
     // the 16 input channels of a system in face-coefficient form (FP64 fine level) with rhs b
     cudaError_t features(const Dims &d, const Coef<double> &cf, const double *b, __nv_bfloat16 *feat);
     float *output() { return out_; }
+    // convolution kernels of the forward pass: 0 warp-level MMA (mma.sync), 1 tcgen05 + TMA
+    void set_mode(int m) { mode_ = m; }
+    int mode() const { return mode_; }
+    long long tc_launches() const { return tc_launches_; }
+    // reads (and clears) the device error flag of the tcgen05 kernels; synchronises the stream
+    cudaError_t check_device_errors();
 
     std::string last_error;
 
@@ -76,6 +82,9 @@ class UNet {
     float *out_ = nullptr, *dout_ = nullptr, *wpart_ = nullptr, *hpart_ = nullptr;
     double *dots_ = nullptr, *dots_host_ = nullptr, *redpart_ = nullptr;
     long long wpart_elems_ = 0;
+    int mode_ = 0;
+    int *err_ = nullptr;
+    long long tc_launches_ = 0;
 };
 
 }  // namespace sf
