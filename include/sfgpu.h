@@ -45,8 +45,9 @@ typedef enum {
 typedef enum {
     SF_PREC_FP64 = 0,   /* plain method: FP64 MGPCG */
     SF_PREC_MIXED = 1,  /* FP32 V-cycle, FP16 coarse coefficients, inner FP32 FCG, FP64 iterative refinement */
-    SF_PREC_LEARNED = 2 /* mixed form started from the attached U-Net's scaled prediction (sf_set_network);
-                           a prediction worse than zero is discarded (SF_STALLED_FALLBACK) */
+    SF_PREC_LEARNED = 2 /* mixed form started from the attached U-Net's prediction y scaled by
+                           gamma = (y,b)/(y,Ay) (never a larger A-norm error than zero); a non-finite
+                           prediction is discarded and the solve starts from zero (SF_STALLED_FALLBACK) */
 } sf_precision;
 
 /* Cell grid of a staggered grid: resolution, spacing and corner (StaggeredGrid ctor,
@@ -93,6 +94,7 @@ typedef struct {
     long long kernel_launches; /* kernels this call launched (graph nodes counted per replay) */
     double smooth_bytes;     /* profile: algorithmic bytes of the timed smoother launches */
     double guess_rel_residual; /* learned form: ||b - A x0|| / ||b|| of the network's initial guess (-1: none) */
+    double guess_energy_ratio; /* learned form: ||x* - x0||_A^2 / ||x*||_A^2 of that guess (-1: none) */
 } sf_solve_stats;
 
 /* ----- context ------------------------------------------------------------------------------------------- */

@@ -53,7 +53,7 @@ class sf_solve_stats(C.Structure):
                 ("ms_total", C.c_double), ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong),
                 ("status_detail", C.c_int), ("smooth_launches", C.c_int), ("smooth_ms", C.c_double),
                 ("kernel_launches", C.c_longlong), ("smooth_bytes", C.c_double),
-                ("guess_rel_residual", C.c_double)]
+                ("guess_rel_residual", C.c_double), ("guess_energy_ratio", C.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}

@@ -123,6 +123,7 @@ void fill_stats(sf_solve_stats *s, const SolveResult &r, long long unknowns) {
     s->smooth_ms = r.smooth_ms;
     s->smooth_bytes = r.smooth_bytes;
     s->guess_rel_residual = r.guess_relres;
+    s->guess_energy_ratio = r.guess_energy;
 }
 
 float ev_ms(cudaEvent_t a, cudaEvent_t b) {

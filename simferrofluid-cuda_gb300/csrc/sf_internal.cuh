@@ -130,16 +130,42 @@ __device__ __forceinline__ void warp_sum(double (&v)[K]) {
         for (int q = 0; q < K; q++) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
 }
 
-// Returns true in exactly one thread (linear thread 0 of the last block), with `tot` holding the grid totals.
-// Blocks must have kRedThreads threads (any shape); `tid` is the linear thread index.
+// Fixed-order tree sum of one value per thread over a kRedThreads block; result valid in tid 0.
+template <int K>
+__device__ __forceinline__ void block_sum(double (&acc)[K], int tid) {
+    __shared__ double sh2[K][kRedThreads];
+#pragma unroll
+    for (int q = 0; q < K; q++) sh2[q][tid] = acc[q];
+    __syncthreads();
+    for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+        if (tid < s)
+#pragma unroll
+            for (int q = 0; q < K; q++) sh2[q][tid] += sh2[q][tid + s];
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < K; q++) acc[q] = sh2[q][0];
+    __syncthreads();
+}
+
+constexpr int kRedGroup = 256;  // blocks per first-level group
+
+// Deterministic grid-wide sum.  Blocks write partials; the last block of each group of kRedGroup blocks sums
+// its group in block order; the last group to finish sums the group partials in group order.  Returns true in
+// exactly one thread (linear thread 0 of that block) with `tot` holding the totals.  Blocks must have
+// kRedThreads threads (any shape).  part: K * (nblk + ngroups) doubles; ticket: 1 + ngroups counters, zero on
+// entry and re-armed on exit.
 template <int K>
 __device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, unsigned *ticket, double (&tot)[K]) {
     __shared__ double sh[K][kRedThreads / 32];
-    __shared__ double sh2[K][kRedThreads];
     __shared__ bool last;
     const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     const int nblk = gridDim.x * gridDim.y * gridDim.z;
     const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const int ngroups = (nblk + kRedGroup - 1) / kRedGroup;
+    const int grp = bid / kRedGroup;
+    const int gsize = min(kRedGroup, nblk - grp * kRedGroup);
+    double *gpart = part + (long long)K * nblk;
     warp_sum<K>(v);
     const int lane = tid & 31, wid = tid >> 5;
     if (lane == 0)
@@ -154,31 +180,40 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, unsign
             part[(long long)q * nblk + bid] = b;
         }
         __threadfence();
-        unsigned t = atomicAdd(ticket, 1u);
-        last = (t == (unsigned)nblk - 1);
+        const unsigned t = atomicAdd(&ticket[1 + grp], 1u);
+        last = (t == (unsigned)gsize - 1);
     }
     __syncthreads();
     if (!last) return false;
+    // last block of the group: sum the group's partials in block order
     __threadfence();
     double acc[K];
 #pragma unroll
-    for (int q = 0; q < K; q++) acc[q] = 0;
-    for (int b = tid; b < nblk; b += kRedThreads)
+    for (int q = 0; q < K; q++)
+        acc[q] = tid < gsize ? ((volatile double *)part)[(long long)q * nblk + grp * kRedGroup + tid] : 0.0;
+    block_sum<K>(acc, tid);
+    if (tid == 0) {
 #pragma unroll
-        for (int q = 0; q < K; q++) acc[q] += ((volatile double *)part)[(long long)q * nblk + b];
-#pragma unroll
-    for (int q = 0; q < K; q++) sh2[q][tid] = acc[q];
-    __syncthreads();
-    for (int s = kRedThreads / 2; s > 0; s >>= 1) {
-        if (tid < s)
-#pragma unroll
-            for (int q = 0; q < K; q++) sh2[q][tid] += sh2[q][tid + s];
-        __syncthreads();
+        for (int q = 0; q < K; q++) gpart[(long long)q * ngroups + grp] = acc[q];
+        ticket[1 + grp] = 0u;
+        __threadfence();
+        const unsigned t = atomicAdd(&ticket[0], 1u);
+        last = (t == (unsigned)ngroups - 1);
     }
+    __syncthreads();
+    if (!last) return false;
+    // last group: sum the group partials in group order
+    __threadfence();
+#pragma unroll
+    for (int q = 0; q < K; q++) acc[q] = 0;
+    for (int g = tid; g < ngroups; g += kRedThreads)
+#pragma unroll
+        for (int q = 0; q < K; q++) acc[q] += ((volatile double *)gpart)[(long long)q * ngroups + g];
+    block_sum<K>(acc, tid);
     if (tid != 0) return false;
 #pragma unroll
-    for (int q = 0; q < K; q++) tot[q] = sh2[q][0];
-    *ticket = 0u;  // re-arm for the next launch on the same stream
+    for (int q = 0; q < K; q++) tot[q] = acc[q];
+    ticket[0] = 0u;
     return true;
 }
 

@@ -800,6 +800,16 @@ __global__ void k_scale_to64(long long n, double g, const float *__restrict__ y,
         x[c] = g * (double)y[c];
 }
 
+// (a, b) of two FP64 vectors -> slot
+__global__ void __launch_bounds__(256) k_dot_dd(long long n, const double *__restrict__ a, const double *__restrict__ b,
+                                                int slot, double *sc, double *part, unsigned *ticket) {
+    double v[1] = {0};
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) v[0] += a[c] * b[c];
+    double tot[1];
+    if (grid_reduce<1>(v, part, ticket, tot)) sc[slot] = tot[0];
+}
+
 // x64 += d32
 __global__ void k_ir_update(long long n, double *__restrict__ x, const float *__restrict__ dlt) {
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
@@ -1035,8 +1045,8 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     x_ = (double *)chk(A(8 * n));
     b_ = (double *)chk(A(8 * n));
     sc_ = (double *)chk(A(8 * S_NSLOTS));
-    part_ = (double *)chk(A(8 * 4 * (size_t)(kMaxTileBlocks > kMaxRedBlocks ? kMaxTileBlocks : kMaxRedBlocks)));
-    ticket_ = (unsigned *)chk(A(256));
+    part_ = (double *)chk(A(8 * 4 * (size_t)(kMaxTileBlocks + kMaxTileBlocks / kRedGroup + 1)));
+    ticket_ = (unsigned *)chk(A(4 * (size_t)(2 + kMaxTileBlocks / kRedGroup)));
     if (p.precision == 0) {
         x64_.assign(L, nullptr);
         b64_.assign(L, nullptr);
@@ -1090,7 +1100,7 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     }
     cudaError_t e = cudaMallocHost(&sc_host_, 8 * S_NSLOTS);
     if (e != cudaSuccess) return e;
-    cudaMemsetAsync(ticket_, 0, 256, st_);
+    cudaMemsetAsync(ticket_, 0, 4 * (size_t)(2 + kMaxTileBlocks / kRedGroup), st_);
     cudaMemsetAsync(sc_, 0, 8 * S_NSLOTS, st_);
     cudaMemsetAsync(x_, 0, 8 * n, st_);
     configured_ = true;
@@ -1306,10 +1316,11 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
             }
         }
         if (guess_) {
-            // a supplied initial guess that is worse than zero (or not finite) is discarded
+            // x0 = gamma y never has a larger A-norm error than zero (gamma minimises it along y); it is
+            // discarded only when it is not finite
             guess_ = false;
             res.guess_relres = std::sqrt(rr / bb);
-            if (!(rr <= bb)) {
+            if (!std::isfinite(rr) || !(guess_yb_ != 0.0)) {
                 res.fallback = true;
                 cudaMemsetAsync(x_, 0, 8 * n, st_);
                 x_zero = true;
@@ -1363,6 +1374,14 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
     res.outer = outer;
     res.relres = std::sqrt(rr / bb);
     res.converged = res.relres <= prm_.tol;
+    if (res.guess_relres >= 0 && !res.fallback && guess_yay_ > 0) {
+        // A-norm error of the guess relative to zero: 1 - (y,b)^2 / ((y,Ay) (b,x*)), x* = the solution
+        k_dot_dd<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, b_, x_, S_AUX2, sc_, part_, ticket_);
+        tk_.launches++;
+        if ((e = read_slots()) != cudaSuccess) return e;
+        const double bx = sc_host_[S_AUX2];
+        if (bx > 0) res.guess_energy = 1.0 - guess_yb_ * guess_yb_ / (guess_yay_ * bx);
+    }
     return cudaGetLastError();
 }
 
@@ -1379,6 +1398,8 @@ cudaError_t MGSolver::set_guess_scaled(const float *y, double &gamma) {
     if (e != cudaSuccess) return e;
     const double yay = sc_host_[S_PQ], yb = sc_host_[S_AUX2];
     gamma = (yay > 0 && std::isfinite(yay) && std::isfinite(yb)) ? yb / yay : 0.0;
+    guess_yb_ = std::isfinite(gamma) ? yb : 0.0;
+    guess_yay_ = yay;
     k_scale_to64<<<flat_grid(d.n), 256, 0, st_>>>(d.n, gamma, y, x_);
     tk_.launches++;
     guess_ = true;

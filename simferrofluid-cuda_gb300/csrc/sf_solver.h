@@ -53,6 +53,7 @@ struct SolveResult {
     bool breakdown = false;
     bool fallback = false;      // the supplied initial guess was discarded
     double guess_relres = -1;   // relative residual of the supplied initial guess
+    double guess_energy = -1;   // its squared A-norm error relative to that of zero
     double relres = 0, bnorm = 0;
 };
 
@@ -123,6 +124,7 @@ class MGSolver {
     size_t bytes_ = 0;
     bool configured_ = false;
     bool guess_ = false;
+    double guess_yb_ = 0, guess_yay_ = 0;
     Dims cfg_dims_{0, 0, 0, 0};
     int cfg_prec_ = -1, cfg_levels_ = -1, cfg_cdim_ = -1;
 
@@ -162,7 +164,7 @@ class MGSolver {
 
 // Launch helpers
 constexpr int kMaxRedBlocks = 152 * 8;
-constexpr int kMaxTileBlocks = 16384;
+constexpr int kMaxTileBlocks = 65536;
 dim3 tile_grid(const Dims &d, int &xpb);
 
 }  // namespace sf

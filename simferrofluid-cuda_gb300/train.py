@@ -132,12 +132,13 @@ def evaluate(ctx, net, scenes=64, n=256, seed=777, tol=1e-6, log=None):
             t = time.perf_counter()
             st = src.solve(inp, prec, tol)
             res[prec] = dict(iters=st["iters"], outer=st["outer_iters"], ms=1e3 * (time.perf_counter() - t),
-                             relres=st["rel_residual"], guess=st["guess_rel_residual"])
+                             relres=st["rel_residual"], guess=st["guess_rel_residual"],
+                             energy=st["guess_energy_ratio"])
         rows.append(dict(kind=i % 2, **res))
         if log:
             log(f"scene {i:3d} kind {i % 2} plain {res['mixed']['iters']:3d} it {res['mixed']['ms']:7.2f} ms | "
                 f"learned {res['learned']['iters']:3d} it {res['learned']['ms']:7.2f} ms guess "
-                f"{res['learned']['guess']:.3f}")
+                f"{res['learned']['guess']:.3f} energy {res['learned']['energy']:.3f}")
     return rows
 
 
@@ -154,6 +155,7 @@ def summarize(rows):
             "plain_ms": float(np.mean([r["mixed"]["ms"] for r in rs])),
             "learned_ms": float(np.mean([r["learned"]["ms"] for r in rs])),
             "guess_rel_residual": float(np.mean([r["learned"]["guess"] for r in rs])),
+            "guess_energy_ratio": float(np.mean([r["learned"]["energy"] for r in rs])),
             "plain_solves_per_s": float(1e3 / np.mean([r["mixed"]["ms"] for r in rs])),
             "learned_solves_per_s": float(1e3 / np.mean([r["learned"]["ms"] for r in rs])),
         }

@@ -98,7 +98,8 @@ def test_learned_solve_converges_and_falls_back(sfpkg, oracle, gpu_ctx, ref):
     assert st["converged"] == 1 and st["rel_residual"] <= 1e-8 * 1.01
     assert rel_l2(P.pressure[liq], p_or[liq]) <= 1e-5
     assert st["guess_rel_residual"] >= 0
-    # garbage network: huge head weights make the prediction overflow -> discarded
+    assert 0.0 <= st["guess_energy_ratio"] <= 1.0 + 1e-9  # gamma scaling: never worse than zero in A-norm
+    # garbage network: huge weights make the prediction overflow to non-finite values -> discarded
     flat = ref.flatten(ref.init_params(16, seed=1))
     flat[:] = 1e30
     net.set_params(flat)
