@@ -551,6 +551,59 @@ __global__ void __launch_bounds__(256) k_prolong(Dims d, T *__restrict__ x, Dims
 }
 
 // Coarsest level: one block, x = 0 then the palindromic sequence red, (black, red) x pairs.
+// Grids of at most kCoarseMax cells keep x in shared memory and each thread's couplings, inverse diagonal and
+// right-hand side in registers, so the sweeps touch no global memory; larger grids sweep in global memory.
+constexpr int kCoarseMax = 1024, kCoarseThreads = 1024;
+
+template <class T, class C>
+__global__ void __launch_bounds__(kCoarseThreads) k_coarse_smem(Dims d, Coef<C> cf, T *__restrict__ x,
+                                                                const T *__restrict__ b, int pairs) {
+    using R = typename Acc<C>::T;
+    __shared__ T xs[kCoarseMax];
+    const int sx = d.ny * d.nz, sy = d.nz;
+    const int c = threadIdx.x;
+    R a[6], inv = 0, bc = 0;
+    int has = 0, col = -1;
+    if (c < d.n) {
+        const int k = c % d.nz, j = (c / d.nz) % d.ny, i = c / (d.nz * d.ny);
+        col = (i + j + k) & 1;
+        // neighbour order and guards of nbsum: -x, +x, -y, +y, -z, +z
+        has = (i > 0) | ((i < d.nx - 1) << 1) | ((j > 0) << 2) | ((j < d.ny - 1) << 3) | ((k > 0) << 4) |
+              ((k < d.nz - 1) << 5);
+        R sum = 0;
+#pragma unroll
+        for (int f = 0; f < 6; f++) {
+            const C *arr = f < 2 ? cf.ax : (f < 4 ? cf.ay : cf.az);
+            const int st = f < 2 ? sx : (f < 4 ? sy : 1);
+            R av = 0;
+            if (has & (1 << f)) {
+                av = (R)ldv(arr, (f & 1) ? c + st : c);  // lower faces stored at c, upper at the neighbour
+                if (sizeof(C) == 2) av *= (R)cf.unscale;
+                sum += av;
+            }
+            a[f] = av;
+        }
+        inv = inv_diag<C>(cf, c, sum);
+        bc = (R)b[c];
+        xs[c] = T(0);
+    }
+    __syncthreads();
+    const int nh = 1 + 2 * pairs;
+    for (int h = 0; h < nh; h++) {
+        if (col == (h & 1)) {
+            R s = 0;
+#pragma unroll
+            for (int f = 0; f < 6; f++) {
+                const int st = f < 2 ? sx : (f < 4 ? sy : 1);
+                if (has & (1 << f)) s += a[f] * (R)xs[(f & 1) ? c + st : c - st];
+            }
+            xs[c] = (T)((bc + s) * inv);
+        }
+        __syncthreads();
+    }
+    if (c < d.n) x[c] = xs[c];
+}
+
 template <class T, class C>
 __global__ void __launch_bounds__(1024) k_coarse(Dims d, Coef<C> cf, T *__restrict__ x, const T *__restrict__ b,
                                                  int pairs) {
@@ -939,6 +992,10 @@ static void restrict_res(cudaStream_t st, Tracker &tk, const Dims &d, const Coef
 template <class T, class C>
 static void coarse_solve(cudaStream_t st, Tracker &tk, const Dims &d, const Coef<C> &cf, T *x, const T *b, int pairs) {
     tk.launches++;
+    if (d.n <= kCoarseMax) {
+        k_coarse_smem<T, C><<<1, kCoarseThreads, 0, st>>>(d, cf, x, b, pairs);
+        return;
+    }
     int nt = d.n >= 1024 ? 1024 : (int)((d.n + 31) / 32 * 32);
     k_coarse<T, C><<<1, nt, 0, st>>>(d, cf, x, b, pairs);
 }
