@@ -45,10 +45,12 @@ void DevBuf::release() {
     n_ = 0;
 }
 
+// At most kMaxTileBlocks / tiles blocks along x, so the grid never exceeds kMaxTileBlocks blocks (the size
+// of the reduction partials) for any cross-section of up to kMaxTileBlocks tiles (checked in configure).
 dim3 tile_grid(const Dims &d, int &xpb) {
     const long long tiles = (long long)((d.nz + 31) / 32) * ((d.ny + 7) / 8);
-    long long x = (tiles * d.nx + kMaxTileBlocks - 1) / kMaxTileBlocks;
-    xpb = (int)(x < 1 ? 1 : x);
+    const long long zmax = tiles < kMaxTileBlocks ? kMaxTileBlocks / tiles : 1;
+    xpb = (int)((d.nx + zmax - 1) / zmax);
     return dim3((d.nz + 31) / 32, (d.ny + 7) / 8, (d.nx + xpb - 1) / xpb);
 }
 
@@ -1063,6 +1065,10 @@ void *MGSolver::alloc(size_t bytes) {
 size_t MGSolver::device_bytes() const { return bytes_; }
 
 cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
+    if ((long long)((d.nz + 31) / 32) * ((d.ny + 7) / 8) > kMaxTileBlocks) {
+        last_error = "grid cross-section above 65536 tiles of 32 (z) x 8 (y) cells";
+        return cudaErrorInvalidValue;
+    }
     // level dims
     std::vector<Dims> dims{d};
     const int cdim = p.coarse_dim > 0 ? p.coarse_dim : 8;
