@@ -1066,7 +1066,7 @@ size_t MGSolver::device_bytes() const { return bytes_; }
 
 cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     if ((long long)((d.nz + 31) / 32) * ((d.ny + 7) / 8) > kMaxTileBlocks) {
-        last_error = "grid cross-section above 65536 tiles of 32 (z) x 8 (y) cells";
+        last_error = "grid cross-section above 16384 tiles of 32 (z) x 8 (y) cells";
         return cudaErrorInvalidValue;
     }
     // level dims

@@ -164,7 +164,7 @@ class MGSolver {
 
 // Launch helpers
 constexpr int kMaxRedBlocks = 152 * 8;
-constexpr int kMaxTileBlocks = 65536;
+constexpr int kMaxTileBlocks = 16384;
 dim3 tile_grid(const Dims &d, int &xpb);
 
 }  // namespace sf
