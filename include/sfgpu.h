@@ -39,7 +39,8 @@ typedef enum {
     SF_NO_DEVICE = 4,       /* no CUDA device, or the device is not sm_103 */
     SF_OUT_OF_MEMORY = 5,
     SF_STALLED_FALLBACK = 6, /* learned solve stalled; the plain MGPCG finished the solve (not an error) */
-    SF_NOT_READY = 7        /* Reproject called before any Project on this context / grid */
+    SF_NOT_READY = 7,       /* Reproject called before any Project on this context / grid */
+    SF_TOO_LARGE = 8        /* grid exceeds the fixed scratch of sf_magnetic_residual_noalloc */
 } sf_status;
 
 typedef enum {
@@ -203,6 +204,31 @@ SF_EXPORT sf_status sf_system_features_dev(void *ctx, int which, void *features_
 
 /* Forget the magnetic warm start (MagneticField ctor zeroes m_Sol, core/MagneticField.cpp:26). */
 SF_EXPORT sf_status sf_magnetic_reset(void *ctx);
+
+/* ----- allocation-free residual check ------------------------------------------------------------------------
+ * No counterpart in the reference: its solvers allocate freely and report only the residual of their own
+ * iterate.  This entry point measures any potential psi (from this library, from the reference's amgcl path, a
+ * warm start, ...) against the reference's pinned FDM system (core/MagneticField.cpp:62-118; row 0 is psi_0 = 0,
+ * b_0 = 0) and writes, on `stream`, result[0] = ||b - A psi|| / ||b|| (||r|| when b = 0) and result[1] = ||b||.
+ * mu and b are formed on the fly from phi, chi, band_width and hext as sf_magnetic_solve forms them.
+ *
+ * It allocates nothing: no cudaMalloc/cudaFree, no context, no staging copies.  It is for callers that cannot
+ * allocate -- a step loop whose device memory is fully reserved by its own pool (an allocation could fail), code
+ * that must not stall its other streams (cudaFree synchronises the device, cudaMalloc may), and the reference's
+ * own FDM step checking its potential without creating a context (sf_create allocates the solver workspaces).
+ * The reduction's scratch is a file-scope device array of about 130 KB per device.
+ *
+ * All pointers are device pointers on the calling thread's current device; `stream` (NULL = default stream)
+ * belongs to that device.  The call is asynchronous: result is valid once the stream reaches it.
+ * Limit: ceil(ny/8) * ceil(nz/32) <= SF_NOALLOC_MAX_BLOCKS tiles per x-plane (e.g. ny, nz <= 1024, or ny = 2048
+ * with nz = 1024); nx is free.  Larger grids return SF_TOO_LARGE without touching the device.
+ * The first call on each device looks up the scratch's address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  Calls that overlap on the GPU (in flight on two
+ * streams at once, or from two threads) share the scratch and race: order them on one stream. */
+#define SF_NOALLOC_MAX_BLOCKS 8192
+SF_EXPORT sf_status sf_magnetic_residual_noalloc(void *stream, const sf_grid *g, const double *phi, double chi,
+                                                 double band_width, const double *const hext[3], const double *psi,
+                                                 double *result);
 
 #ifdef __cplusplus
 }

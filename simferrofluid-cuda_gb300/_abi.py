@@ -18,6 +18,8 @@ SF_NO_DEVICE = 4
 SF_OUT_OF_MEMORY = 5
 SF_STALLED_FALLBACK = 6
 SF_NOT_READY = 7
+SF_TOO_LARGE = 8
+SF_NOALLOC_MAX_BLOCKS = 8192
 
 SF_PREC_FP64 = 0
 SF_PREC_MIXED = 1
@@ -30,7 +32,7 @@ EXPORTED = [
     "sf_collider_box_fractions", "sf_collider_face_fractions",
     "sf_unet_create", "sf_unet_destroy", "sf_unet_num_params", "sf_unet_set_params", "sf_unet_get_params",
     "sf_unet_forward_dev", "sf_unet_backward_dev", "sf_unet_train_step_dev", "sf_set_network",
-    "sf_system_features_dev", "sf_unet_set_mode", "sf_unet_tc_launches",
+    "sf_system_features_dev", "sf_unet_set_mode", "sf_unet_tc_launches", "sf_magnetic_residual_noalloc",
 ]
 
 
@@ -100,6 +102,8 @@ def load(path: str | None = None):
         f.restype = C.c_int
     L.sf_magnetic_reset.argtypes = [V]
     L.sf_magnetic_reset.restype = C.c_int
+    L.sf_magnetic_residual_noalloc.argtypes = [V, G, V, C.c_double, C.c_double, _P3, V, V]
+    L.sf_magnetic_residual_noalloc.restype = C.c_int
     L.sf_collider_box_fractions.argtypes = [G, C.c_int, _P3, V]
     L.sf_collider_box_fractions.restype = C.c_int
     L.sf_collider_face_fractions.argtypes = [G, V, _P3]

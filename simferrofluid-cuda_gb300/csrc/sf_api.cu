@@ -371,6 +371,7 @@ const char *sf_status_string(int s) {
         case SF_OUT_OF_MEMORY: return "out of device memory";
         case SF_STALLED_FALLBACK: return "learned solve stalled; plain MGPCG finished it";
         case SF_NOT_READY: return "no previous projection on this context";
+        case SF_TOO_LARGE: return "grid exceeds the allocation-free scratch (ceil(ny/8)*ceil(nz/32) > 8192)";
         default: return "unknown status";
     }
 }
@@ -491,6 +492,36 @@ sf_status sf_magnetic_solve_dev(void *ctx, const sf_grid *g, const double *phi, 
                                 const sf_solve_opts *opts, sf_solve_stats *stats) {
     return magnetic_impl(C(ctx), g, phi, chi, band_width, hext, psi_out, H_out, opts, stats, true);
 }
+sf_status sf_magnetic_residual_noalloc(void *stream, const sf_grid *g, const double *phi, double chi,
+                                       double band_width, const double *const hext[3], const double *psi,
+                                       double *result) {
+    static_assert(SF_NOALLOC_MAX_BLOCKS == 8192, "scratch size of sf_ops.cu");
+    if (!grid_ok(g) || !phi || !hext || !psi || !result || !std::isfinite(chi) || !(band_width > 0) ||
+        !std::isfinite(band_width))
+        return SF_BAD_ARG;
+    for (int a = 0; a < 3; a++)
+        if (!hext[a]) return SF_BAD_ARG;
+    const Dims d = make_dims(g->nx, g->ny, g->nz);
+    if (!noalloc_fits(d)) return SF_TOO_LARGE;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return SF_NO_DEVICE;
+    const void *ptrs[6] = {phi, psi, result, hext[0], hext[1], hext[2]};
+    for (const void *p : ptrs) {  // device (or managed) memory of the current device only
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+            cudaGetLastError();
+            return SF_BAD_ARG;
+        }
+        if ((at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) ||
+            (at.type == cudaMemoryTypeDevice && at.device != dev))
+            return SF_BAD_ARG;
+    }
+    Faces fh{{hext[0], hext[1], hext[2]}};
+    const cudaError_t e = launch_magnetic_residual_noalloc((cudaStream_t)stream, d, phi, chi, band_width, fh, g->h,
+                                                           psi, result);
+    return e == cudaSuccess ? SF_OK : SF_CUDA_ERROR;
+}
+
 sf_status sf_magnetic_reset(void *ctx) {
     Ctx *c = C(ctx);
     if (!c) return SF_BAD_ARG;

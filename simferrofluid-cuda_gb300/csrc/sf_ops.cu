@@ -5,6 +5,7 @@
 // assembly on the same inputs, and the velocity / field updates are too.
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "sf_ops.h"
 
@@ -245,6 +246,69 @@ __global__ void __launch_bounds__(256) k_total_field(Dims d, int a, const double
     H[f] = v;
 }
 
+// ---------------------------------------------------------------------------------- allocation-free residual
+// Scratch of the allocation-free residual: the deterministic reduction's block partials (2 sums per block and
+// per group of kRedGroup blocks) and its tickets.  File-scope device memory (about 130 KB), so a call
+// allocates nothing.  One copy per device; calls that overlap on the GPU share it and race.
+constexpr int kNoAllocBlocks = 8192;  // = SF_NOALLOC_MAX_BLOCKS of the C ABI
+constexpr int kNoAllocGroups = (kNoAllocBlocks + kRedGroup - 1) / kRedGroup;
+static __device__ __align__(256) double g_noalloc_part[2 * (kNoAllocBlocks + kNoAllocGroups)];
+static __device__ __align__(256) unsigned g_noalloc_ticket[1 + kNoAllocGroups];
+
+// ||b - A psi|| / ||b|| on the reference's pinned system (core/MagneticField.cpp:62-118): row 0 is psi_0 = 0
+// with b_0 = 0, the other rows drop column 0.  mu, D and b are formed per cell exactly as k_magnetic_mu and
+// k_magnetic_rows form them (each face value is evaluated by both of its cells), so nothing is stored.
+// Tiles of 32 (z) x 8 (y) cells, `xpb` x-planes per block; result[0] = relative residual, result[1] = ||b||.
+__global__ void __launch_bounds__(256) k_magnetic_residual(Dims d, int xpb, const double *__restrict__ phi,
+                                                           double chi, double bw, long long khi, long long klo,
+                                                           double one_plus_chi, Faces hext, double h,
+                                                           const double *__restrict__ psi, double *part,
+                                                           unsigned *ticket, double *result) {
+    double v[2] = {0., 0.};  // (r, r), (b, b)
+    const int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+    if (k < d.nz && j < d.ny) {
+        const long long sx = (long long)d.ny * d.nz, sy = d.nz;
+        const int i_end = min(d.nx, (int)(blockIdx.z + 1) * xpb);
+        for (int i = blockIdx.z * xpb; i < i_end; i++) {
+            const long long c = cid(d, i, j, k);
+            if (c == 0) {  // pinned row: 1 * psi_0 = 0
+                const double r0 = -psi[0];
+                v[0] += r0 * r0;
+                continue;
+            }
+            const double pc = phi[c];
+            double diag = 0., rhs = 0., s = 0.;
+#pragma unroll
+            for (int ord = 0; ord < 6; ord++) {  // -x, +x, -y, +y, -z, +z
+                const int a = ord >> 1, up = ord & 1;
+                const int ia = a == 0 ? i : (a == 1 ? j : k);
+                const int na = a == 0 ? d.nx : (a == 1 ? d.ny : d.nz);
+                if (up ? (ia >= na - 1) : (ia <= 0)) continue;
+                const long long st = a == 0 ? sx : (a == 1 ? sy : 1);
+                const long long nb = up ? c + st : c - st;
+                const double pn = phi[nb];
+                const double mu = up ? mu_face_fast(pc, pn, chi, bw, khi, klo, one_plus_chi)
+                                     : mu_face_fast(pn, pc, chi, bw, khi, klo, one_plus_chi);
+                diag += mu;
+                if (mu != 1.) {
+                    const int fi = i + (a == 0) * up, fj = j + (a == 1) * up, fk = k + (a == 2) * up;
+                    const double side = up ? 1.0 : -1.0;
+                    rhs += (mu - 1.) * hext.p[a][fid(d, a, fi, fj, fk)] * (-side) * h;
+                }
+                if (nb != 0) s += mu * psi[nb];
+            }
+            const double rc = (rhs - diag * psi[c]) + s;
+            v[0] += rc * rc;
+            v[1] += rhs * rhs;
+        }
+    }
+    double tot[2];
+    if (grid_reduce<2>(v, part, ticket, tot)) {
+        result[0] = tot[1] > 0. ? sqrt(tot[0] / tot[1]) : sqrt(tot[0]);
+        result[1] = sqrt(tot[1]);
+    }
+}
+
 __global__ void k_copy(long long n, const double *__restrict__ a, double *__restrict__ o) {
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
         o[c] = a[c];
@@ -289,6 +353,63 @@ int launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, dou
     k_magnetic_mu<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, chi, bw, key(t), key(-t), one_plus_chi, cf);
     k_magnetic_rows<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, hext, h, cf, b, want_invd ? 1 : 0);
     return 2;
+}
+
+bool noalloc_fits(const Dims &d) {
+    return (long long)((d.nz + 31) / 32) * ((d.ny + 7) / 8) <= kNoAllocBlocks;
+}
+
+// Device addresses of the scratch, looked up once per device (with that device current) and cached.
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double *g_noalloc_part_ptr[kNoAllocMaxDevices];
+unsigned *g_noalloc_ticket_ptr[kNoAllocMaxDevices];
+
+cudaError_t noalloc_scratch(double **part, unsigned **ticket) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_part_ptr[dev]) {
+        void *p = nullptr, *t = nullptr;
+        if ((e = cudaGetSymbolAddress(&p, g_noalloc_part)) != cudaSuccess) return e;
+        if ((e = cudaGetSymbolAddress(&t, g_noalloc_ticket)) != cudaSuccess) return e;
+        g_noalloc_ticket_ptr[dev] = static_cast<unsigned *>(t);
+        g_noalloc_part_ptr[dev] = static_cast<double *>(p);
+    }
+    *part = g_noalloc_part_ptr[dev];
+    *ticket = g_noalloc_ticket_ptr[dev];
+    return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t launch_magnetic_residual_noalloc(cudaStream_t st, const Dims &d, const double *phi, double chi,
+                                             double bw, const Faces &hext, double h, const double *psi,
+                                             double *result) {
+    double *part = nullptr;
+    unsigned *ticket = nullptr;
+    cudaError_t e = noalloc_scratch(&part, &ticket);
+    if (e != cudaSuccess) return e;
+    // at most kNoAllocBlocks / tiles blocks along x: the grid never exceeds the scratch (tiles <= kNoAllocBlocks)
+    const long long tiles = (long long)((d.nz + 31) / 32) * ((d.ny + 7) / 8);
+    if (tiles > kNoAllocBlocks) return cudaErrorInvalidValue;
+    const long long zmax = kNoAllocBlocks / tiles;
+    const int xpb = (int)((d.nx + zmax - 1) / zmax);
+    const dim3 grid((d.nz + 31) / 32, (d.ny + 7) / 8, (d.nx + xpb - 1) / xpb);
+    // the tickets must start at zero (the reduction re-arms them, but a call cut short would not)
+    if ((e = cudaMemsetAsync(ticket, 0, sizeof(g_noalloc_ticket), st)) != cudaSuccess) return e;
+    const double t = bw * (1.0 + std::ldexp(1.0, -40));  // same band keys as launch_build_magnetic
+    auto key = [](double v) {
+        long long b;
+        std::memcpy(&b, &v, 8);
+        return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+    };
+    const double one_plus_chi = 1. + (1. - 0.) * chi;
+    k_magnetic_residual<<<grid, blk2(), 0, st>>>(d, xpb, phi, chi, bw, key(t), key(-t), one_plus_chi, hext, h, psi,
+                                                 part, ticket, result);
+    return cudaGetLastError();
 }
 
 void launch_total_field(cudaStream_t st, const Dims &d, const double *psi, const Faces &hext, double invh,

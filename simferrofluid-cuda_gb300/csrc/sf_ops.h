@@ -21,6 +21,11 @@ int launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, dou
                           const Faces &hext, double h, Coef<double> &cf, double *b, bool want_invd);
 void launch_total_field(cudaStream_t st, const Dims &d, const double *psi, const Faces &hext, double invh,
                         const Faces &H);
+// Allocation-free residual of a potential on the pinned magnetostatic system (static scratch, see sf_ops.cu).
+bool noalloc_fits(const Dims &d);
+cudaError_t launch_magnetic_residual_noalloc(cudaStream_t st, const Dims &d, const double *phi, double chi,
+                                             double bw, const Faces &hext, double h, const double *psi,
+                                             double *result);
 void launch_copy(cudaStream_t st, long long n, const double *a, double *o);
 void launch_to_f32(cudaStream_t st, long long n, const double *a, float *o);
 
