@@ -33,7 +33,7 @@ METRIC = "Poisson solves/s at 256^3 to 1e-6 rel. residual (pressure + magnetic p
 UNIT = "solves/s"
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--pre", type=int, default=None)
     ap.add_argument("--post", type=int, default=None)
     ap.add_argument("--smoother", type=int, default=None, help="0 two-colour (default), 1 fused one-pass")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 # ------------------------------------------------------------------------------------------------ distributed
