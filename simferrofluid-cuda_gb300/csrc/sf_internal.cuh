@@ -230,6 +230,7 @@ enum Slot {
     S_AUX0,
     S_AUX1,
     S_AUX2,
+    S_ERR,  // set to 1 by a kernel whose bounded wait timed out
     S_NSLOTS = 16
 };
 

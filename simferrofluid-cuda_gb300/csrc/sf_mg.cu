@@ -19,8 +19,12 @@
 #include <cstdio>
 #include <cstring>
 
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <type_traits>
 
+#include "sf_rbgs_tma.cuh"
 #include "sf_solver.h"
 
 namespace sf {
@@ -913,10 +917,72 @@ static inline int fused_chunk(const Dims &d) {
     return chunk < d.nx ? chunk : d.nx;
 }
 
+// TMA-staged one-pass sweep of the finest FP32 level (sf_rbgs_tma.cuh).  Needs nz a multiple of 4 (16-byte
+// row strides for the tensor maps) and a grid at least one box wide in y and z.
+static bool rbt_ok(const Dims &d) {
+    return d.nz % 4 == 0 && d.nz >= rbt::BZ && d.ny >= rbt::BY && tensor_map_encoder() != nullptr;
+}
+
+// Tensor maps of finest-level arrays, encoded once per (address, dims): an address that is freed and reused with
+// the same dims maps the same bytes, so entries never go stale.
+static bool rbt_map(const float *p, const Dims &d, CUtensorMap &out) {
+    static std::mutex mu;
+    static std::map<std::tuple<const void *, int, int, int>, CUtensorMap> cache;
+    const auto key = std::make_tuple(static_cast<const void *>(p), d.nx, d.ny, d.nz);
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        out = it->second;
+        return true;
+    }
+    auto enc = tensor_map_encoder();
+    if (!enc || !p || (reinterpret_cast<uintptr_t>(p) & 15u)) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)d.nz, (cuuint64_t)d.ny, (cuuint64_t)d.nx};
+    const cuuint64_t strides[2] = {(cuuint64_t)d.nz * 4, (cuuint64_t)d.ny * d.nz * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)rbt::BZ, (cuuint32_t)rbt::BY, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    CUtensorMap m;
+    if (enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(p), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    cache.emplace(key, m);
+    out = m;
+    return true;
+}
+
+template <int MODE>
+static bool launch_rbgs_tma(cudaStream_t st, Tracker &tk, const Dims &d, const Coef<float> &cf, const float *xin,
+                            float *xout, const float *b) {
+    if (!tk.sc) return false;
+    rbt::Maps m;
+    if (!rbt_map(MODE == 0 ? b : xin, d, m.x) || !rbt_map(cf.ax, d, m.ax) || !rbt_map(cf.ay, d, m.ay) ||
+        !rbt_map(cf.az, d, m.az) || !rbt_map(cf.dex, d, m.dex) || !rbt_map(b, d, m.b))
+        return false;
+    // planes per block: 32, or fewer while the grid would not fill the 152 SMs (two blocks each) three times
+    const long long tiles = (long long)((d.nz + rbt::TZ - 1) / rbt::TZ) * ((d.ny + rbt::TY - 1) / rbt::TY);
+    int chunk = 32;
+    while (chunk > 4 && tiles * ((d.nx + chunk - 1) / chunk) < 152 * 2 * 3) chunk /= 2;
+    if (chunk > d.nx) chunk = d.nx;
+    const dim3 g((d.nx + chunk - 1) / chunk, (d.nz + rbt::TZ - 1) / rbt::TZ, (d.ny + rbt::TY - 1) / rbt::TY);
+    if (cudaFuncSetAttribute(rbt::k_rbgs_tma<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)rbt::kSmemBytes) != cudaSuccess)
+        return false;
+    // x in (not from zero) + x out + b + 3 couplings + dex
+    const double per = (MODE == 0 ? 0.0 : 4.0) + 4.0 + 4.0 + 12.0 + 4.0;
+    tk.before(st, true);
+    rbt::k_rbgs_tma<MODE><<<g, dim3(32, 8), rbt::kSmemBytes, st>>>(m, d, xout, chunk, tk.sc, (int)S_ERR);
+    tk.after(st, true, per * d.n);
+    return true;
+}
+
 template <class T, class C, int MODE>
 static void fused(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const Coef<C> &cf, const T *xin, T *xout,
                   const T *b) {
     if constexpr (std::is_same<T, C>::value) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (fine && rbt_ok(d) && launch_rbgs_tma<MODE>(st, tk, d, cf, xin, xout, b)) return;
+        }
         if (fine) {
             // pipelined kernel: two blocks (FP32) or one (FP64) per SM, blocks marching 32 planes
             const long long tiles = (long long)((d.nz + FTZ - 1) / FTZ) * ((d.ny + FTY - 1) / FTY);
@@ -1108,6 +1174,7 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     x_ = (double *)chk(A(8 * n));
     b_ = (double *)chk(A(8 * n));
     sc_ = (double *)chk(A(8 * S_NSLOTS));
+    tk_.sc = sc_;
     part_ = (double *)chk(A(8 * 4 * (size_t)(kMaxTileBlocks + kMaxTileBlocks / kRedGroup + 1)));
     ticket_ = (unsigned *)chk(A(4 * (size_t)(2 + kMaxTileBlocks / kRedGroup)));
     if (p.precision == 0) {
@@ -1268,7 +1335,13 @@ cudaError_t MGSolver::run_iter(bool mixed) {
 
 cudaError_t MGSolver::read_slots() {
     cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
-    return cudaStreamSynchronize(st_);
+    const cudaError_t e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return e;
+    if (sc_host_[S_ERR] != 0) {
+        last_error = "a smoother's TMA load did not arrive within its bounded wait";
+        return cudaErrorLaunchTimeout;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t MGSolver::solve(bool x_is_zero, SolveResult &res) {

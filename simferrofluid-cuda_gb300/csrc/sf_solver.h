@@ -33,6 +33,7 @@ struct SolverParams {
 struct Tracker {
     long long launches = 0;
     bool prof = false;
+    double *sc = nullptr;  // the solver's scalar slots (S_ERR receives bounded-wait timeouts)
     std::vector<cudaEvent_t> ev;
     size_t used = 0;
     double bytes = 0;
