@@ -49,7 +49,7 @@ def parse(argv=None):
     ap.add_argument("--coarse-dim", type=int, default=None)
     ap.add_argument("--pre", type=int, default=None)
     ap.add_argument("--post", type=int, default=None)
-    ap.add_argument("--smoother", type=int, default=None, help="0 two-colour (default), 1 fused one-pass")
+    ap.add_argument("--smoother", type=int, default=None, help="0 two-colour, 1 fused one-pass, 2 (default) two-colour with FP16 finest-level smoothing coefficients")
     return ap.parse_args(argv)
 
 
@@ -251,8 +251,13 @@ def run_ours(args, ws, rank, local):
     peak_src = "measured" if peak else "fallback"
     peak = peak or 6800.0
     achieved = bytes_tot / (ms_tot / 1e3) / 1e9 if ms_tot > 0 else 0.0
-    kname = "k_rbgs_fused (one full red-black sweep per launch)" if args.smoother == 1 else \
-        "k_rbgs (one colour of a red-black sweep per launch)"
+    smoother = 2 if args.smoother is None else args.smoother
+    if smoother == 1:
+        kname = "k_rbgs_tma (one full red-black sweep per launch, TMA-staged)"
+    elif smoother == 2 and args.precision == "mixed":
+        kname = "k_rbgs<float, __half> (one colour of a red-black sweep per launch, FP16 operator copy)"
+    else:
+        kname = "k_rbgs (one colour of a red-black sweep per launch)"
     roofline = {"bound": "hbm", "kernel": kname + ", finest level",
                 "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": None,

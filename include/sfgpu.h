@@ -75,7 +75,9 @@ typedef struct {
     int report_ref_residual; /* also compute the residual on the reference's own operator (default 1) */
     double inner_tol;    /* mixed: floor of the inner relative reduction (default 1e-4) */
     int profile;         /* time every finest-level smoother launch with CUDA events (disables graphs) */
-    int smoother;        /* 0: two in-place colour passes (default), 1: fused one-pass red-black sweep */
+    int smoother;        /* 0: two in-place colour passes, 1: fused one-pass red-black sweep (TMA-staged at the
+                            finest FP32 level), 2 (default): as 0, and in the mixed form the finest level's
+                            smoother reads an FP16 copy of the operator (residuals and the CG operator stay FP32) */
     int reserved[6];
 } sf_solve_opts;
 
@@ -201,6 +203,46 @@ SF_EXPORT long long sf_unet_tc_launches(void *net);
 SF_EXPORT sf_status sf_set_network(void *ctx, void *net);
 /* features of the last assembled pressure (which = 0) or potential (1) system and its solution (FP32) */
 SF_EXPORT sf_status sf_system_features_dev(void *ctx, int which, void *features_bf16, float *solution);
+
+/* ----- velocity pipeline after the projection (core/Simulation.cpp:236-241) -------------------------------------
+ * Extrapolation::Solve (core/Extrapolation.cpp:4-30) of the projected velocity over max_steps layers, with the
+ * simulation's validity predicate (core/Simulation.cpp:237-240: fraction < 1 and an adjacent cell liquid);
+ * faces left without a valid neighbour take clear_val.  vel is updated in place. */
+SF_EXPORT sf_status sf_extrapolate_velocity(void *ctx, const sf_grid *g, double *const vel[3], const double *phi,
+                                            const double *const frac[3], double clear_val, int max_steps);
+SF_EXPORT sf_status sf_extrapolate_velocity_dev(void *ctx, const sf_grid *g, double *const vel[3], const double *phi,
+                                                const double *const frac[3], double clear_val, int max_steps);
+/* Collider::Enforce (core/Collider.cpp:75-86): on faces with fraction 1 the velocity becomes the trilinearly
+ * interpolated old velocity minus its normal component relative to the solid velocity (solid_vel NULL: zero).
+ * normal: the collider's face normals (sf_collider_face_normals). */
+SF_EXPORT sf_status sf_collider_enforce(void *ctx, const sf_grid *g, double *const vel[3], const double *const frac[3],
+                                        const double *const normal[3], const double *const solid_vel[3]);
+SF_EXPORT sf_status sf_collider_enforce_dev(void *ctx, const sf_grid *g, double *const vel[3],
+                                            const double *const frac[3], const double *const normal[3],
+                                            const double *const solid_vel[3]);
+/* Collider::Finish normals (core/Collider.cpp:30-44) from the node level set (host). */
+SF_EXPORT sf_status sf_collider_face_normals(const sf_grid *g, const double *node_ls, double *const normal[3]);
+
+/* ----- interface coupling (core/Simulation.cpp:204-235) ----------------------------------------------------------
+ * MagneticField::CalculateVertexPressures (core/MagneticField.cpp:37-48): p_m at each surface-mesh vertex from the
+ * total field H (the H_out of sf_magnetic_solve): H trilinear at the vertex, p = mu0/2 chi (|H|^2 +
+ * chi^2/(4chi+4) (H.n)^2).  positions, normals: nverts x 3 doubles (SurfaceMesh::Positions / Normals). */
+SF_EXPORT sf_status sf_magnetic_vertex_pressures(void *ctx, const sf_grid *g, double chi, const double *const H[3],
+                                                 const double *positions, const double *normals, long long nverts,
+                                                 double *pressures);
+SF_EXPORT sf_status sf_magnetic_vertex_pressures_dev(void *ctx, const sf_grid *g, double chi, const double *const H[3],
+                                                     const double *positions, const double *normals,
+                                                     long long nverts, double *pressures);
+/* The pressure jump J(axis, face) of the simulation's callback (core/Simulation.cpp:216-235) on every face, for
+ * sf_pressure_project's jump argument: with v = Contour::VertexIndexOf(axis, face - e_axis) (edge_mark[a]: int32
+ * per edge of the cell grid along a, size res - e_a, -1 = no vertex), J = curvature[v] st_coeff / density / h dt
+ * (if curvature) - mag_pressure[v] / density / h dt (if mag_pressure); 0 where there is no vertex. */
+SF_EXPORT sf_status sf_pressure_jump(void *ctx, const sf_grid *g, const int32_t *const edge_mark[3],
+                                     const double *curvature, const double *mag_pressure, long long nverts,
+                                     double st_coeff, double density, double dt, double *const jump[3]);
+SF_EXPORT sf_status sf_pressure_jump_dev(void *ctx, const sf_grid *g, const int32_t *const edge_mark[3],
+                                         const double *curvature, const double *mag_pressure, long long nverts,
+                                         double st_coeff, double density, double dt, double *const jump[3]);
 
 /* Forget the magnetic warm start (MagneticField ctor zeroes m_Sol, core/MagneticField.cpp:26). */
 SF_EXPORT sf_status sf_magnetic_reset(void *ctx);

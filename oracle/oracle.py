@@ -102,6 +102,12 @@ def lib():
         L.or_collider_box_levelset.argtypes = [G, C.c_int, _D]
         L.or_collider_face_fractions.argtypes = [G, _D, _D3]
         L.or_num_threads.restype = C.c_int
+        L.or_extrapolate_velocity.argtypes = [G, _D3, _D, _D3, C.c_double, C.c_int]
+        L.or_collider_face_normals.argtypes = [G, _D, _D3]
+        L.or_collider_enforce.argtypes = [G, _D3, _D3, _D3, C.c_void_p]
+        L.or_vertex_pressures.argtypes = [G, C.c_double, _D3, _D, _D, C.c_int64, _D]
+        L.or_pressure_jump.argtypes = [G, C.c_void_p * 3, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                       C.c_double, _D3]
         L.or_amg_solve.argtypes = [C.c_int, C.c_int64, _I64, _I32, _D, _D, _D, C.c_double, C.c_int,
                                    C.POINTER(_AmgInfo)]
         L.or_amg_solve.restype = C.c_int
@@ -298,6 +304,59 @@ def box_collider_fractions(g: Grid, bw: int = 0):
     frac = [np.empty(g.face_shape(a)) for a in range(3)]
     lib().or_collider_face_fractions(C.byref(g.c()), _p(ls), _D3(*[_p(a) for a in frac]))
     return frac
+
+
+def box_collider(g: Grid, bw: int = 0):
+    """Collider(sgrid) + Finish: node level set (after fast marching), face fractions and face normals."""
+    ls = np.empty((g.nx + 1, g.ny + 1, g.nz + 1))
+    lib().or_collider_box_levelset(C.byref(g.c()), int(bw), _p(ls))
+    lib().or_fast_marching(g.nx + 1, g.ny + 1, g.nz + 1, float(g.h), _p(ls))
+    frac = [np.empty(g.face_shape(a)) for a in range(3)]
+    lib().or_collider_face_fractions(C.byref(g.c()), _p(ls), _D3(*[_p(a) for a in frac]))
+    normal = [np.empty(g.face_shape(a)) for a in range(3)]
+    lib().or_collider_face_normals(C.byref(g.c()), _p(ls), _D3(*[_p(a) for a in normal]))
+    return ls, frac, normal
+
+
+def extrapolate_velocity(g: Grid, u, phi, frac, clear_val=0.0, max_steps=6):
+    """Extrapolation::Solve of the projected velocity (core/Simulation.cpp:237-241); returns new arrays."""
+    u = [np.array(a, dtype=np.float64, copy=True) for a in u]
+    fr, fp = _faces(frac)
+    lib().or_extrapolate_velocity(C.byref(g.c()), _D3(*[_p(a) for a in u]), _p(_f64(phi)), fp, float(clear_val),
+                                  int(max_steps))
+    return u
+
+
+def collider_enforce(g: Grid, u, frac, normal, us=None):
+    """Collider::Enforce (core/Collider.cpp:75-86); returns new arrays."""
+    u = [np.array(a, dtype=np.float64, copy=True) for a in u]
+    fr, fp = _faces(frac)
+    nr, npp = _faces(normal)
+    ur, up = _opt_faces(us)
+    lib().or_collider_enforce(C.byref(g.c()), _D3(*[_p(a) for a in u]), fp, npp, up)
+    return u
+
+
+def vertex_pressures(g: Grid, chi, H, positions, normals):
+    """MagneticField::CalculateVertexPressures (core/MagneticField.cpp:37-48) from the total field H."""
+    hr, hp = _faces(H)
+    pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+    nrm = np.ascontiguousarray(normals, dtype=np.float64).reshape(-1, 3)
+    out = np.empty(pos.shape[0])
+    lib().or_vertex_pressures(C.byref(g.c()), float(chi), hp, _p(pos), _p(nrm), pos.shape[0], _p(out))
+    return out
+
+
+def pressure_jump(g: Grid, edge_mark, kappa=None, pm=None, sigma=0.0, rho=1.0, dt=1.0):
+    """The jump callback of core/Simulation.cpp:216-235 on every face (three face arrays)."""
+    em = [np.ascontiguousarray(e, dtype=np.int32) for e in edge_mark]
+    kp = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+    pp = None if pm is None else np.ascontiguousarray(pm, dtype=np.float64)
+    jump = [np.empty(g.face_shape(a)) for a in range(3)]
+    lib().or_pressure_jump(C.byref(g.c()), (C.c_void_p * 3)(*[e.ctypes.data for e in em]),
+                           None if kp is None else kp.ctypes.data, None if pp is None else pp.ctypes.data,
+                           float(sigma), float(rho), float(dt), _D3(*[_p(a) for a in jump]))
+    return jump
 
 
 def num_threads() -> int:

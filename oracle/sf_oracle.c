@@ -705,3 +705,236 @@ void or_collider_face_fractions(const or_grid *g, const double *ls, double *cons
                 }
     }
 }
+
+/* ------------------------------------------------------------------------------------------------------------
+ * Post-projection velocity pipeline (core/Simulation.cpp:237-241).
+ * ---------------------------------------------------------------------------------------------------------- */
+
+/* Validity of a face for the extrapolation (core/Simulation.cpp:237-240): fraction < 1 and one of the two
+ * adjacent cells (AdjCellOfFace, core/StaggeredGrid.h:58: face - e_a and face) is liquid.  A cell outside the
+ * grid counts as not liquid (the reference reads outside its array there; shipped scenes never reach it
+ * because their boundary faces have fraction 1). */
+static int face_valid_init(const or_grid *g, const double *phi, const double *const frac[3], int a, int i, int j,
+                           int k) {
+    if (!(frac[a][fidx(g, a, i, j, k)] < 1)) return 0;
+    int c0[3] = {i, j, k};
+    c0[a] -= 1;
+    int l0 = cell_valid(g, c0[0], c0[1], c0[2]) && phi[cidx(g, c0[0], c0[1], c0[2])] <= 0;
+    int l1 = cell_valid(g, i, j, k) && phi[cidx(g, i, j, k)] <= 0;
+    return l0 || l1;
+}
+
+/* Extrapolation::Solve (core/Extrapolation.cpp:4-30) on each face grid: max_steps sweeps; an invalid face with
+ * valid neighbours (6-neighbourhood on its own face grid, order -x,+x,-y,+y,-z,+z) takes their mean and becomes
+ * valid for the next sweep, one without takes clear_val.  Valid faces are never written within a sweep, so the
+ * in-place update reads only values of the previous sweep. */
+void or_extrapolate_velocity(const or_grid *g, double *const u[3], const double *phi, const double *const frac[3],
+                             double clear_val, int max_steps) {
+    for (int a = 0; a < 3; a++) {
+        int fx, fy, fz;
+        fdims(g, a, &fx, &fy, &fz);
+        int64_t nf = (int64_t)fx * fy * fz;
+        uint8_t *valid = (uint8_t *)malloc(nf), *valid1 = (uint8_t *)malloc(nf);
+        for (int i = 0; i < fx; i++)
+            for (int j = 0; j < fy; j++)
+                for (int k = 0; k < fz; k++) valid[fidx(g, a, i, j, k)] = (uint8_t)face_valid_init(g, phi, frac, a, i, j, k);
+        memcpy(valid1, valid, nf);
+        for (int it = 0; it < max_steps; it++) {
+            for (int i = 0; i < fx; i++)
+                for (int j = 0; j < fy; j++)
+                    for (int k = 0; k < fz; k++) {
+                        int64_t f = fidx(g, a, i, j, k);
+                        if (!valid[f]) {
+                            int cnt = 0;
+                            double sum = 0;
+                            for (int o = 0; o < 6; o++) {
+                                int ni = i + NB[o][0], nj = j + NB[o][1], nk = k + NB[o][2];
+                                if (ni < 0 || nj < 0 || nk < 0 || ni >= fx || nj >= fy || nk >= fz) continue;
+                                int64_t nb = fidx(g, a, ni, nj, nk);
+                                if (valid[nb]) {
+                                    sum += u[a][nb];
+                                    cnt++;
+                                }
+                            }
+                            if (cnt > 0) {
+                                u[a][f] = sum / cnt;
+                                valid1[f] = 1;
+                            } else {
+                                u[a][f] = clear_val;
+                            }
+                        } else {
+                            valid1[f] = 1;
+                        }
+                    }
+            uint8_t *t = valid;
+            valid = valid1;
+            valid1 = t;
+        }
+        free(valid);
+        free(valid1);
+    }
+}
+
+/* FiniteDiff::CalcFirstDrv on the node grid (core/FiniteDiff.h:9-19, 50-52). */
+static double node_drv(const double *ls, int sx, int sy, int sz, int i, int j, int k, int a, double invh) {
+    int s3[3] = {sx, sy, sz};
+    int c[3] = {i, j, k};
+    double f[5];
+    for (int o = -2; o <= 2; o++) {
+        int q[3] = {i, j, k};
+        q[a] += o;
+        f[o + 2] = (q[a] >= 0 && q[a] < s3[a]) ? ls[(int64_t)q[2] + (int64_t)sz * ((int64_t)q[1] + (int64_t)sy * q[0])]
+                                               : 0.0;
+    }
+    if (c[a] == 0) return (4 * f[3] - 3 * f[2] - f[4]) * invh * .5;
+    if (c[a] + 1 == s3[a]) return (3 * f[2] - 4 * f[1] + f[0]) * invh * .5;
+    return (f[3] - f[1]) * invh * .5;
+}
+
+/* Collider::Finish normals (core/Collider.cpp:30-44): normal[a] on each face of axis a = mean over the face's 4
+ * nodes (NodeOfFace order, core/StaggeredGrid.h:64) of the a-derivative of the node level set. */
+void or_collider_face_normals(const or_grid *g, const double *ls, double *const normal[3]) {
+    int sx = g->nx + 1, sy = g->ny + 1, sz = g->nz + 1;
+    double invh = 1 / g->h;
+    for (int a = 0; a < 3; a++) {
+        int fx, fy, fz;
+        fdims(g, a, &fx, &fy, &fz);
+        int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+        for (int i = 0; i < fx; i++)
+            for (int j = 0; j < fy; j++)
+                for (int k = 0; k < fz; k++) {
+                    double sum = 0;
+                    for (int q = 0; q < 4; q++) {
+                        int n[3] = {i, j, k};
+                        n[b1] += q & 1;
+                        n[b2] += (q >> 1) & 1;
+                        sum += node_drv(ls, sx, sy, sz, n[0], n[1], n[2], a, invh);
+                    }
+                    normal[a][fidx(g, a, i, j, k)] = sum / 4;
+                }
+    }
+}
+
+/* TriLerp::Interpolate of face grid b (size res + e_b, origin = grid corner + h/2 on the other axes) at p. */
+static double trilerp_face(const or_grid *g, const double *v, int b, const double p[3]) {
+    double o[3] = {g->ox, g->oy, g->oz};
+    int sz3[3] = {g->nx, g->ny, g->nz};
+    double co[3];
+    int s[3];
+    for (int a = 0; a < 3; a++) {
+        co[a] = a == b ? o[a] : o[a] + g->h / 2; /* face grid origin (core/StaggeredGrid.h:16-20) */
+        s[a] = sz3[a] + (a == b);
+    }
+    double invh = 1 / g->h;
+    int lo[3];
+    double fr[3];
+    for (int a = 0; a < 3; a++) {
+        lo[a] = (int)floor((p[a] - co[a]) * invh - 0.0);
+        fr[a] = (p[a] - co[a] - (double)lo[a] * g->h) * invh;
+    }
+    double w[2][3];
+    for (int a = 0; a < 3; a++) {
+        w[0][a] = 1. - fr[a];
+        w[1][a] = fr[a];
+    }
+    double val = 0;
+    for (int q = 0; q < 8; q++) {
+        int dx = q & 1, dy = (q >> 1) & 1, dz = (q >> 2) & 1;
+        int ci[3] = {lo[0] + dx, lo[1] + dy, lo[2] + dz};
+        for (int a = 0; a < 3; a++) ci[a] = ci[a] < 0 ? 0 : (ci[a] > s[a] - 1 ? s[a] - 1 : ci[a]);
+        double wt = w[dx][0] * w[dy][1] * w[dz][2];
+        val += v[(int64_t)ci[2] + (int64_t)s[2] * ((int64_t)ci[1] + (int64_t)s[1] * ci[0])] * wt;
+    }
+    return val;
+}
+
+/* Collider::Enforce (core/Collider.cpp:75-86): on faces with fraction == 1 the fluid velocity becomes the
+ * interpolated old velocity minus its normal component relative to the solid velocity (us == NULL: zero). */
+void or_collider_enforce(const or_grid *g, double *const u[3], const double *const frac[3],
+                         const double *const normal[3], const double *const us[3]) {
+    double *old[3];
+    for (int b = 0; b < 3; b++) {
+        int fx, fy, fz;
+        fdims(g, b, &fx, &fy, &fz);
+        int64_t nf = (int64_t)fx * fy * fz;
+        old[b] = (double *)malloc(8 * nf);
+        memcpy(old[b], u[b], 8 * nf);
+    }
+    double o[3] = {g->ox, g->oy, g->oz};
+    for (int a = 0; a < 3; a++) {
+        int fx, fy, fz;
+        fdims(g, a, &fx, &fy, &fz);
+        for (int i = 0; i < fx; i++)
+            for (int j = 0; j < fy; j++)
+                for (int k = 0; k < fz; k++) {
+                    int64_t f = fidx(g, a, i, j, k);
+                    if (frac[a][f] != 1.) continue;
+                    int c3[3] = {i, j, k};
+                    double p[3];
+                    for (int b = 0; b < 3; b++)
+                        p[b] = (b == a ? o[b] : o[b] + g->h / 2) + (double)c3[b] * g->h; /* Grid::PositionOf */
+                    double vel[3], vel0[3], n[3];
+                    for (int b = 0; b < 3; b++) {
+                        vel[b] = trilerp_face(g, old[b], b, p);
+                        vel0[b] = us ? trilerp_face(g, us[b], b, p) : 0.0;
+                        n[b] = trilerp_face(g, normal[b], b, p);
+                    }
+                    double nn = sqrt((n[0] * n[0] + n[1] * n[1]) + n[2] * n[2]);
+                    if (nn > 0)
+                        for (int b = 0; b < 3; b++) n[b] = n[b] / nn;
+                    double dv[3] = {vel[0] - vel0[0], vel[1] - vel0[1], vel[2] - vel0[2]};
+                    double dn = (dv[0] * n[0] + dv[1] * n[1]) + dv[2] * n[2];
+                    u[a][f] = vel[a] - dn * n[a];
+                }
+    }
+    for (int b = 0; b < 3; b++) free(old[b]);
+}
+
+/* ------------------------------------------------------------------------------------------------------------
+ * Interface coupling: vertex magnetic pressures and the pressure jump (core/Simulation.cpp:204-235).
+ * ---------------------------------------------------------------------------------------------------------- */
+
+/* MagneticField::CalculateVertexPressures (core/MagneticField.cpp:37-48): H trilinear at each vertex position
+ * (TriLerp of the three face grids of the total field), p = mu0/2 chi (|H|^2 + chi^2/(4chi+4) (H.n)^2) with
+ * mu0 = 4e-7 pi (core/MagneticField.cpp:7-8).  positions / normals: nverts x 3, row-major. */
+void or_vertex_pressures(const or_grid *g, double chi, const double *const H[3], const double *pos,
+                         const double *nrm, int64_t nverts, double *out) {
+    const double pi = 3.141592653589793238462643383279502884;
+    const double mu0 = 4e-7 * pi;
+    for (int64_t v = 0; v < nverts; v++) {
+        const double *p = pos + 3 * v, *n = nrm + 3 * v;
+        double h[3];
+        for (int b = 0; b < 3; b++) h[b] = trilerp_face(g, H[b], b, p);
+        double coeff = (h[0] * h[0] + h[1] * h[1]) + h[2] * h[2];
+        double hn = (h[0] * n[0] + h[1] * n[1]) + h[2] * n[2];
+        coeff += chi * chi / (4 * chi + 4) * hn * hn;
+        out[v] = mu0 * 0.5 * chi * coeff;
+    }
+}
+
+/* The pressure-jump callback of core/Simulation.cpp:216-235 evaluated on every face (theta is unused): with the
+ * vertex of edge (axis, face - e_axis) (Contour::VertexIndexOf, core/Contour.h:19-21; edge grid of axis a has the
+ * cell-grid size minus e_a, entries -1 where no vertex), J = kappa[v] sigma / rho / h dt (when curvature is
+ * given) - p_m[v] / rho / h dt (when magnetic pressures are given); 0 without a vertex. */
+void or_pressure_jump(const or_grid *g, const int32_t *const edge_mark[3], const double *kappa, const double *pm,
+                      double sigma, double rho, double dt, double *const jump[3]) {
+    double invh = 1 / g->h;
+    for (int a = 0; a < 3; a++) {
+        int fx, fy, fz;
+        fdims(g, a, &fx, &fy, &fz);
+        int ex = g->nx - (a == 0), ey = g->ny - (a == 1), ez = g->nz - (a == 2);
+        for (int i = 0; i < fx; i++)
+            for (int j = 0; j < fy; j++)
+                for (int k = 0; k < fz; k++) {
+                    int e[3] = {i, j, k};
+                    e[a] -= 1;
+                    int idx = -1;
+                    if (e[0] >= 0 && e[1] >= 0 && e[2] >= 0 && e[0] < ex && e[1] < ey && e[2] < ez)
+                        idx = edge_mark[a][(int64_t)e[2] + (int64_t)ez * ((int64_t)e[1] + (int64_t)ey * e[0])];
+                    double pressure = 0;
+                    if (kappa && idx >= 0) pressure += kappa[idx] * sigma / rho * invh * dt;
+                    if (pm && idx >= 0) pressure -= pm[idx] / rho * invh * dt;
+                    jump[a][fidx(g, a, i, j, k)] = pressure;
+                }
+    }
+}

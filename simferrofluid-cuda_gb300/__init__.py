@@ -367,3 +367,116 @@ class MagneticField:
         self.total_field = H_out
         self.status = s
         return self.stats
+
+    def calculate_vertex_pressures(self, positions, normals, H=None, device=False, out=None):
+        """MagneticField::CalculateVertexPressures (core/MagneticField.cpp:37-48) at the mesh vertices
+        (positions, normals: nverts x 3) from H (default: the total field of the last solve)."""
+        g, keep = self.grid, []
+        H = self.total_field if H is None else H
+        if H is None:
+            raise ValueError("no total field: solve first or pass H")
+        fs = [g.face_shape(a) for a in range(3)]
+        hp = [_ptr(H[a], fs[a], f"H[{a}]", device, False, keep) for a in range(3)]
+        nv = int(positions.shape[0]) if hasattr(positions, "shape") else len(positions) // 3
+        if not device:
+            positions = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+            normals = np.ascontiguousarray(normals, dtype=np.float64).reshape(-1, 3)
+            if out is None:
+                out = np.empty(nv)
+        pp = _ptr(positions, (nv, 3), "positions", device, False, keep)
+        np_ = _ptr(normals, (nv, 3), "normals", device, False, keep)
+        op = _ptr(out, (nv,), "out", device, True)
+        fn = self.ctx.lib.sf_magnetic_vertex_pressures_dev if device else self.ctx.lib.sf_magnetic_vertex_pressures
+        st = fn(self.ctx.handle, C.byref(g.c_grid()), self.chi, _abi.p3(hp), C.c_void_p(pp), C.c_void_p(np_), nv,
+                C.c_void_p(op))
+        _check(self.ctx, st, None, "vertex pressures", True)
+        return out
+
+
+def pressure_jump(sgrid: StaggeredGrid, edge_mark, curvature=None, mag_pressure=None, st_coeff=0.0, density=1.0,
+                  dt=1.0, ctx: Context | None = None, device=False, out=None):
+    """The pressure jump of core/Simulation.cpp:216-235 on every face (three face arrays) from the contour's edge
+    marks (int32 per cell-grid edge, -1 = no vertex), vertex curvatures and vertex magnetic pressures."""
+    ctx = ctx or default_context()
+    g, keep = sgrid, []
+    fs = [g.face_shape(a) for a in range(3)]
+    es = [tuple(g.shape[b] - (b == a) for b in range(3)) for a in range(3)]
+    if device:
+        em = [int(edge_mark[a].data_ptr()) for a in range(3)]
+    else:
+        ems = [np.ascontiguousarray(edge_mark[a], dtype=np.int32) for a in range(3)]
+        for a in range(3):
+            if ems[a].size != int(np.prod(es[a])):
+                raise ValueError(f"edge_mark[{a}]: {ems[a].size} entries, expected {int(np.prod(es[a]))}")
+        keep += ems
+        em = [e.ctypes.data for e in ems]
+    nv = 0
+    for v in (curvature, mag_pressure):
+        if v is not None:
+            nv = int(v.numel()) if hasattr(v, "numel") else int(np.asarray(v).size)
+    kp = _ptr(curvature, (nv,), "curvature", device, False, keep) if curvature is not None else None
+    mp = _ptr(mag_pressure, (nv,), "mag_pressure", device, False, keep) if mag_pressure is not None else None
+    if out is None and not device:
+        out = [np.zeros(fs[a]) for a in range(3)]
+    jp = [_ptr(out[a], fs[a], f"jump[{a}]", device, True) for a in range(3)]
+    fn = ctx.lib.sf_pressure_jump_dev if device else ctx.lib.sf_pressure_jump
+    st = fn(ctx.handle, C.byref(g.c_grid()), _abi.p3(em), C.c_void_p(kp) if kp else None,
+            C.c_void_p(mp) if mp else None, nv, float(st_coeff), float(density), float(dt), _abi.p3(jp))
+    _check(ctx, st, None, "pressure jump", True)
+    return out
+
+
+# ------------------------------------------------------------------------------------------------ velocity pipeline
+def collider_face_normals(sgrid: StaggeredGrid, node_level_set):
+    """Collider::Finish normals (core/Collider.cpp:30-44) from the collider's node level set (host)."""
+    lib = load_library()
+    ls = np.ascontiguousarray(node_level_set, dtype=np.float64)
+    normal = [np.empty(sgrid.face_shape(a)) for a in range(3)]
+    s = lib.sf_collider_face_normals(C.byref(sgrid.c_grid()), C.c_void_p(ls.ctypes.data),
+                                     _abi.p3([n.ctypes.data for n in normal]))
+    if s != _abi.SF_OK:
+        raise SolveError(s, "sf_collider_face_normals: " + lib.sf_status_string(s).decode())
+    return normal
+
+
+class Extrapolation:
+    """Extrapolation::Solve of the projected velocity (core/Extrapolation.cpp:4-30) with the simulation's
+    validity predicate (core/Simulation.cpp:237-240), on the GPU."""
+
+    def __init__(self, sgrid: StaggeredGrid, ctx: Context | None = None):
+        self.grid = sgrid
+        self.ctx = ctx or default_context()
+
+    def solve(self, velocity, level_set, fraction, clear_val=0.0, max_steps=6, device=False):
+        g, keep = self.grid, []
+        fs = [g.face_shape(a) for a in range(3)]
+        vel = [_ptr(velocity[a], fs[a], f"velocity[{a}]", device, True, keep) for a in range(3)]
+        fr = [_ptr(fraction[a], fs[a], f"fraction[{a}]", device, False, keep) for a in range(3)]
+        phi = _ptr(level_set, g.shape, "level_set", device, False, keep)
+        fn = self.ctx.lib.sf_extrapolate_velocity_dev if device else self.ctx.lib.sf_extrapolate_velocity
+        s = fn(self.ctx.handle, C.byref(g.c_grid()), _abi.p3(vel), C.c_void_p(phi), _abi.p3(fr), float(clear_val),
+               int(max_steps))
+        _check(self.ctx, s, None, "velocity extrapolation", True)
+
+
+class ColliderEnforce:
+    """Collider::Enforce (core/Collider.cpp:75-86) with the collider's fractions and face normals, on the GPU."""
+
+    def __init__(self, sgrid: StaggeredGrid, fraction, normal, solid_velocity=None, ctx: Context | None = None):
+        self.grid = sgrid
+        self.ctx = ctx or default_context()
+        self.fraction, self.normal, self.solid_velocity = fraction, normal, solid_velocity
+
+    def enforce(self, velocity, device=False):
+        g, keep = self.grid, []
+        fs = [g.face_shape(a) for a in range(3)]
+        vel = [_ptr(velocity[a], fs[a], f"velocity[{a}]", device, True, keep) for a in range(3)]
+        fr = [_ptr(self.fraction[a], fs[a], f"fraction[{a}]", device, False, keep) for a in range(3)]
+        nm = [_ptr(self.normal[a], fs[a], f"normal[{a}]", device, False, keep) for a in range(3)]
+        us = None if self.solid_velocity is None else [
+            _ptr(self.solid_velocity[a], fs[a], "solid_velocity", device, False, keep) for a in range(3)]
+        us_ref = _abi.p3_ref(us)
+        fn = self.ctx.lib.sf_collider_enforce_dev if device else self.ctx.lib.sf_collider_enforce
+        s = fn(self.ctx.handle, C.byref(g.c_grid()), _abi.p3(vel), _abi.p3(fr), _abi.p3(nm),
+               us_ref[0] if us_ref else None)
+        _check(self.ctx, s, None, "collider enforce", True)

@@ -33,6 +33,9 @@ EXPORTED = [
     "sf_unet_create", "sf_unet_destroy", "sf_unet_num_params", "sf_unet_set_params", "sf_unet_get_params",
     "sf_unet_forward_dev", "sf_unet_backward_dev", "sf_unet_train_step_dev", "sf_set_network",
     "sf_system_features_dev", "sf_unet_set_mode", "sf_unet_tc_launches", "sf_magnetic_residual_noalloc",
+    "sf_extrapolate_velocity", "sf_extrapolate_velocity_dev", "sf_collider_enforce", "sf_collider_enforce_dev",
+    "sf_collider_face_normals", "sf_magnetic_vertex_pressures", "sf_magnetic_vertex_pressures_dev",
+    "sf_pressure_jump", "sf_pressure_jump_dev",
 ]
 
 
@@ -102,6 +105,24 @@ def load(path: str | None = None):
         f.restype = C.c_int
     L.sf_magnetic_reset.argtypes = [V]
     L.sf_magnetic_reset.restype = C.c_int
+    for name in ("sf_extrapolate_velocity", "sf_extrapolate_velocity_dev"):
+        f = getattr(L, name)
+        f.argtypes = [V, G, _P3, V, _P3, C.c_double, C.c_int]
+        f.restype = C.c_int
+    for name in ("sf_collider_enforce", "sf_collider_enforce_dev"):
+        f = getattr(L, name)
+        f.argtypes = [V, G, _P3, _P3, _P3, V]
+        f.restype = C.c_int
+    for name in ("sf_magnetic_vertex_pressures", "sf_magnetic_vertex_pressures_dev"):
+        f = getattr(L, name)
+        f.argtypes = [V, G, C.c_double, _P3, V, V, C.c_longlong, V]
+        f.restype = C.c_int
+    for name in ("sf_pressure_jump", "sf_pressure_jump_dev"):
+        f = getattr(L, name)
+        f.argtypes = [V, G, _P3, V, V, C.c_longlong, C.c_double, C.c_double, C.c_double, _P3]
+        f.restype = C.c_int
+    L.sf_collider_face_normals.argtypes = [G, V, _P3]
+    L.sf_collider_face_normals.restype = C.c_int
     L.sf_magnetic_residual_noalloc.argtypes = [V, G, V, C.c_double, C.c_double, _P3, V, V]
     L.sf_magnetic_residual_noalloc.restype = C.c_int
     L.sf_collider_box_fractions.argtypes = [G, C.c_int, _P3, V]

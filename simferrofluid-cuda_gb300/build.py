@@ -1,8 +1,8 @@
 """Build ``libsfgpu.so`` (the C-ABI library) in-tree with nvcc for sm_103a.
 
-Three translation units are compiled in parallel and linked into one shared library next to this file.
-``sf_ops.cu`` is compiled with ``-fmad=false`` so that its assembly and update kernels round exactly like the
-reference's C++ code.
+The translation units are compiled in parallel and linked into one shared library next to this file.
+``sf_ops.cu`` and ``sf_post.cu`` are compiled with ``-fmad=false`` so that their assembly and update kernels round
+exactly like the reference's C++ code.
 """
 from __future__ import annotations
 
@@ -22,6 +22,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           "-I" + INCLUDE, "-I" + CSRC]
 UNITS = {
     "sf_ops.cu": ["-fmad=false"],
+    "sf_post.cu": ["-fmad=false"],
     "sf_mg.cu": [],
     "sf_api.cu": [],
     "sf_collider.cu": ["-Xcompiler", "-ffp-contract=off"],

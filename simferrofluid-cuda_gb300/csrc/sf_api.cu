@@ -30,6 +30,10 @@ struct Ctx {
     Dims mag_dims{0, 0, 0, 0};
     // staging buffers for the host-pointer entry points
     DevBuf phi, frac[3], vel[3], us[3], jump[3], hext[3], H[3], cells;
+    // velocity pipeline after the projection: extrapolation masks, enforce's copy of the old velocity, normals
+    DevBuf mask[6], old[3], normal[3];
+    // interface coupling: mesh vertices, vertex values and edge marks
+    DevBuf vpos, vnrm, vval, kappa, edge[3];
     // learned form: attached network (not owned) and its buffers; every network created on this context is
     // registered so that destroying the context first leaves the network handles safe to destroy later
     UNet *net = nullptr;
@@ -83,7 +87,7 @@ SolverParams params_from(const sf_solve_opts *o, int which) {
     p.inner_tol = o->inner_tol > 0 ? o->inner_tol : def.inner_tol;
     p.flexible = false;
     p.profile = o->profile != 0;
-    p.smoother = o->smoother == 1 ? 1 : 0;
+    p.smoother = o->smoother;
     return p;
 }
 
@@ -91,7 +95,7 @@ bool opts_ok(const sf_solve_opts *o) {
     if (!o) return true;
     if (o->precision != SF_PREC_FP64 && o->precision != SF_PREC_MIXED && o->precision != SF_PREC_LEARNED) return false;
     if (o->max_levels < 0 || o->coarse_dim < 0) return false;
-    if (o->smoother != 0 && o->smoother != 1) return false;
+    if (o->smoother < 0 || o->smoother > 2) return false;
     return true;
 }
 
@@ -349,6 +353,172 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
     return res.fallback ? SF_STALLED_FALLBACK : SF_OK;
 }
 
+// ----- velocity pipeline after the projection ------------------------------------------------------------
+sf_status post_common(Ctx *c, const sf_grid *g, double *const vel[3]) {
+    if (!c) return SF_BAD_ARG;
+    if (!grid_ok(g) || !vel) return fail(c, SF_BAD_ARG, "bad grid or velocity pointer");
+    for (int a = 0; a < 3; a++)
+        if (!vel[a]) return fail(c, SF_BAD_ARG, "null velocity array");
+    return SF_OK;
+}
+
+sf_status stage_vel(Ctx *c, const sf_grid *g, double *const vel[3], bool dev, double *dvel[3], long long &h2d) {
+    for (int a = 0; a < 3; a++) {
+        const double *p;
+        sf_status s = stage_in(c, c->vel[a], vel[a], face_count(g, a), dev, &p, h2d);
+        if (s != SF_OK) return s;
+        dvel[a] = const_cast<double *>(p);
+    }
+    return SF_OK;
+}
+
+sf_status unstage_vel(Ctx *c, const sf_grid *g, double *const vel[3], bool dev, double *const dvel[3]) {
+    if (!dev)
+        for (int a = 0; a < 3; a++)
+            CK(cudaMemcpyAsync(vel[a], dvel[a], 8 * (size_t)face_count(g, a), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    CK(cudaGetLastError());
+    return SF_OK;
+}
+
+sf_status extrapolate_impl(Ctx *c, const sf_grid *g, double *const vel[3], const double *phi,
+                           const double *const frac[3], double clear_val, int max_steps, bool dev) {
+    sf_status s = post_common(c, g, vel);
+    if (s != SF_OK) return s;
+    if (!phi || !frac || !frac[0] || !frac[1] || !frac[2] || max_steps < 0 || !std::isfinite(clear_val))
+        return fail(c, SF_BAD_ARG, "bad level set, fraction pointer, step count or clear value");
+    CK(cudaSetDevice(c->device));
+    const Dims d = make_dims(g->nx, g->ny, g->nz);
+    long long h2d = 0;
+    double *dvel[3];
+    const double *dphi;
+    Faces ff{};
+    if ((s = stage_vel(c, g, vel, dev, dvel, h2d)) != SF_OK) return s;
+    if ((s = stage_in(c, c->phi, phi, d.n, dev, &dphi, h2d)) != SF_OK) return s;
+    uint8_t *m0[3], *m1[3];
+    for (int a = 0; a < 3; a++) {
+        if ((s = stage_in(c, c->frac[a], frac[a], face_count(g, a), dev, &ff.p[a], h2d)) != SF_OK) return s;
+        CK(c->mask[a].ensure((size_t)face_count(g, a)));
+        CK(c->mask[3 + a].ensure((size_t)face_count(g, a)));
+        m0[a] = (uint8_t *)c->mask[a].get();
+        m1[a] = (uint8_t *)c->mask[3 + a].get();
+    }
+    launch_extrapolate(c->st, d, dphi, ff, dvel, m0, m1, clear_val, max_steps);
+    CK(cudaGetLastError());
+    return unstage_vel(c, g, vel, dev, dvel);
+}
+
+// Stage n elements of `bytes_per` bytes (host) into buf, or pass a device pointer through.
+template <class T>
+sf_status stage_raw(Ctx *c, DevBuf &buf, const T *src, long long n, bool dev, const T **out, long long &h2d) {
+    if (!src || dev) {
+        *out = src;
+        return SF_OK;
+    }
+    CK(buf.ensure(sizeof(T) * (size_t)n));
+    CK(cudaMemcpyAsync(buf.get(), src, sizeof(T) * (size_t)n, cudaMemcpyHostToDevice, c->st));
+    h2d += (long long)sizeof(T) * n;
+    *out = (const T *)buf.get();
+    return SF_OK;
+}
+
+sf_status vertex_pressures_impl(Ctx *c, const sf_grid *g, double chi, const double *const H[3], const double *pos,
+                                const double *nrm, long long nv, double *out, bool dev) {
+    if (!c) return SF_BAD_ARG;
+    if (!grid_ok(g) || !H || !H[0] || !H[1] || !H[2] || nv < 0 || (nv > 0 && (!pos || !nrm || !out)) ||
+        !std::isfinite(chi))
+        return fail(c, SF_BAD_ARG, "bad grid, field, vertex arrays, count or susceptibility");
+    if (nv == 0) return SF_OK;
+    CK(cudaSetDevice(c->device));
+    const Dims d = make_dims(g->nx, g->ny, g->nz);
+    long long h2d = 0;
+    Faces fh{};
+    sf_status s;
+    for (int a = 0; a < 3; a++)
+        if ((s = stage_in(c, c->H[a], H[a], face_count(g, a), dev, &fh.p[a], h2d)) != SF_OK) return s;
+    const double *dpos, *dnrm;
+    if ((s = stage_raw(c, c->vpos, pos, 3 * nv, dev, &dpos, h2d)) != SF_OK) return s;
+    if ((s = stage_raw(c, c->vnrm, nrm, 3 * nv, dev, &dnrm, h2d)) != SF_OK) return s;
+    double *dout = out;
+    if (!dev) {
+        CK(c->vval.ensure(8 * (size_t)nv));
+        dout = (double *)c->vval.get();
+    }
+    launch_vertex_pressures(c->st, d, g->origin, g->h, fh, chi, dpos, dnrm, nv, dout);
+    CK(cudaGetLastError());
+    if (!dev) CK(cudaMemcpyAsync(out, dout, 8 * (size_t)nv, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return SF_OK;
+}
+
+sf_status pressure_jump_impl(Ctx *c, const sf_grid *g, const int32_t *const edge_mark[3], const double *kappa,
+                             const double *pm, long long nv, double sigma, double rho, double dt,
+                             double *const jump[3], bool dev) {
+    if (!c) return SF_BAD_ARG;
+    if (!grid_ok(g) || !edge_mark || !jump || nv < 0 || !(rho != 0) || !std::isfinite(rho) || !std::isfinite(dt) ||
+        !std::isfinite(sigma) || ((kappa || pm) && nv == 0))
+        return fail(c, SF_BAD_ARG, "bad grid, edge marks, jump arrays, vertex count or constants");
+    for (int a = 0; a < 3; a++)
+        if (!edge_mark[a] || !jump[a]) return fail(c, SF_BAD_ARG, "edge marks and jump arrays come in threes");
+    CK(cudaSetDevice(c->device));
+    const Dims d = make_dims(g->nx, g->ny, g->nz);
+    long long h2d = 0;
+    sf_status s;
+    const int32_t *dem[3];
+    for (int a = 0; a < 3; a++) {
+        const long long ne = (long long)(g->nx - (a == 0)) * (g->ny - (a == 1)) * (g->nz - (a == 2));
+        if ((s = stage_raw(c, c->edge[a], edge_mark[a], ne > 0 ? ne : 0, dev, &dem[a], h2d)) != SF_OK) return s;
+    }
+    const double *dk, *dpm;
+    if ((s = stage_raw(c, c->kappa, kappa, nv, dev, &dk, h2d)) != SF_OK) return s;
+    if ((s = stage_raw(c, c->vval, pm, nv, dev, &dpm, h2d)) != SF_OK) return s;
+    double *dj[3];
+    for (int a = 0; a < 3; a++) {
+        if (dev) {
+            dj[a] = jump[a];
+        } else {
+            CK(c->jump[a].ensure(8 * (size_t)face_count(g, a)));
+            dj[a] = (double *)c->jump[a].get();
+        }
+    }
+    launch_pressure_jump(c->st, d, dem, dk, dpm, sigma, rho, g->h, dt, dj);
+    CK(cudaGetLastError());
+    if (!dev)
+        for (int a = 0; a < 3; a++)
+            CK(cudaMemcpyAsync(jump[a], dj[a], 8 * (size_t)face_count(g, a), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return SF_OK;
+}
+
+sf_status enforce_impl(Ctx *c, const sf_grid *g, double *const vel[3], const double *const frac[3],
+                       const double *const normal[3], const double *const us[3], bool dev) {
+    sf_status s = post_common(c, g, vel);
+    if (s != SF_OK) return s;
+    if (!frac || !normal) return fail(c, SF_BAD_ARG, "null fraction or normal arrays");
+    for (int a = 0; a < 3; a++)
+        if (!frac[a] || !normal[a] || (us && !us[a]))
+            return fail(c, SF_BAD_ARG, "fraction, normal and solid-velocity arrays come in threes");
+    CK(cudaSetDevice(c->device));
+    const Dims d = make_dims(g->nx, g->ny, g->nz);
+    long long h2d = 0;
+    double *dvel[3];
+    Faces ff{}, fn{}, fus{}, fold{};
+    if ((s = stage_vel(c, g, vel, dev, dvel, h2d)) != SF_OK) return s;
+    for (int a = 0; a < 3; a++) {
+        const long long nf = face_count(g, a);
+        if ((s = stage_in(c, c->frac[a], frac[a], nf, dev, &ff.p[a], h2d)) != SF_OK) return s;
+        if ((s = stage_in(c, c->normal[a], normal[a], nf, dev, &fn.p[a], h2d)) != SF_OK) return s;
+        if ((s = stage_in(c, c->us[a], us ? us[a] : nullptr, nf, dev, &fus.p[a], h2d)) != SF_OK) return s;
+        // Collider::Enforce interpolates the velocity as it was before the call
+        CK(c->old[a].ensure(8 * (size_t)nf));
+        launch_copy(c->st, nf, dvel[a], (double *)c->old[a].get());
+        fold.p[a] = (const double *)c->old[a].get();
+    }
+    launch_enforce(c->st, d, g->origin, g->h, fold, fus, fn, ff, dvel);
+    CK(cudaGetLastError());
+    return unstage_vel(c, g, vel, dev, dvel);
+}
+
 }  // namespace
 
 struct NetHandle {
@@ -392,6 +562,7 @@ void sf_default_opts(sf_solve_opts *o, int which) {
     o->check_every = 1;
     o->report_ref_residual = 1;
     o->inner_tol = 1e-4;
+    o->smoother = 2;  // mixed form: FP16 finest-level smoothing coefficients; FP64: two colour passes
 }
 
 sf_status sf_create(int device, void *stream, void **out) {
@@ -492,6 +663,46 @@ sf_status sf_magnetic_solve_dev(void *ctx, const sf_grid *g, const double *phi, 
                                 const sf_solve_opts *opts, sf_solve_stats *stats) {
     return magnetic_impl(C(ctx), g, phi, chi, band_width, hext, psi_out, H_out, opts, stats, true);
 }
+sf_status sf_extrapolate_velocity(void *ctx, const sf_grid *g, double *const vel[3], const double *phi,
+                                  const double *const frac[3], double clear_val, int max_steps) {
+    return extrapolate_impl(C(ctx), g, vel, phi, frac, clear_val, max_steps, false);
+}
+sf_status sf_extrapolate_velocity_dev(void *ctx, const sf_grid *g, double *const vel[3], const double *phi,
+                                      const double *const frac[3], double clear_val, int max_steps) {
+    return extrapolate_impl(C(ctx), g, vel, phi, frac, clear_val, max_steps, true);
+}
+sf_status sf_collider_enforce(void *ctx, const sf_grid *g, double *const vel[3], const double *const frac[3],
+                              const double *const normal[3], const double *const solid_vel[3]) {
+    return enforce_impl(C(ctx), g, vel, frac, normal, solid_vel, false);
+}
+sf_status sf_collider_enforce_dev(void *ctx, const sf_grid *g, double *const vel[3], const double *const frac[3],
+                                  const double *const normal[3], const double *const solid_vel[3]) {
+    return enforce_impl(C(ctx), g, vel, frac, normal, solid_vel, true);
+}
+
+sf_status sf_magnetic_vertex_pressures(void *ctx, const sf_grid *g, double chi, const double *const H[3],
+                                      const double *positions, const double *normals, long long nverts,
+                                      double *pressures) {
+    return vertex_pressures_impl(C(ctx), g, chi, H, positions, normals, nverts, pressures, false);
+}
+sf_status sf_magnetic_vertex_pressures_dev(void *ctx, const sf_grid *g, double chi, const double *const H[3],
+                                          const double *positions, const double *normals, long long nverts,
+                                          double *pressures) {
+    return vertex_pressures_impl(C(ctx), g, chi, H, positions, normals, nverts, pressures, true);
+}
+sf_status sf_pressure_jump(void *ctx, const sf_grid *g, const int32_t *const edge_mark[3], const double *curvature,
+                           const double *mag_pressure, long long nverts, double st_coeff, double density, double dt,
+                           double *const jump[3]) {
+    return pressure_jump_impl(C(ctx), g, edge_mark, curvature, mag_pressure, nverts, st_coeff, density, dt, jump,
+                              false);
+}
+sf_status sf_pressure_jump_dev(void *ctx, const sf_grid *g, const int32_t *const edge_mark[3],
+                               const double *curvature, const double *mag_pressure, long long nverts,
+                               double st_coeff, double density, double dt, double *const jump[3]) {
+    return pressure_jump_impl(C(ctx), g, edge_mark, curvature, mag_pressure, nverts, st_coeff, density, dt, jump,
+                              true);
+}
+
 sf_status sf_magnetic_residual_noalloc(void *stream, const sf_grid *g, const double *phi, double chi,
                                        double band_width, const double *const hext[3], const double *psi,
                                        double *result) {

@@ -165,6 +165,47 @@ SF_EXPORT sf_status sf_collider_face_fractions(const sf_grid *g, const double *n
     return SF_OK;
 }
 
+// Collider::Finish normals (core/Collider.cpp:30-44): on each face of axis a, the mean over its four nodes
+// (NodeOfFace order) of FiniteDiff::CalcFirstDrv of the node level set along a (core/FiniteDiff.h:9-19,50-52:
+// one-sided second-order stencils at the node-grid ends).
+SF_EXPORT sf_status sf_collider_face_normals(const sf_grid *g, const double *node_ls, double *const normal[3]) {
+    if (!g || g->nx <= 0 || g->ny <= 0 || g->nz <= 0 || !(g->h > 0) || !node_ls || !normal || !normal[0] ||
+        !normal[1] || !normal[2])
+        return SF_BAD_ARG;
+    const int s3[3] = {g->nx + 1, g->ny + 1, g->nz + 1};
+    const double invh = 1 / g->h;
+    auto at = [&](int i, int j, int k) {
+        return node_ls[(int64_t)k + (int64_t)s3[2] * ((int64_t)j + (int64_t)s3[1] * i)];
+    };
+    auto drv = [&](const int n[3], int a) {
+        auto f = [&](int o) {
+            int q[3] = {n[0], n[1], n[2]};
+            q[a] += o;
+            return at(q[0], q[1], q[2]);
+        };
+        if (n[a] == 0) return (4 * f(1) - 3 * f(0) - f(2)) * invh * .5;
+        if (n[a] + 1 == s3[a]) return (3 * f(0) - 4 * f(-1) + f(-2)) * invh * .5;
+        return (f(1) - f(-1)) * invh * .5;
+    };
+    for (int a = 0; a < 3; a++) {
+        const int fx = g->nx + (a == 0), fy = g->ny + (a == 1), fz = g->nz + (a == 2);
+        const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+        for (int i = 0; i < fx; i++)
+            for (int j = 0; j < fy; j++)
+                for (int k = 0; k < fz; k++) {
+                    double sum = 0;
+                    for (int q = 0; q < 4; q++) {
+                        int n[3] = {i, j, k};
+                        n[b1] += q & 1;
+                        n[b2] += (q >> 1) & 1;
+                        sum += drv(n, a);
+                    }
+                    normal[a][(int64_t)k + (int64_t)fz * ((int64_t)j + (int64_t)fy * i)] = sum / 4;
+                }
+    }
+    return SF_OK;
+}
+
 SF_EXPORT sf_status sf_collider_box_fractions(const sf_grid *g, int boundary_width, double *const frac[3],
                                               double *node_ls_out) {
     if (!g || g->nx <= 0 || g->ny <= 0 || g->nz <= 0 || !(g->h > 0) || boundary_width < 0 || !frac)

@@ -702,6 +702,17 @@ __global__ void k_to32(long long n, Coef<double> f, Coef<float> o) {
     }
 }
 
+// FP64 level 0 -> FP16 copy read only by the finest-level smoother (smoother 2); scale 1 (ghost-fluid excesses
+// stay below 6000, couplings in [0, 1 + chi]).
+__global__ void k_to16(long long n, Coef<double> f, Coef<__half> o) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        o.ax[c] = __float2half_rn((float)f.ax[c]);
+        o.ay[c] = __float2half_rn((float)f.ay[c]);
+        o.az[c] = __float2half_rn((float)f.az[c]);
+        o.dex[c] = __float2half_rn((float)f.dex[c]);
+    }
+}
+
 // ------------------------------------------------------------------------------------------------ Krylov kernels
 // Stencil kernels with a reduction: block (32, 8) over a (z, y) tile, each block walks `xpb` consecutive x
 // planes (so x +- 1 neighbours come from its own previous/next plane), at most kMaxTileBlocks blocks.  Threads
@@ -900,7 +911,7 @@ static void rb(cudaStream_t st, Tracker &tk, bool fine, bool zero, const Dims &d
                int color) {
     const dim3 g = grid_pairs(d), bk = blk2();
     // algorithmic bytes of one colour: half of (x r/w + b + 3 couplings + diagonal term)
-    const double per = (sizeof(C) == 8 ? 56.0 : 28.0) / 2.0;
+    const double per = (3.0 * sizeof(T) + 4.0 * sizeof(C)) / 2.0;
     tk.before(st, fine);
     if (zero)
         k_rbgs<T, C, true><<<g, bk, 0, st>>>(d, cf, x, b, color);
@@ -1070,16 +1081,19 @@ static void coarse_solve(cudaStream_t st, Tracker &tk, const Dims &d, const Coef
 
 // V-cycle z = M r.  Level 0 uses coefficient type C0, coarse levels Cc (cc[l] for level l >= 1).  ts[l] is a
 // scratch vector of level l for the fused smoother (nullptr entries select the in-place two-colour smoother).
-template <class T, class C0, class Cc>
+// c0s: level-0 coefficients read by the level-0 smoother (c0 itself, or a lower-precision copy); residuals and
+// restriction use c0.
+template <class T, class C0, class Cc, class C0S>
 static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, const Coef<C0> &c0,
-                   const std::vector<Coef<Cc>> &cc, T *z, const T *r, const std::vector<T *> &xs,
-                   const std::vector<T *> &bs, const std::vector<T *> &ts, const SolverParams &p) {
+                   const Coef<C0S> &c0s, const std::vector<Coef<Cc>> &cc, T *z, const T *r,
+                   const std::vector<T *> &xs, const std::vector<T *> &bs, const std::vector<T *> &ts,
+                   const SolverParams &p) {
     const int L = (int)dims.size();
     if (L == 1) {
         coarse_solve<T, C0>(st, tk, dims[0], c0, z, r, p.coarse_sweeps);
         return;
     }
-    smooth<T, C0>(st, tk, true, dims[0], c0, z, ts[0], r, p.pre, true);
+    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true);
     restrict_res<T, C0>(st, tk, dims[0], c0, z, r, dims[1], bs[1]);
     for (int l = 1; l < L - 1; l++) {
         smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.pre, true);
@@ -1093,7 +1107,7 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
     }
     tk.launches++;
     k_prolong<T><<<grid_cells(dims[0]), blk2(), 0, st>>>(dims[0], z, dims[1], xs[1]);
-    smooth<T, C0>(st, tk, true, dims[0], c0, z, ts[0], r, p.post, false);
+    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false);
 }
 
 // ------------------------------------------------------------------------------------------------ MGSolver
@@ -1145,7 +1159,8 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
         dims.push_back(make_dims((t.nx + 1) / 2, (t.ny + 1) / 2, (t.nz + 1) / 2));
     }
     const bool same = configured_ && cfg_dims_.nx == d.nx && cfg_dims_.ny == d.ny && cfg_dims_.nz == d.nz &&
-                      cfg_prec_ == p.precision && cfg_levels_ == (int)dims.size() && cfg_cdim_ == cdim;
+                      cfg_prec_ == p.precision && cfg_levels_ == (int)dims.size() && cfg_cdim_ == cdim &&
+                      (p.precision == 0 || (cfg_smoother_ == 2) == (p.smoother == 2));
     prm_ = p;
     if (same) return cudaSuccess;
     destroy_graphs();
@@ -1197,6 +1212,14 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
         c32_.dex = (float *)chk(A(4 * n));
         c32_.D = c32_.invd = nullptr;
         c32_.scale = c32_.unscale = 1.f;
+        c16s0_ = Coef<__half>{};
+        if (p.smoother == 2) {
+            c16s0_.ax = (__half *)chk(A(2 * n));
+            c16s0_.ay = (__half *)chk(A(2 * n));
+            c16s0_.az = (__half *)chk(A(2 * n));
+            c16s0_.dex = (__half *)chk(A(2 * n));
+            c16s0_.scale = c16s0_.unscale = 1.f;
+        }
         c16_.assign(L, Coef<__half>{});
         x32_.assign(L, nullptr);
         b32_.assign(L, nullptr);
@@ -1238,6 +1261,7 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     cfg_prec_ = p.precision;
     cfg_levels_ = L;
     cfg_cdim_ = cdim;
+    cfg_smoother_ = p.smoother;
     return cudaGetLastError();
 }
 
@@ -1250,6 +1274,10 @@ cudaError_t MGSolver::build_hierarchy() {
                                                                                     lev_dims_[l], c64_[l]);
     } else {
         k_to32<<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0].n, c64_[0], c32_);
+        if (prm_.smoother == 2) {
+            k_to16<<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0].n, c64_[0], c16s0_);
+            tk_.launches++;
+        }
         if (L > 1)
             k_coarsen<double, __half><<<grid_cells(lev_dims_[1]), blk2(), 0, st_>>>(lev_dims_[0], c64_[0],
                                                                                     lev_dims_[1], c16_[1]);
@@ -1266,8 +1294,9 @@ void MGSolver::enqueue_iter64() {
     int xpb;
     const dim3 tg = tile_grid(d, xpb);
     const long long l0 = tk_.launches;
-    vcycle<double, double, double>(st_, tk_, lev_dims_, c64_[0], c64_, z_, r_, x64_, b64_,
-                                   prm_.smoother == 1 ? t64_ : std::vector<double *>(t64_.size(), nullptr), prm_);
+    vcycle<double, double, double, double>(st_, tk_, lev_dims_, c64_[0], c64_[0], c64_, z_, r_, x64_, b64_,
+                                           prm_.smoother == 1 ? t64_ : std::vector<double *>(t64_.size(), nullptr),
+                                           prm_);
     k_dot_rz<double><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, r_, z_, q_, prm_.flexible ? 1 : 0, sc_, part_,
                                                               ticket_);
     k_xpby<double><<<flat_grid(n), 256, 0, st_>>>(n, z_, p_, sc_);
@@ -1284,8 +1313,13 @@ void MGSolver::enqueue_iter32() {
     int xpb;
     const dim3 tg = tile_grid(d, xpb);
     const long long l0 = tk_.launches;
-    vcycle<float, float, __half>(st_, tk_, lev_dims_, c32_, c16_, z32_, ri32_, x32_, b32_,
-                                 prm_.smoother == 1 ? t32_ : std::vector<float *>(t32_.size(), nullptr), prm_);
+    const std::vector<float *> ts = prm_.smoother == 1 ? t32_ : std::vector<float *>(t32_.size(), nullptr);
+    if (prm_.smoother == 2)
+        vcycle<float, float, __half, __half>(st_, tk_, lev_dims_, c32_, c16s0_, c16_, z32_, ri32_, x32_, b32_, ts,
+                                             prm_);
+    else
+        vcycle<float, float, __half, float>(st_, tk_, lev_dims_, c32_, c32_, c16_, z32_, ri32_, x32_, b32_, ts,
+                                            prm_);
     k_dot_rz<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, ri32_, z32_, q32_, 1, sc_, part_, ticket_);
     k_xpby<float><<<flat_grid(n), 256, 0, st_>>>(n, z32_, p32_, sc_);
     k_apply_dot<float, float><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c32_, p32_, q32_, sc_, part_, ticket_);

@@ -26,6 +26,15 @@ bool noalloc_fits(const Dims &d);
 cudaError_t launch_magnetic_residual_noalloc(cudaStream_t st, const Dims &d, const double *phi, double chi,
                                              double bw, const Faces &hext, double h, const double *psi,
                                              double *result);
+// Velocity pipeline after the projection (sf_post.cu).
+void launch_extrapolate(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, double *const u[3],
+                        uint8_t *const valid[3], uint8_t *const valid1[3], double clear_val, int max_steps);
+void launch_enforce(cudaStream_t st, const Dims &d, const double origin[3], double h, const Faces &old,
+                    const Faces &us, const Faces &normal, const Faces &frac, double *const u[3]);
+void launch_vertex_pressures(cudaStream_t st, const Dims &d, const double origin[3], double h, const Faces &H,
+                             double chi, const double *pos, const double *nrm, long long nv, double *out);
+void launch_pressure_jump(cudaStream_t st, const Dims &d, const int32_t *const edge_mark[3], const double *kappa,
+                          const double *pm, double sigma, double rho, double h, double dt, double *const jump[3]);
 void launch_copy(cudaStream_t st, long long n, const double *a, double *o);
 void launch_to_f32(cudaStream_t st, long long n, const double *a, float *o);
 

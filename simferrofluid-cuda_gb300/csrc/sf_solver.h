@@ -127,7 +127,7 @@ class MGSolver {
     bool guess_ = false;
     double guess_yb_ = 0, guess_yay_ = 0;
     Dims cfg_dims_{0, 0, 0, 0};
-    int cfg_prec_ = -1, cfg_levels_ = -1, cfg_cdim_ = -1;
+    int cfg_prec_ = -1, cfg_levels_ = -1, cfg_cdim_ = -1, cfg_smoother_ = -1;
 
     // FP64 hierarchy (precision 0) or fine FP64 operator only (precision 1)
     std::vector<Coef<double>> c64_;
@@ -136,6 +136,7 @@ class MGSolver {
     // mixed: level 0 FP32, levels >= 1 FP16
     Coef<float> c32_{};
     std::vector<Coef<__half>> c16_;  // index l-1 for level l
+    Coef<__half> c16s0_{};           // level 0 in FP16, read only by the level-0 smoother (smoother 2)
     std::vector<float *> x32_, b32_, t32_;
 
     double *x_ = nullptr, *b_ = nullptr;

@@ -234,3 +234,22 @@ def test_fused_smoother_bit_identical(sfpkg, gpu_ctx, precision, shape):
     assert out[0][1] == out[1][1] and out[0][3] == out[1][3]
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("n,seed", [(32, 2), (48, 3)])
+def test_fp16_smoothing_coefficients_same_answer(sfpkg, oracle, gpu_ctx, n, seed):
+    """Smoother 2 (finest-level smoothing from an FP16 copy of the operator) changes only the preconditioner: the
+    mixed solve reaches the same tolerance on the FP64 operator and the same answer as the oracle."""
+    sc = scenes().pool_sphere(n, seed=seed)
+    og = oracle_grid(oracle, sc.grid)
+    u_or, p_or, _ = oracle.pressure_project(og, sc.phi, sc.frac, sc.vel, tol=1e-13)
+    psi_or, _, _ = oracle.magnetic_solve(og, sc.phi, sc.chi, sc.band_width, sc.hext, tol=1e-13)
+    P = sfpkg.Pressure(sc.grid, gpu_ctx)
+    st = P.project(_copy(sc.vel), sc.phi, sc.frac, opts=sfpkg.options("pressure", precision="mixed", smoother=2))
+    liquid = sc.phi <= 0
+    assert st["converged"] == 1 and st["rel_residual"] <= 1e-8 * 1.01
+    assert rel_l2(P.pressure[liquid], p_or[liquid]) <= P_TOL
+    M = sfpkg.MagneticField(sc.grid, sc.chi, sc.band_width, gpu_ctx)
+    sm = M.solve(sc.phi, sc.hext, opts=sfpkg.options("magnetic", precision="mixed", smoother=2, tol=1e-9))
+    assert sm["converged"] == 1 and sm["rel_residual_ref"] <= 1e-9 * 1.05
+    assert rel_l2(M.potential, psi_or) <= P_TOL
