@@ -86,6 +86,22 @@ def max_over_ranks(ws, v):
     return float(t.item())
 
 
+def profiled_traffic(summary, n):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the reported kernel, from the ncu
+    capture summarised in profiles/<summary> (a 256^3 launch), scaled to n^3 cells; None without a capture."""
+    if not summary:
+        return None
+    try:
+        with open(os.path.join(ROOT, "profiles", summary)) as f:
+            for line in f:
+                if line.startswith("| dram__bytes_read.sum + dram__bytes_write.sum"):
+                    mb = float(line.split("=")[-1].split("MB")[0])
+                    return round(mb * 1e6 * (n / 256.0) ** 3)
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 # ------------------------------------------------------------------------------------------------ clocks
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms while the timed region runs."""
@@ -254,13 +270,16 @@ def run_ours(args, ws, rank, local):
     smoother = 2 if args.smoother is None else args.smoother
     if smoother == 1:
         kname = "k_rbgs_tma (one full red-black sweep per launch, TMA-staged)"
+        prof = "k_rbgs_tma_pool_sphere_256.md"
     elif smoother == 2 and args.precision == "mixed":
         kname = "k_rbgs<float, __half> (one colour of a red-black sweep per launch, FP16 operator copy)"
+        prof = "k_rbgs_f16_finest_pool_sphere_256.md"
     else:
         kname = "k_rbgs (one colour of a red-black sweep per launch)"
+        prof = "k_rbgs_f32_finest_pool_sphere_256.md" if args.precision == "mixed" else None
     roofline = {"bound": "hbm", "kernel": kname + ", finest level",
                 "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None,
+                "frac": round(achieved / peak, 4), "traffic": profiled_traffic(prof, args.n),
                 "bytes_per_launch": bytes_tot / max(n_launch, 1), "ms_per_launch": ms_tot / max(n_launch, 1),
                 "launches_timed": n_launch}
 

@@ -49,13 +49,14 @@ void DevBuf::release() {
     n_ = 0;
 }
 
-// At most kMaxTileBlocks / tiles blocks along x, so the grid never exceeds kMaxTileBlocks blocks (the size
-// of the reduction partials) for any cross-section of up to kMaxTileBlocks tiles (checked in configure).
-dim3 tile_grid(const Dims &d, int &xpb) {
-    const long long tiles = (long long)((d.nz + 31) / 32) * ((d.ny + 7) / 8);
-    const long long zmax = tiles < kMaxTileBlocks ? kMaxTileBlocks / tiles : 1;
-    xpb = (int)((d.nx + zmax - 1) / zmax);
-    return dim3((d.nz + 31) / 32, (d.ny + 7) / 8, (d.nx + xpb - 1) / xpb);
+// Grid of the stencil reductions: work items of one 32 (z) x 8 (y) tile and `xpb` consecutive x planes, at most
+// max_blocks blocks looping over the items.  Memory-bound kernels take one item per block (kApplyBlocks); the
+// FP64-bound residual takes a persistent grid of 8 blocks per SM (kStencilBlocks), which shortens its tail.
+dim3 tile_grid(const Dims &d, int &xpb, int max_blocks) {
+    xpb = kStencilPlanes;
+    const long long items =
+        (long long)((d.nz + 31) / 32) * ((d.ny + 7) / 8) * ((d.nx + kStencilPlanes - 1) / kStencilPlanes);
+    return dim3((unsigned)(items < max_blocks ? items : max_blocks), 1, 1);
 }
 
 void Tracker::before(cudaStream_t st, bool fine) {
@@ -95,7 +96,10 @@ Tracker::~Tracker() {
 // Stencil kernels: block (32, 8) over (z, y), grid.z = x.  Red-black kernels cover cell pairs along z.
 static inline dim3 blk2() { return dim3(32, 8, 1); }
 static inline dim3 grid_cells(const Dims &d) { return dim3((d.nz + 31) / 32, (d.ny + 7) / 8, d.nx); }
-static inline dim3 grid_pairs(const Dims &d) { return dim3(((d.nz + 1) / 2 + 31) / 32, (d.ny + 7) / 8, d.nx); }
+constexpr int kRbRows = 1;  // rows per thread of the half sweep (block rows 8 apart); 2 measured slower
+static inline dim3 grid_pairs(const Dims &d) {
+    return dim3(((d.nz + 1) / 2 + 31) / 32, (d.ny + 8 * kRbRows - 1) / (8 * kRbRows), d.nx);
+}
 
 // ------------------------------------------------------------------------------------------------ smoothers
 template <class C>
@@ -121,34 +125,50 @@ __device__ __forceinline__ T couplings_sum(const Dims &d, const Coef<C> &cf, int
     return (T)sa;
 }
 
-// Red-black Gauss-Seidel half sweep.  Thread (kp, j, i) owns cells (i, j, 2kp) and (i, j, 2kp+1) and updates
-// the one whose colour (i + j + k) & 1 equals `color`.  Inactive cells (D = 0) are written 0.
-// ZERO: first half sweep of a V-cycle from x = 0; the other cell of the pair is zeroed, so x needs no
-// clearing beforehand and never carries stale values into the sweep.
+// Red-black Gauss-Seidel half sweep.  Thread (kp, j, i) owns cells (i, j, 2kp) and (i, j, 2kp+1) of kRbRows rows
+// j (8 apart) and updates the one of each pair whose colour (i + j + k) & 1 equals `color`.  Inactive cells
+// (D = 0) are written 0.  All rows are loaded before any is stored (more loads in flight per thread); the cells
+// written are of one colour and read only the other, so the order does not change the result.
+// ZERO: first half sweep of a V-cycle from x = 0; the other cell of each pair is zeroed, so x needs no clearing
+// beforehand and never carries stale values into the sweep.
 template <class T, class C, bool ZERO>
 __global__ void __launch_bounds__(256) k_rbgs(Dims d, Coef<C> cf, T *__restrict__ x, const T *__restrict__ b,
                                               int color) {
     const int kp = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
-    if (j >= d.ny) return;
-    const int par = (i + j + color) & 1;
-    const int k = 2 * kp + par;
-    if (ZERO) {
-        const int ko = 2 * kp + (par ^ 1);
-        if (ko < d.nz) x[cid(d, i, j, ko)] = T(0);
+    const int j0 = blockIdx.y * (8 * kRbRows) + threadIdx.y;
+    T res[kRbRows];
+    long long cc[kRbRows];
+    bool act[kRbRows];
+#pragma unroll
+    for (int r = 0; r < kRbRows; r++) {
+        const int j = j0 + 8 * r;
+        const int k = 2 * kp + ((i + j + color) & 1);
+        act[r] = j < d.ny && k < d.nz;
+        cc[r] = 0;
+        res[r] = T(0);
+        if (!act[r]) continue;
+        const long long c = cid(d, i, j, k);
+        T s, sa;
+        if (ZERO) {
+            s = T(0);
+            sa = (sizeof(C) == 8) ? T(0) : couplings_sum<T, C>(d, cf, i, j, k, c);
+        } else {
+            s = nbsum<T, C, sizeof(C) != 8>(d, cf, x, i, j, k, c, sa);
+        }
+        const T inv = (T)inv_diag<C>(cf, c, (typename Acc<C>::T)sa);
+        res[r] = (b[c] + s) * inv;
+        cc[r] = c;
     }
-    if (k >= d.nz) return;
-    const long long c = cid(d, i, j, k);
-    T s, sa;
-    if (ZERO) {
-        s = T(0);
-        sa = (sizeof(C) == 8) ? T(0) : couplings_sum<T, C>(d, cf, i, j, k, c);
-    } else {
-        s = nbsum<T, C, sizeof(C) != 8>(d, cf, x, i, j, k, c, sa);
+#pragma unroll
+    for (int r = 0; r < kRbRows; r++) {
+        const int j = j0 + 8 * r;
+        if (ZERO && j < d.ny) {
+            const int ko = 2 * kp + (((i + j + color) & 1) ^ 1);
+            if (ko < d.nz) x[cid(d, i, j, ko)] = T(0);
+        }
+        if (act[r]) x[cc[r]] = res[r];
     }
-    const T inv = (T)inv_diag<C>(cf, c, (typename Acc<C>::T)sa);
-    x[c] = (b[c] + s) * inv;
 }
 
 // ------------------------------------------------------------------------------------------------ fused sweep
@@ -714,18 +734,23 @@ __global__ void k_to16(long long n, Coef<double> f, Coef<__half> o) {
 }
 
 // ------------------------------------------------------------------------------------------------ Krylov kernels
-// Stencil kernels with a reduction: block (32, 8) over a (z, y) tile, each block walks `xpb` consecutive x
-// planes (so x +- 1 neighbours come from its own previous/next plane), at most kMaxTileBlocks blocks.  Threads
-// outside the grid keep looping so that every thread reaches the block reduction.
-#define TILE_LOOP(d, xpb)                                                                     \
-    const int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;           \
-    const bool inb = k < (d).nz && j < (d).ny;                                                \
-    const int i_end = min((d).nx, (int)(blockIdx.z + 1) * (xpb));                             \
-    for (int i = blockIdx.z * (xpb); i < i_end; i++) {                                        \
-        if (!inb) continue;                                                                   \
-        const long long c = cid((d), i, j, k);
+// Stencil kernels with a reduction: block (32, 8) looping over work items (tile_grid).  Item w = (z-tile
+// fastest, y-tile, x-chunk of `xpb` planes); consecutive blocks take neighbouring tiles of the same planes.
+// Threads outside the grid skip their cells but stay in the loop, so that every thread reaches the reduction.
+#define TILE_LOOP(d, xpb)                                                                          \
+    const unsigned tz_n = ((d).nz + 31) / 32, ty_n = ((d).ny + 7) / 8;                             \
+    const unsigned items = tz_n * ty_n * (((d).nx + (xpb)-1) / (xpb));                             \
+    for (unsigned w = blockIdx.x; w < items; w += gridDim.x) {                                     \
+        const unsigned tzi = w % tz_n, rest = w / tz_n, tyi = rest % ty_n, chunk = rest / ty_n;   \
+        const int k = (int)tzi * 32 + threadIdx.x, j = (int)tyi * 8 + threadIdx.y;                  \
+        if (k >= (d).nz || j >= (d).ny) continue;                                                  \
+        const int i_end = min((d).nx, (int)(chunk + 1) * (xpb));                                   \
+        for (int i = (int)chunk * (xpb); i < i_end; i++) {                                         \
+            const long long c = cid((d), i, j, k);
 
-#define TILE_LOOP_END }
+#define TILE_LOOP_END \
+    }                 \
+    }
 
 // q = A p ; slot PQ = (p, q) ; alpha = rho / pq (0 and breakdown flag if pq <= 0)
 // Per-thread partial sums are accumulated in the vector type (FP32 for FP32 vectors: FP64 arithmetic and
@@ -1081,8 +1106,9 @@ static void coarse_solve(cudaStream_t st, Tracker &tk, const Dims &d, const Coef
 
 // V-cycle z = M r.  Level 0 uses coefficient type C0, coarse levels Cc (cc[l] for level l >= 1).  ts[l] is a
 // scratch vector of level l for the fused smoother (nullptr entries select the in-place two-colour smoother).
-// c0s: level-0 coefficients read by the level-0 smoother (c0 itself, or a lower-precision copy); residuals and
-// restriction use c0.
+// c0s: level-0 coefficients read by the level-0 smoother and the residual restriction (c0 itself, or a
+// lower-precision copy, making the V-cycle a multigrid cycle for that copy); the coarsest solve of a one-level
+// hierarchy uses c0.
 template <class T, class C0, class Cc, class C0S>
 static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, const Coef<C0> &c0,
                    const Coef<C0S> &c0s, const std::vector<Coef<Cc>> &cc, T *z, const T *r,
@@ -1094,7 +1120,7 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
         return;
     }
     smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true);
-    restrict_res<T, C0>(st, tk, dims[0], c0, z, r, dims[1], bs[1]);
+    restrict_res<T, C0S>(st, tk, dims[0], c0s, z, r, dims[1], bs[1]);  // the residual of the smoothed operator
     for (int l = 1; l < L - 1; l++) {
         smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.pre, true);
         restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1]);
@@ -1145,10 +1171,6 @@ void *MGSolver::alloc(size_t bytes) {
 size_t MGSolver::device_bytes() const { return bytes_; }
 
 cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
-    if ((long long)((d.nz + 31) / 32) * ((d.ny + 7) / 8) > kMaxTileBlocks) {
-        last_error = "grid cross-section above 16384 tiles of 32 (z) x 8 (y) cells";
-        return cudaErrorInvalidValue;
-    }
     // level dims
     std::vector<Dims> dims{d};
     const int cdim = p.coarse_dim > 0 ? p.coarse_dim : 8;
@@ -1190,8 +1212,8 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     b_ = (double *)chk(A(8 * n));
     sc_ = (double *)chk(A(8 * S_NSLOTS));
     tk_.sc = sc_;
-    part_ = (double *)chk(A(8 * 4 * (size_t)(kMaxTileBlocks + kMaxTileBlocks / kRedGroup + 1)));
-    ticket_ = (unsigned *)chk(A(4 * (size_t)(2 + kMaxTileBlocks / kRedGroup)));
+    part_ = (double *)chk(A(8 * 4 * (size_t)(kMaxRedGrid + kMaxRedGrid / kRedGroup + 1)));
+    ticket_ = (unsigned *)chk(A(4 * (size_t)(2 + kMaxRedGrid / kRedGroup)));
     if (p.precision == 0) {
         x64_.assign(L, nullptr);
         b64_.assign(L, nullptr);
@@ -1253,7 +1275,7 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     }
     cudaError_t e = cudaMallocHost(&sc_host_, 8 * S_NSLOTS);
     if (e != cudaSuccess) return e;
-    cudaMemsetAsync(ticket_, 0, 4 * (size_t)(2 + kMaxTileBlocks / kRedGroup), st_);
+    cudaMemsetAsync(ticket_, 0, 4 * (size_t)(2 + kMaxRedGrid / kRedGroup), st_);
     cudaMemsetAsync(sc_, 0, 8 * S_NSLOTS, st_);
     cudaMemsetAsync(x_, 0, 8 * n, st_);
     configured_ = true;
@@ -1292,7 +1314,7 @@ void MGSolver::enqueue_iter64() {
     const Dims &d = lev_dims_[0];
     const long long n = d.n;
     int xpb;
-    const dim3 tg = tile_grid(d, xpb);
+    const dim3 tg = tile_grid(d, xpb, kApplyBlocks);
     const long long l0 = tk_.launches;
     vcycle<double, double, double, double>(st_, tk_, lev_dims_, c64_[0], c64_[0], c64_, z_, r_, x64_, b64_,
                                            prm_.smoother == 1 ? t64_ : std::vector<double *>(t64_.size(), nullptr),
@@ -1311,7 +1333,7 @@ void MGSolver::enqueue_iter32() {
     const Dims &d = lev_dims_[0];
     const long long n = d.n;
     int xpb;
-    const dim3 tg = tile_grid(d, xpb);
+    const dim3 tg = tile_grid(d, xpb, kApplyBlocks);
     const long long l0 = tk_.launches;
     const std::vector<float *> ts = prm_.smoother == 1 ? t32_ : std::vector<float *>(t32_.size(), nullptr);
     if (prm_.smoother == 2)
@@ -1397,7 +1419,7 @@ cudaError_t MGSolver::solve64(bool x_is_zero, SolveResult &res) {
     const Dims &d = lev_dims_[0];
     const long long n = d.n;
     int xpb;
-    const dim3 tg = tile_grid(d, xpb);
+    const dim3 tg = tile_grid(d, xpb, kStencilBlocks);
     cudaError_t e;
     if (x_is_zero) {
         cudaMemsetAsync(x_, 0, 8 * n, st_);
@@ -1457,7 +1479,7 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
     const Dims &d = lev_dims_[0];
     const long long n = d.n;
     int xpb;
-    const dim3 tg = tile_grid(d, xpb);
+    const dim3 tg = tile_grid(d, xpb, kStencilBlocks);
     cudaError_t e;
     if (x_is_zero) cudaMemsetAsync(x_, 0, 8 * n, st_);
     double bb = -1, rr = 0;
@@ -1559,7 +1581,7 @@ cudaError_t MGSolver::set_guess_scaled(const float *y, double &gamma) {
     if (prm_.precision != 1) return cudaErrorInvalidValue;
     const Dims &d = lev_dims_[0];
     int xpb;
-    const dim3 tg = tile_grid(d, xpb);
+    const dim3 tg = tile_grid(d, xpb, kApplyBlocks);
     // (y, A y) on the FP32 level-0 operator and (y, b); gamma minimises the A-norm error along y
     k_apply_dot<float, float><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c32_, y, q32_, sc_, part_, ticket_);
     k_dot_fd<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(d.n, y, b_, S_AUX2, sc_, part_, ticket_);
@@ -1579,7 +1601,7 @@ cudaError_t MGSolver::set_guess_scaled(const float *y, double &gamma) {
 cudaError_t MGSolver::true_relres(bool skip0, double &relres, double &bnorm) {
     const Dims &d = lev_dims_[0];
     int xpb;
-    const dim3 tg = tile_grid(d, xpb);
+    const dim3 tg = tile_grid(d, xpb, kStencilBlocks);
     k_residual64<double><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c64_[0], x_, b_, (double *)nullptr, skip0 ? 1 : 0,
                                                       S_AUX1, S_AUX2, sc_, part_, ticket_);
     tk_.launches++;

@@ -166,7 +166,10 @@ class MGSolver {
 
 // Launch helpers
 constexpr int kMaxRedBlocks = 152 * 8;
-constexpr int kMaxTileBlocks = 16384;
-dim3 tile_grid(const Dims &d, int &xpb);
+constexpr int kStencilBlocks = 152 * 8;  // persistent grid of the FP64 residual
+constexpr int kApplyBlocks = 16384;      // one work item per block for the memory-bound stencil reductions
+constexpr int kStencilPlanes = 4;        // x planes per work item
+constexpr int kMaxRedGrid = kApplyBlocks;
+dim3 tile_grid(const Dims &d, int &xpb, int max_blocks);
 
 }  // namespace sf

@@ -1,0 +1,177 @@
+"""A long sequence of substeps at large resolution: one magnetic potential solve (warm-started from the previous
+substep's potential, as the reference's m_Sol) and one pressure projection per substep, on device-resident
+inputs, for the mixed form and the plain FP64 method in turn.
+
+Scene (seeded, synthetic): pool of depth 0.2 with a 1% height perturbation (0.01 n(x, z), n seeded uniform
+[-1, 1] on an 8x8 lattice, bilinear), chi = 1.5, walls on the grid faces, vertical applied field H0 = (0, s/S, 0)
+at substep s = 1..S, and per substep a fresh velocity of seeded smooth noise with |u| <= 0.5 (uniform [-1, 1] on a
+9^3 lattice, trilinear, times 0.5).  Every input is generated on the device.
+
+The collider fractions of the box walls are the library's (sf_collider_box_fractions) on a 12^3 grid of the same
+spacing, extended to the full grid: a face's fraction depends only on the walls within a few cells of it (the
+fast-marching distance near a wall is computed outward from the wall), so faces more than 6 cells from every
+wall take the interior value.  The extension agrees with the full-size collider to the last bits of the
+level-set arithmetic.
+
+  python -m <package>.sequence --n 768 --substeps 50
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+def _pkg():
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
+    return importlib.import_module(os.path.basename(HERE))
+
+
+def _stretch(m_large, m_small, c):
+    """Index map of a large axis onto a small one: the first and last c entries kept, the middle -> c."""
+    i = np.arange(m_large)
+    out = np.full(m_large, c)
+    out[i < c] = i[i < c]
+    hi = (m_large - 1 - i) < c
+    out[hi] = (m_small - 1) - (m_large - 1 - i[hi])
+    return out
+
+
+def box_fractions_device(sf, scenes, torch, g, dev, c=6):
+    n = 2 * c
+    small = sf.StaggeredGrid.from_origin(g.spacing, (n, n, n))
+    fs = scenes.box_fractions(small)
+    out = []
+    for a in range(3):
+        idx = [torch.from_numpy(_stretch(g.shape[b] + (b == a), n + (b == a), c)).to(dev) for b in range(3)]
+        src = torch.from_numpy(fs[a]).to(dev)
+        out.append(src[idx[0]][:, idx[1]][:, :, idx[2]].contiguous())
+    return out
+
+
+def pool_phi_device(scenes, torch, g, dev, seed, depth=0.2, noise=0.01):
+    rng = np.random.default_rng(seed)
+    xs, ys, zs = (scenes.cell_centres(g, a) for a in range(3))
+    nz = torch.from_numpy(scenes.lattice_noise(xs, zs, rng)).to(dev)
+    y = torch.from_numpy(ys).to(dev)
+    return (y.view(1, -1, 1) - depth + noise * nz.view(g.shape[0], 1, g.shape[2])).contiguous()
+
+
+def smooth_velocity(torch, g, dev, gen, vmax=0.5, lattice=9):
+    import torch.nn.functional as F
+    out = []
+    for a in range(3):
+        lat = torch.rand((1, 1, lattice, lattice, lattice), generator=gen, device=dev, dtype=torch.float64) * 2 - 1
+        out.append((F.interpolate(lat, size=g.face_shape(a), mode="trilinear", align_corners=True)[0, 0] * vmax)
+                   .contiguous())
+    return out
+
+
+def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None):
+    import torch
+    sf = _pkg()
+    scenes = importlib.import_module(sf.__name__ + ".scenes")
+    dev = torch.device("cuda", 0)
+    g = sf.StaggeredGrid.from_origin(1.0 / n, (n, n, n))
+    t0 = time.time()
+    phi = pool_phi_device(scenes, torch, g, dev, seed)
+    frac = box_fractions_device(sf, scenes, torch, g, dev)
+    hext = [torch.zeros(g.face_shape(a), dtype=torch.float64, device=dev) for a in range(3)]
+    H = [torch.zeros(g.face_shape(a), dtype=torch.float64, device=dev) for a in range(3)]
+    psi = torch.zeros(g.shape, dtype=torch.float64, device=dev)
+    p_out = torch.zeros(g.shape, dtype=torch.float64, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    torch.cuda.synchronize()
+    setup_s = time.time() - t0
+    ctx = sf.Context(0, stream=torch.cuda.current_stream().cuda_stream)
+    M = sf.MagneticField(g, 1.5, 2 * g.spacing, ctx)
+    P = sf.Pressure(g, ctx)
+    rows = []
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    solve_ms = 0.0
+    for s in range(1, substeps + 1):
+        hext[1].fill_(s / substeps)
+        vel = smooth_velocity(torch, g, dev, gen)
+        prof = 1 if (profile_last and s == substeps) else 0
+        e0.record()
+        sm = M.solve(phi, hext, device=True, psi_out=psi, H_out=H,
+                     opts=sf.options("magnetic", precision=precision, profile=prof))
+        e1.record()
+        sp = P.project(vel, phi, frac, device=True, p_out=p_out,
+                       opts=sf.options("pressure", precision=precision, tol=1e-6, profile=prof))
+        e2.record()
+        torch.cuda.synchronize()
+        ms_m, ms_p = e0.elapsed_time(e1), e1.elapsed_time(e2)
+        if not prof:
+            solve_ms += ms_m + ms_p
+        rows.append(dict(substep=s, mag_iters=sm["iters"], mag_ms=ms_m, mag_relres=sm["rel_residual_ref"],
+                         pres_iters=sp["iters"], pres_ms=ms_p, pres_relres=sp["rel_residual"],
+                         smooth_ms=sm["smooth_ms"] + sp["smooth_ms"], smooth_bytes=sm["smooth_bytes"] + sp["smooth_bytes"],
+                         smooth_launches=sm["smooth_launches"] + sp["smooth_launches"]))
+        if log:
+            r = rows[-1]
+            log(f"{precision} substep {s:3d}: potential {r['mag_iters']:3d} it {ms_m:8.1f} ms | pressure "
+                f"{r['pres_iters']:3d} it {ms_p:8.1f} ms")
+        del vel
+    timed = [r for r in rows if not (profile_last and r["substep"] == substeps)]
+    last = rows[-1]
+    out = dict(precision=precision, grid=[n, n, n], substeps=substeps, setup_s=round(setup_s, 2),
+               solve_s=round(solve_ms / 1e3, 3), solves=2 * len(timed),
+               solves_per_s=round(2 * len(timed) / (solve_ms / 1e3), 3) if solve_ms > 0 else None,
+               mean_ms=dict(potential=float(np.mean([r["mag_ms"] for r in timed])),
+                            pressure=float(np.mean([r["pres_ms"] for r in timed]))),
+               iters=dict(potential=[r["mag_iters"] for r in rows], pressure=[r["pres_iters"] for r in rows]),
+               max_rel_residual=dict(potential=max(r["mag_relres"] for r in rows),
+                                     pressure=max(r["pres_relres"] for r in rows)),
+               device_bytes=ctx.device_bytes())
+    if profile_last and last["smooth_launches"]:
+        out["smoother"] = dict(ms_per_launch=last["smooth_ms"] / last["smooth_launches"],
+                               bytes_per_launch=last["smooth_bytes"] / last["smooth_launches"],
+                               achieved_gbs=last["smooth_bytes"] / (last["smooth_ms"] / 1e3) / 1e9)
+    ctx.close()
+    del phi, frac, hext, H, psi, p_out
+    torch.cuda.empty_cache()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=768)
+    ap.add_argument("--substeps", type=int, default=50)
+    ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--precision", default="both", choices=["mixed", "fp64", "both"])
+    ap.add_argument("--out", default=None)
+    args = ap.parse_args()
+    import torch
+    torch.cuda.set_device(0)
+    precs = ["mixed", "fp64"] if args.precision == "both" else [args.precision]
+    res = {p: run(p, args.n, args.substeps, args.seed, log=lambda m: print(m, flush=True)) for p in precs}
+    if len(precs) == 2:
+        res["speedup_mixed_vs_fp64"] = round(res["fp64"]["solve_s"] / res["mixed"]["solve_s"], 3)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    for p in precs:
+        if "smoother" in res[p] and peaks.get("hbm_gbs"):
+            res[p]["smoother"]["frac_of_measured_hbm"] = res[p]["smoother"]["achieved_gbs"] / peaks["hbm_gbs"]
+    print(json.dumps(res), flush=True)
+    if args.out:
+        with open(args.out, "w") as f:
+            json.dump(res, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()
