@@ -244,6 +244,19 @@ SF_EXPORT sf_status sf_pressure_jump_dev(void *ctx, const sf_grid *g, const int3
                                          const double *curvature, const double *mag_pressure, long long nverts,
                                          double st_coeff, double density, double dt, double *const jump[3]);
 
+/* ----- level-set neighbours (core/Simulation.cpp:164-165, 265) --------------------------------------------------
+ * Advection::Solve<2> (core/Advection.h:33-59): semi-Lagrangian advection over dt with the TVD RK2 trace through
+ * the velocity (trilinear per face grid); the level set is interpolated tricubically (TriCuInterp), the velocity
+ * (advected by itself) trilinearly.  Reinitialization::Solve (core/Reinitialization.cpp:36-76): max_steps TVD-RK3
+ * steps of the reinitialisation equation with WENO5 derivatives, dt = h/2.  All update their arrays in place. */
+SF_EXPORT sf_status sf_advect_levelset(void *ctx, const sf_grid *g, double *phi, const double *const vel[3], double dt);
+SF_EXPORT sf_status sf_advect_levelset_dev(void *ctx, const sf_grid *g, double *phi, const double *const vel[3],
+                                           double dt);
+SF_EXPORT sf_status sf_advect_velocity(void *ctx, const sf_grid *g, double *const vel[3], double dt);
+SF_EXPORT sf_status sf_advect_velocity_dev(void *ctx, const sf_grid *g, double *const vel[3], double dt);
+SF_EXPORT sf_status sf_reinitialize(void *ctx, const sf_grid *g, double *phi, int max_steps);
+SF_EXPORT sf_status sf_reinitialize_dev(void *ctx, const sf_grid *g, double *phi, int max_steps);
+
 /* Forget the magnetic warm start (MagneticField ctor zeroes m_Sol, core/MagneticField.cpp:26). */
 SF_EXPORT sf_status sf_magnetic_reset(void *ctx);
 

@@ -110,16 +110,53 @@ inline void check(void *ctx, sf_status s, const sf_solve_stats &st, bool verbose
 struct Collider {
     SGridData Fraction;
     SGridData Velocity;
+    SGridData Normal;  // m_Normal: face means of the node level set's derivatives (core/Collider.cpp:30-44)
     static Collider Box(const StaggeredGrid &g) {
         Collider c;
         c.Fraction = SGridData(g);
         c.Velocity = SGridData(g);
+        c.Normal = SGridData(g);
         sf_grid cg = g.C();
+        std::vector<double> ls((size_t)(g.Resolution[0] + 1) * (g.Resolution[1] + 1) * (g.Resolution[2] + 1));
         double *fr[3] = {c.Fraction[0].data(), c.Fraction[1].data(), c.Fraction[2].data()};
-        sf_status s = sf_collider_box_fractions(&cg, g.BoundaryWidth, fr, nullptr);
+        sf_status s = sf_collider_box_fractions(&cg, g.BoundaryWidth, fr, ls.data());
         if (s != SF_OK) throw Error(s, "sf_collider_box_fractions failed");
+        double *nm[3] = {c.Normal[0].data(), c.Normal[1].data(), c.Normal[2].data()};
+        if ((s = sf_collider_face_normals(&cg, ls.data(), nm)) != SF_OK) throw Error(s, "sf_collider_face_normals failed");
         return c;
     }
+    // Collider::Enforce (core/Collider.cpp:75-86) on the GPU.
+    void Enforce(Context &ctx, const StaggeredGrid &g, SGridData &fluidVelocity) const {
+        sf_grid cg = g.C();
+        double *v[3] = {fluidVelocity[0].data(), fluidVelocity[1].data(), fluidVelocity[2].data()};
+        const double *fr[3] = {Fraction[0].data(), Fraction[1].data(), Fraction[2].data()};
+        const double *nm[3] = {Normal[0].data(), Normal[1].data(), Normal[2].data()};
+        const double *us[3] = {Velocity[0].data(), Velocity[1].data(), Velocity[2].data()};
+        sf_status s = sf_collider_enforce(ctx.Handle(), &cg, v, fr, nm, Velocity[0].empty() ? nullptr : us);
+        if (s != SF_OK) throw Error(s, std::string("sf_collider_enforce: ") + sf_last_error(ctx.Handle()));
+    }
+};
+
+// Extrapolation::Solve of the projected velocity (core/Extrapolation.cpp:4-30) with the simulation's validity
+// predicate (core/Simulation.cpp:237-240), on the GPU.
+struct Extrapolation {
+    static void Solve(Context &ctx, const StaggeredGrid &g, SGridData &velocity, const GridData &levelSet,
+                      const Collider &collider, double clearVal = 0., int maxSteps = 6) {
+        sf_grid cg = g.C();
+        double *v[3] = {velocity[0].data(), velocity[1].data(), velocity[2].data()};
+        const double *fr[3] = {collider.Fraction[0].data(), collider.Fraction[1].data(), collider.Fraction[2].data()};
+        sf_status s = sf_extrapolate_velocity(ctx.Handle(), &cg, v, levelSet.data(), fr, clearVal, maxSteps);
+        if (s != SF_OK) throw Error(s, std::string("sf_extrapolate_velocity: ") + sf_last_error(ctx.Handle()));
+    }
+};
+
+// The parts of core/SurfaceMesh.h the interface coupling reads, and the contour's edge marks
+// (Contour::VertexIndexOf, core/Contour.h:19-21: one int per cell-grid edge along each axis, -1 = no vertex).
+struct SurfaceMesh {
+    std::vector<std::array<double, 3>> Positions, Normals;
+    std::vector<double> MeanCurvatures;
+    std::array<std::vector<int32_t>, 3> EdgeMark;
+    int size() const { return (int)Positions.size(); }
 };
 
 // Pressure projection (core/Pressure.h:8-56).
@@ -135,6 +172,22 @@ class Pressure {
     template <typename Func>
     void SetPressureJump(Func &&f) {
         jump_ = JumpFunc(std::forward<Func>(f));
+        jump_array_ = false;
+    }
+    // The simulation's jump (core/Simulation.cpp:216-235) built on the GPU from the mesh: curvature term when
+    // stCoeff != 0, magnetic term from magPressures (CalculateVertexPressures) when given.
+    void SetPressureJump(const StaggeredGrid &g, const SurfaceMesh &mesh, const std::vector<double> *magPressures,
+                         double stCoeff, double density, double dt) {
+        sf_grid cg = g.C();
+        const int32_t *em[3] = {mesh.EdgeMark[0].data(), mesh.EdgeMark[1].data(), mesh.EdgeMark[2].data()};
+        for (int a = 0; a < 3; a++) jarr_[a].assign(g_.NumFaces(a), 0.0);
+        double *jp[3] = {jarr_[0].data(), jarr_[1].data(), jarr_[2].data()};
+        sf_status s = sf_pressure_jump(ctx_.Handle(), &cg, em, stCoeff != 0 ? mesh.MeanCurvatures.data() : nullptr,
+                                       magPressures ? magPressures->data() : nullptr, mesh.size(), stCoeff, density,
+                                       dt, jp);
+        if (s != SF_OK) throw Error(s, std::string("sf_pressure_jump: ") + sf_last_error(ctx_.Handle()));
+        jump_ = nullptr;
+        jump_array_ = true;
     }
 
     void Project(SGridData &velocity, const GridData &levelSet, const Collider &collider, double volError = 0) {
@@ -176,14 +229,14 @@ class Pressure {
         const double *us[3] = {col.Velocity[0].data(), col.Velocity[1].data(), col.Velocity[2].data()};
         const double *jp[3] = {nullptr, nullptr, nullptr};
         bool has_us = !col.Velocity[0].empty();
-        if (jump_) {
-            fill_jump(phi, col);
+        if (jump_) fill_jump(phi, col);
+        const bool has_jump = jump_ || jump_array_;
+        if (has_jump)
             for (int a = 0; a < 3; a++) jp[a] = jarr_[a].data();
-        }
         p_.assign(g_.NumCells(), 0.0);
         sf_grid cg = g_.C();
         sf_status s = (re ? sf_pressure_reproject : sf_pressure_project)(
-            ctx_.Handle(), &cg, v, phi.data(), fr, has_us ? us : nullptr, jump_ ? jp : nullptr, volError, p_.data(),
+            ctx_.Handle(), &cg, v, phi.data(), fr, has_us ? us : nullptr, has_jump ? jp : nullptr, volError, p_.data(),
             &opts_, &stats_);
         check(ctx_.Handle(), s, stats_, Verbose);
     }
@@ -191,6 +244,7 @@ class Pressure {
     Context &ctx_;
     StaggeredGrid g_;
     JumpFunc jump_;
+    bool jump_array_ = false;
     std::array<std::vector<double>, 3> jarr_;
     GridData p_;
     sf_solve_opts opts_;
@@ -222,6 +276,18 @@ class MagneticField {
 
     const GridData &Potential() const { return psi_; }
     const SGridData &TotalField() const { return H_; }
+
+    // MagneticField::CalculateVertexPressures (core/MagneticField.cpp:37-48) from the last solve's total field.
+    std::vector<double> CalculateVertexPressures(const SurfaceMesh &mesh) const {
+        std::vector<double> p(mesh.Positions.size());
+        if (p.empty()) return p;
+        sf_grid cg = g_.C();
+        const double *H[3] = {H_[0].data(), H_[1].data(), H_[2].data()};
+        sf_status s = sf_magnetic_vertex_pressures(ctx_.Handle(), &cg, chi_, H, mesh.Positions[0].data(),
+                                                   mesh.Normals[0].data(), (long long)p.size(), p.data());
+        if (s != SF_OK) throw Error(s, std::string("sf_magnetic_vertex_pressures: ") + sf_last_error(ctx_.Handle()));
+        return p;
+    }
     sf_solve_opts &Options() { return opts_; }
     const sf_solve_stats &LastStats() const { return stats_; }
     bool Verbose = false;

@@ -106,6 +106,9 @@ def lib():
         L.or_collider_face_normals.argtypes = [G, _D, _D3]
         L.or_collider_enforce.argtypes = [G, _D3, _D3, _D3, C.c_void_p]
         L.or_vertex_pressures.argtypes = [G, C.c_double, _D3, _D, _D, C.c_int64, _D]
+        L.or_advect_levelset.argtypes = [G, _D, _D3, C.c_double, _D]
+        L.or_advect_velocity.argtypes = [G, _D3, C.c_double, _D3]
+        L.or_reinitialize.argtypes = [G, _D, C.c_int]
         L.or_pressure_jump.argtypes = [G, C.c_void_p * 3, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                        C.c_double, _D3]
         L.or_amg_solve.argtypes = [C.c_int, C.c_int64, _I64, _I32, _D, _D, _D, C.c_double, C.c_int,
@@ -357,6 +360,30 @@ def pressure_jump(g: Grid, edge_mark, kappa=None, pm=None, sigma=0.0, rho=1.0, d
                            None if kp is None else kp.ctypes.data, None if pp is None else pp.ctypes.data,
                            float(sigma), float(rho), float(dt), _D3(*[_p(a) for a in jump]))
     return jump
+
+
+def advect_levelset(g: Grid, phi, u, dt):
+    """Advection::Solve<2>(levelSet, velocity, dt) (core/Advection.h:40-49); returns the new level set."""
+    phi = _f64(phi)
+    ur, up = _faces(u)
+    out = np.empty(g.shape)
+    lib().or_advect_levelset(C.byref(g.c()), _p(phi), up, float(dt), _p(out))
+    return out
+
+
+def advect_velocity(g: Grid, u, dt):
+    """Advection::Solve<2>(velocity, velocity, dt) (core/Advection.h:51-59); returns the new face arrays."""
+    ur, up = _faces(u)
+    out = [np.empty(g.face_shape(a)) for a in range(3)]
+    lib().or_advect_velocity(C.byref(g.c()), up, float(dt), _D3(*[_p(a) for a in out]))
+    return out
+
+
+def reinitialize(g: Grid, phi, max_steps=10):
+    """Reinitialization::Solve (core/Reinitialization.cpp:36-46); returns the new level set."""
+    out = np.array(phi, dtype=np.float64, copy=True)
+    lib().or_reinitialize(C.byref(g.c()), _p(out), int(max_steps))
+    return out
 
 
 def num_threads() -> int:

@@ -938,3 +938,182 @@ void or_pressure_jump(const or_grid *g, const int32_t *const edge_mark[3], const
                 }
     }
 }
+
+/* ------------------------------------------------------------------------------------------------------------
+ * Level-set neighbours of the path (core/Simulation.cpp:164-165, 265): semi-Lagrangian advection and
+ * WENO5/TVD-RK3 reinitialisation.
+ * ---------------------------------------------------------------------------------------------------------- */
+
+static inline double dmax(double a, double b) { return (a < b) ? b : a; } /* std::max(a, b) */
+
+/* TriLerp of the three face grids at p (TriLerp::Interpolate(SGridData), core/TriLerp.h:62-66). */
+static void trilerp_flow(const or_grid *g, const double *const u[3], const double p[3], double out[3]) {
+    for (int b = 0; b < 3; b++) out[b] = trilerp_face(g, u[b], b, p);
+}
+
+/* Advection::Trace<2> (core/Advection.h:15-18): the TVD Runge-Kutta trace of second order from p over dt. */
+static void trace_rk2(const or_grid *g, const double *const u[3], const double p[3], double dt, double out[3]) {
+    double v0[3], v1[3], q[3];
+    trilerp_flow(g, u, p, v0);
+    for (int a = 0; a < 3; a++) q[a] = p[a] + v0[a] * dt;
+    trilerp_flow(g, u, q, v1);
+    for (int a = 0; a < 3; a++) out[a] = p[a] + (v0[a] + v1[a]) * dt / 2;
+}
+
+/* TriCuInterp::Interpolate of the cell grid at p (core/TriCuInterp.h:12-37): CalcLower<3> = floor((p - o)/h - 1),
+ * cubic Lagrange weights per axis, 64 points in (k, j, i) order, clamped At(). */
+static double tricubic_cell(const or_grid *g, const double *f, const double p[3]) {
+    double co[3] = {g->ox + g->h / 2, g->oy + g->h / 2, g->oz + g->h / 2};
+    int sz[3] = {g->nx, g->ny, g->nz};
+    double invh = 1 / g->h;
+    int lo[3];
+    double w[4][3];
+    for (int a = 0; a < 3; a++) {
+        lo[a] = (int)floor((p[a] - co[a]) * invh - 1.0);
+        double fr = (p[a] - co[a] - (double)lo[a] * g->h) * invh;
+        w[0][a] = (fr - 1) * (fr - 2) * (fr - 3) / -6;
+        w[1][a] = fr * (fr - 2) * (fr - 3) / 2;
+        w[2][a] = fr * (fr - 1) * (fr - 3) / -2;
+        w[3][a] = fr * (fr - 1) * (fr - 2) / 6;
+    }
+    double val = 0;
+    for (int k = 0; k < 4; k++)
+        for (int j = 0; j < 4; j++)
+            for (int i = 0; i < 4; i++) {
+                int ci[3] = {lo[0] + i, lo[1] + j, lo[2] + k};
+                for (int a = 0; a < 3; a++) ci[a] = ci[a] < 0 ? 0 : (ci[a] > sz[a] - 1 ? sz[a] - 1 : ci[a]);
+                val += f[cidx(g, ci[0], ci[1], ci[2])] * (w[i][0] * w[j][1] * w[k][2]);
+            }
+    return val;
+}
+
+/* Advection::Solve<2>(levelSet, velocity, dt) (core/Advection.h:40-49): phi at the RK2 departure point of each
+ * cell centre, by tricubic interpolation of the old phi.  phi_out must not alias phi. */
+void or_advect_levelset(const or_grid *g, const double *phi, const double *const u[3], double dt, double *phi_out) {
+    double co[3] = {g->ox + g->h / 2, g->oy + g->h / 2, g->oz + g->h / 2};
+    for (int i = 0; i < g->nx; i++)
+        for (int j = 0; j < g->ny; j++)
+            for (int k = 0; k < g->nz; k++) {
+                double p[3] = {co[0] + (double)i * g->h, co[1] + (double)j * g->h, co[2] + (double)k * g->h};
+                double q[3];
+                trace_rk2(g, u, p, -dt, q);
+                phi_out[cidx(g, i, j, k)] = tricubic_cell(g, phi, q);
+            }
+}
+
+/* Advection::Solve<2>(velocity, velocity, dt) (core/Advection.h:51-59): each face value at the RK2 departure
+ * point of its face, by trilinear interpolation of its own old face grid.  u_out must not alias u. */
+void or_advect_velocity(const or_grid *g, const double *const u[3], double dt, double *const u_out[3]) {
+    double o[3] = {g->ox, g->oy, g->oz};
+    for (int a = 0; a < 3; a++) {
+        int fx, fy, fz;
+        fdims(g, a, &fx, &fy, &fz);
+        for (int i = 0; i < fx; i++)
+            for (int j = 0; j < fy; j++)
+                for (int k = 0; k < fz; k++) {
+                    int c3[3] = {i, j, k};
+                    double p[3], q[3];
+                    for (int b = 0; b < 3; b++) p[b] = (b == a ? o[b] : o[b] + g->h / 2) + (double)c3[b] * g->h;
+                    trace_rk2(g, u, p, -dt, q);
+                    u_out[a][fidx(g, a, i, j, k)] = trilerp_face(g, u[a], a, q);
+                }
+    }
+}
+
+/* GetDrv (core/Reinitialization.cpp:4-27): WENO5 one-sided derivatives (minus, plus) from 7 values. */
+static void weno_drv(const double v[7], double invdx, double *dm, double *dp) {
+    for (int s = 0; s < 2; s++) {
+        double dev[5];
+        if (s) {
+            dev[0] = v[6] - v[5]; dev[1] = v[5] - v[4]; dev[2] = v[4] - v[3]; dev[3] = v[3] - v[2]; dev[4] = v[2] - v[1];
+        } else {
+            dev[0] = v[1] - v[0]; dev[1] = v[2] - v[1]; dev[2] = v[3] - v[2]; dev[3] = v[4] - v[3]; dev[4] = v[5] - v[4];
+        }
+        double eps = 0;
+        for (int j = 0; j < 5; j++) eps = dmax(eps, dev[j] * dev[j]);
+        eps = eps * 1e-6 + 1e-99;
+        double phix1 = dev[0] / 3 - dev[1] * 7 / 6 + dev[2] * 11 / 6;
+        double phix2 = -dev[1] / 6 + dev[2] * 5 / 6 + dev[3] / 3;
+        double phix3 = dev[2] / 3 + dev[3] * 5 / 6 - dev[4] / 6;
+        double t;
+        t = dev[0] - 2 * dev[1] + dev[2];
+        double s1 = t * t * 13 / 12;
+        t = dev[0] - 4 * dev[1] + 3 * dev[2];
+        s1 = s1 + t * t / 4;
+        t = dev[1] - 2 * dev[2] + dev[3];
+        double s2 = t * t * 13 / 12;
+        t = dev[1] - dev[3];
+        s2 = s2 + t * t / 4;
+        t = dev[2] - 2 * dev[3] + dev[4];
+        double s3 = t * t * 13 / 12;
+        t = 3 * dev[2] - 4 * dev[3] + dev[4];
+        s3 = s3 + t * t / 4;
+        t = s1 + eps;
+        double alpha1 = .1 / (t * t);
+        t = s2 + eps;
+        double alpha2 = .6 / (t * t);
+        t = s3 + eps;
+        double alpha3 = .3 / (t * t);
+        double sum = alpha1 + alpha2 + alpha3;
+        double d = (alpha1 * phix1 + alpha2 * phix2 + alpha3 * phix3) / sum * invdx;
+        if (s) *dp = d; else *dm = d;
+    }
+}
+
+/* Reinitialization::Advance (core/Reinitialization.cpp:48-74) into out (must not alias f). */
+static void reinit_advance(const or_grid *g, const double *f, double *out, double dt) {
+    int sz[3] = {g->nx, g->ny, g->nz};
+    double invdx = 1 / g->h;
+    for (int i = 0; i < g->nx; i++)
+        for (int j = 0; j < g->ny; j++)
+            for (int k = 0; k < g->nz; k++) {
+                double dm[3], dp[3];
+                for (int a = 0; a < 3; a++) {
+                    double v[7];
+                    for (int q = 0; q < 7; q++) {
+                        int c[3] = {i, j, k};
+                        c[a] += q - 3;
+                        c[a] = c[a] < 0 ? 0 : (c[a] > sz[a] - 1 ? sz[a] - 1 : c[a]); /* At(): clamped */
+                        v[q] = f[cidx(g, c[0], c[1], c[2])];
+                    }
+                    weno_drv(v, invdx, &dm[a], &dp[a]);
+                }
+                double fc = f[cidx(g, i, j, k)];
+                double sum = 0, t;
+                if (fc < 0) {
+                    for (int a = 0; a < 3; a++) {
+                        t = dm[a] < 0. ? dm[a] : 0.; /* std::min(x, 0.) */
+                        sum += t * t;
+                        t = dmax(dp[a], 0.);
+                        sum += t * t;
+                    }
+                } else {
+                    for (int a = 0; a < 3; a++) {
+                        t = dmax(dm[a], 0.);
+                        sum += t * t;
+                        t = dp[a] < 0. ? dp[a] : 0.;
+                        sum += t * t;
+                    }
+                }
+                sum = sqrt(sum);
+                double sp = g->h * sum;
+                double sgn = fc / sqrt(fc * fc + sp * sp);
+                out[cidx(g, i, j, k)] = fc + dt * sgn * (1. - sum);
+            }
+}
+
+/* Reinitialization::Solve (core/Reinitialization.cpp:36-46): max_steps TVD-RK3 steps with dt = h / 2. */
+void or_reinitialize(const or_grid *g, double *phi, int max_steps) {
+    int64_t n = (int64_t)g->nx * g->ny * g->nz;
+    double *p1 = (double *)malloc(8 * n), *p2 = (double *)malloc(8 * n);
+    double dt = g->h * .5;
+    for (int it = 0; it < max_steps; it++) {
+        reinit_advance(g, phi, p1, dt);
+        reinit_advance(g, p1, p2, dt);
+        for (int64_t c = 0; c < n; c++) p1[c] = (phi[c] * 3 + p2[c]) / 4;
+        reinit_advance(g, p1, p2, dt);
+        for (int64_t c = 0; c < n; c++) phi[c] = (phi[c] + p2[c] * 2) / 3;
+    }
+    free(p1);
+    free(p2);
+}

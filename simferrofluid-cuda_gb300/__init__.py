@@ -480,3 +480,46 @@ class ColliderEnforce:
         s = fn(self.ctx.handle, C.byref(g.c_grid()), _abi.p3(vel), _abi.p3(fr), _abi.p3(nm),
                us_ref[0] if us_ref else None)
         _check(self.ctx, s, None, "collider enforce", True)
+
+
+# ------------------------------------------------------------------------------------------------ level set
+class Advection:
+    """Advection::Solve<2> (core/Advection.h:33-59) on the GPU: semi-Lagrangian with the TVD RK2 trace."""
+
+    def __init__(self, sgrid: StaggeredGrid, ctx: Context | None = None):
+        self.grid = sgrid
+        self.ctx = ctx or default_context()
+
+    def solve_levelset(self, level_set, velocity, dt, device=False):
+        """Advection::Solve<2>(levelSet, velocity, dt): the level set (updated in place), tricubic."""
+        g, keep = self.grid, []
+        fs = [g.face_shape(a) for a in range(3)]
+        phi = _ptr(level_set, g.shape, "level_set", device, True, keep)
+        vel = [_ptr(velocity[a], fs[a], f"velocity[{a}]", device, False, keep) for a in range(3)]
+        fn = self.ctx.lib.sf_advect_levelset_dev if device else self.ctx.lib.sf_advect_levelset
+        s = fn(self.ctx.handle, C.byref(g.c_grid()), C.c_void_p(phi), _abi.p3(vel), float(dt))
+        _check(self.ctx, s, None, "level-set advection", True)
+
+    def solve_velocity(self, velocity, dt, device=False):
+        """Advection::Solve<2>(velocity, velocity, dt): the velocity advected by itself (in place), trilinear."""
+        g, keep = self.grid, []
+        fs = [g.face_shape(a) for a in range(3)]
+        vel = [_ptr(velocity[a], fs[a], f"velocity[{a}]", device, True, keep) for a in range(3)]
+        fn = self.ctx.lib.sf_advect_velocity_dev if device else self.ctx.lib.sf_advect_velocity
+        s = fn(self.ctx.handle, C.byref(g.c_grid()), _abi.p3(vel), float(dt))
+        _check(self.ctx, s, None, "velocity advection", True)
+
+
+class Reinitialization:
+    """Reinitialization::Solve (core/Reinitialization.cpp:36-76) on the GPU: WENO5 + TVD-RK3, dt = h/2."""
+
+    def __init__(self, sgrid: StaggeredGrid, ctx: Context | None = None):
+        self.grid = sgrid
+        self.ctx = ctx or default_context()
+
+    def solve(self, level_set, max_steps=10, device=False):
+        g, keep = self.grid, []
+        phi = _ptr(level_set, g.shape, "level_set", device, True, keep)
+        fn = self.ctx.lib.sf_reinitialize_dev if device else self.ctx.lib.sf_reinitialize
+        s = fn(self.ctx.handle, C.byref(g.c_grid()), C.c_void_p(phi), int(max_steps))
+        _check(self.ctx, s, None, "reinitialization", True)

@@ -35,7 +35,8 @@ EXPORTED = [
     "sf_system_features_dev", "sf_unet_set_mode", "sf_unet_tc_launches", "sf_magnetic_residual_noalloc",
     "sf_extrapolate_velocity", "sf_extrapolate_velocity_dev", "sf_collider_enforce", "sf_collider_enforce_dev",
     "sf_collider_face_normals", "sf_magnetic_vertex_pressures", "sf_magnetic_vertex_pressures_dev",
-    "sf_pressure_jump", "sf_pressure_jump_dev",
+    "sf_pressure_jump", "sf_pressure_jump_dev", "sf_advect_levelset", "sf_advect_levelset_dev",
+    "sf_advect_velocity", "sf_advect_velocity_dev", "sf_reinitialize", "sf_reinitialize_dev",
 ]
 
 
@@ -120,6 +121,18 @@ def load(path: str | None = None):
     for name in ("sf_pressure_jump", "sf_pressure_jump_dev"):
         f = getattr(L, name)
         f.argtypes = [V, G, _P3, V, V, C.c_longlong, C.c_double, C.c_double, C.c_double, _P3]
+        f.restype = C.c_int
+    for name in ("sf_advect_levelset", "sf_advect_levelset_dev"):
+        f = getattr(L, name)
+        f.argtypes = [V, G, V, _P3, C.c_double]
+        f.restype = C.c_int
+    for name in ("sf_advect_velocity", "sf_advect_velocity_dev"):
+        f = getattr(L, name)
+        f.argtypes = [V, G, _P3, C.c_double]
+        f.restype = C.c_int
+    for name in ("sf_reinitialize", "sf_reinitialize_dev"):
+        f = getattr(L, name)
+        f.argtypes = [V, G, V, C.c_int]
         f.restype = C.c_int
     L.sf_collider_face_normals.argtypes = [G, V, _P3]
     L.sf_collider_face_normals.restype = C.c_int

@@ -34,6 +34,8 @@ struct Ctx {
     DevBuf mask[6], old[3], normal[3];
     // interface coupling: mesh vertices, vertex values and edge marks
     DevBuf vpos, vnrm, vval, kappa, edge[3];
+    // level-set operations: two scratch cell fields
+    DevBuf ls1, ls2;
     // learned form: attached network (not owned) and its buffers; every network created on this context is
     // registered so that destroying the context first leaves the network handles safe to destroy later
     UNet *net = nullptr;
@@ -490,6 +492,77 @@ sf_status pressure_jump_impl(Ctx *c, const sf_grid *g, const int32_t *const edge
     return SF_OK;
 }
 
+sf_status stage_cells_inout(Ctx *c, const sf_grid *g, double *phi, bool dev, double **dphi, long long &h2d) {
+    const double *p;
+    sf_status s = stage_in(c, c->phi, phi, (long long)g->nx * g->ny * g->nz, dev, &p, h2d);
+    *dphi = const_cast<double *>(p);
+    return s;
+}
+
+sf_status advect_levelset_impl(Ctx *c, const sf_grid *g, double *phi, const double *const vel[3], double dt,
+                               bool dev) {
+    if (!c) return SF_BAD_ARG;
+    if (!grid_ok(g) || !phi || !vel || !vel[0] || !vel[1] || !vel[2] || !std::isfinite(dt))
+        return fail(c, SF_BAD_ARG, "bad grid, level set, velocity or time step");
+    CK(cudaSetDevice(c->device));
+    const Dims d = make_dims(g->nx, g->ny, g->nz);
+    long long h2d = 0;
+    sf_status s;
+    double *dphi;
+    if ((s = stage_cells_inout(c, g, phi, dev, &dphi, h2d)) != SF_OK) return s;
+    Faces fu{};
+    for (int a = 0; a < 3; a++)
+        if ((s = stage_in(c, c->vel[a], vel[a], face_count(g, a), dev, &fu.p[a], h2d)) != SF_OK) return s;
+    CK(c->ls1.ensure(8 * (size_t)d.n));
+    double *out = (double *)c->ls1.get();
+    launch_advect_levelset(c->st, d, g->origin, g->h, fu, dt, dphi, out);
+    launch_copy(c->st, d.n, out, dphi);  // Advection::Solve replaces the field with the advected one
+    CK(cudaGetLastError());
+    if (!dev) CK(cudaMemcpyAsync(phi, dphi, 8 * (size_t)d.n, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return SF_OK;
+}
+
+sf_status advect_velocity_impl(Ctx *c, const sf_grid *g, double *const vel[3], double dt, bool dev) {
+    sf_status s = post_common(c, g, vel);
+    if (s != SF_OK) return s;
+    if (!std::isfinite(dt)) return fail(c, SF_BAD_ARG, "bad time step");
+    CK(cudaSetDevice(c->device));
+    const Dims d = make_dims(g->nx, g->ny, g->nz);
+    long long h2d = 0;
+    double *dvel[3];
+    if ((s = stage_vel(c, g, vel, dev, dvel, h2d)) != SF_OK) return s;
+    // the flow is the old velocity: trace and interpolate from copies, write the new values in place
+    Faces fold{};
+    for (int a = 0; a < 3; a++) {
+        const long long nf = face_count(g, a);
+        CK(c->old[a].ensure(8 * (size_t)nf));
+        launch_copy(c->st, nf, dvel[a], (double *)c->old[a].get());
+        fold.p[a] = (const double *)c->old[a].get();
+    }
+    launch_advect_velocity(c->st, d, g->origin, g->h, fold, dt, dvel);
+    CK(cudaGetLastError());
+    return unstage_vel(c, g, vel, dev, dvel);
+}
+
+sf_status reinitialize_impl(Ctx *c, const sf_grid *g, double *phi, int max_steps, bool dev) {
+    if (!c) return SF_BAD_ARG;
+    if (!grid_ok(g) || !phi || max_steps < 0) return fail(c, SF_BAD_ARG, "bad grid, level set or step count");
+    CK(cudaSetDevice(c->device));
+    const Dims d = make_dims(g->nx, g->ny, g->nz);
+    long long h2d = 0;
+    sf_status s;
+    double *dphi;
+    if ((s = stage_cells_inout(c, g, phi, dev, &dphi, h2d)) != SF_OK) return s;
+    CK(c->ls1.ensure(8 * (size_t)d.n));
+    CK(c->ls2.ensure(8 * (size_t)d.n));
+    launch_reinitialize(c->st, d, g->h, dphi, (double *)c->ls1.get(), (double *)c->ls2.get(), max_steps);
+    CK(cudaGetLastError());
+    if (!dev) CK(cudaMemcpyAsync(phi, dphi, 8 * (size_t)d.n, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return SF_OK;
+}
+
 sf_status enforce_impl(Ctx *c, const sf_grid *g, double *const vel[3], const double *const frac[3],
                        const double *const normal[3], const double *const us[3], bool dev) {
     sf_status s = post_common(c, g, vel);
@@ -701,6 +774,25 @@ sf_status sf_pressure_jump_dev(void *ctx, const sf_grid *g, const int32_t *const
                                double st_coeff, double density, double dt, double *const jump[3]) {
     return pressure_jump_impl(C(ctx), g, edge_mark, curvature, mag_pressure, nverts, st_coeff, density, dt, jump,
                               true);
+}
+
+sf_status sf_advect_levelset(void *ctx, const sf_grid *g, double *phi, const double *const vel[3], double dt) {
+    return advect_levelset_impl(C(ctx), g, phi, vel, dt, false);
+}
+sf_status sf_advect_levelset_dev(void *ctx, const sf_grid *g, double *phi, const double *const vel[3], double dt) {
+    return advect_levelset_impl(C(ctx), g, phi, vel, dt, true);
+}
+sf_status sf_advect_velocity(void *ctx, const sf_grid *g, double *const vel[3], double dt) {
+    return advect_velocity_impl(C(ctx), g, vel, dt, false);
+}
+sf_status sf_advect_velocity_dev(void *ctx, const sf_grid *g, double *const vel[3], double dt) {
+    return advect_velocity_impl(C(ctx), g, vel, dt, true);
+}
+sf_status sf_reinitialize(void *ctx, const sf_grid *g, double *phi, int max_steps) {
+    return reinitialize_impl(C(ctx), g, phi, max_steps, false);
+}
+sf_status sf_reinitialize_dev(void *ctx, const sf_grid *g, double *phi, int max_steps) {
+    return reinitialize_impl(C(ctx), g, phi, max_steps, true);
 }
 
 sf_status sf_magnetic_residual_noalloc(void *stream, const sf_grid *g, const double *phi, double chi,

@@ -52,6 +52,16 @@ void DevBuf::release() {
 // Grid of the stencil reductions: work items of one 32 (z) x 8 (y) tile and `xpb` consecutive x planes, at most
 // max_blocks blocks looping over the items.  Memory-bound kernels take one item per block (kApplyBlocks); the
 // FP64-bound residual takes a persistent grid of 8 blocks per SM (kStencilBlocks), which shortens its tail.
+// 3-D grid of one block per work item (z-tile, y-tile, x-chunk), for kernels using TILE_BLOCK: at most
+// kApplyBlocks blocks (the reduction partials), with x-chunks lengthened when the grid would exceed it.
+dim3 tile_grid3(const Dims &d, int &xpb) {
+    const long long tiles = (long long)((d.nz + 31) / 32) * ((d.ny + 7) / 8);
+    const long long zmax = tiles < kApplyBlocks ? kApplyBlocks / tiles : 1;
+    xpb = (int)((d.nx + zmax - 1) / zmax);
+    if (xpb < kStencilPlanes) xpb = kStencilPlanes;
+    return dim3((d.nz + 31) / 32, (d.ny + 7) / 8, (d.nx + xpb - 1) / xpb);
+}
+
 dim3 tile_grid(const Dims &d, int &xpb, int max_blocks) {
     xpb = kStencilPlanes;
     const long long items =
@@ -169,6 +179,116 @@ __global__ void __launch_bounds__(256) k_rbgs(Dims d, Coef<C> cf, T *__restrict_
         }
         if (act[r]) x[cc[r]] = res[r];
     }
+}
+
+// z-vectorised half sweep (FP32 vectors, FP32 or FP16 operator; nz a multiple of 4): thread (q, j, i) owns
+// cells k0 = 4q .. 4q+3 of row (i, j) and updates the two of them whose colour equals `color`.  x rows are read
+// as float4 (the z-neighbours inside the group come from the same vector), FP32 arrays as float4 and FP16 arrays
+// as 4 halves in 8 bytes; the group is written back whole, the two other cells with the values just read (no
+// other thread writes them during this half sweep).  Same arithmetic, in the same order, as k_rbgs.
+__device__ __forceinline__ void ld4(const float *p, float (&v)[4]) {
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = t.x;
+    v[1] = t.y;
+    v[2] = t.z;
+    v[3] = t.w;
+}
+__device__ __forceinline__ void ld4(const __half *p, float (&v)[4]) {
+    const uint2 t = *reinterpret_cast<const uint2 *>(p);
+    const __half2 lo = *reinterpret_cast<const __half2 *>(&t.x), hi = *reinterpret_cast<const __half2 *>(&t.y);
+    v[0] = __low2float(lo);
+    v[1] = __high2float(lo);
+    v[2] = __low2float(hi);
+    v[3] = __high2float(hi);
+}
+
+template <class C, bool ZERO>
+__global__ void __launch_bounds__(256) k_rbgs4(Dims d, Coef<C> cf, float *__restrict__ x, const float *__restrict__ b,
+                                               int color) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    const int k0 = 4 * q;
+    if (j >= d.ny || k0 >= d.nz) return;
+    const long long c0 = cid(d, i, j, k0);
+    const long long sx = (long long)d.ny * d.nz, sy = d.nz;
+    const bool xl = i > 0, xu = i < d.nx - 1, yl = j > 0, yu = j < d.ny - 1, zr_in = k0 + 4 < d.nz;
+    float xc[4] = {0, 0, 0, 0}, xm[4] = {0, 0, 0, 0}, xp[4] = {0, 0, 0, 0}, ym[4] = {0, 0, 0, 0},
+          yp[4] = {0, 0, 0, 0};
+    float zl = 0.f, zr = 0.f;
+    if (!ZERO) {
+        ld4(x + c0, xc);
+        if (xl) ld4(x + c0 - sx, xm);
+        if (xu) ld4(x + c0 + sx, xp);
+        if (yl) ld4(x + c0 - sy, ym);
+        if (yu) ld4(x + c0 + sy, yp);
+        if (k0 > 0) zl = x[c0 - 1];
+        if (zr_in) zr = x[c0 + 4];
+    }
+    float axl[4], axu[4] = {0, 0, 0, 0}, ayl[4], ayu[4] = {0, 0, 0, 0}, azl[4], dx[4], bv[4];
+    ld4(cf.ax + c0, axl);
+    if (xu) ld4(cf.ax + c0 + sx, axu);
+    ld4(cf.ay + c0, ayl);
+    if (yu) ld4(cf.ay + c0 + sy, ayu);
+    ld4(cf.az + c0, azl);
+    const float azr = zr_in ? ldv(cf.az, c0 + 4) : 0.f;
+    ld4(cf.dex + c0, dx);
+    ld4(b + c0, bv);
+    float out[4] = {xc[0], xc[1], xc[2], xc[3]};  // ZERO: the other colour is cleared
+    // cell t of the group (compile-time index: the four values stay in registers)
+    auto upd = [&](auto tc) {
+        constexpr int t = decltype(tc)::value;
+        const int k = k0 + t;
+        float s = 0.f, sa = 0.f;
+        if (xl) {
+            const float a = axl[t];
+            if (!ZERO) s += a * xm[t];
+            sa += a;
+        }
+        if (xu) {
+            const float a = axu[t];
+            if (!ZERO) s += a * xp[t];
+            sa += a;
+        }
+        if (yl) {
+            const float a = ayl[t];
+            if (!ZERO) s += a * ym[t];
+            sa += a;
+        }
+        if (yu) {
+            const float a = ayu[t];
+            if (!ZERO) s += a * yp[t];
+            sa += a;
+        }
+        if (k > 0) {
+            const float a = azl[t];
+            if (!ZERO) s += a * (t == 0 ? zl : xc[t == 0 ? 0 : t - 1]);
+            sa += a;
+        }
+        if (k < d.nz - 1) {
+            const float a = t == 3 ? azr : azl[t == 3 ? 3 : t + 1];
+            if (!ZERO) s += a * (t == 3 ? zr : xc[t == 3 ? 3 : t + 1]);
+            sa += a;
+        }
+        if (sizeof(C) == 2) {
+            if (!ZERO) s *= cf.unscale;
+            sa *= cf.unscale;
+        }
+        float e = dx[t];
+        if (sizeof(C) == 2) e *= cf.unscale;
+        const float D = sa + e;
+        const float inv = D > 0.f ? 1.f / D : 0.f;
+        out[t] = (bv[t] + s) * inv;
+    };
+    // the colour's cells are t = 0, 2 or t = 1, 3; k0 is even, so the choice is uniform across a warp (one j)
+    if (((color - i - j) & 1) == 0) {
+        upd(std::integral_constant<int, 0>{});
+        upd(std::integral_constant<int, 2>{});
+    } else {
+        upd(std::integral_constant<int, 1>{});
+        upd(std::integral_constant<int, 3>{});
+    }
+    *reinterpret_cast<float4 *>(x + c0) = make_float4(out[0], out[1], out[2], out[3]);
 }
 
 // ------------------------------------------------------------------------------------------------ fused sweep
@@ -748,6 +868,16 @@ __global__ void k_to16(long long n, Coef<double> f, Coef<__half> o) {
         for (int i = (int)chunk * (xpb); i < i_end; i++) {                                         \
             const long long c = cid((d), i, j, k);
 
+// One work item per block of a 3-D grid (tile_grid3): block (z-tile, y-tile), `xpb` planes from blockIdx.z.
+#define TILE_BLOCK(d, xpb)                                                                    \
+    {                                                                                         \
+        const int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;       \
+        const bool inb = k < (d).nz && j < (d).ny;                                            \
+        const int i_end = min((d).nx, (int)(blockIdx.z + 1) * (xpb));                         \
+        for (int i = blockIdx.z * (xpb); i < i_end; i++) {                                    \
+            if (!inb) continue;                                                               \
+            const long long c = cid((d), i, j, k);
+
 #define TILE_LOOP_END \
     }                 \
     }
@@ -759,7 +889,7 @@ template <class T, class C>
 __global__ void __launch_bounds__(256) k_apply_dot(Dims d, int xpb, Coef<C> cf, const T *__restrict__ p,
                                                    T *__restrict__ q, double *sc, double *part, unsigned *ticket) {
     T acc = 0;
-    TILE_LOOP(d, xpb)
+    TILE_BLOCK(d, xpb)
     T sa;
     T s = nbsum<T, C, sizeof(C) != 8>(d, cf, p, i, j, k, c, sa);
     T D = (T)diag_of<C>(cf, c, (typename Acc<C>::T)sa);
@@ -779,6 +909,104 @@ __global__ void __launch_bounds__(256) k_apply_dot(Dims d, int xpb, Coef<C> cf, 
             sc[S_AUX0] = 1;  // breakdown
         }
     }
+}
+
+// FP32 q = A p with (p, q), z-vectorised (nz a multiple of 4): thread (q4, j) of a 3-D grid block owns cells
+// k0 = 4 q4 .. 4 q4 + 3 of row j over `xpb` x planes; float4 loads of p and of the operator arrays, the z-neighbours
+// inside the group from the same vector.  Each cell's q is computed as in k_apply_dot.
+__global__ void __launch_bounds__(256) k_apply_dot4(Dims d, int xpb, Coef<float> cf, const float *__restrict__ p,
+                                                    float *__restrict__ q, double *sc, double *part,
+                                                    unsigned *ticket) {
+    float acc = 0.f;
+    const int k0 = 4 * (blockIdx.x * 32 + threadIdx.x), j = blockIdx.y * 8 + threadIdx.y;
+    if (k0 < d.nz && j < d.ny) {
+        const long long sx = (long long)d.ny * d.nz, sy = d.nz;
+        const bool yl = j > 0, yu = j < d.ny - 1, zl = k0 > 0, zu = k0 + 4 < d.nz;
+        const int i_end = min(d.nx, (int)(blockIdx.z + 1) * xpb);
+        for (int i = blockIdx.z * xpb; i < i_end; i++) {
+            const long long c0 = cid(d, i, j, k0);
+            const bool xl = i > 0, xu = i < d.nx - 1;
+            float pc[4], pxm[4] = {0, 0, 0, 0}, pxp[4] = {0, 0, 0, 0}, pym[4] = {0, 0, 0, 0}, pyp[4] = {0, 0, 0, 0};
+            float axl[4], axu[4] = {0, 0, 0, 0}, ayl[4], ayu[4] = {0, 0, 0, 0}, azl[4], dx[4];
+            ld4(p + c0, pc);
+            if (xl) ld4(p + c0 - sx, pxm);
+            if (xu) ld4(p + c0 + sx, pxp);
+            if (yl) ld4(p + c0 - sy, pym);
+            if (yu) ld4(p + c0 + sy, pyp);
+            const float pzl = zl ? p[c0 - 1] : 0.f, pzr = zu ? p[c0 + 4] : 0.f;
+            ld4(cf.ax + c0, axl);
+            if (xu) ld4(cf.ax + c0 + sx, axu);
+            ld4(cf.ay + c0, ayl);
+            if (yu) ld4(cf.ay + c0 + sy, ayu);
+            ld4(cf.az + c0, azl);
+            const float azr = zu ? cf.az[c0 + 4] : 0.f;
+            ld4(cf.dex + c0, dx);
+            float out[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const int k = k0 + t;
+                float s = 0.f, sa = 0.f;
+                if (xl) {
+                    s += axl[t] * pxm[t];
+                    sa += axl[t];
+                }
+                if (xu) {
+                    s += axu[t] * pxp[t];
+                    sa += axu[t];
+                }
+                if (yl) {
+                    s += ayl[t] * pym[t];
+                    sa += ayl[t];
+                }
+                if (yu) {
+                    s += ayu[t] * pyp[t];
+                    sa += ayu[t];
+                }
+                if (k > 0) {
+                    const float a = azl[t];
+                    s += a * (t == 0 ? pzl : pc[t == 0 ? 0 : t - 1]);
+                    sa += a;
+                }
+                if (k < d.nz - 1) {
+                    const float a = t == 3 ? azr : azl[t == 3 ? 3 : t + 1];
+                    s += a * (t == 3 ? pzr : pc[t == 3 ? 3 : t + 1]);
+                    sa += a;
+                }
+                const float D = sa + dx[t];
+                out[t] = D * pc[t] - s;
+                acc += pc[t] * out[t];
+            }
+            *reinterpret_cast<float4 *>(q + c0) = make_float4(out[0], out[1], out[2], out[3]);
+        }
+    }
+    double v[1] = {(double)acc};
+    double tot[1];
+    if (grid_reduce<1>(v, part, ticket, tot)) {
+        sc[S_PQ] = tot[0];
+        if (tot[0] > 0 && isfinite(tot[0])) {
+            sc[S_ALPHA] = sc[S_RHO] / tot[0];
+        } else {
+            sc[S_ALPHA] = 0;
+            sc[S_AUX0] = 1;  // breakdown
+        }
+    }
+}
+
+// Launch q = A p, (p, q) on the FP32 level-0 operator: z-vectorised when rows are 16-byte aligned.
+static void apply_dot32(cudaStream_t st, const Dims &d, const Coef<float> &cf, const float *p, float *q, double *sc,
+                        double *part, unsigned *ticket) {
+    int xpb;
+    if (d.nz % 4 == 0) {
+        const long long tiles = (long long)((d.nz + 127) / 128) * ((d.ny + 7) / 8);
+        const long long zmax = tiles < kApplyBlocks ? kApplyBlocks / tiles : 1;
+        xpb = (int)((d.nx + zmax - 1) / zmax);
+        if (xpb < 2) xpb = 2;
+        const dim3 g((d.nz + 127) / 128, (d.ny + 7) / 8, (d.nx + xpb - 1) / xpb);
+        k_apply_dot4<<<g, dim3(32, 8), 0, st>>>(d, xpb, cf, p, q, sc, part, ticket);
+        return;
+    }
+    const dim3 tg = tile_grid3(d, xpb);
+    k_apply_dot<float, float><<<tg, dim3(32, 8), 0, st>>>(d, xpb, cf, p, q, sc, part, ticket);
 }
 
 // rho_new = (r, z), zq = (z, q); beta = flexible ? -alpha*zq/rho : rho_new/rho; rho = rho_new
@@ -938,6 +1166,17 @@ static void rb(cudaStream_t st, Tracker &tk, bool fine, bool zero, const Dims &d
     // algorithmic bytes of one colour: half of (x r/w + b + 3 couplings + diagonal term)
     const double per = (3.0 * sizeof(T) + 4.0 * sizeof(C)) / 2.0;
     tk.before(st, fine);
+    if constexpr (std::is_same<T, float>::value && sizeof(C) <= 4) {
+        if (d.nz % 4 == 0) {  // rows start 16-byte aligned: z-vectorised kernel
+            const dim3 g4((d.nz / 4 + 31) / 32, (d.ny + 7) / 8, d.nx);
+            if (zero)
+                k_rbgs4<C, true><<<g4, bk, 0, st>>>(d, cf, x, b, color);
+            else
+                k_rbgs4<C, false><<<g4, bk, 0, st>>>(d, cf, x, b, color);
+            tk.after(st, fine, per * d.n);
+            return;
+        }
+    }
     if (zero)
         k_rbgs<T, C, true><<<g, bk, 0, st>>>(d, cf, x, b, color);
     else
@@ -1171,6 +1410,10 @@ void *MGSolver::alloc(size_t bytes) {
 size_t MGSolver::device_bytes() const { return bytes_; }
 
 cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
+    if ((long long)((d.nz + 31) / 32) * ((d.ny + 7) / 8) > kApplyBlocks) {  // tile_grid3's one block per tile
+        last_error = "grid cross-section above 16384 tiles of 32 (z) x 8 (y) cells";
+        return cudaErrorInvalidValue;
+    }
     // level dims
     std::vector<Dims> dims{d};
     const int cdim = p.coarse_dim > 0 ? p.coarse_dim : 8;
@@ -1314,7 +1557,7 @@ void MGSolver::enqueue_iter64() {
     const Dims &d = lev_dims_[0];
     const long long n = d.n;
     int xpb;
-    const dim3 tg = tile_grid(d, xpb, kApplyBlocks);
+    const dim3 tg = tile_grid3(d, xpb);
     const long long l0 = tk_.launches;
     vcycle<double, double, double, double>(st_, tk_, lev_dims_, c64_[0], c64_[0], c64_, z_, r_, x64_, b64_,
                                            prm_.smoother == 1 ? t64_ : std::vector<double *>(t64_.size(), nullptr),
@@ -1332,8 +1575,6 @@ void MGSolver::enqueue_iter64() {
 void MGSolver::enqueue_iter32() {
     const Dims &d = lev_dims_[0];
     const long long n = d.n;
-    int xpb;
-    const dim3 tg = tile_grid(d, xpb, kApplyBlocks);
     const long long l0 = tk_.launches;
     const std::vector<float *> ts = prm_.smoother == 1 ? t32_ : std::vector<float *>(t32_.size(), nullptr);
     if (prm_.smoother == 2)
@@ -1344,7 +1585,7 @@ void MGSolver::enqueue_iter32() {
                                             prm_);
     k_dot_rz<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, ri32_, z32_, q32_, 1, sc_, part_, ticket_);
     k_xpby<float><<<flat_grid(n), 256, 0, st_>>>(n, z32_, p32_, sc_);
-    k_apply_dot<float, float><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c32_, p32_, q32_, sc_, part_, ticket_);
+    apply_dot32(st_, d, c32_, p32_, q32_, sc_, part_, ticket_);
     k_update<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, d32_, ri32_, p32_, q32_, sc_, part_, ticket_);
     tk_.launches += 4;
     iter_launches32_ = tk_.launches - l0;
@@ -1580,10 +1821,8 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
 cudaError_t MGSolver::set_guess_scaled(const float *y, double &gamma) {
     if (prm_.precision != 1) return cudaErrorInvalidValue;
     const Dims &d = lev_dims_[0];
-    int xpb;
-    const dim3 tg = tile_grid(d, xpb, kApplyBlocks);
     // (y, A y) on the FP32 level-0 operator and (y, b); gamma minimises the A-norm error along y
-    k_apply_dot<float, float><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c32_, y, q32_, sc_, part_, ticket_);
+    apply_dot32(st_, d, c32_, y, q32_, sc_, part_, ticket_);
     k_dot_fd<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(d.n, y, b_, S_AUX2, sc_, part_, ticket_);
     tk_.launches += 2;
     cudaError_t e = read_slots();

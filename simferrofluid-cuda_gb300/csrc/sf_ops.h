@@ -35,6 +35,12 @@ void launch_vertex_pressures(cudaStream_t st, const Dims &d, const double origin
                              double chi, const double *pos, const double *nrm, long long nv, double *out);
 void launch_pressure_jump(cudaStream_t st, const Dims &d, const int32_t *const edge_mark[3], const double *kappa,
                           const double *pm, double sigma, double rho, double h, double dt, double *const jump[3]);
+void launch_advect_levelset(cudaStream_t st, const Dims &d, const double origin[3], double h, const Faces &u,
+                            double dt, const double *phi, double *out);
+void launch_advect_velocity(cudaStream_t st, const Dims &d, const double origin[3], double h, const Faces &u,
+                            double dt, double *const out[3]);
+void launch_reinitialize(cudaStream_t st, const Dims &d, double h, double *phi, double *p1, double *p2,
+                         int max_steps);
 void launch_copy(cudaStream_t st, long long n, const double *a, double *o);
 void launch_to_f32(cudaStream_t st, long long n, const double *a, float *o);
 

@@ -6,6 +6,7 @@
 // to the CPU restatement on the same inputs.
 #include <cmath>
 
+#include "sf_interp.cuh"
 #include "sf_ops.h"
 
 namespace sf {
@@ -84,38 +85,6 @@ __global__ void __launch_bounds__(256) k_extrap_step(Dims d, int a, double *__re
     }
 }
 
-// TriLerp::Interpolate (core/TriLerp.h:28-36, 54-58) of face grid b at p: Grid::CalcLower<1> / CalcLowerFrac
-// (core/Grid.h:33-35) and clamped At() (core/GridData.h:31).
-__device__ double trilerp_face(const Dims &d, const double *__restrict__ v, int b, const double o[3], double h,
-                               double invh, const double p[3]) {
-    const int s[3] = {d.nx + (b == 0), d.ny + (b == 1), d.nz + (b == 2)};
-    int lo[3];
-    double w[2][3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const double co = a == b ? o[a] : o[a] + h / 2;  // face grid origin (core/StaggeredGrid.h:16-20)
-        lo[a] = (int)floor((p[a] - co) * invh - 0.0);
-        const double fr = (p[a] - co - (double)lo[a] * h) * invh;
-        w[0][a] = 1. - fr;
-        w[1][a] = fr;
-    }
-    double val = 0;
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-        const int dx = q & 1, dy = (q >> 1) & 1, dz = (q >> 2) & 1;
-        int ci[3] = {lo[0] + dx, lo[1] + dy, lo[2] + dz};
-#pragma unroll
-        for (int a = 0; a < 3; a++) ci[a] = ci[a] < 0 ? 0 : (ci[a] > s[a] - 1 ? s[a] - 1 : ci[a]);
-        const double wt = w[dx][0] * w[dy][1] * w[dz][2];
-        val += v[(long long)ci[2] + (long long)s[2] * ((long long)ci[1] + (long long)s[1] * ci[0])] * wt;
-    }
-    return val;
-}
-
-struct Origin {
-    double o[3];
-};
-
 // Collider::Enforce (core/Collider.cpp:75-86) on the faces of axis a with fraction == 1: the interpolated old
 // velocity minus its normal component relative to the solid velocity (us.p[0] == nullptr: zero).
 __global__ void __launch_bounds__(256) k_enforce(Dims d, int a, Origin og, double h, double invh, Faces old,
@@ -191,7 +160,181 @@ __global__ void __launch_bounds__(256) k_pressure_jump(Dims d, int a, EdgeMarks 
     jump[fidx(f, i, j, k)] = pressure;
 }
 
+// ------------------------------------------------------------------------------------------------ level set
+// Advection::Trace<2> (core/Advection.h:15-18): TVD Runge-Kutta trace of second order from p over dt.
+__device__ __forceinline__ void trace_rk2(const Dims &d, const Faces &u, const double o[3], double h, double invh,
+                                          const double p[3], double dt, double out[3]) {
+    double v0[3], v1[3], q[3];
+#pragma unroll
+    for (int b = 0; b < 3; b++) v0[b] = trilerp_face(d, u.p[b], b, o, h, invh, p);
+#pragma unroll
+    for (int b = 0; b < 3; b++) q[b] = p[b] + v0[b] * dt;
+#pragma unroll
+    for (int b = 0; b < 3; b++) v1[b] = trilerp_face(d, u.p[b], b, o, h, invh, q);
+#pragma unroll
+    for (int b = 0; b < 3; b++) out[b] = p[b] + (v0[b] + v1[b]) * dt / 2;
+}
+
+// Advection::Solve<2>(levelSet, velocity, dt) (core/Advection.h:40-49): phi at each cell centre's RK2 departure
+// point (trace over -dt), by tricubic interpolation of the old phi.
+__global__ void __launch_bounds__(256) k_advect_levelset(Dims d, Origin og, double h, double invh, Faces u,
+                                                         double dt, const double *__restrict__ phi,
+                                                         double *__restrict__ out) {
+    const int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y, i = blockIdx.z;
+    if (k >= d.nz || j >= d.ny) return;
+    const double p[3] = {og.o[0] + h / 2 + (double)i * h, og.o[1] + h / 2 + (double)j * h,
+                         og.o[2] + h / 2 + (double)k * h};
+    double q[3];
+    trace_rk2(d, u, og.o, h, invh, p, -dt, q);
+    out[cid(d, i, j, k)] = tricubic_cell(d, phi, og.o, h, invh, q);
+}
+
+// Advection::Solve<2>(velocity, velocity, dt) (core/Advection.h:51-59) for the faces of axis a: trilinear
+// interpolation of the old face grid a at each face's RK2 departure point.
+__global__ void __launch_bounds__(256) k_advect_velocity(Dims d, int a, Origin og, double h, double invh, Faces u,
+                                                         const double *__restrict__ ua, double dt,
+                                                         double *__restrict__ out) {
+    const FDims f = fdims(d, a);
+    const int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y, i = blockIdx.z;
+    if (k >= f.fz || j >= f.fy) return;
+    const int c3[3] = {i, j, k};
+    double p[3], q[3];
+#pragma unroll
+    for (int b = 0; b < 3; b++) p[b] = (b == a ? og.o[b] : og.o[b] + h / 2) + (double)c3[b] * h;
+    trace_rk2(d, u, og.o, h, invh, p, -dt, q);
+    out[fidx(f, i, j, k)] = trilerp_face(d, ua, a, og.o, h, invh, q);
+}
+
+__device__ __forceinline__ double dmax0(double a, double b) { return (a < b) ? b : a; }  // std::max(a, b)
+
+// GetDrv (core/Reinitialization.cpp:4-27): WENO5 one-sided derivatives from 7 values (s = 0 minus, 1 plus).
+__device__ __forceinline__ double weno_side(const double v[7], int s, double invdx) {
+    double dev[5];
+    if (s) {
+        dev[0] = v[6] - v[5];
+        dev[1] = v[5] - v[4];
+        dev[2] = v[4] - v[3];
+        dev[3] = v[3] - v[2];
+        dev[4] = v[2] - v[1];
+    } else {
+        dev[0] = v[1] - v[0];
+        dev[1] = v[2] - v[1];
+        dev[2] = v[3] - v[2];
+        dev[3] = v[4] - v[3];
+        dev[4] = v[5] - v[4];
+    }
+    double eps = 0;
+#pragma unroll
+    for (int j = 0; j < 5; j++) eps = dmax0(eps, dev[j] * dev[j]);
+    eps = eps * 1e-6 + 1e-99;
+    const double phix1 = dev[0] / 3 - dev[1] * 7 / 6 + dev[2] * 11 / 6;
+    const double phix2 = -dev[1] / 6 + dev[2] * 5 / 6 + dev[3] / 3;
+    const double phix3 = dev[2] / 3 + dev[3] * 5 / 6 - dev[4] / 6;
+    double t = dev[0] - 2 * dev[1] + dev[2];
+    double s1 = t * t * 13 / 12;
+    t = dev[0] - 4 * dev[1] + 3 * dev[2];
+    s1 = s1 + t * t / 4;
+    t = dev[1] - 2 * dev[2] + dev[3];
+    double s2 = t * t * 13 / 12;
+    t = dev[1] - dev[3];
+    s2 = s2 + t * t / 4;
+    t = dev[2] - 2 * dev[3] + dev[4];
+    double s3 = t * t * 13 / 12;
+    t = 3 * dev[2] - 4 * dev[3] + dev[4];
+    s3 = s3 + t * t / 4;
+    t = s1 + eps;
+    const double alpha1 = .1 / (t * t);
+    t = s2 + eps;
+    const double alpha2 = .6 / (t * t);
+    t = s3 + eps;
+    const double alpha3 = .3 / (t * t);
+    const double sum = alpha1 + alpha2 + alpha3;
+    return (alpha1 * phix1 + alpha2 * phix2 + alpha3 * phix3) / sum * invdx;
+}
+
+// Reinitialization::Advance (core/Reinitialization.cpp:48-74): one explicit step of the reinitialisation
+// equation with Godunov upwinding of the WENO5 derivatives (clamped stencils at the grid ends).
+__global__ void __launch_bounds__(256) k_reinit_advance(Dims d, double h, double invdx, double dt,
+                                                        const double *__restrict__ f, double *__restrict__ out) {
+    const int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y, i = blockIdx.z;
+    if (k >= d.nz || j >= d.ny) return;
+    const int c3[3] = {i, j, k};
+    const int sz[3] = {d.nx, d.ny, d.nz};
+    const double fc = f[cid(d, i, j, k)];
+    double sum = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        double v[7];
+#pragma unroll
+        for (int q = 0; q < 7; q++) {
+            int c[3] = {c3[0], c3[1], c3[2]};
+            c[a] += q - 3;
+            c[a] = c[a] < 0 ? 0 : (c[a] > sz[a] - 1 ? sz[a] - 1 : c[a]);
+            v[q] = f[cid(d, c[0], c[1], c[2])];
+        }
+        const double dm = weno_side(v, 0, invdx), dp = weno_side(v, 1, invdx);
+        double t;
+        if (fc < 0) {
+            t = dm < 0. ? dm : 0.;
+            sum += t * t;
+            t = dmax0(dp, 0.);
+            sum += t * t;
+        } else {
+            t = dmax0(dm, 0.);
+            sum += t * t;
+            t = dp < 0. ? dp : 0.;
+            sum += t * t;
+        }
+    }
+    sum = sqrt(sum);
+    const double sp = h * sum;
+    const double sgn = fc / sqrt(fc * fc + sp * sp);
+    out[cid(d, i, j, k)] = fc + dt * sgn * (1. - sum);
+}
+
+// TVD-RK3 combinations of Reinitialization::Solve (core/Reinitialization.cpp:41-44).
+__global__ void k_rk3_stage(long long n, const double *__restrict__ phi, const double *__restrict__ p2,
+                            double *__restrict__ p1) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        p1[c] = (phi[c] * 3 + p2[c]) / 4;
+}
+__global__ void k_rk3_final(long long n, double *__restrict__ phi, const double *__restrict__ p2) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        phi[c] = (phi[c] + p2[c] * 2) / 3;
+}
+
+inline dim3 cell_grid(const Dims &d) { return dim3((d.nz + 31) / 32, (d.ny + 7) / 8, d.nx); }
+inline unsigned flat_blocks(long long n) {
+    long long b = (n + 255) / 256;
+    return (unsigned)(b > 152 * 16 ? 152 * 16 : (b < 1 ? 1 : b));
+}
+
 }  // namespace
+
+void launch_advect_levelset(cudaStream_t st, const Dims &d, const double origin[3], double h, const Faces &u,
+                            double dt, const double *phi, double *out) {
+    Origin og{{origin[0], origin[1], origin[2]}};
+    k_advect_levelset<<<cell_grid(d), blk2(), 0, st>>>(d, og, h, 1 / h, u, dt, phi, out);
+}
+
+void launch_advect_velocity(cudaStream_t st, const Dims &d, const double origin[3], double h, const Faces &u,
+                            double dt, double *const out[3]) {
+    Origin og{{origin[0], origin[1], origin[2]}};
+    for (int a = 0; a < 3; a++)
+        k_advect_velocity<<<face_grid(d, a), blk2(), 0, st>>>(d, a, og, h, 1 / h, u, u.p[a], dt, out[a]);
+}
+
+void launch_reinitialize(cudaStream_t st, const Dims &d, double h, double *phi, double *p1, double *p2,
+                         int max_steps) {
+    const double dt = h * .5, invdx = 1 / h;
+    for (int it = 0; it < max_steps; it++) {
+        k_reinit_advance<<<cell_grid(d), blk2(), 0, st>>>(d, h, invdx, dt, phi, p1);
+        k_reinit_advance<<<cell_grid(d), blk2(), 0, st>>>(d, h, invdx, dt, p1, p2);
+        k_rk3_stage<<<flat_blocks(d.n), 256, 0, st>>>(d.n, phi, p2, p1);
+        k_reinit_advance<<<cell_grid(d), blk2(), 0, st>>>(d, h, invdx, dt, p1, p2);
+        k_rk3_final<<<flat_blocks(d.n), 256, 0, st>>>(d.n, phi, p2);
+    }
+}
 
 void launch_vertex_pressures(cudaStream_t st, const Dims &d, const double origin[3], double h, const Faces &H,
                              double chi, const double *pos, const double *nrm, long long nv, double *out) {

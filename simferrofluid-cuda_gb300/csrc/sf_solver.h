@@ -171,5 +171,6 @@ constexpr int kApplyBlocks = 16384;      // one work item per block for the memo
 constexpr int kStencilPlanes = 4;        // x planes per work item
 constexpr int kMaxRedGrid = kApplyBlocks;
 dim3 tile_grid(const Dims &d, int &xpb, int max_blocks);
+dim3 tile_grid3(const Dims &d, int &xpb);
 
 }  // namespace sf
