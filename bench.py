@@ -272,8 +272,8 @@ def run_ours(args, ws, rank, local):
         kname = "k_rbgs_tma (one full red-black sweep per launch, TMA-staged)"
         prof = "k_rbgs_tma_pool_sphere_256.md"
     elif smoother == 2 and args.precision == "mixed":
-        kname = "k_rbgs<float, __half> (one colour of a red-black sweep per launch, FP16 operator copy)"
-        prof = "k_rbgs_f16_finest_pool_sphere_256.md"
+        kname = "k_rbgs4<__half> (one colour of a red-black sweep per launch, FP16 operator copy)"
+        prof = "k_rbgs4_f16_finest_pool_sphere_256.md"
     else:
         kname = "k_rbgs (one colour of a red-black sweep per launch)"
         prof = "k_rbgs_f32_finest_pool_sphere_256.md" if args.precision == "mixed" else None
