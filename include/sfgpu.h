@@ -203,6 +203,13 @@ SF_EXPORT long long sf_unet_tc_launches(void *net);
 SF_EXPORT sf_status sf_set_network(void *ctx, void *net);
 /* features of the last assembled pressure (which = 0) or potential (1) system and its solution (FP32) */
 SF_EXPORT sf_status sf_system_features_dev(void *ctx, int which, void *features_bf16, float *solution);
+/* Read back the finest-level operator and right-hand side of the last assembled pressure (which = 0) or
+ * potential (1) system on this context into host arrays of nx*ny*nz doubles (any pointer may be NULL): the
+ * diagonal, the couplings on each cell's lower x / y / z face (the off-diagonal entry is minus the coupling)
+ * and b.  Pressure rows of air cells are all zero; the potential keeps row 0 in its unpinned (Neumann) form.
+ * For checking the assembly against the reference's matrices (core/Pressure.cpp:38-78,
+ * core/MagneticField.cpp:62-118).  Synchronises the context's stream. */
+SF_EXPORT sf_status sf_system_operator(void *ctx, int which, double *diag, double *const lower[3], double *rhs);
 
 /* ----- velocity pipeline after the projection (core/Simulation.cpp:236-241) -------------------------------------
  * Extrapolation::Solve (core/Extrapolation.cpp:4-30) of the projected velocity over max_steps layers, with the

@@ -138,6 +138,18 @@ class Context:
             raise SolveError(s, self.last_error())
         self.network = net
 
+    def system_operator(self, which, shape):
+        """(diag, [lower_x, lower_y, lower_z], rhs) of the last assembled system (0 pressure, 1 potential), as
+        host arrays of the cell grid's shape (sf_system_operator)."""
+        diag, rhs = np.empty(shape), np.empty(shape)
+        lower = [np.empty(shape) for _ in range(3)]
+        lp = _abi.p3_ref([a.ctypes.data for a in lower])
+        s = self.lib.sf_system_operator(self.handle, int(which), C.c_void_p(diag.ctypes.data), lp[0],
+                                        C.c_void_p(rhs.ctypes.data))
+        if s != _abi.SF_OK:
+            raise SolveError(s, "sf_system_operator: " + self.last_error())
+        return diag, lower, rhs
+
     def system_features(self, which, features=None, solution=None):
         """Network features (BF16 [n][16], device) and FP32 solution of the last pressure (0) / potential (1)
         system assembled on this context; arguments are CUDA tensors or None."""

@@ -33,6 +33,7 @@ EXPORTED = [
     "sf_unet_create", "sf_unet_destroy", "sf_unet_num_params", "sf_unet_set_params", "sf_unet_get_params",
     "sf_unet_forward_dev", "sf_unet_backward_dev", "sf_unet_train_step_dev", "sf_set_network",
     "sf_system_features_dev", "sf_unet_set_mode", "sf_unet_tc_launches", "sf_magnetic_residual_noalloc",
+    "sf_system_operator",
     "sf_extrapolate_velocity", "sf_extrapolate_velocity_dev", "sf_collider_enforce", "sf_collider_enforce_dev",
     "sf_collider_face_normals", "sf_magnetic_vertex_pressures", "sf_magnetic_vertex_pressures_dev",
     "sf_pressure_jump", "sf_pressure_jump_dev", "sf_advect_levelset", "sf_advect_levelset_dev",
@@ -166,6 +167,8 @@ def load(path: str | None = None):
     L.sf_set_network.restype = C.c_int
     L.sf_system_features_dev.argtypes = [V, C.c_int, V, V]
     L.sf_system_features_dev.restype = C.c_int
+    L.sf_system_operator.argtypes = [V, C.c_int, V, V, V]
+    L.sf_system_operator.restype = C.c_int
     _lib = L
     return L
 

@@ -923,6 +923,27 @@ sf_status sf_set_network(void *ctx, void *net) {
     c->net = h ? h->net.get() : nullptr;
     return SF_OK;
 }
+sf_status sf_system_operator(void *ctx, int which, double *diag, double *const lower[3], double *rhs) {
+    Ctx *c = C(ctx);
+    if (!c || (which != 0 && which != 1)) return SF_BAD_ARG;
+    MGSolver *S = which == 0 ? c->pres.get() : c->mag.get();
+    if (!S || (which == 0 && !c->pres_ready) || (which == 1 && !c->mag_has_x))
+        return fail(c, SF_NOT_READY, "no assembled system of that kind on this context");
+    CK(cudaSetDevice(c->device));
+    const Dims d = S->dims();
+    const size_t bytes = 8 * (size_t)d.n;
+    Coef<double> &cf = S->fine();
+    if (diag) CK(cudaMemcpyAsync(diag, cf.D, bytes, cudaMemcpyDeviceToHost, c->st));
+    if (lower) {
+        double *src[3] = {cf.ax, cf.ay, cf.az};
+        for (int a = 0; a < 3; a++)
+            if (lower[a]) CK(cudaMemcpyAsync(lower[a], src[a], bytes, cudaMemcpyDeviceToHost, c->st));
+    }
+    if (rhs) CK(cudaMemcpyAsync(rhs, S->b(), bytes, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return SF_OK;
+}
+
 sf_status sf_system_features_dev(void *ctx, int which, void *features, float *solution) {
     Ctx *c = C(ctx);
     if (!c || (which != 0 && which != 1)) return SF_BAD_ARG;

@@ -19,10 +19,24 @@ __device__ __forceinline__ long long fid(const Dims &d, int a, int i, int j, int
     return (long long)k + (long long)fz * ((long long)j + (long long)fy * i);
 }
 
+// Comparisons as integer tests on the bits, so they do not occupy the FP64 pipe (the assembly kernels are
+// bound by it).  le0(v) == (v <= 0) for every double, NaN included; is_zero(v) == (v == 0).
+constexpr long long kOneBits = 0x3FF0000000000000LL;  // 1.0
+__device__ __forceinline__ bool le0(double v) {
+    const long long b = __double_as_longlong(v);
+    return b == 0 || (b < 0 && (b & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL);
+}
+__device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
+
 // ------------------------------------------------------------------------------------------------ pressure
 // Pressure::SetUnKnowns + BuildProjectionMatrix (core/Pressure.cpp:104-123, 38-78) for one cell.
 // Liquid cells are phi <= 0.  The face weight is w = 1 - fraction; faces on the outer grid boundary are
 // closed (w = 0).  D is the reference's diagonal bit for bit (same summation order, 1 for an isolated cell).
+//
+// Fast path with the same bits: an interior cell whose six fractions are zero (w = 1 exactly) and, when the
+// operator is built, whose six neighbours are liquid.  The general loop then sums six ones (D = 6), stores
+// unit couplings, adds no ghost or solid-velocity term, and each face's -side * w * u is exactly -side * u,
+// so the divergence is six additions / subtractions in the same order.
 __global__ void __launch_bounds__(256) k_build_pressure(Dims d, const double *__restrict__ phi, Faces frac,
                                                         Faces u, Faces us, Faces jump, double vol_error,
                                                         Coef<double> cf, double *__restrict__ b, int rhs_only,
@@ -40,7 +54,37 @@ __global__ void __launch_bounds__(256) k_build_pressure(Dims d, const double *__
         }
     }
     const double pc = phi[c];
-    const bool liquid = rhs_only ? true : (pc <= 0);
+    const bool liquid = rhs_only ? true : le0(pc);
+    if (liquid && i > 0 && i < d.nx - 1 && j > 0 && j < d.ny - 1 && k > 0 && k < d.nz - 1) {
+        const long long sx = (long long)d.ny * d.nz, sy = d.nz;
+        const long long fx0 = fid(d, 0, i, j, k), fx1 = fid(d, 0, i + 1, j, k);
+        const long long fy0 = fid(d, 1, i, j, k), fy1 = fid(d, 1, i, j + 1, k);
+        const long long fz0 = fid(d, 2, i, j, k), fz1 = fid(d, 2, i, j, k + 1);
+        bool open = is_zero(frac.p[0][fx0]) & is_zero(frac.p[0][fx1]) & is_zero(frac.p[1][fy0]) &
+                    is_zero(frac.p[1][fy1]) & is_zero(frac.p[2][fz0]) & is_zero(frac.p[2][fz1]);
+        if (open && !rhs_only)
+            open = le0(phi[c - sx]) & le0(phi[c + sx]) & le0(phi[c - sy]) & le0(phi[c + sy]) & le0(phi[c - 1]) &
+                   le0(phi[c + 1]);
+        if (open) {
+            double div = 0;
+            div += u.p[0][fx0];  // ord -x: div -= (-1 * 1) * u
+            div -= u.p[0][fx1];  // ord +x: div -= (+1 * 1) * u
+            div += u.p[1][fy0];
+            div -= u.p[1][fy1];
+            div += u.p[2][fz0];
+            div -= u.p[2][fz1];
+            div += vol_error;
+            b[c] = div;
+            if (rhs_only) return;
+            cf.ax[c] = 1.;
+            cf.ay[c] = 1.;
+            cf.az[c] = 1.;
+            cf.dex[c] = 0.;
+            cf.D[c] = 6.;
+            if (want_invd) cf.invd[c] = 1. / 6.;
+            return;
+        }
+    }
     double lower[3] = {0, 0, 0};
     double diag = 0, dexv = 0, div = 0;
     if (liquid) {
@@ -61,7 +105,7 @@ __global__ void __launch_bounds__(256) k_build_pressure(Dims d, const double *__
                 if (!rhs_only) {
                     const long long nb = cid(d, n3[0], n3[1], n3[2]);
                     const double pn = phi[nb];
-                    if (pn <= 0) {
+                    if (le0(pn)) {
                         diag += w;
                         if (!up) lower[a] = w;
                     } else {
@@ -90,12 +134,15 @@ __global__ void __launch_bounds__(256) k_build_pressure(Dims d, const double *__
     cf.az[c] = lower[2];
     cf.dex[c] = dexv;
     cf.D[c] = D;
-    if (want_invd) cf.invd[c] = D > 0 ? 1. / D : 0.0;
+    if (want_invd) cf.invd[c] = liquid ? (D > 0 ? 1. / D : 0.0) : 0.0;
 }
 
 // Pressure::ApplyProjection (core/Pressure.cpp:137-166) for the faces of axis a.  p is the solution on
-// cells; liquid = phi <= 0.
-__global__ void __launch_bounds__(256) k_apply_projection(Dims d, int a, const double *__restrict__ phi, Faces frac,
+// cells; liquid = phi <= 0.  w = 1 - fraction is 0 exactly when the fraction is 1, and 1 exactly when it is
+// zero, where (p1 - p0) * w is p1 - p0: both are tested on the bits, so air faces and open liquid faces take no
+// FP64 operation beyond the update itself.
+template <int a>
+__global__ void __launch_bounds__(256) k_apply_projection(Dims d, const double *__restrict__ phi, Faces frac,
                                                           Faces jump, const double *__restrict__ p,
                                                           double *__restrict__ u) {
     const int fx = d.nx + (a == 0), fy = d.ny + (a == 1), fz = d.nz + (a == 2);
@@ -109,17 +156,20 @@ __global__ void __launch_bounds__(256) k_apply_projection(Dims d, int a, const d
     const int fa = a == 0 ? i : (a == 1 ? j : k);
     if (fa <= 0 || fa >= dn[a]) return;  // closed boundary face
     const long long f = (long long)k + (long long)fz * ((long long)j + (long long)fy * i);
-    const double w = 1. - frac.p[a][f];
-    if (w == 0.) return;
+    const double fr = frac.p[a][f];
+    if (__double_as_longlong(fr) == kOneBits) return;  // w == 0
     const long long c1 = cid(d, i, j, k);
     const long long c0 = cid(d, c0i[0], c0i[1], c0i[2]);
     const double phi0 = phi[c0], phi1 = phi[c1];
-    const bool l0 = phi0 <= 0, l1 = phi1 <= 0;
+    const bool l0 = le0(phi0), l1 = le0(phi1);
     if (!l0 && !l1) return;
     double v = u[f];
-    if (l0 && l1) {
-        v -= (p[c1] - p[c0]) * w;
+    if (l0 && l1 && is_zero(fr)) {
+        v -= p[c1] - p[c0];  // w == 1
+    } else if (l0 && l1) {
+        v -= (p[c1] - p[c0]) * (1. - fr);
     } else {
+        const double w = 1. - fr;
         const double theta = phi0 / (phi0 - phi1);
         const double pin = l0 ? p[c0] : p[c1];
         const double pj = jump.p[0] ? jump.p[a][f] : 0.;
@@ -193,14 +243,52 @@ __global__ void __launch_bounds__(256) k_magnetic_mu(Dims d, const double *__res
 // in-grid faces in the reference's face order, rhs = sum (mu - 1) Hext (-side) h in the same order (faces with
 // mu == 1 add a signed zero, which leaves the sum unchanged, and are skipped).  Row 0 keeps its unpinned value:
 // the reference's pinned row 0 is recovered by the psi[0] = 0 gauge after the solve.
+//
+// Fast paths with the same bits, for interior cells whose six face values are one bit pattern: all 1 (air
+// away from the interface) gives D = 6 (six ones summed exactly) and rhs = 0; all 1 + chi (liquid away from
+// it) gives D = sv6, the six-term sum of 1 + chi formed on the host in the same order, and per face
+// (mu - 1) = m1, also formed on the host; the sign -side is an exact negation.  Bit patterns are compared as
+// integers, so air cells take no FP64 operation.
 __global__ void __launch_bounds__(256) k_magnetic_rows(Dims d, Faces hext, double h, Coef<double> cf,
-                                                       double *__restrict__ b, int want_invd) {
+                                                       double *__restrict__ b, int want_invd,
+                                                       long long liq_bits, double m1, double sv6,
+                                                       double inv_sv6) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
     if (k >= d.nz || j >= d.ny) return;
     const long long c = cid(d, i, j, k);
     const long long sx = (long long)d.ny * d.nz, sy = d.nz;
+    if (i > 0 && i < d.nx - 1 && j > 0 && j < d.ny - 1 && k > 0 && k < d.nz - 1) {
+        const long long m[6] = {__double_as_longlong(cf.ax[c]), __double_as_longlong(cf.ax[c + sx]),
+                                __double_as_longlong(cf.ay[c]), __double_as_longlong(cf.ay[c + sy]),
+                                __double_as_longlong(cf.az[c]), __double_as_longlong(cf.az[c + 1])};
+        const bool air = (m[0] == kOneBits) & (m[1] == kOneBits) & (m[2] == kOneBits) & (m[3] == kOneBits) &
+                         (m[4] == kOneBits) & (m[5] == kOneBits);
+        const bool liq = (m[0] == liq_bits) & (m[1] == liq_bits) & (m[2] == liq_bits) & (m[3] == liq_bits) &
+                         (m[4] == liq_bits) & (m[5] == liq_bits);
+        if (air) {
+            cf.dex[c] = 0.;
+            cf.D[c] = 6.;
+            if (want_invd) cf.invd[c] = 1. / 6.;
+            b[c] = 0.;
+            return;
+        }
+        if (liq) {
+            double rhs = 0.;
+            rhs += (m1 * hext.p[0][fid(d, 0, i, j, k)]) * h;       // ord -x: -side = +1
+            rhs += -(m1 * hext.p[0][fid(d, 0, i + 1, j, k)]) * h;  // ord +x: -side = -1
+            rhs += (m1 * hext.p[1][fid(d, 1, i, j, k)]) * h;
+            rhs += -(m1 * hext.p[1][fid(d, 1, i, j + 1, k)]) * h;
+            rhs += (m1 * hext.p[2][fid(d, 2, i, j, k)]) * h;
+            rhs += -(m1 * hext.p[2][fid(d, 2, i, j, k + 1)]) * h;
+            cf.dex[c] = 0.;
+            cf.D[c] = sv6;
+            if (want_invd) cf.invd[c] = inv_sv6;
+            b[c] = rhs;
+            return;
+        }
+    }
     double diag = 0., rhs = 0.;
     // (mu, valid, face index) in ord order -x, +x, -y, +y, -z, +z
 #pragma unroll
@@ -213,7 +301,7 @@ __global__ void __launch_bounds__(256) k_magnetic_rows(Dims d, Faces hext, doubl
         const double *arr = a == 0 ? cf.ax : (a == 1 ? cf.ay : cf.az);
         const double mu = up ? arr[c + st] : arr[c];
         diag += mu;
-        if (mu != 1.) {
+        if (__double_as_longlong(mu) != kOneBits) {
             const int fi = i + (a == 0) * up, fj = j + (a == 1) * up, fk = k + (a == 2) * up;
             const double side = up ? 1.0 : -1.0;
             rhs += (mu - 1.) * hext.p[a][fid(d, a, fi, fj, fk)] * (-side) * h;
@@ -226,8 +314,9 @@ __global__ void __launch_bounds__(256) k_magnetic_rows(Dims d, Faces hext, doubl
 }
 
 // AssignTotalField (core/MagneticField.cpp:125-143) for the faces of axis a.
-__global__ void __launch_bounds__(256) k_total_field(Dims d, int a, const double *__restrict__ psi, Faces hext,
-                                                     double invh, double *__restrict__ H) {
+template <int a>
+__global__ void __launch_bounds__(256) k_total_field(Dims d, const double *__restrict__ psi, Faces hext, double invh,
+                                                     double *__restrict__ H) {
     const int fx = d.nx + (a == 0), fy = d.ny + (a == 1), fz = d.nz + (a == 2);
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -331,9 +420,13 @@ void launch_build_pressure(cudaStream_t st, const Dims &d, const double *phi, co
 
 void launch_apply_projection(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &jump,
                              const double *p, const Faces &u) {
-    for (int a = 0; a < 3; a++)
-        k_apply_projection<<<grid3(d.nx + (a == 0), d.ny + (a == 1), d.nz + (a == 2)), blk2(), 0, st>>>(
-            d, a, phi, frac, jump, p, const_cast<double *>(u.p[a]));
+    // the face axis is a template parameter: the per-axis index arithmetic stays in registers
+    k_apply_projection<0><<<grid3(d.nx + 1, d.ny, d.nz), blk2(), 0, st>>>(d, phi, frac, jump, p,
+                                                                         const_cast<double *>(u.p[0]));
+    k_apply_projection<1><<<grid3(d.nx, d.ny + 1, d.nz), blk2(), 0, st>>>(d, phi, frac, jump, p,
+                                                                         const_cast<double *>(u.p[1]));
+    k_apply_projection<2><<<grid3(d.nx, d.ny, d.nz + 1), blk2(), 0, st>>>(d, phi, frac, jump, p,
+                                                                         const_cast<double *>(u.p[2]));
 }
 
 void launch_gather_cells(cudaStream_t st, long long n, const double *D, const double *x, double *out) {
@@ -350,8 +443,16 @@ int launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, dou
         return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
     };
     const double one_plus_chi = 1. + (1. - 0.) * chi;  // the reference's expression with H = 0
+    // the rows kernel's constants for cells whose six faces are 1 + chi: the diagonal summed in face order
+    // from 0, its reciprocal, and mu - 1
+    double sv6 = 0.;
+    for (int q = 0; q < 6; q++) sv6 += one_plus_chi;
+    const double m1 = one_plus_chi - 1.;
+    long long liq_bits;
+    std::memcpy(&liq_bits, &one_plus_chi, 8);
     k_magnetic_mu<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, chi, bw, key(t), key(-t), one_plus_chi, cf);
-    k_magnetic_rows<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, hext, h, cf, b, want_invd ? 1 : 0);
+    k_magnetic_rows<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, hext, h, cf, b, want_invd ? 1 : 0, liq_bits, m1,
+                                                                 sv6, sv6 > 0 ? 1. / sv6 : 0.);
     return 2;
 }
 
@@ -414,9 +515,9 @@ cudaError_t launch_magnetic_residual_noalloc(cudaStream_t st, const Dims &d, con
 
 void launch_total_field(cudaStream_t st, const Dims &d, const double *psi, const Faces &hext, double invh,
                         const Faces &H) {
-    for (int a = 0; a < 3; a++)
-        k_total_field<<<grid3(d.nx + (a == 0), d.ny + (a == 1), d.nz + (a == 2)), blk2(), 0, st>>>(
-            d, a, psi, hext, invh, const_cast<double *>(H.p[a]));
+    k_total_field<0><<<grid3(d.nx + 1, d.ny, d.nz), blk2(), 0, st>>>(d, psi, hext, invh, const_cast<double *>(H.p[0]));
+    k_total_field<1><<<grid3(d.nx, d.ny + 1, d.nz), blk2(), 0, st>>>(d, psi, hext, invh, const_cast<double *>(H.p[1]));
+    k_total_field<2><<<grid3(d.nx, d.ny, d.nz + 1), blk2(), 0, st>>>(d, psi, hext, invh, const_cast<double *>(H.p[2]));
 }
 
 __global__ void k_to_f32(long long n, const double *__restrict__ a, float *__restrict__ o) {
