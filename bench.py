@@ -49,7 +49,9 @@ def parse(argv=None):
     ap.add_argument("--coarse-dim", type=int, default=None)
     ap.add_argument("--pre", type=int, default=None)
     ap.add_argument("--post", type=int, default=None)
-    ap.add_argument("--smoother", type=int, default=None, help="0 two-colour, 1 fused one-pass, 2 (default) two-colour with FP16 finest-level smoothing coefficients")
+    ap.add_argument("--smoother", type=int, default=None,
+                    help="0 two-colour, 1 fused one-pass, 2 two-colour with FP16 finest-level smoothing coefficients, "
+                         "3 (default) as 2 with the finest level stored colour by colour")
     return ap.parse_args(argv)
 
 
@@ -267,11 +269,14 @@ def run_ours(args, ws, rank, local):
     peak_src = "measured" if peak else "fallback"
     peak = peak or 6800.0
     achieved = bytes_tot / (ms_tot / 1e3) / 1e9 if ms_tot > 0 else 0.0
-    smoother = 2 if args.smoother is None else args.smoother
+    smoother = 3 if args.smoother is None else args.smoother
     if smoother == 1:
         kname = "k_rbgs_tma (one full red-black sweep per launch, TMA-staged)"
         prof = "k_rbgs_tma_pool_sphere_256.md"
-    elif smoother == 2 and args.precision == "mixed":
+    elif smoother == 3 and args.precision == "mixed" and args.n % 8 == 0:
+        kname = "k_rbgs4s<__half> (one colour of a red-black sweep per launch, colour-split level, FP16 operator copy)"
+        prof = "k_rbgs4s_f16_split_finest_pool_sphere_256.md"
+    elif smoother in (2, 3) and args.precision == "mixed":
         kname = "k_rbgs4<__half> (one colour of a red-black sweep per launch, FP16 operator copy)"
         prof = "k_rbgs4_f16_finest_pool_sphere_256.md"
     else:

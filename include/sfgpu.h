@@ -76,8 +76,11 @@ typedef struct {
     double inner_tol;    /* mixed: floor of the inner relative reduction (default 1e-4) */
     int profile;         /* time every finest-level smoother launch with CUDA events (disables graphs) */
     int smoother;        /* 0: two in-place colour passes, 1: fused one-pass red-black sweep (TMA-staged at the
-                            finest FP32 level), 2 (default): as 0, and in the mixed form the finest level's
-                            smoother reads an FP16 copy of the operator (residuals and the CG operator stay FP32) */
+                            finest FP32 level), 2: as 0, and in the mixed form the finest level's smoother reads
+                            an FP16 copy of the operator (residuals and the CG operator stay FP32), 3 (default):
+                            as 2, with the mixed form's finest-level FP32 vectors and operator copies stored
+                            colour by colour (each half sweep streams one colour); needs nz % 8 == 0 and two or
+                            more levels, else runs as 2.  FP64 solves run 2 and 3 as 0. */
     int reserved[6];
 } sf_solve_opts;
 

@@ -97,7 +97,7 @@ bool opts_ok(const sf_solve_opts *o) {
     if (!o) return true;
     if (o->precision != SF_PREC_FP64 && o->precision != SF_PREC_MIXED && o->precision != SF_PREC_LEARNED) return false;
     if (o->max_levels < 0 || o->coarse_dim < 0) return false;
-    if (o->smoother < 0 || o->smoother > 2) return false;
+    if (o->smoother < 0 || o->smoother > 3) return false;
     return true;
 }
 
@@ -635,7 +635,7 @@ void sf_default_opts(sf_solve_opts *o, int which) {
     o->check_every = 1;
     o->report_ref_residual = 1;
     o->inner_tol = 1e-4;
-    o->smoother = 2;  // mixed form: FP16 finest-level smoothing coefficients; FP64: two colour passes
+    o->smoother = 3;  // mixed form: FP16 smoothing copy, colour-split finest level; FP64: two colour passes
 }
 
 sf_status sf_create(int device, void *stream, void **out) {

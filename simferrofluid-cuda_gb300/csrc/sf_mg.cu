@@ -1009,6 +1009,8 @@ static void apply_dot32(cudaStream_t st, const Dims &d, const Coef<float> &cf, c
     k_apply_dot<float, float><<<tg, dim3(32, 8), 0, st>>>(d, xpb, cf, p, q, sc, part, ticket);
 }
 
+#include "sf_split.cuh"
+
 // rho_new = (r, z), zq = (z, q); beta = flexible ? -alpha*zq/rho : rho_new/rho; rho = rho_new
 template <class T>
 __global__ void __launch_bounds__(256) k_dot_rz(long long n, const T *__restrict__ r, const T *__restrict__ z,
@@ -1061,20 +1063,20 @@ __global__ void __launch_bounds__(256) k_update(long long n, T *__restrict__ x, 
     if (grid_reduce<1>(v, part, ticket, tot)) sc[S_RR] = tot[0];
 }
 
-// r = b - A x (FP64 operator), written as TR (double, or float for the refinement's inner rhs);
-// slots: rr_slot = (r, r) in FP64, bb_slot = (b, b).  skip0: leave row 0 out of both sums.
+// r = b - A x (FP64 operator), written as TR (double, or float for the refinement's inner rhs, in the split
+// layout when `split`); slots: rr_slot = (r, r) in FP64, bb_slot = (b, b).  skip0: leave row 0 out of both sums.
 template <class TR>
 __global__ void __launch_bounds__(256) k_residual64(Dims d, int xpb, Coef<double> cf, const double *__restrict__ x,
                                                     const double *__restrict__ b, TR *__restrict__ r, int skip0,
                                                     int rr_slot, int bb_slot, double *sc, double *part,
-                                                    unsigned *ticket) {
+                                                    unsigned *ticket, int split = 0) {
     double v[2] = {0, 0};
     TILE_LOOP(d, xpb)
     double sa;
     double s = nbsum<double, double, false>(d, cf, x, i, j, k, c, sa);
     const double bc = b[c];
     double rc = (bc - cf.D[c] * x[c]) + s;
-    if (r) r[c] = (TR)rc;
+    if (r) r[split ? split_index(d, i, j, k) : c] = (TR)rc;
     if (!(skip0 && c == 0)) {
         v[0] += rc * rc;
         if (bb_slot >= 0) v[1] += bc * bc;
@@ -1087,16 +1089,17 @@ __global__ void __launch_bounds__(256) k_residual64(Dims d, int xpb, Coef<double
     }
 }
 
-// r = b for x = 0 (the first refinement step): cast to the inner precision; slots rr = bb = (b, b).
+// r = b for x = 0 (the first refinement step): cast to the inner precision (split layout when `split`, with d
+// the grid); slots rr = bb = (b, b).
 template <class TR>
 __global__ void __launch_bounds__(256) k_cast_rhs(long long n, const double *__restrict__ b, TR *__restrict__ r,
                                                   int rr_slot, int bb_slot, double *sc, double *part,
-                                                  unsigned *ticket) {
+                                                  unsigned *ticket, Dims d = Dims{0, 0, 0, 0}, int split = 0) {
     double v[1] = {0};
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
         const double bc = b[c];
-        r[c] = (TR)bc;
+        r[split ? split_of(d, c) : c] = (TR)bc;
         v[0] += bc * bc;
     }
     double tot[1];
@@ -1133,10 +1136,10 @@ __global__ void __launch_bounds__(256) k_dot_dd(long long n, const double *__res
     if (grid_reduce<1>(v, part, ticket, tot)) sc[slot] = tot[0];
 }
 
-// x64 += d32
-__global__ void k_ir_update(long long n, double *__restrict__ x, const float *__restrict__ dlt) {
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
-        x[c] += (double)dlt[c];
+// x64 += d32 (d32 in the split layout when `split`)
+__global__ void k_ir_update(Dims d, int split, double *__restrict__ x, const float *__restrict__ dlt) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < d.n; c += (long long)gridDim.x * blockDim.x)
+        x[c] += (double)dlt[split ? split_of(d, c) : c];
 }
 
 __global__ void k_shift(long long n, double *__restrict__ x) {
@@ -1287,9 +1290,36 @@ static void fused(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const 
 
 // nu sweeps; the result always ends in x.  pre: starts from x = 0 (x's input value is ignored).
 // fused (tmp != nullptr): one kernel per sweep, ping-ponging between x and tmp; else two in-place colours.
+// Half sweep of the split level 0 (smoother 3); same algorithmic bytes as the natural half sweep.
+template <class C>
+static void rb_split(cudaStream_t st, Tracker &tk, bool zero, const Dims &d, const Coef<C> &cf, float *x,
+                     const float *b, int color) {
+    const dim3 g(((d.nz >> 1) / 4 + 31) / 32, (d.ny + 7) / 8, d.nx);
+    tk.before(st, true);
+    if (zero)
+        k_rbgs4s<C, true><<<g, blk2(), 0, st>>>(d, cf, x, b, color);
+    else
+        k_rbgs4s<C, false><<<g, blk2(), 0, st>>>(d, cf, x, b, color);
+    tk.after(st, true, (3.0 * sizeof(float) + 4.0 * sizeof(C)) / 2.0 * d.n);
+}
+
 template <class T, class C>
 static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const Coef<C> &cf, T *x, T *tmp,
-                   const T *b, int nu, bool pre) {
+                   const T *b, int nu, bool pre, bool split = false) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (split) {
+            for (int s = 0; s < nu; s++) {
+                if (pre) {
+                    rb_split<C>(st, tk, s == 0, d, cf, x, b, 0);
+                    rb_split<C>(st, tk, false, d, cf, x, b, 1);
+                } else {
+                    rb_split<C>(st, tk, false, d, cf, x, b, 1);
+                    rb_split<C>(st, tk, false, d, cf, x, b, 0);
+                }
+            }
+            return;
+        }
+    }
     if (!tmp) {
         for (int s = 0; s < nu; s++) {
             if (pre) {
@@ -1327,8 +1357,14 @@ static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const
 
 template <class T, class C>
 static void restrict_res(cudaStream_t st, Tracker &tk, const Dims &d, const Coef<C> &cf, const T *x, const T *b,
-                         const Dims &dc, T *bc) {
+                         const Dims &dc, T *bc, bool split = false) {
     tk.launches++;
+    if constexpr (std::is_same<T, float>::value) {
+        if (split) {
+            k_resid_restrict_s<C><<<grid_cells(dc), blk2(), 0, st>>>(d, cf, x, b, dc, bc);
+            return;
+        }
+    }
     k_resid_restrict<T, C><<<grid_cells(dc), blk2(), 0, st>>>(d, cf, x, b, dc, bc);
 }
 
@@ -1352,14 +1388,14 @@ template <class T, class C0, class Cc, class C0S>
 static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, const Coef<C0> &c0,
                    const Coef<C0S> &c0s, const std::vector<Coef<Cc>> &cc, T *z, const T *r,
                    const std::vector<T *> &xs, const std::vector<T *> &bs, const std::vector<T *> &ts,
-                   const SolverParams &p) {
+                   const SolverParams &p, bool split0 = false) {
     const int L = (int)dims.size();
     if (L == 1) {
         coarse_solve<T, C0>(st, tk, dims[0], c0, z, r, p.coarse_sweeps);
         return;
     }
-    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true);
-    restrict_res<T, C0S>(st, tk, dims[0], c0s, z, r, dims[1], bs[1]);  // the residual of the smoothed operator
+    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true, split0);
+    restrict_res<T, C0S>(st, tk, dims[0], c0s, z, r, dims[1], bs[1], split0);  // the residual of the smoothed operator
     for (int l = 1; l < L - 1; l++) {
         smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.pre, true);
         restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1]);
@@ -1371,6 +1407,15 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
         smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.post, false);
     }
     tk.launches++;
+    if constexpr (std::is_same<T, float>::value) {
+        if (split0) {
+            const Dims &d0 = dims[0];
+            k_prolong_s<<<dim3(((d0.nz >> 1) / 4 + 31) / 32, (d0.ny + 7) / 8, d0.nx), blk2(), 0, st>>>(d0, z, dims[1],
+                                                                                                    xs[1]);
+            smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true);
+            return;
+        }
+    }
     k_prolong<T><<<grid_cells(dims[0]), blk2(), 0, st>>>(dims[0], z, dims[1], xs[1]);
     smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false);
 }
@@ -1423,9 +1468,15 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
         if (t.nx <= cdim && t.ny <= cdim && t.nz <= cdim) break;
         dims.push_back(make_dims((t.nx + 1) / 2, (t.ny + 1) / 2, (t.nz + 1) / 2));
     }
+    // smoother 3 (split level 0) needs rows of whole 16-byte vectors per colour, a coarse level, and a split
+    // Krylov operator grid within the reduction's block budget; otherwise it runs as smoother 2
+    const bool split0 = p.precision == 1 && p.smoother == 3 && d.nz % 8 == 0 && dims.size() >= 2 &&
+                        (long long)(((d.nz >> 1) + 127) / 128) * 2 * ((d.ny + 7) / 8) <= kApplyBlocks;
+    const bool fp16copy = p.smoother == 2 || p.smoother == 3;
     const bool same = configured_ && cfg_dims_.nx == d.nx && cfg_dims_.ny == d.ny && cfg_dims_.nz == d.nz &&
                       cfg_prec_ == p.precision && cfg_levels_ == (int)dims.size() && cfg_cdim_ == cdim &&
-                      (p.precision == 0 || (cfg_smoother_ == 2) == (p.smoother == 2));
+                      (p.precision == 0 ||
+                       ((cfg_smoother_ == 2 || cfg_smoother_ == 3) == fp16copy && cfg_split_ == split0));
     prm_ = p;
     if (same) return cudaSuccess;
     destroy_graphs();
@@ -1478,7 +1529,7 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
         c32_.D = c32_.invd = nullptr;
         c32_.scale = c32_.unscale = 1.f;
         c16s0_ = Coef<__half>{};
-        if (p.smoother == 2) {
+        if (fp16copy) {
             c16s0_.ax = (__half *)chk(A(2 * n));
             c16s0_.ay = (__half *)chk(A(2 * n));
             c16s0_.az = (__half *)chk(A(2 * n));
@@ -1527,6 +1578,7 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     cfg_levels_ = L;
     cfg_cdim_ = cdim;
     cfg_smoother_ = p.smoother;
+    cfg_split_ = split0_ = split0;
     return cudaGetLastError();
 }
 
@@ -1538,10 +1590,16 @@ cudaError_t MGSolver::build_hierarchy() {
             k_coarsen<double, double><<<grid_cells(lev_dims_[l]), blk2(), 0, st_>>>(lev_dims_[l - 1], c64_[l - 1],
                                                                                     lev_dims_[l], c64_[l]);
     } else {
-        k_to32<<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0].n, c64_[0], c32_);
-        if (prm_.smoother == 2) {
-            k_to16<<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0].n, c64_[0], c16s0_);
+        if (split0_) {
+            k_to_split<float><<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0], c64_[0], c32_);
+            k_to_split<__half><<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0], c64_[0], c16s0_);
             tk_.launches++;
+        } else {
+            k_to32<<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0].n, c64_[0], c32_);
+            if (prm_.smoother == 2 || prm_.smoother == 3) {
+                k_to16<<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0].n, c64_[0], c16s0_);
+                tk_.launches++;
+            }
         }
         if (L > 1)
             k_coarsen<double, __half><<<grid_cells(lev_dims_[1]), blk2(), 0, st_>>>(lev_dims_[0], c64_[0],
@@ -1577,15 +1635,18 @@ void MGSolver::enqueue_iter32() {
     const long long n = d.n;
     const long long l0 = tk_.launches;
     const std::vector<float *> ts = prm_.smoother == 1 ? t32_ : std::vector<float *>(t32_.size(), nullptr);
-    if (prm_.smoother == 2)
+    if (prm_.smoother == 2 || prm_.smoother == 3)
         vcycle<float, float, __half, __half>(st_, tk_, lev_dims_, c32_, c16s0_, c16_, z32_, ri32_, x32_, b32_, ts,
-                                             prm_);
+                                             prm_, split0_);
     else
         vcycle<float, float, __half, float>(st_, tk_, lev_dims_, c32_, c32_, c16_, z32_, ri32_, x32_, b32_, ts,
                                             prm_);
     k_dot_rz<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, ri32_, z32_, q32_, 1, sc_, part_, ticket_);
     k_xpby<float><<<flat_grid(n), 256, 0, st_>>>(n, z32_, p32_, sc_);
-    apply_dot32(st_, d, c32_, p32_, q32_, sc_, part_, ticket_);
+    if (split0_)
+        apply_dot32s(st_, d, c32_, p32_, q32_, sc_, part_, ticket_);
+    else
+        apply_dot32(st_, d, c32_, p32_, q32_, sc_, part_, ticket_);
     k_update<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, d32_, ri32_, p32_, q32_, sc_, part_, ticket_);
     tk_.launches += 4;
     iter_launches32_ = tk_.launches - l0;
@@ -1730,11 +1791,12 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
     while (true) {
         // outer FP64 residual, cast to the FP32 inner right-hand side
         if (x_zero) {
-            k_cast_rhs<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, b_, r32_, S_AUX1, S_BB, sc_, part_, ticket_);
+            k_cast_rhs<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, b_, r32_, S_AUX1, S_BB, sc_, part_, ticket_, d,
+                                                                       split0_ ? 1 : 0);
             x_zero = false;
         } else {
             k_residual64<float><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c64_[0], x_, b_, r32_, 0, S_AUX1,
-                                                             bb < 0 ? S_BB : -1, sc_, part_, ticket_);
+                                                             bb < 0 ? S_BB : -1, sc_, part_, ticket_, split0_ ? 1 : 0);
         }
         tk_.launches++;
         if ((e = read_slots()) != cudaSuccess) return e;
@@ -1794,7 +1856,7 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
             if (slow >= 2) break;
         }
         total_inner += it;
-        k_ir_update<<<flat_grid(n), 256, 0, st_>>>(n, x_, d32_);
+        k_ir_update<<<flat_grid(n), 256, 0, st_>>>(d, split0_ ? 1 : 0, x_, d32_);
         tk_.launches++;
         outer++;
         if (sc_host_[S_AUX0] != 0) {
@@ -1822,7 +1884,13 @@ cudaError_t MGSolver::set_guess_scaled(const float *y, double &gamma) {
     if (prm_.precision != 1) return cudaErrorInvalidValue;
     const Dims &d = lev_dims_[0];
     // (y, A y) on the FP32 level-0 operator and (y, b); gamma minimises the A-norm error along y
-    apply_dot32(st_, d, c32_, y, q32_, sc_, part_, ticket_);
+    if (split0_) {
+        k_vec_to_split<<<flat_grid(d.n), 256, 0, st_>>>(d, y, z32_);
+        apply_dot32s(st_, d, c32_, z32_, q32_, sc_, part_, ticket_);
+        tk_.launches++;
+    } else {
+        apply_dot32(st_, d, c32_, y, q32_, sc_, part_, ticket_);
+    }
     k_dot_fd<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(d.n, y, b_, S_AUX2, sc_, part_, ticket_);
     tk_.launches += 2;
     cudaError_t e = read_slots();

@@ -136,7 +136,10 @@ class MGSolver {
     // mixed: level 0 FP32, levels >= 1 FP16
     Coef<float> c32_{};
     std::vector<Coef<__half>> c16_;  // index l-1 for level l
-    Coef<__half> c16s0_{};           // level 0 in FP16, read only by the level-0 smoother (smoother 2)
+    Coef<__half> c16s0_{};           // level 0 in FP16, read only by the level-0 smoother (smoothers 2 and 3)
+    // smoother 3 in effect: level 0's FP32 vectors and both of its operator copies are stored colour by colour
+    // (sf_split.cuh); the FP64 operator and vectors keep the natural layout
+    bool split0_ = false, cfg_split_ = false;
     std::vector<float *> x32_, b32_, t32_;
 
     double *x_ = nullptr, *b_ = nullptr;

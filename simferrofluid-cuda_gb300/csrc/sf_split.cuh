@@ -1,0 +1,362 @@
+// sf_split.cuh -- finest level of the mixed form stored colour by colour (smoother 3).  Included by sf_mg.cu.
+//
+// Layout.  Cell (i, j, k) has colour col = (i + j + k) & 1.  Every FP32 vector of level 0 and both level-0
+// operator copies (FP32 for the Krylov operator, FP16 for the smoother) hold colour 0 in their first half and
+// colour 1 in their second half; inside a half, row (i, j) holds its nz / 2 cells of that colour in k order:
+//     s(col, i, j, m) = col * n/2 + (i * ny + j) * nz/2 + m,      k = 2 m + ((i + j + col) & 1).
+// (nz a multiple of 8, so every row of a colour is a whole number of 16-byte vectors.)  The same-k neighbours
+// in x and y of a cell sit at the same m in the other colour's half; its z neighbours sit at m - 1 and m
+// (k - 1, k + 1) when k is even, at m and m + 1 when k is odd.  A coarse cell's eight children are the
+// entries m = K of both colours in four rows.
+//
+// Why: a red-black half sweep updates one colour from the other.  In the natural layout every launch streams
+// both colours of x, b and the operator (about 20 bytes per cell); here it reads the updated colour's b,
+// diagonal excess and lower couplings, the other colour's x and lower couplings above, and writes the updated
+// colour (about 13 bytes per cell).  The arithmetic of every cell -- which couplings, in which order -- is the
+// natural kernels' own, so a V-cycle gives the same values in permuted order.
+
+__host__ __device__ __forceinline__ long long split_index(const Dims &d, int i, int j, int k) {
+    const int col = (i + j + k) & 1;
+    return (long long)col * (d.n >> 1) + ((long long)i * d.ny + j) * (d.nz >> 1) + (k >> 1);
+}
+
+// Natural index -> split index (flat loops over natural cells).
+__device__ __forceinline__ long long split_of(const Dims &d, long long c) {
+    const long long row = c / d.nz;
+    const int k = (int)(c - row * d.nz);
+    const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
+    return split_index(d, i, j, k);
+}
+
+// FP64 level 0 -> split FP32 / FP16 copy (same roundings as k_to32 / k_to16).
+template <class C>
+__device__ __forceinline__ C cvt_coef(double v);
+template <>
+__device__ __forceinline__ float cvt_coef<float>(double v) {
+    return (float)v;
+}
+template <>
+__device__ __forceinline__ __half cvt_coef<__half>(double v) {
+    return __float2half_rn((float)v);
+}
+template <class C>
+__global__ void k_to_split(Dims d, Coef<double> f, Coef<C> o) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < d.n; c += (long long)gridDim.x * blockDim.x) {
+        const long long s = split_of(d, c);
+        o.ax[s] = cvt_coef<C>(f.ax[c]);
+        o.ay[s] = cvt_coef<C>(f.ay[c]);
+        o.az[s] = cvt_coef<C>(f.az[c]);
+        o.dex[s] = cvt_coef<C>(f.dex[c]);
+    }
+}
+
+// Natural FP32 vector -> split copy.
+__global__ void k_vec_to_split(Dims d, const float *__restrict__ y, float *__restrict__ o) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < d.n; c += (long long)gridDim.x * blockDim.x)
+        o[split_of(d, c)] = y[c];
+}
+
+// Red-black half sweep of colour `col` in the split layout (the counterpart of k_rbgs4).  Thread (q4, j, i)
+// updates the four colour-`col` cells m0 = 4 q4 .. m0 + 3 of row (i, j); QZ = (i + j + col) & 1 is uniform
+// over a warp (one j) and selects where the z neighbours sit.
+template <class C, bool ZERO>
+__global__ void __launch_bounds__(256) k_rbgs4s(Dims d, Coef<C> cf, float *__restrict__ x, const float *__restrict__ b,
+                                                int col) {
+    const int nh = d.nz >> 1;
+    const int m0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (j >= d.ny || m0 >= nh) return;
+    const long long row = ((long long)i * d.ny + j) * nh + m0;
+    const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
+    const long long sx = (long long)d.ny * nh, sy = nh;
+    const bool xl = i > 0, xu = i < d.nx - 1, yl = j > 0, yu = j < d.ny - 1;
+    float xm[4] = {0, 0, 0, 0}, xp[4] = {0, 0, 0, 0}, ym[4] = {0, 0, 0, 0}, yp[4] = {0, 0, 0, 0}, zo[4] = {0, 0, 0, 0};
+    float axl[4], axu[4] = {0, 0, 0, 0}, ayl[4], ayu[4] = {0, 0, 0, 0}, azl[4], azo[4], dx[4], bv[4];
+    ld4(cf.ax + own, axl);
+    if (xu) ld4(cf.ax + oth + sx, axu);
+    ld4(cf.ay + own, ayl);
+    if (yu) ld4(cf.ay + oth + sy, ayu);
+    ld4(cf.az + own, azl);
+    ld4(cf.az + oth, azo);
+    ld4(cf.dex + own, dx);
+    ld4(b + own, bv);
+    if (!ZERO) {
+        if (xl) ld4(x + oth - sx, xm);
+        if (xu) ld4(x + oth + sx, xp);
+        if (yl) ld4(x + oth - sy, ym);
+        if (yu) ld4(x + oth + sy, yp);
+        ld4(x + oth, zo);
+    }
+    float out[4];
+    auto sweep = [&](auto qc) {
+        constexpr int QZ = decltype(qc)::value;
+        // the other colour's entry just outside the vector: m0 - 1 (below, k even) or m0 + 4 (above, k odd)
+        float zx = 0.f, azx = 0.f;
+        if (QZ == 0) {
+            if (!ZERO && m0 > 0) zx = x[oth - 1];
+        } else if (m0 + 4 < nh) {
+            if (!ZERO) zx = x[oth + 4];
+            azx = ldv(cf.az, oth + 4);
+        }
+        auto upd = [&](auto tc) {
+            constexpr int t = decltype(tc)::value;
+            const int k = 2 * (m0 + t) + QZ;
+            float s = 0.f, sa = 0.f;
+            if (xl) {
+                const float a = axl[t];
+                if (!ZERO) s += a * xm[t];
+                sa += a;
+            }
+            if (xu) {
+                const float a = axu[t];
+                if (!ZERO) s += a * xp[t];
+                sa += a;
+            }
+            if (yl) {
+                const float a = ayl[t];
+                if (!ZERO) s += a * ym[t];
+                sa += a;
+            }
+            if (yu) {
+                const float a = ayu[t];
+                if (!ZERO) s += a * yp[t];
+                sa += a;
+            }
+            if (k > 0) {  // below: m - 1 (k even) or m (k odd) of the other colour
+                const float a = azl[t];
+                if (!ZERO) s += a * (QZ == 0 ? (t == 0 ? zx : zo[t == 0 ? 0 : t - 1]) : zo[t]);
+                sa += a;
+            }
+            if (k < d.nz - 1) {  // above: m (k even) or m + 1 (k odd), whose lower z coupling is this face's
+                const float a = QZ == 0 ? azo[t] : (t == 3 ? azx : azo[t == 3 ? 3 : t + 1]);
+                if (!ZERO) s += a * (QZ == 0 ? zo[t] : (t == 3 ? zx : zo[t == 3 ? 3 : t + 1]));
+                sa += a;
+            }
+            if (sizeof(C) == 2) {
+                if (!ZERO) s *= cf.unscale;
+                sa *= cf.unscale;
+            }
+            float e = dx[t];
+            if (sizeof(C) == 2) e *= cf.unscale;
+            const float D = sa + e;
+            const float inv = D > 0.f ? 1.f / D : 0.f;
+            out[t] = (bv[t] + s) * inv;
+        };
+        upd(std::integral_constant<int, 0>{});
+        upd(std::integral_constant<int, 1>{});
+        upd(std::integral_constant<int, 2>{});
+        upd(std::integral_constant<int, 3>{});
+    };
+    if (((i + j + col) & 1) == 0)
+        sweep(std::integral_constant<int, 0>{});
+    else
+        sweep(std::integral_constant<int, 1>{});
+    *reinterpret_cast<float4 *>(x + own) = make_float4(out[0], out[1], out[2], out[3]);
+}
+
+// Residual b - A x of colour-`col` cell (i, j, m), evaluated as nbsum + diag_of do for the natural layout.
+template <class C>
+__device__ __forceinline__ float resid_split(const Dims &d, const Coef<C> &cf, const float *__restrict__ x,
+                                             const float *__restrict__ b, int col, int i, int j, int m) {
+    const int nh = d.nz >> 1;
+    const long long row = ((long long)i * d.ny + j) * nh + m;
+    const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
+    const long long sx = (long long)d.ny * nh, sy = nh;
+    const int qz = (i + j + col) & 1, k = 2 * m + qz;
+    float s = 0.f, sa = 0.f;
+    if (i > 0) {
+        const float a = ldv(cf.ax, own);
+        s += a * x[oth - sx];
+        sa += a;
+    }
+    if (i < d.nx - 1) {
+        const float a = ldv(cf.ax, oth + sx);
+        s += a * x[oth + sx];
+        sa += a;
+    }
+    if (j > 0) {
+        const float a = ldv(cf.ay, own);
+        s += a * x[oth - sy];
+        sa += a;
+    }
+    if (j < d.ny - 1) {
+        const float a = ldv(cf.ay, oth + sy);
+        s += a * x[oth + sy];
+        sa += a;
+    }
+    if (k > 0) {
+        const float a = ldv(cf.az, own);
+        s += a * x[qz ? oth : oth - 1];
+        sa += a;
+    }
+    if (k < d.nz - 1) {
+        const long long u = qz ? oth + 1 : oth;
+        const float a = ldv(cf.az, u);
+        s += a * x[u];
+        sa += a;
+    }
+    if (sizeof(C) == 2) {
+        s *= cf.unscale;
+        sa *= cf.unscale;
+    }
+    float e = ldv(cf.dex, own);
+    if (sizeof(C) == 2) e *= cf.unscale;
+    const float D = sa + e;
+    return (b[own] - D * x[own]) + s;
+}
+
+// Restriction of the split level-0 residual to the (natural) level 1, children in k_resid_restrict's order.
+template <class C>
+__global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, const float *__restrict__ x,
+                                                          const float *__restrict__ b, Dims dc, float *__restrict__ bc) {
+    const int K = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int I = blockIdx.z;
+    if (K >= dc.nz || J >= dc.ny) return;
+    float acc = 0.f;
+#pragma unroll
+    for (int di = 0; di < 2; di++) {
+        const int i = 2 * I + di;
+        if (i >= d.nx) break;
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++) {
+            const int j = 2 * J + dj;
+            if (j >= d.ny) break;
+#pragma unroll
+            for (int dk = 0; dk < 2; dk++) acc += resid_split<C>(d, cf, x, b, (i + j + dk) & 1, i, j, K);
+        }
+    }
+    bc[cid(dc, I, J, K)] = acc;
+}
+
+// x += P xc on the split level 0 (piecewise constant): both colours' entries m of row (i, j) take coarse cell
+// (i/2, j/2, m).
+__global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x, Dims dc, const float *__restrict__ xc) {
+    const int nh = d.nz >> 1;
+    const int m0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (j >= d.ny || m0 >= nh) return;
+    float v[4];
+    ld4(xc + cid(dc, i >> 1, j >> 1, m0), v);
+    const long long row = ((long long)i * d.ny + j) * nh + m0;
+#pragma unroll
+    for (int col = 0; col < 2; col++) {
+        float *p = x + (long long)col * (d.n >> 1) + row;
+        float4 t = *reinterpret_cast<float4 *>(p);
+        t.x += v[0];
+        t.y += v[1];
+        t.z += v[2];
+        t.w += v[3];
+        *reinterpret_cast<float4 *>(p) = t;
+    }
+}
+
+// q = A p and (p, q) on the split FP32 level-0 operator (the counterpart of k_apply_dot4; each cell's q as in
+// k_apply_dot).  Block rows alternate colours: blockIdx.y = 2 * (y tile) + colour.
+__global__ void __launch_bounds__(256) k_apply_dot4s(Dims d, int xpb, Coef<float> cf, const float *__restrict__ p,
+                                                     float *__restrict__ q, double *sc, double *part, unsigned *ticket) {
+    float acc = 0.f;
+    const int nh = d.nz >> 1;
+    const int col = blockIdx.y & 1;
+    const int m0 = 4 * (blockIdx.x * 32 + threadIdx.x), j = (blockIdx.y >> 1) * 8 + threadIdx.y;
+    if (m0 < nh && j < d.ny) {
+        const long long sx = (long long)d.ny * nh, sy = nh;
+        const bool yl = j > 0, yu = j < d.ny - 1;
+        const int i_end = min(d.nx, (int)(blockIdx.z + 1) * xpb);
+        for (int i = blockIdx.z * xpb; i < i_end; i++) {
+            const long long row = ((long long)i * d.ny + j) * nh + m0;
+            const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
+            const bool xl = i > 0, xu = i < d.nx - 1;
+            const int qz = (i + j + col) & 1;
+            float pc[4], pxm[4] = {0, 0, 0, 0}, pxp[4] = {0, 0, 0, 0}, pym[4] = {0, 0, 0, 0}, pyp[4] = {0, 0, 0, 0}, po[4];
+            float axl[4], axu[4] = {0, 0, 0, 0}, ayl[4], ayu[4] = {0, 0, 0, 0}, azl[4], azo[4], dx[4];
+            ld4(p + own, pc);
+            ld4(p + oth, po);
+            if (xl) ld4(p + oth - sx, pxm);
+            if (xu) ld4(p + oth + sx, pxp);
+            if (yl) ld4(p + oth - sy, pym);
+            if (yu) ld4(p + oth + sy, pyp);
+            ld4(cf.ax + own, axl);
+            if (xu) ld4(cf.ax + oth + sx, axu);
+            ld4(cf.ay + own, ayl);
+            if (yu) ld4(cf.ay + oth + sy, ayu);
+            ld4(cf.az + own, azl);
+            ld4(cf.az + oth, azo);
+            ld4(cf.dex + own, dx);
+            float out[4];
+            auto body = [&](auto qc) {
+                constexpr int QZ = decltype(qc)::value;
+                float zx = 0.f, azx = 0.f;
+                if (QZ == 0) {
+                    if (m0 > 0) zx = p[oth - 1];
+                } else if (m0 + 4 < nh) {
+                    zx = p[oth + 4];
+                    azx = cf.az[oth + 4];
+                }
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    const int k = 2 * (m0 + t) + QZ;
+                    float s = 0.f, sa = 0.f;
+                    if (xl) {
+                        s += axl[t] * pxm[t];
+                        sa += axl[t];
+                    }
+                    if (xu) {
+                        s += axu[t] * pxp[t];
+                        sa += axu[t];
+                    }
+                    if (yl) {
+                        s += ayl[t] * pym[t];
+                        sa += ayl[t];
+                    }
+                    if (yu) {
+                        s += ayu[t] * pyp[t];
+                        sa += ayu[t];
+                    }
+                    if (k > 0) {
+                        const float a = azl[t];
+                        s += a * (QZ == 0 ? (t == 0 ? zx : po[t == 0 ? 0 : t - 1]) : po[t]);
+                        sa += a;
+                    }
+                    if (k < d.nz - 1) {
+                        const float a = QZ == 0 ? azo[t] : (t == 3 ? azx : azo[t == 3 ? 3 : t + 1]);
+                        s += a * (QZ == 0 ? po[t] : (t == 3 ? zx : po[t == 3 ? 3 : t + 1]));
+                        sa += a;
+                    }
+                    const float D = sa + dx[t];
+                    out[t] = D * pc[t] - s;
+                    acc += pc[t] * out[t];
+                }
+            };
+            if (qz == 0)
+                body(std::integral_constant<int, 0>{});
+            else
+                body(std::integral_constant<int, 1>{});
+            *reinterpret_cast<float4 *>(q + own) = make_float4(out[0], out[1], out[2], out[3]);
+        }
+    }
+    double v[1] = {(double)acc};
+    double tot[1];
+    if (grid_reduce<1>(v, part, ticket, tot)) {
+        sc[S_PQ] = tot[0];
+        if (tot[0] > 0 && isfinite(tot[0])) {
+            sc[S_ALPHA] = sc[S_RHO] / tot[0];
+        } else {
+            sc[S_ALPHA] = 0;
+            sc[S_AUX0] = 1;  // breakdown
+        }
+    }
+}
+
+static void apply_dot32s(cudaStream_t st, const Dims &d, const Coef<float> &cf, const float *p, float *q, double *sc,
+                         double *part, unsigned *ticket) {
+    const int nh = d.nz >> 1;
+    const long long tiles = (long long)((nh + 127) / 128) * 2 * ((d.ny + 7) / 8);
+    const long long zmax = tiles < kApplyBlocks ? kApplyBlocks / tiles : 1;
+    int xpb = (int)((d.nx + zmax - 1) / zmax);
+    if (xpb < 2) xpb = 2;
+    const dim3 g((nh + 127) / 128, 2 * ((d.ny + 7) / 8), (d.nx + xpb - 1) / xpb);
+    k_apply_dot4s<<<g, dim3(32, 8), 0, st>>>(d, xpb, cf, p, q, sc, part, ticket);
+}
