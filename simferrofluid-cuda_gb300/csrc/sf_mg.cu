@@ -1089,17 +1089,16 @@ __global__ void __launch_bounds__(256) k_residual64(Dims d, int xpb, Coef<double
     }
 }
 
-// r = b for x = 0 (the first refinement step): cast to the inner precision (split layout when `split`, with d
-// the grid); slots rr = bb = (b, b).
+// r = b for x = 0 (the first refinement step): cast to the inner precision; slots rr = bb = (b, b).
 template <class TR>
 __global__ void __launch_bounds__(256) k_cast_rhs(long long n, const double *__restrict__ b, TR *__restrict__ r,
                                                   int rr_slot, int bb_slot, double *sc, double *part,
-                                                  unsigned *ticket, Dims d = Dims{0, 0, 0, 0}, int split = 0) {
+                                                  unsigned *ticket) {
     double v[1] = {0};
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
         const double bc = b[c];
-        r[split ? split_of(d, c) : c] = (TR)bc;
+        r[c] = (TR)bc;
         v[0] += bc * bc;
     }
     double tot[1];
@@ -1136,10 +1135,10 @@ __global__ void __launch_bounds__(256) k_dot_dd(long long n, const double *__res
     if (grid_reduce<1>(v, part, ticket, tot)) sc[slot] = tot[0];
 }
 
-// x64 += d32 (d32 in the split layout when `split`)
-__global__ void k_ir_update(Dims d, int split, double *__restrict__ x, const float *__restrict__ dlt) {
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < d.n; c += (long long)gridDim.x * blockDim.x)
-        x[c] += (double)dlt[split ? split_of(d, c) : c];
+// x64 += d32
+__global__ void k_ir_update(long long n, double *__restrict__ x, const float *__restrict__ dlt) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        x[c] += (double)dlt[c];
 }
 
 __global__ void k_shift(long long n, double *__restrict__ x) {
@@ -1361,7 +1360,8 @@ static void restrict_res(cudaStream_t st, Tracker &tk, const Dims &d, const Coef
     tk.launches++;
     if constexpr (std::is_same<T, float>::value) {
         if (split) {
-            k_resid_restrict_s<C><<<grid_cells(dc), blk2(), 0, st>>>(d, cf, x, b, dc, bc);
+            k_resid_restrict_s<C><<<dim3((dc.nz / 4 + 31) / 32, (dc.ny + 7) / 8, dc.nx), blk2(), 0, st>>>(d, cf, x, b,
+                                                                                                 dc, bc);
             return;
         }
     }
@@ -1591,9 +1591,7 @@ cudaError_t MGSolver::build_hierarchy() {
                                                                                     lev_dims_[l], c64_[l]);
     } else {
         if (split0_) {
-            k_to_split<float><<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0], c64_[0], c32_);
-            k_to_split<__half><<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0], c64_[0], c16s0_);
-            tk_.launches++;
+            k_to_split<<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(lev_dims_[0], c64_[0], c32_, c16s0_);
         } else {
             k_to32<<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0].n, c64_[0], c32_);
             if (prm_.smoother == 2 || prm_.smoother == 3) {
@@ -1791,8 +1789,11 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
     while (true) {
         // outer FP64 residual, cast to the FP32 inner right-hand side
         if (x_zero) {
-            k_cast_rhs<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, b_, r32_, S_AUX1, S_BB, sc_, part_, ticket_, d,
-                                                                       split0_ ? 1 : 0);
+            if (split0_)
+                k_cast_rhs_s<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(d, b_, r32_, S_AUX1, S_BB, sc_, part_, ticket_);
+            else
+                k_cast_rhs<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, b_, r32_, S_AUX1, S_BB, sc_, part_,
+                                                                           ticket_);
             x_zero = false;
         } else {
             k_residual64<float><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c64_[0], x_, b_, r32_, 0, S_AUX1,
@@ -1856,7 +1857,10 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
             if (slow >= 2) break;
         }
         total_inner += it;
-        k_ir_update<<<flat_grid(n), 256, 0, st_>>>(d, split0_ ? 1 : 0, x_, d32_);
+        if (split0_)
+            k_ir_update_s<<<split_rows_grid(d), dim3(32, 8), 0, st_>>>(d, x_, d32_);
+        else
+            k_ir_update<<<flat_grid(n), 256, 0, st_>>>(n, x_, d32_);
         tk_.launches++;
         outer++;
         if (sc_host_[S_AUX0] != 0) {
@@ -1885,7 +1889,7 @@ cudaError_t MGSolver::set_guess_scaled(const float *y, double &gamma) {
     const Dims &d = lev_dims_[0];
     // (y, A y) on the FP32 level-0 operator and (y, b); gamma minimises the A-norm error along y
     if (split0_) {
-        k_vec_to_split<<<flat_grid(d.n), 256, 0, st_>>>(d, y, z32_);
+        k_vec_to_split<<<split_rows_grid(d), dim3(32, 8), 0, st_>>>(d, y, z32_);
         apply_dot32s(st_, d, c32_, z32_, q32_, sc_, part_, ticket_);
         tk_.launches++;
     } else {

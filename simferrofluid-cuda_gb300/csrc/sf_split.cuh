@@ -20,40 +20,82 @@ __host__ __device__ __forceinline__ long long split_index(const Dims &d, int i, 
     return (long long)col * (d.n >> 1) + ((long long)i * d.ny + j) * (d.nz >> 1) + (k >> 1);
 }
 
-// Natural index -> split index (flat loops over natural cells).
-__device__ __forceinline__ long long split_of(const Dims &d, long long c) {
-    const long long row = c / d.nz;
-    const int k = (int)(c - row * d.nz);
-    const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
-    return split_index(d, i, j, k);
+// Grid-stride loop over the rows (i, j) of the split layout, blockDim.y rows per block and blockDim.x threads
+// along a row, without a per-element division: for each m, cell k = 2m + p is colour 0 and k = 2m + 1 - p is
+// colour 1 (p the row's parity), both stored at m of their colour's half.  `nat` is the row's first natural
+// index and `sp` its first index inside a colour's half.
+#define SPLIT_ROWS(d)                                                                                        \
+    const int nh_ = (d).nz >> 1;                                                                              \
+    const long long hn_ = (d).n >> 1, nrows_ = (long long)(d).nx * (d).ny;                                     \
+    for (long long row = blockIdx.x * (long long)blockDim.y + threadIdx.y; row < nrows_;                     \
+         row += (long long)gridDim.x * blockDim.y) {                                                          \
+        const int i_ = (int)(row / (d).ny), j_ = (int)(row - (long long)i_ * (d).ny);                        \
+        const int p = (i_ + j_) & 1;                                                                          \
+        const long long nat = row * (d).nz, sp = row * nh_;                                                   \
+        for (int m = threadIdx.x; m < nh_; m += blockDim.x) {                                                 \
+            const long long n0 = nat + 2 * m + p, n1 = nat + 2 * m + 1 - p, s0 = sp + m, s1 = hn_ + sp + m;
+
+#define SPLIT_ROWS_END \
+    }                  \
+    }
+
+static inline int split_rows_grid(const Dims &d) {
+    long long g = ((long long)d.nx * d.ny + 7) / 8;
+    if (g > 152 * 16) g = 152 * 16;
+    return (int)(g < 1 ? 1 : g);
 }
 
-// FP64 level 0 -> split FP32 / FP16 copy (same roundings as k_to32 / k_to16).
-template <class C>
-__device__ __forceinline__ C cvt_coef(double v);
-template <>
-__device__ __forceinline__ float cvt_coef<float>(double v) {
-    return (float)v;
-}
-template <>
-__device__ __forceinline__ __half cvt_coef<__half>(double v) {
-    return __float2half_rn((float)v);
-}
-template <class C>
-__global__ void k_to_split(Dims d, Coef<double> f, Coef<C> o) {
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < d.n; c += (long long)gridDim.x * blockDim.x) {
-        const long long s = split_of(d, c);
-        o.ax[s] = cvt_coef<C>(f.ax[c]);
-        o.ay[s] = cvt_coef<C>(f.ay[c]);
-        o.az[s] = cvt_coef<C>(f.az[c]);
-        o.dex[s] = cvt_coef<C>(f.dex[c]);
+// FP64 level 0 -> split FP32 copy (Krylov operator) and FP16 copy (smoother) in one pass, with the roundings
+// of k_to32 / k_to16.
+__global__ void __launch_bounds__(256) k_to_split(Dims d, Coef<double> f, Coef<float> o32, Coef<__half> o16) {
+    SPLIT_ROWS(d)
+    const double *src[4] = {f.ax, f.ay, f.az, f.dex};
+    float *d32[4] = {o32.ax, o32.ay, o32.az, o32.dex};
+    __half *d16[4] = {o16.ax, o16.ay, o16.az, o16.dex};
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const float v0 = (float)src[a][n0], v1 = (float)src[a][n1];
+        d32[a][s0] = v0;
+        d32[a][s1] = v1;
+        d16[a][s0] = __float2half_rn(v0);
+        d16[a][s1] = __float2half_rn(v1);
     }
+    SPLIT_ROWS_END
 }
 
 // Natural FP32 vector -> split copy.
-__global__ void k_vec_to_split(Dims d, const float *__restrict__ y, float *__restrict__ o) {
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < d.n; c += (long long)gridDim.x * blockDim.x)
-        o[split_of(d, c)] = y[c];
+__global__ void __launch_bounds__(256) k_vec_to_split(Dims d, const float *__restrict__ y, float *__restrict__ o) {
+    SPLIT_ROWS(d)
+    o[s0] = y[n0];
+    o[s1] = y[n1];
+    SPLIT_ROWS_END
+}
+
+// First refinement step from x = 0 on the split level: r = (float) b in the split layout; slots rr = bb = (b, b).
+__global__ void __launch_bounds__(256) k_cast_rhs_s(Dims d, const double *__restrict__ b, float *__restrict__ r,
+                                                    int rr_slot, int bb_slot, double *sc, double *part,
+                                                    unsigned *ticket) {
+    double v[1] = {0};
+    SPLIT_ROWS(d)
+    const double b0 = b[n0], b1 = b[n1];
+    r[s0] = (float)b0;
+    r[s1] = (float)b1;
+    v[0] += b0 * b0;
+    v[0] += b1 * b1;
+    SPLIT_ROWS_END
+    double tot[1];
+    if (grid_reduce<1>(v, part, ticket, tot)) {
+        sc[rr_slot] = tot[0];
+        sc[bb_slot] = tot[0];
+    }
+}
+
+// x64 += d32 with d32 in the split layout.
+__global__ void __launch_bounds__(256) k_ir_update_s(Dims d, double *__restrict__ x, const float *__restrict__ dlt) {
+    SPLIT_ROWS(d)
+    x[n0] += (double)dlt[s0];
+    x[n1] += (double)dlt[s1];
+    SPLIT_ROWS_END
 }
 
 // Red-black half sweep of colour `col` in the split layout (the counterpart of k_rbgs4).  Thread (q4, j, i)
@@ -155,79 +197,119 @@ __global__ void __launch_bounds__(256) k_rbgs4s(Dims d, Coef<C> cf, float *__res
     *reinterpret_cast<float4 *>(x + own) = make_float4(out[0], out[1], out[2], out[3]);
 }
 
-// Residual b - A x of colour-`col` cell (i, j, m), evaluated as nbsum + diag_of do for the natural layout.
+// Residuals b - A x of the four colour-`col` cells m0 .. m0 + 3 of row (i, j), each evaluated as nbsum +
+// diag_of do for the natural layout, with vector loads.
 template <class C>
-__device__ __forceinline__ float resid_split(const Dims &d, const Coef<C> &cf, const float *__restrict__ x,
-                                             const float *__restrict__ b, int col, int i, int j, int m) {
+__device__ __forceinline__ void resid4_split(const Dims &d, const Coef<C> &cf, const float *__restrict__ x,
+                                             const float *__restrict__ b, int col, int i, int j, int m0,
+                                             float (&r)[4]) {
     const int nh = d.nz >> 1;
-    const long long row = ((long long)i * d.ny + j) * nh + m;
+    const long long row = ((long long)i * d.ny + j) * nh + m0;
     const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
     const long long sx = (long long)d.ny * nh, sy = nh;
-    const int qz = (i + j + col) & 1, k = 2 * m + qz;
-    float s = 0.f, sa = 0.f;
-    if (i > 0) {
-        const float a = ldv(cf.ax, own);
-        s += a * x[oth - sx];
-        sa += a;
-    }
-    if (i < d.nx - 1) {
-        const float a = ldv(cf.ax, oth + sx);
-        s += a * x[oth + sx];
-        sa += a;
-    }
-    if (j > 0) {
-        const float a = ldv(cf.ay, own);
-        s += a * x[oth - sy];
-        sa += a;
-    }
-    if (j < d.ny - 1) {
-        const float a = ldv(cf.ay, oth + sy);
-        s += a * x[oth + sy];
-        sa += a;
-    }
-    if (k > 0) {
-        const float a = ldv(cf.az, own);
-        s += a * x[qz ? oth : oth - 1];
-        sa += a;
-    }
-    if (k < d.nz - 1) {
-        const long long u = qz ? oth + 1 : oth;
-        const float a = ldv(cf.az, u);
-        s += a * x[u];
-        sa += a;
-    }
-    if (sizeof(C) == 2) {
-        s *= cf.unscale;
-        sa *= cf.unscale;
-    }
-    float e = ldv(cf.dex, own);
-    if (sizeof(C) == 2) e *= cf.unscale;
-    const float D = sa + e;
-    return (b[own] - D * x[own]) + s;
+    const bool xl = i > 0, xu = i < d.nx - 1, yl = j > 0, yu = j < d.ny - 1;
+    float xc[4], xm[4] = {0, 0, 0, 0}, xp[4] = {0, 0, 0, 0}, ym[4] = {0, 0, 0, 0}, yp[4] = {0, 0, 0, 0}, zo[4];
+    float axl[4], axu[4] = {0, 0, 0, 0}, ayl[4], ayu[4] = {0, 0, 0, 0}, azl[4], azo[4], dx[4], bv[4];
+    ld4(x + own, xc);
+    ld4(x + oth, zo);
+    if (xl) ld4(x + oth - sx, xm);
+    if (xu) ld4(x + oth + sx, xp);
+    if (yl) ld4(x + oth - sy, ym);
+    if (yu) ld4(x + oth + sy, yp);
+    ld4(cf.ax + own, axl);
+    if (xu) ld4(cf.ax + oth + sx, axu);
+    ld4(cf.ay + own, ayl);
+    if (yu) ld4(cf.ay + oth + sy, ayu);
+    ld4(cf.az + own, azl);
+    ld4(cf.az + oth, azo);
+    ld4(cf.dex + own, dx);
+    ld4(b + own, bv);
+    auto body = [&](auto qc) {
+        constexpr int QZ = decltype(qc)::value;
+        float zx = 0.f, azx = 0.f;
+        if (QZ == 0) {
+            if (m0 > 0) zx = x[oth - 1];
+        } else if (m0 + 4 < nh) {
+            zx = x[oth + 4];
+            azx = ldv(cf.az, oth + 4);
+        }
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const int k = 2 * (m0 + t) + QZ;
+            float s = 0.f, sa = 0.f;
+            if (xl) {
+                const float a = axl[t];
+                s += a * xm[t];
+                sa += a;
+            }
+            if (xu) {
+                const float a = axu[t];
+                s += a * xp[t];
+                sa += a;
+            }
+            if (yl) {
+                const float a = ayl[t];
+                s += a * ym[t];
+                sa += a;
+            }
+            if (yu) {
+                const float a = ayu[t];
+                s += a * yp[t];
+                sa += a;
+            }
+            if (k > 0) {
+                const float a = azl[t];
+                s += a * (QZ == 0 ? (t == 0 ? zx : zo[t == 0 ? 0 : t - 1]) : zo[t]);
+                sa += a;
+            }
+            if (k < d.nz - 1) {
+                const float a = QZ == 0 ? azo[t] : (t == 3 ? azx : azo[t == 3 ? 3 : t + 1]);
+                s += a * (QZ == 0 ? zo[t] : (t == 3 ? zx : zo[t == 3 ? 3 : t + 1]));
+                sa += a;
+            }
+            if (sizeof(C) == 2) {
+                s *= cf.unscale;
+                sa *= cf.unscale;
+            }
+            float e = dx[t];
+            if (sizeof(C) == 2) e *= cf.unscale;
+            const float D = sa + e;
+            r[t] = (bv[t] - D * xc[t]) + s;
+        }
+    };
+    if (((i + j + col) & 1) == 0)
+        body(std::integral_constant<int, 0>{});
+    else
+        body(std::integral_constant<int, 1>{});
 }
 
-// Restriction of the split level-0 residual to the (natural) level 1, children in k_resid_restrict's order.
+// Restriction of the split level-0 residual to the (natural) level 1: thread (q4, J, I) sums the children of
+// coarse cells K0 = 4 q4 .. K0 + 3 in k_resid_restrict's order (x child, y child, then k = 2K, 2K + 1).
 template <class C>
 __global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, const float *__restrict__ x,
                                                           const float *__restrict__ b, Dims dc, float *__restrict__ bc) {
-    const int K = blockIdx.x * blockDim.x + threadIdx.x;
+    const int K0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int I = blockIdx.z;
-    if (K >= dc.nz || J >= dc.ny) return;
-    float acc = 0.f;
-#pragma unroll
+    if (K0 >= dc.nz || J >= dc.ny) return;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
     for (int di = 0; di < 2; di++) {
         const int i = 2 * I + di;
         if (i >= d.nx) break;
-#pragma unroll
         for (int dj = 0; dj < 2; dj++) {
             const int j = 2 * J + dj;
             if (j >= d.ny) break;
+            float r0[4], r1[4];
+            resid4_split<C>(d, cf, x, b, (i + j) & 1, i, j, K0, r0);      // k = 2K
+            resid4_split<C>(d, cf, x, b, (i + j + 1) & 1, i, j, K0, r1);  // k = 2K + 1
 #pragma unroll
-            for (int dk = 0; dk < 2; dk++) acc += resid_split<C>(d, cf, x, b, (i + j + dk) & 1, i, j, K);
+            for (int t = 0; t < 4; t++) {
+                acc[t] += r0[t];
+                acc[t] += r1[t];
+            }
         }
     }
-    bc[cid(dc, I, J, K)] = acc;
+    *reinterpret_cast<float4 *>(bc + cid(dc, I, J, K0)) = make_float4(acc[0], acc[1], acc[2], acc[3]);
 }
 
 // x += P xc on the split level 0 (piecewise constant): both colours' entries m of row (i, j) take coarse cell
