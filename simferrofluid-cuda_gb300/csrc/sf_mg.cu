@@ -1305,7 +1305,7 @@ static void rb_split(cudaStream_t st, Tracker &tk, bool zero, const Dims &d, con
 template <class T, class C>
 static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const Coef<C> &cf, T *x, T *tmp,
                    const T *b, int nu, bool pre, bool split = false) {
-    if constexpr (std::is_same<T, float>::value) {
+    if constexpr (std::is_same<T, float>::value && std::is_same<C, __half>::value) {  // split: FP16 copy only
         if (split) {
             for (int s = 0; s < nu; s++) {
                 if (pre) {
@@ -1358,7 +1358,7 @@ template <class T, class C>
 static void restrict_res(cudaStream_t st, Tracker &tk, const Dims &d, const Coef<C> &cf, const T *x, const T *b,
                          const Dims &dc, T *bc, bool split = false) {
     tk.launches++;
-    if constexpr (std::is_same<T, float>::value) {
+    if constexpr (std::is_same<T, float>::value && std::is_same<C, __half>::value) {
         if (split) {
             k_resid_restrict_s<C><<<dim3((dc.nz / 4 + 31) / 32, (dc.ny + 7) / 8, dc.nx), blk2(), 0, st>>>(d, cf, x, b,
                                                                                                  dc, bc);

@@ -13,7 +13,8 @@
 // both colours of x, b and the operator (about 20 bytes per cell); here it reads the updated colour's b,
 // diagonal excess and lower couplings, the other colour's x and lower couplings above, and writes the updated
 // colour (about 13 bytes per cell).  The arithmetic of every cell -- which couplings, in which order -- is the
-// natural kernels' own, so a V-cycle gives the same values in permuted order.
+// natural kernels' own; the restriction after the pre-smoothing sums only the colour that was not updated last
+// (the other colour's residual is zero up to rounding), so a V-cycle agrees with the natural one to rounding.
 
 __host__ __device__ __forceinline__ long long split_index(const Dims &d, int i, int j, int k) {
     const int col = (i + j + k) & 1;
@@ -98,11 +99,35 @@ __global__ void __launch_bounds__(256) k_ir_update_s(Dims d, double *__restrict_
     SPLIT_ROWS_END
 }
 
+// Four consecutive operator entries held as loaded: FP32 as four floats, FP16 packed two to a register and
+// converted where used (same values as ld4), which keeps the split kernels' register count at four blocks of
+// 256 threads per SM.  Index with compile-time t.
+template <class C>
+struct Cv4;
+template <>
+struct Cv4<float> {
+    float v[4];
+    __device__ __forceinline__ void load(const float *p) { ld4(p, v); }
+    __device__ __forceinline__ void zero() { v[0] = v[1] = v[2] = v[3] = 0.f; }
+    __device__ __forceinline__ float operator[](int t) const { return v[t]; }
+};
+template <>
+struct Cv4<__half> {
+    uint2 r;
+    __device__ __forceinline__ void load(const __half *p) { r = *reinterpret_cast<const uint2 *>(p); }
+    __device__ __forceinline__ void zero() { r = make_uint2(0u, 0u); }
+    __device__ __forceinline__ float operator[](int t) const {
+        const unsigned w = t < 2 ? r.x : r.y;
+        const __half2 h = *reinterpret_cast<const __half2 *>(&w);
+        return (t & 1) ? __high2float(h) : __low2float(h);
+    }
+};
+
 // Red-black half sweep of colour `col` in the split layout (the counterpart of k_rbgs4).  Thread (q4, j, i)
 // updates the four colour-`col` cells m0 = 4 q4 .. m0 + 3 of row (i, j); QZ = (i + j + col) & 1 is uniform
 // over a warp (one j) and selects where the z neighbours sit.
 template <class C, bool ZERO>
-__global__ void __launch_bounds__(256) k_rbgs4s(Dims d, Coef<C> cf, float *__restrict__ x, const float *__restrict__ b,
+__global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__restrict__ x, const float *__restrict__ b,
                                                 int col) {
     const int nh = d.nz >> 1;
     const int m0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
@@ -114,14 +139,17 @@ __global__ void __launch_bounds__(256) k_rbgs4s(Dims d, Coef<C> cf, float *__res
     const long long sx = (long long)d.ny * nh, sy = nh;
     const bool xl = i > 0, xu = i < d.nx - 1, yl = j > 0, yu = j < d.ny - 1;
     float xm[4] = {0, 0, 0, 0}, xp[4] = {0, 0, 0, 0}, ym[4] = {0, 0, 0, 0}, yp[4] = {0, 0, 0, 0}, zo[4] = {0, 0, 0, 0};
-    float axl[4], axu[4] = {0, 0, 0, 0}, ayl[4], ayu[4] = {0, 0, 0, 0}, azl[4], azo[4], dx[4], bv[4];
-    ld4(cf.ax + own, axl);
-    if (xu) ld4(cf.ax + oth + sx, axu);
-    ld4(cf.ay + own, ayl);
-    if (yu) ld4(cf.ay + oth + sy, ayu);
-    ld4(cf.az + own, azl);
-    ld4(cf.az + oth, azo);
-    ld4(cf.dex + own, dx);
+    float bv[4];
+    Cv4<C> axl, axu, ayl, ayu, azl, azo, dx;
+    axu.zero();
+    ayu.zero();
+    axl.load(cf.ax + own);
+    if (xu) axu.load(cf.ax + oth + sx);
+    ayl.load(cf.ay + own);
+    if (yu) ayu.load(cf.ay + oth + sy);
+    azl.load(cf.az + own);
+    azo.load(cf.az + oth);
+    dx.load(cf.dex + own);
     ld4(b + own, bv);
     if (!ZERO) {
         if (xl) ld4(x + oth - sx, xm);
@@ -209,20 +237,23 @@ __device__ __forceinline__ void resid4_split(const Dims &d, const Coef<C> &cf, c
     const long long sx = (long long)d.ny * nh, sy = nh;
     const bool xl = i > 0, xu = i < d.nx - 1, yl = j > 0, yu = j < d.ny - 1;
     float xc[4], xm[4] = {0, 0, 0, 0}, xp[4] = {0, 0, 0, 0}, ym[4] = {0, 0, 0, 0}, yp[4] = {0, 0, 0, 0}, zo[4];
-    float axl[4], axu[4] = {0, 0, 0, 0}, ayl[4], ayu[4] = {0, 0, 0, 0}, azl[4], azo[4], dx[4], bv[4];
+    float bv[4];
+    Cv4<C> axl, axu, ayl, ayu, azl, azo, dx;
+    axu.zero();
+    ayu.zero();
     ld4(x + own, xc);
     ld4(x + oth, zo);
     if (xl) ld4(x + oth - sx, xm);
     if (xu) ld4(x + oth + sx, xp);
     if (yl) ld4(x + oth - sy, ym);
     if (yu) ld4(x + oth + sy, yp);
-    ld4(cf.ax + own, axl);
-    if (xu) ld4(cf.ax + oth + sx, axu);
-    ld4(cf.ay + own, ayl);
-    if (yu) ld4(cf.ay + oth + sy, ayu);
-    ld4(cf.az + own, azl);
-    ld4(cf.az + oth, azo);
-    ld4(cf.dex + own, dx);
+    axl.load(cf.ax + own);
+    if (xu) axu.load(cf.ax + oth + sx);
+    ayl.load(cf.ay + own);
+    if (yu) ayu.load(cf.ay + oth + sy);
+    azl.load(cf.az + own);
+    azo.load(cf.az + oth);
+    dx.load(cf.dex + own);
     ld4(b + own, bv);
     auto body = [&](auto qc) {
         constexpr int QZ = decltype(qc)::value;
@@ -283,11 +314,16 @@ __device__ __forceinline__ void resid4_split(const Dims &d, const Coef<C> &cf, c
         body(std::integral_constant<int, 1>{});
 }
 
-// Restriction of the split level-0 residual to the (natural) level 1: thread (q4, J, I) sums the children of
-// coarse cells K0 = 4 q4 .. K0 + 3 in k_resid_restrict's order (x child, y child, then k = 2K, 2K + 1).
+// Restriction of the split level-0 residual to the (natural) level 1, right after the pre-smoothing, whose
+// last half sweep updates colour 1: a colour-1 cell's new value is (b + sum a x) / D of colour-0 values that
+// did not change afterwards, so its residual is zero up to the rounding of that update, and only colour-0
+// residuals are summed.  (The natural kernel evaluates all eight children; the difference is at rounding
+// level.)  Thread (q4, J, I) sums coarse cells K0 = 4 q4 .. K0 + 3 over their x and y children, in the order
+// of k_resid_restrict; in each fine row the colour-0 child of coarse cell K is the entry m = K.
 template <class C>
-__global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, const float *__restrict__ x,
-                                                          const float *__restrict__ b, Dims dc, float *__restrict__ bc) {
+__global__ void __launch_bounds__(256, 4) k_resid_restrict_s(Dims d, Coef<C> cf, const float *__restrict__ x,
+                                                             const float *__restrict__ b, Dims dc,
+                                                             float *__restrict__ bc) {
     const int K0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int I = blockIdx.z;
@@ -299,14 +335,10 @@ __global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, co
         for (int dj = 0; dj < 2; dj++) {
             const int j = 2 * J + dj;
             if (j >= d.ny) break;
-            float r0[4], r1[4];
-            resid4_split<C>(d, cf, x, b, (i + j) & 1, i, j, K0, r0);      // k = 2K
-            resid4_split<C>(d, cf, x, b, (i + j + 1) & 1, i, j, K0, r1);  // k = 2K + 1
+            float r[4];
+            resid4_split<C>(d, cf, x, b, 0, i, j, K0, r);
 #pragma unroll
-            for (int t = 0; t < 4; t++) {
-                acc[t] += r0[t];
-                acc[t] += r1[t];
-            }
+            for (int t = 0; t < 4; t++) acc[t] += r[t];
         }
     }
     *reinterpret_cast<float4 *>(bc + cid(dc, I, J, K0)) = make_float4(acc[0], acc[1], acc[2], acc[3]);

@@ -261,10 +261,11 @@ def test_fp16_smoothing_coefficients_same_answer(sfpkg, oracle, gpu_ctx, n, seed
 @pytest.mark.parametrize("shape", [(32, 32, 32), (20, 16, 40), (9, 13, 8), (37, 21, 70), (16, 16, 12)])
 def test_split_level_matches_natural(sfpkg, gpu_ctx, shape):
     """Smoother 3 against smoother 2 in the mixed form.  Where nz is a multiple of 8 the finest level is stored
-    colour by colour: every cell's smoothing, restriction and operator arithmetic is the natural kernels', but
-    the Krylov dot products sum in the permuted order, so the two solves take the same number of iterations
-    (+-1) and agree to the solve's accuracy (relative L2 1e-6 at tolerances 1e-9 / 1e-8).  Otherwise smoother 3
-    runs as smoother 2: bit for bit."""
+    colour by colour: every cell's smoothing and operator arithmetic is the natural kernels', the restriction
+    leaves out the colour whose residual the last pre-smoothing half sweep zeroed (to rounding), and the Krylov
+    dot products sum in the permuted order, so the two solves take the same number of iterations (+-1) and agree
+    to the solve's accuracy (relative L2 1e-6 at tolerances 1e-9 / 1e-8).  Otherwise smoother 3 runs as
+    smoother 2: bit for bit."""
     g = sfpkg.StaggeredGrid.from_origin(1.0 / shape[0], shape)
     rng = np.random.default_rng(sum(shape) + 7)
     ys = scenes().cell_centres(g, 1)
