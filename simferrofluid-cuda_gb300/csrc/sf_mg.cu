@@ -111,6 +111,14 @@ static inline dim3 grid_pairs(const Dims &d) {
     return dim3(((d.nz + 1) / 2 + 31) / 32, (d.ny + 8 * kRbRows - 1) / (8 * kRbRows), d.nx);
 }
 
+// Row activity: rows[(i * ny + j)] == 0 marks a row (i, j) of the level whose cells are all inactive (D = 0:
+// air in the pressure system).  Kernels given flags skip such rows entirely; every vector of the level is zero
+// there (cleared when the hierarchy is built, never written afterwards), which is what processing them would
+// produce.  nullptr: all rows active.
+__device__ __forceinline__ bool row_on(const uint8_t *rows, const Dims &d, int i, int j) {
+    return !rows || rows[(long long)i * d.ny + j];
+}
+
 // ------------------------------------------------------------------------------------------------ smoothers
 template <class C>
 __device__ __forceinline__ typename Acc<C>::T inv_diag(const Coef<C> &cf, long long c, typename Acc<C>::T suma) {
@@ -143,7 +151,7 @@ __device__ __forceinline__ T couplings_sum(const Dims &d, const Coef<C> &cf, int
 // beforehand and never carries stale values into the sweep.
 template <class T, class C, bool ZERO>
 __global__ void __launch_bounds__(256) k_rbgs(Dims d, Coef<C> cf, T *__restrict__ x, const T *__restrict__ b,
-                                              int color) {
+                                              int color, const uint8_t *__restrict__ rows = nullptr) {
     const int kp = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.z;
     const int j0 = blockIdx.y * (8 * kRbRows) + threadIdx.y;
@@ -154,7 +162,7 @@ __global__ void __launch_bounds__(256) k_rbgs(Dims d, Coef<C> cf, T *__restrict_
     for (int r = 0; r < kRbRows; r++) {
         const int j = j0 + 8 * r;
         const int k = 2 * kp + ((i + j + color) & 1);
-        act[r] = j < d.ny && k < d.nz;
+        act[r] = j < d.ny && k < d.nz && row_on(rows, d, i, j);
         cc[r] = 0;
         res[r] = T(0);
         if (!act[r]) continue;
@@ -173,7 +181,7 @@ __global__ void __launch_bounds__(256) k_rbgs(Dims d, Coef<C> cf, T *__restrict_
 #pragma unroll
     for (int r = 0; r < kRbRows; r++) {
         const int j = j0 + 8 * r;
-        if (ZERO && j < d.ny) {
+        if (ZERO && j < d.ny && row_on(rows, d, i, j)) {
             const int ko = 2 * kp + (((i + j + color) & 1) ^ 1);
             if (ko < d.nz) x[cid(d, i, j, ko)] = T(0);
         }
@@ -204,12 +212,12 @@ __device__ __forceinline__ void ld4(const __half *p, float (&v)[4]) {
 
 template <class C, bool ZERO>
 __global__ void __launch_bounds__(256) k_rbgs4(Dims d, Coef<C> cf, float *__restrict__ x, const float *__restrict__ b,
-                                               int color) {
+                                               int color, const uint8_t *__restrict__ rows = nullptr) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
     const int k0 = 4 * q;
-    if (j >= d.ny || k0 >= d.nz) return;
+    if (j >= d.ny || k0 >= d.nz || !row_on(rows, d, i, j)) return;
     const long long c0 = cid(d, i, j, k0);
     const long long sx = (long long)d.ny * d.nz, sy = d.nz;
     const bool xl = i > 0, xu = i < d.nx - 1, yl = j > 0, yu = j < d.ny - 1, zr_in = k0 + 4 < d.nz;
@@ -657,11 +665,13 @@ __global__ void __launch_bounds__(256) k_rbgs_pipe(Dims d, Coef<T> cf, const T *
 // r = b - A x on the fine level, summed over each coarse cell's (up to) 8 children -> coarse rhs.
 template <class T, class C>
 __global__ void __launch_bounds__(256) k_resid_restrict(Dims d, Coef<C> cf, const T *__restrict__ x,
-                                                        const T *__restrict__ b, Dims dc, T *__restrict__ bc) {
+                                                        const T *__restrict__ b, Dims dc, T *__restrict__ bc,
+                                                        const uint8_t *__restrict__ rows = nullptr,
+                                                        const uint8_t *__restrict__ rows_c = nullptr) {
     const int K = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int I = blockIdx.z;
-    if (K >= dc.nz || J >= dc.ny) return;
+    if (K >= dc.nz || J >= dc.ny || !row_on(rows_c, dc, I, J)) return;
     T acc = 0;
 #pragma unroll
     for (int di = 0; di < 2; di++) {
@@ -671,6 +681,7 @@ __global__ void __launch_bounds__(256) k_resid_restrict(Dims d, Coef<C> cf, cons
         for (int dj = 0; dj < 2; dj++) {
             const int j = 2 * J + dj;
             if (j >= d.ny) break;
+            if (!row_on(rows, d, i, j)) continue;  // residual zero
 #pragma unroll
             for (int dk = 0; dk < 2; dk++) {
                 const int k = 2 * K + dk;
@@ -688,11 +699,12 @@ __global__ void __launch_bounds__(256) k_resid_restrict(Dims d, Coef<C> cf, cons
 
 // x += P xc (piecewise constant).
 template <class T>
-__global__ void __launch_bounds__(256) k_prolong(Dims d, T *__restrict__ x, Dims dc, const T *__restrict__ xc) {
+__global__ void __launch_bounds__(256) k_prolong(Dims d, T *__restrict__ x, Dims dc, const T *__restrict__ xc,
+                                                 const uint8_t *__restrict__ rows = nullptr) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
-    if (k >= d.nz || j >= d.ny) return;
+    if (k >= d.nz || j >= d.ny || !row_on(rows, d, i, j)) return;
     x[cid(d, i, j, k)] += xc[cid(dc, i >> 1, j >> 1, k >> 1)];
 }
 
@@ -1069,9 +1081,14 @@ template <class TR>
 __global__ void __launch_bounds__(256) k_residual64(Dims d, int xpb, Coef<double> cf, const double *__restrict__ x,
                                                     const double *__restrict__ b, TR *__restrict__ r, int skip0,
                                                     int rr_slot, int bb_slot, double *sc, double *part,
-                                                    unsigned *ticket, int split = 0) {
+                                                    unsigned *ticket, int split = 0,
+                                                    const uint8_t *__restrict__ rows = nullptr) {
     double v[2] = {0, 0};
     TILE_LOOP(d, xpb)
+    if (!row_on(rows, d, i, j)) {  // residual zero
+        if (r) r[split ? split_index(d, i, j, k) : c] = (TR)0;
+        continue;
+    }
     double sa;
     double s = nbsum<double, double, false>(d, cf, x, i, j, k, c, sa);
     const double bc = b[c];
@@ -1163,7 +1180,7 @@ static inline int flat_grid(long long n) {
 // ------------------------------------------------------------------------------------------------ V-cycle
 template <class T, class C>
 static void rb(cudaStream_t st, Tracker &tk, bool fine, bool zero, const Dims &d, const Coef<C> &cf, T *x, const T *b,
-               int color) {
+               int color, const uint8_t *rows = nullptr) {
     const dim3 g = grid_pairs(d), bk = blk2();
     // algorithmic bytes of one colour: half of (x r/w + b + 3 couplings + diagonal term)
     const double per = (3.0 * sizeof(T) + 4.0 * sizeof(C)) / 2.0;
@@ -1172,17 +1189,17 @@ static void rb(cudaStream_t st, Tracker &tk, bool fine, bool zero, const Dims &d
         if (d.nz % 4 == 0) {  // rows start 16-byte aligned: z-vectorised kernel
             const dim3 g4((d.nz / 4 + 31) / 32, (d.ny + 7) / 8, d.nx);
             if (zero)
-                k_rbgs4<C, true><<<g4, bk, 0, st>>>(d, cf, x, b, color);
+                k_rbgs4<C, true><<<g4, bk, 0, st>>>(d, cf, x, b, color, rows);
             else
-                k_rbgs4<C, false><<<g4, bk, 0, st>>>(d, cf, x, b, color);
+                k_rbgs4<C, false><<<g4, bk, 0, st>>>(d, cf, x, b, color, rows);
             tk.after(st, fine, per * d.n);
             return;
         }
     }
     if (zero)
-        k_rbgs<T, C, true><<<g, bk, 0, st>>>(d, cf, x, b, color);
+        k_rbgs<T, C, true><<<g, bk, 0, st>>>(d, cf, x, b, color, rows);
     else
-        k_rbgs<T, C, false><<<g, bk, 0, st>>>(d, cf, x, b, color);
+        k_rbgs<T, C, false><<<g, bk, 0, st>>>(d, cf, x, b, color, rows);
     tk.after(st, fine, per * d.n);
 }
 
@@ -1292,28 +1309,28 @@ static void fused(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const 
 // Half sweep of the split level 0 (smoother 3); same algorithmic bytes as the natural half sweep.
 template <class C>
 static void rb_split(cudaStream_t st, Tracker &tk, bool zero, const Dims &d, const Coef<C> &cf, float *x,
-                     const float *b, int color) {
+                     const float *b, int color, const uint8_t *rows) {
     const dim3 g(((d.nz >> 1) / 4 + 31) / 32, (d.ny + 7) / 8, d.nx);
     tk.before(st, true);
     if (zero)
-        k_rbgs4s<C, true><<<g, blk2(), 0, st>>>(d, cf, x, b, color);
+        k_rbgs4s<C, true><<<g, blk2(), 0, st>>>(d, cf, x, b, color, rows);
     else
-        k_rbgs4s<C, false><<<g, blk2(), 0, st>>>(d, cf, x, b, color);
+        k_rbgs4s<C, false><<<g, blk2(), 0, st>>>(d, cf, x, b, color, rows);
     tk.after(st, true, (3.0 * sizeof(float) + 4.0 * sizeof(C)) / 2.0 * d.n);
 }
 
 template <class T, class C>
 static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const Coef<C> &cf, T *x, T *tmp,
-                   const T *b, int nu, bool pre, bool split = false) {
+                   const T *b, int nu, bool pre, bool split = false, const uint8_t *rows = nullptr) {
     if constexpr (std::is_same<T, float>::value && std::is_same<C, __half>::value) {  // split: FP16 copy only
         if (split) {
             for (int s = 0; s < nu; s++) {
                 if (pre) {
-                    rb_split<C>(st, tk, s == 0, d, cf, x, b, 0);
-                    rb_split<C>(st, tk, false, d, cf, x, b, 1);
+                    rb_split<C>(st, tk, s == 0, d, cf, x, b, 0, rows);
+                    rb_split<C>(st, tk, false, d, cf, x, b, 1, rows);
                 } else {
-                    rb_split<C>(st, tk, false, d, cf, x, b, 1);
-                    rb_split<C>(st, tk, false, d, cf, x, b, 0);
+                    rb_split<C>(st, tk, false, d, cf, x, b, 1, rows);
+                    rb_split<C>(st, tk, false, d, cf, x, b, 0, rows);
                 }
             }
             return;
@@ -1322,11 +1339,11 @@ static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const
     if (!tmp) {
         for (int s = 0; s < nu; s++) {
             if (pre) {
-                rb<T, C>(st, tk, fine, s == 0, d, cf, x, b, 0);
-                rb<T, C>(st, tk, fine, false, d, cf, x, b, 1);
+                rb<T, C>(st, tk, fine, s == 0, d, cf, x, b, 0, rows);
+                rb<T, C>(st, tk, fine, false, d, cf, x, b, 1, rows);
             } else {
-                rb<T, C>(st, tk, fine, false, d, cf, x, b, 1);
-                rb<T, C>(st, tk, fine, false, d, cf, x, b, 0);
+                rb<T, C>(st, tk, fine, false, d, cf, x, b, 1, rows);
+                rb<T, C>(st, tk, fine, false, d, cf, x, b, 0, rows);
             }
         }
         return;
@@ -1356,16 +1373,17 @@ static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const
 
 template <class T, class C>
 static void restrict_res(cudaStream_t st, Tracker &tk, const Dims &d, const Coef<C> &cf, const T *x, const T *b,
-                         const Dims &dc, T *bc, bool split = false) {
+                         const Dims &dc, T *bc, bool split = false, const uint8_t *rows = nullptr,
+                         const uint8_t *rows_c = nullptr) {
     tk.launches++;
     if constexpr (std::is_same<T, float>::value && std::is_same<C, __half>::value) {
         if (split) {
-            k_resid_restrict_s<C><<<dim3((dc.nz / 4 + 31) / 32, (dc.ny + 7) / 8, dc.nx), blk2(), 0, st>>>(d, cf, x, b,
-                                                                                                 dc, bc);
+            k_resid_restrict_s<C><<<dim3((dc.nz / 4 + 31) / 32, (dc.ny + 7) / 8, dc.nx), blk2(), 0, st>>>(
+                d, cf, x, b, dc, bc, rows, rows_c);
             return;
         }
     }
-    k_resid_restrict<T, C><<<grid_cells(dc), blk2(), 0, st>>>(d, cf, x, b, dc, bc);
+    k_resid_restrict<T, C><<<grid_cells(dc), blk2(), 0, st>>>(d, cf, x, b, dc, bc, rows, rows_c);
 }
 
 template <class T, class C>
@@ -1388,36 +1406,38 @@ template <class T, class C0, class Cc, class C0S>
 static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, const Coef<C0> &c0,
                    const Coef<C0S> &c0s, const std::vector<Coef<Cc>> &cc, T *z, const T *r,
                    const std::vector<T *> &xs, const std::vector<T *> &bs, const std::vector<T *> &ts,
-                   const SolverParams &p, bool split0 = false) {
+                   const SolverParams &p, bool split0 = false, const std::vector<uint8_t *> *rows = nullptr) {
     const int L = (int)dims.size();
     if (L == 1) {
         coarse_solve<T, C0>(st, tk, dims[0], c0, z, r, p.coarse_sweeps);
         return;
     }
-    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true, split0);
-    restrict_res<T, C0S>(st, tk, dims[0], c0s, z, r, dims[1], bs[1], split0);  // the residual of the smoothed operator
+    auto R = [&](int l) -> const uint8_t * { return rows ? (*rows)[l] : nullptr; };
+    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true, split0, R(0));
+    // the residual of the smoothed operator
+    restrict_res<T, C0S>(st, tk, dims[0], c0s, z, r, dims[1], bs[1], split0, R(0), R(1));
     for (int l = 1; l < L - 1; l++) {
-        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.pre, true);
-        restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1]);
+        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.pre, true, false, R(l));
+        restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1], false, R(l), R(l + 1));
     }
     coarse_solve<T, Cc>(st, tk, dims[L - 1], cc[L - 1], xs[L - 1], bs[L - 1], p.coarse_sweeps);
     for (int l = L - 2; l >= 1; l--) {
         tk.launches++;
-        k_prolong<T><<<grid_cells(dims[l]), blk2(), 0, st>>>(dims[l], xs[l], dims[l + 1], xs[l + 1]);
-        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.post, false);
+        k_prolong<T><<<grid_cells(dims[l]), blk2(), 0, st>>>(dims[l], xs[l], dims[l + 1], xs[l + 1], R(l));
+        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.post, false, false, R(l));
     }
     tk.launches++;
     if constexpr (std::is_same<T, float>::value) {
         if (split0) {
             const Dims &d0 = dims[0];
             k_prolong_s<<<dim3(((d0.nz >> 1) / 4 + 31) / 32, (d0.ny + 7) / 8, d0.nx), blk2(), 0, st>>>(d0, z, dims[1],
-                                                                                                    xs[1]);
-            smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true);
+                                                                                                    xs[1], R(0));
+            smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true, R(0));
             return;
         }
     }
-    k_prolong<T><<<grid_cells(dims[0]), blk2(), 0, st>>>(dims[0], z, dims[1], xs[1]);
-    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false);
+    k_prolong<T><<<grid_cells(dims[0]), blk2(), 0, st>>>(dims[0], z, dims[1], xs[1], R(0));
+    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, false, R(0));
 }
 
 // ------------------------------------------------------------------------------------------------ MGSolver
@@ -1555,6 +1575,8 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
             x32_[l] = (float *)chk(A(4 * m));
             b32_[l] = (float *)chk(A(4 * m));
         }
+        rows_.assign(split0 ? L : 0, nullptr);
+        for (int l = 0; l < (int)rows_.size(); l++) rows_[l] = (uint8_t *)chk(A((size_t)dims[l].nx * dims[l].ny));
         r32_ = (float *)chk(A(4 * n));
         d32_ = (float *)chk(A(4 * n));
         z32_ = (float *)chk(A(4 * n));
@@ -1591,7 +1613,20 @@ cudaError_t MGSolver::build_hierarchy() {
                                                                                     lev_dims_[l], c64_[l]);
     } else {
         if (split0_) {
-            k_to_split<<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(lev_dims_[0], c64_[0], c32_, c16s0_);
+            k_to_split<<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(lev_dims_[0], c64_[0], c32_, c16s0_,
+                                                                                rows_[0]);
+            // rows that hold no active cell are skipped by every level-l kernel; their vector entries must be
+            // zero, and stay so
+            cudaMemsetAsync(z32_, 0, 4 * (size_t)lev_dims_[0].n, st_);
+            for (int l = 1; l < L; l++) {
+                const Dims &dl = lev_dims_[l];
+                const long long nr = (long long)dl.nx * dl.ny;
+                k_rows_coarsen<<<(int)std::min<long long>((nr + 255) / 256, 152 * 8), 256, 0, st_>>>(
+                    lev_dims_[l - 1], rows_[l - 1], dl, rows_[l]);
+                cudaMemsetAsync(x32_[l], 0, 4 * (size_t)dl.n, st_);
+                cudaMemsetAsync(b32_[l], 0, 4 * (size_t)dl.n, st_);
+            }
+            tk_.launches += L - 1;
         } else {
             k_to32<<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0].n, c64_[0], c32_);
             if (prm_.smoother == 2 || prm_.smoother == 3) {
@@ -1633,18 +1668,30 @@ void MGSolver::enqueue_iter32() {
     const long long n = d.n;
     const long long l0 = tk_.launches;
     const std::vector<float *> ts = prm_.smoother == 1 ? t32_ : std::vector<float *>(t32_.size(), nullptr);
+    if (split0_) {
+        // colour-split level 0 with row flags on every level (vectors in split rows, inactive rows skipped)
+        const uint8_t *r0 = rows_[0];
+        vcycle<float, float, __half, __half>(st_, tk_, lev_dims_, c32_, c16s0_, c16_, z32_, ri32_, x32_, b32_, ts,
+                                             prm_, true, &rows_);
+        const int vg = (int)std::min<long long>((2LL * d.nx * d.ny + 7) / 8, 152 * 16);
+        k_dot_rz_s<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(d, ri32_, z32_, q32_, r0, 1, sc_, part_, ticket_);
+        k_xpby_s<<<vg, dim3(32, 8), 0, st_>>>(d, z32_, p32_, r0, sc_);
+        apply_dot32s(st_, d, c32_, p32_, q32_, r0, sc_, part_, ticket_);
+        k_update_s<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(d, d32_, ri32_, p32_, q32_, r0, sc_, part_, ticket_);
+        tk_.launches += 4;
+        iter_launches32_ = tk_.launches - l0;
+        cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
+        return;
+    }
     if (prm_.smoother == 2 || prm_.smoother == 3)
         vcycle<float, float, __half, __half>(st_, tk_, lev_dims_, c32_, c16s0_, c16_, z32_, ri32_, x32_, b32_, ts,
-                                             prm_, split0_);
+                                             prm_);
     else
         vcycle<float, float, __half, float>(st_, tk_, lev_dims_, c32_, c32_, c16_, z32_, ri32_, x32_, b32_, ts,
                                             prm_);
     k_dot_rz<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, ri32_, z32_, q32_, 1, sc_, part_, ticket_);
     k_xpby<float><<<flat_grid(n), 256, 0, st_>>>(n, z32_, p32_, sc_);
-    if (split0_)
-        apply_dot32s(st_, d, c32_, p32_, q32_, sc_, part_, ticket_);
-    else
-        apply_dot32(st_, d, c32_, p32_, q32_, sc_, part_, ticket_);
+    apply_dot32(st_, d, c32_, p32_, q32_, sc_, part_, ticket_);
     k_update<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, d32_, ri32_, p32_, q32_, sc_, part_, ticket_);
     tk_.launches += 4;
     iter_launches32_ = tk_.launches - l0;
@@ -1797,7 +1844,8 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
             x_zero = false;
         } else {
             k_residual64<float><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c64_[0], x_, b_, r32_, 0, S_AUX1,
-                                                             bb < 0 ? S_BB : -1, sc_, part_, ticket_, split0_ ? 1 : 0);
+                                                             bb < 0 ? S_BB : -1, sc_, part_, ticket_, split0_ ? 1 : 0,
+                                                             split0_ ? rows_[0] : nullptr);
         }
         tk_.launches++;
         if ((e = read_slots()) != cudaSuccess) return e;
@@ -1858,7 +1906,7 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
         }
         total_inner += it;
         if (split0_)
-            k_ir_update_s<<<split_rows_grid(d), dim3(32, 8), 0, st_>>>(d, x_, d32_);
+            k_ir_update_s<<<split_rows_grid(d), dim3(32, 8), 0, st_>>>(d, x_, d32_, rows_[0]);
         else
             k_ir_update<<<flat_grid(n), 256, 0, st_>>>(n, x_, d32_);
         tk_.launches++;
@@ -1889,8 +1937,9 @@ cudaError_t MGSolver::set_guess_scaled(const float *y, double &gamma) {
     const Dims &d = lev_dims_[0];
     // (y, A y) on the FP32 level-0 operator and (y, b); gamma minimises the A-norm error along y
     if (split0_) {
-        k_vec_to_split<<<split_rows_grid(d), dim3(32, 8), 0, st_>>>(d, y, z32_);
-        apply_dot32s(st_, d, c32_, z32_, q32_, sc_, part_, ticket_);
+        // scratch: q32 and p32, cleared before the solve's first inner iteration
+        k_vec_to_split<<<split_rows_grid(d), dim3(32, 8), 0, st_>>>(d, y, q32_);
+        apply_dot32s(st_, d, c32_, q32_, p32_, rows_[0], sc_, part_, ticket_);
         tk_.launches++;
     } else {
         apply_dot32(st_, d, c32_, y, q32_, sc_, part_, ticket_);
@@ -1914,7 +1963,8 @@ cudaError_t MGSolver::true_relres(bool skip0, double &relres, double &bnorm) {
     int xpb;
     const dim3 tg = tile_grid(d, xpb, kStencilBlocks);
     k_residual64<double><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c64_[0], x_, b_, (double *)nullptr, skip0 ? 1 : 0,
-                                                      S_AUX1, S_AUX2, sc_, part_, ticket_);
+                                                      S_AUX1, S_AUX2, sc_, part_, ticket_, 0,
+                                                      split0_ ? rows_[0] : nullptr);
     tk_.launches++;
     cudaError_t e = read_slots();
     if (e != cudaSuccess) return e;

@@ -140,6 +140,8 @@ class MGSolver {
     // smoother 3 in effect: level 0's FP32 vectors and both of its operator copies are stored colour by colour
     // (sf_split.cuh); the FP64 operator and vectors keep the natural layout
     bool split0_ = false, cfg_split_ = false;
+    // with split0_: per level, one byte per row (i, j), 0 when every cell of the row is inactive (D = 0)
+    std::vector<uint8_t *> rows_;
     std::vector<float *> x32_, b32_, t32_;
 
     double *x_ = nullptr, *b_ = nullptr;

@@ -47,21 +47,53 @@ static inline int split_rows_grid(const Dims &d) {
 }
 
 // FP64 level 0 -> split FP32 copy (Krylov operator) and FP16 copy (smoother) in one pass, with the roundings
-// of k_to32 / k_to16.
-__global__ void __launch_bounds__(256) k_to_split(Dims d, Coef<double> f, Coef<float> o32, Coef<__half> o16) {
-    SPLIT_ROWS(d)
-    const double *src[4] = {f.ax, f.ay, f.az, f.dex};
-    float *d32[4] = {o32.ax, o32.ay, o32.az, o32.dex};
-    __half *d16[4] = {o16.ax, o16.ay, o16.az, o16.dex};
+// of k_to32 / k_to16, and the level's row flags (a row is active when one of its cells has D > 0).  One warp
+// per row: blockDim = (32, 8).
+__global__ void __launch_bounds__(256) k_to_split(Dims d, Coef<double> f, Coef<float> o32, Coef<__half> o16,
+                                                  uint8_t *__restrict__ rows) {
+    const int nh = d.nz >> 1;
+    const long long hn = d.n >> 1, nrows = (long long)d.nx * d.ny;
+    for (long long row = blockIdx.x * (long long)blockDim.y + threadIdx.y; row < nrows;
+         row += (long long)gridDim.x * blockDim.y) {
+        const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
+        const int p = (i + j) & 1;
+        const long long nat = row * d.nz, sp = row * nh;
+        bool act = false;
+        for (int m = threadIdx.x; m < nh; m += blockDim.x) {
+            const long long n0 = nat + 2 * m + p, n1 = nat + 2 * m + 1 - p, s0 = sp + m, s1 = hn + sp + m;
+            const double *src[4] = {f.ax, f.ay, f.az, f.dex};
+            float *d32[4] = {o32.ax, o32.ay, o32.az, o32.dex};
+            __half *d16[4] = {o16.ax, o16.ay, o16.az, o16.dex};
 #pragma unroll
-    for (int a = 0; a < 4; a++) {
-        const float v0 = (float)src[a][n0], v1 = (float)src[a][n1];
-        d32[a][s0] = v0;
-        d32[a][s1] = v1;
-        d16[a][s0] = __float2half_rn(v0);
-        d16[a][s1] = __float2half_rn(v1);
+            for (int a = 0; a < 4; a++) {
+                const float v0 = (float)src[a][n0], v1 = (float)src[a][n1];
+                d32[a][s0] = v0;
+                d32[a][s1] = v1;
+                d16[a][s0] = __float2half_rn(v0);
+                d16[a][s1] = __float2half_rn(v1);
+            }
+            act |= (f.D[n0] > 0.0) | (f.D[n1] > 0.0);
+        }
+        act = __any_sync(0xffffffffu, act);
+        if (threadIdx.x == 0) rows[row] = act ? 1 : 0;
     }
-    SPLIT_ROWS_END
+}
+
+// Row flags of a coarse level from the next finer one: coarse row (I, J) is active when one of the fine rows
+// (2I + di, 2J + dj) is (a coarse cell whose children are all inactive has an all-zero operator row).
+__global__ void k_rows_coarsen(Dims df, const uint8_t *__restrict__ rf, Dims dc, uint8_t *__restrict__ rc) {
+    const long long nrows = (long long)dc.nx * dc.ny;
+    for (long long row = blockIdx.x * (long long)blockDim.x + threadIdx.x; row < nrows;
+         row += (long long)gridDim.x * blockDim.x) {
+        const int I = (int)(row / dc.ny), J = (int)(row - (long long)I * dc.ny);
+        uint8_t a = 0;
+        for (int di = 0; di < 2; di++)
+            for (int dj = 0; dj < 2; dj++) {
+                const int i = 2 * I + di, j = 2 * J + dj;
+                if (i < df.nx && j < df.ny) a |= rf[(long long)i * df.ny + j];
+            }
+        rc[row] = a;
+    }
 }
 
 // Natural FP32 vector -> split copy.
@@ -91,12 +123,97 @@ __global__ void __launch_bounds__(256) k_cast_rhs_s(Dims d, const double *__rest
     }
 }
 
-// x64 += d32 with d32 in the split layout.
-__global__ void __launch_bounds__(256) k_ir_update_s(Dims d, double *__restrict__ x, const float *__restrict__ dlt) {
+// x64 += d32 with d32 in the split layout (zero in inactive rows, which are skipped).
+__global__ void __launch_bounds__(256) k_ir_update_s(Dims d, double *__restrict__ x, const float *__restrict__ dlt,
+                                                     const uint8_t *__restrict__ rows) {
     SPLIT_ROWS(d)
+    if (rows && !rows[row]) break;
     x[n0] += (double)dlt[s0];
     x[n1] += (double)dlt[s1];
     SPLIT_ROWS_END
+}
+
+// Krylov vector kernels of the split level, one warp per row of one colour (float4 along the row), inactive
+// rows skipped: (r, z) and (z, q) with the beta of k_dot_rz; p = z + beta p; x += alpha p, r -= alpha q, (r, r).
+#define SPLIT_VEC_ROWS(d, rows)                                                                                \
+    const int nq_ = (d).nz >> 3; /* float4 per row of a colour */                                              \
+    const long long nrows_ = (long long)(d).nx * (d).ny;                                                         \
+    for (long long rr = blockIdx.x * (long long)blockDim.y + threadIdx.y; rr < 2 * nrows_;                     \
+         rr += (long long)gridDim.x * blockDim.y) {                                                             \
+        if ((rows) && !(rows)[rr < nrows_ ? rr : rr - nrows_]) continue;                                        \
+        for (int t = threadIdx.x; t < nq_; t += blockDim.x) {                                                   \
+            const long long v4 = rr * nq_ + t;
+
+__global__ void __launch_bounds__(256) k_dot_rz_s(Dims d, const float *__restrict__ r, const float *__restrict__ z,
+                                                  const float *__restrict__ q, const uint8_t *__restrict__ rows,
+                                                  int flexible, double *sc, double *part, unsigned *ticket) {
+    float a0 = 0.f, a1 = 0.f;
+    SPLIT_VEC_ROWS(d, rows)
+    const float4 rv = reinterpret_cast<const float4 *>(r)[v4], zv = reinterpret_cast<const float4 *>(z)[v4],
+                 qv = reinterpret_cast<const float4 *>(q)[v4];
+    a0 += rv.x * zv.x;
+    a0 += rv.y * zv.y;
+    a0 += rv.z * zv.z;
+    a0 += rv.w * zv.w;
+    a1 += zv.x * qv.x;
+    a1 += zv.y * qv.y;
+    a1 += zv.z * qv.z;
+    a1 += zv.w * qv.w;
+    SPLIT_ROWS_END
+    double v[2] = {(double)a0, (double)a1};
+    double tot[2];
+    if (grid_reduce<2>(v, part, ticket, tot)) {
+        const double rho = sc[S_RHO];
+        double beta = flexible ? (-sc[S_ALPHA] * tot[1] / rho) : (tot[0] / rho);
+        if (!isfinite(beta)) beta = 0;
+        sc[S_RHONEW] = tot[0];
+        sc[S_ZQ] = tot[1];
+        sc[S_BETA] = beta;
+        sc[S_RHO] = tot[0];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_xpby_s(Dims d, const float *__restrict__ z, float *__restrict__ p,
+                                                const uint8_t *__restrict__ rows, const double *sc) {
+    const float beta = (float)sc[S_BETA];
+    SPLIT_VEC_ROWS(d, rows)
+    const float4 zv = reinterpret_cast<const float4 *>(z)[v4];
+    float4 pv = reinterpret_cast<float4 *>(p)[v4];
+    pv.x = zv.x + beta * pv.x;
+    pv.y = zv.y + beta * pv.y;
+    pv.z = zv.z + beta * pv.z;
+    pv.w = zv.w + beta * pv.w;
+    reinterpret_cast<float4 *>(p)[v4] = pv;
+    SPLIT_ROWS_END
+}
+
+__global__ void __launch_bounds__(256) k_update_s(Dims d, float *__restrict__ x, float *__restrict__ r,
+                                                  const float *__restrict__ p, const float *__restrict__ q,
+                                                  const uint8_t *__restrict__ rows, double *sc, double *part,
+                                                  unsigned *ticket) {
+    const float alpha = (float)sc[S_ALPHA];
+    float acc = 0.f;
+    SPLIT_VEC_ROWS(d, rows)
+    float4 xv = reinterpret_cast<float4 *>(x)[v4], rv = reinterpret_cast<float4 *>(r)[v4];
+    const float4 pv = reinterpret_cast<const float4 *>(p)[v4], qv = reinterpret_cast<const float4 *>(q)[v4];
+    xv.x += alpha * pv.x;
+    xv.y += alpha * pv.y;
+    xv.z += alpha * pv.z;
+    xv.w += alpha * pv.w;
+    rv.x = rv.x - alpha * qv.x;
+    rv.y = rv.y - alpha * qv.y;
+    rv.z = rv.z - alpha * qv.z;
+    rv.w = rv.w - alpha * qv.w;
+    reinterpret_cast<float4 *>(x)[v4] = xv;
+    reinterpret_cast<float4 *>(r)[v4] = rv;
+    acc += rv.x * rv.x;
+    acc += rv.y * rv.y;
+    acc += rv.z * rv.z;
+    acc += rv.w * rv.w;
+    SPLIT_ROWS_END
+    double v[1] = {(double)acc};
+    double tot[1];
+    if (grid_reduce<1>(v, part, ticket, tot)) sc[S_RR] = tot[0];
 }
 
 // Four consecutive operator entries held as loaded: FP32 as four floats, FP16 packed two to a register and
@@ -128,12 +245,12 @@ struct Cv4<__half> {
 // over a warp (one j) and selects where the z neighbours sit.
 template <class C, bool ZERO>
 __global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__restrict__ x, const float *__restrict__ b,
-                                                int col) {
+                                                int col, const uint8_t *__restrict__ rows) {
     const int nh = d.nz >> 1;
     const int m0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
-    if (j >= d.ny || m0 >= nh) return;
+    if (j >= d.ny || m0 >= nh || !row_on(rows, d, i, j)) return;
     const long long row = ((long long)i * d.ny + j) * nh + m0;
     const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
     const long long sx = (long long)d.ny * nh, sy = nh;
@@ -323,11 +440,12 @@ __device__ __forceinline__ void resid4_split(const Dims &d, const Coef<C> &cf, c
 template <class C>
 __global__ void __launch_bounds__(256, 4) k_resid_restrict_s(Dims d, Coef<C> cf, const float *__restrict__ x,
                                                              const float *__restrict__ b, Dims dc,
-                                                             float *__restrict__ bc) {
+                                                             float *__restrict__ bc, const uint8_t *__restrict__ rows,
+                                                             const uint8_t *__restrict__ rows_c) {
     const int K0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int I = blockIdx.z;
-    if (K0 >= dc.nz || J >= dc.ny) return;
+    if (K0 >= dc.nz || J >= dc.ny || !row_on(rows_c, dc, I, J)) return;
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     for (int di = 0; di < 2; di++) {
         const int i = 2 * I + di;
@@ -335,6 +453,7 @@ __global__ void __launch_bounds__(256, 4) k_resid_restrict_s(Dims d, Coef<C> cf,
         for (int dj = 0; dj < 2; dj++) {
             const int j = 2 * J + dj;
             if (j >= d.ny) break;
+            if (!row_on(rows, d, i, j)) continue;  // residual zero
             float r[4];
             resid4_split<C>(d, cf, x, b, 0, i, j, K0, r);
 #pragma unroll
@@ -346,12 +465,13 @@ __global__ void __launch_bounds__(256, 4) k_resid_restrict_s(Dims d, Coef<C> cf,
 
 // x += P xc on the split level 0 (piecewise constant): both colours' entries m of row (i, j) take coarse cell
 // (i/2, j/2, m).
-__global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x, Dims dc, const float *__restrict__ xc) {
+__global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x, Dims dc, const float *__restrict__ xc,
+                                                   const uint8_t *__restrict__ rows) {
     const int nh = d.nz >> 1;
     const int m0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
-    if (j >= d.ny || m0 >= nh) return;
+    if (j >= d.ny || m0 >= nh || !row_on(rows, d, i, j)) return;
     float v[4];
     ld4(xc + cid(dc, i >> 1, j >> 1, m0), v);
     const long long row = ((long long)i * d.ny + j) * nh + m0;
@@ -370,7 +490,8 @@ __global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x
 // q = A p and (p, q) on the split FP32 level-0 operator (the counterpart of k_apply_dot4; each cell's q as in
 // k_apply_dot).  Block rows alternate colours: blockIdx.y = 2 * (y tile) + colour.
 __global__ void __launch_bounds__(256) k_apply_dot4s(Dims d, int xpb, Coef<float> cf, const float *__restrict__ p,
-                                                     float *__restrict__ q, double *sc, double *part, unsigned *ticket) {
+                                                     float *__restrict__ q, const uint8_t *__restrict__ rows,
+                                                     double *sc, double *part, unsigned *ticket) {
     float acc = 0.f;
     const int nh = d.nz >> 1;
     const int col = blockIdx.y & 1;
@@ -380,6 +501,7 @@ __global__ void __launch_bounds__(256) k_apply_dot4s(Dims d, int xpb, Coef<float
         const bool yl = j > 0, yu = j < d.ny - 1;
         const int i_end = min(d.nx, (int)(blockIdx.z + 1) * xpb);
         for (int i = blockIdx.z * xpb; i < i_end; i++) {
+            if (!row_on(rows, d, i, j)) continue;  // q stays zero
             const long long row = ((long long)i * d.ny + j) * nh + m0;
             const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
             const bool xl = i > 0, xu = i < d.nx - 1;
@@ -464,13 +586,13 @@ __global__ void __launch_bounds__(256) k_apply_dot4s(Dims d, int xpb, Coef<float
     }
 }
 
-static void apply_dot32s(cudaStream_t st, const Dims &d, const Coef<float> &cf, const float *p, float *q, double *sc,
-                         double *part, unsigned *ticket) {
+static void apply_dot32s(cudaStream_t st, const Dims &d, const Coef<float> &cf, const float *p, float *q,
+                         const uint8_t *rows, double *sc, double *part, unsigned *ticket) {
     const int nh = d.nz >> 1;
     const long long tiles = (long long)((nh + 127) / 128) * 2 * ((d.ny + 7) / 8);
     const long long zmax = tiles < kApplyBlocks ? kApplyBlocks / tiles : 1;
     int xpb = (int)((d.nx + zmax - 1) / zmax);
     if (xpb < 2) xpb = 2;
     const dim3 g((nh + 127) / 128, 2 * ((d.ny + 7) / 8), (d.nx + xpb - 1) / xpb);
-    k_apply_dot4s<<<g, dim3(32, 8), 0, st>>>(d, xpb, cf, p, q, sc, part, ticket);
+    k_apply_dot4s<<<g, dim3(32, 8), 0, st>>>(d, xpb, cf, p, q, rows, sc, part, ticket);
 }
