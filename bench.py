@@ -282,9 +282,14 @@ def run_ours(args, ws, rank, local):
     else:
         kname = "k_rbgs (one colour of a red-black sweep per launch)"
         prof = "k_rbgs_f32_finest_pool_sphere_256.md" if args.precision == "mixed" else None
+    traffic = profiled_traffic(prof, args.n)
+    if traffic is not None and smoother == 3 and args.precision == "mixed" and args.n % 8 == 0:
+        # the capture is of a launch over every row; launches skip rows without an active cell, so the
+        # per-launch traffic is scaled by the processed share, as the algorithmic bytes are
+        traffic = round(traffic * (bytes_tot / max(n_launch, 1)) / (10.0 * args.n ** 3))
     roofline = {"bound": "hbm", "kernel": kname + ", finest level",
                 "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": profiled_traffic(prof, args.n),
+                "frac": round(achieved / peak, 4), "traffic": traffic,
                 "bytes_per_launch": bytes_tot / max(n_launch, 1), "ms_per_launch": ms_tot / max(n_launch, 1),
                 "launches_timed": n_launch}
 

@@ -1310,13 +1310,15 @@ static void fused(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const 
 template <class C>
 static void rb_split(cudaStream_t st, Tracker &tk, bool zero, const Dims &d, const Coef<C> &cf, float *x,
                      const float *b, int color, const uint8_t *rows) {
-    const dim3 g(((d.nz >> 1) / 4 + 31) / 32, (d.ny + 7) / 8, d.nx);
+    const long long items = split_items((long long)d.nx * d.ny, d.nz >> 3);
     tk.before(st, true);
     if (zero)
-        k_rbgs4s<C, true><<<g, blk2(), 0, st>>>(d, cf, x, b, color, rows);
+        k_rbgs4s<C, true><<<row_grid((const void *)k_rbgs4s<C, true>, items), blk2(), 0, st>>>(d, cf, x, b, color,
+                                                                                             rows);
     else
-        k_rbgs4s<C, false><<<g, blk2(), 0, st>>>(d, cf, x, b, color, rows);
-    tk.after(st, true, (3.0 * sizeof(float) + 4.0 * sizeof(C)) / 2.0 * d.n);
+        k_rbgs4s<C, false><<<row_grid((const void *)k_rbgs4s<C, false>, items), blk2(), 0, st>>>(d, cf, x, b, color,
+                                                                                               rows);
+    tk.after(st, true, (3.0 * sizeof(float) + 4.0 * sizeof(C)) / 2.0 * d.n * tk.frac0);
 }
 
 template <class T, class C>
@@ -1378,8 +1380,8 @@ static void restrict_res(cudaStream_t st, Tracker &tk, const Dims &d, const Coef
     tk.launches++;
     if constexpr (std::is_same<T, float>::value && std::is_same<C, __half>::value) {
         if (split) {
-            k_resid_restrict_s<C><<<dim3((dc.nz / 4 + 31) / 32, (dc.ny + 7) / 8, dc.nx), blk2(), 0, st>>>(
-                d, cf, x, b, dc, bc, rows, rows_c);
+            const int g = row_grid((const void *)k_resid_restrict_s<C>, split_items((long long)dc.nx * dc.ny, dc.nz >> 2));
+            k_resid_restrict_s<C><<<g, blk2(), 0, st>>>(d, cf, x, b, dc, bc, rows, rows_c);
             return;
         }
     }
@@ -1430,8 +1432,8 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
     if constexpr (std::is_same<T, float>::value) {
         if (split0) {
             const Dims &d0 = dims[0];
-            k_prolong_s<<<dim3(((d0.nz >> 1) / 4 + 31) / 32, (d0.ny + 7) / 8, d0.nx), blk2(), 0, st>>>(d0, z, dims[1],
-                                                                                                    xs[1], R(0));
+            const int g = row_grid((const void *)k_prolong_s, split_items((long long)d0.nx * d0.ny, d0.nz >> 3));
+            k_prolong_s<<<g, blk2(), 0, st>>>(d0, z, dims[1], xs[1], R(0));
             smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true, R(0));
             return;
         }
@@ -1601,6 +1603,13 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     cfg_cdim_ = cdim;
     cfg_smoother_ = p.smoother;
     cfg_split_ = split0_ = split0;
+    if (split0) {  // occupancy lookups of the persistent split kernels, here rather than inside a graph capture
+        const void *ks[] = {(const void *)k_rbgs4s<__half, true>, (const void *)k_rbgs4s<__half, false>,
+                            (const void *)k_resid_restrict_s<__half>, (const void *)k_prolong_s,
+                            (const void *)k_apply_dot4s, (const void *)k_dot_rz_s, (const void *)k_xpby_s,
+                            (const void *)k_update_s, (const void *)k_ir_update_s};
+        for (const void *k : ks) resident_grid(k);
+    }
     return cudaGetLastError();
 }
 
@@ -1627,6 +1636,17 @@ cudaError_t MGSolver::build_hierarchy() {
                 cudaMemsetAsync(b32_[l], 0, 4 * (size_t)dl.n, st_);
             }
             tk_.launches += L - 1;
+            tk_.frac0 = 1.0;
+            if (prm_.profile) {  // profiled runs synchronise anyway: count the active level-0 rows
+                const Dims &d0 = lev_dims_[0];
+                std::vector<uint8_t> h((size_t)d0.nx * d0.ny);
+                cudaMemcpyAsync(h.data(), rows_[0], h.size(), cudaMemcpyDeviceToHost, st_);
+                const cudaError_t e = cudaStreamSynchronize(st_);
+                if (e != cudaSuccess) return e;
+                long long on = 0;
+                for (uint8_t v : h) on += v ? 1 : 0;
+                tk_.frac0 = h.empty() ? 1.0 : (double)on / (double)h.size();
+            }
         } else {
             k_to32<<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0].n, c64_[0], c32_);
             if (prm_.smoother == 2 || prm_.smoother == 3) {
@@ -1673,11 +1693,13 @@ void MGSolver::enqueue_iter32() {
         const uint8_t *r0 = rows_[0];
         vcycle<float, float, __half, __half>(st_, tk_, lev_dims_, c32_, c16s0_, c16_, z32_, ri32_, x32_, b32_, ts,
                                              prm_, true, &rows_);
-        const int vg = (int)std::min<long long>((2LL * d.nx * d.ny + 7) / 8, 152 * 16);
-        k_dot_rz_s<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(d, ri32_, z32_, q32_, r0, 1, sc_, part_, ticket_);
-        k_xpby_s<<<vg, dim3(32, 8), 0, st_>>>(d, z32_, p32_, r0, sc_);
+        const long long vitems = split_items(2LL * d.nx * d.ny, d.nz >> 3);
+        k_dot_rz_s<<<row_grid((const void *)k_dot_rz_s, vitems), dim3(32, 8), 0, st_>>>(d, ri32_, z32_, q32_, r0, 1,
+                                                                                       sc_, part_, ticket_);
+        k_xpby_s<<<row_grid((const void *)k_xpby_s, vitems), dim3(32, 8), 0, st_>>>(d, z32_, p32_, r0, sc_);
         apply_dot32s(st_, d, c32_, p32_, q32_, r0, sc_, part_, ticket_);
-        k_update_s<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(d, d32_, ri32_, p32_, q32_, r0, sc_, part_, ticket_);
+        k_update_s<<<row_grid((const void *)k_update_s, vitems), dim3(32, 8), 0, st_>>>(d, d32_, ri32_, p32_, q32_, r0,
+                                                                                      sc_, part_, ticket_);
         tk_.launches += 4;
         iter_launches32_ = tk_.launches - l0;
         cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
@@ -1906,7 +1928,8 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
         }
         total_inner += it;
         if (split0_)
-            k_ir_update_s<<<split_rows_grid(d), dim3(32, 8), 0, st_>>>(d, x_, d32_, rows_[0]);
+            k_ir_update_s<<<row_grid((const void *)k_ir_update_s, (long long)d.nx * d.ny * (((d.nz >> 1) + 31) / 32)),
+                            dim3(32, 8), 0, st_>>>(d, x_, d32_, rows_[0]);
         else
             k_ir_update<<<flat_grid(n), 256, 0, st_>>>(n, x_, d32_);
         tk_.launches++;

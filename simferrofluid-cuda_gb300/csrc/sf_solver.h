@@ -37,6 +37,9 @@ struct Tracker {
     std::vector<cudaEvent_t> ev;
     size_t used = 0;
     double bytes = 0;
+    // profile: fraction of level-0 rows holding an active cell (split level with row flags: a half sweep
+    // processes only those rows, and its algorithmic bytes are counted for them)
+    double frac0 = 1.0;
     void before(cudaStream_t st, bool fine);
     void after(cudaStream_t st, bool fine, double algo_bytes);
     // after a stream sync: summed milliseconds, launch count and algorithmic bytes of the bracketed

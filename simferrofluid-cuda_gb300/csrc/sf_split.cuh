@@ -46,6 +46,57 @@ static inline int split_rows_grid(const Dims &d) {
     return (int)(g < 1 ? 1 : g);
 }
 
+// Persistent loop of a grid's warps (blockDim = (32, 8)) over the items (r, chunk) of `nr` rows, `nch` chunks of
+// 32 lanes per row, in row order: warp w takes items w, w + W, ...  Rows whose flag rows[r mod period] is 0 are
+// skipped; the next item's flag is loaded before the current item's work, so a skipped row costs no load
+// latency of its own.  The assignment depends only on the grid and the sizes: reductions stay deterministic.
+template <class F>
+__device__ __forceinline__ void for_row_items(long long nr, int nch, const uint8_t *__restrict__ rows,
+                                              long long period, F &&f) {
+    const long long stride = (long long)gridDim.x * blockDim.y, nit = nr * nch;
+    auto flag = [&](long long it) {
+        if (it >= nit) return false;
+        if (!rows) return true;
+        long long r = it / nch;
+        if (r >= period) r -= period;
+        return rows[r] != 0;
+    };
+    long long it = blockIdx.x * (long long)blockDim.y + threadIdx.y;
+    bool on = flag(it);
+    for (; it < nit; it += stride) {
+        const bool on_next = flag(it + stride);
+        if (on) {
+            const long long r = it / nch;
+            f(r, (int)(it - r * nch));
+        }
+        on = on_next;
+    }
+}
+
+// Grid of a persistent row kernel: the blocks that fit on the device at once (its occupancy), at most one warp
+// per item.  Occupancies are looked up once per device and kernel.
+static int resident_grid(const void *kernel) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, int> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    const auto key = std::make_pair(dev, kernel);
+    const auto f = cache.find(key);
+    if (f != cache.end()) return f->second;
+    int nb = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, 256, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int g = (nb > 0 ? nb : 1) * (sms > 0 ? sms : 1);
+    cache[key] = g;
+    return g;
+}
+static int row_grid(const void *kernel, long long items) {
+    const long long need = (items + 7) / 8;
+    const long long g = resident_grid(kernel);
+    return (int)(need < 1 ? 1 : (need < g ? need : g));
+}
+
 // FP64 level 0 -> split FP32 copy (Krylov operator) and FP16 copy (smoother) in one pass, with the roundings
 // of k_to32 / k_to16, and the level's row flags (a row is active when one of its cells has D > 0).  One warp
 // per row: blockDim = (32, 8).
@@ -126,40 +177,48 @@ __global__ void __launch_bounds__(256) k_cast_rhs_s(Dims d, const double *__rest
 // x64 += d32 with d32 in the split layout (zero in inactive rows, which are skipped).
 __global__ void __launch_bounds__(256) k_ir_update_s(Dims d, double *__restrict__ x, const float *__restrict__ dlt,
                                                      const uint8_t *__restrict__ rows) {
-    SPLIT_ROWS(d)
-    if (rows && !rows[row]) break;
-    x[n0] += (double)dlt[s0];
-    x[n1] += (double)dlt[s1];
-    SPLIT_ROWS_END
+    const int nh = d.nz >> 1;
+    const long long hn = d.n >> 1;
+    for_row_items((long long)d.nx * d.ny, (nh + 31) / 32, rows, (long long)d.nx * d.ny, [&](long long row, int ch) {
+        const int m = ch * 32 + threadIdx.x;
+        if (m >= nh) return;
+        const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
+        const int p = (i + j) & 1;
+        const long long nat = row * d.nz + 2 * m, sp = row * nh + m;
+        x[nat + p] += (double)dlt[sp];
+        x[nat + 1 - p] += (double)dlt[hn + sp];
+    });
 }
 
-// Krylov vector kernels of the split level, one warp per row of one colour (float4 along the row), inactive
-// rows skipped: (r, z) and (z, q) with the beta of k_dot_rz; p = z + beta p; x += alpha p, r -= alpha q, (r, r).
-#define SPLIT_VEC_ROWS(d, rows)                                                                                \
-    const int nq_ = (d).nz >> 3; /* float4 per row of a colour */                                              \
-    const long long nrows_ = (long long)(d).nx * (d).ny;                                                         \
-    for (long long rr = blockIdx.x * (long long)blockDim.y + threadIdx.y; rr < 2 * nrows_;                     \
-         rr += (long long)gridDim.x * blockDim.y) {                                                             \
-        if ((rows) && !(rows)[rr < nrows_ ? rr : rr - nrows_]) continue;                                        \
-        for (int t = threadIdx.x; t < nq_; t += blockDim.x) {                                                   \
-            const long long v4 = rr * nq_ + t;
+// Krylov vector kernels of the split level: items are the rows of one colour (2 n_rows of them, float4 along a
+// row), inactive rows skipped: (r, z) and (z, q) with the beta of k_dot_rz; p = z + beta p; x += alpha p,
+// r -= alpha q, (r, r).
+template <class F>
+__device__ __forceinline__ void for_vec_rows(const Dims &d, const uint8_t *rows, F &&f) {
+    const int nq = d.nz >> 3;  // float4 per row of a colour
+    const long long nrows = (long long)d.nx * d.ny;
+    for_row_items(2 * nrows, (nq + 31) / 32, rows, nrows, [&](long long rr, int ch) {
+        const int t = ch * 32 + threadIdx.x;
+        if (t < nq) f(rr * nq + t);
+    });
+}
 
 __global__ void __launch_bounds__(256) k_dot_rz_s(Dims d, const float *__restrict__ r, const float *__restrict__ z,
                                                   const float *__restrict__ q, const uint8_t *__restrict__ rows,
                                                   int flexible, double *sc, double *part, unsigned *ticket) {
     float a0 = 0.f, a1 = 0.f;
-    SPLIT_VEC_ROWS(d, rows)
-    const float4 rv = reinterpret_cast<const float4 *>(r)[v4], zv = reinterpret_cast<const float4 *>(z)[v4],
-                 qv = reinterpret_cast<const float4 *>(q)[v4];
-    a0 += rv.x * zv.x;
-    a0 += rv.y * zv.y;
-    a0 += rv.z * zv.z;
-    a0 += rv.w * zv.w;
-    a1 += zv.x * qv.x;
-    a1 += zv.y * qv.y;
-    a1 += zv.z * qv.z;
-    a1 += zv.w * qv.w;
-    SPLIT_ROWS_END
+    for_vec_rows(d, rows, [&](long long v4) {
+        const float4 rv = reinterpret_cast<const float4 *>(r)[v4], zv = reinterpret_cast<const float4 *>(z)[v4],
+                     qv = reinterpret_cast<const float4 *>(q)[v4];
+        a0 += rv.x * zv.x;
+        a0 += rv.y * zv.y;
+        a0 += rv.z * zv.z;
+        a0 += rv.w * zv.w;
+        a1 += zv.x * qv.x;
+        a1 += zv.y * qv.y;
+        a1 += zv.z * qv.z;
+        a1 += zv.w * qv.w;
+    });
     double v[2] = {(double)a0, (double)a1};
     double tot[2];
     if (grid_reduce<2>(v, part, ticket, tot)) {
@@ -176,15 +235,15 @@ __global__ void __launch_bounds__(256) k_dot_rz_s(Dims d, const float *__restric
 __global__ void __launch_bounds__(256) k_xpby_s(Dims d, const float *__restrict__ z, float *__restrict__ p,
                                                 const uint8_t *__restrict__ rows, const double *sc) {
     const float beta = (float)sc[S_BETA];
-    SPLIT_VEC_ROWS(d, rows)
-    const float4 zv = reinterpret_cast<const float4 *>(z)[v4];
-    float4 pv = reinterpret_cast<float4 *>(p)[v4];
-    pv.x = zv.x + beta * pv.x;
-    pv.y = zv.y + beta * pv.y;
-    pv.z = zv.z + beta * pv.z;
-    pv.w = zv.w + beta * pv.w;
-    reinterpret_cast<float4 *>(p)[v4] = pv;
-    SPLIT_ROWS_END
+    for_vec_rows(d, rows, [&](long long v4) {
+        const float4 zv = reinterpret_cast<const float4 *>(z)[v4];
+        float4 pv = reinterpret_cast<float4 *>(p)[v4];
+        pv.x = zv.x + beta * pv.x;
+        pv.y = zv.y + beta * pv.y;
+        pv.z = zv.z + beta * pv.z;
+        pv.w = zv.w + beta * pv.w;
+        reinterpret_cast<float4 *>(p)[v4] = pv;
+    });
 }
 
 __global__ void __launch_bounds__(256) k_update_s(Dims d, float *__restrict__ x, float *__restrict__ r,
@@ -193,24 +252,24 @@ __global__ void __launch_bounds__(256) k_update_s(Dims d, float *__restrict__ x,
                                                   unsigned *ticket) {
     const float alpha = (float)sc[S_ALPHA];
     float acc = 0.f;
-    SPLIT_VEC_ROWS(d, rows)
-    float4 xv = reinterpret_cast<float4 *>(x)[v4], rv = reinterpret_cast<float4 *>(r)[v4];
-    const float4 pv = reinterpret_cast<const float4 *>(p)[v4], qv = reinterpret_cast<const float4 *>(q)[v4];
-    xv.x += alpha * pv.x;
-    xv.y += alpha * pv.y;
-    xv.z += alpha * pv.z;
-    xv.w += alpha * pv.w;
-    rv.x = rv.x - alpha * qv.x;
-    rv.y = rv.y - alpha * qv.y;
-    rv.z = rv.z - alpha * qv.z;
-    rv.w = rv.w - alpha * qv.w;
-    reinterpret_cast<float4 *>(x)[v4] = xv;
-    reinterpret_cast<float4 *>(r)[v4] = rv;
-    acc += rv.x * rv.x;
-    acc += rv.y * rv.y;
-    acc += rv.z * rv.z;
-    acc += rv.w * rv.w;
-    SPLIT_ROWS_END
+    for_vec_rows(d, rows, [&](long long v4) {
+        float4 xv = reinterpret_cast<float4 *>(x)[v4], rv = reinterpret_cast<float4 *>(r)[v4];
+        const float4 pv = reinterpret_cast<const float4 *>(p)[v4], qv = reinterpret_cast<const float4 *>(q)[v4];
+        xv.x += alpha * pv.x;
+        xv.y += alpha * pv.y;
+        xv.z += alpha * pv.z;
+        xv.w += alpha * pv.w;
+        rv.x = rv.x - alpha * qv.x;
+        rv.y = rv.y - alpha * qv.y;
+        rv.z = rv.z - alpha * qv.z;
+        rv.w = rv.w - alpha * qv.w;
+        reinterpret_cast<float4 *>(x)[v4] = xv;
+        reinterpret_cast<float4 *>(r)[v4] = rv;
+        acc += rv.x * rv.x;
+        acc += rv.y * rv.y;
+        acc += rv.z * rv.z;
+        acc += rv.w * rv.w;
+    });
     double v[1] = {(double)acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) sc[S_RR] = tot[0];
@@ -240,17 +299,13 @@ struct Cv4<__half> {
     }
 };
 
-// Red-black half sweep of colour `col` in the split layout (the counterpart of k_rbgs4).  Thread (q4, j, i)
-// updates the four colour-`col` cells m0 = 4 q4 .. m0 + 3 of row (i, j); QZ = (i + j + col) & 1 is uniform
-// over a warp (one j) and selects where the z neighbours sit.
+// Red-black half sweep of colour `col` in the split layout (the counterpart of k_rbgs4), on the four
+// colour-`col` cells m0 .. m0 + 3 of row (i, j); QZ = (i + j + col) & 1 is uniform over a warp (one row) and
+// selects where the z neighbours sit.
 template <class C, bool ZERO>
-__global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__restrict__ x, const float *__restrict__ b,
-                                                int col, const uint8_t *__restrict__ rows) {
+__device__ __forceinline__ void rbgs4s_cells(const Dims &d, const Coef<C> &cf, float *__restrict__ x,
+                                             const float *__restrict__ b, int col, int i, int j, int m0) {
     const int nh = d.nz >> 1;
-    const int m0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int i = blockIdx.z;
-    if (j >= d.ny || m0 >= nh || !row_on(rows, d, i, j)) return;
     const long long row = ((long long)i * d.ny + j) * nh + m0;
     const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
     const long long sx = (long long)d.ny * nh, sy = nh;
@@ -340,6 +395,20 @@ __global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__
     else
         sweep(std::integral_constant<int, 1>{});
     *reinterpret_cast<float4 *>(x + own) = make_float4(out[0], out[1], out[2], out[3]);
+}
+
+// Persistent half sweep: warps over (row, chunk of 32 vectors), rows without an active cell skipped.
+template <class C, bool ZERO>
+__global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__restrict__ x, const float *__restrict__ b,
+                                                int col, const uint8_t *__restrict__ rows) {
+    const int nq = d.nz >> 3;
+    const long long nrows = (long long)d.nx * d.ny;
+    for_row_items(nrows, (nq + 31) / 32, rows, nrows, [&](long long row, int ch) {
+        const int q4 = ch * 32 + threadIdx.x;
+        if (q4 >= nq) return;
+        const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
+        rbgs4s_cells<C, ZERO>(d, cf, x, b, col, i, j, 4 * q4);
+    });
 }
 
 // Residuals b - A x of the four colour-`col` cells m0 .. m0 + 3 of row (i, j), each evaluated as nbsum +
@@ -438,14 +507,10 @@ __device__ __forceinline__ void resid4_split(const Dims &d, const Coef<C> &cf, c
 // level.)  Thread (q4, J, I) sums coarse cells K0 = 4 q4 .. K0 + 3 over their x and y children, in the order
 // of k_resid_restrict; in each fine row the colour-0 child of coarse cell K is the entry m = K.
 template <class C>
-__global__ void __launch_bounds__(256, 4) k_resid_restrict_s(Dims d, Coef<C> cf, const float *__restrict__ x,
-                                                             const float *__restrict__ b, Dims dc,
-                                                             float *__restrict__ bc, const uint8_t *__restrict__ rows,
-                                                             const uint8_t *__restrict__ rows_c) {
-    const int K0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
-    const int J = blockIdx.y * blockDim.y + threadIdx.y;
-    const int I = blockIdx.z;
-    if (K0 >= dc.nz || J >= dc.ny || !row_on(rows_c, dc, I, J)) return;
+__device__ __forceinline__ void resid_restrict_s_cells(const Dims &d, const Coef<C> &cf, const float *__restrict__ x,
+                                                       const float *__restrict__ b, const Dims &dc,
+                                                       float *__restrict__ bc, const uint8_t *__restrict__ rows,
+                                                       int I, int J, int K0) {
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     for (int di = 0; di < 2; di++) {
         const int i = 2 * I + di;
@@ -463,46 +528,66 @@ __global__ void __launch_bounds__(256, 4) k_resid_restrict_s(Dims d, Coef<C> cf,
     *reinterpret_cast<float4 *>(bc + cid(dc, I, J, K0)) = make_float4(acc[0], acc[1], acc[2], acc[3]);
 }
 
+template <class C>
+__global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, const float *__restrict__ x,
+                                                             const float *__restrict__ b, Dims dc,
+                                                             float *__restrict__ bc, const uint8_t *__restrict__ rows,
+                                                             const uint8_t *__restrict__ rows_c) {
+    const int nq = dc.nz >> 2;  // coarse float4 per row (dc.nz = nz / 2, a multiple of 4)
+    const long long nrows = (long long)dc.nx * dc.ny;
+    for_row_items(nrows, (nq + 31) / 32, rows_c, nrows, [&](long long row, int ch) {
+        const int q4 = ch * 32 + threadIdx.x;
+        if (q4 >= nq) return;
+        const int I = (int)(row / dc.ny), J = (int)(row - (long long)I * dc.ny);
+        resid_restrict_s_cells<C>(d, cf, x, b, dc, bc, rows, I, J, 4 * q4);
+    });
+}
+
 // x += P xc on the split level 0 (piecewise constant): both colours' entries m of row (i, j) take coarse cell
 // (i/2, j/2, m).
 __global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x, Dims dc, const float *__restrict__ xc,
                                                    const uint8_t *__restrict__ rows) {
-    const int nh = d.nz >> 1;
-    const int m0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int i = blockIdx.z;
-    if (j >= d.ny || m0 >= nh || !row_on(rows, d, i, j)) return;
-    float v[4];
-    ld4(xc + cid(dc, i >> 1, j >> 1, m0), v);
-    const long long row = ((long long)i * d.ny + j) * nh + m0;
+    const int nh = d.nz >> 1, nq = nh >> 2;
+    const long long nrows = (long long)d.nx * d.ny;
+    for_row_items(nrows, (nq + 31) / 32, rows, nrows, [&](long long r, int ch) {
+        const int q4 = ch * 32 + threadIdx.x;
+        if (q4 >= nq) return;
+        const int i = (int)(r / d.ny), j = (int)(r - (long long)i * d.ny), m0 = 4 * q4;
+        float v[4];
+        ld4(xc + cid(dc, i >> 1, j >> 1, m0), v);
+        const long long row = r * nh + m0;
 #pragma unroll
-    for (int col = 0; col < 2; col++) {
-        float *p = x + (long long)col * (d.n >> 1) + row;
-        float4 t = *reinterpret_cast<float4 *>(p);
-        t.x += v[0];
-        t.y += v[1];
-        t.z += v[2];
-        t.w += v[3];
-        *reinterpret_cast<float4 *>(p) = t;
-    }
+        for (int col = 0; col < 2; col++) {
+            float *p = x + (long long)col * (d.n >> 1) + row;
+            float4 t = *reinterpret_cast<float4 *>(p);
+            t.x += v[0];
+            t.y += v[1];
+            t.z += v[2];
+            t.w += v[3];
+            *reinterpret_cast<float4 *>(p) = t;
+        }
+    });
 }
 
 // q = A p and (p, q) on the split FP32 level-0 operator (the counterpart of k_apply_dot4; each cell's q as in
-// k_apply_dot).  Block rows alternate colours: blockIdx.y = 2 * (y tile) + colour.
-__global__ void __launch_bounds__(256) k_apply_dot4s(Dims d, int xpb, Coef<float> cf, const float *__restrict__ p,
+// k_apply_dot).  Persistent: warps over (colour row, chunk of 32 vectors), rows without an active cell skipped
+// (q stays zero there).
+__global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, const float *__restrict__ p,
                                                      float *__restrict__ q, const uint8_t *__restrict__ rows,
                                                      double *sc, double *part, unsigned *ticket) {
     float acc = 0.f;
-    const int nh = d.nz >> 1;
-    const int col = blockIdx.y & 1;
-    const int m0 = 4 * (blockIdx.x * 32 + threadIdx.x), j = (blockIdx.y >> 1) * 8 + threadIdx.y;
-    if (m0 < nh && j < d.ny) {
+    const int nh = d.nz >> 1, nq = nh >> 2;
+    const long long nrows = (long long)d.nx * d.ny;
+    for_row_items(2 * nrows, (nq + 31) / 32, rows, nrows, [&](long long rr, int ch) {
+        const int q4 = ch * 32 + threadIdx.x;
+        if (q4 >= nq) return;
+        const int col = rr >= nrows ? 1 : 0;
+        const long long rw = rr - col * nrows;
+        const int i = (int)(rw / d.ny), j = (int)(rw - (long long)i * d.ny), m0 = 4 * q4;
         const long long sx = (long long)d.ny * nh, sy = nh;
         const bool yl = j > 0, yu = j < d.ny - 1;
-        const int i_end = min(d.nx, (int)(blockIdx.z + 1) * xpb);
-        for (int i = blockIdx.z * xpb; i < i_end; i++) {
-            if (!row_on(rows, d, i, j)) continue;  // q stays zero
-            const long long row = ((long long)i * d.ny + j) * nh + m0;
+        {
+            const long long row = rw * nh + m0;
             const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
             const bool xl = i > 0, xu = i < d.nx - 1;
             const int qz = (i + j + col) & 1;
@@ -572,7 +657,7 @@ __global__ void __launch_bounds__(256) k_apply_dot4s(Dims d, int xpb, Coef<float
                 body(std::integral_constant<int, 1>{});
             *reinterpret_cast<float4 *>(q + own) = make_float4(out[0], out[1], out[2], out[3]);
         }
-    }
+    });
     double v[1] = {(double)acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) {
@@ -586,13 +671,11 @@ __global__ void __launch_bounds__(256) k_apply_dot4s(Dims d, int xpb, Coef<float
     }
 }
 
+// Items of the persistent split kernels: rows x chunks of 32 float4.
+static inline long long split_items(long long nrows, int nq) { return nrows * ((nq + 31) / 32); }
+
 static void apply_dot32s(cudaStream_t st, const Dims &d, const Coef<float> &cf, const float *p, float *q,
                          const uint8_t *rows, double *sc, double *part, unsigned *ticket) {
-    const int nh = d.nz >> 1;
-    const long long tiles = (long long)((nh + 127) / 128) * 2 * ((d.ny + 7) / 8);
-    const long long zmax = tiles < kApplyBlocks ? kApplyBlocks / tiles : 1;
-    int xpb = (int)((d.nx + zmax - 1) / zmax);
-    if (xpb < 2) xpb = 2;
-    const dim3 g((nh + 127) / 128, 2 * ((d.ny + 7) / 8), (d.nx + xpb - 1) / xpb);
-    k_apply_dot4s<<<g, dim3(32, 8), 0, st>>>(d, xpb, cf, p, q, rows, sc, part, ticket);
+    const int g = row_grid((const void *)k_apply_dot4s, split_items(2LL * d.nx * d.ny, d.nz >> 3));
+    k_apply_dot4s<<<g, dim3(32, 8), 0, st>>>(d, cf, p, q, rows, sc, part, ticket);
 }
