@@ -1309,30 +1309,31 @@ static void fused(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const 
 // Half sweep of the split level 0 (smoother 3); same algorithmic bytes as the natural half sweep.
 template <class C>
 static void rb_split(cudaStream_t st, Tracker &tk, bool zero, const Dims &d, const Coef<C> &cf, float *x,
-                     const float *b, int color, const uint8_t *rows) {
+                     const float *b, int color, const int *list, const int *count) {
     const long long items = split_items((long long)d.nx * d.ny, d.nz >> 3);
     tk.before(st, true);
     if (zero)
         k_rbgs4s<C, true><<<row_grid((const void *)k_rbgs4s<C, true>, items), blk2(), 0, st>>>(d, cf, x, b, color,
-                                                                                             rows);
+                                                                                             list, count);
     else
         k_rbgs4s<C, false><<<row_grid((const void *)k_rbgs4s<C, false>, items), blk2(), 0, st>>>(d, cf, x, b, color,
-                                                                                               rows);
+                                                                                               list, count);
     tk.after(st, true, (3.0 * sizeof(float) + 4.0 * sizeof(C)) / 2.0 * d.n * tk.frac0);
 }
 
 template <class T, class C>
 static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const Coef<C> &cf, T *x, T *tmp,
-                   const T *b, int nu, bool pre, bool split = false, const uint8_t *rows = nullptr) {
+                   const T *b, int nu, bool pre, bool split = false, const uint8_t *rows = nullptr,
+                   const int *list = nullptr, const int *count = nullptr) {
     if constexpr (std::is_same<T, float>::value && std::is_same<C, __half>::value) {  // split: FP16 copy only
         if (split) {
             for (int s = 0; s < nu; s++) {
                 if (pre) {
-                    rb_split<C>(st, tk, s == 0, d, cf, x, b, 0, rows);
-                    rb_split<C>(st, tk, false, d, cf, x, b, 1, rows);
+                    rb_split<C>(st, tk, s == 0, d, cf, x, b, 0, list, count);
+                    rb_split<C>(st, tk, false, d, cf, x, b, 1, list, count);
                 } else {
-                    rb_split<C>(st, tk, false, d, cf, x, b, 1, rows);
-                    rb_split<C>(st, tk, false, d, cf, x, b, 0, rows);
+                    rb_split<C>(st, tk, false, d, cf, x, b, 1, list, count);
+                    rb_split<C>(st, tk, false, d, cf, x, b, 0, list, count);
                 }
             }
             return;
@@ -1376,12 +1377,13 @@ static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const
 template <class T, class C>
 static void restrict_res(cudaStream_t st, Tracker &tk, const Dims &d, const Coef<C> &cf, const T *x, const T *b,
                          const Dims &dc, T *bc, bool split = false, const uint8_t *rows = nullptr,
-                         const uint8_t *rows_c = nullptr) {
+                         const uint8_t *rows_c = nullptr, const int *list_c = nullptr,
+                         const int *count_c = nullptr) {
     tk.launches++;
     if constexpr (std::is_same<T, float>::value && std::is_same<C, __half>::value) {
         if (split) {
             const int g = row_grid((const void *)k_resid_restrict_s<C>, split_items((long long)dc.nx * dc.ny, dc.nz >> 2));
-            k_resid_restrict_s<C><<<g, blk2(), 0, st>>>(d, cf, x, b, dc, bc, rows, rows_c);
+            k_resid_restrict_s<C><<<g, blk2(), 0, st>>>(d, cf, x, b, dc, bc, rows, list_c, count_c);
             return;
         }
     }
@@ -1404,20 +1406,29 @@ static void coarse_solve(cudaStream_t st, Tracker &tk, const Dims &d, const Coef
 // c0s: level-0 coefficients read by the level-0 smoother and the residual restriction (c0 itself, or a
 // lower-precision copy, making the V-cycle a multigrid cycle for that copy); the coarsest solve of a one-level
 // hierarchy uses c0.
+// Row activity of a hierarchy with a split level 0: flags per level, and the ordered active rows of levels 0
+// and 1 (the persistent split kernels walk those lists).
+struct RowSets {
+    const std::vector<uint8_t *> *flags;
+    const int *list[2], *count[2];
+};
+
 template <class T, class C0, class Cc, class C0S>
 static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, const Coef<C0> &c0,
                    const Coef<C0S> &c0s, const std::vector<Coef<Cc>> &cc, T *z, const T *r,
                    const std::vector<T *> &xs, const std::vector<T *> &bs, const std::vector<T *> &ts,
-                   const SolverParams &p, bool split0 = false, const std::vector<uint8_t *> *rows = nullptr) {
+                   const SolverParams &p, bool split0 = false, const RowSets *rs = nullptr) {
     const int L = (int)dims.size();
     if (L == 1) {
         coarse_solve<T, C0>(st, tk, dims[0], c0, z, r, p.coarse_sweeps);
         return;
     }
-    auto R = [&](int l) -> const uint8_t * { return rows ? (*rows)[l] : nullptr; };
-    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true, split0, R(0));
+    auto R = [&](int l) -> const uint8_t * { return rs ? (*rs->flags)[l] : nullptr; };
+    const int *l0 = rs ? rs->list[0] : nullptr, *n0 = rs ? rs->count[0] : nullptr;
+    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true, split0, R(0), l0, n0);
     // the residual of the smoothed operator
-    restrict_res<T, C0S>(st, tk, dims[0], c0s, z, r, dims[1], bs[1], split0, R(0), R(1));
+    restrict_res<T, C0S>(st, tk, dims[0], c0s, z, r, dims[1], bs[1], split0, R(0), R(1), rs ? rs->list[1] : nullptr,
+                         rs ? rs->count[1] : nullptr);
     for (int l = 1; l < L - 1; l++) {
         smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.pre, true, false, R(l));
         restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1], false, R(l), R(l + 1));
@@ -1433,8 +1444,8 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
         if (split0) {
             const Dims &d0 = dims[0];
             const int g = row_grid((const void *)k_prolong_s, split_items((long long)d0.nx * d0.ny, d0.nz >> 3));
-            k_prolong_s<<<g, blk2(), 0, st>>>(d0, z, dims[1], xs[1], R(0));
-            smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true, R(0));
+            k_prolong_s<<<g, blk2(), 0, st>>>(d0, z, dims[1], xs[1], l0, n0);
+            smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true, R(0), l0, n0);
             return;
         }
     }
@@ -1579,6 +1590,12 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
         }
         rows_.assign(split0 ? L : 0, nullptr);
         for (int l = 0; l < (int)rows_.size(); l++) rows_[l] = (uint8_t *)chk(A((size_t)dims[l].nx * dims[l].ny));
+        list_[0] = list_[1] = nullptr;
+        count_ = nullptr;
+        if (split0) {
+            for (int l = 0; l < 2; l++) list_[l] = (int *)chk(A(4 * (size_t)dims[l].nx * dims[l].ny));
+            count_ = (int *)chk(A(8));
+        }
         r32_ = (float *)chk(A(4 * n));
         d32_ = (float *)chk(A(4 * n));
         z32_ = (float *)chk(A(4 * n));
@@ -1635,7 +1652,10 @@ cudaError_t MGSolver::build_hierarchy() {
                 cudaMemsetAsync(x32_[l], 0, 4 * (size_t)dl.n, st_);
                 cudaMemsetAsync(b32_[l], 0, 4 * (size_t)dl.n, st_);
             }
-            tk_.launches += L - 1;
+            for (int l = 0; l < 2; l++)
+                k_rows_list<<<1, 1024, 0, st_>>>((long long)lev_dims_[l].nx * lev_dims_[l].ny, rows_[l], list_[l],
+                                                 count_ + l);
+            tk_.launches += L - 1 + 2;
             tk_.frac0 = 1.0;
             if (prm_.profile) {  // profiled runs synchronise anyway: count the active level-0 rows
                 const Dims &d0 = lev_dims_[0];
@@ -1690,16 +1710,17 @@ void MGSolver::enqueue_iter32() {
     const std::vector<float *> ts = prm_.smoother == 1 ? t32_ : std::vector<float *>(t32_.size(), nullptr);
     if (split0_) {
         // colour-split level 0 with row flags on every level (vectors in split rows, inactive rows skipped)
-        const uint8_t *r0 = rows_[0];
+        const RowSets rs{&rows_, {list_[0], list_[1]}, {count_, count_ + 1}};
+        const int *lst0 = list_[0], *cnt0 = count_;
         vcycle<float, float, __half, __half>(st_, tk_, lev_dims_, c32_, c16s0_, c16_, z32_, ri32_, x32_, b32_, ts,
-                                             prm_, true, &rows_);
+                                             prm_, true, &rs);
         const long long vitems = split_items(2LL * d.nx * d.ny, d.nz >> 3);
-        k_dot_rz_s<<<row_grid((const void *)k_dot_rz_s, vitems), dim3(32, 8), 0, st_>>>(d, ri32_, z32_, q32_, r0, 1,
-                                                                                       sc_, part_, ticket_);
-        k_xpby_s<<<row_grid((const void *)k_xpby_s, vitems), dim3(32, 8), 0, st_>>>(d, z32_, p32_, r0, sc_);
-        apply_dot32s(st_, d, c32_, p32_, q32_, r0, sc_, part_, ticket_);
-        k_update_s<<<row_grid((const void *)k_update_s, vitems), dim3(32, 8), 0, st_>>>(d, d32_, ri32_, p32_, q32_, r0,
-                                                                                      sc_, part_, ticket_);
+        k_dot_rz_s<<<row_grid((const void *)k_dot_rz_s, vitems), dim3(32, 8), 0, st_>>>(d, ri32_, z32_, q32_, lst0, cnt0,
+                                                                                       1, sc_, part_, ticket_);
+        k_xpby_s<<<row_grid((const void *)k_xpby_s, vitems), dim3(32, 8), 0, st_>>>(d, z32_, p32_, lst0, cnt0, sc_);
+        apply_dot32s(st_, d, c32_, p32_, q32_, lst0, cnt0, sc_, part_, ticket_);
+        k_update_s<<<row_grid((const void *)k_update_s, vitems), dim3(32, 8), 0, st_>>>(d, d32_, ri32_, p32_, q32_, lst0,
+                                                                                      cnt0, sc_, part_, ticket_);
         tk_.launches += 4;
         iter_launches32_ = tk_.launches - l0;
         cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
@@ -1929,7 +1950,7 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
         total_inner += it;
         if (split0_)
             k_ir_update_s<<<row_grid((const void *)k_ir_update_s, (long long)d.nx * d.ny * (((d.nz >> 1) + 31) / 32)),
-                            dim3(32, 8), 0, st_>>>(d, x_, d32_, rows_[0]);
+                            dim3(32, 8), 0, st_>>>(d, x_, d32_, list_[0], count_);
         else
             k_ir_update<<<flat_grid(n), 256, 0, st_>>>(n, x_, d32_);
         tk_.launches++;
@@ -1962,7 +1983,7 @@ cudaError_t MGSolver::set_guess_scaled(const float *y, double &gamma) {
     if (split0_) {
         // scratch: q32 and p32, cleared before the solve's first inner iteration
         k_vec_to_split<<<split_rows_grid(d), dim3(32, 8), 0, st_>>>(d, y, q32_);
-        apply_dot32s(st_, d, c32_, q32_, p32_, rows_[0], sc_, part_, ticket_);
+        apply_dot32s(st_, d, c32_, q32_, p32_, list_[0], count_, sc_, part_, ticket_);
         tk_.launches++;
     } else {
         apply_dot32(st_, d, c32_, y, q32_, sc_, part_, ticket_);

@@ -145,6 +145,8 @@ class MGSolver {
     bool split0_ = false, cfg_split_ = false;
     // with split0_: per level, one byte per row (i, j), 0 when every cell of the row is inactive (D = 0)
     std::vector<uint8_t *> rows_;
+    int *list_[2] = {nullptr, nullptr};  // ordered active rows of levels 0 and 1
+    int *count_ = nullptr;               // their counts (device)
     std::vector<float *> x32_, b32_, t32_;
 
     double *x_ = nullptr, *b_ = nullptr;

@@ -46,30 +46,44 @@ static inline int split_rows_grid(const Dims &d) {
     return (int)(g < 1 ? 1 : g);
 }
 
-// Persistent loop of a grid's warps (blockDim = (32, 8)) over the items (r, chunk) of `nr` rows, `nch` chunks of
-// 32 lanes per row, in row order: warp w takes items w, w + W, ...  Rows whose flag rows[r mod period] is 0 are
-// skipped; the next item's flag is loaded before the current item's work, so a skipped row costs no load
-// latency of its own.  The assignment depends only on the grid and the sizes: reductions stay deterministic.
+// Ordered list of a level's active rows (one block of 1024 threads): list[0 .. *count) holds, ascending, the rows
+// r with rows[r] != 0.
+__global__ void __launch_bounds__(1024) k_rows_list(long long nrows, const uint8_t *__restrict__ rows,
+                                                     int *__restrict__ list, int *__restrict__ count) {
+    __shared__ int sh[1024];
+    const int t = threadIdx.x;
+    const long long per = (nrows + 1023) / 1024;
+    const long long r0 = t * per, r1 = r0 + per < nrows ? r0 + per : nrows;
+    int c = 0;
+    for (long long r = r0; r < r1; r++) c += rows[r] != 0;
+    sh[t] = c;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {  // inclusive scan
+        const int v = t >= off ? sh[t - off] : 0;
+        __syncthreads();
+        sh[t] += v;
+        __syncthreads();
+    }
+    int pos = sh[t] - c;
+    for (long long r = r0; r < r1; r++)
+        if (rows[r]) list[pos++] = (int)r;
+    if (t == 1023) *count = sh[1023];
+}
+
+// Persistent loop of a grid's warps (blockDim = (32, 8)) over the items (rep, list entry, chunk): `reps` passes
+// (colours) over the *count listed rows, `nch` chunks of 32 lanes per row; warp w takes items w, w + W, ...
+// Every warp gets an equal share of the active rows, and the assignment depends only on the grid and the list,
+// so reductions stay deterministic.  f(rep, row, chunk).
 template <class F>
-__device__ __forceinline__ void for_row_items(long long nr, int nch, const uint8_t *__restrict__ rows,
-                                              long long period, F &&f) {
-    const long long stride = (long long)gridDim.x * blockDim.y, nit = nr * nch;
-    auto flag = [&](long long it) {
-        if (it >= nit) return false;
-        if (!rows) return true;
-        long long r = it / nch;
-        if (r >= period) r -= period;
-        return rows[r] != 0;
-    };
-    long long it = blockIdx.x * (long long)blockDim.y + threadIdx.y;
-    bool on = flag(it);
-    for (; it < nit; it += stride) {
-        const bool on_next = flag(it + stride);
-        if (on) {
-            const long long r = it / nch;
-            f(r, (int)(it - r * nch));
-        }
-        on = on_next;
+__device__ __forceinline__ void for_list_items(const int *__restrict__ list, const int *__restrict__ count, int reps,
+                                               int nch, F &&f) {
+    const long long n = *count;
+    const long long nit = (long long)reps * n * nch, stride = (long long)gridDim.x * blockDim.y;
+    for (long long it = blockIdx.x * (long long)blockDim.y + threadIdx.y; it < nit; it += stride) {
+        const long long rr = it / nch;
+        const int ch = (int)(it - rr * nch);
+        const int rep = (int)(rr / n);
+        f(rep, list[rr - rep * n], ch);
     }
 }
 
@@ -176,10 +190,10 @@ __global__ void __launch_bounds__(256) k_cast_rhs_s(Dims d, const double *__rest
 
 // x64 += d32 with d32 in the split layout (zero in inactive rows, which are skipped).
 __global__ void __launch_bounds__(256) k_ir_update_s(Dims d, double *__restrict__ x, const float *__restrict__ dlt,
-                                                     const uint8_t *__restrict__ rows) {
+                                                     const int *__restrict__ list, const int *__restrict__ count) {
     const int nh = d.nz >> 1;
     const long long hn = d.n >> 1;
-    for_row_items((long long)d.nx * d.ny, (nh + 31) / 32, rows, (long long)d.nx * d.ny, [&](long long row, int ch) {
+    for_list_items(list, count, 1, (nh + 31) / 32, [&](int, long long row, int ch) {
         const int m = ch * 32 + threadIdx.x;
         if (m >= nh) return;
         const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
@@ -194,20 +208,21 @@ __global__ void __launch_bounds__(256) k_ir_update_s(Dims d, double *__restrict_
 // row), inactive rows skipped: (r, z) and (z, q) with the beta of k_dot_rz; p = z + beta p; x += alpha p,
 // r -= alpha q, (r, r).
 template <class F>
-__device__ __forceinline__ void for_vec_rows(const Dims &d, const uint8_t *rows, F &&f) {
+__device__ __forceinline__ void for_vec_rows(const Dims &d, const int *list, const int *count, F &&f) {
     const int nq = d.nz >> 3;  // float4 per row of a colour
     const long long nrows = (long long)d.nx * d.ny;
-    for_row_items(2 * nrows, (nq + 31) / 32, rows, nrows, [&](long long rr, int ch) {
+    for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, long long row, int ch) {
         const int t = ch * 32 + threadIdx.x;
-        if (t < nq) f(rr * nq + t);
+        if (t < nq) f((col * nrows + row) * nq + t);
     });
 }
 
 __global__ void __launch_bounds__(256) k_dot_rz_s(Dims d, const float *__restrict__ r, const float *__restrict__ z,
-                                                  const float *__restrict__ q, const uint8_t *__restrict__ rows,
-                                                  int flexible, double *sc, double *part, unsigned *ticket) {
+                                                  const float *__restrict__ q, const int *__restrict__ list,
+                                                  const int *__restrict__ count, int flexible, double *sc,
+                                                  double *part, unsigned *ticket) {
     float a0 = 0.f, a1 = 0.f;
-    for_vec_rows(d, rows, [&](long long v4) {
+    for_vec_rows(d, list, count, [&](long long v4) {
         const float4 rv = reinterpret_cast<const float4 *>(r)[v4], zv = reinterpret_cast<const float4 *>(z)[v4],
                      qv = reinterpret_cast<const float4 *>(q)[v4];
         a0 += rv.x * zv.x;
@@ -233,9 +248,10 @@ __global__ void __launch_bounds__(256) k_dot_rz_s(Dims d, const float *__restric
 }
 
 __global__ void __launch_bounds__(256) k_xpby_s(Dims d, const float *__restrict__ z, float *__restrict__ p,
-                                                const uint8_t *__restrict__ rows, const double *sc) {
+                                                const int *__restrict__ list, const int *__restrict__ count,
+                                                const double *sc) {
     const float beta = (float)sc[S_BETA];
-    for_vec_rows(d, rows, [&](long long v4) {
+    for_vec_rows(d, list, count, [&](long long v4) {
         const float4 zv = reinterpret_cast<const float4 *>(z)[v4];
         float4 pv = reinterpret_cast<float4 *>(p)[v4];
         pv.x = zv.x + beta * pv.x;
@@ -248,11 +264,11 @@ __global__ void __launch_bounds__(256) k_xpby_s(Dims d, const float *__restrict_
 
 __global__ void __launch_bounds__(256) k_update_s(Dims d, float *__restrict__ x, float *__restrict__ r,
                                                   const float *__restrict__ p, const float *__restrict__ q,
-                                                  const uint8_t *__restrict__ rows, double *sc, double *part,
-                                                  unsigned *ticket) {
+                                                  const int *__restrict__ list, const int *__restrict__ count,
+                                                  double *sc, double *part, unsigned *ticket) {
     const float alpha = (float)sc[S_ALPHA];
     float acc = 0.f;
-    for_vec_rows(d, rows, [&](long long v4) {
+    for_vec_rows(d, list, count, [&](long long v4) {
         float4 xv = reinterpret_cast<float4 *>(x)[v4], rv = reinterpret_cast<float4 *>(r)[v4];
         const float4 pv = reinterpret_cast<const float4 *>(p)[v4], qv = reinterpret_cast<const float4 *>(q)[v4];
         xv.x += alpha * pv.x;
@@ -397,13 +413,12 @@ __device__ __forceinline__ void rbgs4s_cells(const Dims &d, const Coef<C> &cf, f
     *reinterpret_cast<float4 *>(x + own) = make_float4(out[0], out[1], out[2], out[3]);
 }
 
-// Persistent half sweep: warps over (row, chunk of 32 vectors), rows without an active cell skipped.
+// Persistent half sweep: warps over the active rows' chunks of 32 vectors.
 template <class C, bool ZERO>
 __global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__restrict__ x, const float *__restrict__ b,
-                                                int col, const uint8_t *__restrict__ rows) {
+                                                int col, const int *__restrict__ list, const int *__restrict__ count) {
     const int nq = d.nz >> 3;
-    const long long nrows = (long long)d.nx * d.ny;
-    for_row_items(nrows, (nq + 31) / 32, rows, nrows, [&](long long row, int ch) {
+    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long row, int ch) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
         const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
@@ -532,10 +547,10 @@ template <class C>
 __global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, const float *__restrict__ x,
                                                              const float *__restrict__ b, Dims dc,
                                                              float *__restrict__ bc, const uint8_t *__restrict__ rows,
-                                                             const uint8_t *__restrict__ rows_c) {
+                                                             const int *__restrict__ list_c,
+                                                             const int *__restrict__ count_c) {
     const int nq = dc.nz >> 2;  // coarse float4 per row (dc.nz = nz / 2, a multiple of 4)
-    const long long nrows = (long long)dc.nx * dc.ny;
-    for_row_items(nrows, (nq + 31) / 32, rows_c, nrows, [&](long long row, int ch) {
+    for_list_items(list_c, count_c, 1, (nq + 31) / 32, [&](int, long long row, int ch) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
         const int I = (int)(row / dc.ny), J = (int)(row - (long long)I * dc.ny);
@@ -546,10 +561,9 @@ __global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, co
 // x += P xc on the split level 0 (piecewise constant): both colours' entries m of row (i, j) take coarse cell
 // (i/2, j/2, m).
 __global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x, Dims dc, const float *__restrict__ xc,
-                                                   const uint8_t *__restrict__ rows) {
+                                                   const int *__restrict__ list, const int *__restrict__ count) {
     const int nh = d.nz >> 1, nq = nh >> 2;
-    const long long nrows = (long long)d.nx * d.ny;
-    for_row_items(nrows, (nq + 31) / 32, rows, nrows, [&](long long r, int ch) {
+    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long r, int ch) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
         const int i = (int)(r / d.ny), j = (int)(r - (long long)i * d.ny), m0 = 4 * q4;
@@ -573,16 +587,14 @@ __global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x
 // k_apply_dot).  Persistent: warps over (colour row, chunk of 32 vectors), rows without an active cell skipped
 // (q stays zero there).
 __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, const float *__restrict__ p,
-                                                     float *__restrict__ q, const uint8_t *__restrict__ rows,
-                                                     double *sc, double *part, unsigned *ticket) {
+                                                     float *__restrict__ q, const int *__restrict__ list,
+                                                     const int *__restrict__ count, double *sc, double *part,
+                                                     unsigned *ticket) {
     float acc = 0.f;
     const int nh = d.nz >> 1, nq = nh >> 2;
-    const long long nrows = (long long)d.nx * d.ny;
-    for_row_items(2 * nrows, (nq + 31) / 32, rows, nrows, [&](long long rr, int ch) {
+    for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, long long rw, int ch) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
-        const int col = rr >= nrows ? 1 : 0;
-        const long long rw = rr - col * nrows;
         const int i = (int)(rw / d.ny), j = (int)(rw - (long long)i * d.ny), m0 = 4 * q4;
         const long long sx = (long long)d.ny * nh, sy = nh;
         const bool yl = j > 0, yu = j < d.ny - 1;
@@ -675,7 +687,7 @@ __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, 
 static inline long long split_items(long long nrows, int nq) { return nrows * ((nq + 31) / 32); }
 
 static void apply_dot32s(cudaStream_t st, const Dims &d, const Coef<float> &cf, const float *p, float *q,
-                         const uint8_t *rows, double *sc, double *part, unsigned *ticket) {
+                         const int *list, const int *count, double *sc, double *part, unsigned *ticket) {
     const int g = row_grid((const void *)k_apply_dot4s, split_items(2LL * d.nx * d.ny, d.nz >> 3));
-    k_apply_dot4s<<<g, dim3(32, 8), 0, st>>>(d, cf, p, q, rows, sc, part, ticket);
+    k_apply_dot4s<<<g, dim3(32, 8), 0, st>>>(d, cf, p, q, list, count, sc, part, ticket);
 }
