@@ -88,20 +88,29 @@ def max_over_ranks(ws, v):
     return float(t.item())
 
 
-def profiled_traffic(summary, n):
+def profiled_traffic(summary, n, bytes_per_launch=None):
     """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the reported kernel, from the ncu
-    capture summarised in profiles/<summary> (a 256^3 launch), scaled to n^3 cells; None without a capture."""
+    capture summarised in profiles/<summary> (a 256^3 launch).  With bytes_per_launch (the bench's mean algorithmic
+    bytes per launch) and the capture's own algorithmic bytes in the summary, it is scaled by their ratio (the
+    launches of a step process different numbers of rows, of two kinds); otherwise by n^3 cells.  None without a
+    capture."""
     if not summary:
         return None
+    mb = alg = None
     try:
         with open(os.path.join(ROOT, "profiles", summary)) as f:
             for line in f:
                 if line.startswith("| dram__bytes_read.sum + dram__bytes_write.sum"):
                     mb = float(line.split("=")[-1].split("MB")[0])
-                    return round(mb * 1e6 * (n / 256.0) ** 3)
+                elif line.startswith("| algorithmic bytes per launch"):
+                    alg = float(line.split("|")[2].split("MB")[0])
     except (OSError, ValueError):
-        pass
-    return None
+        return None
+    if mb is None:
+        return None
+    if bytes_per_launch and alg:
+        return round(mb * bytes_per_launch / alg)
+    return round(mb * 1e6 * (n / 256.0) ** 3)
 
 
 # ------------------------------------------------------------------------------------------------ clocks
@@ -282,15 +291,15 @@ def run_ours(args, ws, rank, local):
     else:
         kname = "k_rbgs (one colour of a red-black sweep per launch)"
         prof = "k_rbgs_f32_finest_pool_sphere_256.md" if args.precision == "mixed" else None
-    traffic = profiled_traffic(prof, args.n)
-    if traffic is not None and smoother == 3 and args.precision == "mixed" and args.n % 8 == 0:
-        # the capture is of a launch over every row; launches skip rows without an active cell, so the
-        # per-launch traffic is scaled by the processed share, as the algorithmic bytes are
-        traffic = round(traffic * (bytes_tot / max(n_launch, 1)) / (10.0 * args.n ** 3))
+    split = smoother == 3 and args.precision == "mixed" and args.n % 8 == 0
+    traffic = profiled_traffic(prof, args.n, bytes_tot / max(n_launch, 1) if split else None)
     roofline = {"bound": "hbm", "kernel": kname + ", finest level",
                 "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
                 "bytes_per_launch": bytes_tot / max(n_launch, 1), "ms_per_launch": ms_tot / max(n_launch, 1),
+                "per_solve": {k: {"bytes_per_launch": r["smooth_bytes"] / max(r["smooth_launches"], 1),
+                                  "ms_per_launch": r["smooth_ms"] / max(r["smooth_launches"], 1)}
+                              for k, r in (("pressure", sp), ("magnetic", sm))},
                 "launches_timed": n_launch}
 
     # e2e: host pointers, pinned buffers

@@ -1309,31 +1309,31 @@ static void fused(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const 
 // Half sweep of the split level 0 (smoother 3); same algorithmic bytes as the natural half sweep.
 template <class C>
 static void rb_split(cudaStream_t st, Tracker &tk, bool zero, const Dims &d, const Coef<C> &cf, float *x,
-                     const float *b, int color, const int *list, const int *count) {
+                     const float *b, int color, const int *list, const int *count, const float *crow) {
     const long long items = split_items((long long)d.nx * d.ny, d.nz >> 3);
     tk.before(st, true);
     if (zero)
         k_rbgs4s<C, true><<<row_grid((const void *)k_rbgs4s<C, true>, items), blk2(), 0, st>>>(d, cf, x, b, color,
-                                                                                             list, count);
+                                                                                             list, count, crow);
     else
         k_rbgs4s<C, false><<<row_grid((const void *)k_rbgs4s<C, false>, items), blk2(), 0, st>>>(d, cf, x, b, color,
-                                                                                               list, count);
-    tk.after(st, true, (3.0 * sizeof(float) + 4.0 * sizeof(C)) / 2.0 * d.n * tk.frac0);
+                                                                                               list, count, crow);
+    tk.after(st, true, tk.bytes0 >= 0 ? tk.bytes0 : (3.0 * sizeof(float) + 4.0 * sizeof(C)) / 2.0 * d.n);
 }
 
 template <class T, class C>
 static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const Coef<C> &cf, T *x, T *tmp,
                    const T *b, int nu, bool pre, bool split = false, const uint8_t *rows = nullptr,
-                   const int *list = nullptr, const int *count = nullptr) {
+                   const int *list = nullptr, const int *count = nullptr, const float *crow = nullptr) {
     if constexpr (std::is_same<T, float>::value && std::is_same<C, __half>::value) {  // split: FP16 copy only
         if (split) {
             for (int s = 0; s < nu; s++) {
                 if (pre) {
-                    rb_split<C>(st, tk, s == 0, d, cf, x, b, 0, list, count);
-                    rb_split<C>(st, tk, false, d, cf, x, b, 1, list, count);
+                    rb_split<C>(st, tk, s == 0, d, cf, x, b, 0, list, count, crow);
+                    rb_split<C>(st, tk, false, d, cf, x, b, 1, list, count, crow);
                 } else {
-                    rb_split<C>(st, tk, false, d, cf, x, b, 1, list, count);
-                    rb_split<C>(st, tk, false, d, cf, x, b, 0, list, count);
+                    rb_split<C>(st, tk, false, d, cf, x, b, 1, list, count, crow);
+                    rb_split<C>(st, tk, false, d, cf, x, b, 0, list, count, crow);
                 }
             }
             return;
@@ -1378,12 +1378,12 @@ template <class T, class C>
 static void restrict_res(cudaStream_t st, Tracker &tk, const Dims &d, const Coef<C> &cf, const T *x, const T *b,
                          const Dims &dc, T *bc, bool split = false, const uint8_t *rows = nullptr,
                          const uint8_t *rows_c = nullptr, const int *list_c = nullptr,
-                         const int *count_c = nullptr) {
+                         const int *count_c = nullptr, const float *crow = nullptr) {
     tk.launches++;
     if constexpr (std::is_same<T, float>::value && std::is_same<C, __half>::value) {
         if (split) {
             const int g = row_grid((const void *)k_resid_restrict_s<C>, split_items((long long)dc.nx * dc.ny, dc.nz >> 2));
-            k_resid_restrict_s<C><<<g, blk2(), 0, st>>>(d, cf, x, b, dc, bc, rows, list_c, count_c);
+            k_resid_restrict_s<C><<<g, blk2(), 0, st>>>(d, cf, x, b, dc, bc, rows, crow, list_c, count_c);
             return;
         }
     }
@@ -1411,6 +1411,7 @@ static void coarse_solve(cudaStream_t st, Tracker &tk, const Dims &d, const Coef
 struct RowSets {
     const std::vector<uint8_t *> *flags;
     const int *list[2], *count[2];
+    const float *crow;  // level 0: the coupling of each uniform row
 };
 
 template <class T, class C0, class Cc, class C0S>
@@ -1425,10 +1426,11 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
     }
     auto R = [&](int l) -> const uint8_t * { return rs ? (*rs->flags)[l] : nullptr; };
     const int *l0 = rs ? rs->list[0] : nullptr, *n0 = rs ? rs->count[0] : nullptr;
-    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true, split0, R(0), l0, n0);
+    const float *cr = rs ? rs->crow : nullptr;
+    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true, split0, R(0), l0, n0, cr);
     // the residual of the smoothed operator
     restrict_res<T, C0S>(st, tk, dims[0], c0s, z, r, dims[1], bs[1], split0, R(0), R(1), rs ? rs->list[1] : nullptr,
-                         rs ? rs->count[1] : nullptr);
+                         rs ? rs->count[1] : nullptr, cr);
     for (int l = 1; l < L - 1; l++) {
         smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.pre, true, false, R(l));
         restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1], false, R(l), R(l + 1));
@@ -1445,7 +1447,7 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
             const Dims &d0 = dims[0];
             const int g = row_grid((const void *)k_prolong_s, split_items((long long)d0.nx * d0.ny, d0.nz >> 3));
             k_prolong_s<<<g, blk2(), 0, st>>>(d0, z, dims[1], xs[1], l0, n0);
-            smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true, R(0), l0, n0);
+            smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true, R(0), l0, n0, cr);
             return;
         }
     }
@@ -1592,9 +1594,11 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
         for (int l = 0; l < (int)rows_.size(); l++) rows_[l] = (uint8_t *)chk(A((size_t)dims[l].nx * dims[l].ny));
         list_[0] = list_[1] = nullptr;
         count_ = nullptr;
+        crow_ = nullptr;
         if (split0) {
             for (int l = 0; l < 2; l++) list_[l] = (int *)chk(A(4 * (size_t)dims[l].nx * dims[l].ny));
             count_ = (int *)chk(A(8));
+            crow_ = (float *)chk(A(4 * (size_t)dims[0].nx * dims[0].ny));
         }
         r32_ = (float *)chk(A(4 * n));
         d32_ = (float *)chk(A(4 * n));
@@ -1641,6 +1645,8 @@ cudaError_t MGSolver::build_hierarchy() {
         if (split0_) {
             k_to_split<<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(lev_dims_[0], c64_[0], c32_, c16s0_,
                                                                                 rows_[0]);
+            k_rows_uniform<<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(lev_dims_[0], c32_, rows_[0], crow_);
+            tk_.launches++;
             // rows that hold no active cell are skipped by every level-l kernel; their vector entries must be
             // zero, and stay so
             cudaMemsetAsync(z32_, 0, 4 * (size_t)lev_dims_[0].n, st_);
@@ -1656,16 +1662,21 @@ cudaError_t MGSolver::build_hierarchy() {
                 k_rows_list<<<1, 1024, 0, st_>>>((long long)lev_dims_[l].nx * lev_dims_[l].ny, rows_[l], list_[l],
                                                  count_ + l);
             tk_.launches += L - 1 + 2;
-            tk_.frac0 = 1.0;
-            if (prm_.profile) {  // profiled runs synchronise anyway: count the active level-0 rows
+            tk_.bytes0 = -1;
+            if (prm_.profile) {  // profiled runs synchronise anyway: count the level-0 rows by kind
                 const Dims &d0 = lev_dims_[0];
                 std::vector<uint8_t> h((size_t)d0.nx * d0.ny);
                 cudaMemcpyAsync(h.data(), rows_[0], h.size(), cudaMemcpyDeviceToHost, st_);
                 const cudaError_t e = cudaStreamSynchronize(st_);
                 if (e != cudaSuccess) return e;
-                long long on = 0;
-                for (uint8_t v : h) on += v ? 1 : 0;
-                tk_.frac0 = h.empty() ? 1.0 : (double)on / (double)h.size();
+                long long gen = 0, uni = 0;
+                for (uint8_t v : h) {
+                    gen += v == 1;
+                    uni += v == 2;
+                }
+                // algorithmic bytes of a half sweep per grid cell: 10 on a general row (x r/w, b, 3 couplings
+                // and the excess, half of each), 6 on a uniform row (x r/w and b)
+                tk_.bytes0 = (10.0 * gen + 6.0 * uni) * d0.nz;
             }
         } else {
             k_to32<<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0].n, c64_[0], c32_);
@@ -1710,7 +1721,7 @@ void MGSolver::enqueue_iter32() {
     const std::vector<float *> ts = prm_.smoother == 1 ? t32_ : std::vector<float *>(t32_.size(), nullptr);
     if (split0_) {
         // colour-split level 0 with row flags on every level (vectors in split rows, inactive rows skipped)
-        const RowSets rs{&rows_, {list_[0], list_[1]}, {count_, count_ + 1}};
+        const RowSets rs{&rows_, {list_[0], list_[1]}, {count_, count_ + 1}, crow_};
         const int *lst0 = list_[0], *cnt0 = count_;
         vcycle<float, float, __half, __half>(st_, tk_, lev_dims_, c32_, c16s0_, c16_, z32_, ri32_, x32_, b32_, ts,
                                              prm_, true, &rs);
@@ -1718,7 +1729,7 @@ void MGSolver::enqueue_iter32() {
         k_dot_rz_s<<<row_grid((const void *)k_dot_rz_s, vitems), dim3(32, 8), 0, st_>>>(d, ri32_, z32_, q32_, lst0, cnt0,
                                                                                        1, sc_, part_, ticket_);
         k_xpby_s<<<row_grid((const void *)k_xpby_s, vitems), dim3(32, 8), 0, st_>>>(d, z32_, p32_, lst0, cnt0, sc_);
-        apply_dot32s(st_, d, c32_, p32_, q32_, lst0, cnt0, sc_, part_, ticket_);
+        apply_dot32s(st_, d, c32_, p32_, q32_, lst0, cnt0, crow_, sc_, part_, ticket_);
         k_update_s<<<row_grid((const void *)k_update_s, vitems), dim3(32, 8), 0, st_>>>(d, d32_, ri32_, p32_, q32_, lst0,
                                                                                       cnt0, sc_, part_, ticket_);
         tk_.launches += 4;
@@ -1983,7 +1994,7 @@ cudaError_t MGSolver::set_guess_scaled(const float *y, double &gamma) {
     if (split0_) {
         // scratch: q32 and p32, cleared before the solve's first inner iteration
         k_vec_to_split<<<split_rows_grid(d), dim3(32, 8), 0, st_>>>(d, y, q32_);
-        apply_dot32s(st_, d, c32_, q32_, p32_, list_[0], count_, sc_, part_, ticket_);
+        apply_dot32s(st_, d, c32_, q32_, p32_, list_[0], count_, crow_, sc_, part_, ticket_);
         tk_.launches++;
     } else {
         apply_dot32(st_, d, c32_, y, q32_, sc_, part_, ticket_);

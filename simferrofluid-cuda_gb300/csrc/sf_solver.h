@@ -37,9 +37,9 @@ struct Tracker {
     std::vector<cudaEvent_t> ev;
     size_t used = 0;
     double bytes = 0;
-    // profile: fraction of level-0 rows holding an active cell (split level with row flags: a half sweep
-    // processes only those rows, and its algorithmic bytes are counted for them)
-    double frac0 = 1.0;
+    // profile: algorithmic bytes of one split level-0 half sweep, counted over the rows it processes and by row
+    // kind (-1: not set, every cell at the general rate)
+    double bytes0 = -1;
     void before(cudaStream_t st, bool fine);
     void after(cudaStream_t st, bool fine, double algo_bytes);
     // after a stream sync: summed milliseconds, launch count and algorithmic bytes of the bracketed
@@ -147,6 +147,7 @@ class MGSolver {
     std::vector<uint8_t *> rows_;
     int *list_[2] = {nullptr, nullptr};  // ordered active rows of levels 0 and 1
     int *count_ = nullptr;               // their counts (device)
+    float *crow_ = nullptr;              // level 0: the coupling of each uniform row
     std::vector<float *> x32_, b32_, t32_;
 
     double *x_ = nullptr, *b_ = nullptr;

@@ -47,7 +47,7 @@ static inline int split_rows_grid(const Dims &d) {
 }
 
 // Ordered list of a level's active rows (one block of 1024 threads): list[0 .. *count) holds, ascending, the rows
-// r with rows[r] != 0.
+// r with rows[r] != 0, with bit 31 set on uniform rows (flag 2).
 __global__ void __launch_bounds__(1024) k_rows_list(long long nrows, const uint8_t *__restrict__ rows,
                                                      int *__restrict__ list, int *__restrict__ count) {
     __shared__ int sh[1024];
@@ -66,14 +66,14 @@ __global__ void __launch_bounds__(1024) k_rows_list(long long nrows, const uint8
     }
     int pos = sh[t] - c;
     for (long long r = r0; r < r1; r++)
-        if (rows[r]) list[pos++] = (int)r;
+        if (rows[r]) list[pos++] = (int)((unsigned)r | (rows[r] == 2 ? 0x80000000u : 0u));
     if (t == 1023) *count = sh[1023];
 }
 
 // Persistent loop of a grid's warps (blockDim = (32, 8)) over the items (rep, list entry, chunk): `reps` passes
 // (colours) over the *count listed rows, `nch` chunks of 32 lanes per row; warp w takes items w, w + W, ...
 // Every warp gets an equal share of the active rows, and the assignment depends only on the grid and the list,
-// so reductions stay deterministic.  f(rep, row, chunk).
+// so reductions stay deterministic.  f(rep, row, chunk, uniform).
 template <class F>
 __device__ __forceinline__ void for_list_items(const int *__restrict__ list, const int *__restrict__ count, int reps,
                                                int nch, F &&f) {
@@ -83,7 +83,8 @@ __device__ __forceinline__ void for_list_items(const int *__restrict__ list, con
         const long long rr = it / nch;
         const int ch = (int)(it - rr * nch);
         const int rep = (int)(rr / n);
-        f(rep, list[rr - rep * n], ch);
+        const int e = list[rr - rep * n];
+        f(rep, (long long)(e & 0x7fffffff), ch, e < 0);
     }
 }
 
@@ -157,7 +158,43 @@ __global__ void k_rows_coarsen(Dims df, const uint8_t *__restrict__ rf, Dims dc,
                 const int i = 2 * I + di, j = 2 * J + dj;
                 if (i < df.nx && j < df.ny) a |= rf[(long long)i * df.ny + j];
             }
-        rc[row] = a;
+        rc[row] = a ? 1 : 0;
+    }
+}
+
+// Uniform rows of the split level 0.  An active row (flag 1) becomes uniform (flag 2) when every cell of it has a
+// zero diagonal excess and every in-grid coupling of its cells equals one FP32 value c > 0: the lower x, y, z
+// faces of its cells, their upper z faces (the next cell's lower face, in the row) and their upper x and y
+// faces (the lower faces of rows (i + 1, j) and (i, j + 1)).  Equal FP32 values have equal FP16 roundings, so
+// both copies of the operator are c on the row.  crow[row] = c.  One warp per row.
+__global__ void __launch_bounds__(256) k_rows_uniform(Dims d, Coef<float> o, uint8_t *__restrict__ rows,
+                                                      float *__restrict__ crow) {
+    const int nh = d.nz >> 1;
+    const long long hn = d.n >> 1, nrows = (long long)d.nx * d.ny;
+    for (long long row = blockIdx.x * (long long)blockDim.y + threadIdx.y; row < nrows;
+         row += (long long)gridDim.x * blockDim.y) {
+        if (!rows[row]) continue;
+        const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
+        const int p = (i + j) & 1;
+        const float c = nh > 0 ? o.az[(long long)(p ^ 1) * hn + row * nh] : 0.f;  // lower z face of cell k = 1
+        bool ok = c > 0.f;
+        for (int m = threadIdx.x; m < nh; m += blockDim.x)
+#pragma unroll
+            for (int col = 0; col < 2; col++) {
+                const long long sidx = (long long)col * hn + row * nh + m, oth = (long long)(col ^ 1) * hn;
+                const int k = 2 * m + ((p + col) & 1);
+                ok &= o.dex[sidx] == 0.f;
+                if (k > 0) ok &= o.az[sidx] == c;
+                if (i > 0) ok &= o.ax[sidx] == c;
+                if (j > 0) ok &= o.ay[sidx] == c;
+                if (i < d.nx - 1) ok &= o.ax[oth + (row + d.ny) * nh + m] == c;
+                if (j < d.ny - 1) ok &= o.ay[oth + (row + 1) * nh + m] == c;
+            }
+        ok = __all_sync(0xffffffffu, ok);
+        if (threadIdx.x == 0) {
+            crow[row] = c;
+            if (ok) rows[row] = 2;
+        }
     }
 }
 
@@ -193,7 +230,7 @@ __global__ void __launch_bounds__(256) k_ir_update_s(Dims d, double *__restrict_
                                                      const int *__restrict__ list, const int *__restrict__ count) {
     const int nh = d.nz >> 1;
     const long long hn = d.n >> 1;
-    for_list_items(list, count, 1, (nh + 31) / 32, [&](int, long long row, int ch) {
+    for_list_items(list, count, 1, (nh + 31) / 32, [&](int, long long row, int ch, bool) {
         const int m = ch * 32 + threadIdx.x;
         if (m >= nh) return;
         const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
@@ -211,7 +248,7 @@ template <class F>
 __device__ __forceinline__ void for_vec_rows(const Dims &d, const int *list, const int *count, F &&f) {
     const int nq = d.nz >> 3;  // float4 per row of a colour
     const long long nrows = (long long)d.nx * d.ny;
-    for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, long long row, int ch) {
+    for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, long long row, int ch, bool) {
         const int t = ch * 32 + threadIdx.x;
         if (t < nq) f((col * nrows + row) * nq + t);
     });
@@ -315,6 +352,147 @@ struct Cv4<__half> {
     }
 };
 
+
+// Uniform rows (every in-grid coupling c, no excess; k_rows_uniform): the operator is c times the graph
+// Laplacian of the in-grid faces, so no coefficient is loaded.  A cell with n in-grid faces has D = c n (exact:
+// the general path's sum of n copies of c is exact too), neighbour sum s = sum x_nb in the general path's face
+// order, and c s in place of sum c x_nb.  c_of returns the value the given copy holds (FP16 rounding, unscaled).
+template <class C>
+__device__ __forceinline__ float c_of(const Coef<C> &cf, float c32) {
+    if (sizeof(C) == 2) return __half2float(__float2half_rn(c32)) * cf.unscale;
+    return c32;
+}
+
+// Loads of a uniform-row update: the other colour's x around the colour-`col` cells m0 .. m0 + 3 of row (i, j).
+struct Nb4 {
+    float xm[4] = {0, 0, 0, 0}, xp[4] = {0, 0, 0, 0}, ym[4] = {0, 0, 0, 0}, yp[4] = {0, 0, 0, 0}, zo[4] = {0, 0, 0, 0};
+    float zx = 0.f;  // the other colour's entry just outside the vector (m0 - 1 for even k, m0 + 4 for odd)
+};
+__device__ __forceinline__ void load_nb4(const Dims &d, const float *__restrict__ x, long long oth, int i, int j,
+                                         int m0, int qz, Nb4 &v) {
+    const int nh = d.nz >> 1;
+    const long long sx = (long long)d.ny * nh, sy = nh;
+    if (i > 0) ld4(x + oth - sx, v.xm);
+    if (i < d.nx - 1) ld4(x + oth + sx, v.xp);
+    if (j > 0) ld4(x + oth - sy, v.ym);
+    if (j < d.ny - 1) ld4(x + oth + sy, v.yp);
+    ld4(x + oth, v.zo);
+    if (qz == 0) {
+        if (m0 > 0) v.zx = x[oth - 1];
+    } else if (m0 + 4 < nh) {
+        v.zx = x[oth + 4];
+    }
+}
+// sum of the in-grid neighbours of cell t (face order of the general path) and their count
+template <int QZ, int t>
+__device__ __forceinline__ void nb_sum(const Dims &d, const Nb4 &v, int i, int j, int m0, bool use_x, float &s,
+                                       float &n) {
+    const int k = 2 * (m0 + t) + QZ;
+    s = 0.f;
+    n = 0.f;
+    if (i > 0) {
+        if (use_x) s += v.xm[t];
+        n += 1.f;
+    }
+    if (i < d.nx - 1) {
+        if (use_x) s += v.xp[t];
+        n += 1.f;
+    }
+    if (j > 0) {
+        if (use_x) s += v.ym[t];
+        n += 1.f;
+    }
+    if (j < d.ny - 1) {
+        if (use_x) s += v.yp[t];
+        n += 1.f;
+    }
+    if (k > 0) {
+        if (use_x) s += QZ == 0 ? (t == 0 ? v.zx : v.zo[t == 0 ? 0 : t - 1]) : v.zo[t];
+        n += 1.f;
+    }
+    if (k < d.nz - 1) {
+        if (use_x) s += QZ == 0 ? v.zo[t] : (t == 3 ? v.zx : v.zo[t == 3 ? 3 : t + 1]);
+        n += 1.f;
+    }
+}
+template <class Fn>
+__device__ __forceinline__ void for_cells4(int qz, Fn &&fn) {
+    auto body = [&](auto qc) {
+        constexpr int QZ = decltype(qc)::value;
+        fn(qc, std::integral_constant<int, 0>{});
+        fn(qc, std::integral_constant<int, 1>{});
+        fn(qc, std::integral_constant<int, 2>{});
+        fn(qc, std::integral_constant<int, 3>{});
+        (void)QZ;
+    };
+    if (qz == 0)
+        body(std::integral_constant<int, 0>{});
+    else
+        body(std::integral_constant<int, 1>{});
+}
+
+template <bool ZERO>
+__device__ __forceinline__ void rbgs4s_uniform(const Dims &d, float c, float *__restrict__ x,
+                                               const float *__restrict__ b, int col, int i, int j, int m0) {
+    const int nh = d.nz >> 1;
+    const long long row = ((long long)i * d.ny + j) * nh + m0;
+    const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
+    const int qz = (i + j + col) & 1;
+    float bv[4], out[4];
+    ld4(b + own, bv);
+    Nb4 v;
+    if (!ZERO) load_nb4(d, x, oth, i, j, m0, qz, v);
+    for_cells4(qz, [&](auto qc, auto tc) {
+        constexpr int QZ = decltype(qc)::value, t = decltype(tc)::value;
+        float s, n;
+        nb_sum<QZ, t>(d, v, i, j, m0, !ZERO, s, n);
+        const float D = c * n;
+        const float inv = D > 0.f ? 1.f / D : 0.f;
+        out[t] = (bv[t] + c * s) * inv;
+    });
+    *reinterpret_cast<float4 *>(x + own) = make_float4(out[0], out[1], out[2], out[3]);
+}
+
+__device__ __forceinline__ void resid4_uniform(const Dims &d, float c, const float *__restrict__ x,
+                                               const float *__restrict__ b, int col, int i, int j, int m0,
+                                               float (&r)[4]) {
+    const int nh = d.nz >> 1;
+    const long long row = ((long long)i * d.ny + j) * nh + m0;
+    const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
+    const int qz = (i + j + col) & 1;
+    float xc[4], bv[4];
+    ld4(x + own, xc);
+    ld4(b + own, bv);
+    Nb4 v;
+    load_nb4(d, x, oth, i, j, m0, qz, v);
+    for_cells4(qz, [&](auto qc, auto tc) {
+        constexpr int QZ = decltype(qc)::value, t = decltype(tc)::value;
+        float s, n;
+        nb_sum<QZ, t>(d, v, i, j, m0, true, s, n);
+        r[t] = (bv[t] - (c * n) * xc[t]) + c * s;
+    });
+}
+
+__device__ __forceinline__ void apply4s_uniform(const Dims &d, float c, const float *__restrict__ p,
+                                                float *__restrict__ q, int col, int i, int j, int m0, float &acc) {
+    const int nh = d.nz >> 1;
+    const long long row = ((long long)i * d.ny + j) * nh + m0;
+    const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
+    const int qz = (i + j + col) & 1;
+    float pc[4], out[4];
+    ld4(p + own, pc);
+    Nb4 v;
+    load_nb4(d, p, oth, i, j, m0, qz, v);
+    for_cells4(qz, [&](auto qc, auto tc) {
+        constexpr int QZ = decltype(qc)::value, t = decltype(tc)::value;
+        float s, n;
+        nb_sum<QZ, t>(d, v, i, j, m0, true, s, n);
+        out[t] = (c * n) * pc[t] - c * s;
+        acc += pc[t] * out[t];
+    });
+    *reinterpret_cast<float4 *>(q + own) = make_float4(out[0], out[1], out[2], out[3]);
+}
+
 // Red-black half sweep of colour `col` in the split layout (the counterpart of k_rbgs4), on the four
 // colour-`col` cells m0 .. m0 + 3 of row (i, j); QZ = (i + j + col) & 1 is uniform over a warp (one row) and
 // selects where the z neighbours sit.
@@ -416,13 +594,17 @@ __device__ __forceinline__ void rbgs4s_cells(const Dims &d, const Coef<C> &cf, f
 // Persistent half sweep: warps over the active rows' chunks of 32 vectors.
 template <class C, bool ZERO>
 __global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__restrict__ x, const float *__restrict__ b,
-                                                int col, const int *__restrict__ list, const int *__restrict__ count) {
+                                                int col, const int *__restrict__ list, const int *__restrict__ count,
+                                                const float *__restrict__ crow) {
     const int nq = d.nz >> 3;
-    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long row, int ch) {
+    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long row, int ch, bool uni) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
         const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
-        rbgs4s_cells<C, ZERO>(d, cf, x, b, col, i, j, 4 * q4);
+        if (uni)
+            rbgs4s_uniform<ZERO>(d, c_of(cf, crow[row]), x, b, col, i, j, 4 * q4);
+        else
+            rbgs4s_cells<C, ZERO>(d, cf, x, b, col, i, j, 4 * q4);
     });
 }
 
@@ -525,7 +707,7 @@ template <class C>
 __device__ __forceinline__ void resid_restrict_s_cells(const Dims &d, const Coef<C> &cf, const float *__restrict__ x,
                                                        const float *__restrict__ b, const Dims &dc,
                                                        float *__restrict__ bc, const uint8_t *__restrict__ rows,
-                                                       int I, int J, int K0) {
+                                                       const float *__restrict__ crow, int I, int J, int K0) {
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     for (int di = 0; di < 2; di++) {
         const int i = 2 * I + di;
@@ -535,7 +717,11 @@ __device__ __forceinline__ void resid_restrict_s_cells(const Dims &d, const Coef
             if (j >= d.ny) break;
             if (!row_on(rows, d, i, j)) continue;  // residual zero
             float r[4];
-            resid4_split<C>(d, cf, x, b, 0, i, j, K0, r);
+            const long long fr = (long long)i * d.ny + j;
+            if (rows && rows[fr] == 2)
+                resid4_uniform(d, c_of(cf, crow[fr]), x, b, 0, i, j, K0, r);
+            else
+                resid4_split<C>(d, cf, x, b, 0, i, j, K0, r);
 #pragma unroll
             for (int t = 0; t < 4; t++) acc[t] += r[t];
         }
@@ -547,14 +733,15 @@ template <class C>
 __global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, const float *__restrict__ x,
                                                              const float *__restrict__ b, Dims dc,
                                                              float *__restrict__ bc, const uint8_t *__restrict__ rows,
+                                                             const float *__restrict__ crow,
                                                              const int *__restrict__ list_c,
                                                              const int *__restrict__ count_c) {
     const int nq = dc.nz >> 2;  // coarse float4 per row (dc.nz = nz / 2, a multiple of 4)
-    for_list_items(list_c, count_c, 1, (nq + 31) / 32, [&](int, long long row, int ch) {
+    for_list_items(list_c, count_c, 1, (nq + 31) / 32, [&](int, long long row, int ch, bool) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
         const int I = (int)(row / dc.ny), J = (int)(row - (long long)I * dc.ny);
-        resid_restrict_s_cells<C>(d, cf, x, b, dc, bc, rows, I, J, 4 * q4);
+        resid_restrict_s_cells<C>(d, cf, x, b, dc, bc, rows, crow, I, J, 4 * q4);
     });
 }
 
@@ -563,7 +750,7 @@ __global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, co
 __global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x, Dims dc, const float *__restrict__ xc,
                                                    const int *__restrict__ list, const int *__restrict__ count) {
     const int nh = d.nz >> 1, nq = nh >> 2;
-    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long r, int ch) {
+    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long r, int ch, bool) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
         const int i = (int)(r / d.ny), j = (int)(r - (long long)i * d.ny), m0 = 4 * q4;
@@ -588,14 +775,18 @@ __global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x
 // (q stays zero there).
 __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, const float *__restrict__ p,
                                                      float *__restrict__ q, const int *__restrict__ list,
-                                                     const int *__restrict__ count, double *sc, double *part,
-                                                     unsigned *ticket) {
+                                                     const int *__restrict__ count, const float *__restrict__ crow,
+                                                     double *sc, double *part, unsigned *ticket) {
     float acc = 0.f;
     const int nh = d.nz >> 1, nq = nh >> 2;
-    for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, long long rw, int ch) {
+    for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, long long rw, int ch, bool uni) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
         const int i = (int)(rw / d.ny), j = (int)(rw - (long long)i * d.ny), m0 = 4 * q4;
+        if (uni) {
+            apply4s_uniform(d, crow[rw], p, q, col, i, j, m0, acc);
+            return;
+        }
         const long long sx = (long long)d.ny * nh, sy = nh;
         const bool yl = j > 0, yu = j < d.ny - 1;
         {
@@ -687,7 +878,8 @@ __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, 
 static inline long long split_items(long long nrows, int nq) { return nrows * ((nq + 31) / 32); }
 
 static void apply_dot32s(cudaStream_t st, const Dims &d, const Coef<float> &cf, const float *p, float *q,
-                         const int *list, const int *count, double *sc, double *part, unsigned *ticket) {
+                         const int *list, const int *count, const float *crow, double *sc, double *part,
+                         unsigned *ticket) {
     const int g = row_grid((const void *)k_apply_dot4s, split_items(2LL * d.nx * d.ny, d.nz >> 3));
-    k_apply_dot4s<<<g, dim3(32, 8), 0, st>>>(d, cf, p, q, list, count, sc, part, ticket);
+    k_apply_dot4s<<<g, dim3(32, 8), 0, st>>>(d, cf, p, q, list, count, crow, sc, part, ticket);
 }
