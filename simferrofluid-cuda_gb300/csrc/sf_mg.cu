@@ -1599,6 +1599,7 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
             for (int l = 0; l < 2; l++) list_[l] = (int *)chk(A(4 * (size_t)dims[l].nx * dims[l].ny));
             count_ = (int *)chk(A(8));
             crow_ = (float *)chk(A(4 * (size_t)dims[0].nx * dims[0].ny));
+            list_cnt_ = (int *)chk(A(8 * (((size_t)dims[0].nx * dims[0].ny + kListRows - 1) / kListRows)));
         }
         r32_ = (float *)chk(A(4 * n));
         d32_ = (float *)chk(A(4 * n));
@@ -1658,10 +1659,13 @@ cudaError_t MGSolver::build_hierarchy() {
                 cudaMemsetAsync(x32_[l], 0, 4 * (size_t)dl.n, st_);
                 cudaMemsetAsync(b32_[l], 0, 4 * (size_t)dl.n, st_);
             }
-            for (int l = 0; l < 2; l++)
-                k_rows_list<<<1, 1024, 0, st_>>>((long long)lev_dims_[l].nx * lev_dims_[l].ny, rows_[l], list_[l],
-                                                 count_ + l);
-            tk_.launches += L - 1 + 2;
+            for (int l = 0; l < 2; l++) {
+                const long long nr = (long long)lev_dims_[l].nx * lev_dims_[l].ny;
+                const int nb = (int)((nr + kListRows - 1) / kListRows);
+                k_rows_count<<<nb, kListRows, 0, st_>>>(nr, rows_[l], list_cnt_);
+                k_rows_scatter<<<nb, kListRows, 0, st_>>>(nr, rows_[l], list_cnt_, list_[l], count_ + l);
+            }
+            tk_.launches += L - 1 + 4;
             tk_.bytes0 = -1;
             if (prm_.profile) {  // profiled runs synchronise anyway: count the level-0 rows by kind
                 const Dims &d0 = lev_dims_[0];

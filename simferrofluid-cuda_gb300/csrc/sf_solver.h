@@ -148,6 +148,7 @@ class MGSolver {
     int *list_[2] = {nullptr, nullptr};  // ordered active rows of levels 0 and 1
     int *count_ = nullptr;               // their counts (device)
     float *crow_ = nullptr;              // level 0: the coupling of each uniform row
+    int *list_cnt_ = nullptr;            // per block of rows: general and uniform counts (list building)
     std::vector<float *> x32_, b32_, t32_;
 
     double *x_ = nullptr, *b_ = nullptr;

@@ -46,28 +46,66 @@ static inline int split_rows_grid(const Dims &d) {
     return (int)(g < 1 ? 1 : g);
 }
 
-// Ordered list of a level's active rows (one block of 1024 threads): list[0 .. *count) holds, ascending, the rows
-// r with rows[r] != 0, with bit 31 set on uniform rows (flag 2).
-__global__ void __launch_bounds__(1024) k_rows_list(long long nrows, const uint8_t *__restrict__ rows,
-                                                     int *__restrict__ list, int *__restrict__ count) {
-    __shared__ int sh[1024];
-    const int t = threadIdx.x;
-    const long long per = (nrows + 1023) / 1024;
-    const long long r0 = t * per, r1 = r0 + per < nrows ? r0 + per : nrows;
-    int c = 0;
-    for (long long r = r0; r < r1; r++) c += rows[r] != 0;
-    sh[t] = c;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {  // inclusive scan
-        const int v = t >= off ? sh[t - off] : 0;
-        __syncthreads();
-        sh[t] += v;
-        __syncthreads();
+// List of a level's active rows, in two segments: the general rows (flag 1) in ascending order, then the uniform
+// rows (flag 2) in ascending order, with bit 31 set; *count = their number.  Rows of one segment cost the same,
+// so the persistent kernels' round-robin split of the list gives every warp an equal share of each kind.
+// Two kernels over blocks of 1024 rows: per-block counts of each kind, then each block's entries at the offsets
+// the counts give (deterministic).
+constexpr int kListRows = 1024;
+__global__ void __launch_bounds__(kListRows) k_rows_count(long long nrows, const uint8_t *__restrict__ rows,
+                                                          int *__restrict__ cnt) {
+    const long long r = blockIdx.x * (long long)kListRows + threadIdx.x;
+    const uint8_t f = r < nrows ? rows[r] : 0;
+    const int g = __syncthreads_count(f == 1), u = __syncthreads_count(f == 2);
+    if (threadIdx.x == 0) {
+        cnt[2 * blockIdx.x] = g;
+        cnt[2 * blockIdx.x + 1] = u;
     }
-    int pos = sh[t] - c;
-    for (long long r = r0; r < r1; r++)
-        if (rows[r]) list[pos++] = (int)((unsigned)r | (rows[r] == 2 ? 0x80000000u : 0u));
-    if (t == 1023) *count = sh[1023];
+}
+__global__ void __launch_bounds__(kListRows) k_rows_scatter(long long nrows, const uint8_t *__restrict__ rows,
+                                                            const int *__restrict__ cnt, int *__restrict__ list,
+                                                            int *__restrict__ count) {
+    __shared__ int wg[32], wu[32], off[2];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if (w == 0) {  // offsets of this block's general and uniform entries, and the total
+        int g_before = 0, u_before = 0, g_all = 0, u_all = 0;
+        for (int b = lane; b < (int)gridDim.x; b += 32) {
+            const int g = cnt[2 * b], u = cnt[2 * b + 1];
+            g_all += g;
+            u_all += u;
+            if (b < (int)blockIdx.x) {
+                g_before += g;
+                u_before += u;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            g_before += __shfl_xor_sync(0xffffffffu, g_before, o);
+            u_before += __shfl_xor_sync(0xffffffffu, u_before, o);
+            g_all += __shfl_xor_sync(0xffffffffu, g_all, o);
+            u_all += __shfl_xor_sync(0xffffffffu, u_all, o);
+        }
+        if (lane == 0) {
+            off[0] = g_before;
+            off[1] = g_all + u_before;
+            if (blockIdx.x == 0) *count = g_all + u_all;
+        }
+    }
+    const long long r = blockIdx.x * (long long)kListRows + t;
+    const uint8_t f = r < nrows ? rows[r] : 0;
+    const unsigned bg = __ballot_sync(0xffffffffu, f == 1), bu = __ballot_sync(0xffffffffu, f == 2);
+    if (lane == 0) {
+        wg[w] = __popc(bg);
+        wu[w] = __popc(bu);
+    }
+    __syncthreads();
+    int pg = off[0], pu = off[1];
+    for (int q = 0; q < w; q++) {
+        pg += wg[q];
+        pu += wu[q];
+    }
+    const unsigned below = (1u << lane) - 1u;
+    if (f == 1) list[pg + __popc(bg & below)] = (int)r;
+    if (f == 2) list[pu + __popc(bu & below)] = (int)((unsigned)r | 0x80000000u);
 }
 
 // Persistent loop of a grid's warps (blockDim = (32, 8)) over the items (rep, list entry, chunk): `reps` passes
@@ -79,12 +117,14 @@ __device__ __forceinline__ void for_list_items(const int *__restrict__ list, con
                                                int nch, F &&f) {
     const long long n = *count;
     const long long nit = (long long)reps * n * nch, stride = (long long)gridDim.x * blockDim.y;
-    for (long long it = blockIdx.x * (long long)blockDim.y + threadIdx.y; it < nit; it += stride) {
+    auto entry = [&](long long it) { return it < nit ? list[(it / nch) % n] : 0; };
+    long long it = blockIdx.x * (long long)blockDim.y + threadIdx.y;
+    int e = entry(it);
+    for (; it < nit; it += stride) {
+        const int e_next = entry(it + stride);  // issued before this item's loads
         const long long rr = it / nch;
-        const int ch = (int)(it - rr * nch);
-        const int rep = (int)(rr / n);
-        const int e = list[rr - rep * n];
-        f(rep, (long long)(e & 0x7fffffff), ch, e < 0);
+        f((int)(rr / n), (long long)(e & 0x7fffffff), (int)(it - rr * nch), e < 0);
+        e = e_next;
     }
 }
 
