@@ -112,18 +112,34 @@ __global__ void __launch_bounds__(kListRows) k_rows_scatter(long long nrows, con
 // (colours) over the *count listed rows, `nch` chunks of 32 lanes per row; warp w takes items w, w + W, ...
 // Every warp gets an equal share of the active rows, and the assignment depends only on the grid and the list,
 // so reductions stay deterministic.  f(rep, row, chunk, uniform).
+// 32-bit item arithmetic (a level has fewer than 2^31 rows); reps is 1 or 2.
 template <class F>
 __device__ __forceinline__ void for_list_items(const int *__restrict__ list, const int *__restrict__ count, int reps,
                                                int nch, F &&f) {
-    const long long n = *count;
-    const long long nit = (long long)reps * n * nch, stride = (long long)gridDim.x * blockDim.y;
-    auto entry = [&](long long it) { return it < nit ? list[(it / nch) % n] : 0; };
-    long long it = blockIdx.x * (long long)blockDim.y + threadIdx.y;
+    const unsigned n = (unsigned)*count;
+    const unsigned nit = reps * n * (unsigned)nch, stride = gridDim.x * blockDim.y;
+    auto split = [&](unsigned it, unsigned &rr, unsigned &ch) {
+        if (nch == 1) {
+            rr = it;
+            ch = 0;
+        } else {
+            rr = it / (unsigned)nch;
+            ch = it - rr * (unsigned)nch;
+        }
+    };
+    auto entry = [&](unsigned it) {
+        if (it >= nit) return 0;
+        unsigned rr, ch;
+        split(it, rr, ch);
+        return list[rr >= n ? rr - n : rr];
+    };
+    unsigned it = blockIdx.x * blockDim.y + threadIdx.y;
     int e = entry(it);
     for (; it < nit; it += stride) {
         const int e_next = entry(it + stride);  // issued before this item's loads
-        const long long rr = it / nch;
-        f((int)(rr / n), (long long)(e & 0x7fffffff), (int)(it - rr * nch), e < 0);
+        unsigned rr, ch;
+        split(it, rr, ch);
+        f(rr >= n ? 1 : 0, (long long)(e & 0x7fffffff), (int)ch, e < 0);
         e = e_next;
     }
 }
@@ -161,7 +177,7 @@ __global__ void __launch_bounds__(256) k_to_split(Dims d, Coef<double> f, Coef<f
     const long long hn = d.n >> 1, nrows = (long long)d.nx * d.ny;
     for (long long row = blockIdx.x * (long long)blockDim.y + threadIdx.y; row < nrows;
          row += (long long)gridDim.x * blockDim.y) {
-        const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
+        const int i = (int)row / d.ny, j = (int)row - i * d.ny;
         const int p = (i + j) & 1;
         const long long nat = row * d.nz, sp = row * nh;
         bool act = false;
@@ -191,7 +207,7 @@ __global__ void k_rows_coarsen(Dims df, const uint8_t *__restrict__ rf, Dims dc,
     const long long nrows = (long long)dc.nx * dc.ny;
     for (long long row = blockIdx.x * (long long)blockDim.x + threadIdx.x; row < nrows;
          row += (long long)gridDim.x * blockDim.x) {
-        const int I = (int)(row / dc.ny), J = (int)(row - (long long)I * dc.ny);
+        const int I = (int)row / dc.ny, J = (int)row - I * dc.ny;
         uint8_t a = 0;
         for (int di = 0; di < 2; di++)
             for (int dj = 0; dj < 2; dj++) {
@@ -214,7 +230,7 @@ __global__ void __launch_bounds__(256) k_rows_uniform(Dims d, Coef<float> o, uin
     for (long long row = blockIdx.x * (long long)blockDim.y + threadIdx.y; row < nrows;
          row += (long long)gridDim.x * blockDim.y) {
         if (!rows[row]) continue;
-        const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
+        const int i = (int)row / d.ny, j = (int)row - i * d.ny;
         const int p = (i + j) & 1;
         const float c = nh > 0 ? o.az[(long long)(p ^ 1) * hn + row * nh] : 0.f;  // lower z face of cell k = 1
         bool ok = c > 0.f;
@@ -273,7 +289,7 @@ __global__ void __launch_bounds__(256) k_ir_update_s(Dims d, double *__restrict_
     for_list_items(list, count, 1, (nh + 31) / 32, [&](int, long long row, int ch, bool) {
         const int m = ch * 32 + threadIdx.x;
         if (m >= nh) return;
-        const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
+        const int i = (int)row / d.ny, j = (int)row - i * d.ny;
         const int p = (i + j) & 1;
         const long long nat = row * d.nz + 2 * m, sp = row * nh + m;
         x[nat + p] += (double)dlt[sp];
@@ -471,6 +487,15 @@ __device__ __forceinline__ void for_cells4(int qz, Fn &&fn) {
         body(std::integral_constant<int, 1>{});
 }
 
+// 1 / (c n) for the row's interior cells (n = the in-grid x and y faces + 2) and for its two end cells (k = 0,
+// k = nz - 1: one z face fewer); c n is exact, as in the general path.
+__device__ __forceinline__ void row_inv(const Dims &d, float c, int i, int j, float &inv_in, float &inv_end) {
+    const float nxy = (float)((i > 0) + (i < d.nx - 1) + (j > 0) + (j < d.ny - 1));
+    const float di = c * (nxy + 2.f), de = c * (nxy + 1.f);
+    inv_in = di > 0.f ? 1.f / di : 0.f;
+    inv_end = de > 0.f ? 1.f / de : 0.f;
+}
+
 template <bool ZERO>
 __device__ __forceinline__ void rbgs4s_uniform(const Dims &d, float c, float *__restrict__ x,
                                                const float *__restrict__ b, int col, int i, int j, int m0) {
@@ -482,12 +507,14 @@ __device__ __forceinline__ void rbgs4s_uniform(const Dims &d, float c, float *__
     ld4(b + own, bv);
     Nb4 v;
     if (!ZERO) load_nb4(d, x, oth, i, j, m0, qz, v);
+    float inv_in, inv_end;
+    row_inv(d, c, i, j, inv_in, inv_end);
     for_cells4(qz, [&](auto qc, auto tc) {
         constexpr int QZ = decltype(qc)::value, t = decltype(tc)::value;
         float s, n;
         nb_sum<QZ, t>(d, v, i, j, m0, !ZERO, s, n);
-        const float D = c * n;
-        const float inv = D > 0.f ? 1.f / D : 0.f;
+        const int k = 2 * (m0 + t) + QZ;
+        const float inv = (k == 0 || k == d.nz - 1) ? inv_end : inv_in;
         out[t] = (bv[t] + c * s) * inv;
     });
     *reinterpret_cast<float4 *>(x + own) = make_float4(out[0], out[1], out[2], out[3]);
@@ -640,7 +667,7 @@ __global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__
     for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long row, int ch, bool uni) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
-        const int i = (int)(row / d.ny), j = (int)(row - (long long)i * d.ny);
+        const int i = (int)row / d.ny, j = (int)row - i * d.ny;
         if (uni)
             rbgs4s_uniform<ZERO>(d, c_of(cf, crow[row]), x, b, col, i, j, 4 * q4);
         else
@@ -780,7 +807,7 @@ __global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, co
     for_list_items(list_c, count_c, 1, (nq + 31) / 32, [&](int, long long row, int ch, bool) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
-        const int I = (int)(row / dc.ny), J = (int)(row - (long long)I * dc.ny);
+        const int I = (int)row / dc.ny, J = (int)row - I * dc.ny;
         resid_restrict_s_cells<C>(d, cf, x, b, dc, bc, rows, crow, I, J, 4 * q4);
     });
 }
@@ -793,7 +820,7 @@ __global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x
     for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long r, int ch, bool) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
-        const int i = (int)(r / d.ny), j = (int)(r - (long long)i * d.ny), m0 = 4 * q4;
+        const int i = (int)r / d.ny, j = (int)r - i * d.ny, m0 = 4 * q4;
         float v[4];
         ld4(xc + cid(dc, i >> 1, j >> 1, m0), v);
         const long long row = r * nh + m0;
@@ -822,7 +849,7 @@ __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, 
     for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, long long rw, int ch, bool uni) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
-        const int i = (int)(rw / d.ny), j = (int)(rw - (long long)i * d.ny), m0 = 4 * q4;
+        const int i = (int)rw / d.ny, j = (int)rw - i * d.ny, m0 = 4 * q4;
         if (uni) {
             apply4s_uniform(d, crow[rw], p, q, col, i, j, m0, acc);
             return;
