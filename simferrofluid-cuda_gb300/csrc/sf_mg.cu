@@ -1689,7 +1689,9 @@ cudaError_t MGSolver::build_hierarchy() {
                 tk_.launches++;
             }
         }
-        if (L > 1)
+        if (split0_)  // from the split FP32 copy (half the bytes of the FP64 operator, FP32 sums)
+            k_coarsen_s<<<grid_cells(lev_dims_[1]), blk2(), 0, st_>>>(lev_dims_[0], c32_, lev_dims_[1], c16_[1]);
+        else if (L > 1)
             k_coarsen<double, __half><<<grid_cells(lev_dims_[1]), blk2(), 0, st_>>>(lev_dims_[0], c64_[0],
                                                                                     lev_dims_[1], c16_[1]);
         for (int l = 2; l < L; l++)

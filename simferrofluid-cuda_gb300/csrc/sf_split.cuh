@@ -941,6 +941,40 @@ __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, 
     }
 }
 
+// Level 1 of the mixed form (FP16, scaled) from the split FP32 level 0: A_c = 1/2 P^T A P as k_coarsen forms
+// it (a coarse face is half the sum of its four fine faces, a coarse excess half the sum of its eight children's),
+// summed in FP32 from the FP32 copy instead of FP64 from the FP64 operator (the result is stored in FP16).  Fine
+// row (i, j) holds both children k = 2K, 2K + 1 of coarse cell K at m = K: colour (i + j) & 1 for k = 2K.
+__global__ void __launch_bounds__(256) k_coarsen_s(Dims d, Coef<float> f, Dims dc, Coef<__half> cc) {
+    const int K = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int I = blockIdx.z;
+    if (K >= dc.nz || J >= dc.ny) return;
+    const int nh = d.nz >> 1;
+    const long long hn = d.n >> 1;
+    // entry m = K of colour col in fine row (i, j)
+    auto at = [&](const float *a, int col, int i, int j) { return a[(long long)col * hn + ((long long)i * d.ny + j) * nh + K]; };
+    float fx = 0.f, fy = 0.f, fz = 0.f, dex = 0.f;
+    for (int u = 0; u < 2; u++)
+        for (int v = 0; v < 2; v++) {
+            // lower x faces of fine cells (2I, 2J + u, 2K + v); lower y faces of (2I + u, 2J, 2K + v)
+            if (I > 0 && 2 * J + u < d.ny) fx += at(f.ax, (u + v) & 1, 2 * I, 2 * J + u);
+            if (J > 0 && 2 * I + u < d.nx) fy += at(f.ay, (u + v) & 1, 2 * I + u, 2 * J);
+            // lower z faces of fine cells (2I + u, 2J + v, 2K): colour (u + v) & 1
+            if (K > 0 && 2 * I + u < d.nx && 2 * J + v < d.ny) fz += at(f.az, (u + v) & 1, 2 * I + u, 2 * J + v);
+            if (2 * I + u < d.nx && 2 * J + v < d.ny) {
+                dex += at(f.dex, 0, 2 * I + u, 2 * J + v);
+                dex += at(f.dex, 1, 2 * I + u, 2 * J + v);
+            }
+        }
+    const float sc = 0.5f * cc.scale;
+    const long long c = cid(dc, I, J, K);
+    cc.ax[c] = __float2half_rn(fx * sc);
+    cc.ay[c] = __float2half_rn(fy * sc);
+    cc.az[c] = __float2half_rn(fz * sc);
+    cc.dex[c] = __float2half_rn(dex * sc);
+}
+
 // Items of the persistent split kernels: rows x chunks of 32 float4.
 static inline long long split_items(long long nrows, int nq) { return nrows * ((nq + 31) / 32); }
 
