@@ -111,6 +111,30 @@ static inline dim3 grid_pairs(const Dims &d) {
     return dim3(((d.nz + 1) / 2 + 31) / 32, (d.ny + 8 * kRbRows - 1) / (8 * kRbRows), d.nx);
 }
 
+// Programmatic dependent launch.  The kernels of a solver iteration are launched with programmatic stream
+// serialisation allowed (launch_pdl) and begin with pdl_entry(): each lets its successor be scheduled once all of
+// its own blocks are running (launch_dependents), then waits for its predecessor to complete and its writes to be
+// visible (wait) before touching memory.  A successor's blocks thus fill free SM slots during the predecessor's
+// last wave instead of after it; a kernel launched without the attribute passes wait at once.
+__device__ __forceinline__ void pdl_entry() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+template <class... KArgs, class... Args>
+static void launch_pdl(void (*k)(KArgs...), dim3 g, dim3 b, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = b;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 // Row activity: rows[(i * ny + j)] == 0 marks a row (i, j) of the level whose cells are all inactive (D = 0:
 // air in the pressure system).  Kernels given flags skip such rows entirely; every vector of the level is zero
 // there (cleared when the hierarchy is built, never written afterwards), which is what processing them would
@@ -152,6 +176,7 @@ __device__ __forceinline__ T couplings_sum(const Dims &d, const Coef<C> &cf, int
 template <class T, class C, bool ZERO>
 __global__ void __launch_bounds__(256) k_rbgs(Dims d, Coef<C> cf, T *__restrict__ x, const T *__restrict__ b,
                                               int color, const uint8_t *__restrict__ rows = nullptr) {
+    pdl_entry();
     const int kp = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.z;
     const int j0 = blockIdx.y * (8 * kRbRows) + threadIdx.y;
@@ -213,6 +238,7 @@ __device__ __forceinline__ void ld4(const __half *p, float (&v)[4]) {
 template <class C, bool ZERO>
 __global__ void __launch_bounds__(256) k_rbgs4(Dims d, Coef<C> cf, float *__restrict__ x, const float *__restrict__ b,
                                                int color, const uint8_t *__restrict__ rows = nullptr) {
+    pdl_entry();
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -668,6 +694,7 @@ __global__ void __launch_bounds__(256) k_resid_restrict(Dims d, Coef<C> cf, cons
                                                         const T *__restrict__ b, Dims dc, T *__restrict__ bc,
                                                         const uint8_t *__restrict__ rows = nullptr,
                                                         const uint8_t *__restrict__ rows_c = nullptr) {
+    pdl_entry();
     const int K = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int I = blockIdx.z;
@@ -701,6 +728,7 @@ __global__ void __launch_bounds__(256) k_resid_restrict(Dims d, Coef<C> cf, cons
 template <class T>
 __global__ void __launch_bounds__(256) k_prolong(Dims d, T *__restrict__ x, Dims dc, const T *__restrict__ xc,
                                                  const uint8_t *__restrict__ rows = nullptr) {
+    pdl_entry();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -716,6 +744,7 @@ constexpr int kCoarseMax = 1024, kCoarseThreads = 1024;
 template <class T, class C>
 __global__ void __launch_bounds__(kCoarseThreads) k_coarse_smem(Dims d, Coef<C> cf, T *__restrict__ x,
                                                                 const T *__restrict__ b, int pairs) {
+    pdl_entry();
     using R = typename Acc<C>::T;
     __shared__ T xs[kCoarseMax];
     const int sx = d.ny * d.nz, sy = d.nz;
@@ -765,6 +794,7 @@ __global__ void __launch_bounds__(kCoarseThreads) k_coarse_smem(Dims d, Coef<C> 
 template <class T, class C>
 __global__ void __launch_bounds__(1024) k_coarse(Dims d, Coef<C> cf, T *__restrict__ x, const T *__restrict__ b,
                                                  int pairs) {
+    pdl_entry();
     for (long long c = threadIdx.x; c < d.n; c += blockDim.x) x[c] = T(0);
     __syncthreads();
     const int nh = 1 + 2 * pairs;
@@ -900,6 +930,7 @@ __global__ void k_to16(long long n, Coef<double> f, Coef<__half> o) {
 template <class T, class C>
 __global__ void __launch_bounds__(256) k_apply_dot(Dims d, int xpb, Coef<C> cf, const T *__restrict__ p,
                                                    T *__restrict__ q, double *sc, double *part, unsigned *ticket) {
+    pdl_entry();
     T acc = 0;
     TILE_BLOCK(d, xpb)
     T sa;
@@ -929,6 +960,7 @@ __global__ void __launch_bounds__(256) k_apply_dot(Dims d, int xpb, Coef<C> cf, 
 __global__ void __launch_bounds__(256) k_apply_dot4(Dims d, int xpb, Coef<float> cf, const float *__restrict__ p,
                                                     float *__restrict__ q, double *sc, double *part,
                                                     unsigned *ticket) {
+    pdl_entry();
     float acc = 0.f;
     const int k0 = 4 * (blockIdx.x * 32 + threadIdx.x), j = blockIdx.y * 8 + threadIdx.y;
     if (k0 < d.nz && j < d.ny) {
@@ -1014,11 +1046,11 @@ static void apply_dot32(cudaStream_t st, const Dims &d, const Coef<float> &cf, c
         xpb = (int)((d.nx + zmax - 1) / zmax);
         if (xpb < 2) xpb = 2;
         const dim3 g((d.nz + 127) / 128, (d.ny + 7) / 8, (d.nx + xpb - 1) / xpb);
-        k_apply_dot4<<<g, dim3(32, 8), 0, st>>>(d, xpb, cf, p, q, sc, part, ticket);
+        launch_pdl(k_apply_dot4, g, dim3(32, 8), st, d, xpb, cf, p, q, sc, part, ticket);
         return;
     }
     const dim3 tg = tile_grid3(d, xpb);
-    k_apply_dot<float, float><<<tg, dim3(32, 8), 0, st>>>(d, xpb, cf, p, q, sc, part, ticket);
+    launch_pdl(k_apply_dot<float, float>, tg, dim3(32, 8), st, d, xpb, cf, p, q, sc, part, ticket);
 }
 
 #include "sf_split.cuh"
@@ -1028,6 +1060,7 @@ template <class T>
 __global__ void __launch_bounds__(256) k_dot_rz(long long n, const T *__restrict__ r, const T *__restrict__ z,
                                                 const T *__restrict__ q, int flexible, double *sc, double *part,
                                                 unsigned *ticket) {
+    pdl_entry();
     T a0 = 0, a1 = 0;
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
@@ -1051,6 +1084,7 @@ __global__ void __launch_bounds__(256) k_dot_rz(long long n, const T *__restrict
 template <class T>
 __global__ void __launch_bounds__(256) k_xpby(long long n, const T *__restrict__ z, T *__restrict__ p,
                                               const double *sc) {
+    pdl_entry();
     const T beta = (T)sc[S_BETA];
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
         p[c] = z[c] + beta * p[c];
@@ -1061,6 +1095,7 @@ template <class T>
 __global__ void __launch_bounds__(256) k_update(long long n, T *__restrict__ x, T *__restrict__ r,
                                                 const T *__restrict__ p, const T *__restrict__ q, double *sc,
                                                 double *part, unsigned *ticket) {
+    pdl_entry();
     const T alpha = (T)sc[S_ALPHA];
     T acc = 0;
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
@@ -1189,17 +1224,17 @@ static void rb(cudaStream_t st, Tracker &tk, bool fine, bool zero, const Dims &d
         if (d.nz % 4 == 0) {  // rows start 16-byte aligned: z-vectorised kernel
             const dim3 g4((d.nz / 4 + 31) / 32, (d.ny + 7) / 8, d.nx);
             if (zero)
-                k_rbgs4<C, true><<<g4, bk, 0, st>>>(d, cf, x, b, color, rows);
+                launch_pdl(k_rbgs4<C, true>, g4, bk, st, d, cf, x, b, color, rows);
             else
-                k_rbgs4<C, false><<<g4, bk, 0, st>>>(d, cf, x, b, color, rows);
+                launch_pdl(k_rbgs4<C, false>, g4, bk, st, d, cf, x, b, color, rows);
             tk.after(st, fine, per * d.n);
             return;
         }
     }
     if (zero)
-        k_rbgs<T, C, true><<<g, bk, 0, st>>>(d, cf, x, b, color, rows);
+        launch_pdl(k_rbgs<T, C, true>, g, bk, st, d, cf, x, b, color, rows);
     else
-        k_rbgs<T, C, false><<<g, bk, 0, st>>>(d, cf, x, b, color, rows);
+        launch_pdl(k_rbgs<T, C, false>, g, bk, st, d, cf, x, b, color, rows);
     tk.after(st, fine, per * d.n);
 }
 
@@ -1313,11 +1348,11 @@ static void rb_split(cudaStream_t st, Tracker &tk, bool zero, const Dims &d, con
     const long long items = split_items((long long)d.nx * d.ny, d.nz >> 3);
     tk.before(st, true);
     if (zero)
-        k_rbgs4s<C, true><<<row_grid((const void *)k_rbgs4s<C, true>, items), blk2(), 0, st>>>(d, cf, x, b, color,
-                                                                                             list, count, crow);
+        launch_pdl(k_rbgs4s<C, true>, row_grid((const void *)k_rbgs4s<C, true>, items), blk2(), st, d, cf, x, b,
+                   color, list, count, crow);
     else
-        k_rbgs4s<C, false><<<row_grid((const void *)k_rbgs4s<C, false>, items), blk2(), 0, st>>>(d, cf, x, b, color,
-                                                                                               list, count, crow);
+        launch_pdl(k_rbgs4s<C, false>, row_grid((const void *)k_rbgs4s<C, false>, items), blk2(), st, d, cf, x, b,
+                   color, list, count, crow);
     tk.after(st, true, tk.bytes0 >= 0 ? tk.bytes0 : (3.0 * sizeof(float) + 4.0 * sizeof(C)) / 2.0 * d.n);
 }
 
@@ -1382,23 +1417,24 @@ static void restrict_res(cudaStream_t st, Tracker &tk, const Dims &d, const Coef
     tk.launches++;
     if constexpr (std::is_same<T, float>::value && std::is_same<C, __half>::value) {
         if (split) {
-            const int g = row_grid((const void *)k_resid_restrict_s<C>, split_items((long long)dc.nx * dc.ny, dc.nz >> 2));
-            k_resid_restrict_s<C><<<g, blk2(), 0, st>>>(d, cf, x, b, dc, bc, rows, crow, list_c, count_c);
+            const int g =
+                row_grid((const void *)k_resid_restrict_s<C>, split_items((long long)dc.nx * dc.ny, dc.nz >> 2));
+            launch_pdl(k_resid_restrict_s<C>, g, blk2(), st, d, cf, x, b, dc, bc, rows, crow, list_c, count_c);
             return;
         }
     }
-    k_resid_restrict<T, C><<<grid_cells(dc), blk2(), 0, st>>>(d, cf, x, b, dc, bc, rows, rows_c);
+    launch_pdl(k_resid_restrict<T, C>, grid_cells(dc), blk2(), st, d, cf, x, b, dc, bc, rows, rows_c);
 }
 
 template <class T, class C>
 static void coarse_solve(cudaStream_t st, Tracker &tk, const Dims &d, const Coef<C> &cf, T *x, const T *b, int pairs) {
     tk.launches++;
     if (d.n <= kCoarseMax) {
-        k_coarse_smem<T, C><<<1, kCoarseThreads, 0, st>>>(d, cf, x, b, pairs);
+        launch_pdl(k_coarse_smem<T, C>, 1, kCoarseThreads, st, d, cf, x, b, pairs);
         return;
     }
     int nt = d.n >= 1024 ? 1024 : (int)((d.n + 31) / 32 * 32);
-    k_coarse<T, C><<<1, nt, 0, st>>>(d, cf, x, b, pairs);
+    launch_pdl(k_coarse<T, C>, 1, nt, st, d, cf, x, b, pairs);
 }
 
 // V-cycle z = M r.  Level 0 uses coefficient type C0, coarse levels Cc (cc[l] for level l >= 1).  ts[l] is a
@@ -1438,7 +1474,7 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
     coarse_solve<T, Cc>(st, tk, dims[L - 1], cc[L - 1], xs[L - 1], bs[L - 1], p.coarse_sweeps);
     for (int l = L - 2; l >= 1; l--) {
         tk.launches++;
-        k_prolong<T><<<grid_cells(dims[l]), blk2(), 0, st>>>(dims[l], xs[l], dims[l + 1], xs[l + 1], R(l));
+        launch_pdl(k_prolong<T>, grid_cells(dims[l]), blk2(), st, dims[l], xs[l], dims[l + 1], xs[l + 1], R(l));
         smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.post, false, false, R(l));
     }
     tk.launches++;
@@ -1446,12 +1482,12 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
         if (split0) {
             const Dims &d0 = dims[0];
             const int g = row_grid((const void *)k_prolong_s, split_items((long long)d0.nx * d0.ny, d0.nz >> 3));
-            k_prolong_s<<<g, blk2(), 0, st>>>(d0, z, dims[1], xs[1], l0, n0);
+            launch_pdl(k_prolong_s, g, blk2(), st, d0, z, dims[1], xs[1], l0, n0);
             smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true, R(0), l0, n0, cr);
             return;
         }
     }
-    k_prolong<T><<<grid_cells(dims[0]), blk2(), 0, st>>>(dims[0], z, dims[1], xs[1], R(0));
+    launch_pdl(k_prolong<T>, grid_cells(dims[0]), blk2(), st, dims[0], z, dims[1], xs[1], R(0));
     smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, false, R(0));
 }
 
@@ -1710,11 +1746,11 @@ void MGSolver::enqueue_iter64() {
     vcycle<double, double, double, double>(st_, tk_, lev_dims_, c64_[0], c64_[0], c64_, z_, r_, x64_, b64_,
                                            prm_.smoother == 1 ? t64_ : std::vector<double *>(t64_.size(), nullptr),
                                            prm_);
-    k_dot_rz<double><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, r_, z_, q_, prm_.flexible ? 1 : 0, sc_, part_,
+    launch_pdl(k_dot_rz<double>, kMaxRedBlocks, dim3(32, 8), st_, n, r_, z_, q_, prm_.flexible ? 1 : 0, sc_, part_,
                                                               ticket_);
-    k_xpby<double><<<flat_grid(n), 256, 0, st_>>>(n, z_, p_, sc_);
-    k_apply_dot<double, double><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c64_[0], p_, q_, sc_, part_, ticket_);
-    k_update<double><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, x_, r_, p_, q_, sc_, part_, ticket_);
+    launch_pdl(k_xpby<double>, flat_grid(n), 256, st_, n, z_, p_, sc_);
+    launch_pdl(k_apply_dot<double, double>, tg, dim3(32, 8), st_, d, xpb, c64_[0], p_, q_, sc_, part_, ticket_);
+    launch_pdl(k_update<double>, kMaxRedBlocks, dim3(32, 8), st_, n, x_, r_, p_, q_, sc_, part_, ticket_);
     tk_.launches += 4;
     iter_launches64_ = tk_.launches - l0;
     cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
@@ -1732,12 +1768,13 @@ void MGSolver::enqueue_iter32() {
         vcycle<float, float, __half, __half>(st_, tk_, lev_dims_, c32_, c16s0_, c16_, z32_, ri32_, x32_, b32_, ts,
                                              prm_, true, &rs);
         const long long vitems = split_items(2LL * d.nx * d.ny, d.nz >> 3);
-        k_dot_rz_s<<<row_grid((const void *)k_dot_rz_s, vitems), dim3(32, 8), 0, st_>>>(d, ri32_, z32_, q32_, lst0, cnt0,
-                                                                                       1, sc_, part_, ticket_);
-        k_xpby_s<<<row_grid((const void *)k_xpby_s, vitems), dim3(32, 8), 0, st_>>>(d, z32_, p32_, lst0, cnt0, sc_);
+        launch_pdl(k_dot_rz_s, row_grid((const void *)k_dot_rz_s, vitems), dim3(32, 8), st_, d, ri32_, z32_, q32_,
+                   lst0, cnt0, 1, sc_, part_, ticket_);
+        launch_pdl(k_xpby_s, row_grid((const void *)k_xpby_s, vitems), dim3(32, 8), st_, d, z32_, p32_, lst0, cnt0,
+                   sc_);
         apply_dot32s(st_, d, c32_, p32_, q32_, lst0, cnt0, crow_, sc_, part_, ticket_);
-        k_update_s<<<row_grid((const void *)k_update_s, vitems), dim3(32, 8), 0, st_>>>(d, d32_, ri32_, p32_, q32_, lst0,
-                                                                                      cnt0, sc_, part_, ticket_);
+        launch_pdl(k_update_s, row_grid((const void *)k_update_s, vitems), dim3(32, 8), st_, d, d32_, ri32_, p32_,
+                   q32_, lst0, cnt0, sc_, part_, ticket_);
         tk_.launches += 4;
         iter_launches32_ = tk_.launches - l0;
         cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
@@ -1749,10 +1786,10 @@ void MGSolver::enqueue_iter32() {
     else
         vcycle<float, float, __half, float>(st_, tk_, lev_dims_, c32_, c32_, c16_, z32_, ri32_, x32_, b32_, ts,
                                             prm_);
-    k_dot_rz<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, ri32_, z32_, q32_, 1, sc_, part_, ticket_);
-    k_xpby<float><<<flat_grid(n), 256, 0, st_>>>(n, z32_, p32_, sc_);
+    launch_pdl(k_dot_rz<float>, kMaxRedBlocks, dim3(32, 8), st_, n, ri32_, z32_, q32_, 1, sc_, part_, ticket_);
+    launch_pdl(k_xpby<float>, flat_grid(n), 256, st_, n, z32_, p32_, sc_);
     apply_dot32(st_, d, c32_, p32_, q32_, sc_, part_, ticket_);
-    k_update<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, d32_, ri32_, p32_, q32_, sc_, part_, ticket_);
+    launch_pdl(k_update<float>, kMaxRedBlocks, dim3(32, 8), st_, n, d32_, ri32_, p32_, q32_, sc_, part_, ticket_);
     tk_.launches += 4;
     iter_launches32_ = tk_.launches - l0;
     cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);

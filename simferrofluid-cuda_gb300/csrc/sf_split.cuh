@@ -314,6 +314,7 @@ __global__ void __launch_bounds__(256) k_dot_rz_s(Dims d, const float *__restric
                                                   const float *__restrict__ q, const int *__restrict__ list,
                                                   const int *__restrict__ count, int flexible, double *sc,
                                                   double *part, unsigned *ticket) {
+    pdl_entry();
     float a0 = 0.f, a1 = 0.f;
     for_vec_rows(d, list, count, [&](long long v4) {
         const float4 rv = reinterpret_cast<const float4 *>(r)[v4], zv = reinterpret_cast<const float4 *>(z)[v4],
@@ -343,6 +344,7 @@ __global__ void __launch_bounds__(256) k_dot_rz_s(Dims d, const float *__restric
 __global__ void __launch_bounds__(256) k_xpby_s(Dims d, const float *__restrict__ z, float *__restrict__ p,
                                                 const int *__restrict__ list, const int *__restrict__ count,
                                                 const double *sc) {
+    pdl_entry();
     const float beta = (float)sc[S_BETA];
     for_vec_rows(d, list, count, [&](long long v4) {
         const float4 zv = reinterpret_cast<const float4 *>(z)[v4];
@@ -359,6 +361,7 @@ __global__ void __launch_bounds__(256) k_update_s(Dims d, float *__restrict__ x,
                                                   const float *__restrict__ p, const float *__restrict__ q,
                                                   const int *__restrict__ list, const int *__restrict__ count,
                                                   double *sc, double *part, unsigned *ticket) {
+    pdl_entry();
     const float alpha = (float)sc[S_ALPHA];
     float acc = 0.f;
     for_vec_rows(d, list, count, [&](long long v4) {
@@ -660,9 +663,11 @@ __device__ __forceinline__ void rbgs4s_cells(const Dims &d, const Coef<C> &cf, f
 
 // Persistent half sweep: warps over the active rows' chunks of 32 vectors.
 template <class C, bool ZERO>
-__global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__restrict__ x, const float *__restrict__ b,
+__global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__restrict__ x,
+                                                  const float *__restrict__ b,
                                                 int col, const int *__restrict__ list, const int *__restrict__ count,
                                                 const float *__restrict__ crow) {
+    pdl_entry();
     const int nq = d.nz >> 3;
     for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long row, int ch, bool uni) {
         const int q4 = ch * 32 + threadIdx.x;
@@ -803,6 +808,7 @@ __global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, co
                                                              const float *__restrict__ crow,
                                                              const int *__restrict__ list_c,
                                                              const int *__restrict__ count_c) {
+    pdl_entry();
     const int nq = dc.nz >> 2;  // coarse float4 per row (dc.nz = nz / 2, a multiple of 4)
     for_list_items(list_c, count_c, 1, (nq + 31) / 32, [&](int, long long row, int ch, bool) {
         const int q4 = ch * 32 + threadIdx.x;
@@ -816,6 +822,7 @@ __global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, co
 // (i/2, j/2, m).
 __global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x, Dims dc, const float *__restrict__ xc,
                                                    const int *__restrict__ list, const int *__restrict__ count) {
+    pdl_entry();
     const int nh = d.nz >> 1, nq = nh >> 2;
     for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long r, int ch, bool) {
         const int q4 = ch * 32 + threadIdx.x;
@@ -844,6 +851,7 @@ __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, 
                                                      float *__restrict__ q, const int *__restrict__ list,
                                                      const int *__restrict__ count, const float *__restrict__ crow,
                                                      double *sc, double *part, unsigned *ticket) {
+    pdl_entry();
     float acc = 0.f;
     const int nh = d.nz >> 1, nq = nh >> 2;
     for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, long long rw, int ch, bool uni) {
@@ -861,7 +869,8 @@ __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, 
             const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
             const bool xl = i > 0, xu = i < d.nx - 1;
             const int qz = (i + j + col) & 1;
-            float pc[4], pxm[4] = {0, 0, 0, 0}, pxp[4] = {0, 0, 0, 0}, pym[4] = {0, 0, 0, 0}, pyp[4] = {0, 0, 0, 0}, po[4];
+            float pc[4], po[4];
+            float pxm[4] = {0, 0, 0, 0}, pxp[4] = {0, 0, 0, 0}, pym[4] = {0, 0, 0, 0}, pyp[4] = {0, 0, 0, 0};
             float axl[4], axu[4] = {0, 0, 0, 0}, ayl[4], ayu[4] = {0, 0, 0, 0}, azl[4], azo[4], dx[4];
             ld4(p + own, pc);
             ld4(p + oth, po);
@@ -953,7 +962,9 @@ __global__ void __launch_bounds__(256) k_coarsen_s(Dims d, Coef<float> f, Dims d
     const int nh = d.nz >> 1;
     const long long hn = d.n >> 1;
     // entry m = K of colour col in fine row (i, j)
-    auto at = [&](const float *a, int col, int i, int j) { return a[(long long)col * hn + ((long long)i * d.ny + j) * nh + K]; };
+    auto at = [&](const float *a, int col, int i, int j) {
+        return a[(long long)col * hn + ((long long)i * d.ny + j) * nh + K];
+    };
     float fx = 0.f, fy = 0.f, fz = 0.f, dex = 0.f;
     for (int u = 0; u < 2; u++)
         for (int v = 0; v < 2; v++) {
@@ -982,5 +993,5 @@ static void apply_dot32s(cudaStream_t st, const Dims &d, const Coef<float> &cf, 
                          const int *list, const int *count, const float *crow, double *sc, double *part,
                          unsigned *ticket) {
     const int g = row_grid((const void *)k_apply_dot4s, split_items(2LL * d.nx * d.ny, d.nz >> 3));
-    k_apply_dot4s<<<g, dim3(32, 8), 0, st>>>(d, cf, p, q, list, count, crow, sc, part, ticket);
+    launch_pdl(k_apply_dot4s, g, dim3(32, 8), st, d, cf, p, q, list, count, crow, sc, part, ticket);
 }
