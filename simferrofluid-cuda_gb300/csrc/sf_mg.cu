@@ -1343,17 +1343,17 @@ static void fused(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const 
 // fused (tmp != nullptr): one kernel per sweep, ping-ponging between x and tmp; else two in-place colours.
 // Half sweep of the split level 0 (smoother 3); same algorithmic bytes as the natural half sweep.
 template <class C>
-static void rb_split(cudaStream_t st, Tracker &tk, bool zero, const Dims &d, const Coef<C> &cf, float *x,
+static void rb_split(cudaStream_t st, Tracker &tk, bool fine, bool zero, const Dims &d, const Coef<C> &cf, float *x,
                      const float *b, int color, const int *list, const int *count, const float *crow) {
     const long long items = split_items((long long)d.nx * d.ny, d.nz >> 3);
-    tk.before(st, true);
+    tk.before(st, fine);
     if (zero)
         launch_pdl(k_rbgs4s<C, true>, row_grid((const void *)k_rbgs4s<C, true>, items), blk2(), st, d, cf, x, b,
                    color, list, count, crow);
     else
         launch_pdl(k_rbgs4s<C, false>, row_grid((const void *)k_rbgs4s<C, false>, items), blk2(), st, d, cf, x, b,
                    color, list, count, crow);
-    tk.after(st, true, tk.bytes0 >= 0 ? tk.bytes0 : (3.0 * sizeof(float) + 4.0 * sizeof(C)) / 2.0 * d.n);
+    tk.after(st, fine, tk.bytes0 >= 0 ? tk.bytes0 : (3.0 * sizeof(float) + 4.0 * sizeof(C)) / 2.0 * d.n);
 }
 
 template <class T, class C>
@@ -1364,11 +1364,11 @@ static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const
         if (split) {
             for (int s = 0; s < nu; s++) {
                 if (pre) {
-                    rb_split<C>(st, tk, s == 0, d, cf, x, b, 0, list, count, crow);
-                    rb_split<C>(st, tk, false, d, cf, x, b, 1, list, count, crow);
+                    rb_split<C>(st, tk, fine, s == 0, d, cf, x, b, 0, list, count, crow);
+                    rb_split<C>(st, tk, fine, false, d, cf, x, b, 1, list, count, crow);
                 } else {
-                    rb_split<C>(st, tk, false, d, cf, x, b, 1, list, count, crow);
-                    rb_split<C>(st, tk, false, d, cf, x, b, 0, list, count, crow);
+                    rb_split<C>(st, tk, fine, false, d, cf, x, b, 1, list, count, crow);
+                    rb_split<C>(st, tk, fine, false, d, cf, x, b, 0, list, count, crow);
                 }
             }
             return;
@@ -1413,13 +1413,17 @@ template <class T, class C>
 static void restrict_res(cudaStream_t st, Tracker &tk, const Dims &d, const Coef<C> &cf, const T *x, const T *b,
                          const Dims &dc, T *bc, bool split = false, const uint8_t *rows = nullptr,
                          const uint8_t *rows_c = nullptr, const int *list_c = nullptr,
-                         const int *count_c = nullptr, const float *crow = nullptr) {
+                         const int *count_c = nullptr, const float *crow = nullptr, bool sout = false) {
     tk.launches++;
     if constexpr (std::is_same<T, float>::value && std::is_same<C, __half>::value) {
         if (split) {
-            const int g =
-                row_grid((const void *)k_resid_restrict_s<C>, split_items((long long)dc.nx * dc.ny, dc.nz >> 2));
-            launch_pdl(k_resid_restrict_s<C>, g, blk2(), st, d, cf, x, b, dc, bc, rows, crow, list_c, count_c);
+            const long long items = split_items((long long)dc.nx * dc.ny, dc.nz >> 2);
+            if (sout)
+                launch_pdl(k_resid_restrict_s<C, true>, row_grid((const void *)k_resid_restrict_s<C, true>, items),
+                           blk2(), st, d, cf, x, b, dc, bc, rows, crow, list_c, count_c);
+            else
+                launch_pdl(k_resid_restrict_s<C, false>, row_grid((const void *)k_resid_restrict_s<C, false>, items),
+                           blk2(), st, d, cf, x, b, dc, bc, rows, crow, list_c, count_c);
             return;
         }
     }
@@ -1446,8 +1450,9 @@ static void coarse_solve(cudaStream_t st, Tracker &tk, const Dims &d, const Coef
 // and 1 (the persistent split kernels walk those lists).
 struct RowSets {
     const std::vector<uint8_t *> *flags;
-    const int *list[2], *count[2];
-    const float *crow;  // level 0: the coupling of each uniform row
+    const int *list[3], *count[3];  // levels 0, 1, 2
+    const float *crow[2];           // levels 0, 1: the coupling of each uniform row
+    const Coef<__half> *c1s;        // split FP16 operator of level 1 when level 1 is split too, else nullptr
 };
 
 template <class T, class C0, class Cc, class C0S>
@@ -1461,19 +1466,42 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
         return;
     }
     auto R = [&](int l) -> const uint8_t * { return rs ? (*rs->flags)[l] : nullptr; };
-    const int *l0 = rs ? rs->list[0] : nullptr, *n0 = rs ? rs->count[0] : nullptr;
-    const float *cr = rs ? rs->crow : nullptr;
-    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true, split0, R(0), l0, n0, cr);
+    auto LST = [&](int l) -> const int * { return rs ? rs->list[l] : nullptr; };
+    auto CNT = [&](int l) -> const int * { return rs ? rs->count[l] : nullptr; };
+    const float *cr = rs ? rs->crow[0] : nullptr, *cr1 = rs ? rs->crow[1] : nullptr;
+    // level 1 split as well: its vectors and its FP16 operator copy *rs->c1s are stored colour by colour
+    bool split1 = false;
+    if constexpr (std::is_same<T, float>::value && std::is_same<Cc, __half>::value) split1 = rs && rs->c1s;
+    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true, split0, R(0), LST(0), CNT(0), cr);
     // the residual of the smoothed operator
-    restrict_res<T, C0S>(st, tk, dims[0], c0s, z, r, dims[1], bs[1], split0, R(0), R(1), rs ? rs->list[1] : nullptr,
-                         rs ? rs->count[1] : nullptr, cr);
+    restrict_res<T, C0S>(st, tk, dims[0], c0s, z, r, dims[1], bs[1], split0, R(0), R(1), LST(1), CNT(1), cr, split1);
     for (int l = 1; l < L - 1; l++) {
+        if constexpr (std::is_same<T, float>::value && std::is_same<Cc, __half>::value) {
+            if (l == 1 && split1) {
+                const Coef<__half> &c1 = *rs->c1s;
+                smooth<T, Cc>(st, tk, false, dims[1], c1, xs[1], nullptr, bs[1], p.pre, true, true, R(1), LST(1),
+                              CNT(1), cr1);
+                restrict_res<T, Cc>(st, tk, dims[1], c1, xs[1], bs[1], dims[2], bs[2], true, R(1), R(2), LST(2),
+                                    CNT(2), cr1);
+                continue;
+            }
+        }
         smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.pre, true, false, R(l));
         restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1], false, R(l), R(l + 1));
     }
     coarse_solve<T, Cc>(st, tk, dims[L - 1], cc[L - 1], xs[L - 1], bs[L - 1], p.coarse_sweeps);
     for (int l = L - 2; l >= 1; l--) {
         tk.launches++;
+        if constexpr (std::is_same<T, float>::value && std::is_same<Cc, __half>::value) {
+            if (l == 1 && split1) {
+                const Dims &d1 = dims[1];
+                const int g = row_grid((const void *)k_prolong_s, split_items((long long)d1.nx * d1.ny, d1.nz >> 3));
+                launch_pdl(k_prolong_s, g, blk2(), st, d1, xs[1], dims[2], xs[2], LST(1), CNT(1));
+                smooth<T, Cc>(st, tk, false, d1, *rs->c1s, xs[1], nullptr, bs[1], p.post, false, true, R(1), LST(1),
+                              CNT(1), cr1);
+                continue;
+            }
+        }
         launch_pdl(k_prolong<T>, grid_cells(dims[l]), blk2(), st, dims[l], xs[l], dims[l + 1], xs[l + 1], R(l));
         smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.post, false, false, R(l));
     }
@@ -1481,9 +1509,14 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
     if constexpr (std::is_same<T, float>::value) {
         if (split0) {
             const Dims &d0 = dims[0];
-            const int g = row_grid((const void *)k_prolong_s, split_items((long long)d0.nx * d0.ny, d0.nz >> 3));
-            launch_pdl(k_prolong_s, g, blk2(), st, d0, z, dims[1], xs[1], l0, n0);
-            smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true, R(0), l0, n0, cr);
+            const long long items = split_items((long long)d0.nx * d0.ny, d0.nz >> 3);
+            if (split1)
+                launch_pdl(k_prolong_ss, row_grid((const void *)k_prolong_ss, items), blk2(), st, d0, z, dims[1], xs[1],
+                           LST(0), CNT(0));
+            else
+                launch_pdl(k_prolong_s, row_grid((const void *)k_prolong_s, items), blk2(), st, d0, z, dims[1], xs[1],
+                           LST(0), CNT(0));
+            smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true, R(0), LST(0), CNT(0), cr);
             return;
         }
     }
@@ -1630,13 +1663,29 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
         for (int l = 0; l < (int)rows_.size(); l++) rows_[l] = (uint8_t *)chk(A((size_t)dims[l].nx * dims[l].ny));
         list_[0] = list_[1] = nullptr;
         count_ = nullptr;
-        crow_ = nullptr;
+        crow_ = crow1_ = nullptr;
+        list_[2] = nullptr;
+        c16s1_ = Coef<__half>{};
+        // level 1 split too when it has a coarser level and whole 16-byte rows per colour
+        const bool split1 = split0 && L >= 3 && dims[1].nz % 8 == 0;
         if (split0) {
-            for (int l = 0; l < 2; l++) list_[l] = (int *)chk(A(4 * (size_t)dims[l].nx * dims[l].ny));
-            count_ = (int *)chk(A(8));
+            for (int l = 0; l < (split1 ? 3 : 2); l++) list_[l] = (int *)chk(A(4 * (size_t)dims[l].nx * dims[l].ny));
+            count_ = (int *)chk(A(16));
             crow_ = (float *)chk(A(4 * (size_t)dims[0].nx * dims[0].ny));
             list_cnt_ = (int *)chk(A(8 * (((size_t)dims[0].nx * dims[0].ny + kListRows - 1) / kListRows)));
+            if (split1) {
+                crow1_ = (float *)chk(A(4 * (size_t)dims[1].nx * dims[1].ny));
+                const long long m = dims[1].n;
+                c16s1_.ax = (__half *)chk(A(2 * m));
+                c16s1_.ay = (__half *)chk(A(2 * m));
+                c16s1_.az = (__half *)chk(A(2 * m));
+                c16s1_.dex = (__half *)chk(A(2 * m));
+                c16s1_.D = c16s1_.invd = nullptr;
+                c16s1_.scale = ldexpf(1.f, -2);  // as level 1's natural copy
+                c16s1_.unscale = ldexpf(1.f, 2);
+            }
         }
+        split1_ = split1;
         r32_ = (float *)chk(A(4 * n));
         d32_ = (float *)chk(A(4 * n));
         z32_ = (float *)chk(A(4 * n));
@@ -1663,9 +1712,10 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     cfg_split_ = split0_ = split0;
     if (split0) {  // occupancy lookups of the persistent split kernels, here rather than inside a graph capture
         const void *ks[] = {(const void *)k_rbgs4s<__half, true>, (const void *)k_rbgs4s<__half, false>,
-                            (const void *)k_resid_restrict_s<__half>, (const void *)k_prolong_s,
-                            (const void *)k_apply_dot4s, (const void *)k_dot_rz_s, (const void *)k_xpby_s,
-                            (const void *)k_update_s, (const void *)k_ir_update_s};
+                            (const void *)k_resid_restrict_s<__half, false>,
+                            (const void *)k_resid_restrict_s<__half, true>, (const void *)k_prolong_s,
+                            (const void *)k_prolong_ss, (const void *)k_apply_dot4s, (const void *)k_dot_rz_s,
+                            (const void *)k_xpby_s, (const void *)k_update_s, (const void *)k_ir_update_s};
         for (const void *k : ks) resident_grid(k);
     }
     return cudaGetLastError();
@@ -1682,7 +1732,8 @@ cudaError_t MGSolver::build_hierarchy() {
         if (split0_) {
             k_to_split<<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(lev_dims_[0], c64_[0], c32_, c16s0_,
                                                                                 rows_[0]);
-            k_rows_uniform<<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(lev_dims_[0], c32_, rows_[0], crow_);
+            k_rows_uniform<float><<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(lev_dims_[0], c32_, rows_[0],
+                                                                                          crow_);
             tk_.launches++;
             // rows that hold no active cell are skipped by every level-l kernel; their vector entries must be
             // zero, and stay so
@@ -1695,13 +1746,23 @@ cudaError_t MGSolver::build_hierarchy() {
                 cudaMemsetAsync(x32_[l], 0, 4 * (size_t)dl.n, st_);
                 cudaMemsetAsync(b32_[l], 0, 4 * (size_t)dl.n, st_);
             }
-            for (int l = 0; l < 2; l++) {
+            // level 1 from the split FP32 copy (half the bytes of the FP64 operator, FP32 sums), with its own split
+            // copy and uniform rows when level 1 is split too
+            k_coarsen_s<<<grid_cells(lev_dims_[1]), blk2(), 0, st_>>>(lev_dims_[0], c32_, lev_dims_[1], c16_[1],
+                                                                       split1_ ? c16s1_ : Coef<__half>{});
+            tk_.launches += L - 1;
+            if (split1_) {
+                k_rows_uniform<__half><<<split_rows_grid(lev_dims_[1]), dim3(32, 8), 0, st_>>>(lev_dims_[1], c16s1_,
+                                                                                               rows_[1], crow1_);
+                tk_.launches++;
+            }
+            for (int l = 0; l < (split1_ ? 3 : 2); l++) {
                 const long long nr = (long long)lev_dims_[l].nx * lev_dims_[l].ny;
                 const int nb = (int)((nr + kListRows - 1) / kListRows);
                 k_rows_count<<<nb, kListRows, 0, st_>>>(nr, rows_[l], list_cnt_);
                 k_rows_scatter<<<nb, kListRows, 0, st_>>>(nr, rows_[l], list_cnt_, list_[l], count_ + l);
+                tk_.launches += 2;
             }
-            tk_.launches += L - 1 + 4;
             tk_.bytes0 = -1;
             if (prm_.profile) {  // profiled runs synchronise anyway: count the level-0 rows by kind
                 const Dims &d0 = lev_dims_[0];
@@ -1725,9 +1786,7 @@ cudaError_t MGSolver::build_hierarchy() {
                 tk_.launches++;
             }
         }
-        if (split0_)  // from the split FP32 copy (half the bytes of the FP64 operator, FP32 sums)
-            k_coarsen_s<<<grid_cells(lev_dims_[1]), blk2(), 0, st_>>>(lev_dims_[0], c32_, lev_dims_[1], c16_[1]);
-        else if (L > 1)
+        if (!split0_ && L > 1)
             k_coarsen<double, __half><<<grid_cells(lev_dims_[1]), blk2(), 0, st_>>>(lev_dims_[0], c64_[0],
                                                                                     lev_dims_[1], c16_[1]);
         for (int l = 2; l < L; l++)
@@ -1763,7 +1822,8 @@ void MGSolver::enqueue_iter32() {
     const std::vector<float *> ts = prm_.smoother == 1 ? t32_ : std::vector<float *>(t32_.size(), nullptr);
     if (split0_) {
         // colour-split level 0 with row flags on every level (vectors in split rows, inactive rows skipped)
-        const RowSets rs{&rows_, {list_[0], list_[1]}, {count_, count_ + 1}, crow_};
+        const RowSets rs{&rows_, {list_[0], list_[1], list_[2]}, {count_, count_ + 1, count_ + 2}, {crow_, crow1_},
+                         split1_ ? &c16s1_ : nullptr};
         const int *lst0 = list_[0], *cnt0 = count_;
         vcycle<float, float, __half, __half>(st_, tk_, lev_dims_, c32_, c16s0_, c16_, z32_, ri32_, x32_, b32_, ts,
                                              prm_, true, &rs);

@@ -145,9 +145,12 @@ class MGSolver {
     bool split0_ = false, cfg_split_ = false;
     // with split0_: per level, one byte per row (i, j), 0 when every cell of the row is inactive (D = 0)
     std::vector<uint8_t *> rows_;
-    int *list_[2] = {nullptr, nullptr};  // ordered active rows of levels 0 and 1
+    int *list_[3] = {nullptr, nullptr, nullptr};  // active rows of levels 0, 1 (and 2 when level 1 is split)
     int *count_ = nullptr;               // their counts (device)
     float *crow_ = nullptr;              // level 0: the coupling of each uniform row
+    float *crow1_ = nullptr;             // level 1 (split): the same
+    bool split1_ = false;                // level 1 stored colour by colour too
+    Coef<__half> c16s1_{};               // its split FP16 operator copy (the natural copy feeds level 2)
     int *list_cnt_ = nullptr;            // per block of rows: general and uniform counts (list building)
     std::vector<float *> x32_, b32_, t32_;
 

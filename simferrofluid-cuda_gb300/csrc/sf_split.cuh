@@ -222,8 +222,10 @@ __global__ void k_rows_coarsen(Dims df, const uint8_t *__restrict__ rf, Dims dc,
 // zero diagonal excess and every in-grid coupling of its cells equals one FP32 value c > 0: the lower x, y, z
 // faces of its cells, their upper z faces (the next cell's lower face, in the row) and their upper x and y
 // faces (the lower faces of rows (i + 1, j) and (i, j + 1)).  Equal FP32 values have equal FP16 roundings, so
-// both copies of the operator are c on the row.  crow[row] = c.  One warp per row.
-__global__ void __launch_bounds__(256) k_rows_uniform(Dims d, Coef<float> o, uint8_t *__restrict__ rows,
+// both copies of the operator are c on the row.  crow[row] = c (as stored, FP16 values converted exactly).  One
+// warp per row.  C is the type of the copy classified (FP32 on level 0, FP16 on a split level 1).
+template <class C>
+__global__ void __launch_bounds__(256) k_rows_uniform(Dims d, Coef<C> o, uint8_t *__restrict__ rows,
                                                       float *__restrict__ crow) {
     const int nh = d.nz >> 1;
     const long long hn = d.n >> 1, nrows = (long long)d.nx * d.ny;
@@ -232,19 +234,19 @@ __global__ void __launch_bounds__(256) k_rows_uniform(Dims d, Coef<float> o, uin
         if (!rows[row]) continue;
         const int i = (int)row / d.ny, j = (int)row - i * d.ny;
         const int p = (i + j) & 1;
-        const float c = nh > 0 ? o.az[(long long)(p ^ 1) * hn + row * nh] : 0.f;  // lower z face of cell k = 1
+        const float c = nh > 0 ? ldv(o.az, (long long)(p ^ 1) * hn + row * nh) : 0.f;  // lower z face, k = 1
         bool ok = c > 0.f;
         for (int m = threadIdx.x; m < nh; m += blockDim.x)
 #pragma unroll
             for (int col = 0; col < 2; col++) {
                 const long long sidx = (long long)col * hn + row * nh + m, oth = (long long)(col ^ 1) * hn;
                 const int k = 2 * m + ((p + col) & 1);
-                ok &= o.dex[sidx] == 0.f;
-                if (k > 0) ok &= o.az[sidx] == c;
-                if (i > 0) ok &= o.ax[sidx] == c;
-                if (j > 0) ok &= o.ay[sidx] == c;
-                if (i < d.nx - 1) ok &= o.ax[oth + (row + d.ny) * nh + m] == c;
-                if (j < d.ny - 1) ok &= o.ay[oth + (row + 1) * nh + m] == c;
+                ok &= ldv(o.dex, sidx) == 0.f;
+                if (k > 0) ok &= ldv(o.az, sidx) == c;
+                if (i > 0) ok &= ldv(o.ax, sidx) == c;
+                if (j > 0) ok &= ldv(o.ay, sidx) == c;
+                if (i < d.nx - 1) ok &= ldv(o.ax, oth + (row + d.ny) * nh + m) == c;
+                if (j < d.ny - 1) ok &= ldv(o.ay, oth + (row + 1) * nh + m) == c;
             }
         ok = __all_sync(0xffffffffu, ok);
         if (threadIdx.x == 0) {
@@ -775,7 +777,9 @@ __device__ __forceinline__ void resid4_split(const Dims &d, const Coef<C> &cf, c
 // residuals are summed.  (The natural kernel evaluates all eight children; the difference is at rounding
 // level.)  Thread (q4, J, I) sums coarse cells K0 = 4 q4 .. K0 + 3 over their x and y children, in the order
 // of k_resid_restrict; in each fine row the colour-0 child of coarse cell K is the entry m = K.
-template <class C>
+// SOUT: the coarse level is split too: coarse cells K0, K0 + 2 (colour (I + J) & 1) and K0 + 1, K0 + 3 (the other)
+// go to entries K0 / 2, K0 / 2 + 1 of their colour's half, as two float2.
+template <class C, bool SOUT>
 __device__ __forceinline__ void resid_restrict_s_cells(const Dims &d, const Coef<C> &cf, const float *__restrict__ x,
                                                        const float *__restrict__ b, const Dims &dc,
                                                        float *__restrict__ bc, const uint8_t *__restrict__ rows,
@@ -798,10 +802,17 @@ __device__ __forceinline__ void resid_restrict_s_cells(const Dims &d, const Coef
             for (int t = 0; t < 4; t++) acc[t] += r[t];
         }
     }
-    *reinterpret_cast<float4 *>(bc + cid(dc, I, J, K0)) = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    if (SOUT) {
+        const int pc = (I + J) & 1;
+        const long long hc = dc.n >> 1, base = ((long long)I * dc.ny + J) * (dc.nz >> 1) + (K0 >> 1);
+        *reinterpret_cast<float2 *>(bc + (long long)pc * hc + base) = make_float2(acc[0], acc[2]);
+        *reinterpret_cast<float2 *>(bc + (long long)(pc ^ 1) * hc + base) = make_float2(acc[1], acc[3]);
+    } else {
+        *reinterpret_cast<float4 *>(bc + cid(dc, I, J, K0)) = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    }
 }
 
-template <class C>
+template <class C, bool SOUT>
 __global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, const float *__restrict__ x,
                                                              const float *__restrict__ b, Dims dc,
                                                              float *__restrict__ bc, const uint8_t *__restrict__ rows,
@@ -814,7 +825,7 @@ __global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, co
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
         const int I = (int)row / dc.ny, J = (int)row - I * dc.ny;
-        resid_restrict_s_cells<C>(d, cf, x, b, dc, bc, rows, crow, I, J, 4 * q4);
+        resid_restrict_s_cells<C, SOUT>(d, cf, x, b, dc, bc, rows, crow, I, J, 4 * q4);
     });
 }
 
@@ -830,6 +841,38 @@ __global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x
         const int i = (int)r / d.ny, j = (int)r - i * d.ny, m0 = 4 * q4;
         float v[4];
         ld4(xc + cid(dc, i >> 1, j >> 1, m0), v);
+        const long long row = r * nh + m0;
+#pragma unroll
+        for (int col = 0; col < 2; col++) {
+            float *p = x + (long long)col * (d.n >> 1) + row;
+            float4 t = *reinterpret_cast<float4 *>(p);
+            t.x += v[0];
+            t.y += v[1];
+            t.z += v[2];
+            t.w += v[3];
+            *reinterpret_cast<float4 *>(p) = t;
+        }
+    });
+}
+
+// x += P xc with both levels split: fine entries m0 .. m0 + 3 of row (i, j) (either colour, k = 2m or 2m + 1) take
+// coarse cells K = m0 .. m0 + 3 of coarse row (i/2, j/2): even K of colour (i/2 + j/2) & 1, odd K of the other,
+// at entries K / 2 (two float2 loads).
+__global__ void __launch_bounds__(256) k_prolong_ss(Dims d, float *__restrict__ x, Dims dc,
+                                                    const float *__restrict__ xc, const int *__restrict__ list,
+                                                    const int *__restrict__ count) {
+    pdl_entry();
+    const int nh = d.nz >> 1, nq = nh >> 2;
+    const long long hc = dc.n >> 1;
+    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long r, int ch, bool) {
+        const int q4 = ch * 32 + threadIdx.x;
+        if (q4 >= nq) return;
+        const int i = (int)r / d.ny, j = (int)r - i * d.ny, m0 = 4 * q4;
+        const int I = i >> 1, J = j >> 1, pc = (I + J) & 1;
+        const long long base = ((long long)I * dc.ny + J) * (dc.nz >> 1) + (m0 >> 1);
+        const float2 ev = *reinterpret_cast<const float2 *>(xc + (long long)pc * hc + base);
+        const float2 od = *reinterpret_cast<const float2 *>(xc + (long long)(pc ^ 1) * hc + base);
+        const float v[4] = {ev.x, od.x, ev.y, od.y};
         const long long row = r * nh + m0;
 #pragma unroll
         for (int col = 0; col < 2; col++) {
@@ -954,7 +997,8 @@ __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, 
 // it (a coarse face is half the sum of its four fine faces, a coarse excess half the sum of its eight children's),
 // summed in FP32 from the FP32 copy instead of FP64 from the FP64 operator (the result is stored in FP16).  Fine
 // row (i, j) holds both children k = 2K, 2K + 1 of coarse cell K at m = K: colour (i + j) & 1 for k = 2K.
-__global__ void __launch_bounds__(256) k_coarsen_s(Dims d, Coef<float> f, Dims dc, Coef<__half> cc) {
+// cs: when its arrays are set, the same values also go to a split copy of the coarse level (nz / 2 % 8 == 0).
+__global__ void __launch_bounds__(256) k_coarsen_s(Dims d, Coef<float> f, Dims dc, Coef<__half> cc, Coef<__half> cs) {
     const int K = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int I = blockIdx.z;
@@ -980,10 +1024,19 @@ __global__ void __launch_bounds__(256) k_coarsen_s(Dims d, Coef<float> f, Dims d
         }
     const float sc = 0.5f * cc.scale;
     const long long c = cid(dc, I, J, K);
-    cc.ax[c] = __float2half_rn(fx * sc);
-    cc.ay[c] = __float2half_rn(fy * sc);
-    cc.az[c] = __float2half_rn(fz * sc);
-    cc.dex[c] = __float2half_rn(dex * sc);
+    const __half hx = __float2half_rn(fx * sc), hy = __float2half_rn(fy * sc), hz = __float2half_rn(fz * sc),
+                 hd = __float2half_rn(dex * sc);
+    cc.ax[c] = hx;
+    cc.ay[c] = hy;
+    cc.az[c] = hz;
+    cc.dex[c] = hd;
+    if (cs.ax) {
+        const long long q = split_index(dc, I, J, K);
+        cs.ax[q] = hx;
+        cs.ay[q] = hy;
+        cs.az[q] = hz;
+        cs.dex[q] = hd;
+    }
 }
 
 // Items of the persistent split kernels: rows x chunks of 32 float4.
