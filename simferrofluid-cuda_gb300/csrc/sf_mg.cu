@@ -1574,7 +1574,8 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     }
     // smoother 3 (split level 0) needs rows of whole 16-byte vectors per colour, a coarse level, and a split
     // Krylov operator grid within the reduction's block budget; otherwise it runs as smoother 2
-    const bool split0 = p.precision == 1 && p.smoother == 3 && d.nz % 8 == 0 && dims.size() >= 2 &&
+    const bool split0 = p.precision == 1 && p.smoother == 3 && d.nz % 8 == 0 && dims.size() >= 2 && d.nx < 32768 &&
+                        d.ny < 65536 &&
                         (long long)(((d.nz >> 1) + 127) / 128) * 2 * ((d.ny + 7) / 8) <= kApplyBlocks;
     const bool fp16copy = p.smoother == 2 || p.smoother == 3;
     const bool same = configured_ && cfg_dims_.nx == d.nx && cfg_dims_.ny == d.ny && cfg_dims_.nz == d.nz &&
@@ -1760,7 +1761,8 @@ cudaError_t MGSolver::build_hierarchy() {
                 const long long nr = (long long)lev_dims_[l].nx * lev_dims_[l].ny;
                 const int nb = (int)((nr + kListRows - 1) / kListRows);
                 k_rows_count<<<nb, kListRows, 0, st_>>>(nr, rows_[l], list_cnt_);
-                k_rows_scatter<<<nb, kListRows, 0, st_>>>(nr, rows_[l], list_cnt_, list_[l], count_ + l);
+                k_rows_scatter<<<nb, kListRows, 0, st_>>>(nr, lev_dims_[l].ny, rows_[l], list_cnt_, list_[l],
+                                                          count_ + l);
                 tk_.launches += 2;
             }
             tk_.bytes0 = -1;

@@ -47,7 +47,8 @@ static inline int split_rows_grid(const Dims &d) {
 }
 
 // List of a level's active rows, in two segments: the general rows (flag 1) in ascending order, then the uniform
-// rows (flag 2) in ascending order, with bit 31 set; *count = their number.  Rows of one segment cost the same,
+// rows (flag 2) in ascending order; an entry is (i << 16) | j, with bit 31 set on uniform rows (nx < 2^15,
+// ny < 2^16); *count = their number.  Rows of one segment cost the same,
 // so the persistent kernels' round-robin split of the list gives every warp an equal share of each kind.
 // Two kernels over blocks of 1024 rows: per-block counts of each kind, then each block's entries at the offsets
 // the counts give (deterministic).
@@ -62,7 +63,7 @@ __global__ void __launch_bounds__(kListRows) k_rows_count(long long nrows, const
         cnt[2 * blockIdx.x + 1] = u;
     }
 }
-__global__ void __launch_bounds__(kListRows) k_rows_scatter(long long nrows, const uint8_t *__restrict__ rows,
+__global__ void __launch_bounds__(kListRows) k_rows_scatter(long long nrows, int ny, const uint8_t *__restrict__ rows,
                                                             const int *__restrict__ cnt, int *__restrict__ list,
                                                             int *__restrict__ count) {
     __shared__ int wg[32], wu[32], off[2];
@@ -104,14 +105,15 @@ __global__ void __launch_bounds__(kListRows) k_rows_scatter(long long nrows, con
         pu += wu[q];
     }
     const unsigned below = (1u << lane) - 1u;
-    if (f == 1) list[pg + __popc(bg & below)] = (int)r;
-    if (f == 2) list[pu + __popc(bu & below)] = (int)((unsigned)r | 0x80000000u);
+    const unsigned e = ((unsigned)(r / ny) << 16) | (unsigned)(r % ny);
+    if (f == 1) list[pg + __popc(bg & below)] = (int)e;
+    if (f == 2) list[pu + __popc(bu & below)] = (int)(e | 0x80000000u);
 }
 
 // Persistent loop of a grid's warps (blockDim = (32, 8)) over the items (rep, list entry, chunk): `reps` passes
 // (colours) over the *count listed rows, `nch` chunks of 32 lanes per row; warp w takes items w, w + W, ...
 // Every warp gets an equal share of the active rows, and the assignment depends only on the grid and the list,
-// so reductions stay deterministic.  f(rep, row, chunk, uniform).
+// so reductions stay deterministic.  f(rep, i, j, chunk, uniform).
 // 32-bit item arithmetic (a level has fewer than 2^31 rows); reps is 1 or 2.
 template <class F>
 __device__ __forceinline__ void for_list_items(const int *__restrict__ list, const int *__restrict__ count, int reps,
@@ -139,7 +141,7 @@ __device__ __forceinline__ void for_list_items(const int *__restrict__ list, con
         const int e_next = entry(it + stride);  // issued before this item's loads
         unsigned rr, ch;
         split(it, rr, ch);
-        f(rr >= n ? 1 : 0, (long long)(e & 0x7fffffff), (int)ch, e < 0);
+        f(rr >= n ? 1 : 0, (e >> 16) & 0x7fff, e & 0xffff, (int)ch, e < 0);
         e = e_next;
     }
 }
@@ -288,10 +290,10 @@ __global__ void __launch_bounds__(256) k_ir_update_s(Dims d, double *__restrict_
                                                      const int *__restrict__ list, const int *__restrict__ count) {
     const int nh = d.nz >> 1;
     const long long hn = d.n >> 1;
-    for_list_items(list, count, 1, (nh + 31) / 32, [&](int, long long row, int ch, bool) {
+    for_list_items(list, count, 1, (nh + 31) / 32, [&](int, int i, int j, int ch, bool) {
         const int m = ch * 32 + threadIdx.x;
         if (m >= nh) return;
-        const int i = (int)row / d.ny, j = (int)row - i * d.ny;
+        const long long row = (long long)i * d.ny + j;
         const int p = (i + j) & 1;
         const long long nat = row * d.nz + 2 * m, sp = row * nh + m;
         x[nat + p] += (double)dlt[sp];
@@ -306,9 +308,9 @@ template <class F>
 __device__ __forceinline__ void for_vec_rows(const Dims &d, const int *list, const int *count, F &&f) {
     const int nq = d.nz >> 3;  // float4 per row of a colour
     const long long nrows = (long long)d.nx * d.ny;
-    for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, long long row, int ch, bool) {
+    for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, int i, int j, int ch, bool) {
         const int t = ch * 32 + threadIdx.x;
-        if (t < nq) f((col * nrows + row) * nq + t);
+        if (t < nq) f((col * nrows + (long long)i * d.ny + j) * nq + t);
     });
 }
 
@@ -497,8 +499,8 @@ __device__ __forceinline__ void for_cells4(int qz, Fn &&fn) {
 __device__ __forceinline__ void row_inv(const Dims &d, float c, int i, int j, float &inv_in, float &inv_end) {
     const float nxy = (float)((i > 0) + (i < d.nx - 1) + (j > 0) + (j < d.ny - 1));
     const float di = c * (nxy + 2.f), de = c * (nxy + 1.f);
-    inv_in = di > 0.f ? 1.f / di : 0.f;
-    inv_end = de > 0.f ? 1.f / de : 0.f;
+    inv_in = di > 0.f ? __frcp_rn(di) : 0.f;  // IEEE round-to-nearest reciprocal: the value of 1.f / di
+    inv_end = de > 0.f ? __frcp_rn(de) : 0.f;
 }
 
 template <bool ZERO>
@@ -648,7 +650,7 @@ __device__ __forceinline__ void rbgs4s_cells(const Dims &d, const Coef<C> &cf, f
             float e = dx[t];
             if (sizeof(C) == 2) e *= cf.unscale;
             const float D = sa + e;
-            const float inv = D > 0.f ? 1.f / D : 0.f;
+            const float inv = D > 0.f ? __frcp_rn(D) : 0.f;  // = 1.f / D (IEEE round to nearest)
             out[t] = (bv[t] + s) * inv;
         };
         upd(std::integral_constant<int, 0>{});
@@ -671,12 +673,11 @@ __global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__
                                                 const float *__restrict__ crow) {
     pdl_entry();
     const int nq = d.nz >> 3;
-    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long row, int ch, bool uni) {
+    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, int i, int j, int ch, bool uni) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
-        const int i = (int)row / d.ny, j = (int)row - i * d.ny;
         if (uni)
-            rbgs4s_uniform<ZERO>(d, c_of(cf, crow[row]), x, b, col, i, j, 4 * q4);
+            rbgs4s_uniform<ZERO>(d, c_of(cf, crow[(long long)i * d.ny + j]), x, b, col, i, j, 4 * q4);
         else
             rbgs4s_cells<C, ZERO>(d, cf, x, b, col, i, j, 4 * q4);
     });
@@ -821,10 +822,9 @@ __global__ void __launch_bounds__(256) k_resid_restrict_s(Dims d, Coef<C> cf, co
                                                              const int *__restrict__ count_c) {
     pdl_entry();
     const int nq = dc.nz >> 2;  // coarse float4 per row (dc.nz = nz / 2, a multiple of 4)
-    for_list_items(list_c, count_c, 1, (nq + 31) / 32, [&](int, long long row, int ch, bool) {
+    for_list_items(list_c, count_c, 1, (nq + 31) / 32, [&](int, int I, int J, int ch, bool) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
-        const int I = (int)row / dc.ny, J = (int)row - I * dc.ny;
         resid_restrict_s_cells<C, SOUT>(d, cf, x, b, dc, bc, rows, crow, I, J, 4 * q4);
     });
 }
@@ -835,10 +835,11 @@ __global__ void __launch_bounds__(256) k_prolong_s(Dims d, float *__restrict__ x
                                                    const int *__restrict__ list, const int *__restrict__ count) {
     pdl_entry();
     const int nh = d.nz >> 1, nq = nh >> 2;
-    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long r, int ch, bool) {
+    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, int i, int j, int ch, bool) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
-        const int i = (int)r / d.ny, j = (int)r - i * d.ny, m0 = 4 * q4;
+        const long long r = (long long)i * d.ny + j;
+        const int m0 = 4 * q4;
         float v[4];
         ld4(xc + cid(dc, i >> 1, j >> 1, m0), v);
         const long long row = r * nh + m0;
@@ -864,10 +865,11 @@ __global__ void __launch_bounds__(256) k_prolong_ss(Dims d, float *__restrict__ 
     pdl_entry();
     const int nh = d.nz >> 1, nq = nh >> 2;
     const long long hc = dc.n >> 1;
-    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, long long r, int ch, bool) {
+    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, int i, int j, int ch, bool) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
-        const int i = (int)r / d.ny, j = (int)r - i * d.ny, m0 = 4 * q4;
+        const long long r = (long long)i * d.ny + j;
+        const int m0 = 4 * q4;
         const int I = i >> 1, J = j >> 1, pc = (I + J) & 1;
         const long long base = ((long long)I * dc.ny + J) * (dc.nz >> 1) + (m0 >> 1);
         const float2 ev = *reinterpret_cast<const float2 *>(xc + (long long)pc * hc + base);
@@ -897,10 +899,11 @@ __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, 
     pdl_entry();
     float acc = 0.f;
     const int nh = d.nz >> 1, nq = nh >> 2;
-    for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, long long rw, int ch, bool uni) {
+    for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, int i, int j, int ch, bool uni) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
-        const int i = (int)rw / d.ny, j = (int)rw - i * d.ny, m0 = 4 * q4;
+        const long long rw = (long long)i * d.ny + j;
+        const int m0 = 4 * q4;
         if (uni) {
             apply4s_uniform(d, crow[rw], p, q, col, i, j, m0, acc);
             return;
