@@ -196,7 +196,7 @@ sf_status pressure_impl(Ctx *c, const sf_grid *g, double *const vel[3], const do
     CK(cudaEventRecord(c->ev[0], c->st));
     // 1/D is read only by FP64 smoothers
     launch_build_pressure(c->st, d, dphi, ffrac, fvel, fus, fjump, vol_error, S.fine(), S.b(), reproject,
-                          prm.precision == 0);
+                          prm.precision == 0, reproject ? nullptr : S.split_targets());
     if (!reproject) CK(S.build_hierarchy());
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->ev[1], c->st));
@@ -289,7 +289,7 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
     CK(S.configure(d, prm));
     const bool warm = (!opts || opts->warm_start) && same_grid;
     CK(cudaEventRecord(c->ev[0], c->st));
-    launch_build_magnetic(c->st, d, dphi, chi, bw, fh, g->h, S.fine(), S.b(), prm.precision == 0);
+    launch_build_magnetic(c->st, d, dphi, chi, bw, fh, g->h, S.fine(), S.b(), prm.precision == 0, S.split_targets());
     CK(S.build_hierarchy());
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->ev[1], c->st));

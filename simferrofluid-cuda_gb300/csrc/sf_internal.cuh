@@ -38,6 +38,21 @@ struct Coef {
     float scale, unscale;
 };
 
+// Colour-split index of cell (i, j, k) (the mixed form's level 0 with smoother 3): colour (i + j + k) & 1 selects
+// the half of the array, row (i, j) holds its nz / 2 cells of that colour in k order.
+__host__ __device__ __forceinline__ long long split_index(const Dims &d, int i, int j, int k) {
+    const int col = (i + j + k) & 1;
+    return (long long)col * (d.n >> 1) + ((long long)i * d.ny + j) * (d.nz >> 1) + (k >> 1);
+}
+
+// Where the assembly kernels also write the split level 0's FP32 and FP16 operator copies and its row flags
+// (1 on a row with an active cell; cleared by the launcher first).  rows == nullptr: not written.
+struct SplitOut {
+    Coef<float> c32;
+    Coef<__half> c16;
+    uint8_t *rows;
+};
+
 __device__ __forceinline__ double ldv(const double *p, long long i) { return p[i]; }
 __device__ __forceinline__ float ldv(const float *p, long long i) { return p[i]; }
 __device__ __forceinline__ float ldv(const __half *p, long long i) { return __half2float(p[i]); }

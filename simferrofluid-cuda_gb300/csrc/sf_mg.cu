@@ -1722,6 +1722,15 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     return cudaGetLastError();
 }
 
+const SplitOut *MGSolver::split_targets() {
+    if (!split0_) return nullptr;
+    so_.c32 = c32_;
+    so_.c16 = c16s0_;
+    so_.rows = rows_[0];
+    copies_written_ = true;
+    return &so_;
+}
+
 cudaError_t MGSolver::build_hierarchy() {
     const int L = (int)lev_dims_.size();
     tk_.launches += prm_.precision == 0 ? (L - 1) : L;
@@ -1731,8 +1740,10 @@ cudaError_t MGSolver::build_hierarchy() {
                                                                                     lev_dims_[l], c64_[l]);
     } else {
         if (split0_) {
-            k_to_split<<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(lev_dims_[0], c64_[0], c32_, c16s0_,
-                                                                                rows_[0]);
+            if (!copies_written_)
+                k_to_split<<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(lev_dims_[0], c64_[0], c32_,
+                                                                                    c16s0_, rows_[0]);
+            copies_written_ = false;
             k_rows_uniform<float><<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(lev_dims_[0], c32_, rows_[0],
                                                                                           crow_);
             tk_.launches++;

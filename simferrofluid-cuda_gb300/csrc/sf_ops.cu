@@ -28,6 +28,23 @@ __device__ __forceinline__ bool le0(double v) {
 }
 __device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
 
+// The split level-0 copies of a cell's stored coefficients (same roundings as the solver's own conversion) and
+// its row's flag when the cell is active.
+__device__ __forceinline__ void split_store(const SplitOut &so, const Dims &d, int i, int j, int k, double ax,
+                                            double ay, double az, double dex, bool active) {
+    const long long q = split_index(d, i, j, k);
+    const float fx = (float)ax, fy = (float)ay, fz = (float)az, fd = (float)dex;
+    so.c32.ax[q] = fx;
+    so.c32.ay[q] = fy;
+    so.c32.az[q] = fz;
+    so.c32.dex[q] = fd;
+    so.c16.ax[q] = __float2half_rn(fx);
+    so.c16.ay[q] = __float2half_rn(fy);
+    so.c16.az[q] = __float2half_rn(fz);
+    so.c16.dex[q] = __float2half_rn(fd);
+    if (active) so.rows[(long long)i * d.ny + j] = 1;  // every writer stores 1
+}
+
 // ------------------------------------------------------------------------------------------------ pressure
 // Pressure::SetUnKnowns + BuildProjectionMatrix (core/Pressure.cpp:104-123, 38-78) for one cell.
 // Liquid cells are phi <= 0.  The face weight is w = 1 - fraction; faces on the outer grid boundary are
@@ -40,7 +57,7 @@ __device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong
 __global__ void __launch_bounds__(256) k_build_pressure(Dims d, const double *__restrict__ phi, Faces frac,
                                                         Faces u, Faces us, Faces jump, double vol_error,
                                                         Coef<double> cf, double *__restrict__ b, int rhs_only,
-                                                        int want_invd) {
+                                                        int want_invd, SplitOut so) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -82,6 +99,7 @@ __global__ void __launch_bounds__(256) k_build_pressure(Dims d, const double *__
             cf.dex[c] = 0.;
             cf.D[c] = 6.;
             if (want_invd) cf.invd[c] = 1. / 6.;
+            if (so.rows) split_store(so, d, i, j, k, 1., 1., 1., 0., true);
             return;
         }
     }
@@ -135,6 +153,7 @@ __global__ void __launch_bounds__(256) k_build_pressure(Dims d, const double *__
     cf.dex[c] = dexv;
     cf.D[c] = D;
     if (want_invd) cf.invd[c] = liquid ? (D > 0 ? 1. / D : 0.0) : 0.0;
+    if (so.rows) split_store(so, d, i, j, k, lower[0], lower[1], lower[2], dexv, D > 0);
 }
 
 // Pressure::ApplyProjection (core/Pressure.cpp:137-166) for the faces of axis a.  p is the solution on
@@ -188,21 +207,26 @@ __global__ void k_gather_cells(long long n, const double *__restrict__ D, const 
 }
 
 // ------------------------------------------------------------------------------------------------ magnetic
-// MagneticField::Heaviside (core/MagneticField.h:44-54).
-__device__ __forceinline__ double heaviside(double phi, double bw) {
-    const double pi = 3.141592653589793238462643383279502884;
+// MagneticField::Heaviside (core/MagneticField.h:44-54): 0 below -bw, 1 above bw (exactly, as the reference),
+// and in the band .5 (1 + t + sin(pi t) / pi) with t = phi / bw.  In the band it is evaluated with 1 / bw formed
+// on the host, sin(pi t) as sinpi(t) and a multiplication by 1 / pi: the reference's three FP64 divisions and
+// sin(pi * phi / bw) bound this kernel by the FP64 rate, and these forms agree with them to a few ulp (band faces
+// already differ from the reference's by the device's and the host's sin in the last bits).
+__device__ __forceinline__ double heaviside(double phi, double bw, double inv_bw) {
+    const double inv_pi = 0.318309886183790671537767526745028724;
     if (phi < -bw) return 0.;
     if (phi > bw) return 1.;
-    return .5 * (1. + phi / bw + sin(pi * phi / bw) / pi);
+    const double t = phi * inv_bw;
+    return .5 * (1. + t + sinpi(t) * inv_pi);
 }
 
 // mu on an interior face between cells lo and hi (core/MagneticField.cpp:57-58).  The reference samples phi
 // trilinearly at the face centre; at a face centre the trilinear weights are exactly (1/2, 1/2, 0, ...) when
 // the grid coordinates are exact binary fractions, which this expression reproduces bit for bit; otherwise
 // it differs from the reference's weights (1/2 +- 1 ulp) by a few ulp of phi.
-__device__ __forceinline__ double mu_face(double philo, double phihi, double chi, double bw) {
+__device__ __forceinline__ double mu_face(double philo, double phihi, double chi, double bw, double inv_bw) {
     const double pf = 0.5 * philo + 0.5 * phihi;
-    return 1. + (1. - heaviside(pf, bw)) * chi;
+    return 1. + (1. - heaviside(pf, bw, inv_bw)) * chi;
 }
 
 // Order-preserving integer key of a double (IEEE total order on finite values): comparisons of keys are
@@ -214,29 +238,35 @@ __device__ __forceinline__ long long okey(double v) {
 
 // mu_face with a fast path: when both cell values lie beyond +-bw (1 + 2^-40) the face value is beyond +-bw
 // too, so H is exactly 0 or 1 and mu is exactly 1 + chi (precomputed, same rounding) or 1.
-__device__ __forceinline__ double mu_face_fast(double philo, double phihi, double chi, double bw, long long khi,
-                                               long long klo, double one_plus_chi) {
+__device__ __forceinline__ double mu_face_fast(double philo, double phihi, double chi, double bw, double inv_bw,
+                                               long long khi, long long klo, double one_plus_chi) {
     const long long a = okey(philo), b = okey(phihi);
     if (a > khi && b > khi) return 1.;
     if (a < klo && b < klo) return one_plus_chi;
-    return mu_face(philo, phihi, chi, bw);
+    return mu_face(philo, phihi, chi, bw, inv_bw);
 }
 
 // BuildMatrix, coefficient pass (core/MagneticField.cpp:51-60): mu on the lower x/y/z face of every cell,
 // stored directly as the lower-face couplings ax/ay/az (0 on the grid boundary, where the reference's mu = 1
 // is never used).  Each face is evaluated once.
 __global__ void __launch_bounds__(256) k_magnetic_mu(Dims d, const double *__restrict__ phi, double chi, double bw,
-                                                     long long khi, long long klo, double one_plus_chi,
-                                                     Coef<double> cf) {
+                                                     double inv_bw, long long khi, long long klo,
+                                                     double one_plus_chi, Coef<double> cf, SplitOut so) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
     if (k >= d.nz || j >= d.ny) return;
     const long long c = cid(d, i, j, k);
     const double pc = phi[c];
-    cf.ax[c] = i > 0 ? mu_face_fast(phi[c - (long long)d.ny * d.nz], pc, chi, bw, khi, klo, one_plus_chi) : 0.0;
-    cf.ay[c] = j > 0 ? mu_face_fast(phi[c - d.nz], pc, chi, bw, khi, klo, one_plus_chi) : 0.0;
-    cf.az[c] = k > 0 ? mu_face_fast(phi[c - 1], pc, chi, bw, khi, klo, one_plus_chi) : 0.0;
+    const long long sx = (long long)d.ny * d.nz;
+    const double mx = i > 0 ? mu_face_fast(phi[c - sx], pc, chi, bw, inv_bw, khi, klo, one_plus_chi) : 0.0;
+    const double my = j > 0 ? mu_face_fast(phi[c - d.nz], pc, chi, bw, inv_bw, khi, klo, one_plus_chi) : 0.0;
+    const double mz = k > 0 ? mu_face_fast(phi[c - 1], pc, chi, bw, inv_bw, khi, klo, one_plus_chi) : 0.0;
+    cf.ax[c] = mx;
+    cf.ay[c] = my;
+    cf.az[c] = mz;
+    // the excess is 0 on every potential row; the row flag is set by k_magnetic_rows (D > 0)
+    if (so.rows) split_store(so, d, i, j, k, mx, my, mz, 0., false);
 }
 
 // BuildMatrix, row pass + AssembleRHS (core/MagneticField.cpp:62-118) in Neumann form: D = sum of mu over the
@@ -252,13 +282,14 @@ __global__ void __launch_bounds__(256) k_magnetic_mu(Dims d, const double *__res
 __global__ void __launch_bounds__(256) k_magnetic_rows(Dims d, Faces hext, double h, Coef<double> cf,
                                                        double *__restrict__ b, int want_invd,
                                                        long long liq_bits, double m1, double sv6,
-                                                       double inv_sv6) {
+                                                       double inv_sv6, uint8_t *__restrict__ rows) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
     if (k >= d.nz || j >= d.ny) return;
     const long long c = cid(d, i, j, k);
     const long long sx = (long long)d.ny * d.nz, sy = d.nz;
+    if (rows) rows[(long long)i * d.ny + j] = 1;  // D > 0: every in-grid mu is at least 1
     if (i > 0 && i < d.nx - 1 && j > 0 && j < d.ny - 1 && k > 0 && k < d.nz - 1) {
         const long long m[6] = {__double_as_longlong(cf.ax[c]), __double_as_longlong(cf.ax[c + sx]),
                                 __double_as_longlong(cf.ay[c]), __double_as_longlong(cf.ay[c + sy]),
@@ -349,7 +380,8 @@ static __device__ __align__(256) unsigned g_noalloc_ticket[1 + kNoAllocGroups];
 // k_magnetic_rows form them (each face value is evaluated by both of its cells), so nothing is stored.
 // Tiles of 32 (z) x 8 (y) cells, `xpb` x-planes per block; result[0] = relative residual, result[1] = ||b||.
 __global__ void __launch_bounds__(256) k_magnetic_residual(Dims d, int xpb, const double *__restrict__ phi,
-                                                           double chi, double bw, long long khi, long long klo,
+                                                           double chi, double bw, double inv_bw, long long khi,
+                                                           long long klo,
                                                            double one_plus_chi, Faces hext, double h,
                                                            const double *__restrict__ psi, double *part,
                                                            unsigned *ticket, double *result) {
@@ -376,8 +408,8 @@ __global__ void __launch_bounds__(256) k_magnetic_residual(Dims d, int xpb, cons
                 const long long st = a == 0 ? sx : (a == 1 ? sy : 1);
                 const long long nb = up ? c + st : c - st;
                 const double pn = phi[nb];
-                const double mu = up ? mu_face_fast(pc, pn, chi, bw, khi, klo, one_plus_chi)
-                                     : mu_face_fast(pn, pc, chi, bw, khi, klo, one_plus_chi);
+                const double mu = up ? mu_face_fast(pc, pn, chi, bw, inv_bw, khi, klo, one_plus_chi)
+                                     : mu_face_fast(pn, pc, chi, bw, inv_bw, khi, klo, one_plus_chi);
                 diag += mu;
                 if (mu != 1.) {
                     const int fi = i + (a == 0) * up, fj = j + (a == 1) * up, fk = k + (a == 2) * up;
@@ -413,9 +445,14 @@ static inline int flat_grid(long long n) {
 // ------------------------------------------------------------------------------------------------ launchers
 void launch_build_pressure(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &u,
                            const Faces &us, const Faces &jump, double vol_error, Coef<double> &cf, double *b,
-                           bool rhs_only, bool want_invd) {
+                           bool rhs_only, bool want_invd, const SplitOut *so) {
+    SplitOut o{};
+    if (so && !rhs_only) {
+        o = *so;
+        cudaMemsetAsync(o.rows, 0, (size_t)d.nx * d.ny, st);
+    }
     k_build_pressure<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, frac, u, us, jump, vol_error, cf, b,
-                                                                  rhs_only ? 1 : 0, want_invd ? 1 : 0);
+                                                                  rhs_only ? 1 : 0, want_invd ? 1 : 0, o);
 }
 
 void launch_apply_projection(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &jump,
@@ -434,7 +471,8 @@ void launch_gather_cells(cudaStream_t st, long long n, const double *D, const do
 }
 
 int launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, double chi, double bw,
-                          const Faces &hext, double h, Coef<double> &cf, double *b, bool want_invd) {
+                          const Faces &hext, double h, Coef<double> &cf, double *b, bool want_invd,
+                          const SplitOut *so) {
     // band thresholds as integer keys: |phi| > bw (1 + 2^-40) on both cells implies |phi_face| > bw exactly
     const double t = bw * (1.0 + std::ldexp(1.0, -40));
     auto key = [](double v) {
@@ -450,9 +488,12 @@ int launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, dou
     const double m1 = one_plus_chi - 1.;
     long long liq_bits;
     std::memcpy(&liq_bits, &one_plus_chi, 8);
-    k_magnetic_mu<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, chi, bw, key(t), key(-t), one_plus_chi, cf);
+    SplitOut o{};
+    if (so) o = *so;
+    k_magnetic_mu<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, chi, bw, 1.0 / bw, key(t), key(-t),
+                                                              one_plus_chi, cf, o);
     k_magnetic_rows<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, hext, h, cf, b, want_invd ? 1 : 0, liq_bits, m1,
-                                                                 sv6, sv6 > 0 ? 1. / sv6 : 0.);
+                                                                 sv6, sv6 > 0 ? 1. / sv6 : 0., o.rows);
     return 2;
 }
 
@@ -508,8 +549,8 @@ cudaError_t launch_magnetic_residual_noalloc(cudaStream_t st, const Dims &d, con
         return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
     };
     const double one_plus_chi = 1. + (1. - 0.) * chi;
-    k_magnetic_residual<<<grid, blk2(), 0, st>>>(d, xpb, phi, chi, bw, key(t), key(-t), one_plus_chi, hext, h, psi,
-                                                 part, ticket, result);
+    k_magnetic_residual<<<grid, blk2(), 0, st>>>(d, xpb, phi, chi, bw, 1.0 / bw, key(t), key(-t), one_plus_chi, hext,
+                                                 h, psi, part, ticket, result);
     return cudaGetLastError();
 }
 

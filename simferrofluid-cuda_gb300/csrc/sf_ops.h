@@ -13,12 +13,13 @@ struct Faces {
 
 void launch_build_pressure(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &u,
                            const Faces &us, const Faces &jump, double vol_error, Coef<double> &cf, double *b,
-                           bool rhs_only, bool want_invd);
+                           bool rhs_only, bool want_invd, const SplitOut *so = nullptr);
 void launch_apply_projection(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &jump,
                              const double *p, const Faces &u);
 void launch_gather_cells(cudaStream_t st, long long n, const double *D, const double *x, double *out);
 int launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, double chi, double bw,
-                          const Faces &hext, double h, Coef<double> &cf, double *b, bool want_invd);
+                          const Faces &hext, double h, Coef<double> &cf, double *b, bool want_invd,
+                          const SplitOut *so = nullptr);
 void launch_total_field(cudaStream_t st, const Dims &d, const double *psi, const Faces &hext, double invh,
                         const Faces &H);
 // Allocation-free residual of a potential on the pinned magnetostatic system (static scratch, see sf_ops.cu).

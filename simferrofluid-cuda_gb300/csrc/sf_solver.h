@@ -95,6 +95,10 @@ class MGSolver {
     // Build coarse levels (and the FP32/FP16 copies for the mixed form) from the fine operator.
     cudaError_t build_hierarchy();
 
+    // Where the assembly kernels may write the split level-0 copies and row flags directly (smoother 3 in the
+    // mixed form), or nullptr; the next build_hierarchy then takes them as written.
+    const SplitOut *split_targets();
+
     // Solve A x = b.  x holds the initial guess unless x_is_zero.  exclude_cell0_norm: report the residual
     // without row 0 (the potential's pinned row).
     cudaError_t solve(bool x_is_zero, SolveResult &res);
@@ -150,6 +154,8 @@ class MGSolver {
     float *crow_ = nullptr;              // level 0: the coupling of each uniform row
     float *crow1_ = nullptr;             // level 1 (split): the same
     bool split1_ = false;                // level 1 stored colour by colour too
+    SplitOut so_{};                      // split_targets()
+    bool copies_written_ = false;        // the assembly wrote the split copies and flags
     Coef<__half> c16s1_{};               // its split FP16 operator copy (the natural copy feeds level 2)
     int *list_cnt_ = nullptr;            // per block of rows: general and uniform counts (list building)
     std::vector<float *> x32_, b32_, t32_;

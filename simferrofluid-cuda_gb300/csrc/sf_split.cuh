@@ -16,11 +16,6 @@
 // natural kernels' own; the restriction after the pre-smoothing sums only the colour that was not updated last
 // (the other colour's residual is zero up to rounding), so a V-cycle agrees with the natural one to rounding.
 
-__host__ __device__ __forceinline__ long long split_index(const Dims &d, int i, int j, int k) {
-    const int col = (i + j + k) & 1;
-    return (long long)col * (d.n >> 1) + ((long long)i * d.ny + j) * (d.nz >> 1) + (k >> 1);
-}
-
 // Grid-stride loop over the rows (i, j) of the split layout, blockDim.y rows per block and blockDim.x threads
 // along a row, without a per-element division: for each m, cell k = 2m + p is colour 0 and k = 2m + 1 - p is
 // colour 1 (p the row's parity), both stored at m of their colour's half.  `nat` is the row's first natural

@@ -130,8 +130,9 @@ def _check_magnetic(sc, mu, A, b, b0n, D, lower, rhs):
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("n", [32, 40])
 def test_magnetic_assembly(sfpkg, oracle, gpu_ctx, precision, n):
-    """Bit for bit on rows away from the interface.  On faces in the band, mu goes through sin(), and the
-    device's double sin() and the host C library's may differ in the last bit; at h = 1/40 the reference's
+    """Bit for bit on rows away from the interface.  On faces in the band, mu goes through the Heaviside's
+    sin(): the device evaluates it as sinpi(phi / bw) with 1 / bw and 1 / pi formed on the host, which agrees
+    with the reference's expression and the host C library's sin() to a few ulp; at h = 1/40 the reference's
     trilinear sample of phi at a face centre also differs from the two-cell mean by an ulp (weights 1/2 +- an
     ulp).  There the entries agree to 1e-13 of their scale."""
     sc = scenes().pool_sphere(n, seed=10, chi=2.0)
