@@ -49,6 +49,8 @@ def parse(argv=None):
     ap.add_argument("--coarse-dim", type=int, default=None)
     ap.add_argument("--pre", type=int, default=None)
     ap.add_argument("--post", type=int, default=None)
+    ap.add_argument("--coarse-pre", type=int, default=None, help="smoothing sweeps before restriction, levels >= 2")
+    ap.add_argument("--coarse-post", type=int, default=None, help="smoothing sweeps after prolongation, levels >= 2")
     ap.add_argument("--smoother", type=int, default=None,
                     help="0 two-colour, 1 fused one-pass, 2 two-colour with FP16 finest-level smoothing coefficients, "
                          "3 (default) as 2 with the finest level stored colour by colour")
@@ -204,6 +206,7 @@ def run_ours(args, ws, rank, local):
     def opts(which, precision, profile=0):
         kw = {}
         for name, key in (("inner_tol", "inner_tol"), ("coarse_dim", "coarse_dim"), ("pre", "pre_smooth"),
+                          ("coarse_pre", "coarse_pre"), ("coarse_post", "coarse_post"),
                           ("post", "post_smooth"), ("smoother", "smoother")):
             v = getattr(args, name)
             if v is not None:
@@ -349,7 +352,8 @@ def run_ours(args, ws, rank, local):
                                f"{args.precision} MGPCG to {args.tol:g} from zero",
                    "grid": [args.n] * 3, "precision": args.precision, "tol": args.tol,
                    "l2": "inputs larger than L2 (each field 134 MB at 256^3)", "parallelism": f"replicas x{ws}",
-                   "solver": {k: getattr(args, k) for k in ("inner_tol", "coarse_dim", "pre", "post", "smoother")
+                   "solver": {k: getattr(args, k)
+                              for k in ("inner_tol", "coarse_dim", "pre", "post", "coarse_pre", "coarse_post", "smoother")
                               if getattr(args, k) is not None}},
         "iters": {"pressure": it_p, "magnetic": it_m}, "max_rel_residual": {"pressure": res_p, "magnetic": res_m},
         "fp64_mgpcg": fp64,

@@ -81,7 +81,9 @@ typedef struct {
                             as 2, with the mixed form's finest-level FP32 vectors and operator copies stored
                             colour by colour (each half sweep streams one colour); needs nz % 8 == 0 and two or
                             more levels, else runs as 2.  FP64 solves run 2 and 3 as 0. */
-    int reserved[6];
+    int coarse_pre;      /* pre- / post-smoothing sweeps on levels 2 and coarser (0: as pre_smooth / post_smooth) */
+    int coarse_post;
+    int reserved[4];
 } sf_solve_opts;
 
 typedef struct {

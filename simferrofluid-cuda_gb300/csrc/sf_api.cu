@@ -82,6 +82,8 @@ SolverParams params_from(const sf_solve_opts *o, int which) {
     p.pre = o->pre_smooth > 0 ? o->pre_smooth : def.pre_smooth;
     p.post = o->post_smooth > 0 ? o->post_smooth : def.post_smooth;
     p.coarse_sweeps = o->coarse_sweeps > 0 ? o->coarse_sweeps : def.coarse_sweeps;
+    p.coarse_pre = o->coarse_pre > 0 ? o->coarse_pre : p.pre;
+    p.coarse_post = o->coarse_post > 0 ? o->coarse_post : p.post;
     p.max_levels = o->max_levels;
     p.coarse_dim = o->coarse_dim > 0 ? o->coarse_dim : def.coarse_dim;
     p.use_graph = o->use_graph != 0;

@@ -1486,7 +1486,8 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
                 continue;
             }
         }
-        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.pre, true, false, R(l));
+        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], l >= 2 ? p.coarse_pre : p.pre, true, false,
+                      R(l));
         restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1], false, R(l), R(l + 1));
     }
     coarse_solve<T, Cc>(st, tk, dims[L - 1], cc[L - 1], xs[L - 1], bs[L - 1], p.coarse_sweeps);
@@ -1503,7 +1504,8 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
             }
         }
         launch_pdl(k_prolong<T>, grid_cells(dims[l]), blk2(), st, dims[l], xs[l], dims[l + 1], xs[l + 1], R(l));
-        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], p.post, false, false, R(l));
+        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], l >= 2 ? p.coarse_post : p.post, false,
+                      false, R(l));
     }
     tk.launches++;
     if constexpr (std::is_same<T, float>::value) {
@@ -1879,7 +1881,7 @@ cudaError_t MGSolver::run_iter(bool mixed) {
         return cudaGetLastError();
     }
     const int key = (prm_.pre << 0) | (prm_.post << 4) | (prm_.coarse_sweeps << 8) | ((prm_.flexible ? 1 : 0) << 20) |
-                    (prm_.smoother << 21);
+                    (prm_.smoother << 21) | (prm_.coarse_pre << 24) | (prm_.coarse_post << 28);
     if (key != graph_key_) destroy_graphs();
     graph_key_ = key;
     cudaGraphExec_t &ge = mixed ? g_iter32_ : g_iter64_;

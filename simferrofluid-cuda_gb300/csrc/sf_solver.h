@@ -20,6 +20,7 @@ struct SolverParams {
     double tol = 1e-8;
     int max_iters = 200;
     int pre = 2, post = 2, coarse_sweeps = 24;
+    int coarse_pre = 2, coarse_post = 2;  // levels 2 and coarser
     int max_levels = 0, coarse_dim = 8;
     bool use_graph = true;
     int check_every = 1;
