@@ -51,6 +51,10 @@ def parse(argv=None):
     ap.add_argument("--post", type=int, default=None)
     ap.add_argument("--coarse-pre", type=int, default=None, help="smoothing sweeps before restriction, levels >= 2")
     ap.add_argument("--coarse-post", type=int, default=None, help="smoothing sweeps after prolongation, levels >= 2")
+    ap.add_argument("--coarse-sweeps", type=int, default=None, help="symmetric sweep pairs on the coarsest level")
+    ap.add_argument("--coarse-tail", type=int, default=None,
+                    help="levels of at most 65,536 cells: 0 one cluster launch (16 CTAs, else 8), 8 / 16 that "
+                         "cluster size, 1 separate kernels")
     ap.add_argument("--smoother", type=int, default=None,
                     help="0 two-colour, 1 fused one-pass, 2 two-colour with FP16 finest-level smoothing coefficients, "
                          "3 (default) as 2 with the finest level stored colour by colour")
@@ -207,7 +211,8 @@ def run_ours(args, ws, rank, local):
         kw = {}
         for name, key in (("inner_tol", "inner_tol"), ("coarse_dim", "coarse_dim"), ("pre", "pre_smooth"),
                           ("coarse_pre", "coarse_pre"), ("coarse_post", "coarse_post"),
-                          ("post", "post_smooth"), ("smoother", "smoother")):
+                          ("post", "post_smooth"), ("smoother", "smoother"),
+                          ("coarse_tail", "coarse_tail"), ("coarse_sweeps", "coarse_sweeps")):
             v = getattr(args, name)
             if v is not None:
                 kw[key] = v
@@ -353,7 +358,8 @@ def run_ours(args, ws, rank, local):
                    "grid": [args.n] * 3, "precision": args.precision, "tol": args.tol,
                    "l2": "inputs larger than L2 (each field 134 MB at 256^3)", "parallelism": f"replicas x{ws}",
                    "solver": {k: getattr(args, k)
-                              for k in ("inner_tol", "coarse_dim", "pre", "post", "coarse_pre", "coarse_post", "smoother")
+                              for k in ("inner_tol", "coarse_dim", "pre", "post", "coarse_pre", "coarse_post", "smoother",
+                                        "coarse_tail", "coarse_sweeps")
                               if getattr(args, k) is not None}},
         "iters": {"pressure": it_p, "magnetic": it_m}, "max_rel_residual": {"pressure": res_p, "magnetic": res_m},
         "fp64_mgpcg": fp64,

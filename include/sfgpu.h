@@ -83,7 +83,10 @@ typedef struct {
                             more levels, else runs as 2.  FP64 solves run 2 and 3 as 0. */
     int coarse_pre;      /* pre- / post-smoothing sweeps on levels 2 and coarser (0: as pre_smooth / post_smooth) */
     int coarse_post;
-    int reserved[4];
+    int coarse_tail;     /* mixed form, levels of at most 65,536 cells: 0 (default) one launch of a thread-block
+                            cluster of 16 CTAs where the device runs it, else 8; 8 or 16 that cluster size; 1 separate
+                            kernels.  All give the same results. */
+    int reserved[3];
 } sf_solve_opts;
 
 typedef struct {

@@ -51,7 +51,7 @@ class sf_solve_opts(C.Structure):
                 ("coarse_dim", C.c_int), ("warm_start", C.c_int), ("use_graph", C.c_int),
                 ("check_every", C.c_int), ("report_ref_residual", C.c_int), ("inner_tol", C.c_double),
                 ("profile", C.c_int), ("smoother", C.c_int), ("coarse_pre", C.c_int), ("coarse_post", C.c_int),
-                ("reserved", C.c_int * 4)]
+                ("coarse_tail", C.c_int), ("reserved", C.c_int * 3)]
 
 
 class sf_solve_stats(C.Structure):

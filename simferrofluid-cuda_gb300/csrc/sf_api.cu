@@ -92,6 +92,7 @@ SolverParams params_from(const sf_solve_opts *o, int which) {
     p.flexible = false;
     p.profile = o->profile != 0;
     p.smoother = o->smoother;
+    p.tail = o->coarse_tail;
     return p;
 }
 
@@ -100,6 +101,7 @@ bool opts_ok(const sf_solve_opts *o) {
     if (o->precision != SF_PREC_FP64 && o->precision != SF_PREC_MIXED && o->precision != SF_PREC_LEARNED) return false;
     if (o->max_levels < 0 || o->coarse_dim < 0) return false;
     if (o->smoother < 0 || o->smoother > 3) return false;
+    if (o->coarse_tail != 0 && o->coarse_tail != 1 && o->coarse_tail != 8 && o->coarse_tail != 16) return false;
     return true;
 }
 

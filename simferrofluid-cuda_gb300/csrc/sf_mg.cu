@@ -15,6 +15,9 @@
 // The FP64 form keeps everything in double.  The mixed form runs the V-cycle in FP32 with FP32 level-0 and
 // FP16 coarse coefficients inside an FP32 flexible CG, wrapped in FP64 iterative refinement: only the outer
 // residual r = b - A x, the update x += d and the dot products stay FP64.
+#include <cooperative_groups.h>
+
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1054,6 +1057,7 @@ static void apply_dot32(cudaStream_t st, const Dims &d, const Coef<float> &cf, c
 }
 
 #include "sf_split.cuh"
+#include "sf_tail.cuh"
 
 // rho_new = (r, z), zq = (z, q); beta = flexible ? -alpha*zq/rho : rho_new/rho; rho = rho_new
 template <class T>
@@ -1459,7 +1463,8 @@ template <class T, class C0, class Cc, class C0S>
 static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, const Coef<C0> &c0,
                    const Coef<C0S> &c0s, const std::vector<Coef<Cc>> &cc, T *z, const T *r,
                    const std::vector<T *> &xs, const std::vector<T *> &bs, const std::vector<T *> &ts,
-                   const SolverParams &p, bool split0 = false, const RowSets *rs = nullptr) {
+                   const SolverParams &p, bool split0 = false, const RowSets *rs = nullptr, int tail_lt = -1,
+                   int tail_smem = 0, int tail_nc = 8, float *const *tail_op = nullptr) {
     const int L = (int)dims.size();
     if (L == 1) {
         coarse_solve<T, C0>(st, tk, dims[0], c0, z, r, p.coarse_sweeps);
@@ -1475,7 +1480,13 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
     smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true, split0, R(0), LST(0), CNT(0), cr);
     // the residual of the smoothed operator
     restrict_res<T, C0S>(st, tk, dims[0], c0s, z, r, dims[1], bs[1], split0, R(0), R(1), LST(1), CNT(1), cr, split1);
-    for (int l = 1; l < L - 1; l++) {
+    // levels from `bottom` on are solved in one piece: the coarsest solve, or the fused tail (one cluster launch
+    // for every level from tail_lt on)
+    bool tail = false;
+    if constexpr (std::is_same<T, float>::value && std::is_same<Cc, __half>::value)
+        tail = tail_lt >= (split1 ? 2 : 1) && tail_lt < L - 1;
+    const int bottom = tail ? tail_lt : L - 1;
+    for (int l = 1; l < bottom; l++) {
         if constexpr (std::is_same<T, float>::value && std::is_same<Cc, __half>::value) {
             if (l == 1 && split1) {
                 const Coef<__half> &c1 = *rs->c1s;
@@ -1490,8 +1501,27 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
                       R(l));
         restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1], false, R(l), R(l + 1));
     }
-    coarse_solve<T, Cc>(st, tk, dims[L - 1], cc[L - 1], xs[L - 1], bs[L - 1], p.coarse_sweeps);
-    for (int l = L - 2; l >= 1; l--) {
+    if constexpr (std::is_same<T, float>::value && std::is_same<Cc, __half>::value) {
+        if (tail) {
+            TailParams P{};
+            int smem = 0;
+            tail_plan(dims, tail_lt, tail_nc, P, smem);
+            for (int l = 0; l < P.nlev; l++) {
+                P.lv[l].cf = cc[tail_lt + l];
+                P.lv[l].unscale = cc[tail_lt + l].unscale;
+                P.lv[l].op = tail_op[tail_lt + l];
+                P.lv[l].pre = tail_lt + l >= 2 ? p.coarse_pre : p.pre;
+                P.lv[l].post = tail_lt + l >= 2 ? p.coarse_post : p.post;
+            }
+            P.b0 = bs[tail_lt];
+            P.x0 = xs[tail_lt];
+            P.pairs = p.coarse_sweeps;
+            tk.launches++;
+            launch_tail(st, tail_nc, P, tail_smem);
+        }
+    }
+    if (!tail) coarse_solve<T, Cc>(st, tk, dims[L - 1], cc[L - 1], xs[L - 1], bs[L - 1], p.coarse_sweeps);
+    for (int l = bottom - 1; l >= 1; l--) {
         tk.launches++;
         if constexpr (std::is_same<T, float>::value && std::is_same<Cc, __half>::value) {
             if (l == 1 && split1) {
@@ -1585,7 +1615,10 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
                       (p.precision == 0 ||
                        ((cfg_smoother_ == 2 || cfg_smoother_ == 3) == fp16copy && cfg_split_ == split0));
     prm_ = p;
-    if (same) return cudaSuccess;
+    if (same) {
+        plan_tail();
+        return cudaSuccess;
+    }
     destroy_graphs();
     free_all();
     lev_dims_ = dims;
@@ -1644,6 +1677,9 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
             c16s0_.scale = c16s0_.unscale = 1.f;
         }
         c16_.assign(L, Coef<__half>{});
+        tail_op_.assign(L, nullptr);
+        for (int l = 1; l < L; l++)
+            if (dims[l].n <= kTailMaxCells) tail_op_[l] = (float *)chk(A(4 * (size_t)kTailOps * dims[l].n));
         x32_.assign(L, nullptr);
         b32_.assign(L, nullptr);
         t32_.assign(L, nullptr);
@@ -1721,7 +1757,32 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
                             (const void *)k_xpby_s, (const void *)k_update_s, (const void *)k_ir_update_s};
         for (const void *k : ks) resident_grid(k);
     }
+    plan_tail();
     return cudaGetLastError();
+}
+
+// The fused tail (sf_tail.cuh) of the mixed V-cycle: from the first level of at most kTailMaxCells cells below
+// the split levels, when its layout fits in shared memory and one cluster of it fits on the device.
+void MGSolver::plan_tail() {
+    tail_lt_ = -1;
+    tail_smem_ = tail_nc_ = 0;
+    if (prm_.precision != 1 || prm_.tail == 1) return;
+    const int L = (int)lev_dims_.size();
+    for (int nc : {16, 8}) {
+        if (prm_.tail != 0 && prm_.tail != nc) continue;
+        for (int lt = split1_ ? 2 : 1; lt < L - 1; lt++) {
+            TailParams P{};
+            int smem = 0;
+            if (lev_dims_[lt].n > kTailMaxCells || !tail_plan(lev_dims_, lt, nc, P, smem)) continue;
+            if (nc == 16 ? tail_launchable<16>(smem) : tail_launchable<8>(smem)) {
+                tail_lt_ = lt;
+                tail_smem_ = smem;
+                tail_nc_ = nc;
+                return;
+            }
+            break;
+        }
+    }
 }
 
 const SplitOut *MGSolver::split_targets() {
@@ -1807,6 +1868,11 @@ cudaError_t MGSolver::build_hierarchy() {
         for (int l = 2; l < L; l++)
             k_coarsen<__half, __half><<<grid_cells(lev_dims_[l]), blk2(), 0, st_>>>(lev_dims_[l - 1], c16_[l - 1],
                                                                                     lev_dims_[l], c16_[l]);
+        // the fused tail's FP32 operator of its levels above the coarsest
+        for (int l = std::max(tail_lt_, 1); tail_lt_ >= 0 && l < L - 1; l++) {
+            k_tail_op<<<grid_cells(lev_dims_[l]), blk2(), 0, st_>>>(lev_dims_[l], c16_[l], tail_op_[l]);
+            tk_.launches++;
+        }
     }
     return cudaGetLastError();
 }
@@ -1841,7 +1907,7 @@ void MGSolver::enqueue_iter32() {
                          split1_ ? &c16s1_ : nullptr};
         const int *lst0 = list_[0], *cnt0 = count_;
         vcycle<float, float, __half, __half>(st_, tk_, lev_dims_, c32_, c16s0_, c16_, z32_, ri32_, x32_, b32_, ts,
-                                             prm_, true, &rs);
+                                             prm_, true, &rs, tail_lt_, tail_smem_, tail_nc_, tail_op_.data());
         const long long vitems = split_items(2LL * d.nx * d.ny, d.nz >> 3);
         launch_pdl(k_dot_rz_s, row_grid((const void *)k_dot_rz_s, vitems), dim3(32, 8), st_, d, ri32_, z32_, q32_,
                    lst0, cnt0, 1, sc_, part_, ticket_);
@@ -1857,10 +1923,10 @@ void MGSolver::enqueue_iter32() {
     }
     if (prm_.smoother == 2 || prm_.smoother == 3)
         vcycle<float, float, __half, __half>(st_, tk_, lev_dims_, c32_, c16s0_, c16_, z32_, ri32_, x32_, b32_, ts,
-                                             prm_);
+                                             prm_, false, nullptr, tail_lt_, tail_smem_, tail_nc_, tail_op_.data());
     else
         vcycle<float, float, __half, float>(st_, tk_, lev_dims_, c32_, c32_, c16_, z32_, ri32_, x32_, b32_, ts,
-                                            prm_);
+                                            prm_, false, nullptr, tail_lt_, tail_smem_, tail_nc_, tail_op_.data());
     launch_pdl(k_dot_rz<float>, kMaxRedBlocks, dim3(32, 8), st_, n, ri32_, z32_, q32_, 1, sc_, part_, ticket_);
     launch_pdl(k_xpby<float>, flat_grid(n), 256, st_, n, z32_, p32_, sc_);
     apply_dot32(st_, d, c32_, p32_, q32_, sc_, part_, ticket_);
@@ -1880,8 +1946,10 @@ cudaError_t MGSolver::run_iter(bool mixed) {
             enqueue_iter64();
         return cudaGetLastError();
     }
-    const int key = (prm_.pre << 0) | (prm_.post << 4) | (prm_.coarse_sweeps << 8) | ((prm_.flexible ? 1 : 0) << 20) |
-                    (prm_.smoother << 21) | (prm_.coarse_pre << 24) | (prm_.coarse_post << 28);
+    const long long key = (long long)prm_.pre | ((long long)prm_.post << 8) | ((long long)prm_.coarse_sweeps << 16) |
+                          ((long long)prm_.flexible << 32) | ((long long)prm_.smoother << 33) |
+                          ((long long)prm_.coarse_pre << 36) | ((long long)prm_.coarse_post << 44) |
+                          ((long long)tail_nc_ << 52);
     if (key != graph_key_) destroy_graphs();
     graph_key_ = key;
     cudaGraphExec_t &ge = mixed ? g_iter32_ : g_iter64_;

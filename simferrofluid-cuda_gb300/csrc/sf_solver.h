@@ -28,6 +28,8 @@ struct SolverParams {
     bool flexible = false;  // Polak-Ribiere beta (needed when the preconditioner is not a fixed SPD operator)
     bool profile = false;   // time finest-level smoother launches with events (no graphs)
     int smoother = 0;       // 0: two in-place colour kernels, 1: fused one-pass red-black sweep
+    int tail = 0;  // mixed form, levels of at most 65,536 cells: 0 one cluster launch (16 CTAs, else 8), 8 / 16 that
+                   // cluster size, 1 separate kernels
 };
 
 // Counts kernel launches and, when profiling, brackets finest-level smoother launches with events.
@@ -143,7 +145,7 @@ class MGSolver {
     std::vector<double *> t64_;        // smoother scratch per level
     // mixed: level 0 FP32, levels >= 1 FP16
     Coef<float> c32_{};
-    std::vector<Coef<__half>> c16_;  // index l-1 for level l
+    std::vector<Coef<__half>> c16_;  // index l for level l >= 1
     Coef<__half> c16s0_{};           // level 0 in FP16, read only by the level-0 smoother (smoothers 2 and 3)
     // smoother 3 in effect: level 0's FP32 vectors and both of its operator copies are stored colour by colour
     // (sf_split.cuh); the FP64 operator and vectors keep the natural layout
@@ -157,6 +159,10 @@ class MGSolver {
     bool split1_ = false;                // level 1 stored colour by colour too
     SplitOut so_{};                      // split_targets()
     bool copies_written_ = false;        // the assembly wrote the split copies and flags
+    int tail_lt_ = -1, tail_smem_ = 0;   // first level of the fused tail (-1: none), its shared memory
+    int tail_nc_ = 0;                    // its cluster size
+    std::vector<float *> tail_op_;       // per level of at most 65,536 cells: the tail's FP32 operator (k_tail_op)
+    void plan_tail();
     Coef<__half> c16s1_{};               // its split FP16 operator copy (the natural copy feeds level 2)
     int *list_cnt_ = nullptr;            // per block of rows: general and uniform counts (list building)
     std::vector<float *> x32_, b32_, t32_;
@@ -171,7 +177,7 @@ class MGSolver {
     unsigned *ticket_ = nullptr;
 
     cudaGraphExec_t g_iter64_ = nullptr, g_iter32_ = nullptr;
-    int graph_key_ = -1;
+    long long graph_key_ = -1;
     long long iter_launches64_ = 0, iter_launches32_ = 0;
     Tracker tk_;
 

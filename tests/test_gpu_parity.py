@@ -293,3 +293,40 @@ def test_split_level_matches_natural(sfpkg, gpu_ctx, shape):
     else:
         assert out[0][1] == out[1][1] and out[0][3] == out[1][3]
         assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("smoother", [2, 3])
+@pytest.mark.parametrize("shape", [(64, 64, 64), (50, 44, 40), (96, 80, 72), (37, 21, 70), (20, 16, 76),
+                                   (80, 80, 80), (9, 13, 8)])
+def test_cluster_tail_bit_identical(sfpkg, gpu_ctx, smoother, shape):
+    """The mixed V-cycle's levels of at most 65,536 cells run by default in one launch of a thread-block cluster
+    (coarse_tail 0: 16 CTAs where the device runs it, else 8; 8 and 16 force the size); coarse_tail=1 runs them as
+    separate kernels.  Every cell's arithmetic is the same, so all forms take the same iterations and return the
+    same bits.  The shapes give tails of two to five levels: all held by CTA 0, distributed over the cluster
+    then held by CTA 0, and (80^3 with smoother 2) two distributed levels; shares of unequal plane counts across
+    the cluster, odd nz, and (9, 13, 8) a hierarchy too short for a tail (same launches)."""
+    g = sfpkg.StaggeredGrid.from_origin(1.0 / shape[0], shape)
+    rng = np.random.default_rng(sum(shape) + 11)
+    ys = scenes().cell_centres(g, 1)
+    phi = np.ascontiguousarray(np.broadcast_to((ys - 0.45 * ys.max())[None, :, None], g.shape)) \
+        + 0.02 * rng.uniform(-1, 1, g.shape)
+    frac = scenes().box_fractions(g)
+    vel = [rng.uniform(-1, 1, g.face_shape(a)) for a in range(3)]
+    hext = scenes().dipole_field(g)
+    out = []
+    for tail in (1, 8, 16, 0):
+        P = sfpkg.Pressure(g, gpu_ctx)
+        st = P.project(_copy(vel), phi, frac, opts=sfpkg.options(
+            "pressure", precision="mixed", smoother=smoother, tol=1e-9, coarse_tail=tail))
+        M = sfpkg.MagneticField(g, 1.5, 2 * g.spacing, gpu_ctx)
+        sm = M.solve(phi, hext, opts=sfpkg.options("magnetic", precision="mixed", smoother=smoother, tol=1e-8,
+                                                     warm_start=0, coarse_tail=tail))
+        assert st["converged"] == 1 and sm["converged"] == 1
+        out.append((P.pressure.copy(), st["iters"], M.potential.copy(), sm["iters"], st["kernel_launches"]))
+    for o in out[1:]:
+        assert o[1] == out[0][1] and o[3] == out[0][3], (out[0][1::2], o[1::2])
+        assert np.array_equal(o[0], out[0][0]) and np.array_equal(o[2], out[0][2])
+        if shape == (9, 13, 8):
+            assert o[4] == out[0][4]
+        else:
+            assert o[4] < out[0][4], (out[0][4], o[4])
