@@ -635,7 +635,7 @@ void sf_default_opts(sf_solve_opts *o, int which) {
     o->max_iters = 200;
     o->pre_smooth = 2;
     o->post_smooth = 2;
-    o->coarse_sweeps = 24;
+    o->coarse_sweeps = 48;
     o->max_levels = 0;
     o->coarse_dim = 8;
     o->warm_start = 1;

@@ -739,10 +739,42 @@ __global__ void __launch_bounds__(256) k_prolong(Dims d, T *__restrict__ x, Dims
     x[cid(d, i, j, k)] += xc[cid(dc, i >> 1, j >> 1, k >> 1)];
 }
 
-// Coarsest level: one block, x = 0 then the palindromic sequence red, (black, red) x pairs.
+// Coarsest level: one block, x = 0 then the palindromic sequence red, (black, red) x pairs.  Grids of at most
+// kCoarseMax cells first make b consistent on a pure-Neumann level (coarse_consistent).
 // Grids of at most kCoarseMax cells keep x in shared memory and each thread's couplings, inverse diagonal and
 // right-hand side in registers, so the sweeps touch no global memory; larger grids sweep in global memory.
 constexpr int kCoarseMax = 1024, kCoarseThreads = 1024;
+
+// A coarsest level without any diagonal excess (a pure-Neumann system: the operator annihilates the constant) is
+// solvable only for a right-hand side of zero sum over its active cells.  The restricted right-hand side misses
+// that by rounding, and Gauss-Seidel sweeps then drift along the constant, the further the more sweeps run (which
+// degrades the preconditioner).  coarse_consistent subtracts the mean of b over the active cells (D > 0) on such
+// a level and returns b unchanged on any other.  Every thread of the block calls it, one cell each; the sums run
+// in a fixed order (warp shuffles, then the warps in order), so equal inputs give equal bits.
+template <class R>
+__device__ __forceinline__ R coarse_consistent(R bc, bool active, bool excess) {
+    __shared__ R s_sum[32];
+    __shared__ int s_cnt[32];
+    if (__syncthreads_or(excess ? 1 : 0)) return bc;
+    R s = active ? bc : R(0);
+    int m = active ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, o);
+        m += __shfl_down_sync(0xffffffffu, m, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_sum[threadIdx.x >> 5] = s;
+        s_cnt[threadIdx.x >> 5] = m;
+    }
+    __syncthreads();
+    R tot = 0;
+    int cnt = 0;
+    for (int w = 0; w < (int)((blockDim.x + 31) >> 5); w++) {
+        tot += s_sum[w];
+        cnt += s_cnt[w];
+    }
+    return active && cnt > 0 ? bc - tot / R(cnt) : bc;
+}
 
 template <class T, class C>
 __global__ void __launch_bounds__(kCoarseThreads) k_coarse_smem(Dims d, Coef<C> cf, T *__restrict__ x,
@@ -777,6 +809,7 @@ __global__ void __launch_bounds__(kCoarseThreads) k_coarse_smem(Dims d, Coef<C> 
         bc = (R)b[c];
         xs[c] = T(0);
     }
+    bc = coarse_consistent<R>(bc, c < d.n && inv > R(0), c < d.n && ldv(cf.dex, c) != R(0));
     __syncthreads();
     const int nh = 1 + 2 * pairs;
     for (int h = 0; h < nh; h++) {

@@ -19,7 +19,7 @@ struct SolverParams {
     int precision = 0;  // 0 FP64 MGPCG, 1 mixed (FP32/FP16 V-cycle + FP32 FCG inside FP64 refinement)
     double tol = 1e-8;
     int max_iters = 200;
-    int pre = 2, post = 2, coarse_sweeps = 24;
+    int pre = 2, post = 2, coarse_sweeps = 48;
     int coarse_pre = 2, coarse_post = 2;  // levels 2 and coarser
     int max_levels = 0, coarse_dim = 8;
     bool use_graph = true;

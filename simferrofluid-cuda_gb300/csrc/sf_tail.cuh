@@ -361,8 +361,9 @@ __device__ void tail_prolong(cg::cluster_group &cl, const TailLv &f, const TailL
     cl.sync();
 }
 
-// The coarsest level solved on CTA 0 as k_coarse_smem does: x = 0, then the palindromic sequence red, (black,
-// red) x pairs, each cell's couplings (FP16, global memory) pre-multiplied by the level's unscale.  x and b are the
+// The coarsest level solved on CTA 0 as k_coarse_smem does: b made consistent on a pure-Neumann level
+// (coarse_consistent), x = 0, then the palindromic sequence red, (black, red) x pairs, each cell's couplings (FP16,
+// global memory) pre-multiplied by the level's unscale.  x and b are the
 // level's arrays in CTA 0, in natural order.
 __device__ void tail_coarse(cg::cluster_group &cl, const TailLv &v, int rank, int pairs) {
     const Dims &d = v.d;
@@ -398,6 +399,7 @@ __device__ void tail_coarse(cg::cluster_group &cl, const TailLv &v, int rank, in
             bc = v.a.b[c];
             xs[c] = 0.f;
         }
+        bc = coarse_consistent<float>(bc, c < d.n && inv > 0.f, c < d.n && __half2float(cf.dex[c]) != 0.f);
         __syncthreads();
         const int nh = 1 + 2 * pairs;
         for (int h = 0; h < nh; h++) {
