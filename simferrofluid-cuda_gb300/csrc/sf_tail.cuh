@@ -488,10 +488,12 @@ static void tail_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *at, cudaSt
     cfg.numAttrs = 1;
 }
 
-// whether one cluster of NC CTAs with smem bytes of dynamic shared memory each runs on this device
+// whether one cluster of NC CTAs with smem bytes of dynamic shared memory each runs on this device.  The kernel's
+// shared-memory ceiling is a property of the function, shared by every solver in the process: it is set to the
+// largest layout any tail plans (kTailSmem), never to one solver's need.
 template <int NC>
 static bool tail_launchable(int smem) {
-    if (cudaFuncSetAttribute(k_tail<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
+    if (cudaFuncSetAttribute(k_tail<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmem) != cudaSuccess ||
         (NC > 8 && cudaFuncSetAttribute(k_tail<NC>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
         cudaGetLastError();
         return false;
