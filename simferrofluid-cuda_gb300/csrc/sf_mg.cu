@@ -2106,11 +2106,6 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
     int total_inner = 0, outer = 0;
     const int max_outer = 30;
     bool x_zero = x_is_zero;
-    // Refinement steps after the first keep the inner solver's search direction (p, q = A32 p) and its scalars
-    // and only replace its residual by the FP64 one (a reliable update): the flexible beta -(z, q) / (p, q)
-    // keeps the next direction A-conjugate to the last, so the steps continue one Krylov sequence instead of
-    // restarting it.  fresh: the next inner solve starts from p = 0.
-    bool fresh = true;
     while (true) {
         // outer FP64 residual, cast to the FP32 inner right-hand side
         if (x_zero) {
@@ -2146,7 +2141,6 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
                 res.fallback = true;
                 cudaMemsetAsync(x_, 0, 8 * n, st_);
                 x_zero = true;
-                fresh = true;
                 bb = -1;
                 continue;
             }
@@ -2159,13 +2153,12 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
         if (tau > 0.5) tau = 0.5;
         const double in_tol2 = tau * tau * rr;
         cudaMemsetAsync(d32_, 0, 4 * n, st_);
-        if (fresh) {
-            cudaMemsetAsync(p32_, 0, 4 * n, st_);
-            cudaMemsetAsync(q32_, 0, 4 * n, st_);
+        cudaMemsetAsync(p32_, 0, 4 * n, st_);
+        cudaMemsetAsync(q32_, 0, 4 * n, st_);
+        {
             double init[4] = {1.0, 0.0, 0.0, 0.0};
             cudaMemcpyAsync(sc_ + S_RHO, init, 8, cudaMemcpyHostToDevice, st_);
             cudaMemcpyAsync(sc_ + S_ALPHA, init + 1, 8 * 3, cudaMemcpyHostToDevice, st_);
-            fresh = false;
         }
         int it = 0;
         double rin = rr, rprev = rr;
