@@ -46,6 +46,27 @@ def test_abi_version_and_defaults():
     assert m.tol == 1e-6 and m.precision == sf.SF_PREC_MIXED
     assert lib.sf_status_string(0) == b"ok"
     assert lib.sf_status_string(1) == b"not converged"
+    # mixed-form defaults: colour-split finest level, 48 coarsest pairs, the fused coarse tail, coarse sweeps as
+    # pre / post
+    assert (m.smoother, m.coarse_sweeps, m.coarse_tail, m.coarse_pre, m.coarse_post) == (3, 48, 0, 0, 0)
+    assert m.inner_tol == 1e-4 and m.coarse_dim == 8 and m.pre_smooth == 2 and m.post_smooth == 2
+
+
+def test_solve_opts_field_offsets_match_header():
+    """Every field of the ctypes sf_solve_opts sits at the C offset (compiled offsetof probe)."""
+    sf = pkg()
+    O = sf._abi.sf_solve_opts
+    names = [f for f, _ in O._fields_]
+    body = "".join(f'printf("%zu\\n", offsetof(sf_solve_opts, {f}));' for f in names)
+    src = '#include "sfgpu.h"\n#include <stdio.h>\n#include <stddef.h>\nint main(){' + body + 'return 0;}\n'
+    tmp = os.path.join(ROOT, "oracle", "_build")
+    os.makedirs(tmp, exist_ok=True)
+    c = os.path.join(tmp, "offsets.c")
+    exe = os.path.join(tmp, "offsets")
+    open(c, "w").write(src)
+    subprocess.check_call(["gcc", "-I" + os.path.join(ROOT, "include"), c, "-o", exe])
+    offs = [int(v) for v in subprocess.check_output([exe]).split()]
+    assert offs == [getattr(O, f).offset for f in names]
 
 
 def test_structs_match_header_sizes():
