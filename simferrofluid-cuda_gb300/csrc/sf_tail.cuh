@@ -7,10 +7,12 @@
 // vectors x and b, and the operator per cell in FP32 (the three lower-face couplings, D and 1 / D, formed once
 // per solve by k_tail_op).  Next to its planes it keeps halo copies of the x-planes on either side (and the
 // x-couplings of the plane above); a CTA that updates a cell of its first or last plane also stores the value
-// into the neighbouring CTA's halo (distributed shared memory).  Every step then reads only the CTA's own shared
-// memory, and ends with a cluster barrier (the hardware barrier.cluster: no spin loop), whose release / acquire
-// order makes those stores visible.  The coarsest level (at most kCoarseMax cells) is held by CTA 0 and solved
-// there.  As separate kernels the same steps are about twenty latency-bound launches per V-cycle.
+// into the neighbouring CTA's halo (distributed shared memory).  The sweeps then read only the CTA's own shared
+// memory; a restriction or prolongation reads a plane held by another CTA where the two levels' plane ranges do
+// not line up, and the coarsest level (at most kCoarseMax cells) is held by CTA 0 and solved there.  Every step
+// ends with a cluster barrier (the hardware barrier.cluster: no spin loop), whose release / acquire order makes
+// the stores into other CTAs visible.  As separate kernels the same steps are about twenty latency-bound launches
+// per V-cycle.
 //
 // Each cell's arithmetic is that of k_rbgs / k_rbgs4, k_resid_restrict, k_prolong and k_coarse_smem, in the same
 // order, so the fused tail returns the same values.  Rows marked inactive there are skipped; here they are
