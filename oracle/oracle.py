@@ -3,8 +3,8 @@
 TEST INFRASTRUCTURE ONLY: the oracle is the checker for the CUDA library.  Tests, the smoke check and the
 CPU-baseline leg of the benchmark import this module; the product never does.
 
-Parity unpinned: the reference has no golden vectors and cannot be built here (see the header of
-``sf_oracle.c``).  Arrays use the reference's layout (core/Grid.h:28): cell arrays are C-contiguous
+Parity pinned: every function here reproduces the reference's own compiled code bit for bit
+(``oracle/_ref``, ``tests/test_ref_pin.py``; see the header of ``sf_oracle.c``).  Arrays use the reference's layout (core/Grid.h:28): cell arrays are C-contiguous
 ``(nx, ny, nz)`` float64, face arrays of axis a are ``(nx+(a==0), ny+(a==1), nz+(a==2))``.
 """
 from __future__ import annotations

@@ -5,11 +5,15 @@
  * TEST INFRASTRUCTURE ONLY.  This file is the oracle: tests, the smoke check and the CPU-baseline leg of the
  * benchmark call it to check (or time beside) the CUDA library.  Nothing in the product links it.
  *
- * Parity status: parity unpinned.  The reference ships no tests, no golden vectors and no known-answer data,
- * and it cannot be compiled here (Eigen, amgcl, TBB, fmt/spdlog, yaml-cpp and cxxopts are absent), so this
- * restatement is pinned only by the known-answer tests in tests/ (hydrostatic pressure, chi=0, slab field),
- * by a second, independent pure-Python restatement on small grids, and by the committed fixtures that
- * script generates.
+ * Parity status: pinned to the reference's own code.  The reference ships no tests or golden vectors, so its
+ * hot-path sources (core/Pressure.cpp, MagneticField.cpp, Collider.cpp, FastMarching.cpp, Extrapolation.cpp,
+ * Reinitialization.cpp, CSG.cpp, Advection.h, TriLerp.h, TriCuInterp.h) are compiled unmodified into
+ * oracle/_ref (oracle/ref.mk, with stand-in headers for Eigen, TBB, fmt/spdlog, yaml-cpp and the amgcl solver
+ * call), and tests/test_ref_pin.py requires every function here to reproduce their outputs bit for bit: on the
+ * committed fixtures tests/golden/ref_*.npz (written from oracle/_ref by tests/golden/make_ref_golden.py) and,
+ * where the sources are present, on further seeded inputs against the live reference code.  Not compiled:
+ * amgcl's solver (absent; the oracle solves the same systems tightly instead) and the jump producer of
+ * core/Simulation.cpp:216-235 (or_pressure_jump; it needs the whole Simulation/Contour).
  *
  * Floating point: compiled with -ffp-contract=off so that every a*b+c rounds twice, as in the reference's
  * x86 build; the assembly loops evaluate each expression in the reference's order so that the CSR matrix

@@ -103,23 +103,6 @@ def test_bad_arguments_rejected_without_gpu():
     assert lib.sf_collider_box_fractions(C.byref(g), 0, nulls, None) == 2
 
 
-@pytest.mark.parametrize("shape,bw", [((12, 9, 10), 0), ((16, 12, 16), 2), ((7, 5, 6), 1)])
-def test_collider_matches_oracle(oracle, shape, bw):
-    """Host collider (Collider ctor + FastMarching + CalcFaceFraction) is bit-identical to the oracle."""
-    sf = pkg()
-    g = sf.StaggeredGrid.from_origin(0.12 / 60, shape, origin=(-0.01, 0.02, 0.0), boundary_width=bw)
-    fr = scenes().box_fractions(g, bw)
-    og = oracle.Grid(*shape, g.spacing, tuple(g.origin))
-    fo = oracle.box_collider_fractions(og, bw)
-    for a in range(3):
-        assert np.array_equal(fr[a], fo[a])
-    # boundary faces of the grid are solid
-    for a in range(3):
-        sl = [slice(None)] * 3
-        sl[a] = 0
-        assert np.all(fr[a][tuple(sl)] == 1.0)
-
-
 def test_package_has_no_cpu_fallback(monkeypatch):
     """The package raises when the library is missing instead of computing on the CPU."""
     sf = pkg()
