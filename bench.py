@@ -8,8 +8,10 @@ faces).  ``value`` counts 2 solves per step, inputs resident in HBM, timed with 
 stream.  ``e2e`` runs the same step through the host-pointer C ABI with pinned host buffers (H2D of every
 input, D2H of velocity, pressure, potential and H inside the timed region).
 
---impl reference times the CPU restatement of the reference's path (the oracle: the reference cannot be
-built here) on the host cores.  With WORLD_SIZE > 1 every rank runs an independent replica (the path does not
+``accuracy`` reports, outside the timed regions, each arm's errors against the oracle's FP64 answer on the same
+inputs.  --impl reference times the CPU restatement of the reference's path (the oracle, pinned bit for bit to
+the reference's own assembly code; amgcl itself is absent, so its SA-AMG solver is restated) on the host
+cores, without loading the CUDA library.  With WORLD_SIZE > 1 every rank runs an independent replica (the path does not
 shard; replicas only).
 """
 from __future__ import annotations
@@ -45,6 +47,7 @@ def parse(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64-arm", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the errors against the oracle's FP64 answer")
     ap.add_argument("--inner-tol", type=float, default=None, help="mixed form: inner relative reduction floor")
     ap.add_argument("--coarse-dim", type=int, default=None)
     ap.add_argument("--pre", type=int, default=None)
@@ -369,16 +372,78 @@ def run_ours(args, ws, rank, local):
     }
     ctx_bytes = ctx.device_bytes()
     out["device_bytes"] = ctx_bytes
+    if rank == 0 and not args.no_accuracy:
+        # errors of one step of each arm against the oracle's FP64 answer (outside every timed region)
+        res = {}
+        for precision in [args.precision] + (["fp64"] if fp64 else []):
+            step(precision)
+            torch.cuda.synchronize(dev)
+            res[precision] = ([v.cpu().numpy() for v in vel], p_out.cpu().numpy(), psi.cpu().numpy())
+        # the headline form at the reference's own tolerances: amgcl's default 1e-8 for the pressure
+        # (core/Pressure.cpp:125-135) and 1e-6 for the potential (core/MagneticField.cpp:93)
+        for a in range(3):
+            vel[a].copy_(vel0[a])
+        o = opts("pressure", args.precision)
+        o.tol = 1e-8
+        P.project(vel, phi, frac, opts=o, device=True, p_out=p_out)
+        o = opts("magnetic", args.precision)
+        o.tol = 1e-6
+        M.solve(phi, hext, opts=o, device=True, psi_out=psi, H_out=H)
+        torch.cuda.synchronize(dev)
+        res[args.precision + " at tol 1e-8 / 1e-6"] = ([v.cpu().numpy() for v in vel], p_out.cpu().numpy(),
+                                                        psi.cpu().numpy())
+        out["accuracy"] = accuracy(sc, res)
+    return out
+
+
+def accuracy(sc, results, tol=1e-10):
+    """Per solve: relative L2 and max|delta| of p (liquid cells) and psi, and the post-projection max|div u|
+    (weighted divergence over liquid cells), against the oracle's FP64 answer -- the reference's assembly
+    (pinned bit for bit to the reference's own code) solved with the restated SA-AMG to ``tol``."""
+    from oracle import oracle as O
+    scenes = importlib.import_module(PKG + ".scenes")
+    O.build()
+    og = O.Grid(*sc.grid.shape, sc.grid.spacing, tuple(sc.grid.origin))
+    t = time.perf_counter()
+    u_or, p_or, ip = O.pressure_project(og, sc.phi, sc.frac, sc.vel, tol=tol, maxit=100, solver="amg")
+    psi_or, _, im = O.magnetic_solve(og, sc.phi, sc.chi, sc.band_width, sc.hext, tol=tol, maxit=100, solver="amg")
+    liq = sc.phi <= 0
+    full = liq & scenes.full_weight_cells(sc.grid, sc.frac)
+
+    def div_max(v):
+        d = np.abs(scenes.divergence(sc.grid, v, sc.frac))
+        return float(d[full].max()), float(d[liq].max())
+
+    dv = div_max(u_or)
+    out = {"oracle": {"tol": tol, "relres_pressure": ip["relres"], "relres_potential": im["relres"],
+                      "max_div_u": dv[0], "max_div_u_partial_faces": dv[1],
+                      "seconds": round(time.perf_counter() - t, 1)},
+           "note": "max_div_u over liquid cells whose faces are fully open or closed (the projection makes it "
+                   "vanish there up to the residual); max_div_u_partial_faces over all liquid cells, where partly "
+                   "open wall faces leave a divergence in the reference's discretisation as well"}
+    for prec, (vel, p, psi) in results.items():
+        dp = np.abs(p[liq] - p_or[liq])
+        dpsi = np.abs(psi - psi_or)
+        dv = div_max(vel)
+        out[prec] = {
+            "pressure": {"rel_l2": float(np.linalg.norm(p[liq] - p_or[liq]) / np.linalg.norm(p_or[liq])),
+                         "max_dp": float(dp.max()), "max_dp_rel": float(dp.max() / np.abs(p_or[liq]).max()),
+                         "max_div_u": dv[0], "max_div_u_partial_faces": dv[1]},
+            "potential": {"rel_l2": float(np.linalg.norm(psi - psi_or) / np.linalg.norm(psi_or)),
+                          "max_dpsi": float(dpsi.max()), "max_dpsi_rel": float(dpsi.max() / np.abs(psi_or).max())}}
     return out
 
 
 # ------------------------------------------------------------------------------------------------ CPU arm
 def _cpu_scene(n):
+    """The bench scene for the CPU arm, built without the CUDA library: the scene's level set, velocity and
+    field (numpy) and the oracle's collider fractions (bit-identical to the reference's Collider)."""
     from oracle import oracle as O
     O.build()
     scenes = importlib.import_module(PKG + ".scenes")
-    sc = scenes.pool_sphere(n, seed=1234)
+    sc = scenes.pool_sphere(n, seed=1234, with_fractions=False)
     og = O.Grid(*sc.grid.shape, sc.grid.spacing, tuple(sc.grid.origin))
+    sc.frac = O.box_collider_fractions(og, 0)
     return O, sc, og
 
 

@@ -148,3 +148,18 @@ def divergence(g: StaggeredGrid, vel, frac=None):
         sl_lo[a] = slice(0, -1)
         d += f[tuple(sl_hi)] - f[tuple(sl_lo)]
     return d
+
+
+def full_weight_cells(g: StaggeredGrid, frac):
+    """Cells whose six face weights w = 1 - fraction are all 0 or 1.  On such a liquid cell the projected
+    velocity's weighted divergence is minus the pressure solve's residual; where a face is partly open the
+    projection scales the update by w and the divergence weighs it by w again, so it does not vanish there
+    (in the reference as well)."""
+    whole = np.ones(g.shape, bool)
+    for a in range(3):
+        f = frac[a]
+        ok = (f == 0) | (f == 1)
+        lo, hi = [slice(None)] * 3, [slice(None)] * 3
+        lo[a], hi[a] = slice(0, -1), slice(1, None)
+        whole &= ok[tuple(lo)] & ok[tuple(hi)]
+    return whole

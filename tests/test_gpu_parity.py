@@ -40,15 +40,19 @@ def test_pressure_pool_vs_oracle(sfpkg, oracle, gpu_ctx, precision, n, seed):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_pressure_sphere_vs_oracle(sfpkg, oracle, gpu_ctx, precision):
+    """Curved interface (pool + sphere, ghost-fluid terms on a sphere) at the reference's pressure tolerance,
+    amgcl's default 1e-8 (core/Pressure.cpp:125-135): p within 1e-5 relative L2 of the oracle."""
     sc = scenes().pool_sphere(40, seed=5)
     og = oracle_grid(oracle, sc.grid)
     u_or, p_or, info = oracle.pressure_project(og, sc.phi, sc.frac, sc.vel, tol=1e-13)
     vel = _copy(sc.vel)
     P = sfpkg.Pressure(sc.grid, gpu_ctx)
-    st = P.project(vel, sc.phi, sc.frac, opts=sfpkg.options("pressure", precision=precision, tol=1e-6))
+    st = P.project(vel, sc.phi, sc.frac, opts=sfpkg.options("pressure", precision=precision, tol=1e-8))
     liquid = sc.phi <= 0
-    assert st["rel_residual"] <= 1e-6 * 1.01
-    assert rel_l2(P.pressure[liquid], p_or[liquid]) <= 1e-4
+    assert st["rel_residual"] <= 1e-8 * 1.01
+    assert rel_l2(P.pressure[liquid], p_or[liquid]) <= P_TOL
+    for a in range(3):
+        assert np.abs(vel[a] - u_or[a]).max() <= 1e-5 * np.abs(sc.vel[a]).max()
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
