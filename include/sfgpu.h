@@ -125,8 +125,9 @@ SF_EXPORT long long sf_device_bytes(void *ctx);
  * (:38-78), SolveLinearSystem (:125-135, amgcl SA+SPAI0 BiCGStab there, MGPCG here) and ApplyProjection
  * (:137-166).
  *   vel[3]      in/out MAC velocity (face arrays)
- *   phi         level set on cells; liquid where phi <= 0
- *   frac[3]     collider solid fraction per face (Collider::GetFraction, 1 = solid)
+ *   phi         level set on cells; liquid where phi <= 0 (NULL: the level set of sf_levelset_upload)
+ *   frac[3]     collider solid fraction per face (Collider::GetFraction, 1 = solid); frac == NULL: the collider of
+ *               sf_collider_upload
  *   solid_vel[3] collider velocity per face (Collider::Velocity), or NULL = 0
  *   jump[3]     per-face value of the pressure-jump callback J(axis, face, theta) = p_liquid - p_air
  *               (core/Pressure.h:20-22), read on liquid-air faces only, or NULL = no callback.  The shipped
@@ -161,7 +162,7 @@ SF_EXPORT sf_status sf_pressure_reproject_dev(void *ctx, const sf_grid *g, doubl
  * phi (BuildMatrix :51-60, Heaviside core/MagneticField.h:44-54), the full-grid variable-coefficient
  * Laplacian with homogeneous Neumann walls and psi[0] = 0 (:62-90), the right-hand side (AssembleRHS
  * :97-118), the solve (amgcl SA+SPAI0 CG there, MGPCG here) and AssignTotalField (:125-143).
- *   phi          level set on the simulation's cell grid
+ *   phi          level set on the simulation's cell grid (NULL: the level set of sf_levelset_upload)
  *   chi          susceptibility (SetSusceptibility), band_width the Heaviside half-width (SetBandWidth)
  *   hext[3]      applied field on faces
  *   psi_out      optional (nx*ny*nz) potential, psi[0] = 0
@@ -274,6 +275,23 @@ SF_EXPORT sf_status sf_reinitialize_dev(void *ctx, const sf_grid *g, double *phi
 
 /* Forget the magnetic warm start (MagneticField ctor zeroes m_Sol, core/MagneticField.cpp:26). */
 SF_EXPORT sf_status sf_magnetic_reset(void *ctx);
+
+/* ----- resident inputs --------------------------------------------------------------------------------------
+ * The reference's simulation keeps its collider and level set in memory across calls: the collider's face
+ * fractions and velocity are computed once per scene (Collider::Finish, core/Collider.cpp:21-45; Velocity is a
+ * public member, core/Collider.h:27-28) and both solves of a substep read the same level set m_LevelSet
+ * (core/Simulation.cpp:204-226).  These calls keep device copies of them on the context, so that the host entry
+ * points need not copy them again on every call:
+ *   sf_collider_upload   fractions (and the collider velocity, or NULL = 0) of grid g; a pressure call with
+ *                        frac == NULL reads them, and with frac == NULL and solid_vel == NULL also the uploaded
+ *                        velocity;
+ *   sf_levelset_upload   a cell level set of grid g; a pressure or magnetic call with phi == NULL reads it.
+ * Pointers may be host or device memory.  Each call copies on the context's stream and returns once the copy has
+ * finished; the copy stays until the next upload or sf_destroy.  A call that passes NULL on a grid of other
+ * dimensions, or before any upload, returns SF_NOT_READY. */
+SF_EXPORT sf_status sf_collider_upload(void *ctx, const sf_grid *g, const double *const frac[3],
+                                       const double *const solid_vel[3]);
+SF_EXPORT sf_status sf_levelset_upload(void *ctx, const sf_grid *g, const double *phi);
 
 /* ----- allocation-free residual check ------------------------------------------------------------------------
  * No counterpart in the reference: its solvers allocate freely and report only the residual of their own

@@ -131,6 +131,29 @@ class Context:
     def device_bytes(self):
         return int(self.lib.sf_device_bytes(self.handle))
 
+    def upload_collider(self, grid, fraction, solid_velocity=None):
+        """Keep the collider's face fractions (and velocity) on the device (sf_collider_upload); pressure calls
+        given fraction=None read them.  Arrays: numpy (host) or CUDA tensors."""
+        ptr = lambda a: int(a.data_ptr()) if hasattr(a, "data_ptr") else np.ascontiguousarray(a, np.float64).ctypes.data  # noqa: E731
+        keep = [a if hasattr(a, "data_ptr") else np.ascontiguousarray(a, np.float64) for a in fraction]
+        us = None
+        if solid_velocity is not None:
+            keep += [a if hasattr(a, "data_ptr") else np.ascontiguousarray(a, np.float64) for a in solid_velocity]
+            us = _abi.p3_ref([ptr(a) for a in keep[3:]])
+        s = self.lib.sf_collider_upload(self.handle, C.byref(grid.c_grid()), _abi.p3([ptr(a) for a in keep[:3]]),
+                                        us[0] if us else None)
+        if s != _abi.SF_OK:
+            raise SolveError(s, "sf_collider_upload: " + self.last_error())
+
+    def upload_level_set(self, grid, level_set):
+        """Keep a cell level set on the device for the substep's solves (sf_levelset_upload); calls given
+        level_set=None read it.  Array: numpy (host) or a CUDA tensor."""
+        a = level_set if hasattr(level_set, "data_ptr") else np.ascontiguousarray(level_set, np.float64)
+        p = int(a.data_ptr()) if hasattr(a, "data_ptr") else a.ctypes.data
+        s = self.lib.sf_levelset_upload(self.handle, C.byref(grid.c_grid()), C.c_void_p(p))
+        if s != _abi.SF_OK:
+            raise SolveError(s, "sf_levelset_upload: " + self.last_error())
+
     def set_network(self, net):
         """Attach the U-Net used by precision="learned" solves (None detaches)."""
         s = self.lib.sf_set_network(self.handle, net.handle if net is not None else None)
@@ -296,7 +319,8 @@ class Pressure:
         keep = []
         fs = [g.face_shape(a) for a in range(3)]
         vel = [_ptr(velocity[a], fs[a], f"velocity[{a}]", device, True, keep) for a in range(3)]
-        fr = [_ptr(fraction[a], fs[a], f"fraction[{a}]", device, False, keep) for a in range(3)]
+        fr = None if fraction is None else [_ptr(fraction[a], fs[a], f"fraction[{a}]", device, False, keep)
+                                             for a in range(3)]
         phi = _ptr(level_set, g.shape, "level_set", device, False, keep)
         us = None if solid_velocity is None else [_ptr(solid_velocity[a], fs[a], "solid_velocity", device,
                                                        False, keep) for a in range(3)]
@@ -304,12 +328,15 @@ class Pressure:
                                              for a in range(3)]
         if p_out is None and not device:
             p_out = np.zeros(g.shape)
+        elif p_out is False:  # no pressure output (the reference keeps p private)
+            p_out = None
         pp = _ptr(p_out, g.shape, "p_out", device, True) if p_out is not None else None
         us_ref = _abi.p3_ref(us)
         jp_ref = _abi.p3_ref(jp)
+        fr_ref = _abi.p3_ref(fr)
         st = _abi.sf_solve_stats()
         o = opts if opts is not None else options("pressure")
-        s = fn(self.ctx.handle, C.byref(g.c_grid()), _abi.p3(vel), C.c_void_p(phi), _abi.p3(fr),
+        s = fn(self.ctx.handle, C.byref(g.c_grid()), _abi.p3(vel), C.c_void_p(phi), fr_ref[0] if fr_ref else None,
                us_ref[0] if us_ref else None, jp_ref[0] if jp_ref else None, float(vol_error),
                C.c_void_p(pp) if pp else None, C.byref(o), C.byref(st))
         self.stats = st.as_dict()
@@ -320,7 +347,8 @@ class Pressure:
 
     def project(self, velocity, level_set, fraction, solid_velocity=None, vol_error=0.0, opts=None, device=False,
                 p_out=None, raise_on_nonconv=True):
-        """Pressure::Project: velocity (3 face arrays) is updated in place; returns the solve statistics."""
+        """Pressure::Project: velocity (3 face arrays) is updated in place; returns the solve statistics.
+        level_set / fraction None: the context's uploaded level set / collider (Context.upload_*)."""
         fn = self.ctx.lib.sf_pressure_project_dev if device else self.ctx.lib.sf_pressure_project
         return self._call(fn, velocity, level_set, fraction, solid_velocity, vol_error, opts, device, p_out,
                           raise_on_nonconv)
@@ -354,7 +382,8 @@ class MagneticField:
 
     def solve(self, level_set, external_field, opts=None, device=False, psi_out=None, H_out=None,
               raise_on_nonconv=True):
-        """MagneticField::Solve: returns statistics; ``potential`` and ``total_field`` hold the results."""
+        """MagneticField::Solve: returns statistics; ``potential`` and ``total_field`` hold the results.
+        level_set None: the context's uploaded level set; psi_out False: no potential output."""
         g = self.grid
         keep = []
         fs = [g.face_shape(a) for a in range(3)]
@@ -365,6 +394,8 @@ class MagneticField:
                 psi_out = np.zeros(g.shape)
             if H_out is None:
                 H_out = [np.zeros(fs[a]) for a in range(3)]
+        if psi_out is False:  # no potential output (the reference keeps psi private)
+            psi_out = None
         pp = _ptr(psi_out, g.shape, "psi_out", device, True) if psi_out is not None else None
         hp = None if H_out is None else [_ptr(H_out[a], fs[a], "H_out", device, True) for a in range(3)]
         hp_ref = _abi.p3_ref(hp)
@@ -463,7 +494,8 @@ class Extrapolation:
         g, keep = self.grid, []
         fs = [g.face_shape(a) for a in range(3)]
         vel = [_ptr(velocity[a], fs[a], f"velocity[{a}]", device, True, keep) for a in range(3)]
-        fr = [_ptr(fraction[a], fs[a], f"fraction[{a}]", device, False, keep) for a in range(3)]
+        fr = None if fraction is None else [_ptr(fraction[a], fs[a], f"fraction[{a}]", device, False, keep)
+                                             for a in range(3)]
         phi = _ptr(level_set, g.shape, "level_set", device, False, keep)
         fn = self.ctx.lib.sf_extrapolate_velocity_dev if device else self.ctx.lib.sf_extrapolate_velocity
         s = fn(self.ctx.handle, C.byref(g.c_grid()), _abi.p3(vel), C.c_void_p(phi), _abi.p3(fr), float(clear_val),

@@ -29,6 +29,7 @@ EXPORTED = [
     "sf_create", "sf_destroy", "sf_status_string", "sf_last_error", "sf_abi_version", "sf_default_opts",
     "sf_device_bytes", "sf_pressure_project", "sf_pressure_project_dev", "sf_pressure_reproject",
     "sf_pressure_reproject_dev", "sf_magnetic_solve", "sf_magnetic_solve_dev", "sf_magnetic_reset",
+    "sf_collider_upload", "sf_levelset_upload",
     "sf_collider_box_fractions", "sf_collider_face_fractions",
     "sf_unet_create", "sf_unet_destroy", "sf_unet_num_params", "sf_unet_set_params", "sf_unet_get_params",
     "sf_unet_forward_dev", "sf_unet_backward_dev", "sf_unet_train_step_dev", "sf_set_network",
@@ -100,7 +101,7 @@ def load(path: str | None = None):
     for name in ("sf_pressure_project", "sf_pressure_project_dev", "sf_pressure_reproject",
                  "sf_pressure_reproject_dev"):
         f = getattr(L, name)
-        f.argtypes = [V, G, _P3, V, _P3, V, V, C.c_double, V, O, S]
+        f.argtypes = [V, G, _P3, V, V, V, V, C.c_double, V, O, S]
         f.restype = C.c_int
     for name in ("sf_magnetic_solve", "sf_magnetic_solve_dev"):
         f = getattr(L, name)
@@ -108,6 +109,10 @@ def load(path: str | None = None):
         f.restype = C.c_int
     L.sf_magnetic_reset.argtypes = [V]
     L.sf_magnetic_reset.restype = C.c_int
+    L.sf_collider_upload.argtypes = [V, G, _P3, V]
+    L.sf_collider_upload.restype = C.c_int
+    L.sf_levelset_upload.argtypes = [V, G, V]
+    L.sf_levelset_upload.restype = C.c_int
     for name in ("sf_extrapolate_velocity", "sf_extrapolate_velocity_dev"):
         f = getattr(L, name)
         f.argtypes = [V, G, _P3, V, _P3, C.c_double, C.c_int]

@@ -42,6 +42,10 @@ struct Ctx {
     std::vector<void *> nets;
     DevBuf feat, guess;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // resident inputs: the collider (fractions, optional velocity) and a level set, read by calls that pass NULL
+    DevBuf rfrac[3], rus[3], rphi;
+    bool rcol = false, rcol_us = false, rls = false;
+    Dims rcol_dims{0, 0, 0, 0}, rls_dims{0, 0, 0, 0};
 };
 
 Ctx *C(void *p) { return reinterpret_cast<Ctx *>(p); }
@@ -159,15 +163,26 @@ sf_status learned_guess(Ctx *c, MGSolver &S, const Dims &d, SolveResult &pre) {
     return SF_OK;
 }
 
+bool same_dims(const Dims &a, const Dims &b) { return a.nx == b.nx && a.ny == b.ny && a.nz == b.nz; }
+
+// The resident level set (phi == NULL) or the staged / passed-through one.
+sf_status level_set_in(Ctx *c, const double *phi, const Dims &d, bool dev, const double **out, long long &h2d) {
+    if (phi) return stage_in(c, c->phi, phi, d.n, dev, out, h2d);
+    if (!c->rls || !same_dims(c->rls_dims, d))
+        return fail(c, SF_NOT_READY, "phi is NULL and no level set of this grid was uploaded (sf_levelset_upload)");
+    *out = (const double *)c->rphi.get();
+    return SF_OK;
+}
+
 // ------------------------------------------------------------------------------------------------ pressure
 sf_status pressure_impl(Ctx *c, const sf_grid *g, double *const vel[3], const double *phi, const double *const frac[3],
                         const double *const us[3], const double *const jump[3], double vol_error, double *p_out,
                         const sf_solve_opts *opts, sf_solve_stats *stats, bool dev, bool reproject) {
     auto t0 = std::chrono::steady_clock::now();
     if (!c) return SF_BAD_ARG;
-    if (!grid_ok(g) || !vel || !phi || !frac || !opts_ok(opts)) return fail(c, SF_BAD_ARG, "bad grid, pointer or option");
+    if (!grid_ok(g) || !vel || !opts_ok(opts)) return fail(c, SF_BAD_ARG, "bad grid, pointer or option");
     for (int a = 0; a < 3; a++)
-        if (!vel[a] || !frac[a]) return fail(c, SF_BAD_ARG, "null velocity or fraction array");
+        if (!vel[a] || (frac && !frac[a])) return fail(c, SF_BAD_ARG, "null velocity or fraction array");
     if (us)
         for (int a = 0; a < 3; a++)
             if (!us[a]) return fail(c, SF_BAD_ARG, "solid_vel must hold three arrays or be NULL");
@@ -185,12 +200,22 @@ sf_status pressure_impl(Ctx *c, const sf_grid *g, double *const vel[3], const do
     const double *dphi;
     Faces ffrac{}, fvel{}, fus{}, fjump{};
     sf_status s;
-    if ((s = stage_in(c, c->phi, phi, d.n, dev, &dphi, h2d)) != SF_OK) return s;
+    if (!frac && !(c->rcol && same_dims(c->rcol_dims, d)))
+        return fail(c, SF_NOT_READY, "frac is NULL and no collider of this grid was uploaded (sf_collider_upload)");
+    if ((s = level_set_in(c, phi, d, dev, &dphi, h2d)) != SF_OK) return s;
     for (int a = 0; a < 3; a++) {
         const long long nf = face_count(g, a);
-        if ((s = stage_in(c, c->frac[a], frac[a], nf, dev, &ffrac.p[a], h2d)) != SF_OK) return s;
+        if (frac) {
+            if ((s = stage_in(c, c->frac[a], frac[a], nf, dev, &ffrac.p[a], h2d)) != SF_OK) return s;
+        } else {
+            ffrac.p[a] = (const double *)c->rfrac[a].get();  // the resident collider
+        }
         if ((s = stage_in(c, c->vel[a], vel[a], nf, dev, &fvel.p[a], h2d)) != SF_OK) return s;
-        if ((s = stage_in(c, c->us[a], us ? us[a] : nullptr, nf, dev, &fus.p[a], h2d)) != SF_OK) return s;
+        if (!frac && !us && c->rcol_us) {
+            fus.p[a] = (const double *)c->rus[a].get();
+        } else if ((s = stage_in(c, c->us[a], us ? us[a] : nullptr, nf, dev, &fus.p[a], h2d)) != SF_OK) {
+            return s;
+        }
         if ((s = stage_in(c, c->jump[a], jump ? jump[a] : nullptr, nf, dev, &fjump.p[a], h2d)) != SF_OK) return s;
     }
     if (!c->pres) c->pres = std::make_unique<MGSolver>(c->st);
@@ -247,7 +272,7 @@ sf_status pressure_impl(Ctx *c, const sf_grid *g, double *const vel[3], const do
     c->pres_prec = prm.precision;
     c->pres_dims = d;
     fill_stats(stats, res, -1);
-    if (stats) stats->kernel_launches = S.take_launches() + 1 + 3 + (p_out ? 1 : 0);
+    if (stats) stats->kernel_launches = S.take_launches() + 1 + 1 + (p_out ? 1 : 0);
     if (stats) {
         stats->rel_residual = relres;
         stats->rel_residual_ref = relres;
@@ -269,7 +294,7 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
                         bool dev) {
     auto t0 = std::chrono::steady_clock::now();
     if (!c) return SF_BAD_ARG;
-    if (!grid_ok(g) || !phi || !hext || !opts_ok(opts) || !std::isfinite(chi) || !(bw > 0) || !std::isfinite(bw))
+    if (!grid_ok(g) || !hext || !opts_ok(opts) || !std::isfinite(chi) || !(bw > 0) || !std::isfinite(bw))
         return fail(c, SF_BAD_ARG, "bad grid, pointer, chi, band width or option");
     for (int a = 0; a < 3; a++)
         if (!hext[a]) return fail(c, SF_BAD_ARG, "null applied-field array");
@@ -283,7 +308,7 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
     const double *dphi;
     Faces fh{};
     sf_status s;
-    if ((s = stage_in(c, c->phi, phi, d.n, dev, &dphi, h2d)) != SF_OK) return s;
+    if ((s = level_set_in(c, phi, d, dev, &dphi, h2d)) != SF_OK) return s;
     for (int a = 0; a < 3; a++)
         if ((s = stage_in(c, c->hext[a], hext[a], face_count(g, a), dev, &fh.p[a], h2d)) != SF_OK) return s;
     if (!c->mag) c->mag = std::make_unique<MGSolver>(c->st);
@@ -293,7 +318,8 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
     CK(S.configure(d, prm));
     const bool warm = (!opts || opts->warm_start) && same_grid;
     CK(cudaEventRecord(c->ev[0], c->st));
-    launch_build_magnetic(c->st, d, dphi, chi, bw, fh, g->h, S.fine(), S.b(), prm.precision == 0, S.split_targets());
+    const int build_launches =
+        launch_build_magnetic(c->st, d, dphi, chi, bw, fh, g->h, S.fine(), S.b(), prm.precision == 0, S.split_targets());
     CK(S.build_hierarchy());
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->ev[1], c->st));
@@ -347,7 +373,7 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
     c->mag_has_x = true;
     c->mag_dims = d;
     fill_stats(stats, res, d.n);
-    if (stats) stats->kernel_launches = S.take_launches() + 2 + (H_out ? 3 : 0) + ((psi_out && dev) ? 1 : 0);
+    if (stats) stats->kernel_launches = S.take_launches() + build_launches + (H_out ? 1 : 0) + ((psi_out && dev) ? 1 : 0);
     if (stats) {
         stats->rel_residual = relres;
         stats->rel_residual_ref = relref;
@@ -837,6 +863,46 @@ sf_status sf_magnetic_reset(void *ctx) {
     Ctx *c = C(ctx);
     if (!c) return SF_BAD_ARG;
     c->mag_has_x = false;
+    return SF_OK;
+}
+
+// ----- resident inputs ---------------------------------------------------------------------------------------
+sf_status sf_collider_upload(void *ctx, const sf_grid *g, const double *const frac[3], const double *const solid_vel[3]) {
+    Ctx *c = C(ctx);
+    if (!c) return SF_BAD_ARG;
+    if (!grid_ok(g) || !frac) return fail(c, SF_BAD_ARG, "bad grid or fraction pointer");
+    for (int a = 0; a < 3; a++)
+        if (!frac[a] || (solid_vel && !solid_vel[a])) return fail(c, SF_BAD_ARG, "null fraction or velocity array");
+    CK(cudaSetDevice(c->device));
+    c->rcol = false;
+    for (int a = 0; a < 3; a++) {
+        const size_t bytes = 8 * (size_t)face_count(g, a);
+        CK(c->rfrac[a].ensure(bytes));
+        CK(cudaMemcpyAsync(c->rfrac[a].get(), frac[a], bytes, cudaMemcpyDefault, c->st));
+        if (solid_vel) {
+            CK(c->rus[a].ensure(bytes));
+            CK(cudaMemcpyAsync(c->rus[a].get(), solid_vel[a], bytes, cudaMemcpyDefault, c->st));
+        }
+    }
+    CK(cudaStreamSynchronize(c->st));
+    c->rcol = true;
+    c->rcol_us = solid_vel != nullptr;
+    c->rcol_dims = make_dims(g->nx, g->ny, g->nz);
+    return SF_OK;
+}
+
+sf_status sf_levelset_upload(void *ctx, const sf_grid *g, const double *phi) {
+    Ctx *c = C(ctx);
+    if (!c) return SF_BAD_ARG;
+    if (!grid_ok(g) || !phi) return fail(c, SF_BAD_ARG, "bad grid or level-set pointer");
+    CK(cudaSetDevice(c->device));
+    c->rls = false;
+    const Dims d = make_dims(g->nx, g->ny, g->nz);
+    CK(c->rphi.ensure(8 * (size_t)d.n));
+    CK(cudaMemcpyAsync(c->rphi.get(), phi, 8 * (size_t)d.n, cudaMemcpyDefault, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    c->rls = true;
+    c->rls_dims = d;
     return SF_OK;
 }
 

@@ -7,6 +7,7 @@
 //   (A v)_c = D_c v_c - sum over the 6 faces of (coupling * v_neighbour),  D_c = sum of the 6 couplings + dex_c
 //   dex_c  = diagonal excess (ghost-fluid Dirichlet terms, the isolated-cell 1); D_c == 0 marks an inactive cell.
 #pragma once
+#include <type_traits>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -165,13 +166,38 @@ __device__ __forceinline__ void block_sum(double (&acc)[K], int tid) {
 
 constexpr int kRedGroup = 256;  // blocks per first-level group
 
+// Warp sum of FP32 values as an unevaluated (hi, lo) pair of floats: each shuffle stage adds the partner's pair
+// with the exact two-sum (Knuth), keeps the rounding error in lo and renormalises, so the sum carries about 48
+// bits.  It runs on the FP32 pipe, which on this GPU issues 64 times as many lanes per clock as the FP64 pipe;
+// lane 0's pair is converted to one double.  Same fixed shuffle order as warp_sum, hence deterministic.
+template <int K>
+__device__ __forceinline__ void warp_sum_df(const float (&v)[K], double (&out)[K]) {
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        float hi = v[q], lo = 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float bh = __shfl_down_sync(0xffffffffu, hi, o);
+            const float bl = __shfl_down_sync(0xffffffffu, lo, o);
+            const float sum = __fadd_rn(hi, bh);
+            const float bb = __fsub_rn(sum, hi);
+            const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bb)), __fsub_rn(bh, bb));
+            const float l = __fadd_rn(__fadd_rn(lo, bl), err);
+            hi = __fadd_rn(sum, l);
+            lo = __fsub_rn(l, __fsub_rn(hi, sum));
+        }
+        out[q] = (double)hi + (double)lo;
+    }
+}
+
 // Deterministic grid-wide sum.  Blocks write partials; the last block of each group of kRedGroup blocks sums
 // its group in block order; the last group to finish sums the group partials in group order.  Returns true in
 // exactly one thread (linear thread 0 of that block) with `tot` holding the totals.  Blocks must have
 // kRedThreads threads (any shape).  part: K * (nblk + ngroups) doubles; ticket: 1 + ngroups counters, zero on
-// entry and re-armed on exit.
-template <int K>
-__device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, unsigned *ticket, double (&tot)[K]) {
+// entry and re-armed on exit.  Per-thread values are doubles (warp stage in FP64) or floats (warp stage as a
+// float pair, warp_sum_df); the block and grid stages are FP64.
+template <int K, class V>
+__device__ __forceinline__ bool grid_reduce(V (&v)[K], double *part, unsigned *ticket, double (&tot)[K]) {
     __shared__ double sh[K][kRedThreads / 32];
     __shared__ bool last;
     const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
@@ -181,11 +207,18 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, unsign
     const int grp = bid / kRedGroup;
     const int gsize = min(kRedGroup, nblk - grp * kRedGroup);
     double *gpart = part + (long long)K * nblk;
-    warp_sum<K>(v);
+    double w[K];
+    if constexpr (std::is_same<V, float>::value) {
+        warp_sum_df<K>(v, w);
+    } else {
+        warp_sum<K>(v);
+#pragma unroll
+        for (int q = 0; q < K; q++) w[q] = v[q];
+    }
     const int lane = tid & 31, wid = tid >> 5;
     if (lane == 0)
 #pragma unroll
-        for (int q = 0; q < K; q++) sh[q][wid] = v[q];
+        for (int q = 0; q < K; q++) sh[q][wid] = w[q];
     __syncthreads();
     if (tid == 0) {
 #pragma unroll

@@ -962,7 +962,8 @@ __global__ void k_to16(long long n, Coef<double> f, Coef<__half> o) {
 
 // q = A p ; slot PQ = (p, q) ; alpha = rho / pq (0 and breakdown flag if pq <= 0)
 // Per-thread partial sums are accumulated in the vector type (FP32 for FP32 vectors: FP64 arithmetic and
-// conversions are scarce on GB300) and promoted to FP64 for the cross-thread reduction.
+// conversions are scarce on GB300); FP32 partials are summed across a warp as a float pair (warp_sum_df) and in
+// FP64 from there on.
 template <class T, class C>
 __global__ void __launch_bounds__(256) k_apply_dot(Dims d, int xpb, Coef<C> cf, const T *__restrict__ p,
                                                    T *__restrict__ q, double *sc, double *part, unsigned *ticket) {
@@ -977,7 +978,7 @@ __global__ void __launch_bounds__(256) k_apply_dot(Dims d, int xpb, Coef<C> cf, 
     q[c] = qc;
     acc += pc * qc;
     TILE_LOOP_END
-    double v[1] = {(double)acc};
+    T v[1] = {acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) {
         sc[S_PQ] = tot[0];
@@ -1059,7 +1060,7 @@ __global__ void __launch_bounds__(256) k_apply_dot4(Dims d, int xpb, Coef<float>
             *reinterpret_cast<float4 *>(q + c0) = make_float4(out[0], out[1], out[2], out[3]);
         }
     }
-    double v[1] = {(double)acc};
+    float v[1] = {acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) {
         sc[S_PQ] = tot[0];
@@ -1105,7 +1106,7 @@ __global__ void __launch_bounds__(256) k_dot_rz(long long n, const T *__restrict
         a0 += r[c] * zc;
         a1 += zc * q[c];
     }
-    double v[2] = {(double)a0, (double)a1};
+    T v[2] = {a0, a1};
     double tot[2];
     if (grid_reduce<2>(v, part, ticket, tot)) {
         const double rho = sc[S_RHO];
@@ -1142,7 +1143,7 @@ __global__ void __launch_bounds__(256) k_update(long long n, T *__restrict__ x, 
         r[c] = rc;
         acc += rc * rc;
     }
-    double v[1] = {(double)acc};
+    T v[1] = {acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) sc[S_RR] = tot[0];
 }
@@ -1200,11 +1201,10 @@ __global__ void __launch_bounds__(256) k_cast_rhs(long long n, const double *__r
 // (y, b) with y FP32 and b FP64 -> slot
 __global__ void __launch_bounds__(256) k_dot_fd(long long n, const float *__restrict__ y, const double *__restrict__ b,
                                                 int slot, double *sc, double *part, unsigned *ticket) {
-    double v[1] = {0};
     float acc = 0.f;
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) acc += y[c] * (float)b[c];
-    v[0] = acc;
+    float v[1] = {acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) sc[slot] = tot[0];
 }
@@ -1381,31 +1381,33 @@ static void fused(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const 
 // Half sweep of the split level 0 (smoother 3); same algorithmic bytes as the natural half sweep.
 template <class C>
 static void rb_split(cudaStream_t st, Tracker &tk, bool fine, bool zero, const Dims &d, const Coef<C> &cf, float *x,
-                     const float *b, int color, const int *list, const int *count, const float *crow) {
+                     const float *b, int color, const int *list, const int *count, const float4 *rc,
+                     const float *dinv) {
     const long long items = split_items((long long)d.nx * d.ny, d.nz >> 3);
     tk.before(st, fine);
     if (zero)
         launch_pdl(k_rbgs4s<C, true>, row_grid((const void *)k_rbgs4s<C, true>, items), blk2(), st, d, cf, x, b,
-                   color, list, count, crow);
+                   color, list, count, rc, dinv);
     else
         launch_pdl(k_rbgs4s<C, false>, row_grid((const void *)k_rbgs4s<C, false>, items), blk2(), st, d, cf, x, b,
-                   color, list, count, crow);
+                   color, list, count, rc, dinv);
     tk.after(st, fine, tk.bytes0 >= 0 ? tk.bytes0 : (3.0 * sizeof(float) + 4.0 * sizeof(C)) / 2.0 * d.n);
 }
 
 template <class T, class C>
 static void smooth(cudaStream_t st, Tracker &tk, bool fine, const Dims &d, const Coef<C> &cf, T *x, T *tmp,
                    const T *b, int nu, bool pre, bool split = false, const uint8_t *rows = nullptr,
-                   const int *list = nullptr, const int *count = nullptr, const float *crow = nullptr) {
+                   const int *list = nullptr, const int *count = nullptr, const float4 *rc = nullptr,
+                   const float *dinv = nullptr) {
     if constexpr (std::is_same<T, float>::value && std::is_same<C, __half>::value) {  // split: FP16 copy only
         if (split) {
             for (int s = 0; s < nu; s++) {
                 if (pre) {
-                    rb_split<C>(st, tk, fine, s == 0, d, cf, x, b, 0, list, count, crow);
-                    rb_split<C>(st, tk, fine, false, d, cf, x, b, 1, list, count, crow);
+                    rb_split<C>(st, tk, fine, s == 0, d, cf, x, b, 0, list, count, rc, dinv);
+                    rb_split<C>(st, tk, fine, false, d, cf, x, b, 1, list, count, rc, dinv);
                 } else {
-                    rb_split<C>(st, tk, fine, false, d, cf, x, b, 1, list, count, crow);
-                    rb_split<C>(st, tk, fine, false, d, cf, x, b, 0, list, count, crow);
+                    rb_split<C>(st, tk, fine, false, d, cf, x, b, 1, list, count, rc, dinv);
+                    rb_split<C>(st, tk, fine, false, d, cf, x, b, 0, list, count, rc, dinv);
                 }
             }
             return;
@@ -1490,6 +1492,8 @@ struct RowSets {
     const int *list[3], *count[3];  // levels 0, 1, 2
     const float *crow[2];           // levels 0, 1: the coupling of each uniform row
     const Coef<__half> *c1s;        // split FP16 operator of level 1 when level 1 is split too, else nullptr
+    const float4 *rc[2];            // levels 0, 1: the smoother's row constants (k_smooth_consts_s)
+    const float *dinv[2];           // levels 0, 1: the smoother's 1 / D on general rows
 };
 
 template <class T, class C0, class Cc, class C0S>
@@ -1510,7 +1514,8 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
     // level 1 split as well: its vectors and its FP16 operator copy *rs->c1s are stored colour by colour
     bool split1 = false;
     if constexpr (std::is_same<T, float>::value && std::is_same<Cc, __half>::value) split1 = rs && rs->c1s;
-    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true, split0, R(0), LST(0), CNT(0), cr);
+    smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.pre, true, split0, R(0), LST(0), CNT(0),
+                   rs ? rs->rc[0] : nullptr, rs ? rs->dinv[0] : nullptr);
     // the residual of the smoothed operator
     restrict_res<T, C0S>(st, tk, dims[0], c0s, z, r, dims[1], bs[1], split0, R(0), R(1), LST(1), CNT(1), cr, split1);
     // levels from `bottom` on are solved in one piece: the coarsest solve, or the fused tail (one cluster launch
@@ -1524,7 +1529,7 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
             if (l == 1 && split1) {
                 const Coef<__half> &c1 = *rs->c1s;
                 smooth<T, Cc>(st, tk, false, dims[1], c1, xs[1], nullptr, bs[1], p.pre, true, true, R(1), LST(1),
-                              CNT(1), cr1);
+                              CNT(1), rs->rc[1], rs->dinv[1]);
                 restrict_res<T, Cc>(st, tk, dims[1], c1, xs[1], bs[1], dims[2], bs[2], true, R(1), R(2), LST(2),
                                     CNT(2), cr1);
                 continue;
@@ -1562,7 +1567,7 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
                 const int g = row_grid((const void *)k_prolong_s, split_items((long long)d1.nx * d1.ny, d1.nz >> 3));
                 launch_pdl(k_prolong_s, g, blk2(), st, d1, xs[1], dims[2], xs[2], LST(1), CNT(1));
                 smooth<T, Cc>(st, tk, false, d1, *rs->c1s, xs[1], nullptr, bs[1], p.post, false, true, R(1), LST(1),
-                              CNT(1), cr1);
+                              CNT(1), rs->rc[1], rs->dinv[1]);
                 continue;
             }
         }
@@ -1581,7 +1586,8 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
             else
                 launch_pdl(k_prolong_s, row_grid((const void *)k_prolong_s, items), blk2(), st, d0, z, dims[1], xs[1],
                            LST(0), CNT(0));
-            smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true, R(0), LST(0), CNT(0), cr);
+            smooth<T, C0S>(st, tk, true, dims[0], c0s, z, ts[0], r, p.post, false, true, R(0), LST(0), CNT(0),
+                           rs->rc[0], rs->dinv[0]);
             return;
         }
     }
@@ -1736,6 +1742,8 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
         list_[0] = list_[1] = nullptr;
         count_ = nullptr;
         crow_ = crow1_ = nullptr;
+        rc_[0] = rc_[1] = nullptr;
+        dinv_[0] = dinv_[1] = nullptr;
         list_[2] = nullptr;
         c16s1_ = Coef<__half>{};
         // level 1 split too when it has a coarser level and whole 16-byte rows per colour
@@ -1744,9 +1752,13 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
             for (int l = 0; l < (split1 ? 3 : 2); l++) list_[l] = (int *)chk(A(4 * (size_t)dims[l].nx * dims[l].ny));
             count_ = (int *)chk(A(16));
             crow_ = (float *)chk(A(4 * (size_t)dims[0].nx * dims[0].ny));
+            rc_[0] = (float4 *)chk(A(16 * (size_t)dims[0].nx * dims[0].ny));
+            dinv_[0] = (float *)chk(A(4 * (size_t)dims[0].n));
             list_cnt_ = (int *)chk(A(8 * (((size_t)dims[0].nx * dims[0].ny + kListRows - 1) / kListRows)));
             if (split1) {
                 crow1_ = (float *)chk(A(4 * (size_t)dims[1].nx * dims[1].ny));
+                rc_[1] = (float4 *)chk(A(16 * (size_t)dims[1].nx * dims[1].ny));
+                dinv_[1] = (float *)chk(A(4 * (size_t)dims[1].n));
                 const long long m = dims[1].n;
                 c16s1_.ax = (__half *)chk(A(2 * m));
                 c16s1_.ay = (__half *)chk(A(2 * m));
@@ -1842,7 +1854,9 @@ cudaError_t MGSolver::build_hierarchy() {
             copies_written_ = false;
             k_rows_uniform<float><<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(lev_dims_[0], c32_, rows_[0],
                                                                                           crow_);
-            tk_.launches++;
+            k_smooth_consts_s<__half><<<split_rows_grid(lev_dims_[0]), dim3(32, 8), 0, st_>>>(
+                lev_dims_[0], c16s0_, rows_[0], crow_, rc_[0], dinv_[0]);
+            tk_.launches += 2;
             // rows that hold no active cell are skipped by every level-l kernel; their vector entries must be
             // zero, and stay so
             cudaMemsetAsync(z32_, 0, 4 * (size_t)lev_dims_[0].n, st_);
@@ -1862,7 +1876,9 @@ cudaError_t MGSolver::build_hierarchy() {
             if (split1_) {
                 k_rows_uniform<__half><<<split_rows_grid(lev_dims_[1]), dim3(32, 8), 0, st_>>>(lev_dims_[1], c16s1_,
                                                                                                rows_[1], crow1_);
-                tk_.launches++;
+                k_smooth_consts_s<__half><<<split_rows_grid(lev_dims_[1]), dim3(32, 8), 0, st_>>>(
+                    lev_dims_[1], c16s1_, rows_[1], crow1_, rc_[1], dinv_[1]);
+                tk_.launches += 2;
             }
             for (int l = 0; l < (split1_ ? 3 : 2); l++) {
                 const long long nr = (long long)lev_dims_[l].nx * lev_dims_[l].ny;
@@ -1884,9 +1900,9 @@ cudaError_t MGSolver::build_hierarchy() {
                     gen += v == 1;
                     uni += v == 2;
                 }
-                // algorithmic bytes of a half sweep per grid cell: 10 on a general row (x r/w, b, 3 couplings
-                // and the excess, half of each), 6 on a uniform row (x r/w and b)
-                tk_.bytes0 = (10.0 * gen + 6.0 * uni) * d0.nz;
+                // algorithmic bytes of a half sweep per grid cell: 11 on a general row (x r/w, b, 3 FP16
+                // couplings and the FP32 1 / D, half of each), 6 on a uniform row (x r/w and b)
+                tk_.bytes0 = (11.0 * gen + 6.0 * uni) * d0.nz;
             }
         } else {
             k_to32<<<flat_grid(lev_dims_[0].n), 256, 0, st_>>>(lev_dims_[0].n, c64_[0], c32_);
@@ -1937,7 +1953,7 @@ void MGSolver::enqueue_iter32() {
     if (split0_) {
         // colour-split level 0 with row flags on every level (vectors in split rows, inactive rows skipped)
         const RowSets rs{&rows_, {list_[0], list_[1], list_[2]}, {count_, count_ + 1, count_ + 2}, {crow_, crow1_},
-                         split1_ ? &c16s1_ : nullptr};
+                         split1_ ? &c16s1_ : nullptr, {rc_[0], rc_[1]}, {dinv_[0], dinv_[1]}};
         const int *lst0 = list_[0], *cnt0 = count_;
         vcycle<float, float, __half, __half>(st_, tk_, lev_dims_, c32_, c16s0_, c16_, z32_, ri32_, x32_, b32_, ts,
                                              prm_, true, &rs, tail_lt_, tail_smem_, tail_nc_, tail_op_.data());

@@ -156,31 +156,21 @@ __global__ void __launch_bounds__(256) k_build_pressure(Dims d, const double *__
     if (so.rows) split_store(so, d, i, j, k, lower[0], lower[1], lower[2], dexv, D > 0);
 }
 
-// Pressure::ApplyProjection (core/Pressure.cpp:137-166) for the faces of axis a.  p is the solution on
-// cells; liquid = phi <= 0.  w = 1 - fraction is 0 exactly when the fraction is 1, and 1 exactly when it is
-// zero, where (p1 - p0) * w is p1 - p0: both are tested on the bits, so air faces and open liquid faces take no
-// FP64 operation beyond the update itself.
-template <int a>
-__global__ void __launch_bounds__(256) k_apply_projection(Dims d, const double *__restrict__ phi, Faces frac,
-                                                          Faces jump, const double *__restrict__ p,
-                                                          double *__restrict__ u) {
-    const int fx = d.nx + (a == 0), fy = d.ny + (a == 1), fz = d.nz + (a == 2);
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int i = blockIdx.z;
-    if (k >= fz || j >= fy || i >= fx) return;
-    int c0i[3] = {i, j, k};
-    c0i[a] -= 1;
-    const int dn[3] = {d.nx, d.ny, d.nz};
-    const int fa = a == 0 ? i : (a == 1 ? j : k);
-    if (fa <= 0 || fa >= dn[a]) return;  // closed boundary face
-    const long long f = (long long)k + (long long)fz * ((long long)j + (long long)fy * i);
+// Pressure::ApplyProjection (core/Pressure.cpp:137-166).  One thread per node (i, j, k) of the cell grid updates
+// the lower x, y and z faces of cell (i, j, k), in one launch over (nx + 1) x (ny + 1) x (nz + 1) points, so phi and
+// p of the cell are loaded once for its three faces.  p is the solution on cells; liquid = phi <= 0.
+// w = 1 - fraction is 0 exactly when the fraction is 1, and 1 exactly when it is zero, where (p1 - p0) * w is
+// p1 - p0: both are tested on the bits, so air faces and open liquid faces take no FP64 operation beyond the
+// update itself.
+__device__ __forceinline__ void project_face(const Dims &d, int a, long long f, long long c0, long long c1, int fa,
+                                             int na, const double *__restrict__ phi, const Faces &frac,
+                                             const Faces &jump, const double *__restrict__ p, double *__restrict__ u,
+                                             double phi1, bool l1) {
+    if (fa <= 0 || fa >= na) return;  // closed boundary face
     const double fr = frac.p[a][f];
     if (__double_as_longlong(fr) == kOneBits) return;  // w == 0
-    const long long c1 = cid(d, i, j, k);
-    const long long c0 = cid(d, c0i[0], c0i[1], c0i[2]);
-    const double phi0 = phi[c0], phi1 = phi[c1];
-    const bool l0 = le0(phi0), l1 = le0(phi1);
+    const double phi0 = phi[c0];
+    const bool l0 = le0(phi0);
     if (!l0 && !l1) return;
     double v = u[f];
     if (l0 && l1 && is_zero(fr)) {
@@ -197,6 +187,28 @@ __global__ void __launch_bounds__(256) k_apply_projection(Dims d, const double *
         v -= (l0 ? 1.0 : -1.0) * (pj - pin) * ic * w;
     }
     u[f] = v;
+}
+
+__global__ void __launch_bounds__(256) k_apply_projection3(Dims d, const double *__restrict__ phi, Faces frac,
+                                                           Faces jump, const double *__restrict__ p, Faces u) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k > d.nz || j > d.ny || i > d.nx) return;
+    const bool cell = i < d.nx && j < d.ny && k < d.nz;
+    const long long c1 = cell ? cid(d, i, j, k) : 0;
+    const double phi1 = cell ? phi[c1] : 1.0;  // a face whose upper cell is outside the grid is a boundary face
+    const bool l1 = cell && le0(phi1);
+    const long long sx = (long long)d.ny * d.nz, sy = d.nz;
+    if (j < d.ny && k < d.nz)
+        project_face(d, 0, fid(d, 0, i, j, k), c1 - sx, c1, i, d.nx, phi, frac, jump, p, const_cast<double *>(u.p[0]),
+                     phi1, l1);
+    if (i < d.nx && k < d.nz)
+        project_face(d, 1, fid(d, 1, i, j, k), c1 - sy, c1, j, d.ny, phi, frac, jump, p, const_cast<double *>(u.p[1]),
+                     phi1, l1);
+    if (i < d.nx && j < d.ny)
+        project_face(d, 2, fid(d, 2, i, j, k), c1 - 1, c1, k, d.nz, phi, frac, jump, p, const_cast<double *>(u.p[2]),
+                     phi1, l1);
 }
 
 // p_out on cells: solution in liquid cells (D > 0 in the stored operator), 0 elsewhere.
@@ -344,26 +356,41 @@ __global__ void __launch_bounds__(256) k_magnetic_rows(Dims d, Faces hext, doubl
     b[c] = rhs;
 }
 
-// AssignTotalField (core/MagneticField.cpp:125-143) for the faces of axis a.
-template <int a>
-__global__ void __launch_bounds__(256) k_total_field(Dims d, const double *__restrict__ psi, Faces hext, double invh,
-                                                     double *__restrict__ H) {
-    const int fx = d.nx + (a == 0), fy = d.ny + (a == 1), fz = d.nz + (a == 2);
+// AssignTotalField (core/MagneticField.cpp:125-143): H = (psi_c0 - psi_c1) / h + Hext on faces with both cells in
+// the grid, H = Hext on the grid's boundary faces.  One thread per node (i, j, k) of the cell grid writes the lower
+// x, y and z faces of cell (i, j, k), in one launch over (nx + 1) x (ny + 1) x (nz + 1) points, so psi of the cell
+// is loaded once for its three faces.
+__global__ void __launch_bounds__(256) k_total_field3(Dims d, const double *__restrict__ psi, Faces hext, double invh,
+                                                      Faces H) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
-    if (k >= fz || j >= fy || i >= fx) return;
-    const long long f = (long long)k + (long long)fz * ((long long)j + (long long)fy * i);
-    const int fa = a == 0 ? i : (a == 1 ? j : k);
-    const int dn[3] = {d.nx, d.ny, d.nz};
-    double v = 0.;
-    if (fa > 0 && fa < dn[a]) {
-        int c0[3] = {i, j, k};
-        c0[a] -= 1;
-        v = (psi[cid(d, c0[0], c0[1], c0[2])] - psi[cid(d, i, j, k)]) * invh;
+    if (k > d.nz || j > d.ny || i > d.nx) return;
+    const bool cell = i < d.nx && j < d.ny && k < d.nz;
+    const long long c1 = cell ? cid(d, i, j, k) : 0;
+    const double p1 = cell ? psi[c1] : 0.0;
+    const long long sx = (long long)d.ny * d.nz, sy = d.nz;
+    if (j < d.ny && k < d.nz) {
+        const long long f = fid(d, 0, i, j, k);
+        double v = 0.;
+        if (i > 0 && i < d.nx) v = (psi[c1 - sx] - p1) * invh;
+        v += hext.p[0][f];
+        const_cast<double *>(H.p[0])[f] = v;
     }
-    v += hext.p[a][f];
-    H[f] = v;
+    if (i < d.nx && k < d.nz) {
+        const long long f = fid(d, 1, i, j, k);
+        double v = 0.;
+        if (j > 0 && j < d.ny) v = (psi[c1 - sy] - p1) * invh;
+        v += hext.p[1][f];
+        const_cast<double *>(H.p[1])[f] = v;
+    }
+    if (i < d.nx && j < d.ny) {
+        const long long f = fid(d, 2, i, j, k);
+        double v = 0.;
+        if (k > 0 && k < d.nz) v = (psi[c1 - 1] - p1) * invh;
+        v += hext.p[2][f];
+        const_cast<double *>(H.p[2])[f] = v;
+    }
 }
 
 // ---------------------------------------------------------------------------------- allocation-free residual
@@ -457,13 +484,7 @@ void launch_build_pressure(cudaStream_t st, const Dims &d, const double *phi, co
 
 void launch_apply_projection(cudaStream_t st, const Dims &d, const double *phi, const Faces &frac, const Faces &jump,
                              const double *p, const Faces &u) {
-    // the face axis is a template parameter: the per-axis index arithmetic stays in registers
-    k_apply_projection<0><<<grid3(d.nx + 1, d.ny, d.nz), blk2(), 0, st>>>(d, phi, frac, jump, p,
-                                                                         const_cast<double *>(u.p[0]));
-    k_apply_projection<1><<<grid3(d.nx, d.ny + 1, d.nz), blk2(), 0, st>>>(d, phi, frac, jump, p,
-                                                                         const_cast<double *>(u.p[1]));
-    k_apply_projection<2><<<grid3(d.nx, d.ny, d.nz + 1), blk2(), 0, st>>>(d, phi, frac, jump, p,
-                                                                         const_cast<double *>(u.p[2]));
+    k_apply_projection3<<<grid3(d.nx + 1, d.ny + 1, d.nz + 1), blk2(), 0, st>>>(d, phi, frac, jump, p, u);
 }
 
 void launch_gather_cells(cudaStream_t st, long long n, const double *D, const double *x, double *out) {
@@ -490,6 +511,8 @@ int launch_build_magnetic(cudaStream_t st, const Dims &d, const double *phi, dou
     std::memcpy(&liq_bits, &one_plus_chi, 8);
     SplitOut o{};
     if (so) o = *so;
+    // two passes: mu of each face is formed once (band faces take FP64 sinpi, which a fused pass forming the
+    // upper faces again would evaluate twice) and the row pass reads it back
     k_magnetic_mu<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, phi, chi, bw, 1.0 / bw, key(t), key(-t),
                                                               one_plus_chi, cf, o);
     k_magnetic_rows<<<grid3(d.nx, d.ny, d.nz), blk2(), 0, st>>>(d, hext, h, cf, b, want_invd ? 1 : 0, liq_bits, m1,
@@ -556,9 +579,7 @@ cudaError_t launch_magnetic_residual_noalloc(cudaStream_t st, const Dims &d, con
 
 void launch_total_field(cudaStream_t st, const Dims &d, const double *psi, const Faces &hext, double invh,
                         const Faces &H) {
-    k_total_field<0><<<grid3(d.nx + 1, d.ny, d.nz), blk2(), 0, st>>>(d, psi, hext, invh, const_cast<double *>(H.p[0]));
-    k_total_field<1><<<grid3(d.nx, d.ny + 1, d.nz), blk2(), 0, st>>>(d, psi, hext, invh, const_cast<double *>(H.p[1]));
-    k_total_field<2><<<grid3(d.nx, d.ny, d.nz + 1), blk2(), 0, st>>>(d, psi, hext, invh, const_cast<double *>(H.p[2]));
+    k_total_field3<<<grid3(d.nx + 1, d.ny + 1, d.nz + 1), blk2(), 0, st>>>(d, psi, hext, invh, H);
 }
 
 __global__ void k_to_f32(long long n, const double *__restrict__ a, float *__restrict__ o) {

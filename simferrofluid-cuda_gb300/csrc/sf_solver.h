@@ -156,6 +156,8 @@ class MGSolver {
     int *count_ = nullptr;               // their counts (device)
     float *crow_ = nullptr;              // level 0: the coupling of each uniform row
     float *crow1_ = nullptr;             // level 1 (split): the same
+    float4 *rc_[2] = {nullptr, nullptr}; // levels 0, 1: the half sweep's row constants (k_smooth_consts_s)
+    float *dinv_[2] = {nullptr, nullptr}; // levels 0, 1: the half sweep's 1 / D on general rows
     bool split1_ = false;                // level 1 stored colour by colour too
     SplitOut so_{};                      // split_targets()
     bool copies_written_ = false;        // the assembly wrote the split copies and flags

@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(256) k_dot_rz_s(Dims d, const float *__restric
         a1 += zv.z * qv.z;
         a1 += zv.w * qv.w;
     });
-    double v[2] = {(double)a0, (double)a1};
+    float v[2] = {a0, a1};
     double tot[2];
     if (grid_reduce<2>(v, part, ticket, tot)) {
         const double rho = sc[S_RHO];
@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(256) k_update_s(Dims d, float *__restrict__ x,
         acc += rv.z * rv.z;
         acc += rv.w * rv.w;
     });
-    double v[1] = {(double)acc};
+    float v[1] = {acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) sc[S_RR] = tot[0];
 }
@@ -498,19 +498,74 @@ __device__ __forceinline__ void row_inv(const Dims &d, float c, int i, int j, fl
     inv_end = de > 0.f ? __frcp_rn(de) : 0.f;
 }
 
+// Constants of the smoother's copy of a split level, formed once per build so that a half sweep loads them instead
+// of forming them per cell on every sweep:
+//   rc[row] = {c, 1 / (c n) of interior cells, 1 / (c n) of the row's two end cells, 0} on a uniform row, c being
+//             the value the copy holds (c_of);
+//   dinv[cell] = 1 / D on every cell of a general row (split layout), D the in-grid couplings of the copy summed in
+//             the face order -x, +x, -y, +y, -z, +z, times the copy's unscale, plus the excess times the unscale;
+//             0 where D = 0.
+// Every FP32 operation is rounded explicitly (no contraction), and the reciprocals are IEEE round-to-nearest.
+template <class C>
+__device__ __forceinline__ float unscaled(const Coef<C> &cf, float v) {
+    return sizeof(C) == 2 ? __fmul_rn(v, cf.unscale) : v;
+}
+
+template <class C>
+__global__ void __launch_bounds__(256) k_smooth_consts_s(Dims d, Coef<C> cf, const uint8_t *__restrict__ rows,
+                                                         const float *__restrict__ crow, float4 *__restrict__ rc,
+                                                         float *__restrict__ dinv) {
+    const int nh = d.nz >> 1;
+    const long long hn = d.n >> 1, nrows = (long long)d.nx * d.ny;
+    const long long sx = (long long)d.ny * nh, sy = nh;
+    for (long long row = blockIdx.x * (long long)blockDim.y + threadIdx.y; row < nrows;
+         row += (long long)gridDim.x * blockDim.y) {
+        const uint8_t kind = rows[row];
+        if (!kind) continue;
+        const int i = (int)row / d.ny, j = (int)row - i * d.ny;
+        if (kind == 2) {
+            if (threadIdx.x == 0) {
+                const float c = c_of(cf, crow[row]);
+                float inv_in, inv_end;
+                row_inv(d, c, i, j, inv_in, inv_end);
+                rc[row] = make_float4(c, inv_in, inv_end, 0.f);
+            }
+            continue;
+        }
+        const bool xl = i > 0, xu = i < d.nx - 1, yl = j > 0, yu = j < d.ny - 1;
+        for (int m = threadIdx.x; m < nh; m += blockDim.x)
+#pragma unroll
+            for (int col = 0; col < 2; col++) {
+                const long long own = (long long)col * hn + row * nh + m, oth = (long long)(col ^ 1) * hn + row * nh + m;
+                const int k = 2 * m + ((i + j + col) & 1);
+                float sa = 0.f;
+                if (xl) sa = __fadd_rn(sa, ldv(cf.ax, own));
+                if (xu) sa = __fadd_rn(sa, ldv(cf.ax, oth + sx));
+                if (yl) sa = __fadd_rn(sa, ldv(cf.ay, own));
+                if (yu) sa = __fadd_rn(sa, ldv(cf.ay, oth + sy));
+                // below: k even -> the other colour's m - 1 is the lower neighbour, whose coupling is this cell's az
+                if (k > 0) sa = __fadd_rn(sa, ldv(cf.az, own));
+                // above: the upper neighbour's lower z coupling (m of the other colour for k even, m + 1 for k odd)
+                if (k < d.nz - 1) sa = __fadd_rn(sa, ldv(cf.az, (k & 1) ? oth + 1 : oth));
+                const float D = __fadd_rn(unscaled(cf, sa), unscaled(cf, ldv(cf.dex, own)));
+                dinv[own] = D > 0.f ? __frcp_rn(D) : 0.f;
+            }
+    }
+}
+
 template <bool ZERO>
-__device__ __forceinline__ void rbgs4s_uniform(const Dims &d, float c, float *__restrict__ x,
+__device__ __forceinline__ void rbgs4s_uniform(const Dims &d, float4 rcv, float *__restrict__ x,
                                                const float *__restrict__ b, int col, int i, int j, int m0) {
     const int nh = d.nz >> 1;
-    const long long row = ((long long)i * d.ny + j) * nh + m0;
-    const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
+    const unsigned row = ((unsigned)i * (unsigned)d.ny + (unsigned)j) * (unsigned)nh + (unsigned)m0;
+    const unsigned hn = (unsigned)(d.n >> 1);
+    const unsigned own = (col ? hn : 0u) + row, oth = (col ? 0u : hn) + row;
     const int qz = (i + j + col) & 1;
+    const float c = rcv.x, inv_in = rcv.y, inv_end = rcv.z;
     float bv[4], out[4];
     ld4(b + own, bv);
     Nb4 v;
     if (!ZERO) load_nb4(d, x, oth, i, j, m0, qz, v);
-    float inv_in, inv_end;
-    row_inv(d, c, i, j, inv_in, inv_end);
     for_cells4(qz, [&](auto qc, auto tc) {
         constexpr int QZ = decltype(qc)::value, t = decltype(tc)::value;
         float s, n;
@@ -567,15 +622,17 @@ __device__ __forceinline__ void apply4s_uniform(const Dims &d, float c, const fl
 // selects where the z neighbours sit.
 template <class C, bool ZERO>
 __device__ __forceinline__ void rbgs4s_cells(const Dims &d, const Coef<C> &cf, float *__restrict__ x,
-                                             const float *__restrict__ b, int col, int i, int j, int m0) {
+                                             const float *__restrict__ b, const float *__restrict__ dinv, int col,
+                                             int i, int j, int m0) {
     const int nh = d.nz >> 1;
-    const long long row = ((long long)i * d.ny + j) * nh + m0;
-    const long long own = (long long)col * (d.n >> 1) + row, oth = (long long)(col ^ 1) * (d.n >> 1) + row;
-    const long long sx = (long long)d.ny * nh, sy = nh;
+    const unsigned row = ((unsigned)i * (unsigned)d.ny + (unsigned)j) * (unsigned)nh + (unsigned)m0;
+    const unsigned hn = (unsigned)(d.n >> 1);
+    const unsigned own = (col ? hn : 0u) + row, oth = (col ? 0u : hn) + row;
+    const unsigned sx = (unsigned)d.ny * (unsigned)nh, sy = (unsigned)nh;
     const bool xl = i > 0, xu = i < d.nx - 1, yl = j > 0, yu = j < d.ny - 1;
     float xm[4] = {0, 0, 0, 0}, xp[4] = {0, 0, 0, 0}, ym[4] = {0, 0, 0, 0}, yp[4] = {0, 0, 0, 0}, zo[4] = {0, 0, 0, 0};
-    float bv[4];
-    Cv4<C> axl, axu, ayl, ayu, azl, azo, dx;
+    float bv[4], iv[4];
+    Cv4<C> axl, axu, ayl, ayu, azl, azo;
     axu.zero();
     ayu.zero();
     axl.load(cf.ax + own);
@@ -584,7 +641,7 @@ __device__ __forceinline__ void rbgs4s_cells(const Dims &d, const Coef<C> &cf, f
     if (yu) ayu.load(cf.ay + oth + sy);
     azl.load(cf.az + own);
     azo.load(cf.az + oth);
-    dx.load(cf.dex + own);
+    ld4(dinv + own, iv);
     ld4(b + own, bv);
     if (!ZERO) {
         if (xl) ld4(x + oth - sx, xm);
@@ -607,46 +664,21 @@ __device__ __forceinline__ void rbgs4s_cells(const Dims &d, const Coef<C> &cf, f
         auto upd = [&](auto tc) {
             constexpr int t = decltype(tc)::value;
             const int k = 2 * (m0 + t) + QZ;
-            float s = 0.f, sa = 0.f;
-            if (xl) {
-                const float a = axl[t];
-                if (!ZERO) s += a * xm[t];
-                sa += a;
+            float s = 0.f;
+            if (!ZERO) {
+                if (xl) s += axl[t] * xm[t];
+                if (xu) s += axu[t] * xp[t];
+                if (yl) s += ayl[t] * ym[t];
+                if (yu) s += ayu[t] * yp[t];
+                // below: m - 1 (k even) or m (k odd) of the other colour
+                if (k > 0) s += azl[t] * (QZ == 0 ? (t == 0 ? zx : zo[t == 0 ? 0 : t - 1]) : zo[t]);
+                // above: m (k even) or m + 1 (k odd), whose lower z coupling is this face's
+                if (k < d.nz - 1)
+                    s += (QZ == 0 ? azo[t] : (t == 3 ? azx : azo[t == 3 ? 3 : t + 1])) *
+                         (QZ == 0 ? zo[t] : (t == 3 ? zx : zo[t == 3 ? 3 : t + 1]));
+                if (sizeof(C) == 2) s *= cf.unscale;
             }
-            if (xu) {
-                const float a = axu[t];
-                if (!ZERO) s += a * xp[t];
-                sa += a;
-            }
-            if (yl) {
-                const float a = ayl[t];
-                if (!ZERO) s += a * ym[t];
-                sa += a;
-            }
-            if (yu) {
-                const float a = ayu[t];
-                if (!ZERO) s += a * yp[t];
-                sa += a;
-            }
-            if (k > 0) {  // below: m - 1 (k even) or m (k odd) of the other colour
-                const float a = azl[t];
-                if (!ZERO) s += a * (QZ == 0 ? (t == 0 ? zx : zo[t == 0 ? 0 : t - 1]) : zo[t]);
-                sa += a;
-            }
-            if (k < d.nz - 1) {  // above: m (k even) or m + 1 (k odd), whose lower z coupling is this face's
-                const float a = QZ == 0 ? azo[t] : (t == 3 ? azx : azo[t == 3 ? 3 : t + 1]);
-                if (!ZERO) s += a * (QZ == 0 ? zo[t] : (t == 3 ? zx : zo[t == 3 ? 3 : t + 1]));
-                sa += a;
-            }
-            if (sizeof(C) == 2) {
-                if (!ZERO) s *= cf.unscale;
-                sa *= cf.unscale;
-            }
-            float e = dx[t];
-            if (sizeof(C) == 2) e *= cf.unscale;
-            const float D = sa + e;
-            const float inv = D > 0.f ? __frcp_rn(D) : 0.f;  // = 1.f / D (IEEE round to nearest)
-            out[t] = (bv[t] + s) * inv;
+            out[t] = (bv[t] + s) * iv[t];  // iv: 1 / D of the copy (k_smooth_consts_s)
         };
         upd(std::integral_constant<int, 0>{});
         upd(std::integral_constant<int, 1>{});
@@ -660,21 +692,21 @@ __device__ __forceinline__ void rbgs4s_cells(const Dims &d, const Coef<C> &cf, f
     *reinterpret_cast<float4 *>(x + own) = make_float4(out[0], out[1], out[2], out[3]);
 }
 
-// Persistent half sweep: warps over the active rows' chunks of 32 vectors.
+// Persistent half sweep: warps over the active rows' chunks of 32 vectors.  rc, dinv: k_smooth_consts_s.
 template <class C, bool ZERO>
 __global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__restrict__ x,
-                                                  const float *__restrict__ b,
-                                                int col, const int *__restrict__ list, const int *__restrict__ count,
-                                                const float *__restrict__ crow) {
+                                                  const float *__restrict__ b, int col, const int *__restrict__ list,
+                                                  const int *__restrict__ count, const float4 *__restrict__ rc,
+                                                  const float *__restrict__ dinv) {
     pdl_entry();
     const int nq = d.nz >> 3;
     for_list_items(list, count, 1, (nq + 31) / 32, [&](int, int i, int j, int ch, bool uni) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
         if (uni)
-            rbgs4s_uniform<ZERO>(d, c_of(cf, crow[(long long)i * d.ny + j]), x, b, col, i, j, 4 * q4);
+            rbgs4s_uniform<ZERO>(d, rc[(unsigned)i * (unsigned)d.ny + (unsigned)j], x, b, col, i, j, 4 * q4);
         else
-            rbgs4s_cells<C, ZERO>(d, cf, x, b, col, i, j, 4 * q4);
+            rbgs4s_cells<C, ZERO>(d, cf, x, b, dinv, col, i, j, 4 * q4);
     });
 }
 
@@ -978,7 +1010,7 @@ __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, 
             *reinterpret_cast<float4 *>(q + own) = make_float4(out[0], out[1], out[2], out[3]);
         }
     });
-    double v[1] = {(double)acc};
+    float v[1] = {acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) {
         sc[S_PQ] = tot[0];

@@ -30,7 +30,8 @@ __global__ void __launch_bounds__(256) k_cos_dots(long long n, const float *__re
         a1 += oc * oc;
         a2 += tc * tc;
     }
-    double v[3] = {a0, a1, a2}, tot[3];
+    float v[3] = {a0, a1, a2};
+    double tot[3];
     if (grid_reduce<3>(v, part, ticket, tot)) {
         out[0] = tot[0];
         out[1] = tot[1];
