@@ -48,6 +48,7 @@ def parse(argv=None):
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64-arm", action="store_true")
+    ap.add_argument("--no-learned-arm", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the errors against the oracle's FP64 answer")
     ap.add_argument("--inner-tol", type=float, default=None, help="mixed form: inner relative reduction floor")
@@ -225,6 +226,7 @@ def run_ours(args, ws, rank, local):
                            profile=profile, **kw)
 
     def step(precision, profile=0, record=None):
+        # the learned form is the mixed solver with the network's correction steps (SF_PREC_LEARNED)
         for a in range(3):
             vel[a].copy_(vel0[a])
         sp = P.project(vel, phi, frac, opts=opts("pressure", precision, profile), device=True, p_out=p_out)
@@ -271,6 +273,28 @@ def run_ours(args, ws, rank, local):
         fp64 = {"solves_per_s": 2 * max(2, args.steps // 2) * ws / (ms64 / 1e3),
                 "ms_per_step": ms64 / max(2, args.steps // 2),
                 "iters_pressure": [r[0]["iters"] for r in rec64], "iters_magnetic": [r[1]["iters"] for r in rec64]}
+
+    # mixed + learned arm: the mixed solver with the trained U-Net's correction steps at the start of every inner
+    # solve (weights/unet.f32; the plain MGPCG finishes every solve and the FP64 residual judges it)
+    learned = None
+    if not args.no_learned_arm and args.precision == "mixed":
+        wpath = os.path.join(ROOT, PKG, "weights", "unet.f32")
+        net = pkg.Network(ctx)
+        net.load(wpath)
+        ctx.set_network(net)
+        nl = max(2, args.steps // 2)
+        msl, recl, _ = timed("learned", nl, 2)
+        ctx.set_network(None)
+        net.close()
+        learned = {"solves_per_s": 2 * nl * ws / (msl / 1e3), "ms_per_step": msl / nl,
+                   "weights": os.path.relpath(wpath, ROOT),
+                   "iters_pressure": [r[0]["iters"] for r in recl], "iters_magnetic": [r[1]["iters"] for r in recl],
+                   "learned_steps": [[r[0]["learned_steps"], r[1]["learned_steps"]] for r in recl],
+                   "guess_energy_ratio": [[round(r[0]["guess_energy_ratio"], 4), round(r[1]["guess_energy_ratio"], 4)]
+                                          for r in recl],
+                   "max_rel_residual": max(max(r[0]["rel_residual"], r[1]["rel_residual"]) for r in recl)}
+        if fp64:
+            learned["speedup_vs_fp64"] = round(learned["solves_per_s"] / fp64["solves_per_s"], 3)
 
     # dominant kernel: finest-level red-black smoother, timed live with CUDA events on the library's stream in
     # a profiled pass of the same workload (opts.profile: every finest-level smoother launch bracketed by events)
@@ -373,6 +397,7 @@ def run_ours(args, ws, rank, local):
         "iters": {"pressure": it_p, "magnetic": it_m}, "max_rel_residual": {"pressure": res_p, "magnetic": res_m},
         "fp64_mgpcg": fp64,
         "speedup_vs_fp64": round(value / fp64["solves_per_s"], 3) if fp64 else None,
+        "mixed_learned": learned,
         "roofline": roofline, "clocks": clk, "e2e": e2e, "gpu_launches": int(launches),
         "scene_build_s": round(t_scene, 2),
     }

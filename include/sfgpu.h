@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SFGPU_ABI_VERSION 1
+#define SFGPU_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define SF_EXPORT __attribute__((visibility("default")))
@@ -38,7 +38,8 @@ typedef enum {
     SF_CUDA_ERROR = 3,      /* a CUDA call failed; sf_last_error() has the message */
     SF_NO_DEVICE = 4,       /* no CUDA device, or the device is not sm_103 */
     SF_OUT_OF_MEMORY = 5,
-    SF_STALLED_FALLBACK = 6, /* learned solve stalled; the plain MGPCG finished the solve (not an error) */
+    SF_STALLED_FALLBACK = 6, /* learned solve: the network stalled (a step removed less than 10% of the residual,
+                                or was not finite); the plain MGPCG finished the solve (not an error) */
     SF_NOT_READY = 7,       /* Reproject called before any Project on this context / grid */
     SF_TOO_LARGE = 8        /* grid exceeds the fixed scratch of sf_magnetic_residual_noalloc */
 } sf_status;
@@ -46,9 +47,12 @@ typedef enum {
 typedef enum {
     SF_PREC_FP64 = 0,   /* plain method: FP64 MGPCG */
     SF_PREC_MIXED = 1,  /* FP32 V-cycle, FP16 coarse coefficients, inner FP32 FCG, FP64 iterative refinement */
-    SF_PREC_LEARNED = 2 /* mixed form started from the attached U-Net's prediction y scaled by
-                           gamma = (y,b)/(y,Ay) (never a larger A-norm error than zero); a non-finite
-                           prediction is discarded and the solve starts from zero (SF_STALLED_FALLBACK) */
+    SF_PREC_LEARNED = 2 /* mixed form with learned correction steps: at the start of every inner flexible-CG
+                           solve of the refinement (the first from r = b), the attached U-Net's prediction y of
+                           A^-1 r, scaled by gamma = (y,r)/(y,Ay) (never a larger A-norm error than no step), is
+                           the first step, and the flexible CG continues from the remaining residual.  A step
+                           that removes less than 10% of ||r|| stalls the network: the rest of the solve is the
+                           plain MGPCG iteration (SF_STALLED_FALLBACK); the FP64 residual judges the result. */
 } sf_precision;
 
 /* Cell grid of a staggered grid: resolution, spacing and corner (StaggeredGrid ctor,
@@ -104,8 +108,11 @@ typedef struct {
     double smooth_ms;        /* profile: their summed device time */
     long long kernel_launches; /* kernels this call launched (graph nodes counted per replay) */
     double smooth_bytes;     /* profile: algorithmic bytes of the timed smoother launches */
-    double guess_rel_residual; /* learned form: ||b - A x0|| / ||b|| of the network's initial guess (-1: none) */
-    double guess_energy_ratio; /* learned form: ||x* - x0||_A^2 / ||x*||_A^2 of that guess (-1: none) */
+    double guess_rel_residual; /* learned form: ||b - A x0|| / ||b|| after the first learned step x0 = gamma y
+                                  (-1: none) */
+    double guess_energy_ratio; /* learned form: ||x* - x0||_A^2 / ||x*||_A^2 of that step (-1: none) */
+    int learned_steps;         /* learned form: correction steps applied */
+    int reserved_stats;
 } sf_solve_stats;
 
 /* ----- context ------------------------------------------------------------------------------------------- */

@@ -62,10 +62,11 @@ class sf_solve_stats(C.Structure):
                 ("ms_total", C.c_double), ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong),
                 ("status_detail", C.c_int), ("smooth_launches", C.c_int), ("smooth_ms", C.c_double),
                 ("kernel_launches", C.c_longlong), ("smooth_bytes", C.c_double),
-                ("guess_rel_residual", C.c_double), ("guess_energy_ratio", C.c_double)]
+                ("guess_rel_residual", C.c_double), ("guess_energy_ratio", C.c_double),
+                ("learned_steps", C.c_int), ("reserved_stats", C.c_int)]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        return {f: getattr(self, f) for f, _ in self._fields_ if not f.startswith("reserved")}
 
 
 _P3 = C.c_void_p * 3

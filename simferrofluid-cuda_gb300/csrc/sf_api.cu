@@ -138,6 +138,7 @@ void fill_stats(sf_solve_stats *s, const SolveResult &r, long long unknowns) {
     s->smooth_bytes = r.smooth_bytes;
     s->guess_rel_residual = r.guess_relres;
     s->guess_energy_ratio = r.guess_energy;
+    s->learned_steps = r.learned_steps;
 }
 
 float ev_ms(cudaEvent_t a, cudaEvent_t b) {
@@ -146,20 +147,40 @@ float ev_ms(cudaEvent_t a, cudaEvent_t b) {
     return ms;
 }
 
-// Learned initial guess: network features of the assembled system -> U-Net -> x0 = gamma y on the solver.
-sf_status learned_guess(Ctx *c, MGSolver &S, const Dims &d, SolveResult &pre) {
+// The learned form's network as the solver's correction step: features of the assembled system are formed once
+// per solve; each step rewrites their right-hand-side channel with the current residual and runs the U-Net.
+struct NetStep final : LearnedStep {
+    Ctx *c = nullptr;
+    Dims d{0, 0, 0, 0};
+    __nv_bfloat16 *feat = nullptr;
+    cudaError_t predict(const float *r, double rr, float *y) override {
+        const double cnt = c->net->active_cells() > 0 ? c->net->active_cells() : 1.0;
+        const double rms = std::sqrt(rr / cnt);
+        cudaError_t e = c->net->set_rhs_channel(d, r, rms > 0 ? 1.0 / rms : 0.0, feat);
+        if (e != cudaSuccess) return e;
+        if ((e = c->net->forward(d, feat, y)) != cudaSuccess) return e;
+        if (c->net->mode() == 1 && (e = c->net->check_device_errors()) != cudaSuccess) return e;
+        return cudaSuccess;
+    }
+};
+
+// Detaches the step from the solver when the solve returns, on every path.
+struct LearnedScope {
+    MGSolver *S = nullptr;
+    ~LearnedScope() {
+        if (S) S->set_learned(nullptr);
+    }
+};
+
+sf_status learned_prepare(Ctx *c, MGSolver &S, const Dims &d, NetStep &step, LearnedScope &scope) {
     if (!c->net) return fail(c, SF_NOT_READY, "learned precision needs a network (sf_set_network)");
     CK(c->feat.ensure(2 * 16 * (size_t)d.n));
-    CK(c->guess.ensure(4 * (size_t)d.n));
-    auto *feat = (__nv_bfloat16 *)c->feat.get();
-    auto *y = (float *)c->guess.get();
-    CK(c->net->features(d, S.fine(), S.b(), feat));
-    CK(c->net->forward(d, feat, y));
-    if (c->net->mode() == 1 && c->net->check_device_errors() != cudaSuccess)
-        return fail(c, SF_CUDA_ERROR, c->net->last_error);
-    double gamma = 0;
-    CK(S.set_guess_scaled(y, gamma));
-    (void)pre;
+    step.c = c;
+    step.d = d;
+    step.feat = (__nv_bfloat16 *)c->feat.get();
+    CK(c->net->features(d, S.fine(), S.b(), step.feat));
+    S.set_learned(&step);
+    scope.S = &S;
     return SF_OK;
 }
 
@@ -230,11 +251,12 @@ sf_status pressure_impl(Ctx *c, const sf_grid *g, double *const vel[3], const do
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->ev[1], c->st));
     SolveResult res;
-    bool zero = !reproject;  // Project starts from zero (core/Pressure.cpp:122); Reproject from the last pressure
+    const bool zero = !reproject;  // Project starts from zero (core/Pressure.cpp:122); Reproject from the last p
+    NetStep step;
+    LearnedScope scope;
     if (opts && opts->precision == SF_PREC_LEARNED && !reproject) {
-        sf_status ls = learned_guess(c, S, d, res);
+        sf_status ls = learned_prepare(c, S, d, step, scope);
         if (ls != SF_OK) return ls;
-        zero = false;
     }
     CK(S.solve(zero, res));
     double relres = res.relres, bn = res.bnorm;
@@ -324,11 +346,12 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->ev[1], c->st));
     SolveResult res;
-    bool zero = !warm;
+    const bool zero = !warm;
+    NetStep step;
+    LearnedScope scope;
     if (opts && opts->precision == SF_PREC_LEARNED) {
-        sf_status ls = learned_guess(c, S, d, res);
+        sf_status ls = learned_prepare(c, S, d, step, scope);
         if (ls != SF_OK) return ls;
-        zero = false;
     }
     CK(S.solve(zero, res));
     CK(S.shift_to_zero_at_origin());

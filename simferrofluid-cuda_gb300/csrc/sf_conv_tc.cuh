@@ -79,11 +79,13 @@ struct Layout {
     static constexpr uint32_t kSmemBytes = kNeed > 30u * 1024u ? kNeed : 30u * 1024u;
 };
 
-// err: first error code of any CTA (1 = TMA/MMA wait timed out)
-template <int CI, int CO>
+// err: first error code of any CTA (1 = TMA/MMA wait timed out).
+// EPI 0: + bias, ReLU, BF16 out (forward).  EPI 1: FP32 out, no bias (input gradient, with the mirrored and
+// transposed weights).
+template <int CI, int CO, int EPI = 0>
 __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUtensorMap tmap_x,
                                                     const __grid_constant__ CUtensorMap tmap_w, Dims d,
-                                                    const float *__restrict__ bias, __nv_bfloat16 *__restrict__ y,
+                                                    const float *__restrict__ bias, void *__restrict__ yout,
                                                     int *err) {
     static_assert(CI % 16 == 0 && CO % 16 == 0 && CO <= kTmemCols, "shape");
     using L = Layout<CI, CO>;
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
         for (int c0 = 0; c0 < CO; c0 += 16) {
             float acc[16];
             tmem_ld_x16<16>(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, acc);
-            if (inb) {
+            if (inb && EPI == 0) {
                 uint32_t pk[8];
 #pragma unroll
                 for (int q = 0; q < 8; q++) {
@@ -194,9 +196,13 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
                     __nv_bfloat162 h2 = __floats2bfloat162_rn(a0, a1);
                     pk[q] = *reinterpret_cast<uint32_t *>(&h2);
                 }
-                uint4 *dst = reinterpret_cast<uint4 *>(y + v * CO + c0);
+                uint4 *dst = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(yout) + v * CO + c0);
                 dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
                 dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            } else if (inb) {
+                float4 *dst = reinterpret_cast<float4 *>(reinterpret_cast<float *>(yout) + v * CO + c0);
+#pragma unroll
+                for (int q = 0; q < 4; q++) dst[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
             }
         }
     }

@@ -279,7 +279,15 @@ enum Slot {
     S_AUX1,
     S_AUX2,
     S_ERR,  // set to 1 by a kernel whose bounded wait timed out
-    S_NSLOTS = 16
+    S_LGAMMA,  // learned step: gamma, (r, y), (y, A y)
+    S_LRY,
+    S_LYAY,
+    S_IT,      // device-side inner loop: iterations run, (target residual)^2, iteration budget, last ||r||^2,
+    S_TOL2,    // consecutive slow iterations
+    S_BUDGET,
+    S_RPREV,
+    S_SLOW,
+    S_NSLOTS = 32
 };
 
 }  // namespace sf

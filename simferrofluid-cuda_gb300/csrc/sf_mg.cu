@@ -1198,6 +1198,41 @@ __global__ void __launch_bounds__(256) k_cast_rhs(long long n, const double *__r
     }
 }
 
+// y = 0 on inactive cells (D = 0), where the solver's vectors are zero
+__global__ void k_mask_active(long long n, const double *__restrict__ D, float *__restrict__ y) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        if (!(D[c] > 0)) y[c] = 0.f;
+}
+
+// Learned step: gamma = (r, y) / (y, A y) from the slots k_dot_rz left (RHONEW = (r, y), ZQ = (y, A y); 0 when
+// not finite or (y, A y) <= 0); d = gamma y, r -= gamma A y, (r, r) -> RR; gamma, (r, y), (y, A y) -> the
+// learned-step slots.
+__global__ void __launch_bounds__(256) k_learned_update(long long n, float *__restrict__ dlt, float *__restrict__ r,
+                                                        const float *__restrict__ y, const float *__restrict__ ay,
+                                                        double *sc, double *part, unsigned *ticket) {
+    const double ry = sc[S_RHONEW], yay = sc[S_ZQ];
+    double g = (yay > 0 && isfinite(yay) && isfinite(ry)) ? ry / yay : 0.0;
+    if (!isfinite(g)) g = 0.0;
+    const float gf = (float)g;
+    float acc = 0.f;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
+        // no step when gamma = 0: y and A y may hold non-finite values, and 0 times those is not zero
+        const float rc = gf != 0.f ? r[c] - gf * ay[c] : r[c];
+        dlt[c] = gf != 0.f ? gf * y[c] : 0.f;
+        r[c] = rc;
+        acc += rc * rc;
+    }
+    float v[1] = {acc};
+    double tot[1];
+    if (grid_reduce<1>(v, part, ticket, tot)) {
+        sc[S_RR] = tot[0];
+        sc[S_LGAMMA] = g;
+        sc[S_LRY] = ry;
+        sc[S_LYAY] = yay;
+    }
+}
+
 // (y, b) with y FP32 and b FP64 -> slot
 __global__ void __launch_bounds__(256) k_dot_fd(long long n, const float *__restrict__ y, const double *__restrict__ b,
                                                 int slot, double *sc, double *part, unsigned *ticket) {
@@ -1605,7 +1640,8 @@ MGSolver::~MGSolver() {
 void MGSolver::destroy_graphs() {
     if (g_iter64_) cudaGraphExecDestroy(g_iter64_);
     if (g_iter32_) cudaGraphExecDestroy(g_iter32_);
-    g_iter64_ = g_iter32_ = nullptr;
+    if (g_loop32_) cudaGraphExecDestroy(g_loop32_);
+    g_iter64_ = g_iter32_ = g_loop32_ = nullptr;
     graph_key_ = -1;
 }
 
@@ -1945,7 +1981,7 @@ void MGSolver::enqueue_iter64() {
     cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
 }
 
-void MGSolver::enqueue_iter32() {
+void MGSolver::enqueue_iter32(bool copy_slots) {
     const Dims &d = lev_dims_[0];
     const long long n = d.n;
     const long long l0 = tk_.launches;
@@ -1967,7 +2003,7 @@ void MGSolver::enqueue_iter32() {
                    q32_, lst0, cnt0, sc_, part_, ticket_);
         tk_.launches += 4;
         iter_launches32_ = tk_.launches - l0;
-        cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
+        if (copy_slots) cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
         return;
     }
     if (prm_.smoother == 2 || prm_.smoother == 3)
@@ -1982,7 +2018,106 @@ void MGSolver::enqueue_iter32() {
     launch_pdl(k_update<float>, kMaxRedBlocks, dim3(32, 8), st_, n, d32_, ri32_, p32_, q32_, sc_, part_, ticket_);
     tk_.launches += 4;
     iter_launches32_ = tk_.launches - l0;
-    cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
+    if (copy_slots) cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
+}
+
+// Control of the device-side inner loop (one thread, the last node of the loop body): counts the iteration and
+// continues while no breakdown or timed-out wait was flagged, ||r||^2 is finite and above its target, the budget
+// is not spent, and the iteration is not stagnating -- the host loop's tests: two consecutive iterations each
+// leaving more than a quarter of ||r||^2 end the inner solve (FP32 stagnation; the refinement takes over).
+__global__ void k_inner_ctl(double *sc, cudaGraphConditionalHandle h) {
+    const double it = sc[S_IT] + 1.0;
+    sc[S_IT] = it;
+    const double rin = sc[S_RR];
+    const double slow = rin > 0.25 * sc[S_RPREV] ? sc[S_SLOW] + 1.0 : 0.0;
+    sc[S_SLOW] = slow;
+    sc[S_RPREV] = rin;
+    const bool go = sc[S_AUX0] == 0.0 && sc[S_ERR] == 0.0 && isfinite(rin) && rin > sc[S_TOL2] &&
+                    it < sc[S_BUDGET] && slow < 2.0;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+cudaError_t MGSolver::build_loop32() {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e != cudaSuccess) return e;
+    cudaGraphConditionalHandle h;
+    cudaGraphNodeParams cp = {};
+    if ((e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault)) == cudaSuccess) {
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+    }
+    if (e == cudaSuccess) {
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        const long long before = tk_.launches;
+        e = cudaStreamBeginCaptureToGraph(st_, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            enqueue_iter32(false);
+            k_inner_ctl<<<1, 1, 0, st_>>>(sc_, h);
+            e = cudaStreamEndCapture(st_, &body);
+        }
+        tk_.launches = before;  // counted per iteration after each loop
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&g_loop32_, g, 0);
+    if (e != cudaSuccess) g_loop32_ = nullptr;
+    cudaGraphDestroy(g);
+    return e;
+}
+
+// Runs inner iterations until the loop's tests stop it (at least one; budget > 0), from the recurrence state
+// already on the device.  One graph launch and one read-back when the device-side loop is available, else one
+// graph launch (or direct launches) and one read-back per iteration.
+cudaError_t MGSolver::inner_loop(int budget, double tol2, double rr, int &iters) {
+    cudaError_t e;
+    iters = 0;
+    if (prm_.use_graph && !prm_.profile && loop_ok_) {
+        // same configuration key as run_iter's graphs (it destroys this one as well when the key changes)
+        if ((e = run_iter_prepare()) != cudaSuccess) return e;
+        if (!g_loop32_ && build_loop32() != cudaSuccess) {
+            cudaGetLastError();
+            loop_ok_ = false;  // the host-driven loop below
+        }
+    }
+    if (prm_.use_graph && !prm_.profile && loop_ok_ && g_loop32_) {
+        const double st[5] = {0.0, tol2, (double)budget, rr, 0.0};  // S_IT, S_TOL2, S_BUDGET, S_RPREV, S_SLOW
+        cudaMemcpyAsync(sc_ + S_IT, st, sizeof(st), cudaMemcpyHostToDevice, st_);
+        if ((e = cudaGraphLaunch(g_loop32_, st_)) != cudaSuccess) return e;
+        if ((e = read_slots()) != cudaSuccess) return e;
+        iters = (int)sc_host_[S_IT];
+        tk_.launches += (long long)iters * (iter_launches32_ + 1);
+        return cudaSuccess;
+    }
+    double rprev = rr;
+    int slow = 0;
+    const int every = prm_.check_every > 0 ? prm_.check_every : 1;
+    while (iters < budget) {
+        for (int s = 0; s < every && iters < budget; s++, iters++)
+            if ((e = run_iter(true)) != cudaSuccess) return e;
+        if ((e = cudaStreamSynchronize(st_)) != cudaSuccess) return e;
+        const double rin = sc_host_[S_RR];
+        if (sc_host_[S_AUX0] != 0) break;
+        if (rin <= tol2 || !std::isfinite(rin)) break;
+        // FP32 stagnation: two consecutive iterations reducing ||r|| by less than 2x -> refine in FP64
+        slow = (rin > 0.25 * rprev) ? slow + 1 : 0;
+        rprev = rin;
+        if (slow >= 2) break;
+    }
+    return cudaSuccess;
+}
+
+// The captured graphs depend on the smoothing configuration: drop them when it changed.
+cudaError_t MGSolver::run_iter_prepare() {
+    const long long key = (long long)prm_.pre | ((long long)prm_.post << 8) | ((long long)prm_.coarse_sweeps << 16) |
+                          ((long long)prm_.flexible << 32) | ((long long)prm_.smoother << 33) |
+                          ((long long)prm_.coarse_pre << 36) | ((long long)prm_.coarse_post << 44) |
+                          ((long long)tail_nc_ << 52);
+    if (key != graph_key_) destroy_graphs();
+    graph_key_ = key;
+    return cudaSuccess;
 }
 
 cudaError_t MGSolver::run_iter(bool mixed) {
@@ -1995,12 +2130,7 @@ cudaError_t MGSolver::run_iter(bool mixed) {
             enqueue_iter64();
         return cudaGetLastError();
     }
-    const long long key = (long long)prm_.pre | ((long long)prm_.post << 8) | ((long long)prm_.coarse_sweeps << 16) |
-                          ((long long)prm_.flexible << 32) | ((long long)prm_.smoother << 33) |
-                          ((long long)prm_.coarse_pre << 36) | ((long long)prm_.coarse_post << 44) |
-                          ((long long)tail_nc_ << 52);
-    if (key != graph_key_) destroy_graphs();
-    graph_key_ = key;
+    run_iter_prepare();
     cudaGraphExec_t &ge = mixed ? g_iter32_ : g_iter64_;
     if (!ge) {
         cudaGraph_t g;
@@ -2038,7 +2168,6 @@ cudaError_t MGSolver::read_slots() {
 
 cudaError_t MGSolver::solve(bool x_is_zero, SolveResult &res) {
     res = SolveResult{};
-    if (x_is_zero) guess_ = false;
     res.levels = (int)lev_dims_.size();
     tk_.prof = prm_.profile;
     cudaError_t e = prm_.precision == 0 ? solve64(x_is_zero, res) : solve_mixed(x_is_zero, res);
@@ -2121,7 +2250,7 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
     double bb = -1, rr = 0;
     int total_inner = 0, outer = 0;
     const int max_outer = 30;
-    bool x_zero = x_is_zero;
+    bool x_zero = x_is_zero, stalled = false;
     while (true) {
         // outer FP64 residual, cast to the FP32 inner right-hand side
         if (x_zero) {
@@ -2148,19 +2277,6 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
                 return cudaStreamSynchronize(st_);
             }
         }
-        if (guess_) {
-            // x0 = gamma y never has a larger A-norm error than zero (gamma minimises it along y); it is
-            // discarded only when it is not finite
-            guess_ = false;
-            res.guess_relres = std::sqrt(rr / bb);
-            if (!std::isfinite(rr) || !(guess_yb_ != 0.0)) {
-                res.fallback = true;
-                cudaMemsetAsync(x_, 0, 8 * n, st_);
-                x_zero = true;
-                bb = -1;
-                continue;
-            }
-        }
         const double rel = std::sqrt(rr / bb);
         if (rel <= prm_.tol || !std::isfinite(rr) || outer >= max_outer || total_inner >= prm_.max_iters) break;
         // inner FCG on A32 d = r32, d = 0
@@ -2176,22 +2292,18 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
             cudaMemcpyAsync(sc_ + S_RHO, init, 8, cudaMemcpyHostToDevice, st_);
             cudaMemcpyAsync(sc_ + S_ALPHA, init + 1, 8 * 3, cudaMemcpyHostToDevice, st_);
         }
+        if (learned_ && !stalled) {
+            if ((e = learned_step(rr, outer == 0, stalled, res)) != cudaSuccess) return e;
+            if (outer == 0) res.guess_relres = std::sqrt(sc_host_[S_RR] / bb);
+        }
         int it = 0;
-        double rin = rr, rprev = rr;
-        int slow = 0;
-        const int every = prm_.check_every > 0 ? prm_.check_every : 1;
         const int budget = prm_.max_iters - total_inner;
-        while (it < budget) {
-            for (int s = 0; s < every && it < budget; s++, it++)
-                if ((e = run_iter(true)) != cudaSuccess) return e;
-            if ((e = cudaStreamSynchronize(st_)) != cudaSuccess) return e;
-            rin = sc_host_[S_RR];
-            if (sc_host_[S_AUX0] != 0) break;
-            if (rin <= in_tol2 || !std::isfinite(rin)) break;
-            // FP32 stagnation: two consecutive iterations reducing ||r|| by less than 2x -> refine in FP64
-            slow = (rin > 0.25 * rprev) ? slow + 1 : 0;
-            rprev = rin;
-            if (slow >= 2) break;
+        // the inner residual after a learned step (it is the FP64 residual otherwise)
+        const double rin0 = (learned_ && res.learned_steps > 0 && !stalled) ? sc_host_[S_RR] : rr;
+        if (budget > 0 && (e = inner_loop(budget, in_tol2, rin0, it)) != cudaSuccess) return e;
+        if (sc_host_[S_ERR] != 0) {
+            last_error = "a smoother's TMA load did not arrive within its bounded wait";
+            return cudaErrorLaunchTimeout;
         }
         total_inner += it;
         if (split0_)
@@ -2211,7 +2323,7 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
     res.outer = outer;
     res.relres = std::sqrt(rr / bb);
     res.converged = res.relres <= prm_.tol;
-    if (res.guess_relres >= 0 && !res.fallback && guess_yay_ > 0) {
+    if (res.guess_relres >= 0 && guess_yay_ > 0 && std::isfinite(guess_yb_)) {
         // A-norm error of the guess relative to zero: 1 - (y,b)^2 / ((y,Ay) (b,x*)), x* = the solution
         k_dot_dd<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, b_, x_, S_AUX2, sc_, part_, ticket_);
         tk_.launches++;
@@ -2222,30 +2334,56 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
     return cudaGetLastError();
 }
 
-cudaError_t MGSolver::set_guess_scaled(const float *y, double &gamma) {
-    if (prm_.precision != 1) return cudaErrorInvalidValue;
+// One learned correction step at the start of an inner solve (d32 = 0, p32 = q32 = 0, r32 = the inner residual,
+// rr its squared norm): y = N(r) on the active cells, q = A y, gamma = (y, r) / (y, q), d32 = gamma y,
+// r32 -= gamma q.  p32 and q32 serve as scratch and are cleared again, with the recurrence's slots.
+cudaError_t MGSolver::learned_step(double rr, bool first, bool &stalled, SolveResult &res) {
     const Dims &d = lev_dims_[0];
-    // (y, A y) on the FP32 level-0 operator and (y, b); gamma minimises the A-norm error along y
+    const long long n = d.n;
+    cudaError_t e;
+    if ((e = lrn_r_.ensure(4 * (size_t)n)) != cudaSuccess) return e;
+    if ((e = lrn_y_.ensure(4 * (size_t)n)) != cudaSuccess) return e;
+    float *rn = (float *)lrn_r_.get(), *yn = (float *)lrn_y_.get();
+    if (split0_)
+        k_split_to_vec<<<split_rows_grid(d), dim3(32, 8), 0, st_>>>(d, r32_, rn);
+    else
+        cudaMemcpyAsync(rn, r32_, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st_);
+    if ((e = learned_->predict(rn, rr, yn)) != cudaSuccess) return e;
+    k_mask_active<<<flat_grid(n), 256, 0, st_>>>(n, c64_[0].D, yn);
+    // (r, y) and (y, A y): q32 = A y (p32 = y), then the flexible beta's dot kernel on (r, y, A y)
     if (split0_) {
-        // scratch: q32 and p32, cleared before the solve's first inner iteration
-        k_vec_to_split<<<split_rows_grid(d), dim3(32, 8), 0, st_>>>(d, y, q32_);
-        apply_dot32s(st_, d, c32_, q32_, p32_, list_[0], count_, crow_, sc_, part_, ticket_);
-        tk_.launches++;
+        k_vec_to_split<<<split_rows_grid(d), dim3(32, 8), 0, st_>>>(d, yn, p32_);
+        apply_dot32s(st_, d, c32_, p32_, q32_, list_[0], count_, crow_, sc_, part_, ticket_);
+        const long long vitems = split_items(2LL * d.nx * d.ny, d.nz >> 3);
+        k_dot_rz_s<<<row_grid((const void *)k_dot_rz_s, vitems), dim3(32, 8), 0, st_>>>(
+            d, r32_, p32_, q32_, list_[0], count_, 1, sc_, part_, ticket_);
     } else {
-        apply_dot32(st_, d, c32_, y, q32_, sc_, part_, ticket_);
+        cudaMemcpyAsync(p32_, yn, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st_);
+        apply_dot32(st_, d, c32_, p32_, q32_, sc_, part_, ticket_);
+        k_dot_rz<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, r32_, p32_, q32_, 1, sc_, part_, ticket_);
     }
-    k_dot_fd<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(d.n, y, b_, S_AUX2, sc_, part_, ticket_);
-    tk_.launches += 2;
-    cudaError_t e = read_slots();
-    if (e != cudaSuccess) return e;
-    const double yay = sc_host_[S_PQ], yb = sc_host_[S_AUX2];
-    gamma = (yay > 0 && std::isfinite(yay) && std::isfinite(yb)) ? yb / yay : 0.0;
-    guess_yb_ = std::isfinite(gamma) ? yb : 0.0;
-    guess_yay_ = yay;
-    k_scale_to64<<<flat_grid(d.n), 256, 0, st_>>>(d.n, gamma, y, x_);
-    tk_.launches++;
-    guess_ = true;
-    return cudaGetLastError();
+    k_learned_update<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, d32_, r32_, p32_, q32_, sc_, part_, ticket_);
+    tk_.launches += 6;
+    cudaMemsetAsync(p32_, 0, 4 * (size_t)n, st_);
+    cudaMemsetAsync(q32_, 0, 4 * (size_t)n, st_);
+    {
+        double init[4] = {1.0, 0.0, 0.0, 0.0};
+        cudaMemcpyAsync(sc_ + S_RHO, init, 8, cudaMemcpyHostToDevice, st_);
+        cudaMemcpyAsync(sc_ + S_ALPHA, init + 1, 8 * 3, cudaMemcpyHostToDevice, st_);
+    }
+    if ((e = read_slots()) != cudaSuccess) return e;
+    const double ry = sc_host_[S_LRY], yay = sc_host_[S_LYAY], rr1 = sc_host_[S_RR];
+    res.learned_steps++;
+    if (first) {
+        guess_yb_ = ry;  // the first step is from r = b: (y, b)
+        guess_yay_ = yay;
+    }
+    // a step that is not finite was not taken (gamma = 0); one that removes less than 10% of ||r|| stalls
+    if (!std::isfinite(rr1) || !(rr1 <= 0.81 * rr)) {
+        stalled = true;
+        res.fallback = true;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t MGSolver::true_relres(bool skip0, double &relres, double &bnorm) {

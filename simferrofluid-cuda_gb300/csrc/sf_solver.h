@@ -58,10 +58,18 @@ struct SolveResult {
     int iters = 0, outer = 0, levels = 0;
     bool converged = false;
     bool breakdown = false;
-    bool fallback = false;      // the supplied initial guess was discarded
-    double guess_relres = -1;   // relative residual of the supplied initial guess
+    bool fallback = false;      // learned form: the network stalled and the plain iteration finished the solve
+    double guess_relres = -1;   // learned form: relative residual after the first learned step (x0 = gamma y)
     double guess_energy = -1;   // its squared A-norm error relative to that of zero
+    int learned_steps = 0;      // learned correction steps applied
     double relres = 0, bnorm = 0;
+};
+
+// The learned form's correction of an inner solve: y = the network's prediction of A^-1 r for an FP32 residual r
+// on the fine level's cells (natural layout), rr = (r, r).
+struct LearnedStep {
+    virtual ~LearnedStep() = default;
+    virtual cudaError_t predict(const float *r, double rr, float *y) = 0;
 };
 
 class DevBuf {
@@ -109,9 +117,13 @@ class MGSolver {
     // ||b - A x|| / ||b|| on the fine FP64 operator; with skip0 row 0 is left out of both norms.
     cudaError_t true_relres(bool skip0, double &relres, double &bnorm);
 
-    // Initial guess x = gamma y, gamma = (y, b) / (y, A y) (mixed form); the next solve(false) starts from it
-    // and discards it if its residual exceeds ||b||.
-    cudaError_t set_guess_scaled(const float *y, double &gamma);
+    // Learned correction steps for the next mixed-form solves (nullptr: none).  At the start of every inner solve
+    // of the iterative refinement -- the first one from r = b -- the network's prediction y of A^-1 r is taken as
+    // the inner solve's first step d = gamma y, gamma = (y, r) / (y, A y) (the multiple that minimises the A-norm
+    // error along y), r -= gamma A y, and the flexible CG continues from there.  A step that reduces ||r|| by less
+    // than 10 % (or is not finite) marks the network as stalled: the rest of the solve runs the plain MGPCG
+    // iteration and SolveResult::fallback is set.
+    void set_learned(LearnedStep *ls) { learned_ = ls; }
 
     // Shift x so that x[0] == 0 (potential gauge).
     cudaError_t shift_to_zero_at_origin();
@@ -134,8 +146,10 @@ class MGSolver {
     std::vector<std::unique_ptr<DevBuf>> bufs_;
     size_t bytes_ = 0;
     bool configured_ = false;
-    bool guess_ = false;
-    double guess_yb_ = 0, guess_yay_ = 0;
+    LearnedStep *learned_ = nullptr;
+    DevBuf lrn_r_, lrn_y_;                      // natural-layout residual and prediction of a learned step
+    double guess_yb_ = 0, guess_yay_ = 0;       // (y, b) and (y, A y) of the first learned step
+    cudaError_t learned_step(double rr, bool first, bool &stalled, SolveResult &res);
     Dims cfg_dims_{0, 0, 0, 0};
     int cfg_prec_ = -1, cfg_levels_ = -1, cfg_cdim_ = -1, cfg_smoother_ = -1;
 
@@ -179,6 +193,13 @@ class MGSolver {
     unsigned *ticket_ = nullptr;
 
     cudaGraphExec_t g_iter64_ = nullptr, g_iter32_ = nullptr;
+    // the mixed form's inner flexible-CG loop as one graph: a conditional WHILE node whose body is one iteration
+    // and k_inner_ctl (loop_ok_ false: the loop is driven from the host, one graph launch per iteration)
+    cudaGraphExec_t g_loop32_ = nullptr;
+    bool loop_ok_ = true;
+    cudaError_t inner_loop(int budget, double tol2, double rr, int &iters);
+    cudaError_t build_loop32();
+    cudaError_t run_iter_prepare();
     long long graph_key_ = -1;
     long long iter_launches64_ = 0, iter_launches32_ = 0;
     Tracker tk_;
@@ -189,7 +210,7 @@ class MGSolver {
     cudaError_t solve64(bool x_is_zero, SolveResult &res);
     cudaError_t solve_mixed(bool x_is_zero, SolveResult &res);
     void enqueue_iter64();
-    void enqueue_iter32();
+    void enqueue_iter32(bool copy_slots = true);
     cudaError_t run_iter(bool mixed);
     cudaError_t read_slots();
 };

@@ -261,6 +261,14 @@ __global__ void __launch_bounds__(256) k_vec_to_split(Dims d, const float *__res
     SPLIT_ROWS_END
 }
 
+// Split copy -> natural FP32 vector.
+__global__ void __launch_bounds__(256) k_split_to_vec(Dims d, const float *__restrict__ s, float *__restrict__ y) {
+    SPLIT_ROWS(d)
+    y[n0] = s[s0];
+    y[n1] = s[s1];
+    SPLIT_ROWS_END
+}
+
 // First refinement step from x = 0 on the split level: r = (float) b in the split layout; slots rr = bb = (b, b).
 __global__ void __launch_bounds__(256) k_cast_rhs_s(Dims d, const double *__restrict__ b, float *__restrict__ r,
                                                     int rr_slot, int bb_slot, double *sc, double *part,

@@ -79,8 +79,8 @@ bool tc_shape_ok(int ci, int co, const Dims &d) {
     return ch && d.nz >= tc::kTileZ && d.ny >= tc::kTileY;
 }
 
-template <int CI, int CO>
-cudaError_t launch_tc(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *w, const float *b, bf16 *y,
+template <int CI, int CO, int EPI>
+cudaError_t launch_tc(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *w, const float *b, void *y,
                       int *err) {
     auto enc = tensor_map_encoder();
     if (!enc || !aligned16(x) || !aligned16(w) || !aligned16(y)) return cudaErrorInvalidValue;
@@ -101,20 +101,22 @@ cudaError_t launch_tc(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
     using L = tc::Layout<CI, CO>;
-    cudaError_t e = cudaFuncSetAttribute(tc::k_conv_tc<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(tc::k_conv_tc<CI, CO, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)L::kSmemBytes);
     if (e != cudaSuccess) return e;
     const long long tiles = (long long)((d.nz + tc::kTileZ - 1) / tc::kTileZ) * ((d.ny + tc::kTileY - 1) / tc::kTileY) *
                             d.nx;
     if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
-    tc::k_conv_tc<CI, CO><<<(unsigned)tiles, 128, L::kSmemBytes, st>>>(mx, mw, d, b, y, err);
+    tc::k_conv_tc<CI, CO, EPI><<<(unsigned)tiles, 128, L::kSmemBytes, st>>>(mx, mw, d, b, y, err);
     return cudaGetLastError();
 }
 
-cudaError_t tc_dispatch(cudaStream_t st, int ci, int co, const Dims &d, const bf16 *x, const bf16 *w, const float *b,
-                        bf16 *y, int *err) {
-#define CASE(A, B) \
-    if (ci == A && co == B) return launch_tc<A, B>(st, d, x, w, b, y, err);
+// epi 0: forward (bias, ReLU, BF16 y); epi 1: input gradient (FP32 y, no bias)
+cudaError_t tc_dispatch(cudaStream_t st, int ci, int co, int epi, const Dims &d, const bf16 *x, const bf16 *w,
+                        const float *b, void *y, int *err) {
+#define CASE(A, B)                                                                              \
+    if (ci == A && co == B)                                                                     \
+        return epi == 0 ? launch_tc<A, B, 0>(st, d, x, w, b, y, err) : launch_tc<A, B, 1>(st, d, x, w, b, y, err);
     CASE(16, 16) CASE(16, 32) CASE(32, 16) CASE(32, 32) CASE(32, 64) CASE(64, 32) CASE(64, 64)
 #undef CASE
     return cudaErrorInvalidValue;
@@ -267,7 +269,7 @@ cudaError_t UNet::ensure(const Dims &d) {
 
 void UNet::conv_fwd(const ConvLayer &L, const Dims &d, const bf16 *x, bf16 *y) {
     if (mode_ == 1 && L.taps == 27 && tc_shape_ok(L.cin, L.cout, d)) {
-        cudaError_t e = tc_dispatch(st_, L.cin, L.cout, d, x, wb_ + L.wbf, p_ + L.boff, y, err_);
+        cudaError_t e = tc_dispatch(st_, L.cin, L.cout, 0, d, x, wb_ + L.wbf, p_ + L.boff, y, err_);
         if (e == cudaSuccess) {
             tc_launches_++;
             return;
@@ -336,7 +338,17 @@ void UNet::conv_bwd(const ConvLayer &L, const Dims &d, const bf16 *x, const bf16
     k_reduce_chunks<<<flat_blocks(mw), 256, 0, st_>>>(wpart_, chunks, mw, g_ + L.woff);
     k_bias_grad<<<chunks, 64, 0, st_>>>(d, dy, L.cout, (int)vchunk, hpart_);
     k_reduce_chunks<<<1, 64, 0, st_>>>(hpart_, chunks, L.cout, g_ + L.boff);
-    if (dx) conv_dispatch(st_, L.cout, L.cin, 1, d, dy, wt_ + L.wbf, nullptr, dx, L.taps);
+    if (!dx) return;
+    // input gradient: the forward convolution with the mirrored, transposed weights (FP32 out, no bias)
+    if (mode_ == 1 && L.taps == 27 && tc_shape_ok(L.cout, L.cin, d)) {
+        const cudaError_t e = tc_dispatch(st_, L.cout, L.cin, 1, d, dy, wt_ + L.wbf, nullptr, dx, err_);
+        if (e == cudaSuccess) {
+            tc_launches_++;
+            return;
+        }
+        last_error = std::string("tcgen05 convolution not launched: ") + cudaGetErrorString(e);
+    }
+    conv_dispatch(st_, L.cout, L.cin, 1, d, dy, wt_ + L.wbf, nullptr, dx, L.taps);
 }
 
 cudaError_t UNet::backward(const Dims &d, const float *dout) {
@@ -384,6 +396,7 @@ cudaError_t UNet::train_step(const Dims &d, const bf16 *feat, const float *targe
     k_cos_grad<<<flat_blocks(d.n), 256, 0, st_>>>(d.n, out_, target, dots_, dout_);
     e = backward(d, dout_);
     if (e != cudaSuccess) return e;
+    if (mode_ == 1 && (e = check_device_errors()) != cudaSuccess) return e;
     step_++;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f - powf(b1, (float)step_), c2 = 1.f - powf(b2, (float)step_);
@@ -446,9 +459,20 @@ cudaError_t UNet::features(const Dims &d, const Coef<double> &cf, const double *
     cudaError_t e = cudaStreamSynchronize(st_);
     if (e != cudaSuccess) return e;
     const double cnt = dots_host_[1] > 0 ? dots_host_[1] : 1.0;
+    active_ = dots_host_[1];
     const double rms = std::sqrt(dots_host_[0] / cnt);
     const double inv = rms > 0 ? 1.0 / rms : 0.0;
     k_features<<<flat_blocks(d.n), 256, 0, st_>>>(d, cf, b, inv, feat);
+    return cudaGetLastError();
+}
+
+__global__ void k_feat_rhs(long long n, const float *__restrict__ r, float inv_rms, bf16 *__restrict__ f) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        f[c * 16] = __float2bfloat16_rn(r[c] * inv_rms);
+}
+
+cudaError_t UNet::set_rhs_channel(const Dims &d, const float *r, double inv_rms, bf16 *feat) {
+    k_feat_rhs<<<flat_blocks(d.n), 256, 0, st_>>>(d.n, r, (float)inv_rms, feat);
     return cudaGetLastError();
 }
 

@@ -45,6 +45,10 @@ class UNet {
 
     // the 16 input channels of a system in face-coefficient form (FP64 fine level) with rhs b
     cudaError_t features(const Dims &d, const Coef<double> &cf, const double *b, __nv_bfloat16 *feat);
+    // active cells (D > 0) counted by the last features()
+    double active_cells() const { return active_; }
+    // channel 0 of existing features set to r * inv_rms (FP32 r on the cells), the other channels unchanged
+    cudaError_t set_rhs_channel(const Dims &d, const float *r, double inv_rms, __nv_bfloat16 *feat);
     float *output() { return out_; }
     // convolution kernels of the forward pass: 0 warp-level MMA (mma.sync), 1 tcgen05 + TMA
     void set_mode(int m) { mode_ = m; }
@@ -83,6 +87,7 @@ class UNet {
     double *dots_ = nullptr, *dots_host_ = nullptr, *redpart_ = nullptr;
     long long wpart_elems_ = 0;
     int mode_ = 0;
+    double active_ = 0;
     int *err_ = nullptr;
     long long tc_launches_ = 0;
 };

@@ -10,6 +10,7 @@ Scenes:
 * ``pool_sphere`` -- pool of depth 0.2 united (min) with a sphere of radius 0.15 at (0.5, 0.55, 0.5); dipole
                     applied field of moment (0, 1, 0) at (0.5, -0.3, 0.5) with the reference's dipole formula
                     (demo/SimBuilder.cpp:80-98) without its time ramp; velocity N(0, 0.5^2).
+* ``random_scene`` -- the learned form's distribution: pool of random depth with 1-8 random spheres.
 """
 from __future__ import annotations
 
@@ -134,6 +135,28 @@ def pool_sphere(n, seed: int = 0, chi: float = 2.0, depth: float = 0.2, centre=(
     frac = box_fractions(g, 0) if with_fractions else None
     return Scene("pool_sphere", g, phi, vel, frac, dipole_field(g, dipole_pos, dipole_orient), chi, 2 * g.spacing,
                  dict(seed=seed, depth=depth, centre=centre, radius=radius))
+
+
+def random_scene(n, seed: int = 0, with_fractions=True) -> Scene:
+    """The learned form's scene distribution: a pool of depth U[0.1, 0.3] united with 1-8 spheres of radius
+    U[0.05, 0.25] at uniform centres, chi U[0.5, 3], a uniform applied field of random direction and magnitude
+    U[0.5, 2], velocity N(0, 0.5^2), walls on the grid faces."""
+    g = unit_grid(n)
+    rng = np.random.default_rng(seed)
+    xs, ys, zs = (cell_centres(g, a) for a in range(3))
+    X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
+    phi = Y - rng.uniform(0.1, 0.3)
+    for _ in range(int(rng.integers(1, 9))):
+        cx, cy, cz = rng.uniform(0, 1, 3)
+        r = rng.uniform(0.05, 0.25)
+        phi = np.minimum(phi, np.sqrt((X - cx) ** 2 + (Y - cy) ** 2 + (Z - cz) ** 2) - r)
+    chi = float(rng.uniform(0.5, 3.0))
+    d = rng.normal(size=3)
+    d = d / np.linalg.norm(d) * rng.uniform(0.5, 2.0)
+    vel = [rng.normal(0.0, 0.5, g.face_shape(a)) for a in range(3)]
+    frac = box_fractions(g, 0) if with_fractions else None
+    return Scene("random", g, np.ascontiguousarray(phi), vel, frac, uniform_field(g, tuple(d)), chi, 2 * g.spacing,
+                 dict(seed=seed))
 
 
 def divergence(g: StaggeredGrid, vel, frac=None):

@@ -39,7 +39,7 @@ def test_library_exports_every_declared_symbol():
 def test_abi_version_and_defaults():
     sf = pkg()
     lib = sf.load_library()
-    assert lib.sf_abi_version() == 1
+    assert lib.sf_abi_version() == 2
     o = sf.options("pressure")
     assert o.tol == 1e-8 and o.precision == sf.SF_PREC_FP64 and o.warm_start == 1
     m = sf.options("magnetic", precision="mixed")

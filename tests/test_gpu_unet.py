@@ -84,7 +84,7 @@ def test_unet_training_reduces_loss(sfpkg, gpu_ctx, ref):
 
 def test_learned_solve_converges_and_falls_back(sfpkg, oracle, gpu_ctx, ref):
     """The learned form reaches the same tolerance and answer as the plain method; a network whose
-    prediction is garbage is discarded (SF_STALLED_FALLBACK) and the plain iteration finishes the solve."""
+    prediction is garbage takes no step (SF_STALLED_FALLBACK) and the plain iteration finishes the solve."""
     sc = scenes().pool(32, seed=4)
     og = oracle_grid(oracle, sc.grid)
     u_or, p_or, _ = oracle.pressure_project(og, sc.phi, sc.frac, sc.vel, tol=1e-13)
@@ -97,7 +97,7 @@ def test_learned_solve_converges_and_falls_back(sfpkg, oracle, gpu_ctx, ref):
     st = P.project(v, sc.phi, sc.frac, opts=sfpkg.options("pressure", precision="learned"))
     assert st["converged"] == 1 and st["rel_residual"] <= 1e-8 * 1.01
     assert rel_l2(P.pressure[liq], p_or[liq]) <= 1e-5
-    assert st["guess_rel_residual"] >= 0
+    assert st["guess_rel_residual"] >= 0 and st["learned_steps"] >= 1
     assert 0.0 <= st["guess_energy_ratio"] <= 1.0 + 1e-9  # gamma scaling: never worse than zero in A-norm
     # garbage network: huge weights make the prediction overflow to non-finite values -> discarded
     flat = ref.flatten(ref.init_params(16, seed=1))
@@ -107,8 +107,43 @@ def test_learned_solve_converges_and_falls_back(sfpkg, oracle, gpu_ctx, ref):
     st = P.project(v, sc.phi, sc.frac, opts=sfpkg.options("pressure", precision="learned"))
     assert P.status == sfpkg._abi.SF_STALLED_FALLBACK
     assert st["converged"] == 1 and rel_l2(P.pressure[liq], p_or[liq]) <= 1e-5
+    assert st["learned_steps"] == 1  # stalled after its first step: the rest is the plain iteration
     gpu_ctx.set_network(None)
     net.close()
+
+
+def test_trained_network_gain(sfpkg, gpu_ctx, ref):
+    """The trained weights (weights/unet.f32) against the same network untrained, on unseen seeded scenes of
+    the training distribution (pool of depth U[0.1, 0.3] with spheres, chi U[0.5, 3]) at 64^3: the first learned
+    step's A-norm error relative to zero (guess_energy_ratio) is lower with the trained weights on the
+    potential, and every learned solve reaches the tolerance.  The measured figures are printed."""
+    import os
+    S = scenes()
+    wpath = os.path.join(os.path.dirname(sfpkg.__file__), "weights", "unet.f32")
+    trained = sfpkg.Network(gpu_ctx)
+    trained.load(wpath)
+    untrained = sfpkg.Network(gpu_ctx)
+    untrained.set_params(ref.flatten(ref.init_params(16, seed=5)))
+    rows = []
+    for seed in (101, 102, 103):
+        sc = S.random_scene(64, seed=seed)
+        for name, net in (("trained", trained), ("untrained", untrained)):
+            gpu_ctx.set_network(net)
+            M = sfpkg.MagneticField(sc.grid, sc.chi, sc.band_width, gpu_ctx)
+            sm = M.solve(sc.phi, sc.hext, opts=sfpkg.options("magnetic", precision="learned", warm_start=0))
+            P = sfpkg.Pressure(sc.grid, gpu_ctx)
+            sp = P.project([a.copy() for a in sc.vel], sc.phi, sc.frac,
+                           opts=sfpkg.options("pressure", precision="learned"))
+            assert sm["converged"] == 1 and sp["converged"] == 1
+            rows.append((seed, name, sm["guess_energy_ratio"], sm["iters"], sp["guess_energy_ratio"], sp["iters"]))
+    gpu_ctx.set_network(None)
+    for r in rows:
+        print("seed %d %-9s potential energy ratio %.4f iters %d | pressure energy ratio %.4f iters %d" % r)
+    tr = np.mean([r[2] for r in rows if r[1] == "trained"])
+    un = np.mean([r[2] for r in rows if r[1] == "untrained"])
+    assert tr < un and tr < 1.0, (tr, un)
+    trained.close()
+    untrained.close()
 
 
 def test_network_outlives_context(sfpkg):

@@ -38,3 +38,44 @@ def test_tcgen05_forward_matches_mma(sfpkg, gpu_ctx, shape):
         out_ref, _ = ref.forward_bf16(P, x)
         assert rel_l2(b, out_ref.ravel()) <= 1e-2
     net.close()
+
+
+@pytest.mark.parametrize("shape", [(6, 12, 40), (9, 8, 64)])
+def test_tcgen05_gradients_match_mma(sfpkg, gpu_ctx, shape):
+    """Training with the tcgen05 kernels: the input gradients of every 3x3x3 layer run on tcgen05 (the forward
+    convolution with the mirrored, transposed weights, FP32 out); the parameter gradients agree with the
+    warp-MMA path's (relative L2 2e-2: BF16 activations, FP32 sums in different orders)."""
+    import torch
+    from oracle import unet_ref as ref
+    g = sfpkg.StaggeredGrid.from_origin(1.0 / shape[0], shape)
+    P = ref.init_params(16, seed=12)
+    rng = np.random.default_rng(4)
+    x = ref.bf16(rng.standard_normal(shape + (16,)))
+    net = sfpkg.Network(gpu_ctx)
+    net.set_params(ref.flatten(P))
+    feat = torch.from_numpy(x).to(torch.bfloat16).cuda().contiguous()
+    dout = torch.from_numpy(rng.standard_normal(int(np.prod(shape))).astype(np.float32)).cuda()
+    out = torch.zeros(g.num_cells, dtype=torch.float32, device="cuda")
+    net.set_mode("mma")
+    net.forward(g, feat, out)
+    g0 = net.gradients(g, feat, dout)
+    net.set_mode("tcgen05")
+    before = net.tc_launches()
+    net.forward(g, feat, out)
+    g1 = net.gradients(g, feat, dout)
+    assert net.tc_launches() - before > 8  # forward and input-gradient convolutions on tcgen05
+    assert np.isfinite(g1).all()
+    assert rel_l2(g1, g0) <= 2e-2, rel_l2(g1, g0)
+    # one Adam step in each mode from the same parameters gives close losses and parameters
+    tgt = torch.from_numpy(rng.standard_normal(int(np.prod(shape))).astype(np.float32)).cuda()
+    net.set_params(ref.flatten(P))
+    net.set_mode("mma")
+    l0 = net.train_step(g, feat, tgt, 1e-3)
+    p0 = net.get_params()
+    net.set_params(ref.flatten(P))
+    net.set_mode("tcgen05")
+    l1 = net.train_step(g, feat, tgt, 1e-3)
+    p1 = net.get_params()
+    assert abs(l1 - l0) <= 1e-3 * max(abs(l0), 1e-6) + 1e-6
+    assert rel_l2(p1, p0) <= 1e-3
+    net.close()
