@@ -90,7 +90,10 @@ typedef struct {
     int coarse_tail;     /* mixed form, levels of at most 65,536 cells: 0 (default) one launch of a thread-block
                             cluster of 16 CTAs where the device runs it, else 8; 8 or 16 that cluster size; 1 separate
                             kernels.  All give the same results. */
-    int reserved[3];
+    int full_sweeps;     /* FP64 form: 1 smooths and iterates over every row of the grid; 0 (default) skips the rows
+                            without an active cell (air in the pressure system) on every level, as the mixed form
+                            does.  Both give the same answer. */
+    int reserved[2];
 } sf_solve_opts;
 
 typedef struct {
@@ -282,6 +285,13 @@ SF_EXPORT sf_status sf_reinitialize_dev(void *ctx, const sf_grid *g, double *phi
 
 /* Forget the magnetic warm start (MagneticField ctor zeroes m_Sol, core/MagneticField.cpp:26). */
 SF_EXPORT sf_status sf_magnetic_reset(void *ctx);
+
+/* ----- self-test of the bounded waits (no counterpart in the reference) ------------------------------------
+ * The TMA-staged kernels wait on mbarriers with a time limit, after which they record an error and return instead
+ * of hanging.  This runs that wait where it cannot succeed: one CTA arms an mbarrier for bytes that no copy
+ * delivers (nothing is in flight) and waits at most limit_ms (0 < limit_ms <= 10000); *timed_out = 1 when the
+ * wait gave up, *waited_ms (nullable) the time it waited.  The context stays usable afterwards. */
+SF_EXPORT sf_status sf_selftest_bounded_wait(void *ctx, double limit_ms, int *timed_out, double *waited_ms);
 
 /* ----- resident inputs --------------------------------------------------------------------------------------
  * The reference's simulation keeps its collider and level set in memory across calls: the collider's face

@@ -29,7 +29,7 @@ EXPORTED = [
     "sf_create", "sf_destroy", "sf_status_string", "sf_last_error", "sf_abi_version", "sf_default_opts",
     "sf_device_bytes", "sf_pressure_project", "sf_pressure_project_dev", "sf_pressure_reproject",
     "sf_pressure_reproject_dev", "sf_magnetic_solve", "sf_magnetic_solve_dev", "sf_magnetic_reset",
-    "sf_collider_upload", "sf_levelset_upload",
+    "sf_collider_upload", "sf_levelset_upload", "sf_selftest_bounded_wait",
     "sf_collider_box_fractions", "sf_collider_face_fractions",
     "sf_unet_create", "sf_unet_destroy", "sf_unet_num_params", "sf_unet_set_params", "sf_unet_get_params",
     "sf_unet_forward_dev", "sf_unet_backward_dev", "sf_unet_train_step_dev", "sf_set_network",
@@ -52,7 +52,7 @@ class sf_solve_opts(C.Structure):
                 ("coarse_dim", C.c_int), ("warm_start", C.c_int), ("use_graph", C.c_int),
                 ("check_every", C.c_int), ("report_ref_residual", C.c_int), ("inner_tol", C.c_double),
                 ("profile", C.c_int), ("smoother", C.c_int), ("coarse_pre", C.c_int), ("coarse_post", C.c_int),
-                ("coarse_tail", C.c_int), ("reserved", C.c_int * 3)]
+                ("coarse_tail", C.c_int), ("full_sweeps", C.c_int), ("reserved", C.c_int * 2)]
 
 
 class sf_solve_stats(C.Structure):
@@ -114,6 +114,8 @@ def load(path: str | None = None):
     L.sf_collider_upload.restype = C.c_int
     L.sf_levelset_upload.argtypes = [V, G, V]
     L.sf_levelset_upload.restype = C.c_int
+    L.sf_selftest_bounded_wait.argtypes = [V, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    L.sf_selftest_bounded_wait.restype = C.c_int
     for name in ("sf_extrapolate_velocity", "sf_extrapolate_velocity_dev"):
         f = getattr(L, name)
         f.argtypes = [V, G, _P3, V, _P3, C.c_double, C.c_int]

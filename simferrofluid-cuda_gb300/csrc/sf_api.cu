@@ -97,6 +97,7 @@ SolverParams params_from(const sf_solve_opts *o, int which) {
     p.profile = o->profile != 0;
     p.smoother = o->smoother;
     p.tail = o->coarse_tail;
+    p.full_sweeps = o->full_sweeps != 0;
     return p;
 }
 
@@ -886,6 +887,22 @@ sf_status sf_magnetic_reset(void *ctx) {
     Ctx *c = C(ctx);
     if (!c) return SF_BAD_ARG;
     c->mag_has_x = false;
+    return SF_OK;
+}
+
+sf_status sf_selftest_bounded_wait(void *ctx, double limit_ms, int *timed_out, double *waited_ms) {
+    Ctx *c = C(ctx);
+    if (!c) return SF_BAD_ARG;
+    if (!(limit_ms > 0) || limit_ms > 10000 || !timed_out) return fail(c, SF_BAD_ARG, "limit_ms in (0, 10000]");
+    CK(cudaSetDevice(c->device));
+    CK(c->cells.ensure(16));
+    auto *d = (unsigned long long *)c->cells.get();
+    CK(selftest_bounded_wait(c->st, (unsigned long long)(limit_ms * 1e6), d));
+    unsigned long long h[2] = {0, 0};
+    CK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    *timed_out = (int)h[0];
+    if (waited_ms) *waited_ms = (double)h[1] * 1e-6;
     return SF_OK;
 }
 

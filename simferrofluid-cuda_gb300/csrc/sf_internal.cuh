@@ -287,6 +287,7 @@ enum Slot {
     S_BUDGET,
     S_RPREV,
     S_SLOW,
+    S_STAG,    // 1: the loop ends on FP32 stagnation (mixed form), 0: no stagnation test (FP64 form)
     S_NSLOTS = 32
 };
 

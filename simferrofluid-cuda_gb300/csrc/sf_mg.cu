@@ -966,10 +966,12 @@ __global__ void k_to16(long long n, Coef<double> f, Coef<__half> o) {
 // FP64 from there on.
 template <class T, class C>
 __global__ void __launch_bounds__(256) k_apply_dot(Dims d, int xpb, Coef<C> cf, const T *__restrict__ p,
-                                                   T *__restrict__ q, double *sc, double *part, unsigned *ticket) {
+                                                   T *__restrict__ q, double *sc, double *part, unsigned *ticket,
+                                                   const uint8_t *__restrict__ rows) {
     pdl_entry();
     T acc = 0;
     TILE_BLOCK(d, xpb)
+    if (!row_on(rows, d, i, j)) continue;  // q stays zero there
     T sa;
     T s = nbsum<T, C, sizeof(C) != 8>(d, cf, p, i, j, k, c, sa);
     T D = (T)diag_of<C>(cf, c, (typename Acc<C>::T)sa);
@@ -1087,25 +1089,38 @@ static void apply_dot32(cudaStream_t st, const Dims &d, const Coef<float> &cf, c
         return;
     }
     const dim3 tg = tile_grid3(d, xpb);
-    launch_pdl(k_apply_dot<float, float>, tg, dim3(32, 8), st, d, xpb, cf, p, q, sc, part, ticket);
+    launch_pdl(k_apply_dot<float, float>, tg, dim3(32, 8), st, d, xpb, cf, p, q, sc, part, ticket,
+               (const uint8_t *)nullptr);
 }
 
 #include "sf_split.cuh"
 #include "sf_tail.cuh"
 
+// Vector kernels of the natural layout walk rows (i, j) of nz cells, one warp per row and 8 rows per block;
+// rows whose flag is 0 (no active cell; rows == nullptr: every row active) are skipped, their entries being
+// zero in every vector.
+#define VEC_ROWS(d, rows)                                                                                     \
+    for (long long row_ = blockIdx.x * 8LL + threadIdx.y, nrows_ = (long long)(d).nx * (d).ny; row_ < nrows_; \
+         row_ += (long long)gridDim.x * 8) {                                                                  \
+        if ((rows) && !(rows)[row_]) continue;                                                                \
+        for (int k_ = threadIdx.x; k_ < (d).nz; k_ += 32) {                                                   \
+            const long long c = row_ * (d).nz + k_;
+#define VEC_ROWS_END \
+    }                \
+    }
+
 // rho_new = (r, z), zq = (z, q); beta = flexible ? -alpha*zq/rho : rho_new/rho; rho = rho_new
 template <class T>
-__global__ void __launch_bounds__(256) k_dot_rz(long long n, const T *__restrict__ r, const T *__restrict__ z,
-                                                const T *__restrict__ q, int flexible, double *sc, double *part,
-                                                unsigned *ticket) {
+__global__ void __launch_bounds__(256) k_dot_rz(Dims d, const uint8_t *__restrict__ rows, const T *__restrict__ r,
+                                                const T *__restrict__ z, const T *__restrict__ q, int flexible,
+                                                double *sc, double *part, unsigned *ticket) {
     pdl_entry();
     T a0 = 0, a1 = 0;
-    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
-    for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
-        const T zc = z[c];
-        a0 += r[c] * zc;
-        a1 += zc * q[c];
-    }
+    VEC_ROWS(d, rows)
+    const T zc = z[c];
+    a0 += r[c] * zc;
+    a1 += zc * q[c];
+    VEC_ROWS_END
     T v[2] = {a0, a1};
     double tot[2];
     if (grid_reduce<2>(v, part, ticket, tot)) {
@@ -1120,29 +1135,29 @@ __global__ void __launch_bounds__(256) k_dot_rz(long long n, const T *__restrict
 }
 
 template <class T>
-__global__ void __launch_bounds__(256) k_xpby(long long n, const T *__restrict__ z, T *__restrict__ p,
-                                              const double *sc) {
+__global__ void __launch_bounds__(256) k_xpby(Dims d, const uint8_t *__restrict__ rows, const T *__restrict__ z,
+                                              T *__restrict__ p, const double *sc) {
     pdl_entry();
     const T beta = (T)sc[S_BETA];
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
-        p[c] = z[c] + beta * p[c];
+    VEC_ROWS(d, rows)
+    p[c] = z[c] + beta * p[c];
+    VEC_ROWS_END
 }
 
 // x += alpha p ; r -= alpha q ; slot RR = (r, r)
 template <class T>
-__global__ void __launch_bounds__(256) k_update(long long n, T *__restrict__ x, T *__restrict__ r,
-                                                const T *__restrict__ p, const T *__restrict__ q, double *sc,
-                                                double *part, unsigned *ticket) {
+__global__ void __launch_bounds__(256) k_update(Dims d, const uint8_t *__restrict__ rows, T *__restrict__ x,
+                                                T *__restrict__ r, const T *__restrict__ p, const T *__restrict__ q,
+                                                double *sc, double *part, unsigned *ticket) {
     pdl_entry();
     const T alpha = (T)sc[S_ALPHA];
     T acc = 0;
-    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
-    for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
-        x[c] += alpha * p[c];
-        T rc = r[c] - alpha * q[c];
-        r[c] = rc;
-        acc += rc * rc;
-    }
+    VEC_ROWS(d, rows)
+    x[c] += alpha * p[c];
+    T rc = r[c] - alpha * q[c];
+    r[c] = rc;
+    acc += rc * rc;
+    VEC_ROWS_END
     T v[1] = {acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) sc[S_RR] = tot[0];
@@ -1195,6 +1210,39 @@ __global__ void __launch_bounds__(256) k_cast_rhs(long long n, const double *__r
     if (grid_reduce<1>(v, part, ticket, tot)) {
         sc[rr_slot] = tot[0];
         sc[bb_slot] = tot[0];
+    }
+}
+
+// Self-test of the bounded waits: one CTA arms an mbarrier for bytes that no copy will deliver (nothing is in
+// flight), waits for it with the same bounded wait as the TMA kernels, and records the outcome: out[0] = 1 when the
+// wait gave up, 0 if it completed; out[1] = the nanoseconds waited.
+__global__ void k_selftest_bounded_wait(unsigned long long limit_ns, unsigned long long *out) {
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t b = tc::smem_u32(&bar);
+    if (threadIdx.x == 0) {
+        tc::mbar_init(b, 1);
+        tc::mbar_fence_init();
+        tc::mbar_expect_tx(b, 16);  // 16 bytes that never arrive
+        const uint64_t t0 = tc::global_ns();
+        const bool done = tc::mbar_wait_ns(b, 0, limit_ns);
+        out[0] = done ? 0ull : 1ull;
+        out[1] = tc::global_ns() - t0;
+    }
+}
+
+cudaError_t selftest_bounded_wait(cudaStream_t st, unsigned long long limit_ns, unsigned long long *out) {
+    k_selftest_bounded_wait<<<1, 32, 0, st>>>(limit_ns, out);
+    return cudaGetLastError();
+}
+
+// rows[row] = 1 when a cell of row (i, j) has D > 0, else 0 (one warp per row)
+__global__ void __launch_bounds__(256) k_rows_from_diag(Dims d, const double *__restrict__ D, uint8_t *__restrict__ rows) {
+    for (long long row = blockIdx.x * 8LL + threadIdx.y, nr = (long long)d.nx * d.ny; row < nr;
+         row += (long long)gridDim.x * 8) {
+        bool on = false;
+        for (int k = threadIdx.x; k < d.nz; k += 32) on |= D[row * d.nz + k] > 0;
+        on = __any_sync(0xffffffffu, on);
+        if (threadIdx.x == 0) rows[row] = on ? 1 : 0;
     }
 }
 
@@ -1641,7 +1689,8 @@ void MGSolver::destroy_graphs() {
     if (g_iter64_) cudaGraphExecDestroy(g_iter64_);
     if (g_iter32_) cudaGraphExecDestroy(g_iter32_);
     if (g_loop32_) cudaGraphExecDestroy(g_loop32_);
-    g_iter64_ = g_iter32_ = g_loop32_ = nullptr;
+    if (g_loop64_) cudaGraphExecDestroy(g_loop64_);
+    g_iter64_ = g_iter32_ = g_loop32_ = g_loop64_ = nullptr;
     graph_key_ = -1;
 }
 
@@ -1685,10 +1734,12 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
                         d.ny < 65536 &&
                         (long long)(((d.nz >> 1) + 127) / 128) * 2 * ((d.ny + 7) / 8) <= kApplyBlocks;
     const bool fp16copy = p.smoother == 2 || p.smoother == 3;
+    // FP64 form: row flags on every level unless every row is swept (the fused one-pass sweep has none)
+    const bool rows64 = p.precision == 0 && !p.full_sweeps && p.smoother != 1;
     const bool same = configured_ && cfg_dims_.nx == d.nx && cfg_dims_.ny == d.ny && cfg_dims_.nz == d.nz &&
                       cfg_prec_ == p.precision && cfg_levels_ == (int)dims.size() && cfg_cdim_ == cdim &&
-                      (p.precision == 0 ||
-                       ((cfg_smoother_ == 2 || cfg_smoother_ == 3) == fp16copy && cfg_split_ == split0));
+                      (p.precision == 0 ? rows64_ == rows64
+                                        : ((cfg_smoother_ == 2 || cfg_smoother_ == 3) == fp16copy && cfg_split_ == split0));
     prm_ = p;
     if (same) {
         plan_tail();
@@ -1697,6 +1748,7 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
     destroy_graphs();
     free_all();
     lev_dims_ = dims;
+    rows64_ = rows64;
     const int L = (int)dims.size();
     const long long n = d.n;
     auto A = [&](size_t bytes) -> void * { return alloc(bytes); };
@@ -1736,6 +1788,8 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
         z_ = (double *)chk(A(8 * n));
         p_ = (double *)chk(A(8 * n));
         q_ = (double *)chk(A(8 * n));
+        rows_.assign(rows64 ? L : 0, nullptr);
+        for (int l = 0; l < (int)rows_.size(); l++) rows_[l] = (uint8_t *)chk(A((size_t)dims[l].nx * dims[l].ny));
     } else {
         c32_.ax = (float *)chk(A(4 * n));
         c32_.ay = (float *)chk(A(4 * n));
@@ -1882,6 +1936,24 @@ cudaError_t MGSolver::build_hierarchy() {
         for (int l = 1; l < L; l++)
             k_coarsen<double, double><<<grid_cells(lev_dims_[l]), blk2(), 0, st_>>>(lev_dims_[l - 1], c64_[l - 1],
                                                                                     lev_dims_[l], c64_[l]);
+        if (rows64_) {
+            // row flags from the fine diagonal (D > 0), coarse rows active where a fine row is; the vectors of
+            // inactive rows must be zero and stay so
+            const Dims &d0 = lev_dims_[0];
+            const long long nr0 = (long long)d0.nx * d0.ny;
+            k_rows_from_diag<<<(int)std::min<long long>((nr0 + 7) / 8, 152 * 16), dim3(32, 8), 0, st_>>>(
+                d0, c64_[0].D, rows_[0]);
+            cudaMemsetAsync(z_, 0, 8 * (size_t)d0.n, st_);
+            for (int l = 1; l < L; l++) {
+                const Dims &dl = lev_dims_[l];
+                const long long nr = (long long)dl.nx * dl.ny;
+                k_rows_coarsen<<<(int)std::min<long long>((nr + 255) / 256, 152 * 8), 256, 0, st_>>>(
+                    lev_dims_[l - 1], rows_[l - 1], dl, rows_[l]);
+                cudaMemsetAsync(x64_[l], 0, 8 * (size_t)dl.n, st_);
+                cudaMemsetAsync(b64_[l], 0, 8 * (size_t)dl.n, st_);
+            }
+            tk_.launches += L;
+        }
     } else {
         if (split0_) {
             if (!copies_written_)
@@ -1962,23 +2034,27 @@ cudaError_t MGSolver::build_hierarchy() {
     return cudaGetLastError();
 }
 
-void MGSolver::enqueue_iter64() {
+void MGSolver::enqueue_iter64(bool copy_slots) {
     const Dims &d = lev_dims_[0];
     const long long n = d.n;
     int xpb;
     const dim3 tg = tile_grid3(d, xpb);
     const long long l0 = tk_.launches;
+    // with row flags (rows64_): the smoothers, transfers and vector kernels skip rows without an active cell
+    const RowSets rs{&rows_, {nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}, {nullptr, nullptr}, nullptr,
+                     {nullptr, nullptr}, {nullptr, nullptr}};
+    const uint8_t *r0 = rows64_ ? rows_[0] : nullptr;
     vcycle<double, double, double, double>(st_, tk_, lev_dims_, c64_[0], c64_[0], c64_, z_, r_, x64_, b64_,
                                            prm_.smoother == 1 ? t64_ : std::vector<double *>(t64_.size(), nullptr),
-                                           prm_);
-    launch_pdl(k_dot_rz<double>, kMaxRedBlocks, dim3(32, 8), st_, n, r_, z_, q_, prm_.flexible ? 1 : 0, sc_, part_,
-                                                              ticket_);
-    launch_pdl(k_xpby<double>, flat_grid(n), 256, st_, n, z_, p_, sc_);
-    launch_pdl(k_apply_dot<double, double>, tg, dim3(32, 8), st_, d, xpb, c64_[0], p_, q_, sc_, part_, ticket_);
-    launch_pdl(k_update<double>, kMaxRedBlocks, dim3(32, 8), st_, n, x_, r_, p_, q_, sc_, part_, ticket_);
+                                           prm_, false, rows64_ ? &rs : nullptr);
+    launch_pdl(k_dot_rz<double>, kMaxRedBlocks, dim3(32, 8), st_, d, r0, r_, z_, q_, prm_.flexible ? 1 : 0, sc_,
+               part_, ticket_);
+    launch_pdl(k_xpby<double>, kMaxRedBlocks, dim3(32, 8), st_, d, r0, z_, p_, sc_);
+    launch_pdl(k_apply_dot<double, double>, tg, dim3(32, 8), st_, d, xpb, c64_[0], p_, q_, sc_, part_, ticket_, r0);
+    launch_pdl(k_update<double>, kMaxRedBlocks, dim3(32, 8), st_, d, r0, x_, r_, p_, q_, sc_, part_, ticket_);
     tk_.launches += 4;
     iter_launches64_ = tk_.launches - l0;
-    cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
+    if (copy_slots) cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
 }
 
 void MGSolver::enqueue_iter32(bool copy_slots) {
@@ -2012,10 +2088,11 @@ void MGSolver::enqueue_iter32(bool copy_slots) {
     else
         vcycle<float, float, __half, float>(st_, tk_, lev_dims_, c32_, c32_, c16_, z32_, ri32_, x32_, b32_, ts,
                                             prm_, false, nullptr, tail_lt_, tail_smem_, tail_nc_, tail_op_.data());
-    launch_pdl(k_dot_rz<float>, kMaxRedBlocks, dim3(32, 8), st_, n, ri32_, z32_, q32_, 1, sc_, part_, ticket_);
-    launch_pdl(k_xpby<float>, flat_grid(n), 256, st_, n, z32_, p32_, sc_);
+    const uint8_t *nr = nullptr;
+    launch_pdl(k_dot_rz<float>, kMaxRedBlocks, dim3(32, 8), st_, d, nr, ri32_, z32_, q32_, 1, sc_, part_, ticket_);
+    launch_pdl(k_xpby<float>, kMaxRedBlocks, dim3(32, 8), st_, d, nr, z32_, p32_, sc_);
     apply_dot32(st_, d, c32_, p32_, q32_, sc_, part_, ticket_);
-    launch_pdl(k_update<float>, kMaxRedBlocks, dim3(32, 8), st_, n, d32_, ri32_, p32_, q32_, sc_, part_, ticket_);
+    launch_pdl(k_update<float>, kMaxRedBlocks, dim3(32, 8), st_, d, nr, d32_, ri32_, p32_, q32_, sc_, part_, ticket_);
     tk_.launches += 4;
     iter_launches32_ = tk_.launches - l0;
     if (copy_slots) cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
@@ -2023,13 +2100,14 @@ void MGSolver::enqueue_iter32(bool copy_slots) {
 
 // Control of the device-side inner loop (one thread, the last node of the loop body): counts the iteration and
 // continues while no breakdown or timed-out wait was flagged, ||r||^2 is finite and above its target, the budget
-// is not spent, and the iteration is not stagnating -- the host loop's tests: two consecutive iterations each
-// leaving more than a quarter of ||r||^2 end the inner solve (FP32 stagnation; the refinement takes over).
+// is not spent, and (mixed form) the iteration is not stagnating -- the host loop's tests: two consecutive
+// iterations each leaving more than a quarter of ||r||^2 end the inner solve (FP32 stagnation; the refinement
+// takes over).
 __global__ void k_inner_ctl(double *sc, cudaGraphConditionalHandle h) {
     const double it = sc[S_IT] + 1.0;
     sc[S_IT] = it;
     const double rin = sc[S_RR];
-    const double slow = rin > 0.25 * sc[S_RPREV] ? sc[S_SLOW] + 1.0 : 0.0;
+    const double slow = (sc[S_STAG] != 0.0 && rin > 0.25 * sc[S_RPREV]) ? sc[S_SLOW] + 1.0 : 0.0;
     sc[S_SLOW] = slow;
     sc[S_RPREV] = rin;
     const bool go = sc[S_AUX0] == 0.0 && sc[S_ERR] == 0.0 && isfinite(rin) && rin > sc[S_TOL2] &&
@@ -2037,7 +2115,7 @@ __global__ void k_inner_ctl(double *sc, cudaGraphConditionalHandle h) {
     cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 
-cudaError_t MGSolver::build_loop32() {
+cudaError_t MGSolver::build_loop(bool mixed) {
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaGraphCreate(&g, 0);
     if (e != cudaSuccess) return e;
@@ -2056,14 +2134,18 @@ cudaError_t MGSolver::build_loop32() {
         const long long before = tk_.launches;
         e = cudaStreamBeginCaptureToGraph(st_, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            enqueue_iter32(false);
+            if (mixed)
+                enqueue_iter32(false);
+            else
+                enqueue_iter64(false);
             k_inner_ctl<<<1, 1, 0, st_>>>(sc_, h);
             e = cudaStreamEndCapture(st_, &body);
         }
         tk_.launches = before;  // counted per iteration after each loop
     }
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&g_loop32_, g, 0);
-    if (e != cudaSuccess) g_loop32_ = nullptr;
+    cudaGraphExec_t &ge = mixed ? g_loop32_ : g_loop64_;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+    if (e != cudaSuccess) ge = nullptr;
     cudaGraphDestroy(g);
     return e;
 }
@@ -2071,24 +2153,28 @@ cudaError_t MGSolver::build_loop32() {
 // Runs inner iterations until the loop's tests stop it (at least one; budget > 0), from the recurrence state
 // already on the device.  One graph launch and one read-back when the device-side loop is available, else one
 // graph launch (or direct launches) and one read-back per iteration.
-cudaError_t MGSolver::inner_loop(int budget, double tol2, double rr, int &iters) {
+cudaError_t MGSolver::inner_loop(bool mixed, int budget, double tol2, double rr, int &iters) {
     cudaError_t e;
     iters = 0;
+    cudaGraphExec_t *ge = nullptr;
     if (prm_.use_graph && !prm_.profile && loop_ok_) {
-        // same configuration key as run_iter's graphs (it destroys this one as well when the key changes)
+        // same configuration key as run_iter's graphs (it destroys these as well when the key changes)
         if ((e = run_iter_prepare()) != cudaSuccess) return e;
-        if (!g_loop32_ && build_loop32() != cudaSuccess) {
+        ge = mixed ? &g_loop32_ : &g_loop64_;
+        if (!*ge && build_loop(mixed) != cudaSuccess) {
             cudaGetLastError();
             loop_ok_ = false;  // the host-driven loop below
+            ge = nullptr;
         }
     }
-    if (prm_.use_graph && !prm_.profile && loop_ok_ && g_loop32_) {
-        const double st[5] = {0.0, tol2, (double)budget, rr, 0.0};  // S_IT, S_TOL2, S_BUDGET, S_RPREV, S_SLOW
+    if (ge && *ge) {
+        // S_IT, S_TOL2, S_BUDGET, S_RPREV, S_SLOW, S_STAG
+        const double st[6] = {0.0, tol2, (double)budget, rr, 0.0, mixed ? 1.0 : 0.0};
         cudaMemcpyAsync(sc_ + S_IT, st, sizeof(st), cudaMemcpyHostToDevice, st_);
-        if ((e = cudaGraphLaunch(g_loop32_, st_)) != cudaSuccess) return e;
+        if ((e = cudaGraphLaunch(*ge, st_)) != cudaSuccess) return e;
         if ((e = read_slots()) != cudaSuccess) return e;
         iters = (int)sc_host_[S_IT];
-        tk_.launches += (long long)iters * (iter_launches32_ + 1);
+        tk_.launches += (long long)iters * ((mixed ? iter_launches32_ : iter_launches64_) + 1);
         return cudaSuccess;
     }
     double rprev = rr;
@@ -2096,11 +2182,12 @@ cudaError_t MGSolver::inner_loop(int budget, double tol2, double rr, int &iters)
     const int every = prm_.check_every > 0 ? prm_.check_every : 1;
     while (iters < budget) {
         for (int s = 0; s < every && iters < budget; s++, iters++)
-            if ((e = run_iter(true)) != cudaSuccess) return e;
+            if ((e = run_iter(mixed)) != cudaSuccess) return e;
         if ((e = cudaStreamSynchronize(st_)) != cudaSuccess) return e;
         const double rin = sc_host_[S_RR];
         if (sc_host_[S_AUX0] != 0) break;
         if (rin <= tol2 || !std::isfinite(rin)) break;
+        if (!mixed) continue;
         // FP32 stagnation: two consecutive iterations reducing ||r|| by less than 2x -> refine in FP64
         slow = (rin > 0.25 * rprev) ? slow + 1 : 0;
         rprev = rin;
@@ -2192,7 +2279,7 @@ cudaError_t MGSolver::solve64(bool x_is_zero, SolveResult &res) {
     } else {
         // r = b - A x, (r,r), (b,b)
         k_residual64<double><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c64_[0], x_, b_, r_, 0, S_RR, S_BB, sc_, part_,
-                                                          ticket_);
+                                                          ticket_, 0, rows64_ ? rows_[0] : nullptr);
     }
     tk_.launches++;
     cudaMemsetAsync(p_, 0, 8 * n, st_);
@@ -2221,18 +2308,13 @@ cudaError_t MGSolver::solve64(bool x_is_zero, SolveResult &res) {
         res.relres = std::sqrt(rr / bb);
         return cudaSuccess;
     }
-    const int every = prm_.check_every > 0 ? prm_.check_every : 1;
     int it = 0;
-    while (it < prm_.max_iters) {
-        for (int s = 0; s < every && it < prm_.max_iters; s++, it++)
-            if ((e = run_iter(false)) != cudaSuccess) return e;
-        if ((e = cudaStreamSynchronize(st_)) != cudaSuccess) return e;
-        rr = sc_host_[S_RR];
-        if (sc_host_[S_AUX0] != 0) {
-            res.breakdown = true;
-            break;
-        }
-        if (rr <= tol2 || !std::isfinite(rr)) break;
+    if ((e = inner_loop(false, prm_.max_iters, tol2, rr, it)) != cudaSuccess) return e;
+    rr = sc_host_[S_RR];
+    if (sc_host_[S_AUX0] != 0) res.breakdown = true;
+    if (sc_host_[S_ERR] != 0) {
+        last_error = "a smoother's TMA load did not arrive within its bounded wait";
+        return cudaErrorLaunchTimeout;
     }
     res.iters = it;
     res.relres = std::sqrt(rr / bb);
@@ -2300,7 +2382,7 @@ cudaError_t MGSolver::solve_mixed(bool x_is_zero, SolveResult &res) {
         const int budget = prm_.max_iters - total_inner;
         // the inner residual after a learned step (it is the FP64 residual otherwise)
         const double rin0 = (learned_ && res.learned_steps > 0 && !stalled) ? sc_host_[S_RR] : rr;
-        if (budget > 0 && (e = inner_loop(budget, in_tol2, rin0, it)) != cudaSuccess) return e;
+        if (budget > 0 && (e = inner_loop(true, budget, in_tol2, rin0, it)) != cudaSuccess) return e;
         if (sc_host_[S_ERR] != 0) {
             last_error = "a smoother's TMA load did not arrive within its bounded wait";
             return cudaErrorLaunchTimeout;
@@ -2360,7 +2442,8 @@ cudaError_t MGSolver::learned_step(double rr, bool first, bool &stalled, SolveRe
     } else {
         cudaMemcpyAsync(p32_, yn, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st_);
         apply_dot32(st_, d, c32_, p32_, q32_, sc_, part_, ticket_);
-        k_dot_rz<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, r32_, p32_, q32_, 1, sc_, part_, ticket_);
+        k_dot_rz<float><<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(d, (const uint8_t *)nullptr, r32_, p32_, q32_, 1, sc_,
+                                                                 part_, ticket_);
     }
     k_learned_update<<<kMaxRedBlocks, dim3(32, 8), 0, st_>>>(n, d32_, r32_, p32_, q32_, sc_, part_, ticket_);
     tk_.launches += 6;
@@ -2392,7 +2475,7 @@ cudaError_t MGSolver::true_relres(bool skip0, double &relres, double &bnorm) {
     const dim3 tg = tile_grid(d, xpb, kStencilBlocks);
     k_residual64<double><<<tg, dim3(32, 8), 0, st_>>>(d, xpb, c64_[0], x_, b_, (double *)nullptr, skip0 ? 1 : 0,
                                                       S_AUX1, S_AUX2, sc_, part_, ticket_, 0,
-                                                      split0_ ? rows_[0] : nullptr);
+                                                      (split0_ || rows64_) ? rows_[0] : nullptr);
     tk_.launches++;
     cudaError_t e = read_slots();
     if (e != cudaSuccess) return e;

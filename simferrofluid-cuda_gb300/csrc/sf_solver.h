@@ -30,6 +30,7 @@ struct SolverParams {
     int smoother = 0;       // 0: two in-place colour kernels, 1: fused one-pass red-black sweep
     int tail = 0;  // mixed form, levels of at most 65,536 cells: 0 one cluster launch (16 CTAs, else 8), 8 / 16 that
                    // cluster size, 1 separate kernels
+    bool full_sweeps = false;  // FP64 form: every row, also rows without an active cell (else they are skipped)
 };
 
 // Counts kernel launches and, when profiling, brackets finest-level smoother launches with events.
@@ -64,6 +65,10 @@ struct SolveResult {
     int learned_steps = 0;      // learned correction steps applied
     double relres = 0, bnorm = 0;
 };
+
+// Launches the bounded-wait self-test (one CTA waits on an mbarrier that nothing completes, for limit_ns; device
+// out[0] = 1 when it gave up, out[1] = nanoseconds waited).
+cudaError_t selftest_bounded_wait(cudaStream_t st, unsigned long long limit_ns, unsigned long long *out);
 
 // The learned form's correction of an inner solve: y = the network's prediction of A^-1 r for an FP32 residual r
 // on the fine level's cells (natural layout), rr = (r, r).
@@ -152,6 +157,7 @@ class MGSolver {
     cudaError_t learned_step(double rr, bool first, bool &stalled, SolveResult &res);
     Dims cfg_dims_{0, 0, 0, 0};
     int cfg_prec_ = -1, cfg_levels_ = -1, cfg_cdim_ = -1, cfg_smoother_ = -1;
+    bool rows64_ = false;  // FP64 form with row flags on every level (rows_): inactive rows are skipped
 
     // FP64 hierarchy (precision 0) or fine FP64 operator only (precision 1)
     std::vector<Coef<double>> c64_;
@@ -193,12 +199,12 @@ class MGSolver {
     unsigned *ticket_ = nullptr;
 
     cudaGraphExec_t g_iter64_ = nullptr, g_iter32_ = nullptr;
-    // the mixed form's inner flexible-CG loop as one graph: a conditional WHILE node whose body is one iteration
+    // the inner (flexible) CG loop of each form as one graph: a conditional WHILE node whose body is one iteration
     // and k_inner_ctl (loop_ok_ false: the loop is driven from the host, one graph launch per iteration)
-    cudaGraphExec_t g_loop32_ = nullptr;
+    cudaGraphExec_t g_loop32_ = nullptr, g_loop64_ = nullptr;
     bool loop_ok_ = true;
-    cudaError_t inner_loop(int budget, double tol2, double rr, int &iters);
-    cudaError_t build_loop32();
+    cudaError_t inner_loop(bool mixed, int budget, double tol2, double rr, int &iters);
+    cudaError_t build_loop(bool mixed);
     cudaError_t run_iter_prepare();
     long long graph_key_ = -1;
     long long iter_launches64_ = 0, iter_launches32_ = 0;
@@ -209,7 +215,7 @@ class MGSolver {
     void destroy_graphs();
     cudaError_t solve64(bool x_is_zero, SolveResult &res);
     cudaError_t solve_mixed(bool x_is_zero, SolveResult &res);
-    void enqueue_iter64();
+    void enqueue_iter64(bool copy_slots = true);
     void enqueue_iter32(bool copy_slots = true);
     cudaError_t run_iter(bool mixed);
     cudaError_t read_slots();
