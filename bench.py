@@ -49,6 +49,9 @@ def parse(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64-arm", action="store_true")
     ap.add_argument("--no-learned-arm", action="store_true")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="launch each solver iteration's kernels from the host (no CUDA graphs; for kernel profilers "
+                         "that do not replay kernels inside conditional graph nodes)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the errors against the oracle's FP64 answer")
     ap.add_argument("--inner-tol", type=float, default=None, help="mixed form: inner relative reduction floor")
@@ -224,6 +227,8 @@ def run_ours(args, ws, rank, local):
             v = getattr(args, name)
             if v is not None:
                 kw[key] = v
+        if args.no_graph:
+            kw["use_graph"] = 0
         return pkg.options(which, precision=precision, tol=args.tol, warm_start=0, report_ref_residual=0,
                            profile=profile, full_sweeps=full_sweeps[0], **kw)
 

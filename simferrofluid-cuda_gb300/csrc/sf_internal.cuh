@@ -169,9 +169,10 @@ constexpr int kRedGroup = 256;  // blocks per first-level group
 // Warp sum of FP32 values as an unevaluated (hi, lo) pair of floats: each shuffle stage adds the partner's pair
 // with the exact two-sum (Knuth), keeps the rounding error in lo and renormalises, so the sum carries about 48
 // bits.  It runs on the FP32 pipe, which on this GPU issues 64 times as many lanes per clock as the FP64 pipe;
-// lane 0's pair is converted to one double.  Same fixed shuffle order as warp_sum, hence deterministic.
+// lane 0 holds the warp's pair (converted to FP64 only in the block stage, by one thread).  Same fixed shuffle
+// order as warp_sum, hence deterministic.
 template <int K>
-__device__ __forceinline__ void warp_sum_df(const float (&v)[K], double (&out)[K]) {
+__device__ __forceinline__ void warp_sum_df(const float (&v)[K], float (&hi_out)[K], float (&lo_out)[K]) {
 #pragma unroll
     for (int q = 0; q < K; q++) {
         float hi = v[q], lo = 0.f;
@@ -186,7 +187,8 @@ __device__ __forceinline__ void warp_sum_df(const float (&v)[K], double (&out)[K
             hi = __fadd_rn(sum, l);
             lo = __fsub_rn(l, __fsub_rn(hi, sum));
         }
-        out[q] = (double)hi + (double)lo;
+        hi_out[q] = hi;
+        lo_out[q] = lo;
     }
 }
 
@@ -199,6 +201,7 @@ __device__ __forceinline__ void warp_sum_df(const float (&v)[K], double (&out)[K
 template <int K, class V>
 __device__ __forceinline__ bool grid_reduce(V (&v)[K], double *part, unsigned *ticket, double (&tot)[K]) {
     __shared__ double sh[K][kRedThreads / 32];
+    __shared__ float shf[K][2][kRedThreads / 32];
     __shared__ bool last;
     const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     const int nblk = gridDim.x * gridDim.y * gridDim.z;
@@ -207,24 +210,30 @@ __device__ __forceinline__ bool grid_reduce(V (&v)[K], double *part, unsigned *t
     const int grp = bid / kRedGroup;
     const int gsize = min(kRedGroup, nblk - grp * kRedGroup);
     double *gpart = part + (long long)K * nblk;
-    double w[K];
-    if constexpr (std::is_same<V, float>::value) {
-        warp_sum_df<K>(v, w);
+    const int lane = tid & 31, wid = tid >> 5;
+    constexpr bool kFloat = std::is_same<V, float>::value;
+    if constexpr (kFloat) {
+        float hi[K], lo[K];
+        warp_sum_df<K>(v, hi, lo);
+        if (lane == 0)
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                shf[q][0][wid] = hi[q];
+                shf[q][1][wid] = lo[q];
+            }
     } else {
         warp_sum<K>(v);
+        if (lane == 0)
 #pragma unroll
-        for (int q = 0; q < K; q++) w[q] = v[q];
+            for (int q = 0; q < K; q++) sh[q][wid] = v[q];
     }
-    const int lane = tid & 31, wid = tid >> 5;
-    if (lane == 0)
-#pragma unroll
-        for (int q = 0; q < K; q++) sh[q][wid] = w[q];
     __syncthreads();
     if (tid == 0) {
 #pragma unroll
         for (int q = 0; q < K; q++) {
             double b = 0;
-            for (int w = 0; w < kRedThreads / 32; w++) b += sh[q][w];
+            for (int w = 0; w < kRedThreads / 32; w++)
+                b += kFloat ? ((double)shf[q][0][w] + (double)shf[q][1][w]) : sh[q][w];
             part[(long long)q * nblk + bid] = b;
         }
         __threadfence();
