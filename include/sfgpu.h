@@ -327,9 +327,12 @@ SF_EXPORT sf_status sf_levelset_upload(void *ctx, const sf_grid *g, const double
  * belongs to that device.  The call is asynchronous: result is valid once the stream reaches it.
  * Limit: ceil(ny/8) * ceil(nz/32) <= SF_NOALLOC_MAX_BLOCKS tiles per x-plane (e.g. ny, nz <= 1024, or ny = 2048
  * with nz = 1024); nx is free.  Larger grids return SF_TOO_LARGE without touching the device.
- * The first call on each device looks up the scratch's address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  Calls that overlap on the GPU (in flight on two
- * streams at once, or from two threads) share the scratch and race: order them on one stream. */
+ * Every call looks up the scratch's address in the current context (cudaGetSymbolAddress, a host-side query), so
+ * it stays valid across cudaDeviceReset and context switches.  With lazy module loading (the CUDA default) the
+ * first call in a context loads the module that holds the scratch, which needs device memory and is not allowed
+ * inside a stream capture: make that first call before the caller reserves its memory pool and before any
+ * capture.  Calls that overlap on the GPU (in flight on two streams at once, or from two threads) share the
+ * scratch and race: order them on one stream. */
 #define SF_NOALLOC_MAX_BLOCKS 8192
 SF_EXPORT sf_status sf_magnetic_residual_noalloc(void *stream, const sf_grid *g, const double *phi, double chi,
                                                  double band_width, const double *const hext[3], const double *psi,

@@ -1638,10 +1638,26 @@ static void vcycle(cudaStream_t st, Tracker &tk, const std::vector<Dims> &dims, 
             P.x0 = xs[tail_lt];
             P.pairs = p.coarse_sweeps;
             tk.launches++;
-            launch_tail(st, tail_nc, P, tail_smem);
+            if (launch_tail(st, tail_nc, P, tail_smem) != cudaSuccess) {
+                cudaGetLastError();
+                tk.tail_failed = true;
+                tail = false;  // the same levels with the separate kernels (same arithmetic, same bits)
+                for (int l = bottom; l < L - 1; l++) {
+                    smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l],
+                                  l >= 2 ? p.coarse_pre : p.pre, true, false, R(l));
+                    restrict_res<T, Cc>(st, tk, dims[l], cc[l], xs[l], bs[l], dims[l + 1], bs[l + 1], false, R(l),
+                                        R(l + 1));
+                }
+            }
         }
     }
     if (!tail) coarse_solve<T, Cc>(st, tk, dims[L - 1], cc[L - 1], xs[L - 1], bs[L - 1], p.coarse_sweeps);
+    for (int l = L - 2; !tail && l >= bottom && bottom < L - 1; l--) {  // after a rejected tail launch
+        tk.launches++;
+        launch_pdl(k_prolong<T>, grid_cells(dims[l]), blk2(), st, dims[l], xs[l], dims[l + 1], xs[l + 1], R(l));
+        smooth<T, Cc>(st, tk, false, dims[l], cc[l], xs[l], nullptr, bs[l], l >= 2 ? p.coarse_post : p.post, false,
+                      false, R(l));
+    }
     for (int l = bottom - 1; l >= 1; l--) {
         tk.launches++;
         if constexpr (std::is_same<T, float>::value && std::is_same<Cc, __half>::value) {
@@ -1692,6 +1708,15 @@ void MGSolver::destroy_graphs() {
     if (g_loop64_) cudaGraphExecDestroy(g_loop64_);
     g_iter64_ = g_iter32_ = g_loop32_ = g_loop64_ = nullptr;
     graph_key_ = -1;
+}
+
+bool MGSolver::drop_tail() {
+    if (!tk_.tail_failed) return false;
+    tk_.tail_failed = false;
+    tail_lt_ = -1;
+    tail_smem_ = tail_nc_ = 0;
+    destroy_graphs();
+    return true;
 }
 
 void MGSolver::free_all() {
@@ -2163,8 +2188,12 @@ cudaError_t MGSolver::inner_loop(bool mixed, int budget, double tol2, double rr,
         ge = mixed ? &g_loop32_ : &g_loop64_;
         if (!*ge && build_loop(mixed) != cudaSuccess) {
             cudaGetLastError();
-            loop_ok_ = false;  // the host-driven loop below
-            ge = nullptr;
+            // a rejected tail launch invalidates the capture: once more without the tail, else the host loop
+            if (!(drop_tail() && run_iter_prepare() == cudaSuccess && build_loop(mixed) == cudaSuccess)) {
+                cudaGetLastError();
+                loop_ok_ = false;  // the host-driven loop below
+                ge = nullptr;
+            }
         }
     }
     if (ge && *ge) {
@@ -2215,6 +2244,7 @@ cudaError_t MGSolver::run_iter(bool mixed) {
             enqueue_iter32();
         else
             enqueue_iter64();
+        drop_tail();  // this iteration ran the separate kernels in its place
         return cudaGetLastError();
     }
     run_iter_prepare();
@@ -2229,7 +2259,12 @@ cudaError_t MGSolver::run_iter(bool mixed) {
         else
             enqueue_iter64();
         e = cudaStreamEndCapture(st_, &g);
-        if (e != cudaSuccess) return e;
+        if (e != cudaSuccess) {
+            tk_.launches = before;
+            if (!drop_tail()) return e;
+            cudaGetLastError();
+            return run_iter(mixed);  // captured again without the tail
+        }
         e = cudaGraphInstantiate(&ge, g, 0);
         cudaGraphDestroy(g);
         tk_.launches = before;  // counted at replay

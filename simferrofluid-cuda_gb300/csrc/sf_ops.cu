@@ -5,7 +5,6 @@
 // assembly on the same inputs, and the velocity / field updates are too.
 #include <cmath>
 #include <cstring>
-#include <mutex>
 
 #include "sf_ops.h"
 
@@ -524,28 +523,17 @@ bool noalloc_fits(const Dims &d) {
     return (long long)((d.nz + 31) / 32) * ((d.ny + 7) / 8) <= kNoAllocBlocks;
 }
 
-// Device addresses of the scratch, looked up once per device (with that device current) and cached.
+// Device addresses of the scratch in the calling thread's current context, looked up on every call (a host-side
+// query, no allocation once the module is loaded), so that no address outlives its context (cudaDeviceReset, a
+// caller that switches driver contexts on the same device).
 namespace {
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-double *g_noalloc_part_ptr[kNoAllocMaxDevices];
-unsigned *g_noalloc_ticket_ptr[kNoAllocMaxDevices];
-
 cudaError_t noalloc_scratch(double **part, unsigned **ticket) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_part_ptr[dev]) {
-        void *p = nullptr, *t = nullptr;
-        if ((e = cudaGetSymbolAddress(&p, g_noalloc_part)) != cudaSuccess) return e;
-        if ((e = cudaGetSymbolAddress(&t, g_noalloc_ticket)) != cudaSuccess) return e;
-        g_noalloc_ticket_ptr[dev] = static_cast<unsigned *>(t);
-        g_noalloc_part_ptr[dev] = static_cast<double *>(p);
-    }
-    *part = g_noalloc_part_ptr[dev];
-    *ticket = g_noalloc_ticket_ptr[dev];
+    void *p = nullptr, *t = nullptr;
+    cudaError_t e;
+    if ((e = cudaGetSymbolAddress(&p, g_noalloc_part)) != cudaSuccess) return e;
+    if ((e = cudaGetSymbolAddress(&t, g_noalloc_ticket)) != cudaSuccess) return e;
+    *part = static_cast<double *>(p);
+    *ticket = static_cast<unsigned *>(t);
     return cudaSuccess;
 }
 }  // namespace

@@ -44,6 +44,7 @@ struct Tracker {
     // profile: algorithmic bytes of one split level-0 half sweep, counted over the rows it processes and by row
     // kind (-1: not set, every cell at the general rate)
     double bytes0 = -1;
+    bool tail_failed = false;  // a fused-tail cluster launch was rejected (the separate kernels ran instead)
     void before(cudaStream_t st, bool fine);
     void after(cudaStream_t st, bool fine, double algo_bytes);
     // after a stream sync: summed milliseconds, launch count and algorithmic bytes of the bracketed
@@ -213,6 +214,7 @@ class MGSolver {
     void *alloc(size_t bytes);
     void free_all();
     void destroy_graphs();
+    bool drop_tail();  // after a rejected fused-tail launch: separate kernels from now on (true if it was on)
     cudaError_t solve64(bool x_is_zero, SolveResult &res);
     cudaError_t solve_mixed(bool x_is_zero, SolveResult &res);
     void enqueue_iter64(bool copy_slots = true);

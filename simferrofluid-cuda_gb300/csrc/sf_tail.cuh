@@ -511,14 +511,15 @@ static bool tail_launchable(int smem) {
     return nc >= 1;
 }
 
-static void launch_tail(cudaStream_t st, int nc, const TailParams &P, int smem) {
+// The launch's own status: a cluster launch the device rejects leaves the tail's levels untouched, and the caller
+// runs the separate kernels instead.
+static cudaError_t launch_tail(cudaStream_t st, int nc, const TailParams &P, int smem) {
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute at[1];
     if (nc == 16) {
         tail_config<16>(cfg, at, st, smem);
-        cudaLaunchKernelEx(&cfg, k_tail<16>, P);
-    } else {
-        tail_config<8>(cfg, at, st, smem);
-        cudaLaunchKernelEx(&cfg, k_tail<8>, P);
+        return cudaLaunchKernelEx(&cfg, k_tail<16>, P);
     }
+    tail_config<8>(cfg, at, st, smem);
+    return cudaLaunchKernelEx(&cfg, k_tail<8>, P);
 }

@@ -103,6 +103,30 @@ def test_bad_arguments_rejected_without_gpu():
     assert lib.sf_collider_box_fractions(C.byref(g), 0, nulls, None) == 2
 
 
+def test_noalloc_rejects_bad_arguments_before_any_device_call():
+    """sf_magnetic_residual_noalloc checks its arguments on the host first: a null hext entry, band_width <= 0 or
+    not finite, a non-finite chi and a null output are SF_BAD_ARG without touching a device (the pointers are
+    never dereferenced on these paths)."""
+    lib = pkg().load_library()
+    abi = pkg()._abi
+    g = pkg().StaggeredGrid.from_origin(0.1, (8, 8, 8)).c_grid()
+    fake = 4096  # any non-null address: rejected before use
+    ok3 = abi.p3([fake, fake, fake])
+
+    def call(hext=ok3, chi=1.0, bw=0.2, phi=fake, psi=fake, result=fake):
+        return lib.sf_magnetic_residual_noalloc(None, C.byref(g), C.c_void_p(phi), chi, bw, hext,
+                                                C.c_void_p(psi), C.c_void_p(result))
+
+    for a in range(3):
+        h = [fake, fake, fake]
+        h[a] = 0
+        assert call(hext=abi.p3(h)) == abi.SF_BAD_ARG
+    for bw in (0.0, -0.1, float("nan"), float("inf")):
+        assert call(bw=bw) == abi.SF_BAD_ARG
+    assert call(chi=float("nan")) == abi.SF_BAD_ARG
+    assert call(phi=0) == abi.SF_BAD_ARG and call(psi=0) == abi.SF_BAD_ARG and call(result=0) == abi.SF_BAD_ARG
+
+
 def test_package_has_no_cpu_fallback(monkeypatch):
     """The package raises when the library is missing instead of computing on the CPU."""
     sf = pkg()
