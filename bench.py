@@ -496,12 +496,14 @@ def _cpu_scene(n):
     return O, sc, og
 
 
-def _cpu_step(O, sc, og, tol):
-    """One substep on the CPU restatement of the reference's path: Pressure::Project and MagneticField::Solve,
-    each assembling its matrix, rebuilding the SA-AMG hierarchy and solving (BiCGStab / CG) to tol."""
+def _cpu_step(O, sc, og, tol, solver="amg"):
+    """One substep on the CPU: Pressure::Project and MagneticField::Solve, each assembling its matrix (the
+    reference's assembly, restated) and solving to tol from zero, with solver "amg" (the restated amgcl path:
+    SA-AMG hierarchy rebuilt per solve, BiCGStab / CG) or "mgpcg" (the library's plain FP64 geometric-MG PCG on
+    the host cores)."""
     t = time.perf_counter()
-    _, _, ip = O.pressure_project(og, sc.phi, sc.frac, sc.vel, tol=tol, solver="amg")
-    _, _, im = O.magnetic_solve(og, sc.phi, sc.chi, sc.band_width, sc.hext, tol=tol, solver="amg")
+    _, _, ip = O.pressure_project(og, sc.phi, sc.frac, sc.vel, tol=tol, solver=solver)
+    _, _, im = O.magnetic_solve(og, sc.phi, sc.chi, sc.band_width, sc.hext, tol=tol, solver=solver)
     return time.perf_counter() - t, ip["iters"], im["iters"]
 
 
@@ -517,6 +519,18 @@ def cpu_baseline(args, n=None, steps=1):
     return {"value": round(2 * steps / tot, 4), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
             "sample": f"pool_sphere {n}^3, {steps} substep(s) = {2 * steps} solves (assembly + SA-AMG setup + "
                       f"BiCGStab/CG to {args.tol:g}), {tot:.1f} s, iterations (pressure, potential) {its}"}
+
+
+def cpu_mgpcg_fp64(args, n=None):
+    """The library's plain FP64 method (geometric-MG PCG, oracle/sf_mgcpu.c) on the host cores, same scene and
+    tolerance: one warm-up substep, then one timed substep (assembly + face form + MGPCG + projection / H)."""
+    n = n or args.n
+    O, sc, og = _cpu_scene(n)
+    _cpu_step(O, sc, og, args.tol, solver="mgpcg")
+    dt, ip, im = _cpu_step(O, sc, og, args.tol, solver="mgpcg")
+    return {"value": round(2 / dt, 4), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+            "sample": f"pool_sphere {n}^3, 1 substep = 2 solves (assembly + MGPCG V(2,2) to {args.tol:g} from "
+                      f"zero), {dt:.2f} s, iterations (pressure, potential) ({ip}, {im})"}
 
 
 def run_reference(args, ws, rank):
@@ -558,6 +572,7 @@ def main():
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args)
+            out["cpu_mgpcg_fp64"] = cpu_mgpcg_fp64(args)
         print(json.dumps(out))
 
 

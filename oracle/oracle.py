@@ -23,7 +23,7 @@ LIB = os.path.join(BUILD, "liboracle.so")
 
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc (OpenMP, no FMA contraction) into oracle/_build/liboracle.so."""
-    srcs = [os.path.join(HERE, f) for f in ("sf_oracle.c", "sf_amg.c")]
+    srcs = [os.path.join(HERE, f) for f in ("sf_oracle.c", "sf_amg.c", "sf_mgcpu.c")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in srcs):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
@@ -114,6 +114,12 @@ def lib():
         L.or_amg_solve.argtypes = [C.c_int, C.c_int64, _I64, _I32, _D, _D, _D, C.c_double, C.c_int,
                                    C.POINTER(_AmgInfo)]
         L.or_amg_solve.restype = C.c_int
+        L.or_pressure_face_form.argtypes = [C.c_int, C.c_int, C.c_int, _I64, C.c_int64, _I64, _I32, _D, _D, _D, _D,
+                                            _D, _D]
+        L.or_magnetic_face_form.argtypes = [C.c_int, C.c_int, C.c_int, _D, _D, _D, _D, _D, _D, _D, _D]
+        L.or_mgpcg_solve.argtypes = [C.c_int, C.c_int, C.c_int, _D, _D, _D, _D, _D, _D, _D, C.c_double, C.c_int,
+                                     C.c_int, C.POINTER(C.c_double)]
+        L.or_mgpcg_solve.restype = C.c_int
     return _lib
 
 
@@ -170,6 +176,25 @@ class CSR:
         rc = lib().or_amg_solve(int(kind), self.n, _p(self.rowptr, _I64), _p(self.col, _I32), _p(self.val), _p(b),
                                 _p(x), float(tol), int(maxit), C.byref(inf))
         return x, dict(iters=inf.iters, resid=inf.resid, levels=inf.levels, setup_s=inf.setup_s, converged=rc == 0)
+
+
+# ------------------------------------------------------------------------------------------------ CPU MGPCG
+def mgpcg_solve(g: Grid, form, b, tol, maxit=200, pairs=48):
+    """The library's plain FP64 method (geometric-MG PCG, sf_mgcpu.c) on the host cores, from x = 0.
+    form = (ax, ay, az, dex, D) on the cell grid; b on the cell grid.  Returns (x, iters, relres)."""
+    ax, ay, az, dex, D = [_f64(a).reshape(-1) for a in form]
+    b = _f64(b).reshape(-1)
+    x = np.empty(g.N)
+    rr = C.c_double()
+    it = lib().or_mgpcg_solve(g.nx, g.ny, g.nz, _p(ax), _p(ay), _p(az), _p(dex), _p(D), _p(b), _p(x), float(tol),
+                              int(maxit), int(pairs), C.byref(rr))
+    if it < 0:
+        raise MemoryError("or_mgpcg_solve: allocation failed")
+    return x, it, rr.value
+
+
+def _empty_form(g: Grid):
+    return [np.empty(g.N) for _ in range(5)]
 
 
 # ------------------------------------------------------------------------------------------------ pressure
@@ -234,6 +259,15 @@ def pressure_project(g: Grid, phi, frac, u, us=None, jump=None, vol_error=0.0, t
         p, inf = A.amg_solve(b, 0, tol=tol, maxit=min(maxit, 100))
         it = inf["iters"]
         rr = float(np.linalg.norm(b - A.matvec(p)) / max(np.linalg.norm(b), 1e-300))
+    elif solver == "mgpcg":
+        form = _empty_form(g)
+        lib().or_pressure_face_form(g.nx, g.ny, g.nz, _p(m2g, _I64), A.n, _p(A.rowptr, _I64), _p(A.col, _I32),
+                                    _p(A.val), *[_p(a) for a in form])
+        bg = np.zeros(g.N)
+        bg[m2g] = b
+        x, it, _ = mgpcg_solve(g, form, bg, tol, maxit=min(maxit, 200))
+        p = x[m2g]
+        rr = float(np.linalg.norm(b - A.matvec(p)) / max(np.linalg.norm(b), 1e-300))
     else:
         p, it, rr = A.solve(b, tol=tol, maxit=maxit)
     u_new = pressure_apply(g, phi, frac, jump, g2m, p, u)
@@ -283,8 +317,19 @@ def magnetic_total_field(g: Grid, psi, hext):
 
 def magnetic_solve(g: Grid, phi, chi, band_width, hext, psi0=None, tol=1e-12, maxit=20000, solver="pcg"):
     """MagneticField::Solve with the pinned system solved to ``tol`` ("pcg", or "amg" = the restated amgcl
-    SA-AMG + CG of core/MagneticField.cpp:92-94,120-123, warm start psi0).  Returns (psi, H, info)."""
+    SA-AMG + CG of core/MagneticField.cpp:92-94,120-123, warm start psi0; or "mgpcg" = the library's plain FP64
+    method on the host cores, on the Neumann system, shifted so that psi_0 = 0, from zero).  Returns
+    (psi, H, info)."""
     mu = magnetic_coeff(g, phi, chi, band_width)
+    if solver == "mgpcg":
+        b, b0n = magnetic_rhs(g, mu, hext)
+        b[0] = b0n  # row 0's natural right-hand side: the consistent Neumann system
+        form = _empty_form(g)
+        lib().or_magnetic_face_form(g.nx, g.ny, g.nz, *[_p(_f64(m)) for m in mu], *[_p(a) for a in form])
+        x, it, rr = mgpcg_solve(g, form, b, tol, maxit=min(maxit, 200))
+        psi = x - x[0]
+        H = magnetic_total_field(g, psi, hext)
+        return psi.reshape(g.shape), H, dict(iters=it, relres=rr, mu=mu, rhs0_neumann=b0n)
     A = magnetic_assemble(g, mu)
     b, b0n = magnetic_rhs(g, mu, hext)
     x0 = None if psi0 is None else _f64(psi0).reshape(-1)

@@ -145,3 +145,32 @@ def test_slab_kat_oracle(oracle):
     yf = np.arange(n + 1) / n
     inside = (yf > 0.05) & (yf < 0.5 - 3 * g.h)
     assert np.abs(H[1][:, inside, :] - 0.5).max() <= 1e-9
+
+
+@pytest.mark.parametrize("shape", [(24, 20, 28), (17, 13, 9)])
+def test_cpu_mgpcg_matches_pcg(oracle, shape):
+    """The CPU geometric-MG PCG (the benchmark's CPU MGPCG FP64 baseline, oracle/sf_mgcpu.c) solves the same
+    pressure and (pinned) potential systems as the oracle's Jacobi-PCG: to 1e-10 on a pool+sphere and on a
+    ragged grid, in a handful of iterations."""
+    import importlib
+    S = importlib.import_module(scenes().__name__)
+    sc = S.pool_sphere(max(shape), seed=8, with_fractions=False)
+    # a ragged grid of the same kind: the scene's fields cropped
+    sl = tuple(slice(0, n) for n in shape)
+    g = oracle.Grid(*shape, sc.grid.spacing)
+    phi = np.ascontiguousarray(sc.phi[sl])
+    frac = oracle.box_collider_fractions(g, 0)
+    rng = np.random.default_rng(3)
+    vel = [rng.normal(0, 0.5, g.face_shape(a)) for a in range(3)]
+    hext = [rng.uniform(-1, 1, g.face_shape(a)) + (a == 1) for a in range(3)]
+    u1, p1, i1 = oracle.pressure_project(g, phi, frac, vel, tol=1e-10, solver="mgpcg")
+    u0, p0, i0 = oracle.pressure_project(g, phi, frac, vel, tol=1e-13)
+    liq = phi <= 0
+    assert i1["relres"] <= 1e-10 and i1["iters"] <= 20
+    assert rel_l2(p1[liq], p0[liq]) <= 1e-8
+    psi1, H1, j1 = oracle.magnetic_solve(g, phi, 2.0, 2 * g.h, hext, tol=1e-10, solver="mgpcg")
+    psi0, H0, j0 = oracle.magnetic_solve(g, phi, 2.0, 2 * g.h, hext, tol=1e-13)
+    assert psi1.ravel()[0] == 0.0 and j1["iters"] <= 20
+    r = np.linalg.norm(j0["b"] - j0["A"].matvec(psi1.ravel())) / np.linalg.norm(j0["b"])
+    assert r <= 2e-10
+    assert rel_l2(psi1, psi0) <= 1e-8
