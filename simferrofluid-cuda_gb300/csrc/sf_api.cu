@@ -159,7 +159,7 @@ struct NetStep final : LearnedStep {
         const double rms = std::sqrt(rr / cnt);
         cudaError_t e = c->net->set_rhs_channel(d, r, rms > 0 ? 1.0 / rms : 0.0, feat);
         if (e != cudaSuccess) return e;
-        if ((e = c->net->forward(d, feat, y)) != cudaSuccess) return e;
+        if ((e = c->net->forward(d, feat, y, false)) != cudaSuccess) return e;
         if (c->net->mode() == 1 && (e = c->net->check_device_errors()) != cudaSuccess) return e;
         return cudaSuccess;
     }
@@ -994,7 +994,7 @@ sf_status sf_unet_forward_dev(void *net, const sf_grid *g, const void *features,
     auto *h = reinterpret_cast<NetHandle *>(net);
     if (!h || !h->ctx || !grid_ok(g) || !features || !out) return SF_BAD_ARG;
     Ctx *c = h->ctx;
-    CK(h->net->forward(make_dims(g->nx, g->ny, g->nz), (const __nv_bfloat16 *)features, out));
+    CK(h->net->forward(make_dims(g->nx, g->ny, g->nz), (const __nv_bfloat16 *)features, out, false));
     if (h->net->check_device_errors() != cudaSuccess) return fail(c, SF_CUDA_ERROR, h->net->last_error);
     return SF_OK;
 }

@@ -11,6 +11,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include "sf_convert.cuh"
+
 #include <cstdint>
 
 namespace sf {
@@ -21,6 +23,15 @@ struct Dims {
 };
 
 static inline Dims make_dims(int nx, int ny, int nz) { return Dims{nx, ny, nz, (long long)nx * ny * nz}; }
+
+// An FP64 value stored at precision T: float through the integer-pipe conversion (sf_convert.cuh), double as is.
+template <class T>
+__device__ __forceinline__ T to_prec(double v) {
+    if constexpr (std::is_same<T, float>::value)
+        return f64_to_f32(v);
+    else
+        return (T)v;
+}
 
 __host__ __device__ __forceinline__ long long cid(const Dims &d, int i, int j, int k) {
     return (long long)k + (long long)d.nz * ((long long)j + (long long)d.ny * i);

@@ -913,10 +913,10 @@ __global__ void __launch_bounds__(256) k_coarsen(Dims d, Coef<CF> f, Dims dc, Co
 // FP64 level 0 -> FP32 copy (mixed form).
 __global__ void k_to32(long long n, Coef<double> f, Coef<float> o) {
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-        o.ax[c] = (float)f.ax[c];
-        o.ay[c] = (float)f.ay[c];
-        o.az[c] = (float)f.az[c];
-        o.dex[c] = (float)f.dex[c];
+        o.ax[c] = f64_to_f32(f.ax[c]);
+        o.ay[c] = f64_to_f32(f.ay[c]);
+        o.az[c] = f64_to_f32(f.az[c]);
+        o.dex[c] = f64_to_f32(f.dex[c]);
     }
 }
 
@@ -924,10 +924,10 @@ __global__ void k_to32(long long n, Coef<double> f, Coef<float> o) {
 // stay below 6000, couplings in [0, 1 + chi]).
 __global__ void k_to16(long long n, Coef<double> f, Coef<__half> o) {
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-        o.ax[c] = __float2half_rn((float)f.ax[c]);
-        o.ay[c] = __float2half_rn((float)f.ay[c]);
-        o.az[c] = __float2half_rn((float)f.az[c]);
-        o.dex[c] = __float2half_rn((float)f.dex[c]);
+        o.ax[c] = __float2half_rn(f64_to_f32(f.ax[c]));
+        o.ay[c] = __float2half_rn(f64_to_f32(f.ay[c]));
+        o.az[c] = __float2half_rn(f64_to_f32(f.az[c]));
+        o.dex[c] = __float2half_rn(f64_to_f32(f.dex[c]));
     }
 }
 
@@ -1203,7 +1203,7 @@ __global__ void __launch_bounds__(256) k_cast_rhs(long long n, const double *__r
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     for (long long c = blockIdx.x * 256LL + tid; c < n; c += (long long)gridDim.x * 256) {
         const double bc = b[c];
-        r[c] = (TR)bc;
+        r[c] = to_prec<TR>(bc);
         v[0] += bc * bc;
     }
     double tot[1];
@@ -1339,6 +1339,7 @@ static void rb(cudaStream_t st, Tracker &tk, bool fine, bool zero, const Dims &d
     const dim3 g = grid_pairs(d), bk = blk2();
     // algorithmic bytes of one colour: half of (x r/w + b + 3 couplings + diagonal term)
     const double per = (3.0 * sizeof(T) + 4.0 * sizeof(C)) / 2.0;
+    const double cells = (fine && rows && tk.active0 >= 0) ? tk.active0 : (double)d.n;  // rows skipped
     tk.before(st, fine);
     if constexpr (std::is_same<T, float>::value && sizeof(C) <= 4) {
         if (d.nz % 4 == 0) {  // rows start 16-byte aligned: z-vectorised kernel
@@ -1347,7 +1348,7 @@ static void rb(cudaStream_t st, Tracker &tk, bool fine, bool zero, const Dims &d
                 launch_pdl(k_rbgs4<C, true>, g4, bk, st, d, cf, x, b, color, rows);
             else
                 launch_pdl(k_rbgs4<C, false>, g4, bk, st, d, cf, x, b, color, rows);
-            tk.after(st, fine, per * d.n);
+            tk.after(st, fine, per * cells);
             return;
         }
     }
@@ -1355,7 +1356,7 @@ static void rb(cudaStream_t st, Tracker &tk, bool fine, bool zero, const Dims &d
         launch_pdl(k_rbgs<T, C, true>, g, bk, st, d, cf, x, b, color, rows);
     else
         launch_pdl(k_rbgs<T, C, false>, g, bk, st, d, cf, x, b, color, rows);
-    tk.after(st, fine, per * d.n);
+    tk.after(st, fine, per * cells);
 }
 
 static inline int fused_chunk(const Dims &d) {
@@ -1978,6 +1979,16 @@ cudaError_t MGSolver::build_hierarchy() {
                 cudaMemsetAsync(b64_[l], 0, 8 * (size_t)dl.n, st_);
             }
             tk_.launches += L;
+            tk_.active0 = -1;
+            if (prm_.profile) {  // profiled runs synchronise anyway: the smoother's bytes over active rows only
+                std::vector<uint8_t> h((size_t)nr0);
+                cudaMemcpyAsync(h.data(), rows_[0], h.size(), cudaMemcpyDeviceToHost, st_);
+                const cudaError_t e = cudaStreamSynchronize(st_);
+                if (e != cudaSuccess) return e;
+                long long act = 0;
+                for (uint8_t v : h) act += v != 0;
+                tk_.active0 = (double)act * d0.nz;
+            }
         }
     } else {
         if (split0_) {

@@ -32,7 +32,8 @@ __device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong
 __device__ __forceinline__ void split_store(const SplitOut &so, const Dims &d, int i, int j, int k, double ax,
                                             double ay, double az, double dex, bool active) {
     const long long q = split_index(d, i, j, k);
-    const float fx = (float)ax, fy = (float)ay, fz = (float)az, fd = (float)dex;
+    // converted on the integer pipe: this kernel is FP64-bound (same bits as the hardware conversion)
+    const float fx = f64_to_f32(ax), fy = f64_to_f32(ay), fz = f64_to_f32(az), fd = f64_to_f32(dex);
     so.c32.ax[q] = fx;
     so.c32.ay[q] = fy;
     so.c32.az[q] = fz;
@@ -572,7 +573,7 @@ void launch_total_field(cudaStream_t st, const Dims &d, const double *psi, const
 
 __global__ void k_to_f32(long long n, const double *__restrict__ a, float *__restrict__ o) {
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
-        o[c] = (float)a[c];
+        o[c] = f64_to_f32(a[c]);
 }
 
 void launch_to_f32(cudaStream_t st, long long n, const double *a, float *o) {

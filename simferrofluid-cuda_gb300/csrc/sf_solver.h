@@ -44,7 +44,9 @@ struct Tracker {
     // profile: algorithmic bytes of one split level-0 half sweep, counted over the rows it processes and by row
     // kind (-1: not set, every cell at the general rate)
     double bytes0 = -1;
-    bool tail_failed = false;  // a fused-tail cluster launch was rejected (the separate kernels ran instead)
+    bool tail_failed = false;
+    // profile, FP64 form with row skipping: cells in active rows of level 0 (-1: every cell counts)
+    double active0 = -1;  // a fused-tail cluster launch was rejected (the separate kernels ran instead)
     void before(cudaStream_t st, bool fine);
     void after(cudaStream_t st, bool fine, double algo_bytes);
     // after a stream sync: summed milliseconds, launch count and algorithmic bytes of the bracketed

@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(256) k_to_split(Dims d, Coef<double> f, Coef<f
             __half *d16[4] = {o16.ax, o16.ay, o16.az, o16.dex};
 #pragma unroll
             for (int a = 0; a < 4; a++) {
-                const float v0 = (float)src[a][n0], v1 = (float)src[a][n1];
+                const float v0 = f64_to_f32(src[a][n0]), v1 = f64_to_f32(src[a][n1]);
                 d32[a][s0] = v0;
                 d32[a][s1] = v1;
                 d16[a][s0] = __float2half_rn(v0);
@@ -276,8 +276,8 @@ __global__ void __launch_bounds__(256) k_cast_rhs_s(Dims d, const double *__rest
     double v[1] = {0};
     SPLIT_ROWS(d)
     const double b0 = b[n0], b1 = b[n1];
-    r[s0] = (float)b0;
-    r[s1] = (float)b1;
+    r[s0] = f64_to_f32(b0);
+    r[s1] = f64_to_f32(b1);
     v[0] += b0 * b0;
     v[0] += b1 * b1;
     SPLIT_ROWS_END

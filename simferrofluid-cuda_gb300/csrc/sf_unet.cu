@@ -225,8 +225,9 @@ cudaError_t UNet::get_grads(float *host) {
     return cudaStreamSynchronize(st_);
 }
 
-cudaError_t UNet::ensure(const Dims &d) {
-    if (have_ws_ && dims_[0].nx == d.nx && dims_[0].ny == d.ny && dims_[0].nz == d.nz) return cudaSuccess;
+cudaError_t UNet::ensure(const Dims &d, bool training) {
+    if (have_ws_ && dims_[0].nx == d.nx && dims_[0].ny == d.ny && dims_[0].nz == d.nz && (ws_training_ || !training))
+        return cudaSuccess;
     for (void *p : ws_) cudaFree(p);
     ws_.clear();
     have_ws_ = false;
@@ -245,6 +246,23 @@ cudaError_t UNet::ensure(const Dims &d) {
     };
     const long long n0 = dims_[0].n, n1 = dims_[1].n, n2 = dims_[2].n, n3 = dims_[3].n;
     auto B = [&](long long n, int c) { return (bf16 *)A(2 * (size_t)n * c); };
+    if (!training) {
+        // each decoder tensor takes a buffer of its level that is dead by then: U = up(..) + S goes where the
+        // first encoder conv's output was, the first decoder conv's output where the skip S was, the second's
+        // where the level's pooled input was (level 0: the first encoder buffer again)
+        A0a = B(n0, 16); S0 = B(n0, 16); U0 = A0a; D0a = S0; D0b = A0a;
+        P1 = B(n1, 16); A1a = B(n1, 32); S1 = B(n1, 32); U1 = A1a; D1a = S1; D1b = P1;
+        P2 = B(n2, 32); A2a = B(n2, 64); S2 = B(n2, 64); U2 = A2a; D2a = S2; D2b = P2;
+        P3 = B(n3, 64); A3a = B(n3, 64); A3b = B(n3, 64);
+        out_ = dout_ = nullptr;
+        if (!ok) {
+            last_error = "U-Net workspace allocation failed";
+            return cudaErrorMemoryAllocation;
+        }
+        have_ws_ = true;
+        ws_training_ = false;
+        return cudaSuccess;
+    }
     A0a = B(n0, 16); S0 = B(n0, 16); U0 = B(n0, 16); D0a = B(n0, 16); D0b = B(n0, 16);
     P1 = B(n1, 16); A1a = B(n1, 32); S1 = B(n1, 32); U1 = B(n1, 32); D1a = B(n1, 32); D1b = B(n1, 16);
     P2 = B(n2, 32); A2a = B(n2, 64); S2 = B(n2, 64); U2 = B(n2, 64); D2a = B(n2, 64); D2b = B(n2, 32);
@@ -264,6 +282,7 @@ cudaError_t UNet::ensure(const Dims &d) {
         return cudaErrorMemoryAllocation;
     }
     have_ws_ = true;
+    ws_training_ = true;
     return cudaSuccess;
 }
 
@@ -293,8 +312,9 @@ cudaError_t UNet::check_device_errors() {
     return cudaSuccess;
 }
 
-cudaError_t UNet::forward(const Dims &d, const bf16 *feat, float *out) {
-    cudaError_t e = ensure(d);
+cudaError_t UNet::forward(const Dims &d, const bf16 *feat, float *out, bool training) {
+    if (!training && !out) return cudaErrorInvalidValue;
+    cudaError_t e = ensure(d, training);
     if (e != cudaSuccess) return e;
     feat_ = feat;
     const ConvLayer *Ls = layers_.data();
@@ -352,7 +372,7 @@ void UNet::conv_bwd(const ConvLayer &L, const Dims &d, const bf16 *x, const bf16
 }
 
 cudaError_t UNet::backward(const Dims &d, const float *dout) {
-    if (!have_ws_ || dims_[0].nx != d.nx || dims_[0].ny != d.ny || dims_[0].nz != d.nz)
+    if (!have_ws_ || !ws_training_ || dims_[0].nx != d.nx || dims_[0].ny != d.ny || dims_[0].nz != d.nz)
         return cudaErrorInvalidValue;
     const ConvLayer *Ls = layers_.data();
     const Dims &d0 = dims_[0], &d1 = dims_[1], &d2 = dims_[2], &d3 = dims_[3];

@@ -36,8 +36,10 @@ class UNet {
     cudaError_t get_params(float *host);
     cudaError_t get_grads(float *host);
 
-    // out[v] = net(features)[v]; features BF16 [n][16] on the device.
-    cudaError_t forward(const Dims &d, const __nv_bfloat16 *features, float *out);
+    // out[v] = net(features)[v]; features BF16 [n][16] on the device.  training = false (inference: out must be
+    // given) runs in a workspace whose decoder reuses the encoder's dead buffers and holds no gradients, about a
+    // quarter of the training workspace; a backward pass needs a training forward first.
+    cudaError_t forward(const Dims &d, const __nv_bfloat16 *features, float *out, bool training = true);
     // gradients of sum(dout * out) w.r.t. the parameters (after a forward on the same features)
     cudaError_t backward(const Dims &d, const float *dout);
     // one Adam step on the cosine loss 1 - (o.t)^2 / (|o|^2 |t|^2); returns the loss before the step
@@ -60,7 +62,7 @@ class UNet {
     std::string last_error;
 
    private:
-    cudaError_t ensure(const Dims &d);
+    cudaError_t ensure(const Dims &d, bool training);
     void conv_fwd(const ConvLayer &L, const Dims &d, const __nv_bfloat16 *x, __nv_bfloat16 *y);
     void conv_bwd(const ConvLayer &L, const Dims &d, const __nv_bfloat16 *x, const __nv_bfloat16 *post,
                   const float *dpost, float *dx /* nullable */);
@@ -76,7 +78,7 @@ class UNet {
     std::vector<void *> persist_;
     // per-grid workspace
     Dims dims_[4]{};
-    bool have_ws_ = false;
+    bool have_ws_ = false, ws_training_ = false;
     std::vector<void *> ws_;
     __nv_bfloat16 *A0a, *S0, *P1, *A1a, *S1, *P2, *A2a, *S2, *P3, *A3a, *A3b, *U2, *D2a, *D2b, *U1, *D1a, *D1b, *U0,
         *D0a, *D0b;

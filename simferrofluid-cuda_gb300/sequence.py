@@ -13,7 +13,11 @@ fast-marching distance near a wall is computed outward from the wall), so faces 
 wall take the interior value.  The extension agrees with the full-size collider to the last bits of the
 level-set arithmetic.
 
-  python -m <package>.sequence --n 768 --substeps 50
+  python simferrofluid-cuda_gb300/sequence.py --n 768 --substeps 50 --precision all
+
+Arms: the mixed form, the mixed form with the trained network's learned correction steps ("learned"), and the plain
+FP64 method with row skipping ("fp64") and sweeping every row ("fp64_full").  The learned arm runs the network's
+inference workspace (decoder buffers reuse the encoder's), about 90 B per cell at 768^3.
 """
 from __future__ import annotations
 
@@ -76,7 +80,9 @@ def smooth_velocity(torch, g, dev, gen, vmax=0.5, lattice=9):
     return out
 
 
-def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None):
+def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None, weights=None):
+    """precision "mixed", "fp64" (row skipping), "fp64_full" (every row swept) or "learned" (the mixed solver with
+    the trained network's correction steps, weights/unet.f32 unless `weights` names another file)."""
     import torch
     sf = _pkg()
     scenes = importlib.import_module(sf.__name__ + ".scenes")
@@ -94,6 +100,15 @@ def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None):
     torch.cuda.synchronize()
     setup_s = time.time() - t0
     ctx = sf.Context(0, stream=torch.cuda.current_stream().cuda_stream)
+    net = None
+    extra = {}
+    if precision == "learned":
+        net = sf.Network(ctx)
+        net.load(weights or os.path.join(HERE, "weights", "unet.f32"))
+        ctx.set_network(net)
+    elif precision == "fp64_full":
+        extra = dict(full_sweeps=1)
+    prec = {"fp64_full": "fp64"}.get(precision, precision)
     M = sf.MagneticField(g, 1.5, 2 * g.spacing, ctx)
     P = sf.Pressure(g, ctx)
     rows = []
@@ -105,16 +120,17 @@ def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None):
         prof = 1 if (profile_last and s == substeps) else 0
         e0.record()
         sm = M.solve(phi, hext, device=True, psi_out=psi, H_out=H,
-                     opts=sf.options("magnetic", precision=precision, profile=prof))
+                     opts=sf.options("magnetic", precision=prec, profile=prof, **extra))
         e1.record()
         sp = P.project(vel, phi, frac, device=True, p_out=p_out,
-                       opts=sf.options("pressure", precision=precision, tol=1e-6, profile=prof))
+                       opts=sf.options("pressure", precision=prec, tol=1e-6, profile=prof, **extra))
         e2.record()
         torch.cuda.synchronize()
         ms_m, ms_p = e0.elapsed_time(e1), e1.elapsed_time(e2)
         if not prof:
             solve_ms += ms_m + ms_p
         rows.append(dict(substep=s, mag_iters=sm["iters"], mag_ms=ms_m, mag_relres=sm["rel_residual_ref"],
+                         learned_steps=(sm["learned_steps"], sp["learned_steps"]),
                          pres_iters=sp["iters"], pres_ms=ms_p, pres_relres=sp["rel_residual"],
                          smooth_ms=sm["smooth_ms"] + sp["smooth_ms"], smooth_bytes=sm["smooth_bytes"] + sp["smooth_bytes"],
                          smooth_launches=sm["smooth_launches"] + sp["smooth_launches"]))
@@ -134,10 +150,15 @@ def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None):
                max_rel_residual=dict(potential=max(r["mag_relres"] for r in rows),
                                      pressure=max(r["pres_relres"] for r in rows)),
                device_bytes=ctx.device_bytes())
+    if precision == "learned":
+        out["learned_steps"] = [r["learned_steps"] for r in rows]
     if profile_last and last["smooth_launches"]:
         out["smoother"] = dict(ms_per_launch=last["smooth_ms"] / last["smooth_launches"],
                                bytes_per_launch=last["smooth_bytes"] / last["smooth_launches"],
                                achieved_gbs=last["smooth_bytes"] / (last["smooth_ms"] / 1e3) / 1e9)
+    if net is not None:
+        ctx.set_network(None)
+        net.close()
     ctx.close()
     del phi, frac, hext, H, psi, p_out
     torch.cuda.empty_cache()
@@ -149,15 +170,26 @@ def main():
     ap.add_argument("--n", type=int, default=768)
     ap.add_argument("--substeps", type=int, default=50)
     ap.add_argument("--seed", type=int, default=5)
-    ap.add_argument("--precision", default="both", choices=["mixed", "fp64", "both"])
+    ap.add_argument("--precision", default="both", choices=["mixed", "fp64", "fp64_full", "learned", "both", "all"],
+                    help="both: mixed and fp64; all: mixed, learned, fp64 and fp64_full")
     ap.add_argument("--out", default=None)
     args = ap.parse_args()
     import torch
     torch.cuda.set_device(0)
-    precs = ["mixed", "fp64"] if args.precision == "both" else [args.precision]
-    res = {p: run(p, args.n, args.substeps, args.seed, log=lambda m: print(m, flush=True)) for p in precs}
-    if len(precs) == 2:
-        res["speedup_mixed_vs_fp64"] = round(res["fp64"]["solve_s"] / res["mixed"]["solve_s"], 3)
+    precs = {"both": ["mixed", "fp64"], "all": ["mixed", "learned", "fp64", "fp64_full"]}.get(args.precision,
+                                                                                             [args.precision])
+    res = {}
+    for p in precs:
+        try:
+            res[p] = run(p, args.n, args.substeps, args.seed, log=lambda m: print(m, flush=True))
+        except Exception as e:  # an arm that does not fit (device memory) is reported, the others still run
+            res[p] = {"error": f"{type(e).__name__}: {e}"}
+            torch.cuda.empty_cache()
+            print(f"{p}: {res[p]['error']}", flush=True)
+    for base in ("fp64", "fp64_full"):
+        for p in ("mixed", "learned"):
+            if base in res and p in res and "solve_s" in res[base] and "solve_s" in res[p]:
+                res[f"speedup_{p}_vs_{base}"] = round(res[base]["solve_s"] / res[p]["solve_s"], 3)
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -165,7 +197,7 @@ def main():
     except OSError:
         pass
     for p in precs:
-        if "smoother" in res[p] and peaks.get("hbm_gbs"):
+        if "smoother" in res.get(p, {}) and peaks.get("hbm_gbs"):
             res[p]["smoother"]["frac_of_measured_hbm"] = res[p]["smoother"]["achieved_gbs"] / peaks["hbm_gbs"]
     print(json.dumps(res), flush=True)
     if args.out:
