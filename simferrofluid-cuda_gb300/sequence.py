@@ -62,6 +62,28 @@ def box_fractions_device(sf, scenes, torch, g, dev, c=6):
     return out
 
 
+def box_normals_device(sf, scenes, torch, g, dev, c=6):
+    """The box collider's face normals (sf_collider_face_normals of the redistanced node level set) on a small grid,
+    extended to the full grid like the fractions: they matter only on faces of fraction 1, next to the walls."""
+    import ctypes as C
+    n = 2 * c
+    small = sf.StaggeredGrid.from_origin(g.spacing, (n, n, n))
+    lib = sf.load_library()
+    fs = [np.empty(small.face_shape(a)) for a in range(3)]
+    ls = np.empty((n + 1, n + 1, n + 1))
+    s = lib.sf_collider_box_fractions(C.byref(small.c_grid()), 0, sf._abi.p3([f.ctypes.data for f in fs]),
+                                      C.c_void_p(ls.ctypes.data))
+    if s != 0:
+        raise RuntimeError(f"sf_collider_box_fractions failed with status {s}")
+    nm = sf.collider_face_normals(small, ls)
+    out = []
+    for a in range(3):
+        idx = [torch.from_numpy(_stretch(g.shape[b] + (b == a), n + (b == a), c)).to(dev) for b in range(3)]
+        src = torch.from_numpy(nm[a]).to(dev)
+        out.append(src[idx[0]][:, idx[1]][:, :, idx[2]].contiguous())
+    return out
+
+
 def pool_phi_device(scenes, torch, g, dev, seed, depth=0.2, noise=0.01):
     rng = np.random.default_rng(seed)
     xs, ys, zs = (scenes.cell_centres(g, a) for a in range(3))
@@ -80,9 +102,14 @@ def smooth_velocity(torch, g, dev, gen, vmax=0.5, lattice=9):
     return out
 
 
-def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None, weights=None):
+def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None, weights=None, full_substep=False):
     """precision "mixed", "fp64" (row skipping), "fp64_full" (every row swept) or "learned" (the mixed solver with
-    the trained network's correction steps, weights/unet.f32 unless `weights` names another file)."""
+    the trained network's correction steps, weights/unet.f32 unless `weights` names another file).
+
+    full_substep: after the two solves, the rest of the reference's substep on the device (core/Simulation.cpp:
+    164-165, 236-241, 265): extrapolation of the projected velocity, Collider::Enforce, advection of the level set
+    and of the velocity (dt = h / max|u|, |u| <= 0.5) and 10 reinitialisation steps.  They run on copies of phi,
+    so every substep solves the same scene; their device time is reported apart (`rest_ms`)."""
     import torch
     sf = _pkg()
     scenes = importlib.import_module(sf.__name__ + ".scenes")
@@ -111,6 +138,12 @@ def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None, weig
     prec = {"fp64_full": "fp64"}.get(precision, precision)
     M = sf.MagneticField(g, 1.5, 2 * g.spacing, ctx)
     P = sf.Pressure(g, ctx)
+    if full_substep:
+        normals = box_normals_device(sf, scenes, torch, g, dev)
+        ext, enf = sf.Extrapolation(g, ctx), sf.ColliderEnforce(g, frac, normals, ctx=ctx)
+        adv, rei = sf.Advection(g, ctx), sf.Reinitialization(g, ctx)
+        e3 = torch.cuda.Event(enable_timing=True)
+        rest = []
     rows = []
     e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
     solve_ms = 0.0
@@ -125,8 +158,19 @@ def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None, weig
         sp = P.project(vel, phi, frac, device=True, p_out=p_out,
                        opts=sf.options("pressure", precision=prec, tol=1e-6, profile=prof, **extra))
         e2.record()
+        if full_substep:
+            ext.solve(vel, phi, frac, device=True)
+            enf.enforce(vel, device=True)
+            phi_w = phi.clone()
+            adv.solve_levelset(phi_w, vel, g.spacing, device=True)
+            adv.solve_velocity(vel, g.spacing, device=True)
+            rei.solve(phi_w, 10, device=True)
+            e3.record()
         torch.cuda.synchronize()
         ms_m, ms_p = e0.elapsed_time(e1), e1.elapsed_time(e2)
+        if full_substep:
+            rest.append(e2.elapsed_time(e3))
+            del phi_w
         if not prof:
             solve_ms += ms_m + ms_p
         rows.append(dict(substep=s, mag_iters=sm["iters"], mag_ms=ms_m, mag_relres=sm["rel_residual_ref"],
@@ -152,6 +196,8 @@ def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None, weig
                device_bytes=ctx.device_bytes())
     if precision == "learned":
         out["learned_steps"] = [r["learned_steps"] for r in rows]
+    if full_substep:
+        out["rest_ms"] = float(np.mean(rest))
     if profile_last and last["smooth_launches"]:
         out["smoother"] = dict(ms_per_launch=last["smooth_ms"] / last["smooth_launches"],
                                bytes_per_launch=last["smooth_bytes"] / last["smooth_launches"],
@@ -173,6 +219,8 @@ def main():
     ap.add_argument("--precision", default="both", choices=["mixed", "fp64", "fp64_full", "learned", "both", "all"],
                     help="both: mixed and fp64; all: mixed, learned, fp64 and fp64_full")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--full-substep", action="store_true",
+                    help="also run the rest of the substep (extrapolation, enforcement, advection, reinitialisation)")
     args = ap.parse_args()
     import torch
     torch.cuda.set_device(0)
@@ -181,7 +229,8 @@ def main():
     res = {}
     for p in precs:
         try:
-            res[p] = run(p, args.n, args.substeps, args.seed, log=lambda m: print(m, flush=True))
+            res[p] = run(p, args.n, args.substeps, args.seed, log=lambda m: print(m, flush=True),
+                         full_substep=args.full_substep)
         except Exception as e:  # an arm that does not fit (device memory) is reported, the others still run
             res[p] = {"error": f"{type(e).__name__}: {e}"}
             torch.cuda.empty_cache()

@@ -173,6 +173,8 @@ def main():
     ap.add_argument("--eval", type=int, default=0, help="then evaluate on this many unseen scenes")
     ap.add_argument("--eval-n", type=int, default=256)
     ap.add_argument("--report", default=None, help="write the training/evaluation summary (JSON) here")
+    ap.add_argument("--tc", action="store_true",
+                    help="forward and input-gradient convolutions on the tcgen05 kernels (Network.set_mode(1))")
     args = ap.parse_args()
     sf = _pkg()
     import torch
@@ -190,8 +192,10 @@ def main():
             flat.append((from_rng.standard_normal(taps * co * ci) * std).astype(np.float32))
             flat.append(np.zeros(co, np.float32))
         net.set_params(np.concatenate(flat))
+    if args.tc:
+        net.set_mode(1)
     ctx.set_network(net)
-    report = {"samples": args.samples, "n": args.n, "lr": args.lr, "seed": args.seed}
+    report = {"samples": args.samples, "n": args.n, "lr": args.lr, "seed": args.seed, "tcgen05": bool(args.tc)}
     if args.samples > 0:
         t0 = time.time()
         losses = train(ctx, net, args.samples, args.n, args.lr, args.seed, log=lambda m: print(m, flush=True))
