@@ -308,7 +308,6 @@ enum Slot {
     S_RPREV,
     S_SLOW,
     S_STAG,    // 1: the loop ends on FP32 stagnation (mixed form), 0: no stagnation test (FP64 form)
-    S_PQG,     // (p, A p) over the general rows of the split level (the uniform rows' kernel adds the rest)
     S_NSLOTS = 32
 };
 

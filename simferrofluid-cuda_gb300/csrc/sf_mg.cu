@@ -1866,7 +1866,7 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
         const bool split1 = split0 && L >= 3 && dims[1].nz % 8 == 0;
         if (split0) {
             for (int l = 0; l < (split1 ? 3 : 2); l++) list_[l] = (int *)chk(A(4 * (size_t)dims[l].nx * dims[l].ny));
-            count_ = (int *)chk(A(8 * sizeof(int)));  // totals [0, 3), general rows [kGenCount, +3)
+            count_ = (int *)chk(A(16));
             crow_ = (float *)chk(A(4 * (size_t)dims[0].nx * dims[0].ny));
             rc_[0] = (float4 *)chk(A(16 * (size_t)dims[0].nx * dims[0].ny));
             dinv_[0] = (float *)chk(A(4 * (size_t)dims[0].n));
@@ -1914,8 +1914,7 @@ cudaError_t MGSolver::configure(const Dims &d, const SolverParams &p) {
         const void *ks[] = {(const void *)k_rbgs4s<__half, true>, (const void *)k_rbgs4s<__half, false>,
                             (const void *)k_resid_restrict_s<__half, false>,
                             (const void *)k_resid_restrict_s<__half, true>, (const void *)k_prolong_s,
-                            (const void *)k_prolong_ss, (const void *)k_apply_dot4s<false>,
-                            (const void *)k_apply_dot4s<true>, (const void *)k_dot_rz_s,
+                            (const void *)k_prolong_ss, (const void *)k_apply_dot4s, (const void *)k_dot_rz_s,
                             (const void *)k_xpby_s, (const void *)k_update_s, (const void *)k_ir_update_s};
         for (const void *k : ks) resident_grid(k);
     }
@@ -2114,7 +2113,7 @@ void MGSolver::enqueue_iter32(bool copy_slots) {
         apply_dot32s(st_, d, c32_, p32_, q32_, lst0, cnt0, crow_, sc_, part_, ticket_);
         launch_pdl(k_update_s, row_grid((const void *)k_update_s, vitems), dim3(32, 8), st_, d, d32_, ri32_, p32_,
                    q32_, lst0, cnt0, sc_, part_, ticket_);
-        tk_.launches += 5;  // k_apply_dot4s is two launches
+        tk_.launches += 4;
         iter_launches32_ = tk_.launches - l0;
         if (copy_slots) cudaMemcpyAsync(sc_host_, sc_, 8 * S_NSLOTS, cudaMemcpyDeviceToHost, st_);
         return;

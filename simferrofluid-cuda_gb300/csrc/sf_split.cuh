@@ -46,9 +46,8 @@ static inline int split_rows_grid(const Dims &d) {
 // ny < 2^16); *count = their number.  Rows of one segment cost the same,
 // so the persistent kernels' round-robin split of the list gives every warp an equal share of each kind.
 // Two kernels over blocks of 1024 rows: per-block counts of each kind, then each block's entries at the offsets
-// the counts give (deterministic).  count[kGenCount] = the number of general rows.
+// the counts give (deterministic).
 constexpr int kListRows = 1024;
-constexpr int kGenCount = 4;  // the counts' array: [0, 3) totals of levels 0..2, [4, 7) their general rows
 __global__ void __launch_bounds__(kListRows) k_rows_count(long long nrows, const uint8_t *__restrict__ rows,
                                                           int *__restrict__ cnt) {
     const long long r = blockIdx.x * (long long)kListRows + threadIdx.x;
@@ -84,10 +83,7 @@ __global__ void __launch_bounds__(kListRows) k_rows_scatter(long long nrows, int
         if (lane == 0) {
             off[0] = g_before;
             off[1] = g_all + u_before;
-            if (blockIdx.x == 0) {
-                count[0] = g_all + u_all;
-                count[kGenCount] = g_all;  // the general rows, listed first
-            }
+            if (blockIdx.x == 0) *count = g_all + u_all;
         }
     }
     const long long r = blockIdx.x * (long long)kListRows + t;
@@ -141,39 +137,6 @@ __device__ __forceinline__ void for_list_items(const int *__restrict__ list, con
         unsigned rr, ch;
         split(it, rr, ch);
         f(rr >= n ? 1 : 0, (e >> 16) & 0x7fff, e & 0xffff, (int)ch, e < 0);
-        e = e_next;
-    }
-}
-
-// The same loop over one segment of the list: seg 0 the general rows, 1 the uniform rows.
-template <class F>
-__device__ __forceinline__ void for_list_segment(const int *__restrict__ list, const int *__restrict__ count, int seg,
-                                                 int reps, int nch, F &&f) {
-    const unsigned n = (unsigned)count[0], g = (unsigned)count[kGenCount];
-    const unsigned lo = seg ? g : 0u, m = seg ? n - g : g;
-    const unsigned nit = reps * m * (unsigned)nch, stride = gridDim.x * blockDim.y;
-    auto split = [&](unsigned it, unsigned &rr, unsigned &ch) {
-        if (nch == 1) {
-            rr = it;
-            ch = 0;
-        } else {
-            rr = it / (unsigned)nch;
-            ch = it - rr * (unsigned)nch;
-        }
-    };
-    auto entry = [&](unsigned it) {
-        if (it >= nit) return 0;
-        unsigned rr, ch;
-        split(it, rr, ch);
-        return list[lo + (rr >= m ? rr - m : rr)];
-    };
-    unsigned it = blockIdx.x * blockDim.y + threadIdx.y;
-    int e = entry(it);
-    for (; it < nit; it += stride) {
-        const int e_next = entry(it + stride);
-        unsigned rr, ch;
-        split(it, rr, ch);
-        f(rr >= m ? 1 : 0, (e >> 16) & 0x7fff, e & 0xffff, (int)ch, e < 0);
         e = e_next;
     }
 }
@@ -963,28 +926,23 @@ __global__ void __launch_bounds__(256) k_prolong_ss(Dims d, float *__restrict__ 
 
 // q = A p and (p, q) on the split FP32 level-0 operator (the counterpart of k_apply_dot4; each cell's q as in
 // k_apply_dot).  Persistent: warps over (colour row, chunk of 32 vectors), rows without an active cell skipped
-// (q stays zero there).  Two launches, one per segment of the row list: UNI = false the general rows (their
-// operator loads need 80 registers a thread: three blocks per SM), then UNI = true the uniform rows (no operator
-// loads: more blocks per SM to cover the latency of the neighbour loads), whose last block adds the general
-// rows' (p, q) and forms alpha.
-template <bool UNI>
-__global__ void __launch_bounds__(256, UNI ? 5 : 3) k_apply_dot4s(Dims d, Coef<float> cf, const float *__restrict__ p,
-                                                               float *__restrict__ q, const int *__restrict__ list,
-                                                               const int *__restrict__ count,
-                                                               const float *__restrict__ crow, double *sc,
-                                                               double *part, unsigned *ticket) {
+// (q stays zero there).
+__global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, const float *__restrict__ p,
+                                                     float *__restrict__ q, const int *__restrict__ list,
+                                                     const int *__restrict__ count, const float *__restrict__ crow,
+                                                     double *sc, double *part, unsigned *ticket) {
     pdl_entry();
     float acc = 0.f;
     const int nh = d.nz >> 1, nq = nh >> 2;
-    for_list_segment(list, count, UNI ? 1 : 0, 2, (nq + 31) / 32, [&](int col, int i, int j, int ch, bool) {
+    for_list_items(list, count, 2, (nq + 31) / 32, [&](int col, int i, int j, int ch, bool uni) {
         const int q4 = ch * 32 + threadIdx.x;
         if (q4 >= nq) return;
         const long long rw = (long long)i * d.ny + j;
         const int m0 = 4 * q4;
-        if constexpr (UNI) {
+        if (uni) {
             apply4s_uniform(d, crow[rw], p, q, col, i, j, m0, acc);
             return;
-        } else {
+        }
         const long long sx = (long long)d.ny * nh, sy = nh;
         const bool yl = j > 0, yu = j < d.ny - 1;
         {
@@ -1059,19 +1017,13 @@ __global__ void __launch_bounds__(256, UNI ? 5 : 3) k_apply_dot4s(Dims d, Coef<f
                 body(std::integral_constant<int, 1>{});
             *reinterpret_cast<float4 *>(q + own) = make_float4(out[0], out[1], out[2], out[3]);
         }
-        }
     });
     float v[1] = {acc};
     double tot[1];
     if (grid_reduce<1>(v, part, ticket, tot)) {
-        if (!UNI) {
-            sc[S_PQG] = tot[0];
-            return;
-        }
-        const double pq = sc[S_PQG] + tot[0];
-        sc[S_PQ] = pq;
-        if (pq > 0 && isfinite(pq)) {
-            sc[S_ALPHA] = sc[S_RHO] / pq;
+        sc[S_PQ] = tot[0];
+        if (tot[0] > 0 && isfinite(tot[0])) {
+            sc[S_ALPHA] = sc[S_RHO] / tot[0];
         } else {
             sc[S_ALPHA] = 0;
             sc[S_AUX0] = 1;  // breakdown
@@ -1128,13 +1080,9 @@ __global__ void __launch_bounds__(256) k_coarsen_s(Dims d, Coef<float> f, Dims d
 // Items of the persistent split kernels: rows x chunks of 32 float4.
 static inline long long split_items(long long nrows, int nq) { return nrows * ((nq + 31) / 32); }
 
-// two launches (general rows, then uniform rows; see k_apply_dot4s)
 static void apply_dot32s(cudaStream_t st, const Dims &d, const Coef<float> &cf, const float *p, float *q,
                          const int *list, const int *count, const float *crow, double *sc, double *part,
                          unsigned *ticket) {
-    const long long items = split_items(2LL * d.nx * d.ny, d.nz >> 3);
-    launch_pdl(k_apply_dot4s<false>, row_grid((const void *)k_apply_dot4s<false>, items), dim3(32, 8), st, d, cf, p,
-               q, list, count, crow, sc, part, ticket);
-    launch_pdl(k_apply_dot4s<true>, row_grid((const void *)k_apply_dot4s<true>, items), dim3(32, 8), st, d, cf, p, q,
-               list, count, crow, sc, part, ticket);
+    const int g = row_grid((const void *)k_apply_dot4s, split_items(2LL * d.nx * d.ny, d.nz >> 3));
+    launch_pdl(k_apply_dot4s, g, dim3(32, 8), st, d, cf, p, q, list, count, crow, sc, part, ticket);
 }
