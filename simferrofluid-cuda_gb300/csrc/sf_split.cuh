@@ -625,6 +625,37 @@ __device__ __forceinline__ void apply4s_uniform(const Dims &d, float c, const fl
     *reinterpret_cast<float4 *>(q + own) = make_float4(out[0], out[1], out[2], out[3]);
 }
 
+// Both colours of a uniform row at once: cells m0 .. m0 + 3 of colour 0 and of colour 1 of row (i, j).  The
+// neighbour rows of one colour are the other colour's, so the two colours' loads serve each other (the own
+// values are the other colour's z row) and p is read from DRAM once per launch instead of once per colour.  Each
+// cell's q is apply4s_uniform's.
+__device__ __forceinline__ void apply4s_uniform2(const Dims &d, float c, const float *__restrict__ p,
+                                                 float *__restrict__ q, int i, int j, int m0, float &acc) {
+    const int nh = d.nz >> 1;
+    const long long row = ((long long)i * d.ny + j) * nh + m0, hn = d.n >> 1;
+    const int qz0 = (i + j) & 1;
+    Nb4 v0, v1;  // v0: the colour-1 rows around colour 0 (v0.zo = colour 1's own row); v1 the converse
+    load_nb4(d, p, hn + row, i, j, m0, qz0, v0);
+    load_nb4(d, p, row, i, j, m0, qz0 ^ 1, v1);
+    float out0[4], out1[4];
+    for_cells4(qz0, [&](auto qc, auto tc) {
+        constexpr int QZ = decltype(qc)::value, t = decltype(tc)::value;
+        float s, n;
+        nb_sum<QZ, t>(d, v0, i, j, m0, true, s, n);
+        out0[t] = (c * n) * v1.zo[t] - c * s;
+        acc += v1.zo[t] * out0[t];
+    });
+    for_cells4(qz0 ^ 1, [&](auto qc, auto tc) {
+        constexpr int QZ = decltype(qc)::value, t = decltype(tc)::value;
+        float s, n;
+        nb_sum<QZ, t>(d, v1, i, j, m0, true, s, n);
+        out1[t] = (c * n) * v0.zo[t] - c * s;
+        acc += v0.zo[t] * out1[t];
+    });
+    *reinterpret_cast<float4 *>(q + row) = make_float4(out0[0], out0[1], out0[2], out0[3]);
+    *reinterpret_cast<float4 *>(q + hn + row) = make_float4(out1[0], out1[1], out1[2], out1[3]);
+}
+
 // Red-black half sweep of colour `col` in the split layout (the counterpart of k_rbgs4), on the four
 // colour-`col` cells m0 .. m0 + 3 of row (i, j); QZ = (i + j + col) & 1 is uniform over a warp (one row) and
 // selects where the z neighbours sit.
@@ -926,7 +957,8 @@ __global__ void __launch_bounds__(256) k_prolong_ss(Dims d, float *__restrict__ 
 
 // q = A p and (p, q) on the split FP32 level-0 operator (the counterpart of k_apply_dot4; each cell's q as in
 // k_apply_dot).  Persistent: warps over (colour row, chunk of 32 vectors), rows without an active cell skipped
-// (q stays zero there).
+// (q stays zero there).  Uniform rows are done for both colours in the colour-0 pass (apply4s_uniform2), so the
+// colour-1 pass reads only the general rows again.
 __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, const float *__restrict__ p,
                                                      float *__restrict__ q, const int *__restrict__ list,
                                                      const int *__restrict__ count, const float *__restrict__ crow,
@@ -939,8 +971,8 @@ __global__ void __launch_bounds__(256, 3) k_apply_dot4s(Dims d, Coef<float> cf, 
         if (q4 >= nq) return;
         const long long rw = (long long)i * d.ny + j;
         const int m0 = 4 * q4;
-        if (uni) {
-            apply4s_uniform(d, crow[rw], p, q, col, i, j, m0, acc);
+        if (uni) {  // both colours in the colour-0 pass
+            if (col == 0) apply4s_uniform2(d, crow[rw], p, q, i, j, m0, acc);
             return;
         }
         const long long sx = (long long)d.ny * nh, sy = nh;
