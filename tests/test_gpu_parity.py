@@ -301,14 +301,15 @@ def test_split_level_matches_natural(sfpkg, gpu_ctx, shape):
 
 @pytest.mark.parametrize("smoother", [2, 3])
 @pytest.mark.parametrize("shape", [(64, 64, 64), (50, 44, 40), (96, 80, 72), (37, 21, 70), (20, 16, 76),
-                                   (80, 80, 80), (9, 13, 8)])
+                                   (80, 80, 80), (9, 13, 8), (192, 192, 192)])
 def test_cluster_tail_bit_identical(sfpkg, gpu_ctx, smoother, shape):
     """The mixed V-cycle's levels of at most 65,536 cells run by default in one launch of a thread-block cluster
     (coarse_tail 0: 16 CTAs where the device runs it, else 8; 8 and 16 force the size); coarse_tail=1 runs them as
     separate kernels.  Every cell's arithmetic is the same, so all forms take the same iterations and return the
     same bits.  The shapes give tails of two to five levels: all held by CTA 0, distributed over the cluster
     then held by CTA 0, and (80^3 with smoother 2) two distributed levels; shares of unequal plane counts across
-    the cluster, odd nz, and (9, 13, 8) a hierarchy too short for a tail (same launches)."""
+    the cluster, odd nz, and (9, 13, 8) a hierarchy too short for a tail (same launches); 192^3 with smoother 3
+    has two split levels above the tail."""
     g = sfpkg.StaggeredGrid.from_origin(1.0 / shape[0], shape)
     rng = np.random.default_rng(sum(shape) + 11)
     ys = scenes().cell_centres(g, 1)
