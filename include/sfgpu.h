@@ -77,7 +77,8 @@ typedef struct {
     int use_graph;       /* capture one PCG iteration in a CUDA graph (default 1) */
     int check_every;     /* read the residual norm back every k iterations (default 1) */
     int report_ref_residual; /* also compute the residual on the reference's own operator (default 1) */
-    double inner_tol;    /* mixed: floor of the inner relative reduction (default 1e-4) */
+    double inner_tol;    /* mixed: floor of the inner relative reduction (default 1e-3: the FP32 inner flexible CG
+                            stagnates near 1e-4 on large grids, and an earlier FP64 refinement step restarts it) */
     int profile;         /* time every finest-level smoother launch with CUDA events (disables graphs) */
     int smoother;        /* 0: two in-place colour passes, 1: fused one-pass red-black sweep (TMA-staged at the
                             finest FP32 level), 2: as 0, and in the mixed form the finest level's smoother reads

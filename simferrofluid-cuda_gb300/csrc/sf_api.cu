@@ -692,7 +692,7 @@ void sf_default_opts(sf_solve_opts *o, int which) {
     o->use_graph = 1;
     o->check_every = 1;
     o->report_ref_residual = 1;
-    o->inner_tol = 1e-4;
+    o->inner_tol = 1e-3;
     o->smoother = 3;  // mixed form: FP16 smoothing copy, colour-split finest level; FP64: two colour passes
 }
 

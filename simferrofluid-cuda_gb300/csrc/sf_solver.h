@@ -24,7 +24,7 @@ struct SolverParams {
     int max_levels = 0, coarse_dim = 8;
     bool use_graph = true;
     int check_every = 1;
-    double inner_tol = 1e-4;
+    double inner_tol = 1e-3;
     bool flexible = false;  // Polak-Ribiere beta (needed when the preconditioner is not a fixed SPD operator)
     bool profile = false;   // time finest-level smoother launches with events (no graphs)
     int smoother = 0;       // 0: two in-place colour kernels, 1: fused one-pass red-black sweep

@@ -103,7 +103,7 @@ def smooth_velocity(torch, g, dev, gen, vmax=0.5, lattice=9):
 
 
 def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None, weights=None, full_substep=False,
-        use_graph=1):
+        use_graph=1, inner_tol=None):
     """precision "mixed", "fp64" (row skipping), "fp64_full" (every row swept) or "learned" (the mixed solver with
     the trained network's correction steps, weights/unet.f32 unless `weights` names another file).
 
@@ -138,6 +138,8 @@ def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None, weig
         extra = dict(full_sweeps=1)
     prec = {"fp64_full": "fp64"}.get(precision, precision)
     extra["use_graph"] = use_graph
+    if inner_tol is not None and precision in ("mixed", "learned"):
+        extra["inner_tol"] = inner_tol
     M = sf.MagneticField(g, 1.5, 2 * g.spacing, ctx)
     P = sf.Pressure(g, ctx)
     if full_substep:
@@ -221,6 +223,8 @@ def main():
     ap.add_argument("--precision", default="both", choices=["mixed", "fp64", "fp64_full", "learned", "both", "all"],
                     help="both: mixed and fp64; all: mixed, learned, fp64 and fp64_full")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--inner-tol", type=float, default=None,
+                    help="mixed and learned arms: floor of the inner relative reduction (library default 1e-3)")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch each solver iteration's kernels from the host (for kernel profilers)")
     ap.add_argument("--full-substep", action="store_true",
@@ -234,7 +238,8 @@ def main():
     for p in precs:
         try:
             res[p] = run(p, args.n, args.substeps, args.seed, log=lambda m: print(m, flush=True),
-                         full_substep=args.full_substep, use_graph=0 if args.no_graph else 1)
+                         full_substep=args.full_substep, use_graph=0 if args.no_graph else 1,
+                         inner_tol=args.inner_tol)
         except Exception as e:  # an arm that does not fit (device memory) is reported, the others still run
             res[p] = {"error": f"{type(e).__name__}: {e}"}
             torch.cuda.empty_cache()
