@@ -1,14 +1,15 @@
 // sf_conv_tc.cuh -- 3x3x3 convolution forward on the 5th-generation tensor cores (tcgen05 + TMA, sm_103a).
 //
-// Implicit GEMM per CTA: M = 128 output voxels (a 32 (z) x 4 (y) x 1 (x) brick), N = Cout, K = 27 taps x Cin.
-// Operands are staged by TMA in the no-swizzle K-major "core matrix" layout: one 4-D box of 8 channels x
-// (32 x 4 x 1) voxels per 8-channel chunk and tap lands as 128 rows x 16 B, i.e. 8-row x 16-B core matrices
-// with a 128-B stride along M and one 2-KB chunk per 8 channels along K; taps outside the grid are filled with
-// zeros by the TMA unit (the convolution's zero padding).  Weights [tap][Cout][Cin] are staged the same way.
-// One thread issues TMA loads and tcgen05.mma (M=128, N=Cout, K=16, BF16 in, FP32 accumulate in TMEM) through
-// a ring of stages guarded by mbarriers; all four warps read the accumulator back with tcgen05.ld and apply
-// bias + ReLU + BF16 conversion.  Every wait is bounded: on timeout the CTA records an error code and returns
-// after releasing its tensor memory.
+// Implicit GEMM per CTA: MT tiles of M = 128 output voxels (a 32 (z) x 4 MT (y) x 1 (x) brick), N = Cout,
+// K = 27 taps x Cin.  Operands are staged by TMA in the no-swizzle K-major "core matrix" layout: one 4-D box of
+// 8 channels x (32 x 4 MT x 1) voxels per 8-channel chunk and tap lands as 128 MT rows x 16 B, i.e. 8-row x 16-B
+// core matrices with a 128-B stride along M, one tile per 2 KB and one (2 MT)-KB chunk per 8 channels along K;
+// taps outside the grid are filled with zeros by the TMA unit (the convolution's zero padding).  Weights
+// [tap][Cout][Cin] are staged the same way, once per tap for all MT tiles.  One thread issues TMA loads and
+// tcgen05.mma (M=128, N=Cout, K=16, BF16 in, FP32 accumulate in TMEM, one accumulator of Cout columns per tile)
+// through a ring of stages guarded by mbarriers; all four warps read the accumulators back with tcgen05.ld and
+// apply bias + ReLU + BF16 conversion.  Every wait is bounded: on timeout the CTA records an error code and
+// returns after releasing its tensor memory.
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -22,8 +23,7 @@
 namespace sf {
 namespace tc {
 
-constexpr int kStages = 4;
-constexpr int kTmemCols = 64;          // FP32 accumulator columns (N <= 64)
+constexpr int kMaxStages = 4;
 // Shared-memory matrix descriptor, no swizzle, K-major: start, leading (K) and stride (M/N) byte offsets in
 // 16-byte units, descriptor version 1 (bits 46..48 = 0b001), swizzle mode 0.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo_bytes, uint32_t sbo_bytes) {
@@ -68,27 +68,49 @@ __device__ __forceinline__ void tmem_ld_x16(uint32_t taddr, float (&v)[16]) {
 
 constexpr int kTileZ = 32, kTileY = 4;
 
+// M tiles per CTA: four (the weights of a tap staged once for 512 voxels), two for 64 input channels, whose
+// stages are twice as large
 template <int CI, int CO>
+constexpr int tiles_per_cta() {
+    return CI == 64 ? 2 : 4;
+}
+
+template <int CI, int CO, int MT>
 struct Layout {
     static constexpr int kChunks = CI / 8;
-    static constexpr uint32_t kABytes = 128u * 16u * kChunks;  // 128 rows x 16 B per 8-channel chunk
+    static constexpr uint32_t kChunkBytes = 128u * 16u * MT;  // 128 MT rows x 16 B per 8-channel chunk
+    static constexpr uint32_t kABytes = kChunkBytes * kChunks;
     static constexpr uint32_t kBBytes = (uint32_t)CO * 16u * kChunks;
     static constexpr uint32_t kStageBytes = kABytes + kBBytes;
+    // stages within about 100 KB, so that two or more CTAs share an SM where the stages are small
+    static constexpr int kStages = (int)(100u * 1024u / kStageBytes) > kMaxStages ? kMaxStages
+                                   : (int)(100u * 1024u / kStageBytes) < 2    ? 2
+                                                                              : (int)(100u * 1024u / kStageBytes);
+    // accumulator columns: one Cout-wide block per tile, allocated as a power of two >= 32
+    static constexpr uint32_t kCols = (uint32_t)(MT * CO) <= 32u    ? 32u
+                                      : (uint32_t)(MT * CO) <= 64u  ? 64u
+                                      : (uint32_t)(MT * CO) <= 128u ? 128u
+                                      : (uint32_t)(MT * CO) <= 256u ? 256u
+                                                                    : 512u;
     static constexpr uint32_t kNeed = kStages * kStageBytes + 1024 /* alignment */ + 256 /* barriers */;
-    // at least 30 KB so that at most 7 CTAs share an SM: 7 x 64 TMEM columns <= 512
-    static constexpr uint32_t kSmemBytes = kNeed > 30u * 1024u ? kNeed : 30u * 1024u;
+    // enough shared memory that at most 512 / kCols CTAs share an SM, so every CTA's TMEM allocation fits
+    static constexpr uint32_t kMinSmem = 233472u / (512u / kCols + 1u) + 1024u;
+    static constexpr uint32_t kSmemBytes = kNeed > kMinSmem ? kNeed : kMinSmem;
+    static_assert(kSmemBytes <= 227u * 1024u, "shared memory");
+    static_assert(MT * CO <= 512, "TMEM columns");
 };
 
 // err: first error code of any CTA (1 = TMA/MMA wait timed out).
 // EPI 0: + bias, ReLU, BF16 out (forward).  EPI 1: FP32 out, no bias (input gradient, with the mirrored and
 // transposed weights).
-template <int CI, int CO, int EPI = 0>
+template <int CI, int CO, int EPI = 0, int MT = tiles_per_cta<CI, CO>()>
 __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUtensorMap tmap_x,
                                                     const __grid_constant__ CUtensorMap tmap_w, Dims d,
                                                     const float *__restrict__ bias, void *__restrict__ yout,
                                                     int *err) {
-    static_assert(CI % 16 == 0 && CO % 16 == 0 && CO <= kTmemCols, "shape");
-    using L = Layout<CI, CO>;
+    static_assert(CI % 16 == 0 && CO % 16 == 0 && CO <= 256, "shape");
+    using L = Layout<CI, CO, MT>;
+    constexpr int kStages = L::kStages;
     extern __shared__ uint8_t smem_raw[];
     // 1024-byte aligned stage buffers, barriers after them
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -97,9 +119,9 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kStages), done = smem_u32(bars + 2 * kStages);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    const int tiles_z = (d.nz + kTileZ - 1) / kTileZ, tiles_y = (d.ny + kTileY - 1) / kTileY;
+    const int tiles_z = (d.nz + kTileZ - 1) / kTileZ, tiles_y = (d.ny + kTileY * MT - 1) / (kTileY * MT);
     const int bz = blockIdx.x % tiles_z, by = (blockIdx.x / tiles_z) % tiles_y, bx = blockIdx.x / (tiles_z * tiles_y);
-    const int z0 = bz * kTileZ, y0 = by * kTileY, x0 = bx;
+    const int z0 = bz * kTileZ, y0 = by * kTileY * MT, x0 = bx;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; s++) {
@@ -112,7 +134,7 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(kTmemCols)
+                     "r"(L::kCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -134,7 +156,7 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
             const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
 #pragma unroll
             for (int c = 0; c < L::kChunks; c++) {
-                tma_load_4d(a + c * 2048u, &tmap_x, bar, 8 * c, z0 + dz, y0 + dy, x0 + dx);
+                tma_load_4d(a + c * L::kChunkBytes, &tmap_x, bar, 8 * c, z0 + dz, y0 + dy, x0 + dx);
                 tma_load_3d(b + c * (uint32_t)CO * 16u, &tmap_w, bar, 8 * c, 0, t);
             }
             issued = t + 1;
@@ -152,10 +174,15 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
             const uint32_t a = smem_u32(smem + s * L::kStageBytes), b = a + L::kABytes;
 #pragma unroll
             for (int j = 0; j < CI / 16; j++) {
-                // K = 16 spans two 8-channel chunks: leading (K) offset = one chunk, stride (M/N) = 8 rows
-                const uint64_t ad = smem_desc(a + j * 2u * 2048u, 2048u, 128u);
+                // K = 16 spans two 8-channel chunks: leading (K) offset = one chunk, stride (M/N) = 8 rows;
+                // tile m's rows start 2 KB further into each chunk, its accumulator CO columns further
                 const uint64_t bd = smem_desc(b + j * 2u * (uint32_t)CO * 16u, (uint32_t)CO * 16u, 128u);
-                mma_bf16(tmem, ad, bd, idesc, (t > 0 || j > 0) ? 1u : 0u);
+#pragma unroll
+                for (int m = 0; m < MT; m++) {
+                    const uint64_t ad = smem_desc(a + j * 2u * L::kChunkBytes + (uint32_t)m * 2048u, L::kChunkBytes,
+                                                  128u);
+                    mma_bf16(tmem + (uint32_t)(m * CO), ad, bd, idesc, (t > 0 || j > 0) ? 1u : 0u);
+                }
             }
             mma_commit(empty0 + 8 * s);
             if (t + kStages < T) {
@@ -179,14 +206,16 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (*flag) {  // uniform across the CTA
+#pragma unroll 1
+        for (int m = 0; m < MT; m++) {
         const int r = 32 * warp + lane;  // TMEM lane = tile row
-        const int z = z0 + (r % kTileZ), yy = y0 + r / kTileZ;
+        const int z = z0 + (r % kTileZ), yy = y0 + kTileY * m + r / kTileZ;
         const bool inb = z < d.nz && yy < d.ny && x0 < d.nx;
         const long long v = inb ? cid(d, x0, yy, z) : 0;
 #pragma unroll
         for (int c0 = 0; c0 < CO; c0 += 16) {
             float acc[16];
-            tmem_ld_x16<16>(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, acc);
+            tmem_ld_x16<16>(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(m * CO + c0), acc);
             if (inb && EPI == 0) {
                 uint32_t pk[8];
 #pragma unroll
@@ -205,11 +234,12 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
                 for (int q = 0; q < 4; q++) dst[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
             }
         }
+        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(L::kCols) : "memory");
     }
 }
 

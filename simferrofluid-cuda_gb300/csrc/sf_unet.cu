@@ -79,15 +79,17 @@ bool tc_shape_ok(int ci, int co, const Dims &d) {
     return ch && d.nz >= tc::kTileZ && d.ny >= tc::kTileY;
 }
 
-template <int CI, int CO, int EPI>
-cudaError_t launch_tc(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *w, const float *b, void *y,
-                      int *err) {
+// MT tiles of 128 voxels per CTA (a 32 x 4 MT brick): the wide brick where the grid holds one along y, else one
+// tile per CTA (the TMA box never extends past the grid along y).
+template <int CI, int CO, int EPI, int MT>
+cudaError_t launch_tc_mt(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *w, const float *b, void *y,
+                         int *err) {
     auto enc = tensor_map_encoder();
     if (!enc || !aligned16(x) || !aligned16(w) || !aligned16(y)) return cudaErrorInvalidValue;
     CUtensorMap mx, mw;
     const cuuint64_t xd[4] = {(cuuint64_t)CI, (cuuint64_t)d.nz, (cuuint64_t)d.ny, (cuuint64_t)d.nx};
     const cuuint64_t xs[3] = {(cuuint64_t)CI * 2, (cuuint64_t)d.nz * CI * 2, (cuuint64_t)d.ny * d.nz * CI * 2};
-    const cuuint32_t xb[4] = {8, tc::kTileZ, tc::kTileY, 1};
+    const cuuint32_t xb[4] = {8, tc::kTileZ, (cuuint32_t)(tc::kTileY * MT), 1};
     const cuuint32_t es[4] = {1, 1, 1, 1};
     if (enc(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(x), xd, xs, xb, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -100,15 +102,23 @@ cudaError_t launch_tc(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
-    using L = tc::Layout<CI, CO>;
-    cudaError_t e = cudaFuncSetAttribute(tc::k_conv_tc<CI, CO, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    using L = tc::Layout<CI, CO, MT>;
+    cudaError_t e = cudaFuncSetAttribute(tc::k_conv_tc<CI, CO, EPI, MT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)L::kSmemBytes);
     if (e != cudaSuccess) return e;
-    const long long tiles = (long long)((d.nz + tc::kTileZ - 1) / tc::kTileZ) * ((d.ny + tc::kTileY - 1) / tc::kTileY) *
-                            d.nx;
+    const long long tiles = (long long)((d.nz + tc::kTileZ - 1) / tc::kTileZ) *
+                            ((d.ny + tc::kTileY * MT - 1) / (tc::kTileY * MT)) * d.nx;
     if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
-    tc::k_conv_tc<CI, CO, EPI><<<(unsigned)tiles, 128, L::kSmemBytes, st>>>(mx, mw, d, b, y, err);
+    tc::k_conv_tc<CI, CO, EPI, MT><<<(unsigned)tiles, 128, L::kSmemBytes, st>>>(mx, mw, d, b, y, err);
     return cudaGetLastError();
+}
+
+template <int CI, int CO, int EPI>
+cudaError_t launch_tc(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *w, const float *b, void *y,
+                      int *err) {
+    constexpr int MT = tc::tiles_per_cta<CI, CO>();
+    if (d.ny >= tc::kTileY * MT) return launch_tc_mt<CI, CO, EPI, MT>(st, d, x, w, b, y, err);
+    return launch_tc_mt<CI, CO, EPI, 1>(st, d, x, w, b, y, err);
 }
 
 // epi 0: forward (bias, ReLU, BF16 y); epi 1: input gradient (FP32 y, no bias)
