@@ -103,9 +103,11 @@ def smooth_velocity(torch, g, dev, gen, vmax=0.5, lattice=9):
 
 
 def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None, weights=None, full_substep=False,
-        use_graph=1, inner_tol=None):
+        use_graph=1, inner_tol=None, pressure_opts=None, magnetic_opts=None):
     """precision "mixed", "fp64" (row skipping), "fp64_full" (every row swept) or "learned" (the mixed solver with
     the trained network's correction steps, weights/unet.f32 unless `weights` names another file).
+
+    pressure_opts / magnetic_opts: further sf_solve_opts fields for the pressure / potential solves.
 
     full_substep: after the two solves, the rest of the reference's substep on the device (core/Simulation.cpp:
     164-165, 236-241, 265): extrapolation of the projected velocity, Collider::Enforce, advection of the level set
@@ -157,10 +159,11 @@ def run(precision, n=768, substeps=50, seed=5, profile_last=True, log=None, weig
         prof = 1 if (profile_last and s == substeps) else 0
         e0.record()
         sm = M.solve(phi, hext, device=True, psi_out=psi, H_out=H,
-                     opts=sf.options("magnetic", precision=prec, profile=prof, **extra))
+                     opts=sf.options("magnetic", precision=prec, profile=prof, **extra, **(magnetic_opts or {})))
         e1.record()
         sp = P.project(vel, phi, frac, device=True, p_out=p_out,
-                       opts=sf.options("pressure", precision=prec, tol=1e-6, profile=prof, **extra))
+                       opts=sf.options("pressure", precision=prec, tol=1e-6, profile=prof, **extra,
+                                       **(pressure_opts or {})))
         e2.record()
         if full_substep:
             ext.solve(vel, phi, frac, device=True)
