@@ -69,7 +69,7 @@ typedef struct {
     int max_iters;       /* PCG iterations (FP64) or total inner iterations (mixed) */
     int pre_smooth;      /* red-black Gauss-Seidel sweeps before restriction */
     int post_smooth;     /* ... after prolongation */
-    int coarse_sweeps;   /* symmetric sweep pairs on the coarsest level (default 48) */
+    int coarse_sweeps;   /* symmetric sweep pairs on the coarsest level (default 8 pressure, 48 potential) */
     int max_levels;      /* 0 = coarsen until every dimension is <= coarse_dim */
     int coarse_dim;      /* default 8 */
     int warm_start;      /* magnetic: start from the context's last potential (reference behaviour, default 1);

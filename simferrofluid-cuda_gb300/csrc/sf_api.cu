@@ -685,7 +685,9 @@ void sf_default_opts(sf_solve_opts *o, int which) {
     o->max_iters = 200;
     o->pre_smooth = 2;
     o->post_smooth = 2;
-    o->coarse_sweeps = 48;
+    // the potential's pure-Neumann coarsest level needs many sweeps; the pressure's, with ghost-fluid (Dirichlet)
+    // terms, is well conditioned: 8 pairs take the same iterations at 256^3 and save 0.1 ms per mixed solve
+    o->coarse_sweeps = which == 1 ? 48 : 8;
     o->max_levels = 0;
     o->coarse_dim = 8;
     o->warm_start = 1;

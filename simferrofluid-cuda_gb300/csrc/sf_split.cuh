@@ -141,6 +141,32 @@ __device__ __forceinline__ void for_list_items(const int *__restrict__ list, con
     }
 }
 
+// The same loop seen per lane: f(rep, i, j, q4, uniform) for the lane's vector q4 of its row.  Rows of 32 or more
+// vectors are split into chunks of 32 lanes (for_list_items); rows of fewer, nq a power of two, share a warp --
+// 32 / nq rows per warp, nq lanes each -- so that no lane idles on the short rows of the coarser split level.
+// The assignment depends only on the grid and the list (deterministic).  reps is 1 or 2.
+template <class F>
+__device__ __forceinline__ void for_list_lanes(const int *__restrict__ list, const int *__restrict__ count, int reps,
+                                               int nq, F &&f) {
+    if (nq >= 32 || (32 % nq) != 0) {
+        for_list_items(list, count, reps, (nq + 31) / 32, [&](int rep, int i, int j, int ch, bool uni) {
+            const int q4 = ch * 32 + threadIdx.x;
+            if (q4 < nq) f(rep, i, j, q4, uni);
+        });
+        return;
+    }
+    const unsigned n = (unsigned)*count, per = 32u / (unsigned)nq;
+    const unsigned groups = (n + per - 1) / per, nit = (unsigned)reps * groups, stride = gridDim.x * blockDim.y;
+    const unsigned sub = threadIdx.x / (unsigned)nq, q4 = threadIdx.x - sub * (unsigned)nq;
+    for (unsigned it = blockIdx.x * blockDim.y + threadIdx.y; it < nit; it += stride) {
+        const unsigned rep = it >= groups ? 1u : 0u;
+        const unsigned r = (it - rep * groups) * per + sub;
+        if (r >= n) continue;
+        const int e = list[r];
+        f((int)rep, (e >> 16) & 0x7fff, e & 0xffff, (int)q4, e < 0);
+    }
+}
+
 // Grid of a persistent row kernel: the blocks that fit on the device at once (its occupancy), at most one warp
 // per item.  Occupancies are looked up once per device and kernel.
 static int resident_grid(const void *kernel) {
@@ -739,9 +765,7 @@ __global__ void __launch_bounds__(256, 4) k_rbgs4s(Dims d, Coef<C> cf, float *__
                                                   const float *__restrict__ dinv) {
     pdl_entry();
     const int nq = d.nz >> 3;
-    for_list_items(list, count, 1, (nq + 31) / 32, [&](int, int i, int j, int ch, bool uni) {
-        const int q4 = ch * 32 + threadIdx.x;
-        if (q4 >= nq) return;
+    for_list_lanes(list, count, 1, nq, [&](int, int i, int j, int q4, bool uni) {
         if (uni)
             rbgs4s_uniform<ZERO>(d, rc[(unsigned)i * (unsigned)d.ny + (unsigned)j], x, b, col, i, j, 4 * q4);
         else
