@@ -1002,7 +1002,7 @@ sf_status sf_unet_forward_dev(void *net, const sf_grid *g, const void *features,
 }
 sf_status sf_unet_set_mode(void *net, int mode) {
     auto *h = reinterpret_cast<NetHandle *>(net);
-    if (!h || !h->ctx || (mode != 0 && mode != 1)) return SF_BAD_ARG;
+    if (!h || !h->ctx || mode < 0 || mode > 2) return SF_BAD_ARG;
     h->net->set_mode(mode);
     return SF_OK;
 }
@@ -1017,6 +1017,7 @@ sf_status sf_unet_backward_dev(void *net, const sf_grid *g, const void *features
     const Dims d = make_dims(g->nx, g->ny, g->nz);
     CK(h->net->forward(d, (const __nv_bfloat16 *)features, nullptr));
     CK(h->net->backward(d, dout));
+    if (h->net->check_device_errors() != cudaSuccess) return fail(c, SF_CUDA_ERROR, h->net->last_error);
     if (grads) CK(h->net->get_grads(grads));
     CK(cudaStreamSynchronize(c->st));
     return SF_OK;

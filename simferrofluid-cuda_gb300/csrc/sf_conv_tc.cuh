@@ -5,10 +5,10 @@
 // 8 channels x (32 x 4 MT x 1) voxels per 8-channel chunk and tap lands as 128 MT rows x 16 B, i.e. 8-row x 16-B
 // core matrices with a 128-B stride along M, one tile per 2 KB and one (2 MT)-KB chunk per 8 channels along K;
 // taps outside the grid are filled with zeros by the TMA unit (the convolution's zero padding).  Weights
-// [tap][Cout][Cin] are staged the same way, once per tap for all MT tiles.  One thread issues TMA loads and
-// tcgen05.mma (M=128, N=Cout, K=16, BF16 in, FP32 accumulate in TMEM, one accumulator of Cout columns per tile)
-// through a ring of stages guarded by mbarriers; all four warps read the accumulators back with tcgen05.ld and
-// apply bias + ReLU + BF16 conversion.  Every wait is bounded: on timeout the CTA records an error code and
+// [tap][Cout][Cin] are staged the same way, once per tap for all MT tiles.  Lane 0 of warp 1 issues the TMA loads
+// and lane 0 of warp 0 the tcgen05.mma (M=128, N=Cout, K=16, BF16 in, FP32 accumulate in TMEM, one accumulator of
+// Cout columns per tile) through a ring of stages guarded by mbarriers; all four warps read the accumulators back
+// with tcgen05.ld and apply bias + ReLU + BF16 conversion.  Every wait is bounded: on timeout the CTA records an error code and
 // returns after releasing its tensor memory.
 #pragma once
 #include <cuda.h>
@@ -115,7 +115,8 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     // 1024-byte aligned stage buffers, barriers after them
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * L::kStageBytes);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 1);  // [0] TMEM base, [1] status
+    // sh: [0] TMEM base, [1] status, [2] MMA side ok, [3] stages waited, [4] TMA side ok, [5] stages issued
+    volatile uint32_t *sh = reinterpret_cast<volatile uint32_t *>(bars + 2 * kStages + 1);
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kStages), done = smem_u32(bars + 2 * kStages);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -129,11 +130,13 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
             mbar_init(empty0 + 8 * s, 1);
         }
         mbar_init(done, 1);
+        for (int k = 1; k < 6; k++) sh[k] = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(const_cast<uint32_t *>(sh))),
                      "r"(L::kCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
@@ -141,15 +144,20 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t tmem = *tmem_slot;
+    const uint32_t tmem = sh[0];
 
-    volatile int *flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
-    if (threadIdx.x == 0) {
-        constexpr uint32_t idesc = instr_desc_bf16(CO);
-        constexpr int T = 27;
-        int issued = 0, waited = 0;
+    // warp specialised: lane 0 of warp 1 issues the TMA loads of the 27 taps through the ring of stages, lane 0 of
+    // warp 0 the MMAs, so a stage is refilled as soon as its MMAs complete without holding up the next MMAs
+    constexpr int T = 27;
+    if (warp == 1 && lane == 0) {
         bool ok = true;
-        auto load = [&](int t, int s) {
+        int issued = 0;
+        for (int t = 0; t < T; t++) {
+            const int s = t % kStages;
+            if (t >= kStages && !mbar_wait(empty0 + 8 * s, (uint32_t)(t / kStages - 1) & 1u)) {
+                ok = false;
+                break;
+            }
             const uint32_t a = smem_u32(smem + s * L::kStageBytes), b = a + L::kABytes;
             const uint32_t bar = full0 + 8 * s;
             mbar_expect_tx(bar, L::kStageBytes);
@@ -160,12 +168,16 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
                 tma_load_3d(b + c * (uint32_t)CO * 16u, &tmap_w, bar, 8 * c, 0, t);
             }
             issued = t + 1;
-        };
-        for (int t = 0; t < kStages && t < T; t++) load(t, t);
+        }
+        sh[4] = ok ? 1u : 0u;
+        sh[5] = (uint32_t)issued;
+    } else if (warp == 0 && lane == 0) {
+        constexpr uint32_t idesc = instr_desc_bf16(CO);
+        bool ok = true;
+        int waited = 0;
         for (int t = 0; t < T; t++) {
             const int s = t % kStages;
-            const uint32_t ph = (uint32_t)(t / kStages) & 1u;
-            if (!mbar_wait(full0 + 8 * s, ph)) {
+            if (!mbar_wait(full0 + 8 * s, (uint32_t)(t / kStages) & 1u)) {
                 ok = false;
                 break;
             }
@@ -185,27 +197,26 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
                 }
             }
             mma_commit(empty0 + 8 * s);
-            if (t + kStages < T) {
-                if (!mbar_wait(empty0 + 8 * s, ph)) {
-                    ok = false;
-                    break;
-                }
-                load(t + kStages, s);
-            }
         }
-        // completion of every MMA issued so far (also on the error path, before TMEM is released)
-        mma_commit(done);
-        if (!mbar_wait(done, 0)) ok = false;
-        if (!ok) {
-            // drain loads still in flight into this CTA's shared memory (bounded)
-            for (int t = waited; t < issued; t++) mbar_wait(full0 + 8 * (t % kStages), (uint32_t)(t / kStages) & 1u);
+        if (waited > 0) {  // completion of every MMA issued (also on the error path, before TMEM is released)
+            mma_commit(done);
+            if (!mbar_wait(done, 0)) ok = false;
+        }
+        sh[2] = ok ? 1u : 0u;
+        sh[3] = (uint32_t)waited;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const bool ok = sh[2] && sh[4];
+        if (!ok) {  // drain loads still in flight into this CTA's shared memory (bounded)
+            for (uint32_t t = sh[3]; t < sh[5]; t++) mbar_wait(full0 + 8 * (t % kStages), (t / kStages) & 1u);
             atomicCAS(err, 0, 1);
         }
-        *flag = ok ? 1 : 0;
+        sh[1] = ok ? 1u : 0u;
     }
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (*flag) {  // uniform across the CTA
+    if (sh[1]) {  // uniform across the CTA
 #pragma unroll 1
         for (int m = 0; m < MT; m++) {
         const int r = 32 * warp + lane;  // TMEM lane = tile row
@@ -240,6 +251,255 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(L::kCols) : "memory");
+    }
+}
+
+// ------------------------------------------------------------------------------------------------ weight gradient
+// dW[tap][co][ci] = sum over voxels v of dY[v][co] X[v + off(tap)][ci]: GEMMs with M = Cout, K = voxels and
+// N = (dz, Cin), both operands K-major with 8 consecutive z per 16-byte row.  k_to_chmajor makes channel-major copies
+// with z split into 8-voxel rows: dYT[zh][x][y][co][zl] and XT[zh][x][y][s][ci][zl] = X[x][y][8 zh + zl + s - 1][ci]
+// (zero outside), the three z shifts s = dz + 1 interleaved per row so that one TMA box starting on a row boundary
+// carries all three.  A job is one (dx, dy) pair over one brick of 32 (z) x 4 (y) x BX (x) voxels: one 5-D TMA box
+// (8, C, 4, BX, 4) lands as rows c + C k of 16 B, k = y + 4 (x + BX zh) the K index of the 8-voxel core matrices,
+// so consecutive K steps are C x 16 B apart (LBO) and 8-row groups 128 B (SBO); the y and x shifts are box
+// coordinates (outside the grid: zero fill).  One MMA (K = 16) then accumulates the three taps (dx, dy, -1..1) into
+// 3 Cin TMEM columns.  M = 128 rows of which the first Cout are dY channels; the rows past them read the next K
+// steps' rows (or a zeroed slack after the buffer) and land in accumulator lanes that are never read.
+// One CTA (one per SM, 512 TMEM columns) runs a group of (dx, dy) pairs over a strided set of bricks, warp
+// specialised: lane 0 of warp 1 issues the TMA loads (dY of a brick once, into one of two buffers; X per pair through
+// a ring of stages), lane 0 of warp 0 the MMAs, so neither waits on the other's latency.  The CTA writes its partial
+// sums part[chunk][tap][co][ci] (FP32), reduced over chunks in fixed order afterwards.  Every wait is bounded as in
+// k_conv_tc.
+constexpr uint32_t kWgSlack = 2048;
+
+template <int CI>
+__host__ __device__ constexpr int wg_bx() {  // x extent of a brick
+    return CI == 16 ? 2 : 1;
+}
+// (dx, dy) pairs per CTA: 3 CI columns each, at most 512
+template <int CI>
+__host__ __device__ constexpr int wg_pairs_per_cta() {
+    return CI == 16 ? 9 : CI == 32 ? 5 : 2;
+}
+
+template <int CI, int CO>
+struct WgLayout {
+    static constexpr int BX = wg_bx<CI>();
+    static constexpr uint32_t kABytes = 256u * CO * BX;  // 8 z x CO x 4 y x BX x x 4 zh, BF16
+    static constexpr uint32_t kBBytes = 768u * CI * BX;  // 8 z x 3 CI x 4 y x BX x x 4 zh
+    static constexpr uint32_t kAStride = kABytes + kWgSlack;
+    static constexpr int kStagesRaw = (int)((216u * 1024u - 2u * kAStride) / kBBytes);
+    static constexpr int kStages = kStagesRaw > 8 ? 8 : kStagesRaw;
+    static constexpr uint32_t kNeed = 2u * kAStride + kStages * kBBytes + 1024u + 512u;
+    // at least 116 KB: one CTA per SM, whose 512 TMEM columns are then always free
+    static constexpr uint32_t kSmemBytes = kNeed > 116u * 1024u ? kNeed : 116u * 1024u;
+    static_assert(kStages >= 2 && kSmemBytes <= 227u * 1024u, "shared memory");
+};
+
+// dst[zh][x][y][s][c][zl] = src[x][y][8 zh + zl + s + shift0][c] where 8 zh + zl < nz and the shifted z lies in the
+// grid, else 0; s < ns, zh < nzh = ceil(nz / 8).  One thread per (zh, x, y, c): 16-byte stores.
+template <int C>
+__global__ void __launch_bounds__(256) k_to_chmajor(Dims d, int ns, int shift0, const __nv_bfloat16 *__restrict__ src,
+                                                    __nv_bfloat16 *__restrict__ dst) {
+    const int nzh = (d.nz + 7) / 8;
+    const long long m = (long long)nzh * d.nx * d.ny * C;
+    const unsigned short *s16 = reinterpret_cast<const unsigned short *>(src);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m; e += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(e % C);
+        const long long r = e / C;  // ((zh nx + x) ny + y)
+        const int y = (int)(r % d.ny);
+        const long long t = r / d.ny;
+        const int x = (int)(t % d.nx), zh = (int)(t / d.nx);
+        const long long row = (((long long)x * d.ny + y) * d.nz) * C + c;  // src index of (x, y, 0, c)
+        for (int s = 0; s < ns; s++) {
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                uint32_t h[2];
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    const int z = 8 * zh + 2 * q + u, zs = z + s + shift0;
+                    h[u] = (z < d.nz && zs >= 0 && zs < d.nz) ? (uint32_t)s16[row + (long long)zs * C] : 0u;
+                }
+                w[q] = h[0] | (h[1] << 16);
+            }
+            *reinterpret_cast<uint4 *>(dst + ((r * ns + s) * C + c) * 8) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    }
+}
+
+template <int CI, int CO>
+__global__ void __launch_bounds__(128, 1) k_wgrad_tc(const __grid_constant__ CUtensorMap tmap_dy,
+                                                     const __grid_constant__ CUtensorMap tmap_x, Dims d,
+                                                     float *__restrict__ part, int *err) {
+    constexpr int NP = wg_pairs_per_cta<CI>();
+    constexpr int N = 3 * CI;
+    static_assert(NP * N <= 512 && CO <= 128 && CI % 16 == 0 && CO % 16 == 0 && N <= 256, "shape");
+    using L = WgLayout<CI, CO>;
+    constexpr int S = L::kStages, BX = L::BX;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t *abuf = smem, *bbuf = smem + 2 * L::kAStride;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(bbuf + S * L::kBBytes);
+    // [0, 2) dY full, [2, 4) dY empty, [4, 4 + S) X full, [4 + S, 4 + 2S) X empty, then done
+    // sh: [0] TMEM base, [1] status, [2] MMA side ok, [3] X jobs waited, [4] bricks waited, [5] TMA side ok,
+    //     [6] X jobs issued, [7] bricks issued
+    volatile uint32_t *sh = reinterpret_cast<volatile uint32_t *>(bars + 4 + 2 * S + 1);
+    const uint32_t afull0 = smem_u32(bars), aempty0 = smem_u32(bars + 2), bfull0 = smem_u32(bars + 4),
+                   bempty0 = smem_u32(bars + 4 + S), done = smem_u32(bars + 4 + 2 * S);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int pair0 = blockIdx.y * NP, npair = min(NP, 9 - pair0);
+    const int bz_n = (d.nz + 31) / 32, by_n = (d.ny + 3) / 4, bx_n = (d.nx + BX - 1) / BX;
+    const long long nbricks = (long long)bz_n * by_n * bx_n;
+    const int nb = nbricks > blockIdx.x ? (int)((nbricks - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+    const int J = nb * npair;
+
+    // zero the slack after each dY buffer (read by the MMA rows past Cout)
+    for (uint32_t i = threadIdx.x; i < kWgSlack / 16; i += blockDim.x) {
+        reinterpret_cast<uint4 *>(abuf + L::kABytes)[i] = make_uint4(0, 0, 0, 0);
+        reinterpret_cast<uint4 *>(abuf + L::kAStride + L::kABytes)[i] = make_uint4(0, 0, 0, 0);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < 2; s++) {
+            mbar_init(afull0 + 8 * s, 1);
+            mbar_init(aempty0 + 8 * s, 1);
+        }
+        for (int s = 0; s < S; s++) {
+            mbar_init(bfull0 + 8 * s, 1);
+            mbar_init(bempty0 + 8 * s, 1);
+        }
+        mbar_init(done, 1);
+        for (int k = 1; k < 8; k++) sh[k] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(const_cast<uint32_t *>(sh))),
+                     "r"(512)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = sh[0];
+
+    auto brick = [&](int bi, int &z0, int &y0, int &x0) {
+        const long long br = blockIdx.x + (long long)bi * gridDim.x;
+        z0 = 32 * (int)(br % bz_n);
+        y0 = 4 * (int)((br / bz_n) % by_n);
+        x0 = BX * (int)(br / ((long long)bz_n * by_n));
+    };
+    if (warp == 1 && lane == 0) {  // TMA producer
+        bool ok = true;
+        int a_issued = 0, b_issued = 0;
+        for (int q = 0; q < J && ok; q++) {
+            const int bi = q / npair, jj = q % npair;
+            int z0, y0, x0;
+            brick(bi, z0, y0, x0);
+            if (jj == 0) {
+                const int ab = bi & 1;
+                if (bi >= 2 && !mbar_wait(aempty0 + 8 * ab, (uint32_t)((bi - 2) >> 1) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                mbar_expect_tx(afull0 + 8 * ab, L::kABytes);
+                tma_load_5d(smem_u32(abuf + ab * L::kAStride), &tmap_dy, afull0 + 8 * ab, 0, 0, y0, x0, z0 / 8);
+                a_issued = bi + 1;
+            }
+            const int pr = pair0 + jj, dx = pr / 3 - 1, dy = pr % 3 - 1;
+            const int s = q % S;
+            if (q >= S && !mbar_wait(bempty0 + 8 * s, (uint32_t)(q / S - 1) & 1u)) {
+                ok = false;
+                break;
+            }
+            mbar_expect_tx(bfull0 + 8 * s, L::kBBytes);
+            tma_load_5d(smem_u32(bbuf + s * L::kBBytes), &tmap_x, bfull0 + 8 * s, 0, 0, y0 + dy, x0 + dx, z0 / 8);
+            b_issued = q + 1;
+        }
+        sh[5] = ok ? 1u : 0u;
+        sh[6] = (uint32_t)b_issued;
+        sh[7] = (uint32_t)a_issued;
+    } else if (warp == 0 && lane == 0) {  // MMA issuer
+        constexpr uint32_t idesc = instr_desc_bf16(N);
+        bool ok = true;
+        int a_waited = 0, b_waited = 0;
+        for (int q = 0; q < J; q++) {
+            const int bi = q / npair, jj = q % npair, ab = bi & 1, s = q % S;
+            if (jj == 0) {
+                if (!mbar_wait(afull0 + 8 * ab, (uint32_t)(bi >> 1) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                a_waited = bi + 1;
+            }
+            if (!mbar_wait(bfull0 + 8 * s, (uint32_t)(q / S) & 1u)) {
+                ok = false;
+                break;
+            }
+            b_waited = q + 1;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint64_t ad0 = smem_desc(smem_u32(abuf + ab * L::kAStride), (uint32_t)CO * 16u, 128u);
+            const uint64_t bd0 = smem_desc(smem_u32(bbuf + s * L::kBBytes), (uint32_t)N * 16u, 128u);
+#pragma unroll
+            for (int p = 0; p < 8 * BX; p++)  // start addresses advance in 16-byte units (no carry: < 256 KB)
+                mma_bf16(tmem + (uint32_t)(jj * N), ad0 + (uint64_t)(2 * p * CO), bd0 + (uint64_t)(2 * p * N), idesc,
+                         (bi > 0 || p > 0) ? 1u : 0u);
+            mma_commit(bempty0 + 8 * s);
+            if (jj == npair - 1) mma_commit(aempty0 + 8 * ab);
+        }
+        if (b_waited > 0) {  // completion of every MMA issued (also on the error path, before TMEM is released)
+            mma_commit(done);
+            if (!mbar_wait(done, 0)) ok = false;
+        }
+        sh[2] = ok ? 1u : 0u;
+        sh[3] = (uint32_t)b_waited;
+        sh[4] = (uint32_t)a_waited;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const bool ok = sh[2] && sh[5];
+        if (!ok) {  // drain copies still in flight into this CTA's shared memory (bounded)
+            for (uint32_t q = sh[3]; q < sh[6]; q++) mbar_wait(bfull0 + 8 * (q % S), (q / S) & 1u);
+            for (uint32_t q = sh[4]; q < sh[7]; q++) mbar_wait(afull0 + 8 * (q & 1), (q >> 1) & 1u);
+            atomicCAS(err, 0, 1);
+        }
+        sh[1] = ok ? (J > 0 ? 1u : 2u) : 0u;
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t st = sh[1];
+    if (st != 0 && 32 * warp < CO) {  // 1: the accumulators hold this CTA's sums; 2: no brick, the sums are zero
+        const int co = 32 * warp + lane;  // TMEM lane = dY channel
+        for (int jj = 0; jj < npair; jj++) {
+#pragma unroll
+            for (int sz = 0; sz < 3; sz++) {
+                float *out = part + (((long long)blockIdx.x * 27 + 3 * (pair0 + jj) + sz) * CO) * CI;
+#pragma unroll
+                for (int c0 = 0; c0 < CI; c0 += 16) {
+                    float acc[16];
+                    if (st == 1) {
+                        tmem_ld_x16<16>(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(jj * N + sz * CI + c0), acc);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 16; q++) acc[q] = 0.f;
+                    }
+                    if (co < CO) {
+                        float4 *dst = reinterpret_cast<float4 *>(out + (long long)co * CI + c0);
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            dst[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
     }
 }
 

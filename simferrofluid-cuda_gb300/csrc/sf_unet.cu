@@ -132,6 +132,60 @@ cudaError_t tc_dispatch(cudaStream_t st, int ci, int co, int epi, const Dims &d,
     return cudaErrorInvalidValue;
 }
 
+// The tcgen05 weight gradient takes 32 (z) x 4 (y) x 1 or 2 (x) bricks: every TMA box dimension within the grid's.
+bool wgrad_tc_ok(int ci, int co, const Dims &d) {
+    const bool ch = (ci == 16 || ci == 32 || ci == 64) && (co == 16 || co == 32 || co == 64);
+    return ch && (d.nz + 7) / 8 >= 4 && d.ny >= 4 && d.nx >= 2;
+}
+
+// channel-major z-row copies of dY and of X with its three z shifts (k_to_chmajor), then k_wgrad_tc over all
+// bricks; chunks receives the number of partial sums written to part
+template <int CI, int CO>
+cudaError_t launch_wgrad_tc(cudaStream_t st, const Dims &d, const bf16 *dy, const bf16 *x, bf16 *dyT, bf16 *xT,
+                            float *part, long long part_cap, int &chunks, int *err) {
+    auto enc = tensor_map_encoder();
+    if (!enc || !aligned16(dyT) || !aligned16(xT) || !aligned16(part)) return cudaErrorInvalidValue;
+    using L = tc::WgLayout<CI, CO>;
+    const long long nzh = (d.nz + 7) / 8;
+    const long long rows = nzh * d.nx * d.ny;  // 8-voxel z rows of one channel
+    auto map5 = [&](CUtensorMap *m, const bf16 *base, int C) {
+        const cuuint64_t dims[5] = {8, (cuuint64_t)C, (cuuint64_t)d.ny, (cuuint64_t)d.nx, (cuuint64_t)nzh};
+        const cuuint64_t str[4] = {16, (cuuint64_t)C * 16, (cuuint64_t)d.ny * C * 16,
+                                   (cuuint64_t)d.nx * d.ny * C * 16};
+        const cuuint32_t box[5] = {8, (cuuint32_t)C, 4, (cuuint32_t)L::BX, 4};
+        const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+        return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(base), dims, str, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    };
+    CUtensorMap mdy, mx;
+    if (!map5(&mdy, dyT, CO) || !map5(&mx, xT, 3 * CI)) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(tc::k_wgrad_tc<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)L::kSmemBytes);
+    if (e != cudaSuccess) return e;
+    constexpr int NP = tc::wg_pairs_per_cta<CI>();
+    constexpr int groups = (9 + NP - 1) / NP;
+    const long long nbricks = (long long)((d.nz + 31) / 32) * ((d.ny + 3) / 4) * ((d.nx + L::BX - 1) / L::BX);
+    long long G = 152 / groups;
+    if (G > nbricks) G = nbricks;
+    if (G * 27 * CO * CI > part_cap) G = part_cap / (27LL * CO * CI);
+    if (G < 1) return cudaErrorInvalidValue;
+    tc::k_to_chmajor<CO><<<flat_blocks(rows * CO), 256, 0, st>>>(d, 1, 0, dy, dyT);
+    tc::k_to_chmajor<CI><<<flat_blocks(rows * CI), 256, 0, st>>>(d, 3, -1, x, xT);
+    tc::k_wgrad_tc<CI, CO><<<dim3((unsigned)G, groups), 128, L::kSmemBytes, st>>>(mdy, mx, d, part, err);
+    chunks = (int)G;
+    return cudaGetLastError();
+}
+
+cudaError_t wgrad_tc_dispatch(cudaStream_t st, int ci, int co, const Dims &d, const bf16 *dy, const bf16 *x,
+                              bf16 *dyT, bf16 *xT, float *part, long long part_cap, int &chunks, int *err) {
+#define CASE(A, B)                                                                             \
+    if (ci == A && co == B) return launch_wgrad_tc<A, B>(st, d, dy, x, dyT, xT, part, part_cap, chunks, err);
+    CASE(16, 16) CASE(16, 32) CASE(32, 16) CASE(32, 32) CASE(32, 64) CASE(64, 32) CASE(64, 64)
+#undef CASE
+    return cudaErrorInvalidValue;
+}
+
 template <int CI, int CO>
 void launch_wgrad(cudaStream_t st, const Dims &d, const bf16 *dy, const bf16 *x, float *part, int taps, int vchunk,
                   int chunks) {
@@ -241,6 +295,7 @@ cudaError_t UNet::ensure(const Dims &d, bool training) {
     for (void *p : ws_) cudaFree(p);
     ws_.clear();
     have_ws_ = false;
+    wg_dy_ = wg_x_ = nullptr;
     dims_[0] = d;
     for (int l = 1; l < 4; l++)
         dims_[l] = make_dims((dims_[l - 1].nx + 1) / 2, (dims_[l - 1].ny + 1) / 2, (dims_[l - 1].nz + 1) / 2);
@@ -293,6 +348,25 @@ cudaError_t UNet::ensure(const Dims &d, bool training) {
     }
     have_ws_ = true;
     ws_training_ = true;
+    return cudaSuccess;
+}
+
+// channel-major copies for the tcgen05 weight gradient, sized for the largest level (allocated on first use)
+cudaError_t UNet::ensure_wgrad_ws() {
+    if (wg_dy_) return cudaSuccess;
+    const int cmax[4] = {16, 32, 64, 64};
+    long long el = 0;
+    for (int l = 0; l < 4; l++) {
+        const long long e = (long long)cmax[l] * dims_[l].nx * dims_[l].ny * 8 * ((dims_[l].nz + 7) / 8);
+        if (e > el) el = e;
+    }
+    void *a = nullptr, *b = nullptr;
+    if (cudaMalloc(&a, 2 * (size_t)el) != cudaSuccess) return cudaErrorMemoryAllocation;
+    ws_.push_back(a);
+    if (cudaMalloc(&b, 6 * (size_t)el) != cudaSuccess) return cudaErrorMemoryAllocation;
+    ws_.push_back(b);
+    wg_dy_ = (bf16 *)a;
+    wg_x_ = (bf16 *)b;
     return cudaSuccess;
 }
 
@@ -363,9 +437,24 @@ void UNet::conv_bwd(const ConvLayer &L, const Dims &d, const bf16 *x, const bf16
     long long vchunk = (d.n + 63) / 64;
     if (vchunk < kVchunkMin) vchunk = kVchunkMin;
     const int chunks = (int)((d.n + vchunk - 1) / vchunk);
-    wgrad_dispatch(st_, L.cin, L.cout, d, dy, x, wpart_, L.taps, (int)vchunk, chunks);
+    int wchunks = 0;
+    if (mode_ >= 1 && L.taps == 27 && wgrad_tc_ok(L.cin, L.cout, d)) {
+        cudaError_t e = ensure_wgrad_ws();
+        if (e == cudaSuccess)
+            e = wgrad_tc_dispatch(st_, L.cin, L.cout, d, dy, x, wg_dy_, wg_x_, wpart_, wpart_elems_, wchunks, err_);
+        if (e == cudaSuccess)
+            tc_launches_++;
+        else {
+            wchunks = 0;
+            last_error = std::string("tcgen05 weight gradient not launched: ") + cudaGetErrorString(e);
+        }
+    }
+    if (wchunks == 0) {
+        wgrad_dispatch(st_, L.cin, L.cout, d, dy, x, wpart_, L.taps, (int)vchunk, chunks);
+        wchunks = chunks;
+    }
     const long long mw = (long long)L.taps * L.cout * L.cin;
-    k_reduce_chunks<<<flat_blocks(mw), 256, 0, st_>>>(wpart_, chunks, mw, g_ + L.woff);
+    k_reduce_chunks<<<flat_blocks(mw), 256, 0, st_>>>(wpart_, wchunks, mw, g_ + L.woff);
     k_bias_grad<<<chunks, 64, 0, st_>>>(d, dy, L.cout, (int)vchunk, hpart_);
     k_reduce_chunks<<<1, 64, 0, st_>>>(hpart_, chunks, L.cout, g_ + L.boff);
     if (!dx) return;
@@ -426,7 +515,7 @@ cudaError_t UNet::train_step(const Dims &d, const bf16 *feat, const float *targe
     k_cos_grad<<<flat_blocks(d.n), 256, 0, st_>>>(d.n, out_, target, dots_, dout_);
     e = backward(d, dout_);
     if (e != cudaSuccess) return e;
-    if (mode_ == 1 && (e = check_device_errors()) != cudaSuccess) return e;
+    if (mode_ >= 1 && (e = check_device_errors()) != cudaSuccess) return e;
     step_++;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f - powf(b1, (float)step_), c2 = 1.f - powf(b2, (float)step_);

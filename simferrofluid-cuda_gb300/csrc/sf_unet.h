@@ -52,7 +52,8 @@ class UNet {
     // channel 0 of existing features set to r * inv_rms (FP32 r on the cells), the other channels unchanged
     cudaError_t set_rhs_channel(const Dims &d, const float *r, double inv_rms, __nv_bfloat16 *feat);
     float *output() { return out_; }
-    // convolution kernels of the forward pass: 0 warp-level MMA (mma.sync), 1 tcgen05 + TMA
+    // convolution kernels: 0 warp-level MMA (mma.sync) throughout; 1 tcgen05 + TMA for the forward, input-gradient
+    // and weight-gradient convolutions; 2 tcgen05 for the weight gradient alone (the rest as mode 0)
     void set_mode(int m) { mode_ = m; }
     int mode() const { return mode_; }
     long long tc_launches() const { return tc_launches_; }
@@ -63,6 +64,7 @@ class UNet {
 
    private:
     cudaError_t ensure(const Dims &d, bool training);
+    cudaError_t ensure_wgrad_ws();
     void conv_fwd(const ConvLayer &L, const Dims &d, const __nv_bfloat16 *x, __nv_bfloat16 *y);
     void conv_bwd(const ConvLayer &L, const Dims &d, const __nv_bfloat16 *x, const __nv_bfloat16 *post,
                   const float *dpost, float *dx /* nullable */);
@@ -85,6 +87,7 @@ class UNet {
     const __nv_bfloat16 *feat_ = nullptr;
     float *gA[4], *gB[4], *gU[3];
     __nv_bfloat16 *gbf[4];
+    __nv_bfloat16 *wg_dy_ = nullptr, *wg_x_ = nullptr;  // channel-major copies for the tcgen05 weight gradient
     float *out_ = nullptr, *dout_ = nullptr, *wpart_ = nullptr, *hpart_ = nullptr;
     double *dots_ = nullptr, *dots_host_ = nullptr, *redpart_ = nullptr;
     long long wpart_elems_ = 0;
