@@ -175,7 +175,7 @@ SF_EXPORT sf_status sf_pressure_reproject_dev(void *ctx, const sf_grid *g, doubl
  * :97-118), the solve (amgcl SA+SPAI0 CG there, MGPCG here) and AssignTotalField (:125-143).
  *   phi          level set on the simulation's cell grid (NULL: the level set of sf_levelset_upload)
  *   chi          susceptibility (SetSusceptibility), band_width the Heaviside half-width (SetBandWidth)
- *   hext[3]      applied field on faces
+ *   hext[3]      applied field on faces (NULL: the field of sf_applied_field_prefetch)
  *   psi_out      optional (nx*ny*nz) potential, psi[0] = 0
  *   H_out[3]     optional total field H = Hext - grad psi on faces (m_TotalField)
  * The solve starts from the context's last potential on the same grid when opts->warm_start (m_Sol). */
@@ -312,6 +312,14 @@ SF_EXPORT sf_status sf_selftest_bounded_wait(void *ctx, double limit_ms, int *ti
 SF_EXPORT sf_status sf_collider_upload(void *ctx, const sf_grid *g, const double *const frac[3],
                                        const double *const solid_vel[3]);
 SF_EXPORT sf_status sf_levelset_upload(void *ctx, const sf_grid *g, const double *phi);
+/* sf_applied_field_prefetch: the applied field hext[3] (host or device face arrays of grid g) of a later magnetic
+ * call, copied asynchronously into buffers of the context: the copy starts on a side stream when the next pressure
+ * call has enqueued its input copies (so it runs under that solve), or else in the magnetic call; a magnetic call
+ * with hext == NULL waits for it and reads it, and so do later ones until the next prefetch.  The arrays must stay
+ * unchanged until the first magnetic call that reads them returns.  No counterpart in the reference, whose
+ * applied field lives in host memory; this lets its host-pointer callers overlap the copy with the pressure solve.
+ * A magnetic call with hext == NULL and no prefetch of its grid returns SF_NOT_READY. */
+SF_EXPORT sf_status sf_applied_field_prefetch(void *ctx, const sf_grid *g, const double *const hext[3]);
 
 /* ----- allocation-free residual check ------------------------------------------------------------------------
  * No counterpart in the reference: its solvers allocate freely and report only the residual of their own

@@ -154,6 +154,18 @@ class Context:
         if s != _abi.SF_OK:
             raise SolveError(s, "sf_levelset_upload: " + self.last_error())
 
+    def prefetch_applied_field(self, grid, field):
+        """Copy a later magnetic call's applied field asynchronously (sf_applied_field_prefetch): the copy runs
+        under the next pressure projection; MagneticField.solve with external_field=None reads it.  Arrays: numpy
+        (host; pinned memory gives a truly asynchronous copy) or CUDA tensors.  They are kept referenced here and
+        must stay unchanged until that magnetic call returns."""
+        keep = [a if hasattr(a, "data_ptr") else np.ascontiguousarray(a, np.float64) for a in field]
+        ptr = lambda a: int(a.data_ptr()) if hasattr(a, "data_ptr") else a.ctypes.data  # noqa: E731
+        s = self.lib.sf_applied_field_prefetch(self.handle, C.byref(grid.c_grid()), _abi.p3([ptr(a) for a in keep]))
+        if s != _abi.SF_OK:
+            raise SolveError(s, "sf_applied_field_prefetch: " + self.last_error())
+        self._prefetched_field = keep
+
     def set_network(self, net):
         """Attach the U-Net used by precision="learned" solves (None detaches)."""
         s = self.lib.sf_set_network(self.handle, net.handle if net is not None else None)
@@ -384,12 +396,14 @@ class MagneticField:
     def solve(self, level_set, external_field, opts=None, device=False, psi_out=None, H_out=None,
               raise_on_nonconv=True):
         """MagneticField::Solve: returns statistics; ``potential`` and ``total_field`` hold the results.
-        level_set None: the context's uploaded level set; psi_out False: no potential output."""
+        level_set None: the context's uploaded level set; external_field None: the context's prefetched applied
+        field (Context.prefetch_applied_field); psi_out False: no potential output."""
         g = self.grid
         keep = []
         fs = [g.face_shape(a) for a in range(3)]
         phi = _ptr(level_set, g.shape, "level_set", device, False, keep)
-        he = [_ptr(external_field[a], fs[a], f"external_field[{a}]", device, False, keep) for a in range(3)]
+        he = None if external_field is None else \
+            [_ptr(external_field[a], fs[a], f"external_field[{a}]", device, False, keep) for a in range(3)]
         if not device:
             if psi_out is None:
                 psi_out = np.zeros(g.shape)
@@ -400,10 +414,12 @@ class MagneticField:
         pp = _ptr(psi_out, g.shape, "psi_out", device, True) if psi_out is not None else None
         hp = None if H_out is None else [_ptr(H_out[a], fs[a], "H_out", device, True) for a in range(3)]
         hp_ref = _abi.p3_ref(hp)
+        he_ref = _abi.p3_ref(he)
         st = _abi.sf_solve_stats()
         o = opts if opts is not None else options("magnetic")
         fn = self.ctx.lib.sf_magnetic_solve_dev if device else self.ctx.lib.sf_magnetic_solve
-        s = fn(self.ctx.handle, C.byref(g.c_grid()), C.c_void_p(phi), self.chi, self.band_width, _abi.p3(he),
+        s = fn(self.ctx.handle, C.byref(g.c_grid()), C.c_void_p(phi), self.chi, self.band_width,
+               he_ref[0] if he_ref else None,
                C.c_void_p(pp) if pp else None, hp_ref[0] if hp_ref else None, C.byref(o), C.byref(st))
         self.stats = st.as_dict()
         _check(self.ctx, s, self.stats, "magnetic solve", raise_on_nonconv)

@@ -29,7 +29,7 @@ EXPORTED = [
     "sf_create", "sf_destroy", "sf_status_string", "sf_last_error", "sf_abi_version", "sf_default_opts",
     "sf_device_bytes", "sf_pressure_project", "sf_pressure_project_dev", "sf_pressure_reproject",
     "sf_pressure_reproject_dev", "sf_magnetic_solve", "sf_magnetic_solve_dev", "sf_magnetic_reset",
-    "sf_collider_upload", "sf_levelset_upload", "sf_selftest_bounded_wait",
+    "sf_collider_upload", "sf_levelset_upload", "sf_applied_field_prefetch", "sf_selftest_bounded_wait",
     "sf_collider_box_fractions", "sf_collider_face_fractions",
     "sf_unet_create", "sf_unet_destroy", "sf_unet_num_params", "sf_unet_set_params", "sf_unet_get_params",
     "sf_unet_forward_dev", "sf_unet_backward_dev", "sf_unet_train_step_dev", "sf_set_network",
@@ -106,7 +106,7 @@ def load(path: str | None = None):
         f.restype = C.c_int
     for name in ("sf_magnetic_solve", "sf_magnetic_solve_dev"):
         f = getattr(L, name)
-        f.argtypes = [V, G, V, C.c_double, C.c_double, _P3, V, V, O, S]
+        f.argtypes = [V, G, V, C.c_double, C.c_double, V, V, V, O, S]  # hext: p3_ref (nullable)
         f.restype = C.c_int
     L.sf_magnetic_reset.argtypes = [V]
     L.sf_magnetic_reset.restype = C.c_int
@@ -114,6 +114,8 @@ def load(path: str | None = None):
     L.sf_collider_upload.restype = C.c_int
     L.sf_levelset_upload.argtypes = [V, G, V]
     L.sf_levelset_upload.restype = C.c_int
+    L.sf_applied_field_prefetch.argtypes = [V, G, _P3]
+    L.sf_applied_field_prefetch.restype = C.c_int
     L.sf_selftest_bounded_wait.argtypes = [V, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     L.sf_selftest_bounded_wait.restype = C.c_int
     for name in ("sf_extrapolate_velocity", "sf_extrapolate_velocity_dev"):

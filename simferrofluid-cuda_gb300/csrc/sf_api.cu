@@ -46,6 +46,15 @@ struct Ctx {
     DevBuf rfrac[3], rus[3], rphi;
     bool rcol = false, rcol_us = false, rls = false;
     Dims rcol_dims{0, 0, 0, 0}, rls_dims{0, 0, 0, 0};
+    // applied field of a later magnetic call (sf_applied_field_prefetch), copied into its own buffers on a side
+    // stream once the next pressure call's inputs are on the device, or by the magnetic call that reads it
+    DevBuf pfield[3];
+    cudaStream_t cst = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_field = nullptr;
+    const double *field_src[3] = {nullptr, nullptr, nullptr};
+    bool field_pending = false, field_ready = false, field_fresh = false;
+    Dims field_dims{0, 0, 0, 0};
+    long long field_n[3] = {0, 0, 0}, field_bytes = 0;
 };
 
 Ctx *C(void *p) { return reinterpret_cast<Ctx *>(p); }
@@ -187,6 +196,21 @@ sf_status learned_prepare(Ctx *c, MGSolver &S, const Dims &d, NetStep &step, Lea
 
 bool same_dims(const Dims &a, const Dims &b) { return a.nx == b.nx && a.ny == b.ny && a.nz == b.nz; }
 
+// Starts a pending applied-field prefetch on the side stream, after everything enqueued on the context's stream so
+// far (a pressure call's input copies): the copy then runs under the pressure solve and its output copies.
+sf_status start_field_copy(Ctx *c) {
+    if (!c->field_pending) return SF_OK;
+    c->field_pending = false;
+    CK(cudaEventRecord(c->ev_in, c->st));
+    CK(cudaStreamWaitEvent(c->cst, c->ev_in, 0));
+    for (int a = 0; a < 3; a++)
+        CK(cudaMemcpyAsync(c->pfield[a].get(), c->field_src[a], 8 * (size_t)c->field_n[a], cudaMemcpyDefault, c->cst));
+    CK(cudaEventRecord(c->ev_field, c->cst));
+    c->field_ready = true;
+    c->field_fresh = true;
+    return SF_OK;
+}
+
 // The resident level set (phi == NULL) or the staged / passed-through one.
 sf_status level_set_in(Ctx *c, const double *phi, const Dims &d, bool dev, const double **out, long long &h2d) {
     if (phi) return stage_in(c, c->phi, phi, d.n, dev, out, h2d);
@@ -240,6 +264,7 @@ sf_status pressure_impl(Ctx *c, const sf_grid *g, double *const vel[3], const do
         }
         if ((s = stage_in(c, c->jump[a], jump ? jump[a] : nullptr, nf, dev, &fjump.p[a], h2d)) != SF_OK) return s;
     }
+    if ((s = start_field_copy(c)) != SF_OK) return s;  // a prefetched applied field, under this solve
     if (!c->pres) c->pres = std::make_unique<MGSolver>(c->st);
     MGSolver &S = *c->pres;
     SolverParams prm = params_from(opts, 0);
@@ -317,10 +342,11 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
                         bool dev) {
     auto t0 = std::chrono::steady_clock::now();
     if (!c) return SF_BAD_ARG;
-    if (!grid_ok(g) || !hext || !opts_ok(opts) || !std::isfinite(chi) || !(bw > 0) || !std::isfinite(bw))
-        return fail(c, SF_BAD_ARG, "bad grid, pointer, chi, band width or option");
-    for (int a = 0; a < 3; a++)
-        if (!hext[a]) return fail(c, SF_BAD_ARG, "null applied-field array");
+    if (!grid_ok(g) || !opts_ok(opts) || !std::isfinite(chi) || !(bw > 0) || !std::isfinite(bw))
+        return fail(c, SF_BAD_ARG, "bad grid, chi, band width or option");
+    if (hext)
+        for (int a = 0; a < 3; a++)
+            if (!hext[a]) return fail(c, SF_BAD_ARG, "null applied-field array");
     if (H_out)
         for (int a = 0; a < 3; a++)
             if (!H_out[a]) return fail(c, SF_BAD_ARG, "H_out must hold three arrays or be NULL");
@@ -332,8 +358,19 @@ sf_status magnetic_impl(Ctx *c, const sf_grid *g, const double *phi, double chi,
     Faces fh{};
     sf_status s;
     if ((s = level_set_in(c, phi, d, dev, &dphi, h2d)) != SF_OK) return s;
-    for (int a = 0; a < 3; a++)
-        if ((s = stage_in(c, c->hext[a], hext[a], face_count(g, a), dev, &fh.p[a], h2d)) != SF_OK) return s;
+    if (hext) {
+        for (int a = 0; a < 3; a++)
+            if ((s = stage_in(c, c->hext[a], hext[a], face_count(g, a), dev, &fh.p[a], h2d)) != SF_OK) return s;
+    } else {  // the prefetched applied field
+        if ((s = start_field_copy(c)) != SF_OK) return s;
+        if (!c->field_ready || !same_dims(c->field_dims, d))
+            return fail(c, SF_NOT_READY,
+                        "hext is NULL and no applied field of this grid was prefetched (sf_applied_field_prefetch)");
+        CK(cudaStreamWaitEvent(c->st, c->ev_field, 0));
+        for (int a = 0; a < 3; a++) fh.p[a] = (const double *)c->pfield[a].get();
+        if (c->field_fresh) h2d += c->field_bytes;
+        c->field_fresh = false;
+    }
     if (!c->mag) c->mag = std::make_unique<MGSolver>(c->st);
     MGSolver &S = *c->mag;
     SolverParams prm = params_from(opts, 1);
@@ -722,6 +759,12 @@ sf_status sf_create(int device, void *stream, void **out) {
         c->own_stream = true;
     }
     for (auto &e : c->ev) cudaEventCreate(&e);
+    if (cudaStreamCreateWithFlags(&c->cst, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_field, cudaEventDisableTiming) != cudaSuccess) {
+        sf_destroy(c);
+        return SF_CUDA_ERROR;
+    }
     *out = c;
     return SF_OK;
 }
@@ -731,6 +774,7 @@ void sf_destroy(void *p) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->st) cudaStreamSynchronize(c->st);
+    if (c->cst) cudaStreamSynchronize(c->cst);
     // networks created on this context lose their device state; their handles stay valid for sf_unet_destroy
     for (void *p : c->nets) {
         auto *h = reinterpret_cast<NetHandle *>(p);
@@ -743,6 +787,9 @@ void sf_destroy(void *p) {
     c->mag.reset();
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
+    if (c->ev_in) cudaEventDestroy(c->ev_in);
+    if (c->ev_field) cudaEventDestroy(c->ev_field);
+    if (c->cst) cudaStreamDestroy(c->cst);
     if (c->own_stream) cudaStreamDestroy(c->st);
     delete c;
 }
@@ -945,6 +992,29 @@ sf_status sf_levelset_upload(void *ctx, const sf_grid *g, const double *phi) {
     CK(cudaStreamSynchronize(c->st));
     c->rls = true;
     c->rls_dims = d;
+    return SF_OK;
+}
+
+sf_status sf_applied_field_prefetch(void *ctx, const sf_grid *g, const double *const hext[3]) {
+    Ctx *c = C(ctx);
+    if (!c) return SF_BAD_ARG;
+    if (!grid_ok(g) || !hext) return fail(c, SF_BAD_ARG, "bad grid or applied-field pointer");
+    for (int a = 0; a < 3; a++)
+        if (!hext[a]) return fail(c, SF_BAD_ARG, "null applied-field array");
+    CK(cudaSetDevice(c->device));
+    // a copy started earlier may still be running into the buffers
+    CK(cudaStreamSynchronize(c->cst));
+    c->field_pending = c->field_ready = c->field_fresh = false;
+    c->field_bytes = 0;
+    for (int a = 0; a < 3; a++) {
+        const size_t bytes = 8 * (size_t)face_count(g, a);
+        CK(c->pfield[a].ensure(bytes));
+        c->field_src[a] = hext[a];
+        c->field_n[a] = face_count(g, a);
+        c->field_bytes += (long long)bytes;
+    }
+    c->field_dims = make_dims(g->nx, g->ny, g->nz);
+    c->field_pending = true;
     return SF_OK;
 }
 

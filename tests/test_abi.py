@@ -127,6 +127,16 @@ def test_noalloc_rejects_bad_arguments_before_any_device_call():
     assert call(phi=0) == abi.SF_BAD_ARG and call(psi=0) == abi.SF_BAD_ARG and call(result=0) == abi.SF_BAD_ARG
 
 
+def test_prefetch_rejects_bad_arguments_before_any_device_call():
+    """sf_applied_field_prefetch checks its arguments on the host: a null context, grid or field pointer, or a
+    null field entry, is SF_BAD_ARG without touching a device."""
+    lib = pkg().load_library()
+    abi = pkg()._abi
+    g = pkg().StaggeredGrid.from_origin(0.1, (8, 8, 8)).c_grid()
+    fake = 4096
+    assert lib.sf_applied_field_prefetch(None, C.byref(g), abi.p3([fake, fake, fake])) == abi.SF_BAD_ARG
+
+
 def test_package_has_no_cpu_fallback(monkeypatch):
     """The package raises when the library is missing instead of computing on the CPU."""
     sf = pkg()

@@ -69,3 +69,63 @@ def test_resident_inputs_not_ready(sfpkg):
         P.project(v, None, None)
     finally:
         ctx.close()
+
+
+def test_prefetched_applied_field_same_bits(sfpkg, gpu_ctx):
+    """sf_applied_field_prefetch: the copy started under a pressure projection (pinned host arrays, side stream)
+    and read by the magnetic call with hext = NULL gives the bits of the call that passes hext; a later call with
+    NULL reads the same field again; the prefetched bytes are counted once."""
+    import torch
+    sc = scenes().pool_sphere(48, seed=10)
+    g = sc.grid
+    o_p = sfpkg.options("pressure", precision="mixed")
+    o_m = sfpkg.options("magnetic", precision="mixed", warm_start=0)
+    M = sfpkg.MagneticField(g, sc.chi, sc.band_width, gpu_ctx)
+    s1 = M.solve(sc.phi, sc.hext, opts=o_m)
+    psi1, H1 = M.potential.copy(), [h.copy() for h in M.total_field]
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+        t.numpy()[...] = a
+        return t.numpy()
+
+    hp = [pinned(h) for h in sc.hext]
+    gpu_ctx.prefetch_applied_field(g, hp)
+    P = sfpkg.Pressure(g, gpu_ctx)
+    P.project([a.copy() for a in sc.vel], sc.phi, sc.frac, opts=o_p)
+    s2 = M.solve(sc.phi, None, opts=o_m)
+    assert np.array_equal(M.potential, psi1)
+    for a in range(3):
+        assert np.array_equal(M.total_field[a], H1[a])
+    assert s2["h2d_bytes"] == s1["h2d_bytes"]
+    s3 = M.solve(sc.phi, None, opts=o_m)  # no new prefetch: the same field, no copy
+    assert np.array_equal(M.potential, psi1)
+    nf = sum(int(np.prod(g.face_shape(a))) for a in range(3))
+    assert s2["h2d_bytes"] - s3["h2d_bytes"] == 8 * nf
+    # a prefetch not followed by a pressure call is copied by the magnetic call itself
+    gpu_ctx.prefetch_applied_field(g, [2.0 * h for h in sc.hext])
+    M.solve(sc.phi, None, opts=o_m)
+    H2 = [h.copy() for h in M.total_field]
+    M.solve(sc.phi, [2.0 * h for h in sc.hext], opts=o_m)
+    for a in range(3):
+        assert np.array_equal(M.total_field[a], H2[a])
+
+
+def test_prefetched_applied_field_not_ready(sfpkg):
+    ctx = sfpkg.Context(0)
+    try:
+        sc = scenes().pool(16, seed=3)
+        M = sfpkg.MagneticField(sc.grid, sc.chi, sc.band_width, ctx)
+        with pytest.raises(sfpkg.SolveError) as e:
+            M.solve(sc.phi, None)
+        assert e.value.status == sfpkg._abi.SF_NOT_READY
+        other = scenes().pool(12, seed=3)
+        ctx.prefetch_applied_field(other.grid, other.hext)
+        with pytest.raises(sfpkg.SolveError) as e:
+            M.solve(sc.phi, None)
+        assert e.value.status == sfpkg._abi.SF_NOT_READY
+        null_entry = sfpkg._abi.p3([0, 0, 0])
+        assert ctx.lib.sf_applied_field_prefetch(ctx.handle, C.byref(sc.grid.c_grid()), null_entry) == \
+            sfpkg._abi.SF_BAD_ARG
+    finally:
+        ctx.close()
