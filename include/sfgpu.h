@@ -214,11 +214,11 @@ SF_EXPORT sf_status sf_unet_backward_dev(void *net, const sf_grid *g, const void
 /* one Adam step (lr) on the scale-invariant loss 1 - (o.t)^2 / (|o|^2 |t|^2); *loss receives the loss */
 SF_EXPORT sf_status sf_unet_train_step_dev(void *net, const sf_grid *g, const void *features_bf16,
                                            const float *target, float lr, double *loss);
-/* convolution kernels: 0 = warp-level tensor-core MMA (mma.sync, default), 1 = tcgen05 tensor cores with TMA
+/* convolution kernels: 0 = warp-level tensor-core MMA (mma.sync), 1 (default) = tcgen05 tensor cores with TMA
  * staging and TMEM accumulators for the forward, input-gradient and weight-gradient convolutions (layers whose grid
- * holds one brick, 32 x 4 for the forward and input gradient, 32 x 4 x 2 for the weight gradient; others use
- * mode 0), 2 = tcgen05 for the weight gradient alone.  sf_unet_tc_launches counts the tcgen05 convolutions
- * launched so far. */
+ * holds one brick: 32 x 4 for the forward and input gradient, 128 x 6 x 4 for the 16-channel line kernel, 32 x 4 x 2
+ * for the weight gradient; others use mode 0), 2 = tcgen05 for the weight gradient alone.  sf_unet_tc_launches
+ * counts the tcgen05 convolutions launched so far. */
 SF_EXPORT sf_status sf_unet_set_mode(void *net, int mode);
 SF_EXPORT long long sf_unet_tc_launches(void *net);
 /* attach (or detach with NULL) the network used by SF_PREC_LEARNED solves on this context */

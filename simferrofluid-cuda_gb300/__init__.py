@@ -249,8 +249,8 @@ class Network:
         return loss.value
 
     def set_mode(self, mode):
-        """Convolution kernels: "mma" (warp-level mma.sync), "tcgen05" (TMA + TMEM for the forward, input-gradient
-        and weight-gradient convolutions) or "tcgen05_wgrad" (tcgen05 for the weight gradient alone)."""
+        """Convolution kernels: "tcgen05" (default: TMA + TMEM for the forward, input-gradient and weight-gradient
+        convolutions), "mma" (warp-level mma.sync) or "tcgen05_wgrad" (tcgen05 for the weight gradient alone)."""
         m = {"mma": 0, "tcgen05": 1, "tcgen05_wgrad": 2}.get(mode, mode)
         self._ok(self.ctx.lib.sf_unet_set_mode(self.handle, int(m)), "set_mode")
 

@@ -169,7 +169,7 @@ struct NetStep final : LearnedStep {
         cudaError_t e = c->net->set_rhs_channel(d, r, rms > 0 ? 1.0 / rms : 0.0, feat);
         if (e != cudaSuccess) return e;
         if ((e = c->net->forward(d, feat, y, false)) != cudaSuccess) return e;
-        if (c->net->mode() == 1 && (e = c->net->check_device_errors()) != cudaSuccess) return e;
+        if (c->net->mode() >= 1 && (e = c->net->check_device_errors()) != cudaSuccess) return e;
         return cudaSuccess;
     }
 };

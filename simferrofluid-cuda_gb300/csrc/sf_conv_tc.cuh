@@ -254,6 +254,214 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     }
 }
 
+// ------------------------------------------------------------------------------------------------ 16-channel lines
+// Forward (and input gradient) for Cin = 16 on grids with nz >= 128: a persistent CTA per SM takes bricks of
+// 128 (z) x 4 (y) x 2 (x) voxels, eight M tiles of one z line of 128 voxels each.  Per z shift dz one TMA box per
+// 8-channel chunk, (8, 128 z, 6 y, 4 x) from (z0 + dz, y0 - 1, x0 - 1), carries the tile rows of all nine (dx, dy)
+// taps: tile (yy, xx) of tap (dx, dy) starts 2 KB x ((yy + 1 + dy) + 6 (xx + 1 + dx)) into the box, so each box
+// is read once for nine taps (the 27-box kernel above reads nine times as many rows).  The 27 taps' weights stay in
+// shared memory for the CTA's whole run.  Warp 1 lane 0 issues the TMA loads through two stages, warp 0 lane 0 the
+// MMAs (M = 128, N = Cout, K = 16 = two chunks) into one of two TMEM accumulator sets, and warps 2-5 read the other
+// set back (bias + ReLU + BF16, or FP32), so the epilogue of a brick overlaps the MMAs of the next.  Every wait is
+// bounded; a timeout stops all roles, drains the copies in flight and sets the error flag.
+constexpr int kLineZ = 128, kLineY = 4, kLineX = 2, kLineTiles = kLineY * kLineX;
+
+template <int CO>
+struct LineLayout {
+    static constexpr uint32_t kBoxRows = kLineZ * (kLineY + 2) * (kLineX + 2);  // 3072
+    static constexpr uint32_t kChunkBytes = kBoxRows * 16u;                     // 48 KB
+    static constexpr uint32_t kStageBytes = 2u * kChunkBytes;
+    static constexpr uint32_t kWChunkRaw = 27u * CO * 16u;  // [tap][co] rows of 8 channels
+    static constexpr uint32_t kWChunk = (kWChunkRaw + 1023u) & ~1023u;
+    static constexpr uint32_t kCols = kLineTiles * CO;  // one accumulator set
+    static constexpr uint32_t kAlloc = 2u * kCols <= 256u ? 256u : 512u;
+    static constexpr uint32_t kSmemBytes = 1024u + 2u * kStageBytes + 2u * kWChunk + 256u;
+    static_assert(2u * kCols <= 512u && kSmemBytes <= 227u * 1024u, "line layout");
+};
+
+template <int CO, int EPI>
+__global__ void __launch_bounds__(192, 1) k_conv_tc_line(const __grid_constant__ CUtensorMap tmap_x,
+                                                         const __grid_constant__ CUtensorMap tmap_w, Dims d,
+                                                         const float *__restrict__ bias, void *__restrict__ yout,
+                                                         int *err) {
+    using L = LineLayout<CO>;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t *wbuf = smem + 2 * L::kStageBytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(wbuf + 2 * L::kWChunk);
+    // barriers: [0,2) stage full, [2,4) stage empty, 4 weights, [5,7) accumulators full, [7,9) accumulators
+    // empty (four epilogue warps), 9 done
+    volatile uint32_t *sh = reinterpret_cast<volatile uint32_t *>(bars + 10);
+    // sh: [0] TMEM base, [1] abort, [2] stage jobs issued, [3] stage jobs waited, [4] weights waited
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + 2), wfull = smem_u32(bars + 4),
+                   tfull0 = smem_u32(bars + 5), tempty0 = smem_u32(bars + 7), done = smem_u32(bars + 9);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int bz_n = (d.nz + kLineZ - 1) / kLineZ, by_n = (d.ny + kLineY - 1) / kLineY;
+    const long long nbricks = (long long)bz_n * by_n * ((d.nx + kLineX - 1) / kLineX);
+    const int nb = nbricks > blockIdx.x ? (int)((nbricks - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+    auto brick = [&](int bi, int &z0, int &y0, int &x0) {
+        const long long br = blockIdx.x + (long long)bi * gridDim.x;
+        z0 = kLineZ * (int)(br % bz_n);
+        y0 = kLineY * (int)((br / bz_n) % by_n);
+        x0 = kLineX * (int)(br / ((long long)bz_n * by_n));
+    };
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < 2; s++) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+            mbar_init(tfull0 + 8 * s, 1);
+            mbar_init(tempty0 + 8 * s, 4);
+        }
+        mbar_init(wfull, 1);
+        mbar_init(done, 1);
+        for (int k = 1; k < 5; k++) sh[k] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(const_cast<uint32_t *>(sh))),
+                     "r"(L::kAlloc)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = sh[0];
+
+    if (warp == 1 && lane == 0 && nb > 0) {  // TMA producer
+        mbar_expect_tx(wfull, 2u * L::kWChunkRaw);
+        for (int c = 0; c < 2; c++) tma_load_3d(smem_u32(wbuf + c * L::kWChunk), &tmap_w, wfull, 8 * c, 0, 0);
+        int q = 0;
+        for (int bi = 0; bi < nb && !sh[1]; bi++) {
+            int z0, y0, x0;
+            brick(bi, z0, y0, x0);
+            for (int dz = 0; dz < 3 && !sh[1]; dz++, q++) {
+                const int s = q & 1;
+                if (q >= 2 && !mbar_wait(empty0 + 8 * s, (uint32_t)((q >> 1) - 1) & 1u)) {
+                    sh[1] = 1;
+                    break;
+                }
+                mbar_expect_tx(full0 + 8 * s, L::kStageBytes);
+                for (int c = 0; c < 2; c++)
+                    tma_load_4d(smem_u32(smem + s * L::kStageBytes + c * L::kChunkBytes), &tmap_x, full0 + 8 * s,
+                                8 * c, z0 + dz - 1, y0 - 1, x0 - 1);
+                sh[2] = (uint32_t)(q + 1);
+            }
+        }
+    } else if (warp == 0 && lane == 0 && nb > 0) {  // MMA issuer
+        constexpr uint32_t idesc = instr_desc_bf16(CO);
+        bool any = false;
+        if (!mbar_wait(wfull, 0)) sh[1] = 1;
+        else sh[4] = 1;
+        int q = 0;
+        for (int bi = 0; bi < nb && !sh[1]; bi++) {
+            const int tb = bi & 1;
+            if (bi >= 2 && !mbar_wait(tempty0 + 8 * tb, (uint32_t)((bi - 2) >> 1) & 1u)) {
+                sh[1] = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int dz = 0; dz < 3; dz++, q++) {
+                const int s = q & 1;
+                if (!mbar_wait(full0 + 8 * s, (uint32_t)(q >> 1) & 1u)) {
+                    sh[1] = 1;
+                    break;
+                }
+                sh[3] = (uint32_t)(q + 1);
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a0 = smem_u32(smem + s * L::kStageBytes);
+#pragma unroll 1
+                for (int pr = 0; pr < 9; pr++) {
+                    const int dx = pr / 3 - 1, dy = pr % 3 - 1, t = 9 * (dx + 1) + 3 * (dy + 1) + dz;
+                    const uint64_t bd = smem_desc(smem_u32(wbuf) + (uint32_t)t * CO * 16u, L::kWChunk, 128u);
+#pragma unroll
+                    for (int tile = 0; tile < kLineTiles; tile++) {
+                        const int yy = tile % kLineY, xx = tile / kLineY;
+                        const uint64_t ad = smem_desc(
+                            a0 + 2048u * (uint32_t)((yy + 1 + dy) + (kLineY + 2) * (xx + 1 + dx)), L::kChunkBytes, 128u);
+                        mma_bf16(tmem + (uint32_t)(tb * L::kCols + tile * CO), ad, bd, idesc,
+                                 (dz > 0 || pr > 0) ? 1u : 0u);
+                    }
+                }
+                any = true;
+                mma_commit(empty0 + 8 * s);
+            }
+            if (sh[1]) break;
+            mma_commit(tfull0 + 8 * tb);
+        }
+        if (any) {  // completion of every MMA issued (also on the error path, before TMEM is released)
+            mma_commit(done);
+            if (!mbar_wait(done, 0)) sh[1] = 1;
+        }
+    } else if (warp >= 2 && nb > 0) {  // epilogue
+        const int q4 = warp & 3;  // TMEM lane quarter of this warp
+        for (int bi = 0; bi < nb; bi++) {
+            const int tb = bi & 1;
+            const uint32_t par = (uint32_t)(bi >> 1) & 1u;
+            // lane 0 decides for the warp, so that the warp-collective TMEM loads below are never divergent
+            int go = 0;
+            if (lane == 0) go = (!sh[1] && mbar_wait(tfull0 + 8 * tb, par)) ? 1 : 0;
+            go = __shfl_sync(0xffffffffu, go, 0);
+            if (!go) {
+                if (lane == 0) sh[1] = 1;
+                break;
+            }
+            mbar_wait(tfull0 + 8 * tb, par);  // completed: returns at once, with this thread's acquire
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            int z0, y0, x0;
+            brick(bi, z0, y0, x0);
+            const int z = z0 + 32 * q4 + lane;
+#pragma unroll 1
+            for (int tile = 0; tile < kLineTiles; tile++) {
+                const int yy = y0 + tile % kLineY, xx = x0 + tile / kLineY;
+                const bool inb = z < d.nz && yy < d.ny && xx < d.nx;
+                const long long v = inb ? cid(d, xx, yy, z) : 0;
+#pragma unroll
+                for (int c0 = 0; c0 < CO; c0 += 16) {
+                    float acc[16];
+                    tmem_ld_x16<16>(tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(tb * L::kCols + tile * CO + c0),
+                                    acc);
+                    if (inb && EPI == 0) {
+                        uint32_t pk[8];
+#pragma unroll
+                        for (int k = 0; k < 8; k++) {
+                            const float a0 = fmaxf(acc[2 * k] + bias[c0 + 2 * k], 0.f);
+                            const float a1 = fmaxf(acc[2 * k + 1] + bias[c0 + 2 * k + 1], 0.f);
+                            __nv_bfloat162 h2 = __floats2bfloat162_rn(a0, a1);
+                            pk[k] = *reinterpret_cast<uint32_t *>(&h2);
+                        }
+                        uint4 *dst = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(yout) + v * CO + c0);
+                        dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                        dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                    } else if (inb) {
+                        float4 *dst = reinterpret_cast<float4 *>(reinterpret_cast<float *>(yout) + v * CO + c0);
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            dst[k] = make_float4(acc[4 * k], acc[4 * k + 1], acc[4 * k + 2], acc[4 * k + 3]);
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty0 + 8 * tb) : "memory");
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && sh[1]) {  // drain copies still in flight into this CTA's shared memory (bounded)
+        for (uint32_t q = sh[3]; q < sh[2]; q++) mbar_wait(full0 + 8 * (q & 1), (q >> 1) & 1u);
+        if (!sh[4] && nb > 0) mbar_wait(wfull, 0);
+        atomicCAS(err, 0, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(L::kAlloc) : "memory");
+    }
+}
+
 // ------------------------------------------------------------------------------------------------ weight gradient
 // dW[tap][co][ci] = sum over voxels v of dY[v][co] X[v + off(tap)][ci]: GEMMs with M = Cout, K = voxels and
 // N = (dz, Cin), both operands K-major with 8 consecutive z per 16-byte row.  k_to_chmajor makes channel-major copies

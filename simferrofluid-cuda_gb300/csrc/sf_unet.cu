@@ -113,9 +113,49 @@ cudaError_t launch_tc_mt(cudaStream_t st, const Dims &d, const bf16 *x, const bf
     return cudaGetLastError();
 }
 
+// 16 input channels on grids holding a 128 x 6 x 4 box: the line kernel (one halo'd box per z shift for nine taps)
+bool line_shape_ok(int ci, int co, const Dims &d) {
+    return ci == 16 && (co == 16 || co == 32) && d.nz >= tc::kLineZ && d.ny >= tc::kLineY + 2 &&
+           d.nx >= tc::kLineX + 2;
+}
+
+template <int CO, int EPI>
+cudaError_t launch_tc_line(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *w, const float *b, void *y,
+                           int *err) {
+    auto enc = tensor_map_encoder();
+    if (!enc || !aligned16(x) || !aligned16(w) || !aligned16(y)) return cudaErrorInvalidValue;
+    CUtensorMap mx, mw;
+    const cuuint64_t xd[4] = {16, (cuuint64_t)d.nz, (cuuint64_t)d.ny, (cuuint64_t)d.nx};
+    const cuuint64_t xs[3] = {16 * 2, (cuuint64_t)d.nz * 16 * 2, (cuuint64_t)d.ny * d.nz * 16 * 2};
+    const cuuint32_t xb[4] = {8, tc::kLineZ, tc::kLineY + 2, tc::kLineX + 2};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    if (enc(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(x), xd, xs, xb, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    const cuuint64_t wd[3] = {16, (cuuint64_t)CO, 27};
+    const cuuint64_t ws[2] = {16 * 2, (cuuint64_t)CO * 16 * 2};
+    const cuuint32_t wb[3] = {8, (cuuint32_t)CO, 27};
+    if (enc(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16 *>(w), wd, ws, wb, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    using L = tc::LineLayout<CO>;
+    cudaError_t e = cudaFuncSetAttribute(tc::k_conv_tc_line<CO, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)L::kSmemBytes);
+    if (e != cudaSuccess) return e;
+    const long long nbricks = (long long)((d.nz + tc::kLineZ - 1) / tc::kLineZ) *
+                              ((d.ny + tc::kLineY - 1) / tc::kLineY) * ((d.nx + tc::kLineX - 1) / tc::kLineX);
+    const int grid = (int)(nbricks < 152 ? nbricks : 152);
+    tc::k_conv_tc_line<CO, EPI><<<grid, 192, L::kSmemBytes, st>>>(mx, mw, d, b, y, err);
+    return cudaGetLastError();
+}
+
 template <int CI, int CO, int EPI>
 cudaError_t launch_tc(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *w, const float *b, void *y,
                       int *err) {
+    if constexpr (CI == 16 && (CO == 16 || CO == 32))
+        if (line_shape_ok(CI, CO, d)) return launch_tc_line<CO, EPI>(st, d, x, w, b, y, err);
     constexpr int MT = tc::tiles_per_cta<CI, CO>();
     if (d.ny >= tc::kTileY * MT) return launch_tc_mt<CI, CO, EPI, MT>(st, d, x, w, b, y, err);
     return launch_tc_mt<CI, CO, EPI, 1>(st, d, x, w, b, y, err);

@@ -52,8 +52,8 @@ class UNet {
     // channel 0 of existing features set to r * inv_rms (FP32 r on the cells), the other channels unchanged
     cudaError_t set_rhs_channel(const Dims &d, const float *r, double inv_rms, __nv_bfloat16 *feat);
     float *output() { return out_; }
-    // convolution kernels: 0 warp-level MMA (mma.sync) throughout; 1 tcgen05 + TMA for the forward, input-gradient
-    // and weight-gradient convolutions; 2 tcgen05 for the weight gradient alone (the rest as mode 0)
+    // convolution kernels: 0 warp-level MMA (mma.sync) throughout; 1 (default) tcgen05 + TMA for the forward,
+    // input-gradient and weight-gradient convolutions; 2 tcgen05 for the weight gradient alone (the rest as mode 0)
     void set_mode(int m) { mode_ = m; }
     int mode() const { return mode_; }
     long long tc_launches() const { return tc_launches_; }
@@ -91,7 +91,7 @@ class UNet {
     float *out_ = nullptr, *dout_ = nullptr, *wpart_ = nullptr, *hpart_ = nullptr;
     double *dots_ = nullptr, *dots_host_ = nullptr, *redpart_ = nullptr;
     long long wpart_elems_ = 0;
-    int mode_ = 0;
+    int mode_ = 1;
     double active_ = 0;
     int *err_ = nullptr;
     long long tc_launches_ = 0;

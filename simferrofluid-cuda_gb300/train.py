@@ -142,6 +142,35 @@ def evaluate(ctx, net, scenes=64, n=256, seed=777, tol=1e-6, log=None):
     return rows
 
 
+def time_forward(ctx, net, n, reps=5):
+    """Milliseconds per network forward at n^3 (inference workspace) with the warp-MMA and the tcgen05 kernels,
+    CUDA events on the context's stream; also the largest difference between the two outputs."""
+    import torch
+    sf = _pkg()
+    g = sf.StaggeredGrid.from_origin(1.0 / n, (n, n, n))
+    dev = torch.device("cuda", ctx.device)
+    rng = np.random.default_rng(1)
+    feat = torch.from_numpy((rng.standard_normal((n ** 3, 16)) * 0.5).astype(np.float32)).to(dev).to(torch.bfloat16)
+    out, res = {}, {}
+    for mode, name in ((0, "mma"), (1, "tcgen05")):
+        net.set_mode(mode)
+        o = torch.zeros(n ** 3, dtype=torch.float32, device=dev)
+        net.forward(g, feat, o)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            net.forward(g, feat, o)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        res[name] = e0.elapsed_time(e1) / reps
+        out[name] = o
+    res["max_abs_diff"] = float((out["mma"] - out["tcgen05"]).abs().max())
+    res["max_abs_out"] = float(out["mma"].abs().max())
+    res["n"] = n
+    return res
+
+
 def summarize(rows):
     out = {}
     for kind in (0, 1):
@@ -174,12 +203,17 @@ def main():
     ap.add_argument("--eval-n", type=int, default=256)
     ap.add_argument("--report", default=None, help="write the training/evaluation summary (JSON) here")
     ap.add_argument("--tc", action="store_true",
-                    help="forward and input-gradient convolutions on the tcgen05 kernels (Network.set_mode(1))")
+                    help="every convolution on the tcgen05 kernels (Network.set_mode(1), the default)")
+    ap.add_argument("--mma", action="store_true",
+                    help="every convolution on the warp-level MMA kernels (Network.set_mode(0))")
+    ap.add_argument("--time-forward", type=int, default=0, metavar="N",
+                    help="time the network forward at N^3 with each kernel set (CUDA events, 5 passes after one "
+                         "warm-up) and add it to the report")
     args = ap.parse_args()
     sf = _pkg()
     import torch
     torch.cuda.set_device(0)
-    ctx = sf.Context(0)
+    ctx = sf.Context(0, stream=torch.cuda.current_stream().cuda_stream)  # torch's stream: events time the library
     net = sf.Network(ctx)
     if args.init:
         net.load(args.init)
@@ -192,10 +226,9 @@ def main():
             flat.append((from_rng.standard_normal(taps * co * ci) * std).astype(np.float32))
             flat.append(np.zeros(co, np.float32))
         net.set_params(np.concatenate(flat))
-    if args.tc:
-        net.set_mode(1)
+    net.set_mode(0 if args.mma and not args.tc else 1)
     ctx.set_network(net)
-    report = {"samples": args.samples, "n": args.n, "lr": args.lr, "seed": args.seed, "tcgen05": bool(args.tc)}
+    report = {"samples": args.samples, "n": args.n, "lr": args.lr, "seed": args.seed, "tcgen05": not (args.mma and not args.tc)}
     if args.samples > 0:
         t0 = time.time()
         losses = train(ctx, net, args.samples, args.n, args.lr, args.seed, log=lambda m: print(m, flush=True))
@@ -208,6 +241,9 @@ def main():
         report.update(train_s=round(time.time() - t0, 1), loss_first=float(np.mean(losses[:k])),
                       loss_last=float(np.mean(losses[-k:])), pressure_loss_last=float(np.mean(lp[-kk:])),
                       potential_loss_last=float(np.mean(lm[-kk:])), out=args.out)
+    if args.time_forward > 0:
+        report["forward_ms"] = time_forward(ctx, net, args.time_forward)
+        net.set_mode(0 if args.mma and not args.tc else 1)
     if args.eval > 0:
         rows = evaluate(ctx, net, args.eval, args.eval_n, log=lambda m: print(m, flush=True))
         report["eval"] = summarize(rows)

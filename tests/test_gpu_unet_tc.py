@@ -8,7 +8,9 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("shape", [(2, 4, 32), (6, 12, 40), (17, 9, 64)])
+# (5, 8, 128) and (8, 12, 256) put the 16-channel layers on the line kernel (a 128 x 6 x 4 box fits the grid;
+# at (8, 12, 256) also the 16 -> 32 layer of level 1)
+@pytest.mark.parametrize("shape", [(2, 4, 32), (6, 12, 40), (17, 9, 64), (5, 8, 128), (8, 12, 256)])
 def test_tcgen05_forward_matches_mma(sfpkg, gpu_ctx, shape):
     import torch
     from oracle import unet_ref as ref
@@ -120,4 +122,50 @@ def test_tcgen05_weight_gradient_matches_mma(sfpkg, gpu_ctx, shape):
             checked += 1
         np.testing.assert_array_equal(g1[b], g0[b])
     assert off == g0.size and checked >= 10
+    net.close()
+
+
+@pytest.mark.parametrize("shape", [(4, 6, 128), (8, 12, 256)])
+def test_tcgen05_line_gradients_against_oracle(sfpkg, gpu_ctx, shape):
+    """Grids that put the 16-channel layers on the line kernel (one halo'd box per z shift for nine taps), whose
+    tap order differs from the warp-MMA kernel's, so the BF16 activations of the two paths are no longer bit
+    for bit the same and their gradients drift apart by a few percent.  Against the FP64 oracle with the same BF16
+    rounding points (oracle/unet_ref.py) the tcgen05 gradients are as close as the warp-MMA ones: per layer the
+    relative L2 error is within twice the warp-MMA error or that error + 0.04, and its mean over the layers within
+    1.3 times the warp-MMA mean (measured at these shapes: per layer 0.5-1.8 times, means 0.9-1.17 times; both
+    paths sit 1-10% from the oracle, a layout error would sit near 100%)."""
+    import torch
+    from oracle import unet_ref as ref
+    g = sfpkg.StaggeredGrid.from_origin(1.0 / shape[0], shape)
+    P = ref.init_params(16, seed=5)
+    rng = np.random.default_rng(4)
+    x = ref.bf16(rng.standard_normal(shape + (16,)))
+    dout = rng.standard_normal(shape).astype(np.float32)
+    net = sfpkg.Network(gpu_ctx)
+    net.set_params(ref.flatten(P))
+    feat = torch.from_numpy(x).to(torch.bfloat16).cuda().contiguous()
+    out = torch.zeros(g.num_cells, dtype=torch.float32, device="cuda")
+    grads = {}
+    for mode in ("mma", "tcgen05"):
+        net.set_mode(mode)
+        before = net.tc_launches()
+        net.forward(g, feat, out)
+        grads[mode] = ref.unflatten(net.gradients(g, feat, torch.from_numpy(dout).cuda()))
+        if mode == "tcgen05":
+            assert net.tc_launches() - before >= 12
+    _, cache = ref.forward_bf16(P, x)
+    G = ref.backward_bf16(P, cache, dout.astype(np.float64))
+    errs = []
+    for name, *_ in ref.LAYERS:
+        for k in (".w", ".b"):
+            b = np.asarray(G[name + k]).reshape(grads["mma"][name + k].shape)
+            if np.linalg.norm(b) == 0:
+                continue
+            e_tc, e_mma = rel_l2(grads["tcgen05"][name + k], b), rel_l2(grads["mma"][name + k], b)
+            assert np.isfinite(grads["tcgen05"][name + k]).all()
+            assert e_tc <= max(2.0 * e_mma, e_mma + 0.04), (name + k, e_tc, e_mma)
+            errs.append((e_tc, e_mma))
+    assert len(errs) >= 28
+    e = np.array(errs)
+    assert e[:, 0].mean() <= 1.3 * e[:, 1].mean(), e.mean(axis=0)
     net.close()
