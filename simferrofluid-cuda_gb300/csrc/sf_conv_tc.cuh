@@ -254,41 +254,49 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     }
 }
 
-// ------------------------------------------------------------------------------------------------ 16-channel lines
-// Forward (and input gradient) for Cin = 16 on grids with nz >= 128: a persistent CTA per SM takes bricks of
-// 128 (z) x 4 (y) x 2 (x) voxels, eight M tiles of one z line of 128 voxels each.  Per z shift dz one TMA box per
-// 8-channel chunk, (8, 128 z, 6 y, 4 x) from (z0 + dz, y0 - 1, x0 - 1), carries the tile rows of all nine (dx, dy)
-// taps: tile (yy, xx) of tap (dx, dy) starts 2 KB x ((yy + 1 + dy) + 6 (xx + 1 + dx)) into the box, so each box
-// is read once for nine taps (the 27-box kernel above reads nine times as many rows).  The 27 taps' weights stay in
-// shared memory for the CTA's whole run.  Warp 1 lane 0 issues the TMA loads through two stages, warp 0 lane 0 the
-// MMAs (M = 128, N = Cout, K = 16 = two chunks) into one of two TMEM accumulator sets, and warps 2-5 read the other
-// set back (bias + ReLU + BF16, or FP32), so the epilogue of a brick overlaps the MMAs of the next.  Every wait is
-// bounded; a timeout stops all roles, drains the copies in flight and sets the error flag.
-constexpr int kLineZ = 128, kLineY = 4, kLineX = 2, kLineTiles = kLineY * kLineX;
+// ------------------------------------------------------------------------------------------------ z lines
+// Forward (and input gradient) for Cin = 16 or 32, Cout <= 32, on grids with nz >= 128: a persistent CTA per SM
+// takes bricks of 128 (z) x 4 (y) x LX (x) voxels (LX = 2 for 16 input channels, 1 for 32), 4 LX M tiles of one
+// z line of 128 voxels each.  A pipeline stage is one z shift dz and one pair of 8-channel chunks (K = 16): one TMA
+// box per chunk, (8, 128 z, 6 y, LX + 2 x) from (z0 + dz, y0 - 1, x0 - 1), carries the tile rows of all nine
+// (dx, dy) taps: tile (yy, xx) of tap (dx, dy) starts 2 KB x ((yy + 1 + dy) + 6 (xx + 1 + dx)) into the box, so each
+// box is read once for nine taps (the 27-box kernel above reads nine times as many rows).  The 27 taps' weights stay
+// in shared memory for the CTA's whole run.  Warp 1 lane 0 issues the TMA loads through two stages, warp 0 lane 0
+// the MMAs (M = 128, N = Cout, K = 16) into one of two TMEM accumulator sets, and warps 2-5 read the other set back
+// (bias + ReLU + BF16, or FP32), so the epilogue of a brick overlaps the MMAs of the next.  Every wait is bounded; a
+// timeout stops all roles, drains the copies in flight and sets the error flag.
+constexpr int kLineZ = 128, kLineY = 4;
 
-template <int CO>
+template <int CI>
+__host__ __device__ constexpr int line_x() {
+    return CI == 16 ? 2 : 1;
+}
+
+template <int CI, int CO>
 struct LineLayout {
-    static constexpr uint32_t kBoxRows = kLineZ * (kLineY + 2) * (kLineX + 2);  // 3072
-    static constexpr uint32_t kChunkBytes = kBoxRows * 16u;                     // 48 KB
+    static constexpr int LX = line_x<CI>(), kTiles = kLineY * LX, KP = CI / 16;  // chunk pairs
+    static constexpr uint32_t kBoxRows = kLineZ * (kLineY + 2) * (LX + 2);
+    static constexpr uint32_t kChunkBytes = kBoxRows * 16u;  // 48 KB (LX 2) or 36 KB (LX 1)
     static constexpr uint32_t kStageBytes = 2u * kChunkBytes;
     static constexpr uint32_t kWChunkRaw = 27u * CO * 16u;  // [tap][co] rows of 8 channels
     static constexpr uint32_t kWChunk = (kWChunkRaw + 1023u) & ~1023u;
-    static constexpr uint32_t kCols = kLineTiles * CO;  // one accumulator set
+    static constexpr uint32_t kCols = kTiles * CO;  // one accumulator set
     static constexpr uint32_t kAlloc = 2u * kCols <= 256u ? 256u : 512u;
-    static constexpr uint32_t kSmemBytes = 1024u + 2u * kStageBytes + 2u * kWChunk + 256u;
-    static_assert(2u * kCols <= 512u && kSmemBytes <= 227u * 1024u, "line layout");
+    static constexpr uint32_t kSmemBytes = 1024u + 2u * kStageBytes + 2u * KP * kWChunk + 256u;
+    static_assert(CI % 16 == 0 && 2u * kCols <= 512u && kSmemBytes <= 227u * 1024u, "line layout");
 };
 
-template <int CO, int EPI>
+template <int CI, int CO, int EPI>
 __global__ void __launch_bounds__(192, 1) k_conv_tc_line(const __grid_constant__ CUtensorMap tmap_x,
                                                          const __grid_constant__ CUtensorMap tmap_w, Dims d,
                                                          const float *__restrict__ bias, void *__restrict__ yout,
                                                          int *err) {
-    using L = LineLayout<CO>;
+    using L = LineLayout<CI, CO>;
+    constexpr int LX = L::LX, kTiles = L::kTiles, KP = L::KP;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *wbuf = smem + 2 * L::kStageBytes;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(wbuf + 2 * L::kWChunk);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(wbuf + 2 * KP * L::kWChunk);
     // barriers: [0,2) stage full, [2,4) stage empty, 4 weights, [5,7) accumulators full, [7,9) accumulators
     // empty (four epilogue warps), 9 done
     volatile uint32_t *sh = reinterpret_cast<volatile uint32_t *>(bars + 10);
@@ -297,13 +305,13 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc_line(const __grid_constant__
                    tfull0 = smem_u32(bars + 5), tempty0 = smem_u32(bars + 7), done = smem_u32(bars + 9);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int bz_n = (d.nz + kLineZ - 1) / kLineZ, by_n = (d.ny + kLineY - 1) / kLineY;
-    const long long nbricks = (long long)bz_n * by_n * ((d.nx + kLineX - 1) / kLineX);
+    const long long nbricks = (long long)bz_n * by_n * ((d.nx + LX - 1) / LX);
     const int nb = nbricks > blockIdx.x ? (int)((nbricks - 1 - blockIdx.x) / gridDim.x + 1) : 0;
     auto brick = [&](int bi, int &z0, int &y0, int &x0) {
         const long long br = blockIdx.x + (long long)bi * gridDim.x;
         z0 = kLineZ * (int)(br % bz_n);
         y0 = kLineY * (int)((br / bz_n) % by_n);
-        x0 = kLineX * (int)(br / ((long long)bz_n * by_n));
+        x0 = LX * (int)(br / ((long long)bz_n * by_n));
     };
 
     if (threadIdx.x == 0) {
@@ -332,14 +340,14 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc_line(const __grid_constant__
     const uint32_t tmem = sh[0];
 
     if (warp == 1 && lane == 0 && nb > 0) {  // TMA producer
-        mbar_expect_tx(wfull, 2u * L::kWChunkRaw);
-        for (int c = 0; c < 2; c++) tma_load_3d(smem_u32(wbuf + c * L::kWChunk), &tmap_w, wfull, 8 * c, 0, 0);
+        mbar_expect_tx(wfull, 2u * KP * L::kWChunkRaw);
+        for (int c = 0; c < 2 * KP; c++) tma_load_3d(smem_u32(wbuf + c * L::kWChunk), &tmap_w, wfull, 8 * c, 0, 0);
         int q = 0;
         for (int bi = 0; bi < nb && !sh[1]; bi++) {
             int z0, y0, x0;
             brick(bi, z0, y0, x0);
-            for (int dz = 0; dz < 3 && !sh[1]; dz++, q++) {
-                const int s = q & 1;
+            for (int st = 0; st < 3 * KP && !sh[1]; st++, q++) {  // stage = (dz, chunk pair)
+                const int dz = st / KP, jp = st % KP, s = q & 1;
                 if (q >= 2 && !mbar_wait(empty0 + 8 * s, (uint32_t)((q >> 1) - 1) & 1u)) {
                     sh[1] = 1;
                     break;
@@ -347,7 +355,7 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc_line(const __grid_constant__
                 mbar_expect_tx(full0 + 8 * s, L::kStageBytes);
                 for (int c = 0; c < 2; c++)
                     tma_load_4d(smem_u32(smem + s * L::kStageBytes + c * L::kChunkBytes), &tmap_x, full0 + 8 * s,
-                                8 * c, z0 + dz - 1, y0 - 1, x0 - 1);
+                                8 * (2 * jp + c), z0 + dz - 1, y0 - 1, x0 - 1);
                 sh[2] = (uint32_t)(q + 1);
             }
         }
@@ -364,8 +372,8 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc_line(const __grid_constant__
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (int dz = 0; dz < 3; dz++, q++) {
-                const int s = q & 1;
+            for (int st = 0; st < 3 * KP; st++, q++) {
+                const int dz = st / KP, jp = st % KP, s = q & 1;
                 if (!mbar_wait(full0 + 8 * s, (uint32_t)(q >> 1) & 1u)) {
                     sh[1] = 1;
                     break;
@@ -376,14 +384,15 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc_line(const __grid_constant__
 #pragma unroll 1
                 for (int pr = 0; pr < 9; pr++) {
                     const int dx = pr / 3 - 1, dy = pr % 3 - 1, t = 9 * (dx + 1) + 3 * (dy + 1) + dz;
-                    const uint64_t bd = smem_desc(smem_u32(wbuf) + (uint32_t)t * CO * 16u, L::kWChunk, 128u);
+                    const uint64_t bd = smem_desc(smem_u32(wbuf) + 2u * jp * L::kWChunk + (uint32_t)t * CO * 16u,
+                                                  L::kWChunk, 128u);
 #pragma unroll
-                    for (int tile = 0; tile < kLineTiles; tile++) {
+                    for (int tile = 0; tile < kTiles; tile++) {
                         const int yy = tile % kLineY, xx = tile / kLineY;
                         const uint64_t ad = smem_desc(
                             a0 + 2048u * (uint32_t)((yy + 1 + dy) + (kLineY + 2) * (xx + 1 + dx)), L::kChunkBytes, 128u);
                         mma_bf16(tmem + (uint32_t)(tb * L::kCols + tile * CO), ad, bd, idesc,
-                                 (dz > 0 || pr > 0) ? 1u : 0u);
+                                 (st > 0 || pr > 0) ? 1u : 0u);
                     }
                 }
                 any = true;
@@ -415,7 +424,7 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc_line(const __grid_constant__
             brick(bi, z0, y0, x0);
             const int z = z0 + 32 * q4 + lane;
 #pragma unroll 1
-            for (int tile = 0; tile < kLineTiles; tile++) {
+            for (int tile = 0; tile < kTiles; tile++) {
                 const int yy = y0 + tile % kLineY, xx = x0 + tile / kLineY;
                 const bool inb = z < d.nz && yy < d.ny && xx < d.nx;
                 const long long v = inb ? cid(d, xx, yy, z) : 0;

@@ -13,6 +13,9 @@ namespace sf {
 namespace {
 constexpr int kVchunkMin = 512;
 
+// launch grid of the per-voxel grid operators: (ceil(nz x groups / 256), ny, nx)
+dim3 line_grid(const Dims &d, int groups) { return dim3((unsigned)((d.nz * groups + 255) / 256), d.ny, d.nx); }
+
 int flat_blocks(long long n) {
     long long g = (n + 255) / 256;
     if (g > 152 * 16) g = 152 * 16;
@@ -113,49 +116,51 @@ cudaError_t launch_tc_mt(cudaStream_t st, const Dims &d, const bf16 *x, const bf
     return cudaGetLastError();
 }
 
-// 16 input channels on grids holding a 128 x 6 x 4 box: the line kernel (one halo'd box per z shift for nine taps)
+// 16 or 32 input channels, at most 32 output channels, on grids holding a 128 x 6 x (LX + 2) box: the z-line
+// kernel (one halo'd box per z shift and chunk for nine taps)
 bool line_shape_ok(int ci, int co, const Dims &d) {
-    return ci == 16 && (co == 16 || co == 32) && d.nz >= tc::kLineZ && d.ny >= tc::kLineY + 2 &&
-           d.nx >= tc::kLineX + 2;
+    const int lx = ci == 16 ? tc::line_x<16>() : tc::line_x<32>();
+    return (ci == 16 || ci == 32) && (co == 16 || co == 32) && d.nz >= tc::kLineZ && d.ny >= tc::kLineY + 2 &&
+           d.nx >= lx + 2;
 }
 
-template <int CO, int EPI>
+template <int CI, int CO, int EPI>
 cudaError_t launch_tc_line(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *w, const float *b, void *y,
                            int *err) {
     auto enc = tensor_map_encoder();
     if (!enc || !aligned16(x) || !aligned16(w) || !aligned16(y)) return cudaErrorInvalidValue;
     CUtensorMap mx, mw;
-    const cuuint64_t xd[4] = {16, (cuuint64_t)d.nz, (cuuint64_t)d.ny, (cuuint64_t)d.nx};
-    const cuuint64_t xs[3] = {16 * 2, (cuuint64_t)d.nz * 16 * 2, (cuuint64_t)d.ny * d.nz * 16 * 2};
-    const cuuint32_t xb[4] = {8, tc::kLineZ, tc::kLineY + 2, tc::kLineX + 2};
+    using L = tc::LineLayout<CI, CO>;
+    const cuuint64_t xd[4] = {(cuuint64_t)CI, (cuuint64_t)d.nz, (cuuint64_t)d.ny, (cuuint64_t)d.nx};
+    const cuuint64_t xs[3] = {(cuuint64_t)CI * 2, (cuuint64_t)d.nz * CI * 2, (cuuint64_t)d.ny * d.nz * CI * 2};
+    const cuuint32_t xb[4] = {8, tc::kLineZ, tc::kLineY + 2, (cuuint32_t)L::LX + 2};
     const cuuint32_t es[4] = {1, 1, 1, 1};
     if (enc(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(x), xd, xs, xb, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
-    const cuuint64_t wd[3] = {16, (cuuint64_t)CO, 27};
-    const cuuint64_t ws[2] = {16 * 2, (cuuint64_t)CO * 16 * 2};
+    const cuuint64_t wd[3] = {(cuuint64_t)CI, (cuuint64_t)CO, 27};
+    const cuuint64_t ws[2] = {(cuuint64_t)CI * 2, (cuuint64_t)CO * CI * 2};
     const cuuint32_t wb[3] = {8, (cuuint32_t)CO, 27};
     if (enc(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16 *>(w), wd, ws, wb, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
-    using L = tc::LineLayout<CO>;
-    cudaError_t e = cudaFuncSetAttribute(tc::k_conv_tc_line<CO, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)L::kSmemBytes);
+    cudaError_t e = cudaFuncSetAttribute(tc::k_conv_tc_line<CI, CO, EPI>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::kSmemBytes);
     if (e != cudaSuccess) return e;
     const long long nbricks = (long long)((d.nz + tc::kLineZ - 1) / tc::kLineZ) *
-                              ((d.ny + tc::kLineY - 1) / tc::kLineY) * ((d.nx + tc::kLineX - 1) / tc::kLineX);
+                              ((d.ny + tc::kLineY - 1) / tc::kLineY) * ((d.nx + L::LX - 1) / L::LX);
     const int grid = (int)(nbricks < 152 ? nbricks : 152);
-    tc::k_conv_tc_line<CO, EPI><<<grid, 192, L::kSmemBytes, st>>>(mx, mw, d, b, y, err);
+    tc::k_conv_tc_line<CI, CO, EPI><<<grid, 192, L::kSmemBytes, st>>>(mx, mw, d, b, y, err);
     return cudaGetLastError();
 }
 
 template <int CI, int CO, int EPI>
 cudaError_t launch_tc(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *w, const float *b, void *y,
                       int *err) {
-    if constexpr (CI == 16 && (CO == 16 || CO == 32))
-        if (line_shape_ok(CI, CO, d)) return launch_tc_line<CO, EPI>(st, d, x, w, b, y, err);
+    if constexpr ((CI == 16 || CI == 32) && (CO == 16 || CO == 32))
+        if (line_shape_ok(CI, CO, d)) return launch_tc_line<CI, CO, EPI>(st, d, x, w, b, y, err);
     constexpr int MT = tc::tiles_per_cta<CI, CO>();
     if (d.ny >= tc::kTileY * MT) return launch_tc_mt<CI, CO, EPI, MT>(st, d, x, w, b, y, err);
     return launch_tc_mt<CI, CO, EPI, 1>(st, d, x, w, b, y, err);
@@ -445,26 +450,26 @@ cudaError_t UNet::forward(const Dims &d, const bf16 *feat, float *out, bool trai
     const Dims &d0 = dims_[0], &d1 = dims_[1], &d2 = dims_[2], &d3 = dims_[3];
     conv_fwd(Ls[0], d0, feat, A0a);
     conv_fwd(Ls[1], d0, A0a, S0);
-    k_pool<<<flat_blocks(d1.n * 16), 256, 0, st_>>>(d0, d1, 16, S0, P1);
+    k_pool<16><<<line_grid(d1, 2), 256, 0, st_>>>(d0, d1, S0, P1);
     conv_fwd(Ls[2], d1, P1, A1a);
     conv_fwd(Ls[3], d1, A1a, S1);
-    k_pool<<<flat_blocks(d2.n * 32), 256, 0, st_>>>(d1, d2, 32, S1, P2);
+    k_pool<32><<<line_grid(d2, 4), 256, 0, st_>>>(d1, d2, S1, P2);
     conv_fwd(Ls[4], d2, P2, A2a);
     conv_fwd(Ls[5], d2, A2a, S2);
-    k_pool<<<flat_blocks(d3.n * 64), 256, 0, st_>>>(d2, d3, 64, S2, P3);
+    k_pool<64><<<line_grid(d3, 8), 256, 0, st_>>>(d2, d3, S2, P3);
     conv_fwd(Ls[6], d3, P3, A3a);
     conv_fwd(Ls[7], d3, A3a, A3b);
-    k_up_add<<<flat_blocks(d2.n * 64), 256, 0, st_>>>(d2, d3, 64, A3b, S2, U2);
+    k_up_add<64><<<line_grid(d2, 8), 256, 0, st_>>>(d2, d3, A3b, S2, U2);
     conv_fwd(Ls[8], d2, U2, D2a);
     conv_fwd(Ls[9], d2, D2a, D2b);
-    k_up_add<<<flat_blocks(d1.n * 32), 256, 0, st_>>>(d1, d2, 32, D2b, S1, U1);
+    k_up_add<32><<<line_grid(d1, 4), 256, 0, st_>>>(d1, d2, D2b, S1, U1);
     conv_fwd(Ls[10], d1, U1, D1a);
     conv_fwd(Ls[11], d1, D1a, D1b);
-    k_up_add<<<flat_blocks(d0.n * 16), 256, 0, st_>>>(d0, d1, 16, D1b, S0, U0);
+    k_up_add<16><<<line_grid(d0, 2), 256, 0, st_>>>(d0, d1, D1b, S0, U0);
     conv_fwd(Ls[12], d0, U0, D0a);
     conv_fwd(Ls[13], d0, D0a, D0b);
     const ConvLayer &H = Ls[14];
-    k_head_fwd<<<flat_blocks(d0.n), 256, 0, st_>>>(d0.n, 16, D0b, p_ + H.woff, p_ + H.boff, out ? out : out_);
+    k_head_fwd<<<flat_blocks(d0.n), 256, 0, st_>>>(d0.n, D0b, p_ + H.woff, p_ + H.boff, out ? out : out_);
     return cudaGetLastError();
 }
 
@@ -526,22 +531,22 @@ cudaError_t UNet::backward(const Dims &d, const float *dout) {
     }
     conv_bwd(Ls[13], d0, D0a, D0b, gA[0], gB[0]);
     conv_bwd(Ls[12], d0, U0, D0a, gB[0], gU[0]);
-    k_up_back<<<flat_blocks(d1.n * 16), 256, 0, st_>>>(d0, d1, 16, gU[0], gA[1]);
+    k_up_back<16><<<line_grid(d1, 4), 256, 0, st_>>>(d0, d1, gU[0], gA[1]);
     conv_bwd(Ls[11], d1, D1a, D1b, gA[1], gB[1]);
     conv_bwd(Ls[10], d1, U1, D1a, gB[1], gU[1]);
-    k_up_back<<<flat_blocks(d2.n * 32), 256, 0, st_>>>(d1, d2, 32, gU[1], gA[2]);
+    k_up_back<32><<<line_grid(d2, 8), 256, 0, st_>>>(d1, d2, gU[1], gA[2]);
     conv_bwd(Ls[9], d2, D2a, D2b, gA[2], gB[2]);
     conv_bwd(Ls[8], d2, U2, D2a, gB[2], gU[2]);
-    k_up_back<<<flat_blocks(d3.n * 64), 256, 0, st_>>>(d2, d3, 64, gU[2], gA[3]);
+    k_up_back<64><<<line_grid(d3, 16), 256, 0, st_>>>(d2, d3, gU[2], gA[3]);
     conv_bwd(Ls[7], d3, A3a, A3b, gA[3], gB[3]);
     conv_bwd(Ls[6], d3, P3, A3a, gB[3], gA[3]);
-    k_pool_back<<<flat_blocks(d2.n * 64), 256, 0, st_>>>(d2, d3, 64, gA[3], gU[2], gA[2]);
+    k_pool_back<64><<<line_grid(d2, 16), 256, 0, st_>>>(d2, d3, gA[3], gU[2], gA[2]);
     conv_bwd(Ls[5], d2, A2a, S2, gA[2], gB[2]);
     conv_bwd(Ls[4], d2, P2, A2a, gB[2], gA[2]);
-    k_pool_back<<<flat_blocks(d1.n * 32), 256, 0, st_>>>(d1, d2, 32, gA[2], gU[1], gA[1]);
+    k_pool_back<32><<<line_grid(d1, 8), 256, 0, st_>>>(d1, d2, gA[2], gU[1], gA[1]);
     conv_bwd(Ls[3], d1, A1a, S1, gA[1], gB[1]);
     conv_bwd(Ls[2], d1, P1, A1a, gB[1], gA[1]);
-    k_pool_back<<<flat_blocks(d0.n * 16), 256, 0, st_>>>(d0, d1, 16, gA[1], gU[0], gA[0]);
+    k_pool_back<16><<<line_grid(d0, 4), 256, 0, st_>>>(d0, d1, gA[1], gU[0], gA[0]);
     conv_bwd(Ls[1], d0, A0a, S0, gA[0], gB[0]);
     conv_bwd(Ls[0], d0, feat_, A0a, gB[0], nullptr);
     return cudaGetLastError();

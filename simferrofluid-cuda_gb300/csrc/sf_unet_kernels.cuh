@@ -234,63 +234,102 @@ __global__ void k_bias_grad(Dims d, const bf16 *__restrict__ dy, int co_n, int v
 // --------------------------------------------------------------------------------------------------------
 // elementwise / resampling kernels (channels-last)
 // --------------------------------------------------------------------------------------------------------
-// 2x2x2 average (children outside the fine grid count as zero), BF16 -> BF16
-__global__ void k_pool(Dims d, Dims dc, int C, const bf16 *__restrict__ x, bf16 *__restrict__ y) {
-    const long long tot = dc.n * C;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
-        const int ch = (int)(e % C);
-        const long long V = e / C;
-        const int K = (int)(V % dc.nz), J = (int)((V / dc.nz) % dc.ny), I = (int)(V / ((long long)dc.nz * dc.ny));
-        float s = 0.f;
-        for (int q = 0; q < 8; q++) {
-            const int i = 2 * I + (q & 1), j = 2 * J + ((q >> 1) & 1), k = 2 * K + (q >> 2);
-            if (i < d.nx && j < d.ny && k < d.nz) s += __bfloat162float(x[cid(d, i, j, k) * C + ch]);
-        }
-        y[e] = __float2bfloat16(s * 0.125f);
+// The grid operators below take one thread per (voxel, group of channels): 8 BF16 channels (16 bytes) or 4 FP32
+// channels (16 bytes), on a launch grid of (ceil(nz x groups / 256), ny, nx) so that no 64-bit division is needed,
+// consecutive threads touch consecutive 16-byte groups, and every sum keeps the order of a per-channel loop.
+__device__ __forceinline__ void bf16x8_to_f32(const uint4 &u, float (&f)[8]) {
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        f[2 * q] = __uint_as_float(w[q] << 16);
+        f[2 * q + 1] = __uint_as_float(w[q] & 0xffff0000u);
     }
+}
+__device__ __forceinline__ uint4 f32_to_bf16x8(const float (&f)[8]) {
+    return make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+}
+
+// 2x2x2 average pooling (children outside the grid count as absent, the sum is still divided by 8), BF16
+template <int C>
+__global__ void __launch_bounds__(256) k_pool(Dims d, Dims dc, const bf16 *__restrict__ x, bf16 *__restrict__ y) {
+    constexpr int G = C / 8;
+    const int t = blockIdx.x * 256 + threadIdx.x, K = t / G, g = t % G, J = blockIdx.y, I = blockIdx.z;
+    if (K >= dc.nz) return;
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int i = 2 * I + (q & 1), j = 2 * J + ((q >> 1) & 1), k = 2 * K + (q >> 2);
+        if (i < d.nx && j < d.ny && k < d.nz) {
+            float f[8];
+            bf16x8_to_f32(*reinterpret_cast<const uint4 *>(x + cid(d, i, j, k) * C + 8 * g), f);
+#pragma unroll
+            for (int e = 0; e < 8; e++) s[e] += f[e];
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < 8; e++) s[e] *= 0.125f;
+    *reinterpret_cast<uint4 *>(y + cid(dc, I, J, K) * C + 8 * g) = f32_to_bf16x8(s);
 }
 
 // y = up(xc) + s  (nearest parent), BF16
-__global__ void k_up_add(Dims d, Dims dc, int C, const bf16 *__restrict__ xc, const bf16 *__restrict__ s,
-                         bf16 *__restrict__ y) {
-    const long long tot = d.n * C;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
-        const int ch = (int)(e % C);
-        const long long v = e / C;
-        const int k = (int)(v % d.nz), j = (int)((v / d.nz) % d.ny), i = (int)(v / ((long long)d.nz * d.ny));
-        const float a = __bfloat162float(xc[cid(dc, i >> 1, j >> 1, k >> 1) * C + ch]);
-        y[e] = __float2bfloat16(a + __bfloat162float(s[e]));
-    }
+template <int C>
+__global__ void __launch_bounds__(256) k_up_add(Dims d, Dims dc, const bf16 *__restrict__ xc,
+                                                const bf16 *__restrict__ s, bf16 *__restrict__ y) {
+    constexpr int G = C / 8;
+    const int t = blockIdx.x * 256 + threadIdx.x, k = t / G, g = t % G, j = blockIdx.y, i = blockIdx.z;
+    if (k >= d.nz) return;
+    const long long v = cid(d, i, j, k);
+    float a[8], b[8];
+    bf16x8_to_f32(*reinterpret_cast<const uint4 *>(xc + cid(dc, i >> 1, j >> 1, k >> 1) * C + 8 * g), a);
+    bf16x8_to_f32(*reinterpret_cast<const uint4 *>(s + v * C + 8 * g), b);
+#pragma unroll
+    for (int e = 0; e < 8; e++) a[e] += b[e];
+    *reinterpret_cast<uint4 *>(y + v * C + 8 * g) = f32_to_bf16x8(a);
 }
 
 // dfine = dcoarse[parent] / 8 (+ dadd), FP32
-__global__ void k_pool_back(Dims d, Dims dc, int C, const float *__restrict__ dcoarse, const float *__restrict__ dadd,
-                            float *__restrict__ dfine) {
-    const long long tot = d.n * C;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
-        const int ch = (int)(e % C);
-        const long long v = e / C;
-        const int k = (int)(v % d.nz), j = (int)((v / d.nz) % d.ny), i = (int)(v / ((long long)d.nz * d.ny));
-        float g = dcoarse[cid(dc, i >> 1, j >> 1, k >> 1) * C + ch] * 0.125f;
-        if (dadd) g += dadd[e];
-        dfine[e] = g;
+template <int C>
+__global__ void __launch_bounds__(256) k_pool_back(Dims d, Dims dc, const float *__restrict__ dcoarse,
+                                                   const float *__restrict__ dadd, float *__restrict__ dfine) {
+    constexpr int G = C / 4;
+    const int t = blockIdx.x * 256 + threadIdx.x, k = t / G, g = t % G, j = blockIdx.y, i = blockIdx.z;
+    if (k >= d.nz) return;
+    const long long e = cid(d, i, j, k) * C + 4 * g;
+    float4 r = *reinterpret_cast<const float4 *>(dcoarse + cid(dc, i >> 1, j >> 1, k >> 1) * C + 4 * g);
+    r.x *= 0.125f;
+    r.y *= 0.125f;
+    r.z *= 0.125f;
+    r.w *= 0.125f;
+    if (dadd) {
+        const float4 q = *reinterpret_cast<const float4 *>(dadd + e);
+        r.x += q.x;
+        r.y += q.y;
+        r.z += q.z;
+        r.w += q.w;
     }
+    *reinterpret_cast<float4 *>(dfine + e) = r;
 }
 
 // dcoarse[V] = sum over the (in-grid) children of dfine, FP32
-__global__ void k_up_back(Dims d, Dims dc, int C, const float *__restrict__ dfine, float *__restrict__ dcoarse) {
-    const long long tot = dc.n * C;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
-        const int ch = (int)(e % C);
-        const long long V = e / C;
-        const int K = (int)(V % dc.nz), J = (int)((V / dc.nz) % dc.ny), I = (int)(V / ((long long)dc.nz * dc.ny));
-        float s = 0.f;
-        for (int q = 0; q < 8; q++) {
-            const int i = 2 * I + (q & 1), j = 2 * J + ((q >> 1) & 1), k = 2 * K + (q >> 2);
-            if (i < d.nx && j < d.ny && k < d.nz) s += dfine[cid(d, i, j, k) * C + ch];
+template <int C>
+__global__ void __launch_bounds__(256) k_up_back(Dims d, Dims dc, const float *__restrict__ dfine,
+                                                 float *__restrict__ dcoarse) {
+    constexpr int G = C / 4;
+    const int t = blockIdx.x * 256 + threadIdx.x, K = t / G, g = t % G, J = blockIdx.y, I = blockIdx.z;
+    if (K >= dc.nz) return;
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int i = 2 * I + (q & 1), j = 2 * J + ((q >> 1) & 1), k = 2 * K + (q >> 2);
+        if (i < d.nx && j < d.ny && k < d.nz) {
+            const float4 f = *reinterpret_cast<const float4 *>(dfine + cid(d, i, j, k) * C + 4 * g);
+            s.x += f.x;
+            s.y += f.y;
+            s.z += f.z;
+            s.w += f.w;
         }
-        dcoarse[e] = s;
     }
+    *reinterpret_cast<float4 *>(dcoarse + cid(dc, I, J, K) * C + 4 * g) = s;
 }
 
 // dpre = dpost * (post > 0), BF16 out (input of the MMA gradient kernels)
@@ -300,13 +339,22 @@ __global__ void k_relu_back(long long m, const float *__restrict__ dpost, const 
         dpre[e] = __float2bfloat16(__bfloat162float(post[e]) > 0.f ? dpost[e] : 0.f);
 }
 
-// 1x1 head: out[v] = b + sum_c w[c] a[v][c]  (FP32 out)
-__global__ void k_head_fwd(long long n, int C, const bf16 *__restrict__ a, const float *__restrict__ w,
-                           const float *__restrict__ b, float *__restrict__ out) {
+// 1x1 head: out[v] = b + sum_c w[c] a[v][c]  (FP32 out), 16 channels read as two 16-byte groups
+__global__ void __launch_bounds__(256) k_head_fwd(long long n, const bf16 *__restrict__ a, const float *__restrict__ w,
+                                                  const float *__restrict__ b, float *__restrict__ out) {
+    float wr[16];
+#pragma unroll
+    for (int c = 0; c < 16; c++) wr[c] = w[c];
     const float b0 = b[0];
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        float f0[8], f1[8];
+        bf16x8_to_f32(*reinterpret_cast<const uint4 *>(a + v * 16), f0);
+        bf16x8_to_f32(*reinterpret_cast<const uint4 *>(a + v * 16 + 8), f1);
         float s = b0;
-        for (int c = 0; c < C; c++) s += w[c] * __bfloat162float(a[v * C + c]);
+#pragma unroll
+        for (int c = 0; c < 8; c++) s += wr[c] * f0[c];
+#pragma unroll
+        for (int c = 0; c < 8; c++) s += wr[8 + c] * f1[c];
         out[v] = s;
     }
 }
