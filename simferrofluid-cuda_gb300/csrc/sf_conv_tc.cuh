@@ -35,6 +35,19 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo_bytes,
     return d;
 }
 
+// The same descriptor for the 32-byte swizzled K-major layout (layout type 6): rows of 32 bytes (16 BF16 along K)
+// whose two 16-byte halves swap in rows 4-7 of every 8-row, 256-byte atom, as TMA writes them with
+// CU_TENSOR_MAP_SWIZZLE_32B; the stride (M/N) byte offset is the 256-byte atom, the leading offset is unused.
+__device__ __forceinline__ uint64_t smem_desc_sw32(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(256u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)6 << 61;
+    return d;
+}
+
 // Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M = 128, N = n.
 __host__ __device__ constexpr uint32_t instr_desc_bf16(int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
@@ -184,16 +197,18 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
             waited = t + 1;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t a = smem_u32(smem + s * L::kStageBytes), b = a + L::kABytes;
+            // K = 16 spans two 8-channel chunks: leading (K) offset = one chunk, stride (M/N) = 8 rows; tile m's rows
+            // start 2 KB further into each chunk, its accumulator CO columns further.  The descriptors are bases plus
+            // compile-time offsets in 16-byte units (no carry: shared addresses stay below 256 KB).
+            const uint64_t ad0 = smem_desc(a, L::kChunkBytes, 128u), bd0 = smem_desc(b, (uint32_t)CO * 16u, 128u);
+            const uint32_t acc0 = t > 0 ? 1u : 0u;
 #pragma unroll
             for (int j = 0; j < CI / 16; j++) {
-                // K = 16 spans two 8-channel chunks: leading (K) offset = one chunk, stride (M/N) = 8 rows;
-                // tile m's rows start 2 KB further into each chunk, its accumulator CO columns further
-                const uint64_t bd = smem_desc(b + j * 2u * (uint32_t)CO * 16u, (uint32_t)CO * 16u, 128u);
+                const uint64_t bd = bd0 + (uint64_t)(j * 2 * CO);
 #pragma unroll
                 for (int m = 0; m < MT; m++) {
-                    const uint64_t ad = smem_desc(a + j * 2u * L::kChunkBytes + (uint32_t)m * 2048u, L::kChunkBytes,
-                                                  128u);
-                    mma_bf16(tmem + (uint32_t)(m * CO), ad, bd, idesc, (t > 0 || j > 0) ? 1u : 0u);
+                    const uint64_t ad = ad0 + (uint64_t)((j * 2 * L::kChunkBytes + m * 2048u) >> 4);
+                    mma_bf16(tmem + (uint32_t)(m * CO), ad, bd, idesc, j > 0 ? 1u : acc0);
                 }
             }
             mma_commit(empty0 + 8 * s);
@@ -257,11 +272,12 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
 // ------------------------------------------------------------------------------------------------ z lines
 // Forward (and input gradient) for Cin = 16 or 32, Cout <= 32, on grids with nz >= 128: a persistent CTA per SM
 // takes bricks of 128 (z) x 4 (y) x LX (x) voxels (LX = 2 for 16 input channels, 1 for 32), 4 LX M tiles of one
-// z line of 128 voxels each.  A pipeline stage is one z shift dz and one pair of 8-channel chunks (K = 16): one TMA
-// box per chunk, (8, 128 z, 6 y, LX + 2 x) from (z0 + dz, y0 - 1, x0 - 1), carries the tile rows of all nine
-// (dx, dy) taps: tile (yy, xx) of tap (dx, dy) starts 2 KB x ((yy + 1 + dy) + 6 (xx + 1 + dx)) into the box, so each
-// box is read once for nine taps (the 27-box kernel above reads nine times as many rows).  The 27 taps' weights stay
-// in shared memory for the CTA's whole run.  Warp 1 lane 0 issues the TMA loads through two stages, warp 0 lane 0
+// z line of 128 voxels each.  A pipeline stage is one z shift dz and one group of 16 channels (K = 16): one TMA box,
+// (16 channels, 128 z, 6 y, LX + 2 x) from (z0 + dz, y0 - 1, x0 - 1), lands as 32-byte rows in the 32-byte swizzled
+// K-major layout and carries the tile rows of all nine (dx, dy) taps: tile (yy, xx) of tap (dx, dy) starts
+// 4 KB x ((yy + 1 + dy) + 6 (xx + 1 + dx)) into the box, so each box is read once for nine taps (the 27-box kernel
+// above reads nine times as many rows, of 16 bytes, each half of a 32-byte sector).  The 27 taps' weights stay in
+// shared memory, swizzled the same way, for the CTA's whole run.  Warp 1 lane 0 issues the TMA loads through two stages, warp 0 lane 0
 // the MMAs (M = 128, N = Cout, K = 16) into one of two TMEM accumulator sets, and warps 2-5 read the other set back
 // (bias + ReLU + BF16, or FP32), so the epilogue of a brick overlaps the MMAs of the next.  Every wait is bounded; a
 // timeout stops all roles, drains the copies in flight and sets the error flag.
@@ -274,15 +290,14 @@ __host__ __device__ constexpr int line_x() {
 
 template <int CI, int CO>
 struct LineLayout {
-    static constexpr int LX = line_x<CI>(), kTiles = kLineY * LX, KP = CI / 16;  // chunk pairs
+    static constexpr int LX = line_x<CI>(), kTiles = kLineY * LX, KP = CI / 16;  // 16-channel groups
     static constexpr uint32_t kBoxRows = kLineZ * (kLineY + 2) * (LX + 2);
-    static constexpr uint32_t kChunkBytes = kBoxRows * 16u;  // 48 KB (LX 2) or 36 KB (LX 1)
-    static constexpr uint32_t kStageBytes = 2u * kChunkBytes;
-    static constexpr uint32_t kWChunkRaw = 27u * CO * 16u;  // [tap][co] rows of 8 channels
+    static constexpr uint32_t kStageBytes = kBoxRows * 32u;  // 96 KB (LX 2) or 72 KB (LX 1)
+    static constexpr uint32_t kWChunkRaw = 27u * CO * 32u;  // [tap][co] rows of 16 channels
     static constexpr uint32_t kWChunk = (kWChunkRaw + 1023u) & ~1023u;
     static constexpr uint32_t kCols = kTiles * CO;  // one accumulator set
     static constexpr uint32_t kAlloc = 2u * kCols <= 256u ? 256u : 512u;
-    static constexpr uint32_t kSmemBytes = 1024u + 2u * kStageBytes + 2u * KP * kWChunk + 256u;
+    static constexpr uint32_t kSmemBytes = 1024u + 2u * kStageBytes + KP * kWChunk + 256u;
     static_assert(CI % 16 == 0 && 2u * kCols <= 512u && kSmemBytes <= 227u * 1024u, "line layout");
 };
 
@@ -296,7 +311,7 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc_line(const __grid_constant__
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *wbuf = smem + 2 * L::kStageBytes;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(wbuf + 2 * KP * L::kWChunk);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(wbuf + KP * L::kWChunk);
     // barriers: [0,2) stage full, [2,4) stage empty, 4 weights, [5,7) accumulators full, [7,9) accumulators
     // empty (four epilogue warps), 9 done
     volatile uint32_t *sh = reinterpret_cast<volatile uint32_t *>(bars + 10);
@@ -340,22 +355,21 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc_line(const __grid_constant__
     const uint32_t tmem = sh[0];
 
     if (warp == 1 && lane == 0 && nb > 0) {  // TMA producer
-        mbar_expect_tx(wfull, 2u * KP * L::kWChunkRaw);
-        for (int c = 0; c < 2 * KP; c++) tma_load_3d(smem_u32(wbuf + c * L::kWChunk), &tmap_w, wfull, 8 * c, 0, 0);
+        mbar_expect_tx(wfull, KP * L::kWChunkRaw);
+        for (int c = 0; c < KP; c++) tma_load_3d(smem_u32(wbuf + c * L::kWChunk), &tmap_w, wfull, 16 * c, 0, 0);
         int q = 0;
         for (int bi = 0; bi < nb && !sh[1]; bi++) {
             int z0, y0, x0;
             brick(bi, z0, y0, x0);
-            for (int st = 0; st < 3 * KP && !sh[1]; st++, q++) {  // stage = (dz, chunk pair)
+            for (int st = 0; st < 3 * KP && !sh[1]; st++, q++) {  // stage = (dz, 16-channel group)
                 const int dz = st / KP, jp = st % KP, s = q & 1;
                 if (q >= 2 && !mbar_wait(empty0 + 8 * s, (uint32_t)((q >> 1) - 1) & 1u)) {
                     sh[1] = 1;
                     break;
                 }
                 mbar_expect_tx(full0 + 8 * s, L::kStageBytes);
-                for (int c = 0; c < 2; c++)
-                    tma_load_4d(smem_u32(smem + s * L::kStageBytes + c * L::kChunkBytes), &tmap_x, full0 + 8 * s,
-                                8 * (2 * jp + c), z0 + dz - 1, y0 - 1, x0 - 1);
+                tma_load_4d(smem_u32(smem + s * L::kStageBytes), &tmap_x, full0 + 8 * s, 16 * jp, z0 + dz - 1, y0 - 1,
+                            x0 - 1);
                 sh[2] = (uint32_t)(q + 1);
             }
         }
@@ -380,19 +394,21 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc_line(const __grid_constant__
                 }
                 sh[3] = (uint32_t)(q + 1);
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t a0 = smem_u32(smem + s * L::kStageBytes);
-#pragma unroll 1
+                // descriptor bases of this stage; every MMA below adds a compile-time offset in 16-byte units (the
+                // start field cannot carry: shared addresses stay below 256 KB)
+                const uint64_t ad0 = smem_desc_sw32(smem_u32(smem + s * L::kStageBytes));
+                const uint64_t bd0 = smem_desc_sw32(smem_u32(wbuf) + jp * L::kWChunk + (uint32_t)dz * CO * 32u);
+                const uint32_t tacc = tmem + (uint32_t)(tb * L::kCols);
+                const uint32_t acc0 = st > 0 ? 1u : 0u;
+#pragma unroll
                 for (int pr = 0; pr < 9; pr++) {
-                    const int dx = pr / 3 - 1, dy = pr % 3 - 1, t = 9 * (dx + 1) + 3 * (dy + 1) + dz;
-                    const uint64_t bd = smem_desc(smem_u32(wbuf) + 2u * jp * L::kWChunk + (uint32_t)t * CO * 16u,
-                                                  L::kWChunk, 128u);
+                    const int dx = pr / 3 - 1, dy = pr % 3 - 1;
+                    const uint64_t bd = bd0 + (uint64_t)((9 * (dx + 1) + 3 * (dy + 1)) * CO * 2);
 #pragma unroll
                     for (int tile = 0; tile < kTiles; tile++) {
                         const int yy = tile % kLineY, xx = tile / kLineY;
-                        const uint64_t ad = smem_desc(
-                            a0 + 2048u * (uint32_t)((yy + 1 + dy) + (kLineY + 2) * (xx + 1 + dx)), L::kChunkBytes, 128u);
-                        mma_bf16(tmem + (uint32_t)(tb * L::kCols + tile * CO), ad, bd, idesc,
-                                 (st > 0 || pr > 0) ? 1u : 0u);
+                        const uint64_t ad = ad0 + (uint64_t)(256 * ((yy + 1 + dy) + (kLineY + 2) * (xx + 1 + dx)));
+                        mma_bf16(tacc + (uint32_t)(tile * CO), ad, bd, idesc, pr > 0 ? 1u : acc0);
                     }
                 }
                 any = true;

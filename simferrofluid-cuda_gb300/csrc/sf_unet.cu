@@ -133,17 +133,18 @@ cudaError_t launch_tc_line(cudaStream_t st, const Dims &d, const bf16 *x, const 
     using L = tc::LineLayout<CI, CO>;
     const cuuint64_t xd[4] = {(cuuint64_t)CI, (cuuint64_t)d.nz, (cuuint64_t)d.ny, (cuuint64_t)d.nx};
     const cuuint64_t xs[3] = {(cuuint64_t)CI * 2, (cuuint64_t)d.nz * CI * 2, (cuuint64_t)d.ny * d.nz * CI * 2};
-    const cuuint32_t xb[4] = {8, tc::kLineZ, tc::kLineY + 2, (cuuint32_t)L::LX + 2};
+    // 16 channels (32 bytes) per box row, written in the 32-byte swizzled layout the MMA descriptors read
+    const cuuint32_t xb[4] = {16, tc::kLineZ, tc::kLineY + 2, (cuuint32_t)L::LX + 2};
     const cuuint32_t es[4] = {1, 1, 1, 1};
     if (enc(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(x), xd, xs, xb, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
     const cuuint64_t wd[3] = {(cuuint64_t)CI, (cuuint64_t)CO, 27};
     const cuuint64_t ws[2] = {(cuuint64_t)CI * 2, (cuuint64_t)CO * CI * 2};
-    const cuuint32_t wb[3] = {8, (cuuint32_t)CO, 27};
+    const cuuint32_t wb[3] = {16, (cuuint32_t)CO, 27};
     if (enc(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16 *>(w), wd, ws, wb, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(tc::k_conv_tc_line<CI, CO, EPI>,
