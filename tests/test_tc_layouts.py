@@ -1,0 +1,172 @@
+"""CPU emulation of the shared-memory layouts of the tcgen05 U-Net kernels (simferrofluid-cuda_gb300/csrc/sf_conv_tc.cuh):
+where each TMA box lands, and which bytes each MMA's shared-memory descriptor reads.  The emulation places the data
+as the TMA unit does (out-of-grid elements zero), reads the A and B operands through the descriptor addressing of
+the K-major layouts (no swizzle: core matrices of 8 rows x 16 B, LBO between K halves, SBO = 128 B; 32-byte swizzle:
+rows of 32 B whose 16-byte halves swap in rows 4-7 of every 256-byte atom, SBO = 256 B), multiplies them as the
+MMA does, and compares the result with a direct convolution.  It also checks that every byte a descriptor reads
+lies inside the buffer it addresses.  No GPU is needed; the kernel's constants are read from the header."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+HDR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "simferrofluid-cuda_gb300", "csrc",
+                   "sf_conv_tc.cuh")
+
+
+def _const(name):
+    m = re.search(r"\b%s\s*=\s*(\d+)" % name, open(HDR).read())
+    assert m, name
+    return int(m.group(1))
+
+
+LZ, LY, SLACK = _const("kLineZ"), _const("kLineY"), _const("kWgSlack")
+
+
+def _direct_forward(X, W):
+    """Y[v][co] = sum_t W[t][co][ci] X[v + off(t)][ci], off(t) = (t/9 - 1, (t/3)%3 - 1, t%3 - 1), zero padding."""
+    nx, ny, nz, _ = X.shape
+    Xp = np.pad(X, ((1, 1), (1, 1), (1, 1), (0, 0)))
+    Y = np.zeros((nx, ny, nz, W.shape[1]))
+    for t in range(27):
+        dx, dy, dz = t // 9 - 1, (t // 3) % 3 - 1, t % 3 - 1
+        Y += np.einsum("xyzi,oi->xyzo", Xp[1 + dx:1 + dx + nx, 1 + dy:1 + dy + ny, 1 + dz:1 + dz + nz], W[t])
+    return Y
+
+
+def _swz32(byte):
+    return byte ^ (((byte >> 7) & 1) << 4)
+
+
+def _write_sw32(buf, base, rows):
+    """TMA with CU_TENSOR_MAP_SWIZZLE_32B: row r (16 BF16) at base + 32 r, 16-byte halves swizzled."""
+    r = np.arange(rows.shape[0])[:, None]
+    e = np.arange(16)[None, :]
+    buf[_swz32(base + r * 32 + (e // 8) * 16 + (e % 8) * 2) // 2] = rows
+
+
+def _read_sw32(buf, start, m_rows):
+    m = np.arange(m_rows)[:, None]
+    k = np.arange(16)[None, :]
+    byte = _swz32(start + (m // 8) * 256 + (m % 8) * 32 + (k // 8) * 16 + (k % 8) * 2)
+    return buf[byte // 2], int(byte.max())
+
+
+def _read_plain(buf, start, lbo, sbo, m_rows):
+    m = np.arange(m_rows)[:, None]
+    k = np.arange(16)[None, :]
+    byte = start + (m // 8) * sbo + (m % 8) * 16 + (k // 8) * lbo + (k % 8) * 2
+    return buf[byte // 2], int(byte.max())
+
+
+@pytest.mark.parametrize("shape,ci,co", [((4, 6, 128), 16, 16), ((3, 7, 130), 16, 32), ((3, 6, 128), 32, 16),
+                                         ((3, 6, 150), 32, 32)])
+def test_line_kernel_layout(shape, ci, co):
+    """k_conv_tc_line: bricks of 128 z x 4 y x LX x; a stage per (dz, 16 channels) is one box (16 ch, 128 z, 6 y,
+    LX + 2 x) at (z0 + dz - 1, y0 - 1, x0 - 1) in the 32-byte swizzled layout; tile (yy, xx) of tap (dx, dy) starts
+    4 KB x ((yy + 1 + dy) + 6 (xx + 1 + dx)) into it; the 27 taps' weights are resident, rows (tap, co) per
+    16-channel group."""
+    nx, ny, nz = shape
+    lx = 2 if ci == 16 else 1
+    kp = ci // 16
+    rng = np.random.default_rng(1)
+    X = rng.standard_normal(shape + (ci,))
+    W = rng.standard_normal((27, co, ci))
+    stage_bytes = LZ * (LY + 2) * (lx + 2) * 32
+    wch = (27 * co * 32 + 1023) // 1024 * 1024
+    wbuf = np.zeros(kp * wch // 2)
+    for c in range(kp):
+        _write_sw32(wbuf, c * wch, W[:, :, 16 * c:16 * c + 16].reshape(-1, 16))
+    out = np.zeros((nx, ny, nz, co))
+    bz_n, by_n, bx_n = -(-nz // LZ), -(-ny // LY), -(-nx // lx)
+    Xp = np.zeros((nx + 2 + lx, ny + 2 + LY, nz + 2 + LZ, ci))  # zero outside the grid
+    Xp[1:1 + nx, 1:1 + ny, 1:1 + nz] = X
+    for br in range(bz_n * by_n * bx_n):
+        z0, y0, x0 = LZ * (br % bz_n), LY * ((br // bz_n) % by_n), lx * (br // (bz_n * by_n))
+        acc = np.zeros((LY * lx, 128, co))
+        for st in range(3 * kp):
+            dz, jp = st // kp, st % kp  # dz index 0..2 = shift dz - 1
+            box = Xp[x0:x0 + lx + 2, y0:y0 + LY + 2, z0 + dz:z0 + dz + LZ, 16 * jp:16 * jp + 16]  # [x][y][z][16]
+            stage = np.zeros(stage_bytes // 2)
+            _write_sw32(stage, 0, box.reshape(-1, 16))
+            for pr in range(9):
+                dx, dy = pr // 3 - 1, pr % 3 - 1
+                B, mb = _read_sw32(wbuf, jp * wch + (9 * (dx + 1) + 3 * (dy + 1) + dz) * co * 32, co)
+                assert mb < kp * wch
+                for tile in range(LY * lx):
+                    yy, xx = tile % LY, tile // LY
+                    A, ma = _read_sw32(stage, 4096 * ((yy + 1 + dy) + (LY + 2) * (xx + 1 + dx)), 128)
+                    assert ma < stage_bytes
+                    acc[tile] += A @ B.T
+        for tile in range(LY * lx):
+            yy, xx = y0 + tile % LY, x0 + tile // LY
+            if yy < ny and xx < nx:
+                zz = min(LZ, nz - z0)
+                out[xx, yy, z0:z0 + zz] = acc[tile, :zz]
+    ref = _direct_forward(X, W)
+    assert np.abs(out - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("shape,ci,co", [((4, 4, 32), 16, 16), ((3, 5, 40), 16, 32), ((3, 5, 26), 32, 16),
+                                         ((2, 4, 32), 64, 64)])
+def test_weight_gradient_layout(shape, ci, co):
+    """k_wgrad_tc: channel-major z-row copies dYT[zh][x][y][co][zl] and XT[zh][x][y][s][ci][zl] (three z shifts
+    interleaved); a job is one (dx, dy) pair over a 32 z x 4 y x BX x brick, boxes (8, C, 4, BX, 4) landing as rows
+    c + C k; MMA p reads A rows from 2p Cout 16 B (LBO Cout 16 B, SBO 128 B; rows past Cout land in unused lanes and
+    may read the slack after the buffer) and B rows from 2p 3Cin 16 B; N = 3 Cin = three dz taps."""
+    nx, ny, nz = shape
+    bx = 2 if ci == 16 else 1
+    N = 3 * ci
+    rng = np.random.default_rng(2)
+    X = rng.standard_normal(shape + (ci,))
+    dY = rng.standard_normal(shape + (co,))
+    nzh = (nz + 7) // 8
+
+    def chmajor(src, C, ns, shift0):
+        out = np.zeros((nzh, nx, ny, ns, C, 8))
+        for s in range(ns):
+            for zh in range(nzh):
+                for zl in range(8):
+                    z = 8 * zh + zl
+                    zs = z + s + shift0
+                    if z < nz and 0 <= zs < nz:
+                        out[zh, :, :, s, :, zl] = src[:, :, zs, :]
+        return out.reshape(nzh, nx, ny, ns * C, 8)
+
+    def box(T, y, x, zh0):  # (8, C, 4, bx, 4) at (0, 0, y, x, zh0), lands [zh][x][y][c][8]
+        C = T.shape[3]
+        b = np.zeros((4, bx, 4, C, 8))
+        for a in range(4):
+            for xx in range(bx):
+                for yy in range(4):
+                    zh, xv, yv = zh0 + a, x + xx, y + yy
+                    if 0 <= zh < nzh and 0 <= xv < nx and 0 <= yv < ny:
+                        b[a, xx, yy] = T[zh, xv, yv]
+        return b.reshape(-1)
+
+    dYT, XT = chmajor(dY, co, 1, 0), chmajor(X, ci, 3, -1)
+    a_bytes = 256 * co * bx
+    acc = np.zeros((9, 128, N))
+    bz_n, by_n, bx_n = -(-nz // 32), -(-ny // 4), -(-nx // bx)
+    for br in range(bz_n * by_n * bx_n):
+        z0, y0, x0 = 32 * (br % bz_n), 4 * ((br // bz_n) % by_n), bx * (br // (bz_n * by_n))
+        abuf = np.concatenate([box(dYT, y0, x0, z0 // 8), np.zeros(SLACK // 2)])
+        for pr in range(9):
+            dx, dy = pr // 3 - 1, pr % 3 - 1
+            bbuf = box(XT, y0 + dy, x0 + dx, z0 // 8)
+            for p in range(8 * bx):
+                A, ma = _read_plain(abuf, 2 * p * co * 16, co * 16, 128, 128)
+                B, mb = _read_plain(bbuf, 2 * p * N * 16, N * 16, 128, N)
+                assert ma < a_bytes + SLACK and mb < bbuf.size * 2
+                acc[pr] += A @ B.T
+    got = np.zeros((27, co, ci))
+    for pr in range(9):
+        for sz in range(3):
+            got[3 * pr + sz] = acc[pr, :co, sz * ci:(sz + 1) * ci]
+    Xp = np.pad(X, ((1, 1), (1, 1), (1, 1), (0, 0)))
+    ref = np.zeros((27, co, ci))
+    for t in range(27):
+        dx, dy, dz = t // 9 - 1, (t // 3) % 3 - 1, t % 3 - 1
+        ref[t] = np.einsum("xyzo,xyzi->oi", dY, Xp[1 + dx:1 + dx + nx, 1 + dy:1 + dy + ny, 1 + dz:1 + dz + nz])
+    assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
