@@ -407,9 +407,16 @@ cudaError_t UNet::ensure_wgrad_ws() {
         if (e > el) el = e;
     }
     void *a = nullptr, *b = nullptr;
-    if (cudaMalloc(&a, 2 * (size_t)el) != cudaSuccess) return cudaErrorMemoryAllocation;
+    // on failure the caller falls back to the warp-MMA kernel: clear the error so that it is not reported later
+    if (cudaMalloc(&a, 2 * (size_t)el) != cudaSuccess) {
+        cudaGetLastError();
+        return cudaErrorMemoryAllocation;
+    }
     ws_.push_back(a);
-    if (cudaMalloc(&b, 6 * (size_t)el) != cudaSuccess) return cudaErrorMemoryAllocation;
+    if (cudaMalloc(&b, 6 * (size_t)el) != cudaSuccess) {
+        cudaGetLastError();
+        return cudaErrorMemoryAllocation;
+    }
     ws_.push_back(b);
     wg_dy_ = (bf16 *)a;
     wg_x_ = (bf16 *)b;
