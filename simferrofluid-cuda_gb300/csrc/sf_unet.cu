@@ -431,6 +431,7 @@ void UNet::conv_fwd(const ConvLayer &L, const Dims &d, const bf16 *x, bf16 *y) {
             return;
         }
         last_error = std::string("tcgen05 convolution not launched: ") + cudaGetErrorString(e);
+        cudaGetLastError();  // the warp-MMA kernel below runs instead: the refused launch is not an error
     }
     conv_dispatch(st_, L.cin, L.cout, 0, d, x, wb_ + L.wbf, p_ + L.boff, y, L.taps);
 }
@@ -500,6 +501,7 @@ void UNet::conv_bwd(const ConvLayer &L, const Dims &d, const bf16 *x, const bf16
         else {
             wchunks = 0;
             last_error = std::string("tcgen05 weight gradient not launched: ") + cudaGetErrorString(e);
+            cudaGetLastError();  // the warp-MMA kernel runs instead
         }
     }
     if (wchunks == 0) {
@@ -519,6 +521,7 @@ void UNet::conv_bwd(const ConvLayer &L, const Dims &d, const bf16 *x, const bf16
             return;
         }
         last_error = std::string("tcgen05 convolution not launched: ") + cudaGetErrorString(e);
+        cudaGetLastError();  // the warp-MMA kernel below runs instead: the refused launch is not an error
     }
     conv_dispatch(st_, L.cout, L.cin, 1, d, dy, wt_ + L.wbf, nullptr, dx, L.taps);
 }
