@@ -487,6 +487,214 @@ __global__ void __launch_bounds__(192, 1) k_conv_tc_line(const __grid_constant__
     }
 }
 
+// ------------------------------------------------------------------------------------------------ 64-long z lines
+// The z-line kernel for grids with 64 <= nz (the 64^3 level of a 256^3 network), any of 16, 32, 64 channels in and
+// out: bricks of 64 (z) x 4 (y) x 2 (x) voxels, four M tiles of 64 z x 2 y (128 rows: two z lines).  A stage is one z
+// shift dz and one group of 16 input channels: the halo'd box (16 channels, 64 z, 6 y, 4 x) from
+// (z0 + dz - 1, y0 - 1, x0 - 1), 32-byte swizzled, whose tile (ty, xx) of tap (dx, dy) starts 2 KB x
+// ((2 ty + 1 + dy) + 6 (xx + 1 + dx)) into it, and the weights of the nine taps (dx, dy, dz) for those 16 channels,
+// one box (16 channels, Cout, 9) of a copy of the weights whose taps are ordered (dz, dx, dy) (the weights of a
+// 64-channel layer do not fit in shared memory whole).  Three stages; otherwise as k_conv_tc_line.
+constexpr int kL64Z = 64, kL64Y = 4, kL64X = 2, kL64Stages = 3;
+
+template <int CI, int CO>
+struct Line64Layout {
+    static constexpr int KP = CI / 16, kTiles = (kL64Y / 2) * kL64X;
+    static constexpr uint32_t kABytes = kL64Z * (kL64Y + 2) * (kL64X + 2) * 32u;  // 48 KB
+    static constexpr uint32_t kWRaw = 9u * CO * 32u;
+    static constexpr uint32_t kWBytes = (kWRaw + 1023u) & ~1023u;
+    static constexpr uint32_t kStageBytes = kABytes + kWBytes;
+    static constexpr uint32_t kCols = kTiles * CO;
+    static constexpr uint32_t kAlloc = 2u * kCols <= 32u ? 32u : 2u * kCols <= 64u ? 64u : 2u * kCols <= 128u ? 128u
+                                                                                    : 2u * kCols <= 256u ? 256u
+                                                                                                         : 512u;
+    static constexpr uint32_t kSmemBytes = 1024u + kL64Stages * kStageBytes + 256u;
+    static_assert(CI % 16 == 0 && CO % 16 == 0 && 2u * kCols <= 512u && kSmemBytes <= 227u * 1024u, "layout");
+};
+
+template <int CI, int CO, int EPI>
+__global__ void __launch_bounds__(192, 1) k_conv_tc_line64(const __grid_constant__ CUtensorMap tmap_x,
+                                                           const __grid_constant__ CUtensorMap tmap_wp, Dims d,
+                                                           const float *__restrict__ bias, void *__restrict__ yout,
+                                                           int *err) {
+    using L = Line64Layout<CI, CO>;
+    constexpr int KP = L::KP, S = kL64Stages, kTiles = L::kTiles;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * L::kStageBytes);
+    // barriers: [0,S) stage full, [S,2S) stage empty, [2S,2S+2) accumulators full, [2S+2,2S+4) accumulators empty
+    // (four epilogue warps), 2S+4 done
+    volatile uint32_t *sh = reinterpret_cast<volatile uint32_t *>(bars + 2 * S + 5);
+    // sh: [0] TMEM base, [1] abort, [2] stage jobs issued, [3] stage jobs waited
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + S), tfull0 = smem_u32(bars + 2 * S),
+                   tempty0 = smem_u32(bars + 2 * S + 2), done = smem_u32(bars + 2 * S + 4);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int bz_n = (d.nz + kL64Z - 1) / kL64Z, by_n = (d.ny + kL64Y - 1) / kL64Y;
+    const long long nbricks = (long long)bz_n * by_n * ((d.nx + kL64X - 1) / kL64X);
+    const int nb = nbricks > blockIdx.x ? (int)((nbricks - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+    auto brick = [&](int bi, int &z0, int &y0, int &x0) {
+        const long long br = blockIdx.x + (long long)bi * gridDim.x;
+        z0 = kL64Z * (int)(br % bz_n);
+        y0 = kL64Y * (int)((br / bz_n) % by_n);
+        x0 = kL64X * (int)(br / ((long long)bz_n * by_n));
+    };
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; s++) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        for (int s = 0; s < 2; s++) {
+            mbar_init(tfull0 + 8 * s, 1);
+            mbar_init(tempty0 + 8 * s, 4);
+        }
+        mbar_init(done, 1);
+        for (int k = 1; k < 4; k++) sh[k] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(const_cast<uint32_t *>(sh))),
+                     "r"(L::kAlloc)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = sh[0];
+
+    if (warp == 1 && lane == 0 && nb > 0) {  // TMA producer
+        int q = 0;
+        for (int bi = 0; bi < nb && !sh[1]; bi++) {
+            int z0, y0, x0;
+            brick(bi, z0, y0, x0);
+            for (int st = 0; st < 3 * KP && !sh[1]; st++, q++) {  // stage = (dz, 16-channel group)
+                const int dz = st / KP, jp = st % KP, s = q % S;
+                if (q >= S && !mbar_wait(empty0 + 8 * s, (uint32_t)(q / S - 1) & 1u)) {
+                    sh[1] = 1;
+                    break;
+                }
+                const uint32_t a = smem_u32(smem + s * L::kStageBytes);
+                mbar_expect_tx(full0 + 8 * s, L::kABytes + L::kWRaw);
+                tma_load_4d(a, &tmap_x, full0 + 8 * s, 16 * jp, z0 + dz - 1, y0 - 1, x0 - 1);
+                tma_load_3d(a + L::kABytes, &tmap_wp, full0 + 8 * s, 16 * jp, 0, 9 * dz);
+                sh[2] = (uint32_t)(q + 1);
+            }
+        }
+    } else if (warp == 0 && lane == 0 && nb > 0) {  // MMA issuer
+        constexpr uint32_t idesc = instr_desc_bf16(CO);
+        bool any = false;
+        int q = 0;
+        for (int bi = 0; bi < nb && !sh[1]; bi++) {
+            const int tb = bi & 1;
+            if (bi >= 2 && !mbar_wait(tempty0 + 8 * tb, (uint32_t)((bi - 2) >> 1) & 1u)) {
+                sh[1] = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int st = 0; st < 3 * KP; st++, q++) {
+                const int s = q % S;
+                if (!mbar_wait(full0 + 8 * s, (uint32_t)(q / S) & 1u)) {
+                    sh[1] = 1;
+                    break;
+                }
+                sh[3] = (uint32_t)(q + 1);
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                // descriptor bases of this stage plus compile-time offsets in 16-byte units (no carry: shared
+                // addresses stay below 256 KB)
+                const uint32_t a = smem_u32(smem + s * L::kStageBytes);
+                const uint64_t ad0 = smem_desc_sw32(a), bd0 = smem_desc_sw32(a + L::kABytes);
+                const uint32_t tacc = tmem + (uint32_t)(tb * L::kCols);
+                const uint32_t acc0 = st > 0 ? 1u : 0u;
+#pragma unroll
+                for (int pr = 0; pr < 9; pr++) {
+                    const int dx = pr / 3 - 1, dy = pr % 3 - 1;
+                    const uint64_t bd = bd0 + (uint64_t)(pr * CO * 2);
+#pragma unroll
+                    for (int tile = 0; tile < kTiles; tile++) {
+                        const int ty = tile % (kL64Y / 2), xx = tile / (kL64Y / 2);
+                        const uint64_t ad = ad0 + (uint64_t)(128 * ((2 * ty + 1 + dy) + (kL64Y + 2) * (xx + 1 + dx)));
+                        mma_bf16(tacc + (uint32_t)(tile * CO), ad, bd, idesc, pr > 0 ? 1u : acc0);
+                    }
+                }
+                any = true;
+                mma_commit(empty0 + 8 * s);
+            }
+            if (sh[1]) break;
+            mma_commit(tfull0 + 8 * tb);
+        }
+        if (any) {  // completion of every MMA issued (also on the error path, before TMEM is released)
+            mma_commit(done);
+            if (!mbar_wait(done, 0)) sh[1] = 1;
+        }
+    } else if (warp >= 2 && nb > 0) {  // epilogue
+        const int q4 = warp & 3;  // TMEM lane quarter of this warp
+        for (int bi = 0; bi < nb; bi++) {
+            const int tb = bi & 1;
+            const uint32_t par = (uint32_t)(bi >> 1) & 1u;
+            // lane 0 decides for the warp, so that the warp-collective TMEM loads below are never divergent
+            int go = 0;
+            if (lane == 0) go = (!sh[1] && mbar_wait(tfull0 + 8 * tb, par)) ? 1 : 0;
+            go = __shfl_sync(0xffffffffu, go, 0);
+            if (!go) {
+                if (lane == 0) sh[1] = 1;
+                break;
+            }
+            mbar_wait(tfull0 + 8 * tb, par);  // completed: returns at once, with this thread's acquire
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            int z0, y0, x0;
+            brick(bi, z0, y0, x0);
+            const int m = 32 * q4 + lane;  // TMEM lane = tile row: z = m % 64, y = m / 64
+            const int z = z0 + (m & (kL64Z - 1));
+#pragma unroll 1
+            for (int tile = 0; tile < kTiles; tile++) {
+                const int yy = y0 + 2 * (tile % (kL64Y / 2)) + (m >> 6), xx = x0 + tile / (kL64Y / 2);
+                const bool inb = z < d.nz && yy < d.ny && xx < d.nx;
+                const long long v = inb ? cid(d, xx, yy, z) : 0;
+#pragma unroll
+                for (int c0 = 0; c0 < CO; c0 += 16) {
+                    float acc[16];
+                    tmem_ld_x16<16>(tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(tb * L::kCols + tile * CO + c0),
+                                    acc);
+                    if (inb && EPI == 0) {
+                        uint32_t pk[8];
+#pragma unroll
+                        for (int k = 0; k < 8; k++) {
+                            const float a0 = fmaxf(acc[2 * k] + bias[c0 + 2 * k], 0.f);
+                            const float a1 = fmaxf(acc[2 * k + 1] + bias[c0 + 2 * k + 1], 0.f);
+                            __nv_bfloat162 h2 = __floats2bfloat162_rn(a0, a1);
+                            pk[k] = *reinterpret_cast<uint32_t *>(&h2);
+                        }
+                        uint4 *dst = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(yout) + v * CO + c0);
+                        dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                        dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                    } else if (inb) {
+                        float4 *dst = reinterpret_cast<float4 *>(reinterpret_cast<float *>(yout) + v * CO + c0);
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            dst[k] = make_float4(acc[4 * k], acc[4 * k + 1], acc[4 * k + 2], acc[4 * k + 3]);
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty0 + 8 * tb) : "memory");
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && sh[1]) {  // drain copies still in flight into this CTA's shared memory (bounded)
+        for (uint32_t q = sh[3]; q < sh[2]; q++) mbar_wait(full0 + 8 * (q % S), (q / S) & 1u);
+        atomicCAS(err, 0, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(L::kAlloc) : "memory");
+    }
+}
+
 // ------------------------------------------------------------------------------------------------ weight gradient
 // dW[tap][co][ci] = sum over voxels v of dY[v][co] X[v + off(tap)][ci]: GEMMs with M = Cout, K = voxels and
 // N = (dz, Cin), both operands K-major with 8 consecutive z per 16-byte row.  k_to_chmajor makes channel-major copies

@@ -157,22 +157,63 @@ cudaError_t launch_tc_line(cudaStream_t st, const Dims &d, const bf16 *x, const 
     return cudaGetLastError();
 }
 
+// grids holding a 64 x 6 x 4 box: the 64-long z-line kernel (weights streamed per stage, taps ordered by z shift)
+bool line64_shape_ok(int ci, int co, const Dims &d) {
+    const bool ch = (ci == 16 || ci == 32 || ci == 64) && (co == 16 || co == 32 || co == 64);
+    return ch && d.nz >= tc::kL64Z && d.ny >= tc::kL64Y + 2 && d.nx >= tc::kL64X + 2;
+}
+
 template <int CI, int CO, int EPI>
-cudaError_t launch_tc(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *w, const float *b, void *y,
-                      int *err) {
+cudaError_t launch_tc_line64(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *wp, const float *b, void *y,
+                             int *err) {
+    auto enc = tensor_map_encoder();
+    if (!enc || !aligned16(x) || !aligned16(wp) || !aligned16(y)) return cudaErrorInvalidValue;
+    using L = tc::Line64Layout<CI, CO>;
+    CUtensorMap mx, mw;
+    const cuuint64_t xd[4] = {(cuuint64_t)CI, (cuuint64_t)d.nz, (cuuint64_t)d.ny, (cuuint64_t)d.nx};
+    const cuuint64_t xs[3] = {(cuuint64_t)CI * 2, (cuuint64_t)d.nz * CI * 2, (cuuint64_t)d.ny * d.nz * CI * 2};
+    const cuuint32_t xb[4] = {16, tc::kL64Z, tc::kL64Y + 2, tc::kL64X + 2};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    if (enc(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(x), xd, xs, xb, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    const cuuint64_t wd[3] = {(cuuint64_t)CI, (cuuint64_t)CO, 27};
+    const cuuint64_t ws[2] = {(cuuint64_t)CI * 2, (cuuint64_t)CO * CI * 2};
+    const cuuint32_t wb[3] = {16, (cuuint32_t)CO, 9};
+    if (enc(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16 *>(wp), wd, ws, wb, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(tc::k_conv_tc_line64<CI, CO, EPI>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::kSmemBytes);
+    if (e != cudaSuccess) return e;
+    const long long nbricks = (long long)((d.nz + tc::kL64Z - 1) / tc::kL64Z) *
+                              ((d.ny + tc::kL64Y - 1) / tc::kL64Y) * ((d.nx + tc::kL64X - 1) / tc::kL64X);
+    const int grid = (int)(nbricks < 152 ? nbricks : 152);
+    tc::k_conv_tc_line64<CI, CO, EPI><<<grid, 192, L::kSmemBytes, st>>>(mx, mw, d, b, y, err);
+    return cudaGetLastError();
+}
+
+template <int CI, int CO, int EPI>
+cudaError_t launch_tc(cudaStream_t st, const Dims &d, const bf16 *x, const bf16 *w, const bf16 *wp, const float *b,
+                      void *y, int *err) {
     if constexpr ((CI == 16 || CI == 32) && (CO == 16 || CO == 32))
         if (line_shape_ok(CI, CO, d)) return launch_tc_line<CI, CO, EPI>(st, d, x, w, b, y, err);
+    if (wp && line64_shape_ok(CI, CO, d)) return launch_tc_line64<CI, CO, EPI>(st, d, x, wp, b, y, err);
     constexpr int MT = tc::tiles_per_cta<CI, CO>();
     if (d.ny >= tc::kTileY * MT) return launch_tc_mt<CI, CO, EPI, MT>(st, d, x, w, b, y, err);
     return launch_tc_mt<CI, CO, EPI, 1>(st, d, x, w, b, y, err);
 }
 
-// epi 0: forward (bias, ReLU, BF16 y); epi 1: input gradient (FP32 y, no bias)
+// epi 0: forward (bias, ReLU, BF16 y); epi 1: input gradient (FP32 y, no bias).  wp: the weights with taps
+// ordered by z shift (the 64-long z-line kernel), or nullptr
 cudaError_t tc_dispatch(cudaStream_t st, int ci, int co, int epi, const Dims &d, const bf16 *x, const bf16 *w,
-                        const float *b, void *y, int *err) {
+                        const bf16 *wp, const float *b, void *y, int *err) {
 #define CASE(A, B)                                                                              \
     if (ci == A && co == B)                                                                     \
-        return epi == 0 ? launch_tc<A, B, 0>(st, d, x, w, b, y, err) : launch_tc<A, B, 1>(st, d, x, w, b, y, err);
+        return epi == 0 ? launch_tc<A, B, 0>(st, d, x, w, wp, b, y, err)                        \
+                        : launch_tc<A, B, 1>(st, d, x, w, wp, b, y, err);
     CASE(16, 16) CASE(16, 32) CASE(32, 16) CASE(32, 32) CASE(32, 64) CASE(64, 32) CASE(64, 64)
 #undef CASE
     return cudaErrorInvalidValue;
@@ -272,6 +313,8 @@ UNet::UNet(cudaStream_t st) : st_(st) {
     m2_ = (float *)alloc(4 * nparams_);
     wb_ = (bf16 *)alloc(2 * nbf_);
     wt_ = (bf16 *)alloc(2 * nbf_);
+    wbp_ = (bf16 *)alloc(2 * nbf_);
+    wtp_ = (bf16 *)alloc(2 * nbf_);
     dots_ = (double *)alloc(8 * 8);
     redpart_ = (double *)alloc(8 * 4 * 1216);
     wpart_elems_ = 64LL * 27 * 64 * 64;
@@ -310,6 +353,8 @@ void UNet::refresh_bf16() {
         const long long m = (long long)L.taps * L.cout * L.cin;
         k_f32_to_bf16<<<flat_blocks(m), 256, 0, st_>>>(m, p_ + L.woff, wb_ + L.wbf);
         k_flip_weights<<<flat_blocks(m), 256, 0, st_>>>(L.taps, L.cout, L.cin, p_ + L.woff, wt_ + L.wbf);
+        k_taps_dz_major<<<flat_blocks(m), 256, 0, st_>>>(m, L.cout * L.cin, wb_ + L.wbf, wbp_ + L.wbf);
+        k_taps_dz_major<<<flat_blocks(m), 256, 0, st_>>>(m, L.cout * L.cin, wt_ + L.wbf, wtp_ + L.wbf);
     }
 }
 
@@ -425,7 +470,7 @@ cudaError_t UNet::ensure_wgrad_ws() {
 
 void UNet::conv_fwd(const ConvLayer &L, const Dims &d, const bf16 *x, bf16 *y) {
     if (mode_ == 1 && L.taps == 27 && tc_shape_ok(L.cin, L.cout, d)) {
-        cudaError_t e = tc_dispatch(st_, L.cin, L.cout, 0, d, x, wb_ + L.wbf, p_ + L.boff, y, err_);
+        cudaError_t e = tc_dispatch(st_, L.cin, L.cout, 0, d, x, wb_ + L.wbf, wbp_ + L.wbf, p_ + L.boff, y, err_);
         if (e == cudaSuccess) {
             tc_launches_++;
             return;
@@ -515,7 +560,7 @@ void UNet::conv_bwd(const ConvLayer &L, const Dims &d, const bf16 *x, const bf16
     if (!dx) return;
     // input gradient: the forward convolution with the mirrored, transposed weights (FP32 out, no bias)
     if (mode_ == 1 && L.taps == 27 && tc_shape_ok(L.cout, L.cin, d)) {
-        const cudaError_t e = tc_dispatch(st_, L.cout, L.cin, 1, d, dy, wt_ + L.wbf, nullptr, dx, err_);
+        const cudaError_t e = tc_dispatch(st_, L.cout, L.cin, 1, d, dy, wt_ + L.wbf, wtp_ + L.wbf, nullptr, dx, err_);
         if (e == cudaSuccess) {
             tc_launches_++;
             return;

@@ -76,6 +76,7 @@ class UNet {
     long long nparams_ = 0, nbf_ = 0;
     float *p_ = nullptr, *g_ = nullptr, *m1_ = nullptr, *m2_ = nullptr;
     __nv_bfloat16 *wb_ = nullptr, *wt_ = nullptr;  // forward weights, mirrored/transposed for input gradients
+    __nv_bfloat16 *wbp_ = nullptr, *wtp_ = nullptr;  // the same with taps ordered by z shift (64-long z lines)
     long long step_ = 0;
     std::vector<void *> persist_;
     // per-grid workspace

@@ -409,6 +409,15 @@ __global__ void k_flip_weights(int taps, int CO, int CI, const float *__restrict
     }
 }
 
+// wp[9 dz + pr][co][ci] = w[3 pr + dz][co][ci]: the 27 taps reordered so that those of one z shift are
+// consecutive (pr = 3 (dx + 1) + (dy + 1), dz the z shift + 1)
+__global__ void k_taps_dz_major(long long m, int coci, const bf16 *__restrict__ w, bf16 *__restrict__ wp) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m; e += (long long)gridDim.x * blockDim.x) {
+        const int tp = (int)(e / coci), r = (int)(e % coci);
+        wp[e] = w[(long long)(3 * (tp % 9) + tp / 9) * coci + r];
+    }
+}
+
 __global__ void k_f32_to_bf16(long long m, const float *__restrict__ a, bf16 *__restrict__ b) {
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m; e += (long long)gridDim.x * blockDim.x)
         b[e] = __float2bfloat16(a[e]);

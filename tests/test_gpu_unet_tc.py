@@ -9,8 +9,10 @@ pytestmark = pytest.mark.gpu
 
 
 # (5, 8, 128) and (8, 12, 256) put the 16-channel layers on the line kernel (a 128 x 6 x 4 box fits the grid;
-# at (8, 12, 256) also the 16 -> 32 layer of level 1)
-@pytest.mark.parametrize("shape", [(2, 4, 32), (6, 12, 40), (17, 9, 64), (5, 8, 128), (8, 12, 256)])
+# at (8, 12, 256) also the 16 -> 32 layer of level 1); (5, 8, 64) and the 64^3-type level of (16, 24, 256) (4 x 6
+# x 64, 32 and 64 channels) run the 64-long z-line kernel
+@pytest.mark.parametrize("shape", [(2, 4, 32), (6, 12, 40), (17, 9, 64), (5, 8, 128), (8, 12, 256), (5, 8, 64),
+                                   (16, 24, 256)])
 def test_tcgen05_forward_matches_mma(sfpkg, gpu_ctx, shape):
     import torch
     from oracle import unet_ref as ref
@@ -42,7 +44,8 @@ def test_tcgen05_forward_matches_mma(sfpkg, gpu_ctx, shape):
     net.close()
 
 
-@pytest.mark.parametrize("shape", [(6, 12, 40), (9, 8, 64)])
+# shapes on the 27-box kernel (no z-line box fits: ny < 6), whose forward equals the warp-MMA kernel's bit for bit
+@pytest.mark.parametrize("shape", [(6, 12, 40), (9, 5, 64)])
 def test_tcgen05_gradients_match_mma(sfpkg, gpu_ctx, shape):
     """Training with the tcgen05 kernels: the input gradients of every 3x3x3 layer run on tcgen05 (the forward
     convolution with the mirrored, transposed weights, FP32 out); the parameter gradients agree with the
@@ -125,7 +128,7 @@ def test_tcgen05_weight_gradient_matches_mma(sfpkg, gpu_ctx, shape):
     net.close()
 
 
-@pytest.mark.parametrize("shape", [(4, 6, 128), (8, 12, 256)])
+@pytest.mark.parametrize("shape", [(4, 6, 128), (8, 12, 256), (5, 8, 64), (16, 24, 256)])
 def test_tcgen05_line_gradients_against_oracle(sfpkg, gpu_ctx, shape):
     """Grids that put the 16-channel layers on the line kernel (one halo'd box per z shift for nine taps), whose
     tap order differs from the warp-MMA kernel's, so the BF16 activations of the two paths are no longer bit
@@ -152,7 +155,7 @@ def test_tcgen05_line_gradients_against_oracle(sfpkg, gpu_ctx, shape):
         net.forward(g, feat, out)
         grads[mode] = ref.unflatten(net.gradients(g, feat, torch.from_numpy(dout).cuda()))
         if mode == "tcgen05":
-            assert net.tc_launches() - before >= 12
+            assert net.tc_launches() - before >= 8
     _, cache = ref.forward_bf16(P, x)
     G = ref.backward_bf16(P, cache, dout.astype(np.float64))
     errs = []

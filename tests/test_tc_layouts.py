@@ -170,3 +170,52 @@ def test_weight_gradient_layout(shape, ci, co):
         dx, dy, dz = t // 9 - 1, (t // 3) % 3 - 1, t % 3 - 1
         ref[t] = np.einsum("xyzo,xyzi->oi", dY, Xp[1 + dx:1 + dx + nx, 1 + dy:1 + dy + ny, 1 + dz:1 + dz + nz])
     assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("shape,ci,co", [((4, 6, 64), 64, 64), ((5, 7, 70), 32, 64), ((4, 6, 64), 16, 32),
+                                         ((4, 9, 64), 64, 16)])
+def test_line64_kernel_layout(shape, ci, co):
+    """k_conv_tc_line64: bricks of 64 z x 4 y x 2 x, four tiles of 64 z x 2 y; a stage per (dz, 16 channels) holds
+    the box (16 ch, 64 z, 6 y, 4 x) at (z0 + dz - 1, y0 - 1, x0 - 1) and the weights of the nine taps of that z
+    shift, rows (pr, co) of a copy whose taps are ordered 9 dz + pr; tile (ty, xx) of tap (dx, dy) starts
+    2 KB x ((2 ty + 1 + dy) + 6 (xx + 1 + dx)) into the box."""
+    z64, y4, x2 = _const("kL64Z"), _const("kL64Y"), _const("kL64X")
+    nx, ny, nz = shape
+    kp = ci // 16
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal(shape + (ci,))
+    W = rng.standard_normal((27, co, ci))
+    Wp = np.stack([W[3 * (tp % 9) + tp // 9] for tp in range(27)])  # k_taps_dz_major
+    a_bytes = z64 * (y4 + 2) * (x2 + 2) * 32
+    w_raw = 9 * co * 32
+    out = np.zeros((nx, ny, nz, co))
+    bz_n, by_n, bx_n = -(-nz // z64), -(-ny // y4), -(-nx // x2)
+    Xp = np.zeros((nx + 2 + x2, ny + 2 + y4, nz + 2 + z64, ci))
+    Xp[1:1 + nx, 1:1 + ny, 1:1 + nz] = X
+    tiles = (y4 // 2) * x2
+    for br in range(bz_n * by_n * bx_n):
+        z0, y0, x0 = z64 * (br % bz_n), y4 * ((br // bz_n) % by_n), x2 * (br // (bz_n * by_n))
+        acc = np.zeros((tiles, 128, co))
+        for st in range(3 * kp):
+            dz, jp = st // kp, st % kp
+            stage = np.zeros((a_bytes + (w_raw + 1023) // 1024 * 1024) // 2)
+            _write_sw32(stage, 0, Xp[x0:x0 + x2 + 2, y0:y0 + y4 + 2, z0 + dz:z0 + dz + z64,
+                                     16 * jp:16 * jp + 16].reshape(-1, 16))
+            _write_sw32(stage, a_bytes, Wp[9 * dz:9 * dz + 9, :, 16 * jp:16 * jp + 16].reshape(-1, 16))
+            for pr in range(9):
+                dx, dy = pr // 3 - 1, pr % 3 - 1
+                B, mb = _read_sw32(stage, a_bytes + pr * co * 32, co)
+                assert a_bytes <= mb < a_bytes + w_raw
+                for tile in range(tiles):
+                    ty, xx = tile % (y4 // 2), tile // (y4 // 2)
+                    A, ma = _read_sw32(stage, 2048 * ((2 * ty + 1 + dy) + (y4 + 2) * (xx + 1 + dx)), 128)
+                    assert ma < a_bytes
+                    acc[tile] += A @ B.T
+        for tile in range(tiles):
+            ty, xx = tile % (y4 // 2), tile // (y4 // 2)
+            for m in range(128):
+                z, yy, xv = z0 + m % z64, y0 + 2 * ty + m // z64, x0 + xx
+                if z < nz and yy < ny and xv < nx:
+                    out[xv, yy, z] = acc[tile, m]
+    ref = _direct_forward(X, W)
+    assert np.abs(out - ref).max() <= 1e-9 * np.abs(ref).max()
