@@ -555,8 +555,17 @@ void UNet::conv_bwd(const ConvLayer &L, const Dims &d, const bf16 *x, const bf16
     }
     const long long mw = (long long)L.taps * L.cout * L.cin;
     k_reduce_chunks<<<flat_blocks(mw), 256, 0, st_>>>(wpart_, wchunks, mw, g_ + L.woff);
-    k_bias_grad<<<chunks, 64, 0, st_>>>(d, dy, L.cout, (int)vchunk, hpart_);
-    k_reduce_chunks<<<1, 64, 0, st_>>>(hpart_, chunks, L.cout, g_ + L.boff);
+    // bias gradient: up to 1024 chunks of at least 256 voxels (partials fit the 4096 x 17 scratch for 64 channels)
+    long long bvchunk = (d.n + 1023) / 1024;
+    if (bvchunk < 256) bvchunk = 256;
+    const int bchunks = (int)((d.n + bvchunk - 1) / bvchunk);
+    if (L.cout == 16)
+        k_bias_grad<16><<<bchunks, 256, 0, st_>>>(d.n, dy, (int)bvchunk, hpart_);
+    else if (L.cout == 32)
+        k_bias_grad<32><<<bchunks, 256, 0, st_>>>(d.n, dy, (int)bvchunk, hpart_);
+    else
+        k_bias_grad<64><<<bchunks, 256, 0, st_>>>(d.n, dy, (int)bvchunk, hpart_);
+    k_reduce_chunks<<<1, 64, 0, st_>>>(hpart_, bchunks, L.cout, g_ + L.boff);
     if (!dx) return;
     // input gradient: the forward convolution with the mirrored, transposed weights (FP32 out, no bias)
     if (mode_ == 1 && L.taps == 27 && tc_shape_ok(L.cout, L.cin, d)) {

@@ -221,13 +221,24 @@ __global__ void k_reduce_chunks(const float *__restrict__ part, int chunks, long
     }
 }
 
-// bias gradient partials: part[chunk][co] = sum_{v in chunk} dy[v][co]
-__global__ void k_bias_grad(Dims d, const bf16 *__restrict__ dy, int co_n, int vchunk, float *__restrict__ part) {
-    const long long v0 = (long long)blockIdx.x * vchunk, v1 = min(v0 + vchunk, d.n);
-    for (int co = threadIdx.x; co < co_n; co += blockDim.x) {
-        float s = 0.f;
-        for (long long v = v0; v < v1; v++) s += __bfloat162float(dy[v * co_n + co]);
-        part[(long long)blockIdx.x * co_n + co] = s;
+// bias gradient partials: part[chunk][co] = sum_{v in chunk} dy[v][co].  256 threads per chunk: thread t sums
+// channel t % C over the voxels v0 + t / C, v0 + t / C + 256 / C, ... (consecutive threads read consecutive
+// channels), then the 256 / C lane sums of each channel are added in lane order: fixed order, deterministic.
+template <int C>
+__global__ void __launch_bounds__(256) k_bias_grad(long long n, const bf16 *__restrict__ dy, int vchunk,
+                                                   float *__restrict__ part) {
+    constexpr int LANES = 256 / C;
+    __shared__ float red[256];
+    const int c = threadIdx.x % C, l = threadIdx.x / C;
+    const long long v0 = (long long)blockIdx.x * vchunk, v1 = min(v0 + vchunk, n);
+    float s = 0.f;
+    for (long long v = v0 + l; v < v1; v += LANES) s += __bfloat162float(dy[v * C + c]);
+    red[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < C) {
+        float t = 0.f;
+        for (int k = 0; k < LANES; k++) t += red[k * C + threadIdx.x];
+        part[(long long)blockIdx.x * C + threadIdx.x] = t;
     }
 }
 
