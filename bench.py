@@ -104,29 +104,43 @@ def max_over_ranks(ws, v):
     return float(t.item())
 
 
-def profiled_traffic(summary, n, bytes_per_launch=None):
-    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the reported kernel, from the ncu
-    capture summarised in profiles/<summary> (a 256^3 launch).  With bytes_per_launch (the bench's mean algorithmic
-    bytes per launch) and the capture's own algorithmic bytes in the summary, it is scaled by their ratio (the
-    launches of a step process different numbers of rows, of two kinds); otherwise by n^3 cells.  None without a
-    capture."""
+def profiled_columns(summary):
+    """(traffic, algorithmic) MB per launch for each captured launch (table column) of the ncu summary
+    profiles/<summary>: traffic = dram__bytes_read.sum + dram__bytes_write.sum, written either "R + W Mbyte = T MB"
+    or "R + W MB" per column.  [] without a summary or those rows."""
     if not summary:
-        return None
-    mb = alg = None
+        return []
+    traffic, alg = [], []
     try:
         with open(os.path.join(ROOT, "profiles", summary)) as f:
             for line in f:
+                cells = [c.strip() for c in line.strip().strip("|").split("|")]
                 if line.startswith("| dram__bytes_read.sum + dram__bytes_write.sum"):
-                    mb = float(line.split("=")[-1].split("MB")[0])
+                    for c in cells[1:]:
+                        if "=" in c:
+                            traffic.append(float(c.split("=")[-1].split("MB")[0]))
+                        else:
+                            traffic.append(sum(float(x.replace("Mbyte", "").replace("MB", "")) for x in c.split("+")))
                 elif line.startswith("| algorithmic bytes per launch"):
-                    alg = float(line.split("|")[2].split("MB")[0])
+                    alg = [float(c.split("MB")[0]) for c in cells[1:]]
     except (OSError, ValueError):
+        return []
+    return list(zip(traffic, alg)) if traffic and len(traffic) == len(alg) else []
+
+
+def profiled_traffic(summary, n, per_solve=None):
+    """DRAM bytes per launch of the reported kernel from the ncu capture summarised in profiles/<summary> (256^3
+    launches).  With per_solve = [(launches, algorithmic bytes per launch), ...] in the capture's column order (the
+    bench's pressure and potential launches), each column's traffic is scaled by the bench's algorithmic bytes over
+    the capture's and the columns are averaged over the launches; otherwise the single column is scaled by n^3
+    cells.  None without a capture."""
+    cols = profiled_columns(summary)
+    if not cols:
         return None
-    if mb is None:
-        return None
-    if bytes_per_launch and alg:
-        return round(mb * bytes_per_launch / alg)
-    return round(mb * 1e6 * (n / 256.0) ** 3)
+    if per_solve and len(per_solve) == len(cols) and sum(k for k, _ in per_solve) > 0:
+        tot = sum(k * t * (b / (a * 1e6)) for (k, b), (t, a) in zip(per_solve, cols))
+        return round(tot * 1e6 / sum(k for k, _ in per_solve))
+    return round(cols[0][0] * 1e6 * (n / 256.0) ** 3)
 
 
 # ------------------------------------------------------------------------------------------------ clocks
@@ -346,7 +360,11 @@ def run_ours(args, ws, rank, local):
         kname = "k_rbgs (one colour of a red-black sweep per launch)"
         prof = "k_rbgs_f32_finest_pool_sphere_256.md" if args.precision == "mixed" else None
     split = smoother == 3 and args.precision == "mixed" and args.n % 8 == 0
-    traffic = profiled_traffic(prof, args.n, bytes_tot / max(n_launch, 1) if split else None)
+    try:  # a reporting figure from the committed capture: never allowed to fail the bench
+        per_solve = [(r["smooth_launches"], r["smooth_bytes"] / max(r["smooth_launches"], 1)) for r in (sp, sm)]
+        traffic = profiled_traffic(prof, args.n, per_solve if split else None)
+    except Exception:
+        traffic = None
     roofline = {"bound": "hbm", "kernel": kname + ", finest level",
                 "achieved": round(achieved, 1), "peak": peak, "peak_source": peak_src, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
