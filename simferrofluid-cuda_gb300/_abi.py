@@ -86,6 +86,7 @@ def load(path: str | None = None):
     G = C.POINTER(sf_grid)
     O = C.POINTER(sf_solve_opts)
     S = C.POINTER(sf_solve_stats)
+    L.sf_abi_version.argtypes = []
     L.sf_create.argtypes = [C.c_int, V, C.POINTER(V)]
     L.sf_create.restype = C.c_int
     L.sf_destroy.argtypes = [V]

@@ -127,6 +127,16 @@ def test_noalloc_rejects_bad_arguments_before_any_device_call():
     assert call(phi=0) == abi.SF_BAD_ARG and call(psi=0) == abi.SF_BAD_ARG and call(result=0) == abi.SF_BAD_ARG
 
 
+def test_every_declared_symbol_has_a_binding():
+    """The ctypes binding gives every entry point of the header its argument types (a wrong or missing one
+    passes arguments as C ints), and its list of exported names is the header's."""
+    lib = pkg().load_library()
+    syms = declared_symbols()
+    for s in syms:
+        assert getattr(lib, s).argtypes is not None, s
+    assert sorted(pkg()._abi.EXPORTED) == syms
+
+
 def test_prefetch_rejects_bad_arguments_before_any_device_call():
     """sf_applied_field_prefetch checks its arguments on the host: a null context, grid or field pointer, or a
     null field entry, is SF_BAD_ARG without touching a device."""
