@@ -219,3 +219,47 @@ def test_line64_kernel_layout(shape, ci, co):
                     out[xv, yy, z] = acc[tile, m]
     ref = _direct_forward(X, W)
     assert np.abs(out - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("shape,ci,co,mt", [((3, 8, 32), 16, 16, 4), ((2, 5, 40), 32, 16, 1), ((2, 8, 32), 64, 32, 2)])
+def test_27_box_kernel_layout(shape, ci, co, mt):
+    """k_conv_tc: a CTA takes MT tiles of 32 z x 4 y (one x plane); per tap and 8-channel chunk one box (8 ch,
+    32 z, 4 MT y, 1 x) at (z0 + dz, y0 + dy, x0 + dx) lands as 128 MT rows of 16 B (no swizzle) and the tap's
+    weights (8 ch, Cout) as Cout rows; MMA j (K = 16, chunks 2j and 2j + 1) of tile m reads A from
+    2 j chunk + 2 KB m (LBO one chunk, SBO 128 B) and B from 2 j Cout 16 B (LBO Cout 16 B)."""
+    nx, ny, nz = shape
+    chunks = ci // 8
+    rng = np.random.default_rng(4)
+    X = rng.standard_normal(shape + (ci,))
+    W = rng.standard_normal((27, co, ci))
+    chunk_bytes = 128 * 16 * mt
+    a_bytes, b_bytes = chunk_bytes * chunks, co * 16 * chunks
+    Xp = np.zeros((nx + 2, ny + 2 + 4 * mt, nz + 2 + 32, ci))
+    Xp[1:1 + nx, 1:1 + ny, 1:1 + nz] = X
+    out = np.zeros((nx, ny, nz, co))
+    tz, ty = -(-nz // 32), -(-ny // (4 * mt))
+    for blk in range(tz * ty * nx):
+        z0, y0, x0 = 32 * (blk % tz), 4 * mt * ((blk // tz) % ty), blk // (tz * ty)
+        acc = np.zeros((mt, 128, co))
+        for t in range(27):
+            dx, dy, dz = t // 9 - 1, (t // 3) % 3 - 1, t % 3 - 1
+            a = np.zeros(a_bytes // 2)
+            b = np.zeros(b_bytes // 2)
+            for c in range(chunks):  # box lands [y][z][8]
+                box = Xp[1 + x0 + dx, 1 + y0 + dy:1 + y0 + dy + 4 * mt, 1 + z0 + dz:1 + z0 + dz + 32, 8 * c:8 * c + 8]
+                a[c * chunk_bytes // 2:(c + 1) * chunk_bytes // 2] = box.reshape(-1)
+                b[c * co * 8:(c + 1) * co * 8] = W[t, :, 8 * c:8 * c + 8].reshape(-1)
+            for j in range(ci // 16):
+                B, mb = _read_plain(b, j * 2 * co * 16, co * 16, 128, co)
+                assert mb < b_bytes
+                for m in range(mt):
+                    A, ma = _read_plain(a, j * 2 * chunk_bytes + m * 2048, chunk_bytes, 128, 128)
+                    assert ma < a_bytes
+                    acc[m] += A @ B.T
+        for m in range(mt):
+            for r in range(128):  # TMEM lane = tile row: z = r % 32, y = 4 m + r / 32
+                z, y = z0 + r % 32, y0 + 4 * m + r // 32
+                if z < nz and y < ny:
+                    out[x0, y, z] = acc[m, r]
+    ref = _direct_forward(X, W)
+    assert np.abs(out - ref).max() <= 1e-9 * np.abs(ref).max()
